@@ -1,0 +1,370 @@
+// C-ABI of libgcr.so (include/gcr.h): argument checks, device buffers of a
+// gcr_context, per-pair descriptors and the engine launches.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include "../../include/gcr.h"
+#include "gcr_engine.cuh"
+#include "gcr_kinds.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+thread_local long long g_last_launches = 0;
+
+gcr_status fail(gcr_status s, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return s;
+}
+
+#define CUDA_TRY(expr)                                                                        \
+  do {                                                                                        \
+    cudaError_t e_ = (expr);                                                                  \
+    if (e_ != cudaSuccess)                                                                    \
+      return fail(GCR_DEVICE_ERROR, "%s failed: %s", #expr, cudaGetErrorString(e_));          \
+  } while (0)
+
+// Growable device allocation.
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    const size_t b = std::max<size_t>(bytes, 256);
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e == cudaSuccess) cap = b;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+const gcr::KindOps* ops_for(gcr_model_kind kind) {
+  switch (kind) {
+    case GCR_HOMOGRAPHY: return gcr::homography_ops();
+    case GCR_FUNDAMENTAL: return gcr::fundamental_ops();
+    case GCR_ESSENTIAL: return gcr::essential_ops();
+  }
+  return nullptr;
+}
+
+}  // namespace
+
+struct gcr_context {
+  int device = 0;
+  int num_sms = 0;
+  DevBuf pairs, slots_meta, slot_mem, pts32, ticket, norm_pts, kinv, row_pair;
+  // staging of the host-buffer entry points
+  DevBuf corr, models, masks, stats;
+  int slot_kind = -1, slot_max_n = 0, slot_count = 0;
+  bool prepared[3] = {false, false, false};
+};
+
+namespace {
+
+gcr_status check_params(gcr_model_kind kind, const gcr_params* p) {
+  if (!p) return fail(GCR_INVALID_ARG, "params is NULL");
+  if (!(p->threshold > 0)) return fail(GCR_INVALID_ARG, "threshold must be > 0");
+  if (!(p->confidence > 0 && p->confidence < 1)) return fail(GCR_INVALID_ARG, "confidence must be in (0, 1)");
+  if (!(p->spatial_coherence_weight >= 0 && p->spatial_coherence_weight <= 1))
+    return fail(GCR_INVALID_ARG, "spatial_coherence_weight must be in [0, 1]");
+  if (p->max_iterations < 0 || p->min_iterations < 0) return fail(GCR_INVALID_ARG, "negative iteration limit");
+  if (p->lo_number < 0 || p->lo_number > GCR_BLOCK)
+    return fail(GCR_UNSUPPORTED, "lo_number must be in [0, %d]", GCR_BLOCK);
+  if (p->sampler != GCR_SAMPLER_UNIFORM && p->sampler != GCR_SAMPLER_PROSAC)
+    return fail(GCR_UNSUPPORTED, "sampler %d is not provided by the device engine (0 uniform, 1 PROSAC)",
+                p->sampler);
+  if (p->scoring != GCR_SCORING_MSAC) return fail(GCR_UNSUPPORTED, "scoring %d is not provided", p->scoring);
+  const bool pairwise = p->spatial_coherence_weight > 0;
+  if (p->neighborhood != GCR_NEIGHBORHOOD_GRID && pairwise)
+    return fail(GCR_UNSUPPORTED, "only the grid neighbourhood (0) is provided with a spatial coherence term");
+  if (p->neighborhood == GCR_NEIGHBORHOOD_GRID && !(p->neighborhood_size >= 1))
+    return fail(GCR_INVALID_ARG, "neighborhood_size must be >= 1 for the grid");
+  (void)kind;
+  return GCR_OK;
+}
+
+int pow2_at_least(int n) {
+  int s = 1;
+  while (s < n) s <<= 1;
+  return s;
+}
+
+}  // namespace
+
+extern "C" {
+
+void gcr_default_params(gcr_model_kind kind, gcr_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->threshold = 1.0;
+  p->confidence = 0.99;
+  p->max_iterations = 10000;
+  p->min_iterations = 50;
+  p->sampler = GCR_SAMPLER_PROSAC;
+  p->lo_number = 50;
+  p->scoring = GCR_SCORING_MSAC;
+  p->use_sprt = 1;
+  p->seed = 0;
+  switch (kind) {
+    case GCR_HOMOGRAPHY:  // bindings.cpp:1158-1178
+      p->spatial_coherence_weight = 0.975;
+      p->neighborhood = GCR_NEIGHBORHOOD_GRID;
+      p->neighborhood_size = 4.0;
+      p->use_space_partitioning = 1;
+      break;
+    case GCR_FUNDAMENTAL:  // bindings.cpp:1003-1022
+      p->spatial_coherence_weight = 0.0;
+      p->neighborhood = GCR_NEIGHBORHOOD_FLANN;
+      p->neighborhood_size = 20.0;
+      break;
+    case GCR_ESSENTIAL:  // bindings.cpp:1091-1112
+      p->spatial_coherence_weight = 0.1;
+      p->neighborhood = GCR_NEIGHBORHOOD_FLANN;
+      p->neighborhood_size = 20.0;
+      break;
+  }
+}
+
+const char* gcr_last_error_string(void) { return g_last_error.c_str(); }
+
+int64_t gcr_last_launch_count(void) { return g_last_launches; }
+
+gcr_status gcr_context_create(gcr_context** ctx) {
+  if (!ctx) return fail(GCR_INVALID_ARG, "ctx is NULL");
+  gcr_context* c = new gcr_context();
+  if (cudaGetDevice(&c->device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess) {
+    delete c;
+    return fail(GCR_DEVICE_ERROR, "no CUDA device available");
+  }
+  *ctx = c;
+  return GCR_OK;
+}
+
+gcr_status gcr_context_destroy(gcr_context* c) {
+  if (!c) return GCR_OK;
+  for (DevBuf* b : {&c->pairs, &c->slots_meta, &c->slot_mem, &c->pts32, &c->ticket, &c->norm_pts, &c->kinv,
+                    &c->row_pair, &c->corr, &c->models, &c->masks, &c->stats})
+    b->release();
+  delete c;
+  return GCR_OK;
+}
+
+// Device-resident batch: bulk arrays are device pointers, per-pair metadata
+// (offsets, intrinsics, image sizes, seeds) are host arrays.
+gcr_status gcr_batch_run_device(gcr_context* c, gcr_model_kind kind, int64_t num_pairs, const double* d_corr,
+                                const int64_t* h_offsets, const double* h_K,
+                                const gcr_image_size* h_sizes, const gcr_params* params, const uint64_t* h_seeds,
+                                double* d_models_out, uint8_t* d_masks_out, gcr_stats* d_stats_out, void* stream) {
+  g_last_launches = 0;
+  if (!c) return fail(GCR_INVALID_ARG, "context is NULL");
+  const gcr::KindOps* ops = ops_for(kind);
+  if (!ops) return fail(GCR_UNSUPPORTED, "model kind %d is not provided by this build", (int)kind);
+  gcr_status st = check_params(kind, params);
+  if (st != GCR_OK) return st;
+  if (num_pairs <= 0) return GCR_OK;
+  if (num_pairs > (1 << 30)) return fail(GCR_CAPACITY, "too many pairs");
+  if (!d_corr || !h_offsets || !h_sizes || !d_models_out || !d_masks_out || !d_stats_out)
+    return fail(GCR_INVALID_ARG, "NULL buffer");
+  if (kind == GCR_ESSENTIAL && !h_K) return fail(GCR_INVALID_ARG, "essential matrices need intrinsics");
+  const int m = ops->sample_size;
+  int max_n = 0;
+  for (int64_t i = 0; i < num_pairs; ++i) {
+    const int64_t n = h_offsets[i + 1] - h_offsets[i];
+    if (n < 0) return fail(GCR_INVALID_ARG, "offsets are not non-decreasing at pair %lld", (long long)i);
+    if (n < m) return fail(GCR_TOO_FEW_POINTS, "pair %lld has %lld correspondences, needs >= %d", (long long)i,
+                           (long long)n, m);
+    if (n >= (1 << 24)) return fail(GCR_CAPACITY, "pair %lld exceeds 2^24 correspondences", (long long)i);
+    max_n = std::max<int>(max_n, (int)n);
+  }
+  const int64_t total = h_offsets[num_pairs] - h_offsets[0];
+  if (h_offsets[0] != 0) return fail(GCR_INVALID_ARG, "offsets[0] must be 0");
+  cudaStream_t s = (cudaStream_t)stream;
+
+  if (!c->prepared[kind]) {
+    CUDA_TRY(ops->prepare());
+    c->prepared[kind] = true;
+  }
+  int per_sm = 0;
+  CUDA_TRY(ops->occupancy(&per_sm));
+  if (per_sm < 1) return fail(GCR_DEVICE_ERROR, "engine kernel does not fit on an SM");
+  const int resident = per_sm * c->num_sms;
+  const int grid = (int)std::min<int64_t>(num_pairs, resident);
+  const int sort_cap = pow2_at_least(max_n);
+
+  // scratch slots (one per resident CTA), grown on demand
+  if (c->slot_kind != (int)kind || c->slot_max_n < max_n || c->slot_count < grid) {
+    const int want_n = std::max(max_n, c->slot_kind == (int)kind ? c->slot_max_n : 0);
+    const int want_cnt = std::max(grid, c->slot_kind == (int)kind ? c->slot_count : 0);
+    const int want_sort = pow2_at_least(want_n);
+    const size_t per = ops->slot_bytes(want_n, want_sort);
+    CUDA_TRY(cudaStreamSynchronize(s));
+    CUDA_TRY(c->slot_mem.ensure(per * (size_t)want_cnt));
+    CUDA_TRY(c->slots_meta.ensure(sizeof(gcr::Slot) * want_cnt));
+    std::vector<gcr::Slot> meta(want_cnt);
+    for (int i = 0; i < want_cnt; ++i)
+      ops->carve((unsigned char*)c->slot_mem.p + per * (size_t)i, want_n, want_sort, &meta[i]);
+    CUDA_TRY(cudaMemcpy(c->slots_meta.p, meta.data(), sizeof(gcr::Slot) * want_cnt, cudaMemcpyHostToDevice));
+    c->slot_kind = (int)kind;
+    c->slot_max_n = want_n;
+    c->slot_count = want_cnt;
+  }
+  (void)sort_cap;
+
+  // per-pair descriptors
+  std::vector<gcr::PairDesc> pd((size_t)num_pairs);
+  const double eps = std::numeric_limits<double>::epsilon();
+  for (int64_t i = 0; i < num_pairs; ++i) {
+    gcr::PairDesc& d = pd[i];
+    const gcr_image_size& z = h_sizes[i];
+    d.offset = h_offsets[i];
+    d.n = (int32_t)(h_offsets[i + 1] - h_offsets[i]);
+    d.n_div = (int32_t)params->neighborhood_size;
+    if (d.n_div < 1) d.n_div = 1;
+    const double nd = (double)d.n_div;
+    d.cell[0] = (z.w1 + eps) / nd;
+    d.cell[1] = (z.h1 + eps) / nd;
+    d.cell[2] = (z.w2 + eps) / nd;
+    d.cell[3] = (z.h2 + eps) / nd;
+    d.threshold = params->threshold;
+    d.centre[0] = 0.5 * z.w1;
+    d.centre[1] = 0.5 * z.h1;
+    d.centre[2] = 0.5 * z.w2;
+    d.centre[3] = 0.5 * z.h2;
+    d.seed = h_seeds ? h_seeds[i] : params->seed + (uint64_t)i;
+  }
+  CUDA_TRY(c->pairs.ensure(sizeof(gcr::PairDesc) * num_pairs));
+  CUDA_TRY(cudaMemcpyAsync(c->pairs.p, pd.data(), sizeof(gcr::PairDesc) * num_pairs, cudaMemcpyHostToDevice, s));
+  if (max_n > gcr::kSmemPoints) CUDA_TRY(c->pts32.ensure(sizeof(float4) * (size_t)total));
+  CUDA_TRY(c->ticket.ensure(sizeof(int)));
+  CUDA_TRY(cudaMemsetAsync(c->ticket.p, 0, sizeof(int), s));
+
+  gcr::Workspace ws;
+  ws.pts64 = d_corr;
+  ws.pix64 = d_corr;
+  ws.pts32 = (float4*)c->pts32.p;
+  ws.pairs = (const gcr::PairDesc*)c->pairs.p;
+  ws.slots = (gcr::Slot*)c->slots_meta.p;
+  ws.ticket = (int*)c->ticket.p;
+  ws.models_out = d_models_out;
+  ws.masks_out = d_masks_out;
+  ws.stats_out = (gcr::StatsOut*)d_stats_out;
+
+  gcr::EngineParams prm;
+  prm.confidence = params->confidence;
+  prm.lambda = params->spatial_coherence_weight;
+  prm.max_iters = params->max_iterations;
+  prm.min_iters = params->min_iterations;
+  prm.lo_number = params->lo_number;
+  prm.sampler = params->sampler;
+  prm.scoring = params->scoring;
+  prm.num_pairs = (int32_t)num_pairs;
+  prm.max_n = max_n;
+  CUDA_TRY(ops->launch(grid, s, ws, prm));
+  g_last_launches = 1;
+  return GCR_OK;
+}
+
+gcr_status gcr_find_batch(gcr_model_kind kind, int64_t num_pairs, const double* corr, const int64_t* offsets,
+                          const double* K, const gcr_image_size* sizes, const gcr_params* params,
+                          const uint64_t* seeds, double* models_out, uint8_t* masks_out, gcr_stats* stats_out) {
+  static thread_local gcr_context* ctx = nullptr;
+  if (!ctx) {
+    gcr_status s = gcr_context_create(&ctx);
+    if (s != GCR_OK) return s;
+  }
+  if (num_pairs <= 0) return GCR_OK;
+  if (!corr || !offsets || !sizes || !models_out || !masks_out || !stats_out)
+    return fail(GCR_INVALID_ARG, "NULL buffer");
+  const int64_t total = offsets[num_pairs];
+  CUDA_TRY(ctx->corr.ensure(sizeof(double) * 4 * (size_t)std::max<int64_t>(total, 1)));
+  CUDA_TRY(ctx->models.ensure(sizeof(double) * 9 * num_pairs));
+  CUDA_TRY(ctx->masks.ensure((size_t)std::max<int64_t>(total, 1)));
+  CUDA_TRY(ctx->stats.ensure(sizeof(gcr_stats) * num_pairs));
+  cudaStream_t s = 0;
+  CUDA_TRY(cudaMemcpyAsync(ctx->corr.p, corr, sizeof(double) * 4 * total, cudaMemcpyHostToDevice, s));
+  gcr_status st = gcr_batch_run_device(ctx, kind, num_pairs, (const double*)ctx->corr.p, offsets, K, sizes,
+                                       params, seeds, (double*)ctx->models.p, (uint8_t*)ctx->masks.p,
+                                       (gcr_stats*)ctx->stats.p, s);
+  if (st != GCR_OK) return st;
+  CUDA_TRY(cudaMemcpyAsync(models_out, ctx->models.p, sizeof(double) * 9 * num_pairs, cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaMemcpyAsync(masks_out, ctx->masks.p, (size_t)total, cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaMemcpyAsync(stats_out, ctx->stats.p, sizeof(gcr_stats) * num_pairs, cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  return GCR_OK;
+}
+
+static gcr_status find_one(gcr_model_kind kind, const double* corr, int64_t n, const double* K1, const double* K2,
+                           const gcr_image_size* size, const gcr_params* params, double* model_out9,
+                           uint8_t* mask_out, gcr_stats* stats_out) {
+  if (!corr || !size || !params || !model_out9 || !mask_out) return fail(GCR_INVALID_ARG, "NULL argument");
+  const int m = kind == GCR_HOMOGRAPHY ? 4 : (kind == GCR_FUNDAMENTAL ? 7 : 5);
+  if (n < m) return fail(GCR_TOO_FEW_POINTS, "%lld correspondences, needs >= %d", (long long)n, m);
+  const int64_t offsets[2] = {0, n};
+  double K[18];
+  if (kind == GCR_ESSENTIAL) {
+    if (!K1 || !K2) return fail(GCR_INVALID_ARG, "essential matrices need K1 and K2");
+    std::memcpy(K, K1, 9 * sizeof(double));
+    std::memcpy(K + 9, K2, 9 * sizeof(double));
+  }
+  gcr_stats st{};
+  const uint64_t seed = params->seed;
+  gcr_status rc = gcr_find_batch(kind, 1, corr, offsets, kind == GCR_ESSENTIAL ? K : nullptr, size, params, &seed,
+                                 model_out9, mask_out, &st);
+  if (rc != GCR_OK) return rc;
+  if (stats_out) *stats_out = st;
+  if (st.status != GCR_OK) {
+    if (st.status == GCR_NO_MODEL) return fail(GCR_NO_MODEL, "no model with more than %d inliers", m);
+    return fail((gcr_status)st.status, "device engine reported status %d", st.status);
+  }
+  return GCR_OK;
+}
+
+gcr_status gcr_find_homography(const double* corr, int64_t n, const gcr_image_size* size, const double* probabilities,
+                               const gcr_params* params, double* model_out9, uint8_t* mask_out,
+                               gcr_stats* stats_out) {
+  (void)probabilities;
+  return find_one(GCR_HOMOGRAPHY, corr, n, nullptr, nullptr, size, params, model_out9, mask_out, stats_out);
+}
+
+gcr_status gcr_find_fundamental(const double* corr, int64_t n, const gcr_image_size* size,
+                                const double* probabilities, const gcr_params* params, double* model_out9,
+                                uint8_t* mask_out, gcr_stats* stats_out) {
+  (void)probabilities;
+  return find_one(GCR_FUNDAMENTAL, corr, n, nullptr, nullptr, size, params, model_out9, mask_out, stats_out);
+}
+
+gcr_status gcr_find_essential(const double* corr, int64_t n, const double* K1, const double* K2,
+                              const gcr_image_size* size, const double* probabilities, const gcr_params* params,
+                              double* model_out9, uint8_t* mask_out, gcr_stats* stats_out) {
+  (void)probabilities;
+  return find_one(GCR_ESSENTIAL, corr, n, K1, K2, size, params, model_out9, mask_out, stats_out);
+}
+
+}  // extern "C"
+
+namespace gcr {
+// Kinds not compiled into this build.
+__attribute__((weak)) const KindOps* fundamental_ops() { return nullptr; }
+__attribute__((weak)) const KindOps* essential_ops() { return nullptr; }
+}  // namespace gcr

@@ -1,0 +1,971 @@
+// Persistent CTA-per-pair Graph-Cut RANSAC engine.
+//
+// One CTA owns one image pair at a time and runs the whole
+// hypothesize-and-verify loop of GCRANSAC::run (src/pygcransac/include/GCRANSAC.h:200-627)
+// for it:
+//   * batched sampling + minimal solves, one sampler call per thread;
+//   * an FP32 scoring pass of every hypothesis against every correspondence
+//     held in shared memory, with an FP64 re-check of points inside the FP32
+//     error band so that inlier counts are exact;
+//   * an ordered commit that replays the reference's sequential decisions
+//     (strict score comparison, validity, adaptive iteration count, LO trigger)
+//     with FP64 scores for every hypothesis that may beat the best one;
+//   * graph-cut local optimisation (GCRANSAC.h:779-1021): the labelling graph of
+//     the grid neighbourhood is a disjoint union of one clique per grid cell, so
+//     every cell is an independent s-t min-cut solved by one warp with
+//     push-relabel;
+//   * the final iterated least squares (GCRANSAC.h:629-758).
+//
+// Control flow: every thread executes the sequential decision logic on
+// thread-private copies of the scalar state; every input of a decision is
+// CTA-uniform, so all threads take the same branches and meet at the same
+// barriers inside the CTA-collective operations.
+#pragma once
+
+#include "gcr_device.cuh"
+#include "gcr_linalg.cuh"
+
+namespace gcr {
+
+constexpr int kMaxFlowCap = 256;        // largest grid cell solved by one warp
+constexpr long long kFlowOpsCap = 20000000;  // push/relabel steps per cell before TIMEOUT
+constexpr double kResidualEps = 1e-12;  // residual capacity treated as saturated
+constexpr int kSmemPoints = 4096;       // correspondences kept resident in shared memory
+constexpr int kLoRegion = GCR_BLOCK;    // model slots reserved for local optimisation
+
+enum PairStatus { ST_OK = 0, ST_NO_MODEL = 3, ST_TIMEOUT = 5, ST_CAPACITY = 6, ST_UNSUPPORTED = 7 };
+
+enum { SAMPLER_UNIFORM = 0, SAMPLER_PROSAC = 1 };
+
+struct EngineParams {
+  double confidence;
+  double lambda;        // spatial coherence weight
+  int64_t max_iters;
+  int64_t min_iters;
+  int32_t lo_number;
+  int32_t sampler;
+  int32_t scoring;
+  int32_t num_pairs;
+  int32_t max_n;
+};
+
+// Per-pair inputs prepared on the device.
+struct PairDesc {
+  int64_t offset;       // first row in the concatenated arrays
+  int32_t n;
+  int32_t n_div;        // grid divisions along every axis
+  double threshold;     // threshold in the coordinates the model is fitted in
+  double cell[4];       // grid cell sizes (pixel coordinates)
+  double centre[4];     // centring of the FP32 copy
+  uint64_t seed;
+};
+
+// Device mirror of gcr_stats (include/gcr.h).
+struct StatsOut {
+  int64_t iteration_number;
+  int64_t graph_cut_number;
+  int64_t local_optimization_number;
+  int64_t inlier_number;
+  double score;
+  int32_t status;
+  int32_t flags;
+};
+
+// Per-CTA scratch in global memory (one slot per resident CTA).
+struct Slot {
+  double* models64;     // [kModels][9]
+  float* models32;      // [kModels][12]
+  int* samples;         // [GCR_BLOCK][kSampleCap]
+  int* list0;           // [max_n]
+  int* list1;           // [max_n]
+  int* list2;           // [max_n]
+  uint8_t* flag;        // [max_n]
+  double* dres;         // [max_n]
+  double* tr;           // [max_n]
+  unsigned long long* sortbuf;  // [pow2 >= max_n]
+  int* cell_pts;        // [max_n]
+  int* cell_start;      // [max_n + 1]
+  double* flow;         // [GCR_WARPS][kMaxFlowCap^2]
+  double* node_d;       // [GCR_WARPS][3 * kMaxFlowCap]  excess, sink residual, scratch
+  int* node_i;          // [GCR_WARPS][3 * kMaxFlowCap]  height, queue, mark
+};
+
+struct Workspace {
+  const double* pts64;  // [total][4] coordinates the model is fitted in
+  const double* pix64;  // [total][4] pixel coordinates for the grid
+  float4* pts32;        // [total] centred FP32 copy of pts64 (pairs too large for shared memory)
+  const PairDesc* pairs;
+  Slot* slots;
+  int* ticket;
+  double* models_out;   // [P][9]
+  uint8_t* masks_out;   // [total]
+  StatsOut* stats_out;  // [P]
+};
+
+struct Score {
+  int count;
+  double value;
+};
+
+// A container of the reference's temp_inner_inliers: the inlier set of one
+// model, kept as (pointer to that model, inlier count).
+struct Container {
+  const double* model;
+  int count;
+};
+
+template <class Est>
+struct Shared {
+  static constexpr int kModels = GCR_BLOCK * Est::MAXSOL + kLoRegion;
+  float4 pts[kSmemPoints];
+  double best_model[9];
+  double cont_model[2][9];
+  double lo_best_model[9];
+  double work_model[9];
+  double fit_model[9];
+  double red_d[GCR_WARPS * 48];
+  int red_i[GCR_WARPS + 2];
+  int n_ok[GCR_BLOCK];
+  int mbase[GCR_BLOCK];
+  int mcount[kModels];
+  float mscore[kModels];
+  float mbound[kModels];
+  int s_cnt[GCR_BLOCK];
+  float s_sum[GCR_BLOCK];
+  float s_err[GCR_BLOCK];
+  int lo_ok[GCR_BLOCK];
+  int fit_ok;
+  int flow_status;
+};
+
+// GCRANSAC::getIterationNumber (GCRANSAC.h:156-172)
+__device__ __forceinline__ long long iteration_number_for(long long inliers, long long points, int m,
+                                                          double log_prob) {
+  const double q = pow((double)inliers / (double)points, (double)m);
+  const double l2 = log(1 - q);
+  if (fabs(l2) < 2.220446049250313e-16) return 0x7fffffffffffffffLL;
+  const double iter = log_prob / l2;
+  if (!(iter < 9.2e18)) return 0x7fffffffffffffffLL;
+  return (long long)iter + 1;
+}
+
+template <class Est>
+struct Engine {
+  static constexpr int m = Est::M;
+  static constexpr int kModels = Shared<Est>::kModels;
+  static constexpr int kBatchModels = GCR_BLOCK * Est::MAXSOL;
+
+  Shared<Est>& sh;
+  const Workspace& ws;
+  const EngineParams& prm;
+  const PairDesc& pd;
+  const Slot& slot;
+  int pair;
+  const double* pts64;
+  const float4* pts32;   // shared-memory or global FP32 copy of this pair
+  double scale = 1.0;    // max |centred coordinate| of this pair
+  int N;
+  double t2;
+  double log_prob;
+  int status = ST_OK;
+  int flags = 0;
+
+  // sequential state (identical in every thread)
+  long long iter = 0, max_iter = 0, gc_number = 0, lo_number = 0, lo_calls = 0;
+  Score best{0, 0.0};
+  Container cont[2];
+  int off = 0;
+
+  __device__ Engine(Shared<Est>& s, const Workspace& w, const EngineParams& p, const PairDesc& d, const Slot& sl,
+                    int pair_)
+      : sh(s), ws(w), prm(p), pd(d), slot(sl), pair(pair_) {
+    N = pd.n;
+    pts64 = ws.pts64 + 4 * pd.offset;
+    const double tt = 1.5 * pd.threshold;
+    t2 = tt * tt;
+    log_prob = log(1.0 - prm.confidence);
+    cont[0] = {nullptr, 0};
+    cont[1] = {nullptr, 0};
+  }
+
+  __device__ __forceinline__ void sync() { __syncthreads(); }
+
+  // thread 0 copies 9 doubles; everyone waits
+  __device__ void copy_model(double* dst, const double* src) {
+    sync();
+    if (threadIdx.x < 9) dst[threadIdx.x] = src[threadIdx.x];
+    sync();
+  }
+
+  // ------------------------------------------------------------------
+  // FP32 scoring of models [k0, k0 + K) of the slot table. Writes exact inlier
+  // counts (points inside the FP32 error band are re-decided in FP64) and an
+  // FP32 MSAC score with an upper bound of its error.
+  __device__ void score_models_f32(int k0, int K) {
+    const float tf = (float)sqrt(t2);
+    const float t2f = (float)t2;
+    const int tid = threadIdx.x;
+    for (int base = 0; base < K; base += GCR_BLOCK) {
+      const int Kb = min(GCR_BLOCK, K - base);
+      const int KP = (Kb + 31) & ~31;
+      const int S = GCR_BLOCK / KP;
+      const int slice = tid / KP, mi = tid % KP;
+      int cnt = 0;
+      float sum = 0.f, err = 0.f;
+      if (slice < S && mi < Kb) {
+        const int k = k0 + base + mi;
+        float h[9];
+        const float* src = slot.models32 + 12 * k;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) h[q] = src[q];
+        const float cm = src[9];
+        const double* m64 = slot.models64 + 9 * k;
+        const int chunk = (N + S - 1) / S;
+        const int i0 = slice * chunk, i1 = min(N, i0 + chunk);
+        float inner = 0.f;
+        int inner_n = 0;
+        for (int i = i0; i < i1; ++i) {
+          const float4 p = pts32[i];
+          float it;
+          const float r2 = Est::r2_f32(p, h, it);
+          const float e = fmaf(cm, fabsf(it), cm);
+          const float eb = fmaf(e, e, 2.f * tf * e);
+          const float dlt = r2 - t2f;
+          if (dlt < -eb) {
+            ++cnt;
+            inner += r2;
+            err += eb;
+          } else if (!(dlt > eb)) {  // inside the band, or NaN
+            const double r2d = Est::r2_f64(pts64 + 4 * i, m64);
+            if (r2d < t2) {
+              ++cnt;
+              inner += (float)r2d;
+            }
+          }
+          if (++inner_n == 64) {
+            sum += inner;
+            inner = 0.f;
+            inner_n = 0;
+          }
+        }
+        sum += inner;
+      }
+      sh.s_cnt[tid] = cnt;
+      sh.s_sum[tid] = sum;
+      sh.s_err[tid] = err;
+      sync();
+      if (tid < Kb) {
+        int c = 0;
+        float s = 0.f, e = 0.f;
+        for (int q = 0; q < S; ++q) {
+          c += sh.s_cnt[q * KP + tid];
+          s += sh.s_sum[q * KP + tid];
+          e += sh.s_err[q * KP + tid];
+        }
+        const int k = k0 + base + tid;
+        sh.mcount[k] = c;
+        sh.mscore[k] = c == 0 ? 0.f : (c * t2f - s) / t2f;
+        // per-point residual error + FP32 summation error + the final division
+        sh.mbound[k] = (e + 2.f * s * (64.f + (float)N / 64.f) * 5.97e-8f) / t2f + 4e-7f * c + 1e-6f;
+      }
+      sync();
+    }
+  }
+
+  // Exact FP64 MSAC score (scoring_function.h:137-233) of a model; optionally
+  // writes the inlier list in index order.
+  __device__ Score exact_score(const double* model, int* list) {
+    double h[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) h[q] = model[q];
+    double acc = 0.0;
+    int total = 0;
+    for (int base = 0; base < N; base += GCR_BLOCK) {
+      const int i = base + threadIdx.x;
+      int f = 0;
+      if (i < N) {
+        const double r2 = Est::r2_f64(pts64 + 4 * i, h);
+        if (r2 < t2) {
+          f = 1;
+          acc -= r2;
+        }
+      }
+      int tot;
+      const int pos = block_exclusive_scan(f, sh.red_i, &tot);
+      if (list && f) list[total + pos] = i;
+      total += tot;
+    }
+    const double s = block_sum(acc, sh.red_d);
+    Score sc;
+    sc.count = total;
+    sc.value = total == 0 ? 0.0 : (s + total * t2) / t2;
+    return sc;
+  }
+
+  __device__ void put_f32(int k) {
+    Est::prepare_f32(slot.models64 + 9 * k, pd.centre, scale, slot.models32 + 12 * k);
+  }
+
+  // Is `cand` (FP32 score + bound of model k) possibly better than `ref`?
+  __device__ __forceinline__ bool maybe_better(int k, double ref) const {
+    return (double)sh.mscore[k] + (double)sh.mbound[k] >= ref;
+  }
+
+  // ------------------------------------------------------------------
+  // Grid neighbourhood: points sorted by (cell key, index); cell_start holds
+  // the cell boundaries. Returns the number of cells.
+  __device__ int build_grid() {
+    unsigned long long* a = slot.sortbuf;
+    const double* pix = ws.pix64 + 4 * pd.offset;
+    const uint64_t nd = (uint64_t)pd.n_div;
+    int sort_n = 1;
+    while (sort_n < N) sort_n <<= 1;
+    for (int i = threadIdx.x; i < sort_n; i += GCR_BLOCK) {
+      if (i < N) {
+        const double* p = pix + 4 * i;
+        uint64_t key = 0, o = 1;
+        for (int d = 0; d < 4; ++d) {
+          const uint64_t idx = (uint64_t)(int64_t)floor(p[d] / pd.cell[d]);
+          key += o * idx;
+          o *= nd;
+        }
+        a[i] = ((key & 0xFFFFFFFFFFull) << 24) | (unsigned long long)i;
+      } else {
+        a[i] = ~0ull;
+      }
+    }
+    sync();
+    block_bitonic_sort(a, sort_n);
+    int ncells = 0;
+    for (int base = 0; base < N; base += GCR_BLOCK) {
+      const int i = base + threadIdx.x;
+      int f = 0;
+      if (i < N) {
+        slot.cell_pts[i] = (int)(a[i] & 0xFFFFFFull);
+        f = (i == 0) || ((a[i] >> 24) != (a[i - 1] >> 24));
+      }
+      int tot;
+      const int pos = block_exclusive_scan(f, sh.red_i, &tot);
+      if (f) slot.cell_start[ncells + pos] = i;
+      ncells += tot;
+    }
+    if (threadIdx.x == 0) slot.cell_start[ncells] = N;
+    sync();
+    return ncells;
+  }
+
+  // ------------------------------------------------------------------
+  // s-t min cut of one grid cell (a clique plus terminal arcs) by one warp.
+  // The labelling graph is built as in GCRANSAC::labeling (GCRANSAC.h:945-1007)
+  // with Energy::add_term1/add_term2 (energy.h:203-253): node i of the cell
+  // gets the terminal capacity tr_i = unary_i - sum_{j>i} lambda (d_i + d_j)/2,
+  // the arc i->j (i < j) lambda - lambda (d_i + d_j)/2 and the arc j->i lambda.
+  // FIFO push-relabel with exact initial distance labels computes a maximum
+  // preflow; then a backward search from the sink over residuals above
+  // kResidualEps marks the SINK side (what_segment == SINK, graph.h:478-483).
+  // Writes slot.flag[point] for the cell's points. Returns false on the step cap.
+  __device__ bool mincut_cell(int c0, int n, int warp) {
+    const int lane = threadIdx.x & 31;
+    const double lam = prm.lambda;
+    double* R = slot.flow + (size_t)warp * kMaxFlowCap * kMaxFlowCap;
+    double* ex = slot.node_d + (size_t)warp * 3 * kMaxFlowCap;
+    double* sr = ex + kMaxFlowCap;
+    int* h = slot.node_i + (size_t)warp * 3 * kMaxFlowCap;
+    int* q = h + kMaxFlowCap;
+    int* mark = q + kMaxFlowCap;
+    const int* gp = slot.cell_pts + c0;
+    const double* d = slot.dres;
+    for (int e = lane; e < n * n; e += 32) {
+      const int i = e / n, j = e - i * n;
+      double v = 0.0;
+      if (i < j) v = lam - (0.5 * (d[gp[i]] + d[gp[j]])) * lam;
+      else if (i > j) v = lam;
+      R[e] = v;
+    }
+    for (int i = lane; i < n; i += 32) {
+      double t = slot.tr[gp[i]];
+      const double di = d[gp[i]];
+      for (int j = i + 1; j < n; ++j) t = t - (0.5 * (di + d[gp[j]])) * lam;
+      ex[i] = t > 0 ? t : 0.0;
+      sr[i] = t < 0 ? -t : 0.0;
+      mark[i] = 0;
+    }
+    __syncwarp();
+    const int dead = n + 2;
+    // exact distance labels: backward BFS from the sink over residual arcs
+    for (int i = lane; i < n; i += 32) h[i] = sr[i] > 0 ? 1 : dead;
+    __syncwarp();
+    for (int level = 1; level <= n; ++level) {
+      bool grew = false;
+      for (int u = lane; u < n; u += 32) {
+        if (h[u] != dead) continue;
+        for (int v = 0; v < n; ++v)
+          if (h[v] == level && R[u * n + v] > 0) {
+            h[u] = -(level + 1);
+            break;
+          }
+      }
+      __syncwarp();
+      for (int u = lane; u < n; u += 32)
+        if (h[u] < 0) {
+          h[u] = -h[u];
+          grew = true;
+        }
+      __syncwarp();
+      if (!__any_sync(0xffffffffu, grew)) break;
+    }
+    // FIFO of active nodes (positive excess and a finite label)
+    int qh = 0, qt = 0;
+    for (int base = 0; base < n; base += 32) {
+      const int u = base + lane;
+      const bool act = u < n && ex[u] > 0 && h[u] < dead;
+      const unsigned b = __ballot_sync(0xffffffffu, act);
+      if (act) {
+        q[(qt + __popc(b & ((1u << lane) - 1))) % kMaxFlowCap] = u;
+        mark[u] = 1;
+      }
+      qt += __popc(b);
+    }
+    __syncwarp();
+    long long ops = 0;
+    bool ok = true;
+    while (qh != qt) {
+      const int u = q[qh % kMaxFlowCap];
+      ++qh;
+      __syncwarp();
+      if (lane == 0) mark[u] = 0;
+      __syncwarp();
+      for (;;) {
+        if (++ops > kFlowOpsCap) { ok = false; break; }
+        double e = ex[u];
+        const int hu = h[u];
+        if (!(e > 0) || hu >= dead) break;
+        if (hu == 1 && sr[u] > 0) {
+          __syncwarp();
+          if (lane == 0) {
+            const double s = sr[u];
+            const double dl = e < s ? e : s;
+            ex[u] = e - dl;
+            sr[u] = s - dl;
+          }
+          __syncwarp();
+          e = ex[u];
+          if (!(e > 0)) break;
+        }
+        for (int base = 0; base < n && e > 0; base += 32) {
+          const int v = base + lane;
+          const bool adm = v < n && v != u && h[v] == hu - 1 && R[u * n + v] > 0;
+          unsigned b = __ballot_sync(0xffffffffu, adm);
+          while (b != 0u && e > 0) {
+            const int vv = base + __ffs(b) - 1;
+            b &= b - 1;
+            int enq = 0;
+            __syncwarp();
+            if (lane == 0) {
+              const double r = R[u * n + vv];
+              const double dl = e < r ? e : r;
+              R[u * n + vv] = r - dl;
+              R[vv * n + u] = R[vv * n + u] + dl;
+              ex[u] = e - dl;
+              ex[vv] = ex[vv] + dl;
+              if (!mark[vv] && h[vv] < dead) {
+                mark[vv] = 1;
+                q[qt % kMaxFlowCap] = vv;
+                enq = 1;
+              }
+            }
+            enq = __shfl_sync(0xffffffffu, enq, 0);
+            qt += enq;
+            __syncwarp();
+            e = ex[u];
+          }
+        }
+        if (!(e > 0)) break;
+        // relabel: 1 + min label over residual arcs (the sink has label 0)
+        int mn = sr[u] > 0 ? 0 : 0x7fffffff;
+        for (int v = lane; v < n; v += 32)
+          if (v != u && R[u * n + v] > 0 && h[v] < mn) mn = h[v];
+        mn = warp_min(mn);
+        __syncwarp();
+        if (lane == 0) h[u] = (mn == 0x7fffffff || mn + 1 >= dead) ? dead : mn + 1;
+        __syncwarp();
+      }
+      if (!ok) break;
+    }
+    __syncwarp();
+    // SINK side: backward search from the sink over residuals > kResidualEps
+    for (int i = lane; i < n; i += 32) mark[i] = sr[i] > kResidualEps ? 1 : 0;
+    __syncwarp();
+    for (int round = 0; round < n; ++round) {
+      bool grew = false;
+      for (int u = lane; u < n; u += 32) {
+        if (mark[u]) continue;
+        for (int v = 0; v < n; ++v)
+          if (mark[v] == 1 && R[u * n + v] > kResidualEps) {
+            mark[u] = 2;
+            break;
+          }
+      }
+      __syncwarp();
+      for (int u = lane; u < n; u += 32)
+        if (mark[u] == 2) {
+          mark[u] = 1;
+          grew = true;
+        }
+      __syncwarp();
+      if (!__any_sync(0xffffffffu, grew)) break;
+    }
+    for (int i = lane; i < n; i += 32) slot.flag[gp[i]] = (uint8_t)mark[i];
+    __syncwarp();
+    return ok;
+  }
+
+  // GCRANSAC::labeling (GCRANSAC.h:912-1021): writes the SINK points in index
+  // order into `list` and returns their number.
+  __device__ int labeling(const double* model, int ncells, int* list) {
+    const double sq = t2;  // thr^2 * 9 / 4
+    const double oml = 1.0 - prm.lambda;
+    double h[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) h[k] = model[k];
+    for (int i = threadIdx.x; i < N; i += GCR_BLOCK) {
+      const double r2 = Est::r2_f64(pts64 + 4 * i, h);
+      double di = r2 / sq;
+      di = di < 0.0 ? 0.0 : (di > 1.0 ? 1.0 : di);
+      const double e = 1 - di;
+      slot.dres[i] = di;
+      slot.tr[i] = r2 <= sq ? 0 - oml * e : oml * (1 - e) - 0;
+    }
+    sync();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) sh.flow_status = 0;
+    sync();
+    const bool pairwise = prm.lambda > 0;
+    for (int c = warp; c < ncells; c += GCR_WARPS) {
+      const int c0 = slot.cell_start[c], n = slot.cell_start[c + 1] - c0;
+      if (n == 1 || !pairwise) {
+        for (int k = lane; k < n; k += 32) {
+          const int p = slot.cell_pts[c0 + k];
+          slot.flag[p] = (uint8_t)(-slot.tr[p] > kResidualEps ? 1 : 0);
+        }
+      } else if (n > kMaxFlowCap) {
+        if (lane == 0) atomicMax(&sh.flow_status, ST_CAPACITY);
+      } else if (!mincut_cell(c0, n, warp)) {
+        if (lane == 0) atomicMax(&sh.flow_status, ST_TIMEOUT);
+      }
+    }
+    sync();
+    if (sh.flow_status != 0 && status == ST_OK) status = sh.flow_status;
+    int total = 0;
+    for (int base = 0; base < N; base += GCR_BLOCK) {
+      const int i = base + threadIdx.x;
+      const int f = (i < N) ? slot.flag[i] : 0;
+      int tot;
+      const int pos = block_exclusive_scan(f, sh.red_i, &tot);
+      if (f) list[total + pos] = i;
+      total += tot;
+    }
+    return total;
+  }
+
+  // ------------------------------------------------------------------
+  // CTA-wide normalised weighted least squares over the rows list[0..n).
+  // weight_mode 0: unit weights; 1: the iterated-least-squares weights of the
+  // reference, where packed row k gets weights[k] of the point INDEX k
+  // (GCRANSAC.h:657-675 with homography_estimator.h:161-165 and
+  // solver_homography_four_point.h:211-224): Tukey^2 of point k under
+  // sh.work_model when point k is in the set (slot.flag), else 0.
+  // Result in sh.fit_model; returns success (uniform).
+  __device__ bool fit_cta(const int* list, int n, int weight_mode) {
+    if (n < Est::NONMIN) return false;
+    double s[4] = {0, 0, 0, 0};
+    for (int k = threadIdx.x; k < n; k += GCR_BLOCK) {
+      const double* p = pts64 + 4 * list[k];
+      s[0] += p[0]; s[1] += p[1]; s[2] += p[2]; s[3] += p[3];
+    }
+    typename Est::Norm nm;
+    nm.ms0 = block_sum(s[0], sh.red_d) / n;
+    nm.ms1 = block_sum(s[1], sh.red_d) / n;
+    nm.md0 = block_sum(s[2], sh.red_d) / n;
+    nm.md1 = block_sum(s[3], sh.red_d) / n;
+    double a = 0, b = 0;
+    for (int k = threadIdx.x; k < n; k += GCR_BLOCK) {
+      const double* p = pts64 + 4 * list[k];
+      const double dx1 = nm.ms0 - p[0], dy1 = nm.ms1 - p[1], dx2 = nm.md0 - p[2], dy2 = nm.md1 - p[3];
+      a += sqrt(dx1 * dx1 + dy1 * dy1);
+      b += sqrt(dx2 * dx2 + dy2 * dy2);
+    }
+    nm.rs = M_SQRT2 / (block_sum(a, sh.red_d) / n);
+    nm.rd = M_SQRT2 / (block_sum(b, sh.red_d) / n);
+    constexpr int NA = Est::NACC;
+    double acc[NA];
+#pragma unroll
+    for (int q = 0; q < NA; ++q) acc[q] = 0;
+    double wm[9];
+    if (weight_mode == 1) {
+#pragma unroll
+      for (int q = 0; q < 9; ++q) wm[q] = sh.work_model[q];
+    }
+    for (int k = threadIdx.x; k < n; k += GCR_BLOCK) {
+      double w = 1.0;
+      if (weight_mode == 1) {
+        w = 0.0;
+        if (k < N && slot.flag[k]) {
+          const double r2 = Est::r2_f64(pts64 + 4 * k, wm);
+          const double wt = fmax(0.0, 1.0 - r2 / t2);
+          w = wt * wt;
+        }
+      }
+      Est::accumulate(nm, pts64 + 4 * list[k], w, acc);
+    }
+    // deterministic reduction: warp trees, then warp partials in order
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NA; ++q) {
+      const double v = warp_sum(acc[q]);
+      if (lane == 0) sh.red_d[warp * 48 + q] = v;
+    }
+    sync();
+    if (threadIdx.x == 0) {
+      double tot[NA];
+      for (int q = 0; q < NA; ++q) {
+        double t = 0;
+        for (int w = 0; w < GCR_WARPS; ++w) t += sh.red_d[w * 48 + q];
+        tot[q] = t;
+      }
+      sh.fit_ok = Est::solve_normal(nm, tot, sh.fit_model) ? 1 : 0;
+    }
+    sync();
+    return sh.fit_ok != 0;
+  }
+
+  // ------------------------------------------------------------------
+  // GCRANSAC::graphCutLocalOptimization (GCRANSAC.h:779-910).
+  __device__ void local_optimization(int ncells) {
+    Score max_score = best;
+    copy_model(sh.lo_best_model, sh.best_model);
+    const int inlier_limit = Est::INLIER_LIMIT;
+    int* L = slot.list0;
+    const int trials = prm.lo_number;
+    ++lo_number;
+    while (++gc_number < 10) {
+      bool updated = false;
+      const int nL = labeling(sh.lo_best_model, ncells, L);
+      const int ss = min(inlier_limit, nL);
+      if (ss < nL) {
+        // trials sample from the labelled inliers with the LO sampler stream
+        const int kb = kBatchModels;
+        if (threadIdx.x < trials) {
+          int* smp = slot.samples + threadIdx.x * Est::SAMPLE_CAP;
+          DrawStream ds(pd.seed, STREAM_LO, (uint64_t)(lo_calls + threadIdx.x));
+          bool ok = unique_set(ds, smp, ss, 0, (uint32_t)(nL - 1));
+          if (ok) {
+            for (int q = 0; q < ss; ++q) smp[q] = L[smp[q]];
+            ok = Est::fit_thread(pts64, smp, ss, nullptr, slot.models64 + 9 * (kb + threadIdx.x));
+          }
+          sh.lo_ok[threadIdx.x] = ok ? 1 : 0;
+          if (ok) put_f32(kb + threadIdx.x);
+        }
+        sync();
+        lo_calls += trials;
+        score_lo_trials(kb, trials, max_score, updated);
+      } else if (m < nL) {
+        if (!fit_cta(L, nL, 0)) {
+          // the reference breaks out of the trial loop; nothing was updated
+        } else {
+          const Score sc = exact_score(sh.fit_model, nullptr);
+          if (max_score.value < sc.value) {
+            updated = true;
+            max_score = sc;
+            copy_model(sh.lo_best_model, sh.fit_model);
+          }
+        }
+      }
+      if (!updated) break;
+    }
+    if (best.value < max_score.value) {
+      best = max_score;
+      copy_model(sh.best_model, sh.lo_best_model);
+      copy_model(sh.cont_model[off], sh.lo_best_model);
+      cont[off] = {sh.cont_model[off], max_score.count};
+    }
+  }
+
+  // Scores the LO trial models kb..kb+trials (their success flags in the
+  // trial-flag array) and replays the sequential best-model update.
+  __device__ void score_lo_trials(int kb, int trials, Score& max_score, bool& updated) {
+    score_models_f32(kb, trials);
+    for (int t = 0; t < trials; ++t) {
+      if (!sh.lo_ok[t]) continue;
+      const int k = kb + t;
+      if (sh.mcount[k] == 0 || !maybe_better(k, max_score.value)) continue;
+      const Score sc = exact_score(slot.models64 + 9 * k, nullptr);
+      if (max_score.value < sc.value) {
+        updated = true;
+        max_score = sc;
+        copy_model(sh.lo_best_model, slot.models64 + 9 * k);
+      }
+    }
+  }
+
+  // ------------------------------------------------------------------
+  // Materialises the inlier list of a container's model into `list`.
+  __device__ int materialise(const Container& c, int* list) {
+    if (c.model == nullptr) return 0;
+    return exact_score(c.model, list).count;
+  }
+
+  // GCRANSAC::iteratedLeastSquaresFitting (GCRANSAC.h:629-758) for estimators
+  // with one model per fit. `list`/`n` is the container being refined in
+  // place (its model is tracked through sh.work_model). Returns iterations > 1.
+  __device__ bool irls(int*& list, int& n, int*& spare) {
+    if (n <= m) return false;
+    int iterations = 0;
+    while (++iterations < 10) {
+      // membership flags of the current set (the weights array of the reference)
+      for (int i = threadIdx.x; i < N; i += GCR_BLOCK) slot.flag[i] = 0;
+      sync();
+      for (int k = threadIdx.x; k < n; k += GCR_BLOCK) slot.flag[list[k]] = 1;
+      sync();
+      if (!fit_cta(list, n, 1)) break;
+      const Score sc = exact_score(sh.fit_model, spare);
+      if (sc.count < m) break;
+      if (sc.count <= n) break;
+      copy_model(sh.work_model, sh.fit_model);
+      int* t = list;
+      list = spare;
+      spare = t;
+      n = sc.count;
+    }
+    return iterations > 1;
+  }
+
+  // ------------------------------------------------------------------
+  // One batch of main-sampler calls [a0, a0 + GCR_BLOCK): thread j draws call
+  // a0 + j, checks the sample, runs the minimal solver and writes its models
+  // compacted into the slot table; sh.n_ok[j] / sh.mbase[j] describe them.
+  __device__ int generate_batch(long long a0, long long& p_kth, long long& p_subset, long long& p_hi,
+                                double& p_Tn, long long& p_Tprime) {
+    const int j = threadIdx.x;
+    int s[Est::M];
+    bool ok = false;
+    if (prm.sampler == SAMPLER_UNIFORM) {
+      DrawStream ds(pd.seed, STREAM_MAIN, (uint64_t)(a0 + j));
+      ok = unique_set(ds, s, m, 0, (uint32_t)(N - 1));
+    } else {
+      // PROSAC (samplers/prosac_sampler.h:51-237): every thread replays the
+      // state machine for the whole batch and keeps its own call's draw range.
+      const long long conv = 100000;
+      long long my_hi = 0, my_last = 0;
+      bool my_global = false;
+      for (int c = 0; c < GCR_BLOCK; ++c) {
+        if (c == j) {
+          my_global = p_kth > conv;
+          my_hi = p_hi;
+          my_last = p_subset - 1;
+        }
+        if (p_kth > conv) continue;
+        ++p_kth;
+        if (p_kth > conv) {
+          p_hi = N - 1;
+        } else {
+          // growth[subset - 1] is kept in p_Tprime; compute the next one lazily
+          if (p_kth > p_Tprime) {
+            const long long before = p_subset;
+            ++p_subset;
+            if (p_subset > N) p_subset = N;
+            p_hi = p_subset - 2;
+            // advance the growth function to index p_subset - 1
+            const long long i = p_subset - 1;
+            if (p_subset != before && i + 1 > m) {
+              const double Tn1 = (double)(i + 1) * p_Tn / (double)(i + 1 - m);
+              p_Tprime = p_Tprime + (long long)(unsigned int)ceil(Tn1 - p_Tn);
+              p_Tn = Tn1;
+            }
+          }
+        }
+      }
+      DrawStream ds(pd.seed, STREAM_MAIN, (uint64_t)(a0 + j));
+      if (my_global) {
+        ok = unique_set(ds, s, m, 0, (uint32_t)(N - 1));
+      } else {
+        ok = unique_set(ds, s, m - 1, 0, (uint32_t)my_hi);
+        s[m - 1] = (int)my_last;
+      }
+    }
+    double mloc[9 * Est::MAXSOL];
+    int nm = 0;
+    if (ok && Est::valid_sample(pts64, s)) nm = Est::minimal(pts64, s, mloc);
+    int total;
+    const int base = block_exclusive_scan(nm, sh.red_i, &total);
+    sh.n_ok[j] = nm;
+    sh.mbase[j] = base;
+    for (int q = 0; q < nm; ++q) {
+      double* dst = slot.models64 + 9 * (base + q);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) dst[k] = mloc[9 * q + k];
+      put_f32(base + q);
+    }
+    sync();
+    return total;
+  }
+
+  // ------------------------------------------------------------------
+  __device__ void run() {
+    const int ncells = build_grid();
+    max_iter = iteration_number_for(1, N, m, log_prob);
+    const long long max_iters = prm.max_iters, min_iters = prm.min_iters;
+    // PROSAC state: kth, subset size, draw range, T_n, growth[subset-1]
+    long long p_kth = 1, p_subset = m, p_hi = m - 1, p_Tprime = 1;
+    double p_Tn = 100000.0;
+    for (int i = 0; i < m; ++i) p_Tn *= (double)(m - i) / (double)(N - i);
+    long long attempt = 0;
+    bool done = false, in_iter = false;
+    int nfail = 0;
+    const long long attempt_cap = (max_iters < 0x7fffffffLL ? max_iters : 0x7fffffffLL) * 101 + 101;
+    while (!done) {
+      generate_batch(attempt, p_kth, p_subset, p_hi, p_Tn, p_Tprime);
+      const int K = sh.mbase[GCR_BLOCK - 1] + sh.n_ok[GCR_BLOCK - 1];
+      score_models_f32(0, K);
+      for (int j = 0; j < GCR_BLOCK; ++j) {
+        if (!in_iter) {
+          const long long lim = max_iter < max_iters ? max_iter : max_iters;
+          if (!(min_iters > iter || iter < lim)) {
+            done = true;
+            break;
+          }
+          ++iter;
+          in_iter = true;
+          nfail = 0;
+        }
+        const int nm = sh.n_ok[j];
+        if (nm == 0) {
+          if (++nfail == 100) {
+            iter += 100;
+            in_iter = false;
+          }
+          continue;
+        }
+        iter += nfail;
+        in_iter = false;
+        bool do_lo = false;
+        for (int q = 0; q < nm; ++q) {
+          const int k = sh.mbase[j] + q;
+          const double* mk = slot.models64 + 9 * k;
+          cont[off] = {mk, sh.mcount[k]};
+          if (sh.mcount[k] == 0 || !maybe_better(k, best.value)) continue;
+          const Score sc = exact_score(mk, nullptr);
+          if (best.value < sc.value && Est::valid_model(mk)) {
+            off ^= 1;
+            copy_model(sh.best_model, mk);
+            best = sc;
+            do_lo = iter > 20 && best.count > m;
+            max_iter = iteration_number_for(best.count, N, m, log_prob);
+          }
+        }
+        if (do_lo) {
+          ++lo_number;
+          local_optimization(ncells);
+          max_iter = iteration_number_for(best.count, N, m, log_prob);
+        }
+      }
+      attempt += GCR_BLOCK;
+      // containers that point into the batch table are copied out before reuse
+      for (int c = 0; c < 2; ++c) {
+        if (cont[c].model != nullptr && cont[c].model >= slot.models64 &&
+            cont[c].model < slot.models64 + 9 * kBatchModels) {
+          copy_model(sh.cont_model[c], cont[c].model);
+          cont[c].model = sh.cont_model[c];
+        }
+      }
+      if (attempt > attempt_cap) {
+        if (status == ST_OK) status = ST_TIMEOUT;
+        done = true;
+      }
+    }
+    finish(ncells);
+  }
+
+  __device__ void finish(int ncells) {
+    StatsOut* so = ws.stats_out + pair;
+    uint8_t* mask = ws.masks_out + pd.offset;
+    if (best.count <= m) {
+      for (int i = threadIdx.x; i < N; i += GCR_BLOCK) mask[i] = 0;
+      if (threadIdx.x < 9) ws.models_out[9 * pair + threadIdx.x] = 0.0;
+      if (threadIdx.x == 0) {
+        so->iteration_number = iter;
+        so->graph_cut_number = gc_number;
+        so->local_optimization_number = lo_number;
+        so->inlier_number = 0;
+        so->score = best.value;
+        so->status = status == ST_OK ? ST_NO_MODEL : status;
+        so->flags = flags;
+      }
+      return;
+    }
+    if (lo_number == 0) {
+      ++lo_number;
+      local_optimization(ncells);
+    }
+    if (cont[off].count != best.count) off ^= 1;
+    if (cont[off].count != best.count) {
+      copy_model(sh.cont_model[off], sh.best_model);
+      best = exact_score(sh.best_model, nullptr);
+      cont[off] = {sh.cont_model[off], best.count};
+    }
+    // materialise the container; the IRLS refines it in place
+    int* list = slot.list1;
+    int* spare = slot.list2;
+    int n = materialise(cont[off], list);
+    copy_model(sh.work_model, sh.best_model);
+    bool irls_applied = false;
+    const bool ok = irls(list, n, spare);
+    if (ok) {
+      // the container now holds the inliers of the IRLS model
+      copy_model(sh.cont_model[off], sh.work_model);
+      cont[off] = {sh.cont_model[off], n};
+      const int idx = off ^ 1;
+      const Score sc = exact_score(sh.work_model, nullptr);
+      copy_model(sh.cont_model[idx], sh.work_model);
+      cont[idx] = {sh.cont_model[idx], sc.count};
+      if (best.value < sc.value) {
+        irls_applied = true;
+        copy_model(sh.best_model, sh.work_model);
+        off = idx;
+      }
+    }
+    if (!irls_applied) {
+      // one least-squares fit on the first best.count points of the container
+      if (fit_cta(list, best.count < n ? best.count : n, 0)) {
+        const int idx = off ^ 1;
+        const Score sc = exact_score(sh.fit_model, nullptr);
+        copy_model(sh.cont_model[idx], sh.fit_model);
+        cont[idx] = {sh.cont_model[idx], sc.count};
+        if (best.value < sc.value) {
+          copy_model(sh.best_model, sh.fit_model);
+          off = idx;
+        }
+      }
+    }
+    if (irls_applied) flags |= 2;
+    if (lo_number > 0) flags |= 1;
+    // output: model and the inliers of the final container
+    const int cnt = materialise(cont[off], list);
+    for (int i = threadIdx.x; i < N; i += GCR_BLOCK) mask[i] = 0;
+    sync();
+    for (int k = threadIdx.x; k < cnt; k += GCR_BLOCK) mask[list[k]] = 1;
+    if (threadIdx.x < 9) ws.models_out[9 * pair + threadIdx.x] = sh.best_model[threadIdx.x];
+    if (threadIdx.x == 0) {
+      so->iteration_number = iter;
+      so->graph_cut_number = gc_number;
+      so->local_optimization_number = lo_number;
+      so->inlier_number = cnt;
+      so->score = best.value;
+      so->status = status;
+      so->flags = flags;
+    }
+    sync();
+  }
+};
+
+}  // namespace gcr

@@ -1,0 +1,35 @@
+// Host-side table of the per-model-kind engine instantiations. Each kind's
+// kernel lives in its own translation unit (gcr_kind_*.cu) so the three
+// compile in parallel.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+namespace gcr {
+
+struct Slot;
+struct Workspace;
+struct EngineParams;
+
+struct KindOps {
+  int sample_size;
+  size_t (*shared_bytes)();
+  size_t (*slot_bytes)(int max_n, int sort_cap);
+  void (*carve)(unsigned char* base, int max_n, int sort_cap, Slot* out);
+  cudaError_t (*prepare)();  // one-time kernel attribute setup
+  cudaError_t (*occupancy)(int* blocks_per_sm);
+  cudaError_t (*launch)(int grid, cudaStream_t stream, const Workspace& ws, const EngineParams& prm);
+};
+
+const KindOps* homography_ops();
+const KindOps* fundamental_ops();
+const KindOps* essential_ops();
+
+// K^-1 normalisation of essential-matrix correspondences (utils.h:65-103 of
+// the reference), one thread per correspondence.
+cudaError_t launch_normalise_essential(const double* corr, const double* kinv, const long long* pair_of_row,
+                                       long long rows, double* out, cudaStream_t stream);
+
+}  // namespace gcr

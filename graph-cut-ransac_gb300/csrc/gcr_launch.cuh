@@ -1,0 +1,108 @@
+// Kernel entry and host-side launcher of the pair engine for one model kind.
+#pragma once
+
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "gcr_engine.cuh"
+
+namespace gcr {
+
+__device__ inline double block_max_abs(double v, double* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  double r = 0;
+  for (int i = 0; i < GCR_WARPS; ++i) r = fmax(r, red[i]);
+  __syncthreads();
+  return r;
+}
+
+// Persistent kernel: each CTA takes pairs from a global ticket until none is
+// left; blockIdx.x selects the CTA's scratch slot.
+template <class Est>
+__global__ void __launch_bounds__(GCR_BLOCK, 1) pair_kernel(Workspace ws, EngineParams prm) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Shared<Est>& sh = *reinterpret_cast<Shared<Est>*>(smem_raw);
+  __shared__ int s_pair;
+  const Slot slot = ws.slots[blockIdx.x];
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_pair = atomicAdd(ws.ticket, 1);
+    __syncthreads();
+    const int pair = s_pair;
+    if (pair >= prm.num_pairs) break;
+    const PairDesc pd = ws.pairs[pair];
+    Engine<Est> eng(sh, ws, prm, pd, slot, pair);
+    // centred FP32 copy of the correspondences: shared memory when it fits
+    const double* p64 = ws.pts64 + 4 * pd.offset;
+    const bool in_smem = pd.n <= kSmemPoints;
+    float4* dst = in_smem ? sh.pts : ws.pts32 + pd.offset;
+    double mx = 0.0;
+    for (int i = threadIdx.x; i < pd.n; i += GCR_BLOCK) {
+      const double a = p64[4 * i] - pd.centre[0], b = p64[4 * i + 1] - pd.centre[1];
+      const double c = p64[4 * i + 2] - pd.centre[2], d = p64[4 * i + 3] - pd.centre[3];
+      dst[i] = make_float4((float)a, (float)b, (float)c, (float)d);
+      mx = fmax(mx, fmax(fmax(fabs(a), fabs(b)), fmax(fabs(c), fabs(d))));
+    }
+    eng.scale = block_max_abs(mx, sh.red_d);
+    eng.pts32 = dst;
+    __syncthreads();
+    eng.run();
+  }
+}
+
+template <class Est>
+size_t shared_bytes() {
+  return sizeof(Shared<Est>);
+}
+
+// Scratch bytes of one slot for pairs of at most max_n correspondences.
+template <class Est>
+size_t slot_bytes(int max_n, int sort_cap) {
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  size_t s = 0;
+  s += al(sizeof(double) * 9 * Shared<Est>::kModels);
+  s += al(sizeof(float) * 12 * Shared<Est>::kModels);
+  s += al(sizeof(int) * GCR_BLOCK * Est::SAMPLE_CAP);
+  s += 3 * al(sizeof(int) * max_n);
+  s += al((size_t)max_n);
+  s += 2 * al(sizeof(double) * max_n);
+  s += al(sizeof(unsigned long long) * sort_cap);
+  s += al(sizeof(int) * max_n);
+  s += al(sizeof(int) * (max_n + 1));
+  s += al(sizeof(double) * GCR_WARPS * kMaxFlowCap * kMaxFlowCap);
+  s += al(sizeof(double) * GCR_WARPS * 3 * kMaxFlowCap);
+  s += al(sizeof(int) * GCR_WARPS * 3 * kMaxFlowCap);
+  return s;
+}
+
+template <class Est>
+Slot carve_slot(unsigned char* base, int max_n, int sort_cap) {
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  Slot s;
+  unsigned char* p = base;
+  auto take = [&](size_t b) { unsigned char* r = p; p += al(b); return r; };
+  s.models64 = (double*)take(sizeof(double) * 9 * Shared<Est>::kModels);
+  s.models32 = (float*)take(sizeof(float) * 12 * Shared<Est>::kModels);
+  s.samples = (int*)take(sizeof(int) * GCR_BLOCK * Est::SAMPLE_CAP);
+  s.list0 = (int*)take(sizeof(int) * max_n);
+  s.list1 = (int*)take(sizeof(int) * max_n);
+  s.list2 = (int*)take(sizeof(int) * max_n);
+  s.flag = (uint8_t*)take((size_t)max_n);
+  s.dres = (double*)take(sizeof(double) * max_n);
+  s.tr = (double*)take(sizeof(double) * max_n);
+  s.sortbuf = (unsigned long long*)take(sizeof(unsigned long long) * sort_cap);
+  s.cell_pts = (int*)take(sizeof(int) * max_n);
+  s.cell_start = (int*)take(sizeof(int) * (max_n + 1));
+  s.flow = (double*)take(sizeof(double) * GCR_WARPS * kMaxFlowCap * kMaxFlowCap);
+  s.node_d = (double*)take(sizeof(double) * GCR_WARPS * 3 * kMaxFlowCap);
+  s.node_i = (int*)take(sizeof(int) * GCR_WARPS * 3 * kMaxFlowCap);
+  return s;
+}
+
+}  // namespace gcr

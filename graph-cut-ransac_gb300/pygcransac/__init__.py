@@ -1,0 +1,171 @@
+"""Drop-in ``pygcransac`` entry points backed by the GB300 engine (libgcr.so).
+
+Function names, argument names, defaults and return conventions follow the
+reference binding (src/pygcransac/src/bindings.cpp:1003-1022, 1091-1112,
+1158-1178): each call returns ``(model 3x3 float64 or None, mask bool[N])`` and
+raises ``ValueError`` for a bad shape or too few correspondences. Added keyword
+arguments: ``seed`` (the sampler streams are seeded and replayable) and, in
+``find_batch``, many image pairs in one device launch.
+
+There is no CPU fallback: a missing libgcr.so raises ImportError on first use,
+and options the device engine does not provide raise NotImplementedError.
+"""
+import numpy as np
+
+from . import _abi
+
+__all__ = ["findHomography", "findFundamentalMatrix", "findEssentialMatrix", "find_batch", "default_params",
+           "GCRError"]
+
+
+class GCRError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{_abi.STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+def default_params(kind):
+    """gcr_params filled with the reference binding's defaults for `kind`."""
+    import ctypes
+    p = _abi.Params()
+    _abi.load().gcr_default_params(kind, ctypes.byref(p))
+    return p
+
+
+def _params(kind, threshold, conf, spatial_coherence_weight, max_iters, min_iters, use_sprt, sampler,
+            neighborhood, neighborhood_size, lo_number, use_space_partitioning=False, seed=0, scoring=0):
+    p = _abi.Params()
+    p.threshold = float(threshold)
+    p.confidence = float(conf)
+    p.spatial_coherence_weight = float(spatial_coherence_weight)
+    p.neighborhood_size = float(neighborhood_size)
+    p.max_iterations = int(max_iters)
+    p.min_iterations = int(min_iters)
+    p.sampler = int(sampler)
+    p.neighborhood = int(neighborhood)
+    p.lo_number = int(lo_number)
+    p.scoring = int(scoring)
+    p.use_sprt = int(bool(use_sprt))
+    p.use_space_partitioning = int(bool(use_space_partitioning))
+    p.seed = int(seed)
+    return p
+
+
+def _check_corr(correspondences, m, what):
+    c = np.ascontiguousarray(correspondences, dtype=np.float64)
+    if c.ndim != 2 or c.shape[1] != 4:
+        raise ValueError(f"correspondences should be an array with dims [n,4], n>={m}")
+    if c.shape[0] < m:
+        raise ValueError(f"correspondences should be an array with dims [n,d], n>={m}")
+    return c
+
+
+def _raise_for(rc, where):
+    if rc in (_abi.GCR_OK, _abi.GCR_NO_MODEL):
+        return
+    msg = _abi.last_error()
+    if rc == _abi.GCR_UNSUPPORTED:
+        raise NotImplementedError(f"{where}: {msg}")
+    if rc in (_abi.GCR_INVALID_ARG, _abi.GCR_TOO_FEW_POINTS):
+        raise ValueError(f"{where}: {msg}")
+    raise GCRError(rc, f"{where}: {msg}")
+
+
+def _run_one(kind, corr, size, params, K1=None, K2=None, return_stats=False):
+    import ctypes
+    lib = _abi.load()
+    n = corr.shape[0]
+    model = np.zeros(9)
+    mask = np.zeros(n, np.uint8)
+    st = _abi.Stats()
+    sz = _abi.ImageSize(*[int(v) for v in size])
+    if kind == _abi.GCR_HOMOGRAPHY:
+        rc = lib.gcr_find_homography(_abi.ptr(corr), n, ctypes.byref(sz), None, ctypes.byref(params),
+                                     _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
+    elif kind == _abi.GCR_FUNDAMENTAL:
+        rc = lib.gcr_find_fundamental(_abi.ptr(corr), n, ctypes.byref(sz), None, ctypes.byref(params),
+                                      _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
+    else:
+        K1 = np.ascontiguousarray(K1, np.float64).reshape(9)
+        K2 = np.ascontiguousarray(K2, np.float64).reshape(9)
+        rc = lib.gcr_find_essential(_abi.ptr(corr), n, _abi.ptr(K1), _abi.ptr(K2), ctypes.byref(sz), None,
+                                    ctypes.byref(params), _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
+    _raise_for(rc, ["findHomography", "findFundamentalMatrix", "findEssentialMatrix"][kind])
+    maskb = mask.astype(bool)
+    out = (None if rc == _abi.GCR_NO_MODEL or maskb.sum() == 0 else model.reshape(3, 3), maskb)
+    return out + (st,) if return_stats else out
+
+
+def findHomography(correspondences, h1, w1, h2, w2, probabilities=None, threshold=1.0, conf=0.99,
+                   spatial_coherence_weight=0.975, max_iters=10000, min_iters=50, use_sprt=True,
+                   min_inlier_ratio_for_sprt=0.00001, sampler=1, neighborhood=0, neighborhood_size=4.0,
+                   use_space_partitioning=True, lo_number=50, sampler_variance=0.1, solver=0, seed=0,
+                   return_stats=False):
+    """Robust homography by Graph-Cut RANSAC (reference: bindings.cpp:859-983)."""
+    if solver != 0:
+        raise NotImplementedError("only point correspondences (solver=0) are provided")
+    c = _check_corr(correspondences, 4, "homography")
+    p = _params(_abi.GCR_HOMOGRAPHY, threshold, conf, spatial_coherence_weight, max_iters, min_iters, use_sprt,
+                sampler, neighborhood, neighborhood_size, lo_number, use_space_partitioning, seed)
+    return _run_one(_abi.GCR_HOMOGRAPHY, c, (h1, w1, h2, w2), p, return_stats=return_stats)
+
+
+def findFundamentalMatrix(correspondences, h1, w1, h2, w2, probabilities=None, threshold=1.0, conf=0.99,
+                          spatial_coherence_weight=0.0, max_iters=10000, min_iters=50, use_sprt=True,
+                          min_inlier_ratio_for_sprt=0.00001, sampler=1, neighborhood=1, neighborhood_size=20.0,
+                          lo_number=50, sampler_variance=0.1, solver=0, seed=0, return_stats=False):
+    """Robust fundamental matrix by Graph-Cut RANSAC (reference: bindings.cpp:279-401)."""
+    if solver != 0:
+        raise NotImplementedError("only point correspondences (solver=0) are provided")
+    c = _check_corr(correspondences, 7, "fundamental")
+    p = _params(_abi.GCR_FUNDAMENTAL, threshold, conf, spatial_coherence_weight, max_iters, min_iters, use_sprt,
+                sampler, neighborhood, neighborhood_size, lo_number, False, seed)
+    return _run_one(_abi.GCR_FUNDAMENTAL, c, (h1, w1, h2, w2), p, return_stats=return_stats)
+
+
+def findEssentialMatrix(correspondences, K1, K2, h1, w1, h2, w2, probabilities=None, threshold=1.0, conf=0.99,
+                        spatial_coherence_weight=0.1, max_iters=10000, min_iters=50, use_sprt=True,
+                        min_inlier_ratio_for_sprt=0.01, sampler=1, neighborhood=1, neighborhood_size=20.0,
+                        lo_number=50, sampler_variance=0.1, solver=0, seed=0, return_stats=False):
+    """Robust essential matrix by Graph-Cut RANSAC (reference: bindings.cpp:710-857)."""
+    if solver != 0:
+        raise NotImplementedError("only point correspondences (solver=0) are provided")
+    c = _check_corr(correspondences, 5, "essential")
+    p = _params(_abi.GCR_ESSENTIAL, threshold, conf, spatial_coherence_weight, max_iters, min_iters, use_sprt,
+                sampler, neighborhood, neighborhood_size, lo_number, False, seed)
+    return _run_one(_abi.GCR_ESSENTIAL, c, (h1, w1, h2, w2), p, K1=K1, K2=K2, return_stats=return_stats)
+
+
+def find_batch(kind, correspondences, sizes, params, seeds=None, K=None):
+    """Many pairs of one model kind in one device launch (host buffers).
+
+    correspondences: list of [n_i, 4] arrays or (concatenated [sum n_i, 4], offsets [P+1]).
+    sizes: [P, 4] (h1, w1, h2, w2); params: an _abi.Params; K: [P, 18] for essential matrices.
+    Returns (models [P, 3, 3], masks list of bool arrays, stats structured array).
+    """
+    lib = _abi.load()
+    if isinstance(correspondences, tuple):
+        corr, offsets = correspondences
+        corr = np.ascontiguousarray(corr, np.float64)
+        offsets = np.ascontiguousarray(offsets, np.int64)
+    else:
+        lens = [len(c) for c in correspondences]
+        offsets = np.zeros(len(lens) + 1, np.int64)
+        offsets[1:] = np.cumsum(lens)
+        corr = np.ascontiguousarray(np.concatenate(correspondences, 0), np.float64)
+    P = len(offsets) - 1
+    sz = np.zeros(P, _abi.SIZE_DTYPE)
+    s = np.asarray(sizes)
+    sz["h1"], sz["w1"], sz["h2"], sz["w2"] = s[:, 0], s[:, 1], s[:, 2], s[:, 3]
+    models = np.zeros((P, 9))
+    masks = np.zeros(int(offsets[-1]), np.uint8)
+    stats = np.zeros(P, _abi.STATS_DTYPE)
+    seeds_a = None if seeds is None else np.ascontiguousarray(seeds, np.uint64)
+    K_a = None if K is None else np.ascontiguousarray(K, np.float64)
+    import ctypes
+    rc = lib.gcr_find_batch(kind, P, _abi.ptr(corr), _abi.ptr(offsets), _abi.ptr(K_a), _abi.ptr(sz),
+                            ctypes.byref(params), _abi.ptr(seeds_a), _abi.ptr(models), _abi.ptr(masks),
+                            _abi.ptr(stats))
+    _raise_for(rc, "find_batch")
+    mb = masks.astype(bool)
+    return models.reshape(P, 3, 3), [mb[offsets[i]:offsets[i + 1]] for i in range(P)], stats

@@ -1,0 +1,195 @@
+"""Seeded synthetic image pairs with known ground truth.
+
+These stand in for the reference's real SIFT-matched image pairs (which need
+OpenCV to produce). Shapes, sizes and value distributions follow the benchmark
+workloads of this engine:
+
+* ``homography_pair``: N=2000 in 640x480, H = T(c) [s R(theta) | t] T(-c) with a
+  perspective row, theta ~ U(+-15 deg), s ~ U(0.8, 1.2), t ~ U(+-50 px),
+  p ~ U(+-1e-4); 40 % inliers with sigma = 1 px, uniform outliers.
+* ``two_view_pair``: points uniform in camera 1's frustum at depth 2-10 m,
+  focal 800 px, 640x480, camera 2 rotated by U(+-30 deg) about a random axis
+  and translated by a unit vector; inliers with sigma = 0.5 px, uniform
+  outliers. Used for both the fundamental (pixels) and essential (K known)
+  workloads.
+
+All generators use numpy ``Generator(PCG64(seed))``.
+"""
+import numpy as np
+
+W, H = 640, 480
+
+
+def _rng(seed):
+    return np.random.Generator(np.random.PCG64(seed))
+
+
+def _rot(axis, ang):
+    axis = axis / np.linalg.norm(axis)
+    K = np.array([[0, -axis[2], axis[1]], [axis[2], 0, -axis[0]], [-axis[1], axis[0], 0]])
+    return np.eye(3) + np.sin(ang) * K + (1 - np.cos(ang)) * K @ K
+
+
+def random_homography(rng, w=W, h=H):
+    th = np.deg2rad(rng.uniform(-15, 15))
+    s = rng.uniform(0.8, 1.2)
+    t = rng.uniform(-50, 50, 2)
+    p = rng.uniform(-1e-4, 1e-4, 2)
+    c = np.array([w / 2, h / 2])
+    A = np.eye(3)
+    A[:2, :2] = s * np.array([[np.cos(th), -np.sin(th)], [np.sin(th), np.cos(th)]])
+    A[:2, 2] = t
+    A[2, :2] = p
+    Tc = np.array([[1, 0, c[0]], [0, 1, c[1]], [0, 0, 1.0]])
+    Tm = np.array([[1, 0, -c[0]], [0, 1, -c[1]], [0, 0, 1.0]])
+    Hm = Tc @ A @ Tm
+    return Hm / Hm[2, 2]
+
+
+def project_h(Hm, x):
+    xh = np.c_[x, np.ones(len(x))] @ Hm.T
+    return xh[:, :2] / xh[:, 2:3]
+
+
+def homography_pair(seed, n=2000, inlier_ratio=0.4, sigma=1.0, w=W, h=H):
+    """Returns dict(corr [n,4] f64, H_gt, inlier_gt bool[n], size (h1,w1,h2,w2))."""
+    rng = _rng(seed)
+    Hm = random_homography(rng, w, h)
+    ni = int(round(n * inlier_ratio))
+    pts1 = np.zeros((0, 2))
+    pts2 = np.zeros((0, 2))
+    while len(pts1) < ni:
+        x1 = rng.uniform([0, 0], [w, h], size=(2 * ni, 2))
+        x2 = project_h(Hm, x1) + rng.normal(0, sigma, size=(2 * ni, 2))
+        ok = (x2[:, 0] >= 0) & (x2[:, 0] < w) & (x2[:, 1] >= 0) & (x2[:, 1] < h)
+        pts1 = np.r_[pts1, x1[ok]]
+        pts2 = np.r_[pts2, x2[ok]]
+    inl = np.c_[pts1[:ni], pts2[:ni]]
+    no = n - ni
+    out = np.c_[rng.uniform([0, 0], [w, h], size=(no, 2)), rng.uniform([0, 0], [w, h], size=(no, 2))]
+    corr = np.r_[inl, out]
+    gt = np.r_[np.ones(ni, bool), np.zeros(no, bool)]
+    perm = rng.permutation(n)
+    return dict(corr=corr[perm], H_gt=Hm, inlier_gt=gt[perm], size=(h, w, h, w))
+
+
+def intrinsics(f=800.0, w=W, h=H):
+    return np.array([[f, 0, w / 2], [0, f, h / 2], [0, 0, 1.0]])
+
+
+def skew(t):
+    return np.array([[0, -t[2], t[1]], [t[2], 0, -t[0]], [-t[1], t[0], 0]])
+
+
+def two_view_pair(seed, n=5000, inlier_ratio=0.25, sigma=0.5, f=800.0, w=W, h=H, max_angle_deg=30.0):
+    """Returns dict(corr [n,4] pixels, K, R, t, F_gt, E_gt, inlier_gt, size)."""
+    rng = _rng(seed)
+    K = intrinsics(f, w, h)
+    Ki = np.linalg.inv(K)
+    ni = int(round(n * inlier_ratio))
+    for _attempt in range(100):
+        R = _rot(rng.normal(size=3), np.deg2rad(rng.uniform(-max_angle_deg, max_angle_deg)))
+        t = rng.normal(size=3)
+        t /= np.linalg.norm(t)
+        pts1 = np.zeros((0, 2))
+        pts2 = np.zeros((0, 2))
+        tries = 0
+        while len(pts1) < ni and tries < 200:
+            tries += 1
+            m = 4 * ni
+            uv = rng.uniform([0, 0], [w, h], size=(m, 2))
+            depth = rng.uniform(2, 10, size=m)
+            X = (np.c_[uv, np.ones(m)] @ Ki.T) * depth[:, None]
+            X2 = X @ R.T + t
+            front = X2[:, 2] > 0.1
+            x2 = (X2 @ K.T)
+            x2 = x2[:, :2] / x2[:, 2:3]
+            x1n = uv + rng.normal(0, sigma, size=(m, 2))
+            x2n = x2 + rng.normal(0, sigma, size=(m, 2))
+            ok = front & (x2n[:, 0] >= 0) & (x2n[:, 0] < w) & (x2n[:, 1] >= 0) & (x2n[:, 1] < h) & \
+                (x1n[:, 0] >= 0) & (x1n[:, 0] < w) & (x1n[:, 1] >= 0) & (x1n[:, 1] < h)
+            pts1 = np.r_[pts1, x1n[ok]]
+            pts2 = np.r_[pts2, x2n[ok]]
+        if len(pts1) >= ni:
+            break
+    inl = np.c_[pts1[:ni], pts2[:ni]]
+    no = n - ni
+    out = np.c_[rng.uniform([0, 0], [w, h], size=(no, 2)), rng.uniform([0, 0], [w, h], size=(no, 2))]
+    corr = np.r_[inl, out]
+    gt = np.r_[np.ones(ni, bool), np.zeros(no, bool)]
+    perm = rng.permutation(n)
+    E = skew(t) @ R
+    F = Ki.T @ E @ Ki
+    return dict(corr=corr[perm], K=K, R=R, t=t, E_gt=E / np.linalg.norm(E), F_gt=F / np.linalg.norm(F),
+                inlier_gt=gt[perm], size=(h, w, h, w))
+
+
+# --- model error against ground truth -------------------------------------
+
+def homography_error(H_est, H_gt, w=W, h=H):
+    """RMS transfer error (px) of a 1000-point grid under H_est vs H_gt."""
+    if H_est is None:
+        return np.inf
+    gx, gy = np.meshgrid(np.linspace(0, w, 40), np.linspace(0, h, 25))
+    x = np.c_[gx.ravel(), gy.ravel()]
+    d = project_h(H_est, x) - project_h(H_gt, x)
+    return float(np.sqrt(np.mean(np.sum(d * d, axis=1))))
+
+
+def sampson_sq(F, corr):
+    x1 = np.c_[corr[:, :2], np.ones(len(corr))]
+    x2 = np.c_[corr[:, 2:4], np.ones(len(corr))]
+    Fx1 = x1 @ F.T
+    Ftx2 = x2 @ F
+    num = np.sum(x2 * Fx1, axis=1) ** 2
+    den = Fx1[:, 0] ** 2 + Fx1[:, 1] ** 2 + Ftx2[:, 0] ** 2 + Ftx2[:, 1] ** 2
+    return num / den
+
+
+def fundamental_error(F_est, pair, n=1000, seed=12345):
+    """Mean Sampson distance (px) of noise-free ground-truth correspondences."""
+    if F_est is None:
+        return np.inf
+    clean = two_view_pair_clean(pair, n, seed)
+    return float(np.mean(np.sqrt(sampson_sq(F_est, clean))))
+
+
+def two_view_pair_clean(pair, n, seed):
+    rng = _rng(seed)
+    K, R, t = pair["K"], pair["R"], pair["t"]
+    Ki = np.linalg.inv(K)
+    h, w = pair["size"][0], pair["size"][1]
+    out = np.zeros((0, 4))
+    while len(out) < n:
+        m = 4 * n
+        uv = rng.uniform([0, 0], [w, h], size=(m, 2))
+        depth = rng.uniform(2, 10, size=m)
+        X = (np.c_[uv, np.ones(m)] @ Ki.T) * depth[:, None]
+        X2 = X @ R.T + t
+        x2 = X2 @ K.T
+        x2 = x2[:, :2] / x2[:, 2:3]
+        ok = (X2[:, 2] > 0.1) & (x2[:, 0] >= 0) & (x2[:, 0] < w) & (x2[:, 1] >= 0) & (x2[:, 1] < h)
+        out = np.r_[out, np.c_[uv[ok], x2[ok]]]
+    return out[:n]
+
+
+def essential_error(E_est, pair):
+    """max(rotation error, translation-direction error) in degrees over the
+    four decompositions of E_est (best one), like a cheirality-free pose check."""
+    if E_est is None:
+        return np.inf
+    U, _, Vt = np.linalg.svd(E_est)
+    if np.linalg.det(U) < 0:
+        U = -U
+    if np.linalg.det(Vt) < 0:
+        Vt = -Vt
+    Wm = np.array([[0, -1, 0], [1, 0, 0], [0, 0, 1.0]])
+    best = np.inf
+    for Rc in (U @ Wm @ Vt, U @ Wm.T @ Vt):
+        for tc in (U[:, 2], -U[:, 2]):
+            cr = np.clip((np.trace(Rc.T @ pair["R"]) - 1) / 2, -1, 1)
+            er = np.degrees(np.arccos(cr))
+            ct = np.clip(np.dot(tc, pair["t"]) / np.linalg.norm(tc) / np.linalg.norm(pair["t"]), -1, 1)
+            et = np.degrees(np.arccos(ct))
+            best = min(best, max(er, et))
+    return float(best)

@@ -1,0 +1,165 @@
+/*
+ * gcr.h — C-ABI of the GB300 Graph-Cut RANSAC engine (libgcr.so).
+ *
+ * This is the drop-in boundary for the hypothesize-and-verify path of
+ * danini/graph-cut-ransac. Every entry point takes plain pointers and sizes,
+ * never throws, and reports failures through gcr_status plus
+ * gcr_last_error_string(). The caller owns every buffer.
+ *
+ * Reference interfaces replaced (paths inside the reference project):
+ *   gcr_find_homography   <- findHomography_        src/pygcransac/src/gcransac_python.cpp:4221
+ *                            (python: findHomography src/pygcransac/src/bindings.cpp:859-983)
+ *   gcr_find_fundamental  <- findFundamentalMatrix_ src/pygcransac/src/gcransac_python.cpp:1600
+ *                            (python: findFundamentalMatrix src/pygcransac/src/bindings.cpp:279-401)
+ *   gcr_find_essential    <- findEssentialMatrix_   src/pygcransac/src/gcransac_python.cpp:2519
+ *                            (python: findEssentialMatrix src/pygcransac/src/bindings.cpp:710-857)
+ *   gcr_find_batch / gcr_batch_run_device
+ *                         <- a loop of the three calls above, one per image pair
+ *                            (the reference has no batched form)
+ *   gcr_params            <- gcransac::utils::Settings src/pygcransac/include/settings.h:44-87
+ *                            plus the driver arguments of the find*_ functions
+ *   gcr_stats             <- gcransac::utils::RANSACStatistics src/pygcransac/include/statistics.h:43-72
+ */
+#ifndef GCR_H_
+#define GCR_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gcr_status {
+  GCR_OK = 0,
+  GCR_INVALID_ARG = 1,     /* bad pointer, shape or parameter value */
+  GCR_TOO_FEW_POINTS = 2,  /* fewer correspondences than the minimal sample */
+  GCR_NO_MODEL = 3,        /* the run ended without a model of more than m inliers */
+  GCR_DEVICE_ERROR = 4,    /* a CUDA call failed */
+  GCR_TIMEOUT = 5,         /* a device loop reached its iteration cap */
+  GCR_CAPACITY = 6,        /* an input exceeds a documented size limit */
+  GCR_UNSUPPORTED = 7      /* option combination not provided by this build */
+} gcr_status;
+
+typedef enum gcr_model_kind {
+  GCR_HOMOGRAPHY = 0,
+  GCR_FUNDAMENTAL = 1,
+  GCR_ESSENTIAL = 2
+} gcr_model_kind;
+
+/* Sampler ids follow examples/gcransac_parameter_types.py:8-12 of the reference. */
+enum {
+  GCR_SAMPLER_UNIFORM = 0,
+  GCR_SAMPLER_PROSAC = 1,
+  GCR_SAMPLER_PNAPSAC = 2,
+  GCR_SAMPLER_IMPORTANCE = 3,
+  GCR_SAMPLER_AR = 4
+};
+
+enum { GCR_NEIGHBORHOOD_GRID = 0, GCR_NEIGHBORHOOD_FLANN = 1 };
+enum { GCR_SCORING_MSAC = 0, GCR_SCORING_MAGSAC = 1 };
+
+typedef struct gcr_image_size {
+  int32_t h1, w1, h2, w2;
+} gcr_image_size;
+
+typedef struct gcr_params {
+  double threshold;                /* inlier-outlier threshold in pixels */
+  double confidence;               /* RANSAC confidence, e.g. 0.99 */
+  double spatial_coherence_weight; /* lambda of the graph-cut energy */
+  double neighborhood_size;        /* grid divisions along every axis */
+  int64_t max_iterations;
+  int64_t min_iterations;
+  int32_t sampler;                 /* GCR_SAMPLER_* */
+  int32_t neighborhood;            /* GCR_NEIGHBORHOOD_GRID only */
+  int32_t lo_number;               /* inner-RANSAC trials per graph-cut */
+  int32_t scoring;                 /* GCR_SCORING_* */
+  int32_t use_sprt;                /* accepted; the engine verifies every model in full */
+  int32_t use_space_partitioning;  /* accepted; the engine scores every point */
+  uint64_t seed;                   /* seed of the counter-based sampler streams */
+} gcr_params;
+
+typedef struct gcr_stats {
+  int64_t iteration_number;
+  int64_t graph_cut_number;
+  int64_t local_optimization_number;
+  int64_t inlier_number;
+  double score;
+  int32_t status;                  /* gcr_status of this pair */
+  int32_t flags;                   /* GCR_FLAG_* */
+} gcr_stats;
+
+enum {
+  GCR_FLAG_LO_APPLIED = 1,         /* at least one graph-cut local optimisation ran */
+  GCR_FLAG_IRLS_APPLIED = 2,       /* the final iterated least-squares model was kept */
+  GCR_FLAG_DEGENSAC_SKIPPED = 4    /* an H-degenerate F sample took the plain path */
+};
+
+/* Fills *p with the defaults of the reference python entry point of `kind`
+ * (src/pygcransac/src/bindings.cpp:1003-1022, 1091-1112, 1158-1178). */
+void gcr_default_params(gcr_model_kind kind, gcr_params* p);
+
+/* Single image pair, host buffers.
+ *   corr           n x 4 row-major doubles (x1, y1, x2, y2)
+ *   probabilities  n doubles or NULL (read only by samplers 3 and 4)
+ *   model_out9     3x3 row-major model
+ *   mask_out       n bytes, 1 = inlier
+ *   stats_out      may be NULL
+ * Returns GCR_NO_MODEL (mask all zero) when no model was found, like the
+ * reference returning (None, mask). */
+gcr_status gcr_find_homography(const double* corr, int64_t n, const gcr_image_size* size,
+                               const double* probabilities, const gcr_params* params,
+                               double* model_out9, uint8_t* mask_out, gcr_stats* stats_out);
+
+gcr_status gcr_find_fundamental(const double* corr, int64_t n, const gcr_image_size* size,
+                                const double* probabilities, const gcr_params* params,
+                                double* model_out9, uint8_t* mask_out, gcr_stats* stats_out);
+
+/* K1, K2: 3x3 row-major intrinsics of the two cameras. */
+gcr_status gcr_find_essential(const double* corr, int64_t n, const double* K1, const double* K2,
+                              const gcr_image_size* size, const double* probabilities,
+                              const gcr_params* params, double* model_out9, uint8_t* mask_out,
+                              gcr_stats* stats_out);
+
+/* Many image pairs of one model kind in one device launch, host buffers.
+ *   corr        concatenated correspondences, offsets[num_pairs] rows in total
+ *   offsets     num_pairs + 1 row offsets (ragged pairs)
+ *   K           num_pairs * 18 doubles (K1 then K2 per pair) for GCR_ESSENTIAL, else NULL
+ *   sizes       num_pairs image sizes
+ *   params      one parameter set shared by all pairs
+ *   seeds       num_pairs seeds, or NULL for params->seed + pair index
+ *   models_out  num_pairs * 9, masks_out offsets[num_pairs] bytes, stats_out num_pairs
+ * Returns GCR_OK when the launch succeeded; per-pair outcomes are in stats_out[i].status. */
+gcr_status gcr_find_batch(gcr_model_kind kind, int64_t num_pairs, const double* corr,
+                          const int64_t* offsets, const double* K, const gcr_image_size* sizes,
+                          const gcr_params* params, const uint64_t* seeds, double* models_out,
+                          uint8_t* masks_out, gcr_stats* stats_out);
+
+/* Device-resident form of gcr_find_batch: the bulk arrays (correspondences,
+ * models, masks, statistics) are device pointers of the current CUDA device,
+ * the small per-pair metadata (offsets, intrinsics, image sizes, seeds) are
+ * host arrays. The work is queued on `stream` (a cudaStream_t, NULL for the
+ * legacy default stream) and the call returns without waiting. Scratch memory
+ * is owned by `ctx`, which grows it on demand; one context per host thread. */
+typedef struct gcr_context gcr_context;
+
+gcr_status gcr_context_create(gcr_context** ctx);
+gcr_status gcr_context_destroy(gcr_context* ctx);
+
+gcr_status gcr_batch_run_device(gcr_context* ctx, gcr_model_kind kind, int64_t num_pairs,
+                                const double* d_corr, const int64_t* h_offsets, const double* h_K,
+                                const gcr_image_size* h_sizes, const gcr_params* params,
+                                const uint64_t* h_seeds, double* d_models_out,
+                                uint8_t* d_masks_out, gcr_stats* d_stats_out, void* stream);
+
+/* Number of kernels the last gcr_batch_run_device / gcr_find_* call launched. */
+int64_t gcr_last_launch_count(void);
+
+/* Message of the last failing call on this host thread. */
+const char* gcr_last_error_string(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GCR_H_ */

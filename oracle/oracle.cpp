@@ -1,0 +1,266 @@
+// Oracle (test infrastructure only): C entry points of the CPU FP64
+// restatement of the reference's findHomography_ / findFundamentalMatrix_ /
+// findEssentialMatrix_ drivers (src/pygcransac/src/gcransac_python.cpp:4221,
+// 1600, 2519). The parameter and result structs are the engine's own public
+// POD types (include/gcr.h) so that tests can hand both the same inputs.
+#include <atomic>
+#include <chrono>
+#include <thread>
+
+#include "../include/gcr.h"
+#include "oracle_essential.hpp"
+#include "oracle_fundamental.hpp"
+#include "oracle_gcransac.hpp"
+#include "oracle_homography.hpp"
+
+namespace oracle {
+
+const MagsacTable& magsac_table() {
+  static MagsacTable t;
+  return t;
+}
+
+// Upper incomplete gamma Gamma(1.5, x) = sqrt(pi) erfc(sqrt x) + 2 sqrt(x) e^-x.
+MagsacTable::MagsacTable() {
+  g.resize(36001);
+  for (int i = 0; i <= 36000; ++i) {
+    const double x = i / 1000.0;
+    g[i] = std::sqrt(M_PI) * 0.5 * std::erfc(std::sqrt(x)) + std::sqrt(x) * std::exp(-x);
+  }
+}
+
+struct Common {
+  const gcr_params* p;
+  const gcr_image_size* sz;
+  uint64_t seed;
+};
+
+static void fill_settings(Settings& s, const gcr_params& p) {
+  s.threshold = p.threshold;
+  s.spatial_coherence_weight = p.spatial_coherence_weight;
+  s.confidence = p.confidence;
+  s.max_local_optimization_number = (size_t)p.lo_number;
+  s.max_iteration_number = (size_t)p.max_iterations;
+  s.min_iteration_number = (size_t)p.min_iterations;
+}
+
+static std::unique_ptr<Sampler> make_main_sampler(const gcr_params& p, const Mat& pts, size_t m,
+                                                  const gcr_image_size& sz, uint64_t seed) {
+  switch (p.sampler) {
+    case GCR_SAMPLER_UNIFORM: return std::make_unique<UniformSampler>(seed, STREAM_MAIN);
+    case GCR_SAMPLER_PROSAC: return std::make_unique<ProsacSampler>(seed, STREAM_MAIN, m, (size_t)pts.rows);
+    case GCR_SAMPLER_PNAPSAC: {
+      const double sizes[4] = {(double)sz.w1, (double)sz.h1, (double)sz.w2, (double)sz.h2};
+      return std::make_unique<ProgressiveNapsacSampler>(seed, pts, std::vector<size_t>{16, 8, 4, 2}, m, sizes, 0.5);
+    }
+    default: return nullptr;
+  }
+}
+
+// The grid of the drivers: (w + eps) / n cells along every axis
+// (gcransac_python.cpp:4290-4297).
+static std::unique_ptr<Grid> make_grid(const Mat& pixel_pts, const gcr_image_size& sz, double ns) {
+  const size_t n = (size_t)ns;
+  const double e = std::numeric_limits<double>::epsilon();
+  const double cs[4] = {(sz.w1 + e) / (double)n, (sz.h1 + e) / (double)n, (sz.w2 + e) / (double)n,
+                        (sz.h2 + e) / (double)n};
+  return std::make_unique<Grid>(pixel_pts, cs, n);
+}
+
+template <class Est, template <class> class Scoring>
+static int run_generic(const Mat& run_pts, const Mat& pixel_pts, const Est& est, const gcr_params& p,
+                       const gcr_image_size& sz, uint64_t seed, const Grid* grid, double threshold,
+                       Model& model, std::vector<size_t>& inliers, gcr_stats* st, double mag_threshold) {
+  auto main_s = make_main_sampler(p, pixel_pts, Est::sample_size(), sz, seed);
+  if (!main_s) return GCR_UNSUPPORTED;
+  UniformSampler lo_s(seed, STREAM_LO);
+  GCRansac<Est, Scoring<Est>> g;
+  fill_settings(g.settings, p);
+  g.settings.threshold = threshold;
+  if constexpr (std::is_same<Scoring<Est>, MAGSACScoring<Est>>::value) g.scoring.threshold = mag_threshold;
+  const bool ok = g.run(run_pts, est, main_s.get(), &lo_s, grid, model);
+  if (st) {
+    st->iteration_number = (int64_t)g.statistics.iteration_number;
+    st->graph_cut_number = (int64_t)g.statistics.graph_cut_number;
+    st->local_optimization_number = (int64_t)g.statistics.local_optimization_number;
+    st->score = g.statistics.score;
+    st->flags = (g.statistics.local_optimization_number ? GCR_FLAG_LO_APPLIED : 0) |
+                (g.statistics.irls_applied ? GCR_FLAG_IRLS_APPLIED : 0);
+  }
+  if (!ok) return GCR_NO_MODEL;
+  inliers = g.statistics.inliers;
+  return GCR_OK;
+}
+
+static int find_homography(const double* corr, int64_t n, const gcr_image_size& sz, const gcr_params& p,
+                           uint64_t seed, double* model_out, uint8_t* mask, gcr_stats* st) {
+  if (n < 4) return GCR_TOO_FEW_POINTS;
+  const Mat pts{corr, n, 4};
+  auto grid = make_grid(pts, sz, p.neighborhood_size);
+  HomographyEstimator est;
+  Model model{};
+  std::vector<size_t> inl;
+  int rc;
+  if (p.scoring == GCR_SCORING_MAGSAC)
+    rc = run_generic<HomographyEstimator, MAGSACScoring>(pts, pts, est, p, sz, seed, grid.get(), p.threshold,
+                                                         model, inl, st, p.threshold);
+  else
+    rc = run_generic<HomographyEstimator, MSACScoring>(pts, pts, est, p, sz, seed, grid.get(), p.threshold,
+                                                       model, inl, st, p.threshold);
+  std::memset(mask, 0, (size_t)n);
+  for (size_t i : inl) mask[i] = 1;
+  if (st) st->inlier_number = (int64_t)inl.size();
+  if (rc == GCR_OK) std::memcpy(model_out, model.data(), 9 * sizeof(double));
+  else std::memset(model_out, 0, 9 * sizeof(double));
+  return rc;
+}
+
+}  // namespace oracle
+
+using namespace oracle;
+
+extern "C" {
+
+int oracle_find(int kind, const double* corr, int64_t n, const double* K1, const double* K2,
+                const gcr_image_size* sz, const gcr_params* p, uint64_t seed, double* model_out,
+                uint8_t* mask_out, gcr_stats* st) {
+  gcr_stats local{};
+  gcr_stats* s = st ? st : &local;
+  std::memset(s, 0, sizeof(*s));
+  int rc;
+  switch (kind) {
+    case GCR_HOMOGRAPHY: rc = find_homography(corr, n, *sz, *p, seed, model_out, mask_out, s); break;
+    case GCR_FUNDAMENTAL: rc = find_fundamental(corr, n, *sz, *p, seed, model_out, mask_out, s); break;
+    case GCR_ESSENTIAL: rc = find_essential(corr, n, K1, K2, *sz, *p, seed, model_out, mask_out, s); break;
+    default: rc = GCR_INVALID_ARG;
+  }
+  s->status = rc;
+  return rc;
+}
+
+// Pair-parallel batch over `threads` host threads (one pair per thread at a
+// time, each pair single-threaded like the reference). Returns wall seconds.
+double oracle_find_batch(int kind, int64_t num_pairs, const double* corr, const int64_t* offsets, const double* K,
+                         const gcr_image_size* sizes, const gcr_params* p, const uint64_t* seeds,
+                         double* models_out, uint8_t* masks_out, gcr_stats* stats_out, int threads) {
+  std::atomic<int64_t> next{0};
+  auto worker = [&]() {
+    for (;;) {
+      const int64_t i = next.fetch_add(1);
+      if (i >= num_pairs) return;
+      const int64_t o = offsets[i], n = offsets[i + 1] - offsets[i];
+      const uint64_t seed = seeds ? seeds[i] : p->seed + (uint64_t)i;
+      oracle_find(kind, corr + o * 4, n, K ? K + 18 * i : nullptr, K ? K + 18 * i + 9 : nullptr, &sizes[i], p,
+                  seed, models_out + 9 * i, masks_out + o, stats_out ? stats_out + i : nullptr);
+    }
+  };
+  const auto t0 = std::chrono::steady_clock::now();
+  if (threads <= 1) worker();
+  else {
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; ++t) pool.emplace_back(worker);
+    for (auto& t : pool) t.join();
+  }
+  return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+// Test hooks.
+double oracle_magsac_gamma(int i) { return magsac_table().g[i]; }
+
+// Labelling of a given model: writes 1 for SINK (inlier) nodes.
+int oracle_labeling(int kind, const double* corr, int64_t n, const gcr_image_size* sz, const gcr_params* p,
+                    const double* model, uint8_t* labels) {
+  const Mat pts{corr, n, 4};
+  auto grid = make_grid(pts, *sz, p->neighborhood_size);
+  Model m;
+  std::memcpy(m.data(), model, sizeof(m));
+  std::vector<size_t> inl;
+  if (kind == GCR_HOMOGRAPHY) {
+    GCRansac<HomographyEstimator, MSACScoring<HomographyEstimator>> g;
+    g.graph = grid.get();
+    g.labeling(pts, m, HomographyEstimator(), p->spatial_coherence_weight, p->threshold, inl);
+  } else if (kind == GCR_FUNDAMENTAL) {
+    GCRansac<FundamentalEstimator, MSACScoring<FundamentalEstimator>> g;
+    g.graph = grid.get();
+    g.labeling(pts, m, FundamentalEstimator(), p->spatial_coherence_weight, p->threshold, inl);
+  } else
+    return GCR_UNSUPPORTED;
+  std::memset(labels, 0, (size_t)n);
+  for (size_t i : inl) labels[i] = 1;
+  return 0;
+}
+
+// Scores a given model with MSAC: returns the value, writes the inlier count.
+double oracle_msac_score(int kind, const double* corr, int64_t n, const double* model, double threshold,
+                         int64_t* count) {
+  const Mat pts{corr, n, 4};
+  Model m;
+  std::memcpy(m.data(), model, sizeof(m));
+  Score s;
+  const double sq = 2.25 * threshold * threshold;
+  if (kind == GCR_HOMOGRAPHY) {
+    MSACScoring<HomographyEstimator> sc;
+    sc.initialize(sq, n);
+    s = sc.get(pts, m, HomographyEstimator(), nullptr);
+  } else {
+    MSACScoring<FundamentalEstimator> sc;
+    sc.initialize(sq, n);
+    s = sc.get(pts, m, FundamentalEstimator(), nullptr);
+  }
+  *count = (int64_t)s.inlier_number;
+  return s.value;
+}
+
+// Minimal-sample solve for tests: writes up to 10 models, returns their count (-1 invalid sample).
+int oracle_minimal(int kind, const double* corr, int64_t n, const int64_t* sample, double* models_out) {
+  const Mat pts{corr, n, 4};
+  std::vector<size_t> s;
+  std::vector<Model> models;
+  if (kind == GCR_HOMOGRAPHY) {
+    HomographyEstimator e;
+    s.assign(sample, sample + 4);
+    if (!e.is_valid_sample(pts, s.data())) return -1;
+    e.estimate_minimal(pts, s.data(), models);
+  } else if (kind == GCR_FUNDAMENTAL) {
+    FundamentalEstimator e;
+    s.assign(sample, sample + 7);
+    if (!e.is_valid_sample(pts, s.data())) return -1;
+    e.estimate_minimal(pts, s.data(), models);
+  } else {
+    EssentialEstimator e;
+    s.assign(sample, sample + 5);
+    if (!e.is_valid_sample(pts, s.data())) return -1;
+    e.estimate_minimal(pts, s.data(), models);
+  }
+  for (size_t i = 0; i < models.size() && i < 10; ++i) std::memcpy(models_out + 9 * i, models[i].data(), 72);
+  return (int)models.size();
+}
+
+// Draw sequence of the main sampler for tests of the device sampler.
+int oracle_sample_sequence(int sampler, int64_t n, int m, uint64_t seed, int64_t calls, const double* corr,
+                           const gcr_image_size* sz, int64_t* out, uint8_t* ok) {
+  gcr_params p{};
+  p.sampler = sampler;
+  const Mat pts{corr, n, 4};
+  auto s = make_main_sampler(p, pts, (size_t)m, *sz, seed);
+  if (!s) return -1;
+  std::vector<size_t> pool(n), sample(m);
+  for (int64_t i = 0; i < n; ++i) pool[i] = (size_t)i;
+  for (int64_t c = 0; c < calls; ++c) {
+    ok[c] = s->sample(pool, sample.data(), (size_t)m);
+    for (int j = 0; j < m; ++j) out[c * m + j] = (int64_t)sample[j];
+  }
+  return 0;
+}
+
+void oracle_philox(const uint32_t* ctr, const uint32_t* key, uint32_t* out) {
+  uint32_t c[4] = {ctr[0], ctr[1], ctr[2], ctr[3]};
+  philox4x32_10(c, key[0], key[1]);
+  for (int i = 0; i < 4; ++i) out[i] = c[i];
+}
+
+uint32_t oracle_draw_u32(uint64_t seed, uint32_t stream, uint64_t call, uint32_t draw) {
+  return draw_u32(seed, stream, call, draw);
+}
+
+}  // extern "C"

@@ -1,0 +1,151 @@
+"""Python handle on the oracle (test infrastructure only).
+
+The oracle is a CPU FP64 restatement of the reference's Graph-Cut RANSAC path;
+tests, smoke() and the CPU-baseline leg of bench.py use it as the checker.
+Parity anchors: the reference ships no golden vectors for this path (its
+tests assert inlier-count floors on SIFT matches that need OpenCV), so the
+oracle is pinned by known-answer tests on exact synthetic data, by the MAGSAC++
+gamma table read from the reference as text, and by self-consistency checks.
+"""
+import ctypes
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+sys.path.insert(0, os.path.join(os.path.dirname(HERE), "graph-cut-ransac_gb300"))
+from pygcransac import _abi  # noqa: E402  (POD types shared with the engine)
+
+_lib = None
+
+
+def build():
+    subprocess.check_call(["sh", os.path.join(HERE, "build.sh")])
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        lib = ctypes.CDLL(LIB)
+        P = ctypes.c_void_p
+        lib.oracle_find.restype = ctypes.c_int
+        lib.oracle_find.argtypes = [ctypes.c_int, P, ctypes.c_int64, P, P, P, P, ctypes.c_uint64, P, P, P]
+        lib.oracle_find_batch.restype = ctypes.c_double
+        lib.oracle_find_batch.argtypes = [ctypes.c_int, ctypes.c_int64, P, P, P, P, P, P, P, P, P, ctypes.c_int]
+        lib.oracle_magsac_gamma.restype = ctypes.c_double
+        lib.oracle_magsac_gamma.argtypes = [ctypes.c_int]
+        lib.oracle_labeling.restype = ctypes.c_int
+        lib.oracle_labeling.argtypes = [ctypes.c_int, P, ctypes.c_int64, P, P, P, P]
+        lib.oracle_msac_score.restype = ctypes.c_double
+        lib.oracle_msac_score.argtypes = [ctypes.c_int, P, ctypes.c_int64, P, ctypes.c_double, P]
+        lib.oracle_minimal.restype = ctypes.c_int
+        lib.oracle_minimal.argtypes = [ctypes.c_int, P, ctypes.c_int64, P, P]
+        lib.oracle_sample_sequence.restype = ctypes.c_int
+        lib.oracle_sample_sequence.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.c_int, ctypes.c_uint64,
+                                               ctypes.c_int64, P, P, P, P]
+        lib.oracle_philox.restype = None
+        lib.oracle_philox.argtypes = [P, P, P]
+        lib.oracle_draw_u32.restype = ctypes.c_uint32
+        lib.oracle_draw_u32.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32]
+        _lib = lib
+    return _lib
+
+
+def _p(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+def make_size(h1, w1, h2, w2):
+    return _abi.ImageSize(int(h1), int(w1), int(h2), int(w2))
+
+
+def find(kind, corr, size, params, seed=None, K1=None, K2=None):
+    """Runs the oracle on one pair. Returns (status, model 3x3, mask bool[N], stats)."""
+    lib = load()
+    corr = np.ascontiguousarray(corr, dtype=np.float64)
+    n = corr.shape[0]
+    model = np.zeros(9)
+    mask = np.zeros(n, np.uint8)
+    st = _abi.Stats()
+    K1 = None if K1 is None else np.ascontiguousarray(K1, np.float64)
+    K2 = None if K2 is None else np.ascontiguousarray(K2, np.float64)
+    seed = params.seed if seed is None else seed
+    rc = lib.oracle_find(kind, _p(corr), n, _p(K1), _p(K2), ctypes.byref(size), ctypes.byref(params),
+                         seed, _p(model), _p(mask), ctypes.byref(st))
+    return rc, model.reshape(3, 3), mask.astype(bool), st
+
+
+def find_batch(kind, corr, offsets, sizes, params, seeds=None, K=None, threads=1):
+    """Pair-parallel oracle batch. Returns (models [P,9], masks, stats, wall seconds)."""
+    lib = load()
+    corr = np.ascontiguousarray(corr, np.float64)
+    offsets = np.ascontiguousarray(offsets, np.int64)
+    P = len(offsets) - 1
+    models = np.zeros((P, 9))
+    masks = np.zeros(int(offsets[-1]), np.uint8)
+    stats = np.zeros(P, _abi.STATS_DTYPE)
+    sizes = np.ascontiguousarray(sizes, _abi.SIZE_DTYPE)
+    seeds = None if seeds is None else np.ascontiguousarray(seeds, np.uint64)
+    K = None if K is None else np.ascontiguousarray(K, np.float64)
+    t = lib.oracle_find_batch(kind, P, _p(corr), _p(offsets), _p(K), _p(sizes), ctypes.byref(params),
+                              _p(seeds), _p(models), _p(masks), _p(stats), threads)
+    return models, masks.astype(bool), stats, t
+
+
+def magsac_gamma(i):
+    return load().oracle_magsac_gamma(i)
+
+
+def labeling(kind, corr, size, params, model):
+    lib = load()
+    corr = np.ascontiguousarray(corr, np.float64)
+    model = np.ascontiguousarray(model, np.float64).reshape(9)
+    out = np.zeros(corr.shape[0], np.uint8)
+    lib.oracle_labeling(kind, _p(corr), corr.shape[0], ctypes.byref(size), ctypes.byref(params), _p(model),
+                        _p(out))
+    return out.astype(bool)
+
+
+def msac_score(kind, corr, model, threshold):
+    lib = load()
+    corr = np.ascontiguousarray(corr, np.float64)
+    model = np.ascontiguousarray(model, np.float64).reshape(9)
+    cnt = np.zeros(1, np.int64)
+    v = lib.oracle_msac_score(kind, _p(corr), corr.shape[0], _p(model), threshold, _p(cnt))
+    return v, int(cnt[0])
+
+
+def minimal(kind, corr, sample):
+    lib = load()
+    corr = np.ascontiguousarray(corr, np.float64)
+    sample = np.ascontiguousarray(sample, np.int64)
+    out = np.zeros((10, 9))
+    k = lib.oracle_minimal(kind, _p(corr), corr.shape[0], _p(sample), _p(out))
+    return k, out[:max(k, 0)].reshape(-1, 3, 3)
+
+
+def sample_sequence(sampler, corr, m, seed, calls, size):
+    lib = load()
+    corr = np.ascontiguousarray(corr, np.float64)
+    out = np.zeros((calls, m), np.int64)
+    ok = np.zeros(calls, np.uint8)
+    lib.oracle_sample_sequence(sampler, corr.shape[0], m, seed, calls, _p(corr), ctypes.byref(size), _p(out),
+                               _p(ok))
+    return out, ok.astype(bool)
+
+
+def philox(ctr, key):
+    c = np.ascontiguousarray(ctr, np.uint32)
+    k = np.ascontiguousarray(key, np.uint32)
+    out = np.zeros(4, np.uint32)
+    load().oracle_philox(_p(c), _p(k), _p(out))
+    return [int(v) for v in out]
+
+
+def draw_u32(seed, stream, call, draw):
+    return load().oracle_draw_u32(seed, stream, call, draw)

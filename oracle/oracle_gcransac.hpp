@@ -1,0 +1,400 @@
+// Oracle (test infrastructure only): graph-cut labelling, MSAC / MAGSAC++
+// scoring and the GC-RANSAC loop, restated from
+// src/pygcransac/include/GCRANSAC.h and scoring_function.h of the reference.
+#pragma once
+
+#include "oracle_common.hpp"
+
+namespace oracle {
+
+// ---------------------------------------------------------------------------
+// s-t min cut for the labelling step. The reference builds an
+// Energy<double,double,double> (src/pygcransac/include/energy.h:203-253) and
+// runs Boykov-Kolmogorov max-flow (maxflow.cpp:471-607); a node is an inlier
+// iff what_segment() is SINK (GCRANSAC.h:1014-1017), i.e. iff the node can
+// still reach the sink in the residual graph of a maximum flow. That set is the
+// same for every maximum flow, so this oracle uses Dinic's algorithm followed
+// by a reverse residual search from the sink. Residuals at or below kResidualEps
+// count as saturated (the engine uses the same rule).
+constexpr double kResidualEps = 1e-12;
+
+struct FlowGraph {
+  struct Arc { int to; int rev; double cap; };
+  int n, S, T;
+  std::vector<std::vector<Arc>> adj;
+  explicit FlowGraph(int n_) : n(n_), S(n_), T(n_ + 1), adj(n_ + 2) {}
+  void add_arc_pair(int u, int v, double c_uv, double c_vu) {
+    adj[u].push_back({v, (int)adj[v].size(), c_uv});
+    adj[v].push_back({u, (int)adj[u].size() - 1, c_vu});
+  }
+  std::vector<int> level, it;
+  bool bfs() {
+    level.assign(n + 2, -1);
+    std::vector<int> q;
+    q.reserve(n + 2);
+    q.push_back(S);
+    level[S] = 0;
+    for (size_t h = 0; h < q.size(); ++h) {
+      const int u = q[h];
+      for (const Arc& a : adj[u])
+        if (a.cap > 0 && level[a.to] < 0) { level[a.to] = level[u] + 1; q.push_back(a.to); }
+    }
+    return level[T] >= 0;
+  }
+  double dfs(int u, double f) {
+    if (u == T) return f;
+    for (int& i = it[u]; i < (int)adj[u].size(); ++i) {
+      Arc& a = adj[u][i];
+      if (a.cap > 0 && level[a.to] == level[u] + 1) {
+        const double d = dfs(a.to, std::min(f, a.cap));
+        if (d > 0) {
+          a.cap -= d;
+          adj[a.to][a.rev].cap += d;
+          return d;
+        }
+      }
+    }
+    return 0;
+  }
+  void maxflow() {
+    for (int rounds = 0; rounds < 1000000 && bfs(); ++rounds) {
+      it.assign(n + 2, 0);
+      while (dfs(S, std::numeric_limits<double>::infinity()) > 0) {}
+    }
+  }
+  // Nodes that reach T through arcs of residual capacity > kResidualEps.
+  std::vector<char> sink_side() {
+    std::vector<char> mark(n + 2, 0);
+    std::vector<int> q{T};
+    mark[T] = 1;
+    for (size_t h = 0; h < q.size(); ++h) {
+      const int v = q[h];
+      for (const Arc& a : adj[v]) {
+        // a: v -> u; residual of u -> v is the sister arc
+        const int u = a.to;
+        if (mark[u]) continue;
+        if (adj[u][a.rev].cap > kResidualEps) { mark[u] = 1; q.push_back(u); }
+      }
+    }
+    return mark;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// MSACScoringFunction::getScore (scoring_function.h:137-233). The early-exit
+// test at :182 compares (N - i) + sum r^2 against -best and cannot fire for a
+// non-negative best score, so it is omitted.
+template <class Est>
+struct MSACScoring {
+  double sq_trunc = 0;
+  void initialize(double sq, size_t) { sq_trunc = sq; }
+  Score get(const Mat& pts, const Model& m, const Est& est, std::vector<size_t>* inliers) const {
+    Score s;
+    if (inliers) inliers->clear();
+    for (int64_t i = 0; i < pts.rows; ++i) {
+      const double r2 = est.squared_residual(pts.row(i), m);
+      if (r2 < sq_trunc) {
+        if (inliers) inliers->push_back((size_t)i);
+        ++s.inlier_number;
+        s.value -= r2;
+      }
+    }
+    if (s.inlier_number == 0) return Score();
+    s.value = (s.value + (double)s.inlier_number * sq_trunc) / sq_trunc;
+    return s;
+  }
+};
+
+// MAGSACScoringFunction::getScore (scoring_function.h:237-348). The weight
+// table stored_gamma_values[x] (gamma_values.cpp:2012) holds the upper
+// incomplete gamma function Gamma(1.5, x / 1000) for x = 0..36000; it is
+// regenerated here from that definition (checked against the reference table
+// text by the tests).
+struct MagsacTable {
+  std::vector<double> g;
+  MagsacTable();
+};
+const MagsacTable& magsac_table();
+
+template <class Est>
+struct MAGSACScoring {
+  double threshold = 0;  // settings.threshold (not the 1.5x truncated one)
+  void initialize(double, size_t) {}
+  Score get(const Mat& pts, const Model& m, const Est& est, std::vector<size_t>* inliers) const {
+    constexpr double k = 3.64;
+    constexpr double C = 0.25;
+    constexpr double gamma_k = 0.0036572608340910764;
+    const double two_ad_dof = std::pow(2.0, 1.5);
+    const double C_times_two_ad_dof = C * two_ad_dof;
+    const double gamma_value = std::tgamma(1.5);
+    const double gamma_difference = gamma_value - gamma_k;
+    const double squared_sigma_max_2 = threshold * threshold * 2.0;
+    const double one_over_sigma = C_times_two_ad_dof / threshold;
+    const double weight_zero = one_over_sigma * gamma_difference;
+    (void)k;
+    const std::vector<double>& table = magsac_table().g;
+    Score s;
+    if (inliers) inliers->clear();
+    for (int64_t i = 0; i < pts.rows; ++i) {
+      const double r = std::sqrt(est.squared_residual(pts.row(i), m));
+      if (r > threshold) continue;
+      double w;
+      if (r < std::numeric_limits<double>::epsilon()) w = weight_zero;
+      else {
+        size_t x = (size_t)std::round(1e4 * (r * r) / squared_sigma_max_2);
+        if (36000 < x) x = 36000;
+        w = one_over_sigma * (table[x] - gamma_k);
+      }
+      s.value += w / weight_zero;
+      if (r > threshold) continue;
+      ++s.inlier_number;
+      if (inliers) inliers->push_back((size_t)i);
+    }
+    return s;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// GCRANSAC<Estimator, GridNeighborhoodGraph<4>, Scoring>::run, restated from
+// GCRANSAC.h:200-627 together with graphCutLocalOptimization (779-910),
+// labeling (912-1021) and iteratedLeastSquaresFitting (629-758).
+template <class Est, class Scoring>
+struct GCRansac {
+  Settings settings;
+  Statistics statistics;
+  Scoring scoring;
+  double truncated_threshold = 0, squared_truncated_threshold = 0, log_probability = 0;
+  const Grid* graph = nullptr;
+  Sampler* main_sampler = nullptr;
+  Sampler* lo_sampler = nullptr;
+
+  // labeling (GCRANSAC.h:912-1021)
+  void labeling(const Mat& pts, const Model& model, const Est& est, double lambda, double thr,
+                std::vector<size_t>& inliers) {
+    const int64_t N = pts.rows;
+    const double sq = thr * thr * 9 / 4;
+    const double oml = 1.0 - lambda;
+    std::vector<double> d(N), tr(N, 0.0);
+    for (int64_t i = 0; i < N; ++i) {
+      const double r2 = est.squared_residual(pts.row(i), model);
+      d[i] = std::min(std::max(r2 / sq, 0.0), 1.0);
+      const double e = 1 - d[i];
+      // add_term1(i, E0, E1) = add_tweights(i, E1, E0): tr_cap = E1 - E0
+      if (r2 <= sq) tr[i] = 0 - oml * e;
+      else tr[i] = oml * (1 - e) - 0;
+    }
+    FlowGraph g((int)N);
+    if (lambda > 0 && graph) {
+      // Each unordered pair of a cell once, smaller index first
+      // (the used_edges de-duplication of GCRANSAC.h:963-989).
+      for (int64_t i = 0; i < N; ++i) {
+        for (size_t j : graph->neighbors((size_t)i)) {
+          if ((int64_t)j <= i) continue;
+          const double e00 = 0.5 * (d[i] + d[j]);
+          // add_term2(i, j, e00*l, l, l, 0): tweights(i, 0, e00*l), edge(i, j, l - e00*l, l)
+          const double A = e00 * lambda;
+          tr[i] = tr[i] - A;
+          g.add_arc_pair((int)i, (int)j, lambda - A, lambda);
+        }
+      }
+    }
+    for (int64_t i = 0; i < N; ++i) {
+      if (tr[i] > 0) g.add_arc_pair(g.S, (int)i, tr[i], 0.0);
+      else if (tr[i] < 0) g.add_arc_pair((int)i, g.T, -tr[i], 0.0);
+    }
+    g.maxflow();
+    const std::vector<char> sink = g.sink_side();
+    inliers.clear();
+    for (int64_t i = 0; i < N; ++i)
+      if (sink[i]) inliers.push_back((size_t)i);
+  }
+
+  bool gc_local_optimization(const Mat& pts, std::vector<size_t>& best_inliers_io, Model& best_model_io,
+                             Score& best_score_io, const Est& est, size_t trials) {
+    const size_t inlier_limit = est.inlier_limit();
+    Score max_score = best_score_io;
+    Model best_model = best_model_io;
+    std::vector<Model> models;
+    std::vector<size_t> best_inliers, inliers, tmp;
+    ++statistics.local_optimization_number;
+    std::vector<size_t> sample(inlier_limit);
+    while (++statistics.graph_cut_number < settings.max_graph_cut_number) {
+      bool updated = false;
+      inliers.clear();
+      labeling(pts, best_model, est, settings.spatial_coherence_weight, settings.threshold, inliers);
+      const size_t ss = std::min(inlier_limit, inliers.size());
+      for (size_t trial = 0; trial < trials; ++trial) {
+        models.clear();
+        if (ss < inliers.size()) {
+          lo_sampler->sample(inliers, sample.data(), ss);
+          if (!est.estimate_nonminimal(pts, sample.data(), ss, models, nullptr)) continue;
+        } else if (Est::sample_size() < inliers.size()) {
+          if (!est.estimate_nonminimal(pts, inliers.data(), inliers.size(), models, nullptr)) break;
+        } else
+          break;
+        for (Model& m : models) {
+          tmp.clear();
+          const Score s = scoring.get(pts, m, est, &tmp);
+          if (max_score < s) {
+            updated = true;
+            max_score = s;
+            best_model = m;
+            best_inliers.swap(tmp);
+            tmp.clear();
+          }
+        }
+      }
+      if (!updated) break;
+    }
+    if (best_score_io < max_score) {
+      best_score_io = max_score;
+      best_model_io = best_model;
+      best_inliers_io.swap(best_inliers);
+      return true;
+    }
+    return false;
+  }
+
+  bool irls(const Mat& pts, const Est& est, std::vector<size_t>& inliers, Model& model) {
+    const size_t m = Est::sample_size();
+    if (inliers.size() <= m) return false;
+    size_t iterations = 0;
+    std::vector<size_t> tmp;
+    std::vector<double> weights(pts.rows, 0.0);
+    Score best_score;
+    while (++iterations < settings.max_least_squares_iterations) {
+      std::vector<Model> models;
+      for (size_t k = 0; k < inliers.size(); ++k) {
+        const size_t p = inliers[k];
+        const double r2 = est.squared_residual(pts.row(p), model);
+        const double w = std::max(0.0, 1.0 - r2 / squared_truncated_threshold);
+        weights[p] = w * w;
+      }
+      est.estimate_nonminimal(pts, inliers.data(), inliers.size(), models, weights.data());
+      for (size_t p : inliers) weights[p] = 0;
+      if (models.empty()) break;
+      if (models.size() == 1) {
+        tmp.clear();
+        const Score s = scoring.get(pts, models[0], est, &tmp);
+        if (tmp.size() < m) break;
+        if (s.inlier_number <= inliers.size()) break;
+        model = models[0];
+        inliers.swap(tmp);
+      } else {
+        bool updated = false;
+        for (Model& mm : models) {
+          tmp.clear();
+          const Score s = scoring.get(pts, mm, est, &tmp);
+          if (tmp.size() < m) continue;
+          if (s.inlier_number <= inliers.size()) continue;
+          if (s.inlier_number >= best_score.inlier_number) {
+            updated = true;
+            best_score = s;
+            model = mm;
+            inliers.swap(tmp);
+          }
+        }
+        if (!updated) break;
+      }
+    }
+    return iterations > 1;
+  }
+
+  // Returns true when a model was found.
+  bool run(const Mat& pts, const Est& est, Sampler* main_s, Sampler* lo_s, const Grid* g, Model& out) {
+    statistics = Statistics();
+    main_sampler = main_s;
+    lo_sampler = lo_s;
+    graph = g;
+    statistics.neighbor_number = g ? g->neighbor_number : 0;
+    const size_t m = Est::sample_size();
+    log_probability = std::log(1.0 - settings.confidence);
+    size_t max_iteration = iteration_number_for(1, pts.rows, m, log_probability);
+    std::vector<size_t> sample(m);
+    const size_t N = (size_t)pts.rows;
+    size_t off = 0;
+    Model best_model{};
+    Score current_score, best_score;
+    std::vector<std::vector<size_t>> cont(2);
+    truncated_threshold = 1.5 * settings.threshold;
+    squared_truncated_threshold = truncated_threshold * truncated_threshold;
+    scoring.initialize(squared_truncated_threshold, N);
+    std::vector<size_t> pool(N);
+    for (size_t i = 0; i < N; ++i) pool[i] = i;
+    std::vector<Model> models;
+    while (settings.min_iteration_number > statistics.iteration_number ||
+           statistics.iteration_number < std::min(max_iteration, settings.max_iteration_number)) {
+      bool do_lo = false;
+      ++statistics.iteration_number;
+      models.clear();
+      int unsuccessful = -1;
+      while (++unsuccessful < (int)settings.max_unsuccessful_model_generations) {
+        if (!main_sampler->sample(pool, sample.data(), m)) continue;
+        if (!est.is_valid_sample(pts, sample.data())) continue;
+        if (est.estimate_minimal(pts, sample.data(), models)) break;
+      }
+      statistics.iteration_number += unsuccessful;
+      for (Model& model : models) {
+        current_score = scoring.get(pts, model, est, &cont[off]);
+        bool updated_model = false;
+        if (best_score < current_score &&
+            est.is_valid_model(model, pts, cont[off], sample.data(), truncated_threshold, updated_model)) {
+          if (updated_model) current_score = scoring.get(pts, model, est, &cont[off]);
+          off = (off + 1) % 2;
+          best_model = model;
+          best_score = current_score;
+          do_lo = statistics.iteration_number > settings.min_iteration_number_before_lo &&
+                  best_score.inlier_number > m;
+          max_iteration = iteration_number_for(best_score.inlier_number, N, m, log_probability);
+        }
+      }
+      if (settings.do_local_optimization && do_lo) {
+        ++statistics.local_optimization_number;
+        gc_local_optimization(pts, cont[off], best_model, best_score, est, settings.max_local_optimization_number);
+        max_iteration = iteration_number_for(best_score.inlier_number, N, m, log_probability);
+      }
+    }
+    if (best_score.inlier_number <= m) return false;
+    if (settings.do_local_optimization && statistics.local_optimization_number == 0) {
+      ++statistics.local_optimization_number;
+      gc_local_optimization(pts, cont[off], best_model, best_score, est, settings.max_local_optimization_number);
+    }
+    if (cont[off].size() != best_score.inlier_number) off = (off + 1) % 2;
+    if (cont[off].size() != best_score.inlier_number) best_score = scoring.get(pts, best_model, est, &cont[off]);
+    bool irls_applied = false;
+    if (settings.do_final_iterated_least_squares) {
+      Model model = best_model;
+      const bool ok = irls(pts, est, cont[off], model);
+      if (ok) {
+        const size_t idx = (off + 1) % 2;
+        cont[idx].clear();
+        current_score = scoring.get(pts, model, est, &cont[idx]);
+        if (best_score < current_score) {
+          irls_applied = true;
+          best_model = model;
+          off = idx;
+        }
+      }
+    }
+    if (!irls_applied) {
+      models.clear();
+      est.estimate_nonminimal(pts, cont[off].data(), best_score.inlier_number, models, nullptr);
+      for (Model& model : models) {
+        const size_t idx = (off + 1) % 2;
+        cont[idx].clear();
+        current_score = scoring.get(pts, model, est, &cont[idx]);
+        if (best_score < current_score) {
+          best_model = model;
+          off = idx;
+        }
+      }
+    }
+    statistics.irls_applied = irls_applied;
+    statistics.inliers.swap(cont[off]);
+    statistics.score = best_score.value;
+    out = best_model;
+    return true;
+  }
+};
+
+}  // namespace oracle

@@ -1,0 +1,152 @@
+// Oracle (test infrastructure only): homography estimator restated from
+// src/pygcransac/include/estimators/homography_estimator.h:58-382 and
+// src/pygcransac/include/estimators/solver_homography_four_point.h:109-286.
+#pragma once
+
+#include "oracle_common.hpp"
+#include "oracle_linalg.hpp"
+
+namespace oracle {
+
+struct HomographyEstimator {
+  static constexpr size_t sample_size() { return 4; }
+  static constexpr size_t non_minimal_sample_size() { return 4; }
+  size_t inlier_limit() const { return 7 * sample_size(); }
+
+  // squaredResidual (homography_estimator.h:181-199)
+  double squared_residual(const double* p, const Model& h) const {
+    const double x1 = p[0], y1 = p[1], x2 = p[2], y2 = p[3];
+    const double t1 = h[0] * x1 + h[1] * y1 + h[2];
+    const double t2 = h[3] * x1 + h[4] * y1 + h[5];
+    const double t3 = h[6] * x1 + h[7] * y1 + h[8];
+    const double d1 = x2 - (t1 / t3);
+    const double d2 = y2 - (t2 / t3);
+    return d1 * d1 + d2 * d2;
+  }
+
+  // HomographyFourPointSolver::estimateMinimalModel (:109-190) on rows
+  // idx(i); weight of row i is weights[idx(i)].
+  static bool minimal_solve(const double* const rows[4], const double* w4, Model& out) {
+    double a[8][9];
+    for (int i = 0; i < 4; ++i) {
+      const double* p = rows[i];
+      const double x1 = p[0], y1 = p[1], x2 = p[2], y2 = p[3];
+      const double w = w4 ? w4[i] : 1.0;
+      const double mwx1 = -w * x1, mwy1 = -w * y1, wx2 = w * x2, wy2 = w * y2;
+      double* r0 = a[2 * i];
+      double* r1 = a[2 * i + 1];
+      r0[0] = mwx1; r0[1] = mwy1; r0[2] = -w; r0[3] = 0; r0[4] = 0; r0[5] = 0;
+      r0[6] = wx2 * x1; r0[7] = wx2 * y1; r0[8] = -wx2;
+      r1[0] = 0; r1[1] = 0; r1[2] = 0; r1[3] = mwx1; r1[4] = mwy1; r1[5] = -w;
+      r1[6] = wy2 * x1; r1[7] = wy2 * y1; r1[8] = -wy2;
+    }
+    double h[8];
+    gauss_elimination<8>(a, h);
+    for (int i = 0; i < 8; ++i)
+      if (std::isnan(h[i])) return false;
+    out = {h[0], h[1], h[2], h[3], h[4], h[5], h[6], h[7], 1.0};
+    return true;
+  }
+
+  bool estimate_minimal(const Mat& pts, const size_t* s, std::vector<Model>& models) const {
+    const double* rows[4] = {pts.row(s[0]), pts.row(s[1]), pts.row(s[2]), pts.row(s[3])};
+    Model h;
+    if (!minimal_solve(rows, nullptr, h)) return false;
+    models.push_back(h);
+    return true;
+  }
+
+  // estimateModelNonminimal (:136-173): Hartley normalisation (:213-310), then
+  // HomographyFourPointSolver::estimateModel on the packed normalised rows with
+  // sample == nullptr, so packed row i is weighted by weights[i] (the weight of
+  // point index i, not of the i-th sample point), then denormalisation.
+  bool estimate_nonminimal(const Mat& pts, const size_t* s, size_t n, std::vector<Model>& models,
+                           const double* weights) const {
+    if (n < non_minimal_sample_size()) return false;
+    double ms[2] = {0, 0}, md[2] = {0, 0};
+    for (size_t i = 0; i < n; ++i) {
+      const double* p = pts.row(s[i]);
+      ms[0] += p[0]; ms[1] += p[1]; md[0] += p[2]; md[1] += p[3];
+    }
+    ms[0] /= n; ms[1] /= n; md[0] /= n; md[1] /= n;
+    double ads = 0, add = 0;
+    for (size_t i = 0; i < n; ++i) {
+      const double* p = pts.row(s[i]);
+      const double dx1 = ms[0] - p[0], dy1 = ms[1] - p[1], dx2 = md[0] - p[2], dy2 = md[1] - p[3];
+      ads += std::sqrt(dx1 * dx1 + dy1 * dy1);
+      add += std::sqrt(dx2 * dx2 + dy2 * dy2);
+    }
+    ads /= n; add /= n;
+    const double rs = M_SQRT2 / ads, rd = M_SQRT2 / add;
+    std::vector<double> np(n * 4);
+    for (size_t i = 0; i < n; ++i) {
+      const double* p = pts.row(s[i]);
+      np[i * 4 + 0] = (p[0] - ms[0]) * rs;
+      np[i * 4 + 1] = (p[1] - ms[1]) * rs;
+      np[i * 4 + 2] = (p[2] - md[0]) * rd;
+      np[i * 4 + 3] = (p[3] - md[1]) * rd;
+    }
+    const double Ts[9] = {rs, 0, -rs * ms[0], 0, rs, -rs * ms[1], 0, 0, 1};
+    const double Td[9] = {rd, 0, -rd * md[0], 0, rd, -rd * md[1], 0, 0, 1};
+    Model hn;
+    if (n == 4) {
+      const double* rows[4] = {&np[0], &np[4], &np[8], &np[12]};
+      double w4[4];
+      if (weights) for (int i = 0; i < 4; ++i) w4[i] = weights[i];
+      if (!minimal_solve(rows, weights ? w4 : nullptr, hn)) return false;
+    } else {
+      const int m = (int)(2 * n);
+      std::vector<double> A((size_t)m * 8), b(m);
+      for (size_t i = 0; i < n; ++i) {
+        const double x1 = np[i * 4], y1 = np[i * 4 + 1], x2 = np[i * 4 + 2], y2 = np[i * 4 + 3];
+        const double w = weights ? weights[i] : 1.0;
+        const double mwx1 = -w * x1, mwy1 = -w * y1, wx2 = w * x2, wy2 = w * y2;
+        double* r0 = &A[(2 * i) * 8];
+        double* r1 = &A[(2 * i + 1) * 8];
+        r0[0] = mwx1; r0[1] = mwy1; r0[2] = -w; r0[3] = 0; r0[4] = 0; r0[5] = 0; r0[6] = wx2 * x1; r0[7] = wx2 * y1;
+        b[2 * i] = -wx2;
+        r1[0] = 0; r1[1] = 0; r1[2] = 0; r1[3] = mwx1; r1[4] = mwy1; r1[5] = -w; r1[6] = wy2 * x1; r1[7] = wy2 * y1;
+        b[2 * i + 1] = -wy2;
+      }
+      double h[8];
+      if (!lstsq_colpiv_qr(A, b, m, 8, h)) return false;
+      hn = {h[0], h[1], h[2], h[3], h[4], h[5], h[6], h[7], 1.0};
+    }
+    double Tdi[9];
+    inverse3(Td, Tdi);
+    double t[9];
+    matmul3(Tdi, hn.data(), t);
+    Model out;
+    matmul3(t, Ts, out.data());
+    models.push_back(out);
+    return true;
+  }
+
+  // isValidModel (:326-342)
+  bool is_valid_model(Model& m, const Mat&, const std::vector<size_t>&, const size_t*, double, bool&) const {
+    return std::abs(det3(m)) >= 1e-2;
+  }
+
+  // isValidSample (:346-381): all four points on the same side of the lines
+  // through two of them, in both images.
+  bool is_valid_sample(const Mat& pts, const size_t* s) const {
+    const double *a = pts.row(s[0]), *b = pts.row(s[1]), *c = pts.row(s[2]), *d = pts.row(s[3]);
+    auto cross = [](double r[3], const double* u, const double* v) {
+      r[0] = u[1] - v[1];
+      r[1] = v[0] - u[0];
+      r[2] = u[0] * v[1] - u[1] * v[0];
+    };
+    double p[3], q[3];
+    cross(p, a, b);
+    cross(q, a + 2, b + 2);
+    if ((p[0] * c[0] + p[1] * c[1] + p[2]) * (q[0] * c[2] + q[1] * c[3] + q[2]) < 0) return false;
+    if ((p[0] * d[0] + p[1] * d[1] + p[2]) * (q[0] * d[2] + q[1] * d[3] + q[2]) < 0) return false;
+    cross(p, c, d);
+    cross(q, c + 2, d + 2);
+    if ((p[0] * a[0] + p[1] * a[1] + p[2]) * (q[0] * a[2] + q[1] * a[3] + q[2]) < 0) return false;
+    if ((p[0] * b[0] + p[1] * b[1] + p[2]) * (q[0] * b[2] + q[1] * b[3] + q[2]) < 0) return false;
+    return true;
+  }
+};
+
+}  // namespace oracle

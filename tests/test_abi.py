@@ -1,0 +1,75 @@
+"""CPU checks of the C-ABI boundary: libgcr.so loads, exports every function
+that include/gcr.h declares, and the ctypes mirror matches the C layout."""
+import os
+import re
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+from pygcransac import _abi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "gcr.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gcr_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_library_exports_header_symbols():
+    lib = _abi.load()
+    names = declared_functions()
+    assert "gcr_find_homography" in names and "gcr_batch_run_device" in names
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(names) <= set(_abi.exported_symbols())
+
+
+def test_struct_layout_matches_header():
+    src = r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "gcr.h"
+int main(void) {
+  printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(gcr_params), sizeof(gcr_stats), sizeof(gcr_image_size),
+         offsetof(gcr_params, seed), offsetof(gcr_params, sampler), offsetof(gcr_stats, status),
+         offsetof(gcr_params, use_space_partitioning));
+  return 0;
+}
+'''
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "t.c")
+        exe = os.path.join(d, "t")
+        open(c, "w").write(src)
+        subprocess.check_call(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), c, "-o", exe])
+        out = [int(v) for v in subprocess.check_output([exe]).split()]
+    P, S, Z = _abi.Params, _abi.Stats, _abi.ImageSize
+    import ctypes
+    assert out == [ctypes.sizeof(P), ctypes.sizeof(S), ctypes.sizeof(Z), P.seed.offset, P.sampler.offset,
+                   S.status.offset, P.use_space_partitioning.offset]
+
+
+def test_python_argument_checks(gcr):
+    with pytest.raises(ValueError):
+        gcr.findHomography(np.zeros((10, 3)), 480, 640, 480, 640)
+    with pytest.raises(ValueError):
+        gcr.findHomography(np.zeros((3, 4)), 480, 640, 480, 640)
+    with pytest.raises(ValueError):
+        gcr.findFundamentalMatrix(np.zeros((6, 4)), 480, 640, 480, 640)
+    with pytest.raises(ValueError):
+        gcr.findEssentialMatrix(np.zeros((4, 4)), np.eye(3), np.eye(3), 480, 640, 480, 640)
+
+
+def test_default_params_follow_reference(gcr):
+    p = gcr.default_params(_abi.GCR_HOMOGRAPHY)
+    assert (p.threshold, p.confidence, p.spatial_coherence_weight, p.max_iterations, p.min_iterations) == \
+        (1.0, 0.99, 0.975, 10000, 50)
+    assert (p.sampler, p.neighborhood, p.neighborhood_size, p.lo_number) == (1, 0, 4.0, 50)
+    f = gcr.default_params(_abi.GCR_FUNDAMENTAL)
+    assert (f.spatial_coherence_weight, f.neighborhood, f.neighborhood_size) == (0.0, 1, 20.0)
+    e = gcr.default_params(_abi.GCR_ESSENTIAL)
+    assert (e.spatial_coherence_weight, e.neighborhood) == (0.1, 1)

@@ -1,0 +1,134 @@
+"""CPU tests of the oracle (the checker): known answers, golden vectors and
+self-consistency. The reference ships no golden vectors for its H/F/E path;
+the pins here are the published Philox known-answer vectors, the reference's
+MAGSAC++ weight table (tests/golden/magsac_gamma_subset.json, made by
+tests/golden/make_magsac_gamma.py) and exact synthetic data."""
+import itertools
+import json
+import os
+
+import numpy as np
+import pytest
+
+from pygcransac import _abi, synthetic as S
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def h_params(**kw):
+    p = _abi.Params(threshold=3.0, confidence=0.99, spatial_coherence_weight=0.975, neighborhood_size=4,
+                    max_iterations=10000, min_iterations=50, sampler=0, neighborhood=0, lo_number=50, seed=0)
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def test_philox_known_answers(oracle):
+    # Philox4x32-10 known-answer vectors published with Random123 (kat_vectors)
+    assert oracle.philox([0, 0, 0, 0], [0, 0]) == [0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8]
+    f = 0xffffffff
+    assert oracle.philox([f, f, f, f], [f, f]) == [0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd]
+    assert oracle.philox([0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344], [0xa4093822, 0x299f31d0]) == \
+        [0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1]
+    # the stream layout: draw d of call c of stream s is word d&3 of counter {d>>2, c_lo, c_hi, s}
+    assert [oracle.draw_u32(0, 0, 0, d) for d in range(4)] == oracle.philox([0, 0, 0, 0], [0, 0])
+    assert oracle.draw_u32((7 << 32) | 5, 3, (2 << 32) | 9, 6) == oracle.philox([1, 9, 2, 3], [5, 7])[2]
+
+
+def test_magsac_table_matches_reference(oracle):
+    g = json.load(open(os.path.join(HERE, "golden", "magsac_gamma_subset.json")))
+    for k, v in g["entries"].items():
+        i = int(k)
+        if i > 36000:  # the lookup clamps at 36000 (scoring_function.h:330)
+            continue
+        assert abs(oracle.magsac_gamma(i) - v) <= 1e-12 * max(1.0, abs(v)), i
+
+
+def test_homography_exact_recovery(oracle):
+    pr = S.homography_pair(3, n=400, inlier_ratio=0.5, sigma=0.0)
+    rc, Hm, mask, st = oracle.find(0, pr["corr"], oracle.make_size(*pr["size"]), h_params(threshold=1.0))
+    assert rc == 0
+    Hn = Hm / Hm[2, 2]
+    assert np.abs(Hn - pr["H_gt"]).max() / np.abs(pr["H_gt"]).max() < 1e-9
+    assert mask[pr["inlier_gt"]].all()
+
+
+def test_homography_cfg_pair(oracle):
+    pr = S.homography_pair(0)
+    rc, Hm, mask, st = oracle.find(0, pr["corr"], oracle.make_size(*pr["size"]), h_params())
+    assert rc == 0
+    assert (mask & pr["inlier_gt"]).sum() >= 790
+    assert S.homography_error(Hm, pr["H_gt"]) < 1.0
+    assert st.local_optimization_number >= 2 and st.graph_cut_number >= 1
+
+
+def test_oracle_deterministic(oracle):
+    pr = S.homography_pair(7, n=600)
+    a = oracle.find(0, pr["corr"], oracle.make_size(*pr["size"]), h_params(seed=5))
+    b = oracle.find(0, pr["corr"], oracle.make_size(*pr["size"]), h_params(seed=5))
+    assert np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
+    assert a[3].iteration_number == b[3].iteration_number
+
+
+def test_too_few_points(oracle):
+    pr = S.homography_pair(1, n=50)
+    rc, *_ = oracle.find(0, pr["corr"][:3], oracle.make_size(*pr["size"]), h_params())
+    assert rc == _abi.GCR_TOO_FEW_POINTS
+
+
+def test_no_model_on_pure_outliers(oracle):
+    rng = np.random.default_rng(0)
+    corr = np.c_[rng.uniform(0, 640, (30, 1)), rng.uniform(0, 480, (30, 1)), rng.uniform(0, 640, (30, 1)),
+                 rng.uniform(0, 480, (30, 1))]
+    rc, Hm, mask, st = oracle.find(0, corr, oracle.make_size(480, 640, 480, 640), h_params(threshold=0.01))
+    assert rc == _abi.GCR_NO_MODEL and mask.sum() == 0
+
+
+def _energy(labels, d, r2le, lam, cells):
+    """Energy of a labelling (label 1 = SINK = inlier) as built by GCRANSAC::labeling."""
+    e = 0.0
+    for i, L in enumerate(labels):
+        if r2le[i]:
+            e += 0.0 if L else (1 - lam) * (1 - d[i])
+        else:
+            e += (1 - lam) * d[i] if L else 0.0
+    for cell in cells:
+        for a, b in itertools.combinations(cell, 2):
+            la, lb = labels[a], labels[b]
+            if la == 0 and lb == 0:
+                e += lam * 0.5 * (d[a] + d[b])
+            elif la != lb:
+                e += lam
+    return e
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_labeling_is_minimal_sink_min_cut(oracle, seed):
+    """The oracle's labelling is the minimiser of the graph-cut energy with the
+    smallest SINK set (the BK convention that free nodes are SOURCE), checked by
+    enumeration on a small problem."""
+    rng = np.random.default_rng(seed)
+    n = 11
+    H = np.eye(3)
+    x1 = rng.uniform(400, 600, (n, 2))
+    x2 = x1 + rng.normal(0, 2.5, (n, 2))
+    corr = np.c_[x1, x2]
+    # one grid cell holds every point, so the graph is a single clique
+    p = h_params(threshold=2.0, spatial_coherence_weight=0.6 + 0.05 * seed, neighborhood_size=1)
+    lab = oracle.labeling(0, corr, oracle.make_size(1000, 1000, 1000, 1000), p, H.reshape(9))
+    r2 = np.sum((x2 - x1) ** 2, axis=1)
+    sq = 2.0 ** 2 * 9 / 4
+    d = np.clip(r2 / sq, 0, 1)
+    cells = [list(range(n))]
+    lam = p.spatial_coherence_weight
+    best = None
+    minimisers = []
+    for bits in range(1 << n):
+        L = [(bits >> i) & 1 for i in range(n)]
+        e = _energy(L, d, r2 <= sq, lam, cells)
+        if best is None or e < best - 1e-12:
+            best, minimisers = e, [L]
+        elif abs(e - best) <= 1e-12:
+            minimisers.append(L)
+    inter = np.all(np.array(minimisers), axis=0)
+    assert np.array_equal(lab, inter.astype(bool))
