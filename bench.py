@@ -1,0 +1,340 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the GB300 Graph-Cut RANSAC engine.
+
+One step = one batch of synthetic image pairs run to completion by the pair
+engine (one persistent launch). `value` is pairs/s with the correspondences
+resident in HBM (device-pointer C-ABI entry, CUDA events on the launching
+stream, L2 flushed between steps by a 256 MiB write); `e2e` is the same metric
+through the host-buffer C-ABI entry gcr_find_batch, host<->device copies
+included. `--impl reference` times the CPU restatement of the reference's
+path (the oracle) on all host cores instead.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gcr|reference]
+                  [--workload homography|fundamental|essential] [--pairs P]
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "graph-cut-ransac_gb300"))
+
+from pygcransac import _abi, synthetic as S  # noqa: E402
+
+METRIC = "image pairs/sec at equal model error; learned vs plain GC-RANSAC on 1 GB300"
+
+# Algorithmic FP32 work of one residual evaluation (one model x one correspondence):
+# H transfer error 21 FLOP, Sampson distance 35 FLOP.
+FLOP_PER_RESIDUAL = {"homography": 21, "fundamental": 35, "essential": 35}
+
+WORKLOADS = {
+    # 2000 correspondences in 640x480, 40 % inliers (sigma 1 px), threshold 3 px,
+    # confidence 0.99, uniform sampler, 4^4 grid, lambda 0.975, 50 LO trials
+    "homography": dict(kind=_abi.GCR_HOMOGRAPHY, n=2000, ratio=0.4, threshold=3.0, sampler=0, grid=4,
+                       lam=0.975, pairs=1216),
+}
+
+
+def build_pairs(workload, pairs, seed0):
+    w = WORKLOADS[workload]
+    corr, sizes, gts = [], [], []
+    for i in range(pairs):
+        if workload == "homography":
+            pr = S.homography_pair(seed0 + i, n=w["n"], inlier_ratio=w["ratio"])
+            gts.append(pr["H_gt"])
+        corr.append(pr["corr"])
+        sizes.append(pr["size"])
+    offsets = np.zeros(pairs + 1, np.int64)
+    offsets[1:] = np.cumsum([len(c) for c in corr])
+    return np.ascontiguousarray(np.concatenate(corr), np.float64), offsets, np.array(sizes), gts
+
+
+def params_for(workload, seed=0):
+    w = WORKLOADS[workload]
+    return _abi.Params(threshold=w["threshold"], confidence=0.99, spatial_coherence_weight=w["lam"],
+                       neighborhood_size=w["grid"], max_iterations=10000, min_iterations=50,
+                       sampler=w["sampler"], neighborhood=0, lo_number=50, seed=seed)
+
+
+def size_array(sizes):
+    z = np.zeros(len(sizes), _abi.SIZE_DTYPE)
+    z["h1"], z["w1"], z["h2"], z["w2"] = sizes[:, 0], sizes[:, 1], sizes[:, 2], sizes[:, 3]
+    return z
+
+
+def model_errors(workload, models, gts):
+    if workload == "homography":
+        return [S.homography_error(m / m[2, 2] if abs(m[2, 2]) > 1e-12 else m, g) for m, g in zip(models, gts)]
+    return []
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].strip() == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def fp32_peak_tflops(torch):
+    """Measured FP32 CUDA-core peak: cuBLAS SGEMM 8192^3 with TF32 disabled."""
+    torch.backends.cuda.matmul.allow_tf32 = False
+    a = torch.randn(8192, 8192, device="cuda")
+    b = torch.randn(8192, 8192, device="cuda")
+    for _ in range(2):
+        a @ b
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        a @ b
+        e1.record()
+        e1.synchronize()
+        best = max(best, 2 * 8192 ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    del a, b
+    return best
+
+
+def cpu_baseline(workload, corr, offsets, sizes, p, target_s=10.0, max_pairs=1 << 30):
+    """The oracle (CPU restatement of the reference path) on all host cores,
+    on a bounded sample of the same workload. Returns (pairs/s, cores, sample)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    kind = WORKLOADS[workload]["kind"]
+    threads = os.cpu_count() or 1
+    P = len(offsets) - 1
+
+    def run(k):
+        # k pairs, cycling over the step's batch when k exceeds it
+        idx = np.arange(k) % P
+        lens = np.diff(offsets)[idx]
+        off = np.zeros(k + 1, np.int64)
+        off[1:] = np.cumsum(lens)
+        c = np.concatenate([corr[offsets[i]:offsets[i + 1]] for i in idx])
+        _, _, _, t = oracle.find_batch(kind, c, off, size_array(sizes[idx]), p,
+                                       seeds=idx.astype(np.uint64), threads=threads)
+        return k, t
+
+    k, t = run(max(2 * threads, 8))
+    rate = k / max(t, 1e-9)
+    k2 = int(min(max_pairs, max(k, rate * target_s)))
+    if k2 > k:
+        k, t = run(k2)
+    return k / t, threads, f"{k} pairs cycling over the step's batch ({t:.1f} s)"
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gcr", choices=["gcr", "reference"])
+    ap.add_argument("--workload", default="homography", choices=sorted(WORKLOADS))
+    ap.add_argument("--pairs", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    w = WORKLOADS[args.workload]
+    P = args.pairs or w["pairs"]
+    cfg = {"workload": f"{args.workload}: {P} pairs/step x {w['n']} correspondences, {int(w['ratio']*100)}% inliers",
+           "pairs_per_step": P, "correspondences": w["n"], "threshold": w["threshold"], "sampler": w["sampler"],
+           "grid": w["grid"], "spatial_coherence_weight": w["lam"], "l2": "flushed between steps (256 MiB write)",
+           "parallelism": f"replicas x{world}"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        corr, offsets, sizes, gts = build_pairs(args.workload, P, 0)
+        p = params_for(args.workload)
+        for _ in range(args.warmup):
+            cpu_baseline(args.workload, corr, offsets, sizes, p, target_s=1.0, max_pairs=64)
+        vals = []
+        for _ in range(args.steps):
+            v, cores, sample = cpu_baseline(args.workload, corr, offsets, sizes, p, target_s=8.0)
+            vals.append(v)
+        v = float(np.median(vals))
+        print(json.dumps({"metric": METRIC, "value": v, "unit": "pairs/s", "n_gpus": args.gpus,
+                          "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * P / v,
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                          "data": "synthetic", "config": cfg, "impl": "reference",
+                          "cpu_baseline": {"value": v, "unit": "pairs/s", "cores": cores, "kind": "port",
+                                           "sample": sample},
+                          "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
+
+    import torch
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+
+    lib = _abi.load()
+    corr, offsets, sizes, gts = build_pairs(args.workload, P, 1000003 * rank)
+    p = params_for(args.workload)
+    kind = w["kind"]
+    seeds = np.arange(P, dtype=np.uint64) + np.uint64(P * rank)
+    szs = size_array(sizes)
+    d_corr = torch.from_numpy(corr).cuda()
+    d_models = torch.zeros(P * 9, dtype=torch.float64, device="cuda")
+    d_masks = torch.zeros(int(offsets[-1]), dtype=torch.uint8, device="cuda")
+    d_stats = torch.zeros(P * _abi.STATS_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    ctx = ctypes.c_void_p()
+    assert lib.gcr_context_create(ctypes.byref(ctx)) == 0, _abi.last_error()
+    stream = torch.cuda.current_stream()
+
+    def step():
+        rc = lib.gcr_batch_run_device(ctx, kind, P, ctypes.c_void_p(d_corr.data_ptr()), _abi.ptr(offsets), None,
+                                      _abi.ptr(szs), ctypes.byref(p), _abi.ptr(seeds),
+                                      ctypes.c_void_p(d_models.data_ptr()), ctypes.c_void_p(d_masks.data_ptr()),
+                                      ctypes.c_void_p(d_stats.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
+        assert rc == 0, _abi.last_error()
+        return lib.gcr_last_launch_count()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local_rank)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    total_ms, launches = 0.0, 0
+    for _ in range(args.steps):
+        flush.fill_(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        launches += step()
+        e1.record(stream)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    t_rank = total_ms / 1e3
+    if dist:
+        t = torch.tensor([t_rank], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_rank = float(t.item())
+        dist.barrier()
+    value = P * world * args.steps / t_rank
+
+    stats = np.frombuffer(d_stats.cpu().numpy().tobytes(), _abi.STATS_DTYPE)
+    models = d_models.cpu().numpy().reshape(P, 3, 3)
+    n_per = np.diff(offsets)
+    flops = float(np.sum(stats["models_scored"] * n_per)) * FLOP_PER_RESIDUAL[args.workload]
+    errs = model_errors(args.workload, models, gts)
+
+    # end to end through the host-buffer entry: pinned inputs, copies timed
+    h_corr = torch.from_numpy(corr).pin_memory()
+    h_models = torch.zeros(P * 9, dtype=torch.float64).pin_memory()
+    h_masks = torch.zeros(int(offsets[-1]), dtype=torch.uint8).pin_memory()
+    h_stats = torch.zeros(P * _abi.STATS_DTYPE.itemsize, dtype=torch.uint8).pin_memory()
+
+    def e2e_step():
+        rc = lib.gcr_find_batch(kind, P, ctypes.c_void_p(h_corr.data_ptr()), _abi.ptr(offsets), None,
+                                _abi.ptr(szs), ctypes.byref(p), _abi.ptr(seeds),
+                                ctypes.c_void_p(h_models.data_ptr()), ctypes.c_void_p(h_masks.data_ptr()),
+                                ctypes.c_void_p(h_stats.data_ptr()))
+        assert rc == 0, _abi.last_error()
+
+    e2e_step()
+    e2e_t = 0.0
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_t += time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_t], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_t = float(t.item())
+    e2e_value = P * world * args.steps / e2e_t
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    peak = fp32_peak_tflops(torch)
+    achieved = flops / (total_ms / args.steps / 1e3) / 1e12
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", f"traffic_{args.workload}.json")
+    if os.path.exists(tp):
+        t = json.load(open(tp))
+        traffic = t["bytes_per_pair"] * P
+    line = {
+        "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32 scoring / fp64 solvers", "data": "synthetic", "config": cfg,
+        "median_model_error": float(np.median(errs)) if errs else None,
+        "status_ok_fraction": float(np.mean(stats["status"] == 0)),
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak if peak else None, "traffic": traffic,
+                     "peak_source": "cuBLAS SGEMM 8192^3, TF32 off, measured in this run",
+                     "work": f"{FLOP_PER_RESIDUAL[args.workload]} FLOP x models_scored x N per pair"},
+        "e2e": {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": int(corr.nbytes),
+                "d2h_bytes_per_step": int(P * 9 * 8 + offsets[-1] + P * _abi.STATS_DTYPE.itemsize)},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline and world == 1:
+        v, cores, sample = cpu_baseline(args.workload, corr, offsets, sizes, p)
+        line["cpu_baseline"] = {"value": v, "unit": "pairs/s", "cores": cores, "kind": "port", "sample": sample}
+    print(json.dumps(line))
+    lib.gcr_context_destroy(ctx)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -27,8 +27,8 @@ def nvcc():
     return cand
 
 
-def compile_one(src, extra):
-    obj = os.path.join(OUT, os.path.splitext(src)[0] + ".o")
+def compile_one(src, extra, out=OUT):
+    obj = os.path.join(out, os.path.splitext(src)[0] + ".o")
     cmd = [nvcc(), *ARCH, *FLAGS, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
@@ -36,17 +36,18 @@ def compile_one(src, extra):
     return obj, r.stderr
 
 
-def build(jobs=4, verbose=False, extra=()):
-    os.makedirs(OUT, exist_ok=True)
+def build(jobs=4, verbose=False, extra=(), out=OUT):
+    """Compiles every source with `extra` nvcc flags into `out`/libgcr.so."""
+    os.makedirs(out, exist_ok=True)
     srcs = [s for s in SOURCES if os.path.exists(os.path.join(CSRC, s))]
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
-        results = list(ex.map(lambda s: compile_one(s, list(extra)), srcs))
+        results = list(ex.map(lambda s: compile_one(s, list(extra), out), srcs))
     objs = [o for o, _ in results]
     if verbose:
         for _, log in results:
             if log.strip():
                 print(log, file=sys.stderr)
-    lib = os.path.join(OUT, "libgcr.so")
+    lib = os.path.join(out, "libgcr.so")
     tmp = lib + ".tmp"
     cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
     subprocess.run(cmd, check=True)

@@ -19,6 +19,7 @@ namespace {
 
 thread_local std::string g_last_error;
 thread_local long long g_last_launches = 0;
+thread_local long long* g_last_phase = nullptr;
 
 gcr_status fail(gcr_status s, const char* fmt, ...) {
   char buf[512];
@@ -72,7 +73,7 @@ const gcr::KindOps* ops_for(gcr_model_kind kind) {
 struct gcr_context {
   int device = 0;
   int num_sms = 0;
-  DevBuf pairs, slots_meta, slot_mem, pts32, ticket, norm_pts, kinv, row_pair;
+  DevBuf pairs, slots_meta, slot_mem, pts32, ticket, norm_pts, kinv, row_pair, phase;
   // staging of the host-buffer entry points
   DevBuf corr, models, masks, stats;
   int slot_kind = -1, slot_max_n = 0, slot_count = 0;
@@ -148,6 +149,11 @@ void gcr_default_params(gcr_model_kind kind, gcr_params* p) {
 const char* gcr_last_error_string(void) { return g_last_error.c_str(); }
 
 int64_t gcr_last_launch_count(void) { return g_last_launches; }
+
+#ifdef GCR_PHASE_PROFILE
+// Device pointer of the [P][16] phase counters of the last launch (profiling builds only).
+void* gcr_debug_phase_counters(void) { return g_last_phase; }
+#endif
 
 gcr_status gcr_context_create(gcr_context** ctx) {
   if (!ctx) return fail(GCR_INVALID_ARG, "ctx is NULL");
@@ -269,6 +275,13 @@ gcr_status gcr_batch_run_device(gcr_context* c, gcr_model_kind kind, int64_t num
   ws.models_out = d_models_out;
   ws.masks_out = d_masks_out;
   ws.stats_out = (gcr::StatsOut*)d_stats_out;
+  ws.phase = nullptr;
+#ifdef GCR_PHASE_PROFILE
+  CUDA_TRY(c->phase.ensure(sizeof(long long) * 16 * num_pairs));
+  CUDA_TRY(cudaMemsetAsync(c->phase.p, 0, sizeof(long long) * 16 * num_pairs, s));
+  ws.phase = (long long*)c->phase.p;
+  g_last_phase = (long long*)c->phase.p;
+#endif
 
   gcr::EngineParams prm;
   prm.confidence = params->confidence;

@@ -44,20 +44,19 @@ struct DrawStream {
   uint32_t stream;
   uint64_t call;
   uint32_t d = 0;
-  uint32_t block[4];
+  uint32_t w0 = 0, w1 = 0, w2 = 0, w3 = 0;  // current 4-word block (kept in registers)
   uint32_t block_id = 0xffffffffu;
   __device__ DrawStream(uint64_t s, uint32_t st, uint64_t c) : seed(s), stream(st), call(c) {}
   __device__ __forceinline__ uint32_t next_u32() {
     const uint32_t b = d >> 2;
     if (b != block_id) {
-      block[0] = b;
-      block[1] = (uint32_t)call;
-      block[2] = (uint32_t)(call >> 32);
-      block[3] = stream;
-      philox4x32_10(block, (uint32_t)seed, (uint32_t)(seed >> 32));
+      uint32_t blk[4] = {b, (uint32_t)call, (uint32_t)(call >> 32), stream};
+      philox4x32_10(blk, (uint32_t)seed, (uint32_t)(seed >> 32));
+      w0 = blk[0]; w1 = blk[1]; w2 = blk[2]; w3 = blk[3];
       block_id = b;
     }
-    return block[(d++) & 3];
+    const uint32_t q = (d++) & 3;
+    return q == 0 ? w0 : (q == 1 ? w1 : (q == 2 ? w2 : w3));
   }
   // uniform integer in [lo, hi] (inclusive)
   __device__ __forceinline__ uint32_t next_in(uint32_t lo, uint32_t hi) {

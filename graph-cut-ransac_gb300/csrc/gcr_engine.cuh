@@ -69,6 +69,7 @@ struct StatsOut {
   double score;
   int32_t status;
   int32_t flags;
+  int64_t models_scored;
 };
 
 // Per-CTA scratch in global memory (one slot per resident CTA).
@@ -100,6 +101,7 @@ struct Workspace {
   double* models_out;   // [P][9]
   uint8_t* masks_out;   // [total]
   StatsOut* stats_out;  // [P]
+  long long* phase;     // [P][16] phase cycle counters (GCR_PHASE_PROFILE builds), else null
 };
 
 struct Score {
@@ -123,6 +125,7 @@ struct Shared {
   double lo_best_model[9];
   double work_model[9];
   double fit_model[9];
+  float mf32[12];                 // FP32 form of the model being scored exactly
   double red_d[GCR_WARPS * 48];
   int red_i[GCR_WARPS + 2];
   int n_ok[GCR_BLOCK];
@@ -172,6 +175,7 @@ struct Engine {
 
   // sequential state (identical in every thread)
   long long iter = 0, max_iter = 0, gc_number = 0, lo_number = 0, lo_calls = 0;
+  long long models_scored = 0;  // models the sequential algorithm scores in full
   Score best{0, 0.0};
   Container cont[2];
   int off = 0;
@@ -189,6 +193,22 @@ struct Engine {
   }
 
   __device__ __forceinline__ void sync() { __syncthreads(); }
+
+  // Optional per-phase cycle counters (built with -DGCR_PHASE_PROFILE).
+  __device__ __forceinline__ long long tick() const {
+#ifdef GCR_PHASE_PROFILE
+    return clock64();
+#else
+    return 0;
+#endif
+  }
+  __device__ __forceinline__ void tock(int id, long long t0, long long count = -1) const {
+#ifdef GCR_PHASE_PROFILE
+    if (threadIdx.x == 0 && ws.phase) ws.phase[pair * 16 + id] += count >= 0 ? count : clock64() - t0;
+#else
+    (void)id; (void)t0; (void)count;
+#endif
+  }
 
   // thread 0 copies 9 doubles; everyone waits
   __device__ void copy_model(double* dst, const double* src) {
@@ -272,22 +292,47 @@ struct Engine {
     }
   }
 
+  // FP32 form of `model` in sh.mf32 (thread 0, then everyone waits).
+  __device__ void prepare_shared_f32(const double* model) {
+    sync();
+    if (threadIdx.x == 0) Est::prepare_f32(model, pd.centre, scale, sh.mf32);
+    sync();
+  }
+
   // Exact FP64 MSAC score (scoring_function.h:137-233) of a model; optionally
-  // writes the inlier list in index order.
-  __device__ Score exact_score(const double* model, int* list) {
+  // writes the inlier list in index order. Points whose FP32 residual lies
+  // above the threshold by more than its error bound are outliers without an
+  // FP64 evaluation; all others are decided and summed in FP64.
+  __device__ Score exact_score(const double* model, int* list, const float* m32 = nullptr) {
+    if (m32 == nullptr) {
+      prepare_shared_f32(model);
+      m32 = sh.mf32;
+    }
     double h[9];
+    float hf[9];
 #pragma unroll
-    for (int q = 0; q < 9; ++q) h[q] = model[q];
+    for (int q = 0; q < 9; ++q) {
+      h[q] = model[q];
+      hf[q] = m32[q];
+    }
+    const float cm = m32[9];
+    const float tf = (float)sqrt(t2), t2f = (float)t2;
     double acc = 0.0;
     int total = 0;
     for (int base = 0; base < N; base += GCR_BLOCK) {
       const int i = base + threadIdx.x;
       int f = 0;
       if (i < N) {
-        const double r2 = Est::r2_f64(pts64 + 4 * i, h);
-        if (r2 < t2) {
-          f = 1;
-          acc -= r2;
+        float it;
+        const float r2f = Est::r2_f32(pts32[i], hf, it);
+        const float e = fmaf(cm, fabsf(it), cm);
+        const float eb = fmaf(e, e, 2.f * tf * e);
+        if (!(r2f - t2f > eb)) {
+          const double r2 = Est::r2_f64(pts64 + 4 * i, h);
+          if (r2 < t2) {
+            f = 1;
+            acc -= r2;
+          }
         }
       }
       int tot;
@@ -364,6 +409,17 @@ struct Engine {
   // preflow; then a backward search from the sink over residuals above
   // kResidualEps marks the SINK side (what_segment == SINK, graph.h:478-483).
   // Writes slot.flag[point] for the cell's points. Returns false on the step cap.
+  // Comparisons of non-negative doubles through their bit patterns (IEEE order
+  // equals integer order for non-negative values) keep the residual tests off
+  // the FP64 pipe.
+  __device__ __forceinline__ static bool dpos(double x) { return __double_as_longlong(x) > 0; }
+  __device__ __forceinline__ static bool dgt(double x, double y) {
+    return __double_as_longlong(x) > __double_as_longlong(y);
+  }
+  __device__ __forceinline__ static bool dlt(double x, double y) {
+    return __double_as_longlong(x) < __double_as_longlong(y);
+  }
+
   __device__ bool mincut_cell(int c0, int n, int warp) {
     const int lane = threadIdx.x & 31;
     const double lam = prm.lambda;
@@ -393,14 +449,14 @@ struct Engine {
     __syncwarp();
     const int dead = n + 2;
     // exact distance labels: backward BFS from the sink over residual arcs
-    for (int i = lane; i < n; i += 32) h[i] = sr[i] > 0 ? 1 : dead;
+    for (int i = lane; i < n; i += 32) h[i] = dpos(sr[i]) ? 1 : dead;
     __syncwarp();
     for (int level = 1; level <= n; ++level) {
       bool grew = false;
       for (int u = lane; u < n; u += 32) {
         if (h[u] != dead) continue;
         for (int v = 0; v < n; ++v)
-          if (h[v] == level && R[u * n + v] > 0) {
+          if (h[v] == level && dpos(R[u * n + v])) {
             h[u] = -(level + 1);
             break;
           }
@@ -418,7 +474,7 @@ struct Engine {
     int qh = 0, qt = 0;
     for (int base = 0; base < n; base += 32) {
       const int u = base + lane;
-      const bool act = u < n && ex[u] > 0 && h[u] < dead;
+      const bool act = u < n && dpos(ex[u]) && h[u] < dead;
       const unsigned b = __ballot_sync(0xffffffffu, act);
       if (act) {
         q[(qt + __popc(b & ((1u << lane) - 1))) % kMaxFlowCap] = u;
@@ -439,31 +495,31 @@ struct Engine {
         if (++ops > kFlowOpsCap) { ok = false; break; }
         double e = ex[u];
         const int hu = h[u];
-        if (!(e > 0) || hu >= dead) break;
-        if (hu == 1 && sr[u] > 0) {
+        if (!dpos(e) || hu >= dead) break;
+        if (hu == 1 && dpos(sr[u])) {
           __syncwarp();
           if (lane == 0) {
             const double s = sr[u];
-            const double dl = e < s ? e : s;
+            const double dl = dlt(e, s) ? e : s;
             ex[u] = e - dl;
             sr[u] = s - dl;
           }
           __syncwarp();
           e = ex[u];
-          if (!(e > 0)) break;
+          if (!dpos(e)) break;
         }
-        for (int base = 0; base < n && e > 0; base += 32) {
+        for (int base = 0; base < n && dpos(e); base += 32) {
           const int v = base + lane;
-          const bool adm = v < n && v != u && h[v] == hu - 1 && R[u * n + v] > 0;
+          const bool adm = v < n && v != u && h[v] == hu - 1 && dpos(R[u * n + v]);
           unsigned b = __ballot_sync(0xffffffffu, adm);
-          while (b != 0u && e > 0) {
+          while (b != 0u && dpos(e)) {
             const int vv = base + __ffs(b) - 1;
             b &= b - 1;
             int enq = 0;
             __syncwarp();
             if (lane == 0) {
               const double r = R[u * n + vv];
-              const double dl = e < r ? e : r;
+              const double dl = dlt(e, r) ? e : r;
               R[u * n + vv] = r - dl;
               R[vv * n + u] = R[vv * n + u] + dl;
               ex[u] = e - dl;
@@ -480,11 +536,11 @@ struct Engine {
             e = ex[u];
           }
         }
-        if (!(e > 0)) break;
+        if (!dpos(e)) break;
         // relabel: 1 + min label over residual arcs (the sink has label 0)
-        int mn = sr[u] > 0 ? 0 : 0x7fffffff;
+        int mn = dpos(sr[u]) ? 0 : 0x7fffffff;
         for (int v = lane; v < n; v += 32)
-          if (v != u && R[u * n + v] > 0 && h[v] < mn) mn = h[v];
+          if (v != u && dpos(R[u * n + v]) && h[v] < mn) mn = h[v];
         mn = warp_min(mn);
         __syncwarp();
         if (lane == 0) h[u] = (mn == 0x7fffffff || mn + 1 >= dead) ? dead : mn + 1;
@@ -494,14 +550,14 @@ struct Engine {
     }
     __syncwarp();
     // SINK side: backward search from the sink over residuals > kResidualEps
-    for (int i = lane; i < n; i += 32) mark[i] = sr[i] > kResidualEps ? 1 : 0;
+    for (int i = lane; i < n; i += 32) mark[i] = dgt(sr[i], kResidualEps) ? 1 : 0;
     __syncwarp();
     for (int round = 0; round < n; ++round) {
       bool grew = false;
       for (int u = lane; u < n; u += 32) {
         if (mark[u]) continue;
         for (int v = 0; v < n; ++v)
-          if (mark[v] == 1 && R[u * n + v] > kResidualEps) {
+          if (mark[v] == 1 && dgt(R[u * n + v], kResidualEps)) {
             mark[u] = 2;
             break;
           }
@@ -525,10 +581,27 @@ struct Engine {
   __device__ int labeling(const double* model, int ncells, int* list) {
     const double sq = t2;  // thr^2 * 9 / 4
     const double oml = 1.0 - prm.lambda;
+    prepare_shared_f32(model);
     double h[9];
+    float hf[9];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) h[k] = model[k];
+    for (int k = 0; k < 9; ++k) {
+      h[k] = model[k];
+      hf[k] = sh.mf32[k];
+    }
+    const float cm = sh.mf32[9];
+    const float tf = (float)sqrt(t2), t2f = (float)t2;
     for (int i = threadIdx.x; i < N; i += GCR_BLOCK) {
+      float it;
+      const float r2f = Est::r2_f32(pts32[i], hf, it);
+      const float ee = fmaf(cm, fabsf(it), cm);
+      const float eb = fmaf(ee, ee, 2.f * tf * ee);
+      if (r2f - t2f > eb) {
+        // certainly beyond the threshold: d = 1 and the unary term is (1 - lambda)
+        slot.dres[i] = 1.0;
+        slot.tr[i] = oml * (1 - 0.0) - 0;
+        continue;
+      }
       const double r2 = Est::r2_f64(pts64 + 4 * i, h);
       double di = r2 / sq;
       di = di < 0.0 ? 0.0 : (di > 1.0 ? 1.0 : di);
@@ -546,7 +619,7 @@ struct Engine {
       if (n == 1 || !pairwise) {
         for (int k = lane; k < n; k += 32) {
           const int p = slot.cell_pts[c0 + k];
-          slot.flag[p] = (uint8_t)(-slot.tr[p] > kResidualEps ? 1 : 0);
+          slot.flag[p] = (uint8_t)(slot.tr[p] < -kResidualEps ? 1 : 0);
         }
       } else if (n > kMaxFlowCap) {
         if (lane == 0) atomicMax(&sh.flow_status, ST_CAPACITY);
@@ -650,30 +723,44 @@ struct Engine {
     ++lo_number;
     while (++gc_number < 10) {
       bool updated = false;
+      long long t0 = tick();
       const int nL = labeling(sh.lo_best_model, ncells, L);
+      tock(4, t0);
+      t0 = tick();
       const int ss = min(inlier_limit, nL);
       if (ss < nL) {
-        // trials sample from the labelled inliers with the LO sampler stream
+        // one thread per trial: sample from the labelled inliers with the LO
+        // sampler stream, then the normalised least-squares fit
         const int kb = kBatchModels;
         if (threadIdx.x < trials) {
+          long long c0 = tick();
           int* smp = slot.samples + threadIdx.x * Est::SAMPLE_CAP;
           DrawStream ds(pd.seed, STREAM_LO, (uint64_t)(lo_calls + threadIdx.x));
           bool ok = unique_set(ds, smp, ss, 0, (uint32_t)(nL - 1));
+          tock(12, c0);
+          c0 = tick();
           if (ok) {
             for (int q = 0; q < ss; ++q) smp[q] = L[smp[q]];
-            ok = Est::fit_thread(pts64, smp, ss, nullptr, slot.models64 + 9 * (kb + threadIdx.x));
+            ok = Est::fit_thread(pts64, smp, ss, slot.models64 + 9 * (kb + threadIdx.x));
           }
+          tock(13, c0);
+          c0 = tick();
           sh.lo_ok[threadIdx.x] = ok ? 1 : 0;
           if (ok) put_f32(kb + threadIdx.x);
+          tock(14, c0);
         }
         sync();
+        tock(5, t0);
         lo_calls += trials;
+        t0 = tick();
         score_lo_trials(kb, trials, max_score, updated);
+        tock(6, t0);
       } else if (m < nL) {
         if (!fit_cta(L, nL, 0)) {
           // the reference breaks out of the trial loop; nothing was updated
         } else {
           const Score sc = exact_score(sh.fit_model, nullptr);
+          models_scored += trials;
           if (max_score.value < sc.value) {
             updated = true;
             max_score = sc;
@@ -697,9 +784,11 @@ struct Engine {
     score_models_f32(kb, trials);
     for (int t = 0; t < trials; ++t) {
       if (!sh.lo_ok[t]) continue;
+      ++models_scored;
       const int k = kb + t;
       if (sh.mcount[k] == 0 || !maybe_better(k, max_score.value)) continue;
-      const Score sc = exact_score(slot.models64 + 9 * k, nullptr);
+      tock(10, 0, 1);
+      const Score sc = exact_score(slot.models64 + 9 * k, nullptr, slot.models32 + 12 * k);
       if (max_score.value < sc.value) {
         updated = true;
         max_score = sc;
@@ -729,6 +818,7 @@ struct Engine {
       sync();
       if (!fit_cta(list, n, 1)) break;
       const Score sc = exact_score(sh.fit_model, spare);
+      ++models_scored;
       if (sc.count < m) break;
       if (sc.count <= n) break;
       copy_model(sh.work_model, sh.fit_model);
@@ -812,7 +902,9 @@ struct Engine {
 
   // ------------------------------------------------------------------
   __device__ void run() {
+    long long t0 = tick();
     const int ncells = build_grid();
+    tock(0, t0);
     max_iter = iteration_number_for(1, N, m, log_prob);
     const long long max_iters = prm.max_iters, min_iters = prm.min_iters;
     // PROSAC state: kth, subset size, draw range, T_n, growth[subset-1]
@@ -824,9 +916,13 @@ struct Engine {
     int nfail = 0;
     const long long attempt_cap = (max_iters < 0x7fffffffLL ? max_iters : 0x7fffffffLL) * 101 + 101;
     while (!done) {
+      t0 = tick();
       generate_batch(attempt, p_kth, p_subset, p_hi, p_Tn, p_Tprime);
+      tock(1, t0);
+      t0 = tick();
       const int K = sh.mbase[GCR_BLOCK - 1] + sh.n_ok[GCR_BLOCK - 1];
       score_models_f32(0, K);
+      tock(2, t0);
       for (int j = 0; j < GCR_BLOCK; ++j) {
         if (!in_iter) {
           const long long lim = max_iter < max_iters ? max_iter : max_iters;
@@ -852,9 +948,13 @@ struct Engine {
         for (int q = 0; q < nm; ++q) {
           const int k = sh.mbase[j] + q;
           const double* mk = slot.models64 + 9 * k;
+          ++models_scored;
           cont[off] = {mk, sh.mcount[k]};
           if (sh.mcount[k] == 0 || !maybe_better(k, best.value)) continue;
-          const Score sc = exact_score(mk, nullptr);
+          t0 = tick();
+          const Score sc = exact_score(mk, nullptr, slot.models32 + 12 * k);
+          tock(3, t0);
+          tock(9, 0, 1);
           if (best.value < sc.value && Est::valid_model(mk)) {
             off ^= 1;
             copy_model(sh.best_model, mk);
@@ -865,7 +965,9 @@ struct Engine {
         }
         if (do_lo) {
           ++lo_number;
+          t0 = tick();
           local_optimization(ncells);
+          tock(11, t0);
           max_iter = iteration_number_for(best.count, N, m, log_prob);
         }
       }
@@ -883,7 +985,9 @@ struct Engine {
         done = true;
       }
     }
+    t0 = tick();
     finish(ncells);
+    tock(8, t0);
   }
 
   __device__ void finish(int ncells) {
@@ -900,6 +1004,7 @@ struct Engine {
         so->score = best.value;
         so->status = status == ST_OK ? ST_NO_MODEL : status;
         so->flags = flags;
+        so->models_scored = models_scored;
       }
       return;
     }
@@ -963,6 +1068,7 @@ struct Engine {
       so->score = best.value;
       so->status = status;
       so->flags = flags;
+      so->models_scored = models_scored;
     }
     sync();
   }

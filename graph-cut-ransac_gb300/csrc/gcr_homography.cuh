@@ -18,7 +18,6 @@ struct HomographyModel {
   static constexpr int NONMIN = 4;     // smallest non-minimal sample
   static constexpr int INLIER_LIMIT = 7 * M;
   static constexpr bool WEIGHTED = true;
-  static constexpr int NACC = 44;          // packed upper 8x8 normal matrix + right side
   static constexpr int SAMPLE_CAP = INLIER_LIMIT;
 
   // orientation test: the four points keep the same side of the lines through
@@ -126,81 +125,129 @@ struct HomographyModel {
     out[11] = 0.f;
   }
 
-  // Hartley normalisation of the selected rows (normalizePoints semantics).
-  // Returns the similarity parameters (mass points and ratios).
+  // Hartley normalisation of the selected rows (normalizePoints semantics):
+  // mass points and sqrt(2) / mean distance ratios of both images.
   struct Norm {
     double ms0, ms1, md0, md1, rs, rd;
   };
 
-  // Normalised least squares over n rows given by idx[] with optional per-row
-  // weights (row k uses wrow[k]), single thread. Denormalised result in out.
-  __device__ static bool fit_thread(const double* pts, const int* idx, int n, const double* wrow, double* out) {
-    if (n < NONMIN) return false;
-    Norm N;
-    {
-      double a = 0, b = 0, c = 0, d = 0;
-      for (int i = 0; i < n; ++i) {
-        const double* p = pts + 4 * idx[i];
-        a += p[0]; b += p[1]; c += p[2]; d += p[3];
-      }
-      N.ms0 = a / n; N.ms1 = b / n; N.md0 = c / n; N.md1 = d / n;
-      double ads = 0, add = 0;
-      for (int i = 0; i < n; ++i) {
-        const double* p = pts + 4 * idx[i];
-        const double dx1 = N.ms0 - p[0], dy1 = N.ms1 - p[1], dx2 = N.md0 - p[2], dy2 = N.md1 - p[3];
-        ads += sqrt(dx1 * dx1 + dy1 * dy1);
-        add += sqrt(dx2 * dx2 + dy2 * dy2);
-      }
-      N.rs = M_SQRT2 / (ads / n);
-      N.rd = M_SQRT2 / (add / n);
-    }
-    double acc[NACC];
-    for (int k = 0; k < NACC; ++k) acc[k] = 0;
-    for (int i = 0; i < n; ++i) {
-      const double* p = pts + 4 * idx[i];
-      const double w = wrow ? wrow[i] : 1.0;
-      accumulate(N, p, w, acc);
-    }
-    return solve_normal(N, acc, out);
-  }
-
-  // Adds the two weighted equations of one correspondence to the packed
-  // normal equations (upper triangle of the 8x8 A^T A, row-major packed).
+  // The weighted least-squares system of the non-minimal solver (rows
+  // w[-x,-y,-1,0,0,0,Xx,Xy] = -wX and w[0,0,0,-x,-y,-1,Yx,Yy] = -wY in
+  // normalised coordinates) has the normal matrix
+  //   [S 0 -B_X; 0 S -B_Y; -B_X^T -B_Y^T C]  with  S = sum w^2 u u^T, u = (x, y, 1),
+  //   B_X = sum w^2 X u v^T, B_Y = sum w^2 Y u v^T, C = sum w^2 (X^2+Y^2) v v^T, v = (x, y),
+  // so 23 sums describe it completely (instead of 44 entries of the dense form).
+  static constexpr int NACC = 23;
+  // acc layout: 0..5 S (xx xy x yy y 1) | 6..10 X (xx xy x yy y) | 11..15 Y (same)
+  //             16..18 R (xx xy yy) | 19 X | 20 Y | 21..22 R (x y)
   __device__ __forceinline__ static void accumulate(const Norm& N, const double* p, double w, double* acc) {
-    double* ata = acc;
-    double* atb = acc + 36;
-    const double x1 = (p[0] - N.ms0) * N.rs, y1 = (p[1] - N.ms1) * N.rs;
-    const double x2 = (p[2] - N.md0) * N.rd, y2 = (p[3] - N.md1) * N.rd;
-    const double mwx1 = -w * x1, mwy1 = -w * y1, wx2 = w * x2, wy2 = w * y2;
-    const double r0[8] = {mwx1, mwy1, -w, 0, 0, 0, wx2 * x1, wx2 * y1};
-    const double r1[8] = {0, 0, 0, mwx1, mwy1, -w, wy2 * x1, wy2 * y1};
-    const double b0 = -wx2, b1 = -wy2;
-    int k = 0;
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-#pragma unroll
-      for (int j = i; j < 8; ++j) ata[k++] += r0[i] * r0[j] + r1[i] * r1[j];
-      atb[i] += r0[i] * b0 + r1[i] * b1;
-    }
+    const double x = (p[0] - N.ms0) * N.rs, y = (p[1] - N.ms1) * N.rs;
+    const double X = (p[2] - N.md0) * N.rd, Y = (p[3] - N.md1) * N.rd;
+    const double w2 = w * w;
+    const double wx = w2 * x, wy = w2 * y;
+    acc[0] += wx * x; acc[1] += wx * y; acc[2] += wx; acc[3] += wy * y; acc[4] += wy; acc[5] += w2;
+    const double Xwx = X * wx, Xwy = X * wy;
+    acc[6] += Xwx * x; acc[7] += Xwx * y; acc[8] += Xwx; acc[9] += Xwy * y; acc[10] += Xwy;
+    const double Ywx = Y * wx, Ywy = Y * wy;
+    acc[11] += Ywx * x; acc[12] += Ywx * y; acc[13] += Ywx; acc[14] += Ywy * y; acc[15] += Ywy;
+    const double R = X * X + Y * Y;
+    const double Rwx = R * wx, Rwy = R * wy;
+    acc[16] += Rwx * x; acc[17] += Rwx * y; acc[18] += Rwy * y;
+    acc[19] += X * w2; acc[20] += Y * w2; acc[21] += Rwx; acc[22] += Rwy;
   }
 
-  __device__ static bool solve_normal(const Norm& N, const double* acc, double* out) {
-    const double* ata = acc;
-    const double* atb = acc + 36;
-    double A[8][8], x[8];
-    int k = 0;
-    for (int i = 0; i < 8; ++i)
-      for (int j = i; j < 8; ++j) { A[i][j] = ata[k]; A[j][i] = ata[k]; ++k; }
-    for (int i = 0; i < 8; ++i) x[i] = atb[i];
-    if (!cholesky_solve<8>(A, x)) return false;
-    const double hn[9] = {x[0], x[1], x[2], x[3], x[4], x[5], x[6], x[7], 1.0};
-    // H = Td^-1 * Hn * Ts with Ts = [rs 0 -rs ms0; 0 rs -rs ms1; 0 0 1]
+  // Solves the normal equations by block elimination (one 3x3 LDL^T of S
+  // shared by both 3x3 blocks, then the 2x2 Schur complement) and
+  // denormalises: H = Td^-1 Hn Ts.
+  __device__ static bool solve_normal(const Norm& N, const double* a, double* out) {
+    // S (symmetric 3x3): s00 s01 s02 / s11 s12 / s22
+    const double s00 = a[0], s01 = a[1], s02 = a[2], s11 = a[3], s12 = a[4], s22 = a[5];
+    // LDL^T. Like the reference's least-squares solver, a degenerate system
+    // still yields a (possibly non-finite) model rather than a failure.
+    const double d0 = s00;
+    const double l10 = s01 / d0, l20 = s02 / d0;
+    const double d1 = s11 - l10 * s01;
+    const double l21 = (s12 - l20 * s01) / d1;
+    const double d2 = s22 - l20 * s02 - l21 * (s12 - l20 * s01);
+    auto solveS = [&](double b0, double b1, double b2, double* z) {
+      const double y0 = b0, y1 = b1 - l10 * y0, y2 = b2 - l20 * y0 - l21 * y1;
+      const double z2 = y2 / d2, z1 = y1 / d1 - l21 * z2, z0 = y0 / d0 - l10 * z1 - l20 * z2;
+      z[0] = z0; z[1] = z1; z[2] = z2;
+    };
+    // B_X columns (u * x, u * y) and B_Y; the off-diagonal blocks are -B
+    const double BX0[3] = {a[6], a[7], a[8]};   // u * x : (xx, yx, x)
+    const double BX1[3] = {a[7], a[9], a[10]};  // u * y : (xy, yy, y)
+    const double BY0[3] = {a[11], a[12], a[13]};
+    const double BY1[3] = {a[12], a[14], a[15]};
+    // right-hand sides: (S_X u, S_Y u, -S_R v)
+    const double b1x[3] = {a[8], a[10], a[19]};
+    const double b1y[3] = {a[13], a[15], a[20]};
+    double ZX0[3], ZX1[3], ZY0[3], ZY1[3], zx[3], zy[3];
+    solveS(BX0[0], BX0[1], BX0[2], ZX0);
+    solveS(BX1[0], BX1[1], BX1[2], ZX1);
+    solveS(BY0[0], BY0[1], BY0[2], ZY0);
+    solveS(BY1[0], BY1[1], BY1[2], ZY1);
+    solveS(b1x[0], b1x[1], b1x[2], zx);
+    solveS(b1y[0], b1y[1], b1y[2], zy);
+    auto dot3 = [](const double* p, const double* q) { return p[0] * q[0] + p[1] * q[1] + p[2] * q[2]; };
+    // Schur complement M = C - B_X^T S^-1 B_X - B_Y^T S^-1 B_Y (the signs of -B cancel)
+    const double m00 = a[16] - dot3(BX0, ZX0) - dot3(BY0, ZY0);
+    const double m01 = a[17] - dot3(BX0, ZX1) - dot3(BY0, ZY1);
+    const double m11 = a[18] - dot3(BX1, ZX1) - dot3(BY1, ZY1);
+    // right side: -S_R v - (-B_X)^T S^-1 b1x - (-B_Y)^T S^-1 b1y
+    const double r0 = -a[21] + dot3(BX0, zx) + dot3(BY0, zy);
+    const double r1 = -a[22] + dot3(BX1, zx) + dot3(BY1, zy);
+    const double det = m00 * m11 - m01 * m01;
+    const double h6 = (r0 * m11 - r1 * m01) / det;
+    const double h7 = (m00 * r1 - m01 * r0) / det;
+    // h1 = S^-1 (b1x + B_X h3), h2 = S^-1 (b1y + B_Y h3)
+    double hn[9];
+    hn[0] = zx[0] + ZX0[0] * h6 + ZX1[0] * h7;
+    hn[1] = zx[1] + ZX0[1] * h6 + ZX1[1] * h7;
+    hn[2] = zx[2] + ZX0[2] * h6 + ZX1[2] * h7;
+    hn[3] = zy[0] + ZY0[0] * h6 + ZY1[0] * h7;
+    hn[4] = zy[1] + ZY0[1] * h6 + ZY1[1] * h7;
+    hn[5] = zy[2] + ZY0[2] * h6 + ZY1[2] * h7;
+    hn[6] = h6;
+    hn[7] = h7;
+    hn[8] = 1.0;
     const double Ts[9] = {N.rs, 0, -N.rs * N.ms0, 0, N.rs, -N.rs * N.ms1, 0, 0, 1};
     const double Tdi[9] = {1.0 / N.rd, 0, N.md0, 0, 1.0 / N.rd, N.md1, 0, 0, 1};
     double t[9];
     matmul3(Tdi, hn, t);
     matmul3(t, Ts, out);
     return true;
+  }
+
+  __device__ static void normalise(const double* pts, const int* idx, int n, Norm& N) {
+    double a = 0, b = 0, c = 0, d = 0;
+    for (int i = 0; i < n; ++i) {
+      const double* p = pts + 4 * idx[i];
+      a += p[0]; b += p[1]; c += p[2]; d += p[3];
+    }
+    N.ms0 = a / n; N.ms1 = b / n; N.md0 = c / n; N.md1 = d / n;
+    double ads = 0, add = 0;
+    for (int i = 0; i < n; ++i) {
+      const double* p = pts + 4 * idx[i];
+      const double dx1 = N.ms0 - p[0], dy1 = N.ms1 - p[1], dx2 = N.md0 - p[2], dy2 = N.md1 - p[3];
+      ads += sqrt(dx1 * dx1 + dy1 * dy1);
+      add += sqrt(dx2 * dx2 + dy2 * dy2);
+    }
+    N.rs = M_SQRT2 / (ads / n);
+    N.rd = M_SQRT2 / (add / n);
+  }
+
+  // Normalised least squares over the n rows idx[] with unit weights by one
+  // thread (the local-optimisation trials run one per lane).
+  __device__ static bool fit_thread(const double* pts, const int* idx, int n, double* out) {
+    if (n < NONMIN) return false;
+    Norm N;
+    normalise(pts, idx, n, N);
+    double acc[NACC];
+#pragma unroll
+    for (int k = 0; k < NACC; ++k) acc[k] = 0;
+    for (int i = 0; i < n; ++i) accumulate(N, pts + 4 * idx[i], 1.0, acc);
+    return solve_normal(N, acc, out);
   }
 };
 

@@ -7,6 +7,11 @@
 
 #include "gcr_engine.cuh"
 
+// Resident CTAs per SM the kernel is compiled for (registers <= 64K / (256 * 2)).
+#ifndef GCR_MIN_BLOCKS
+#define GCR_MIN_BLOCKS 2
+#endif
+
 namespace gcr {
 
 __device__ inline double block_max_abs(double v, double* red) {
@@ -25,7 +30,7 @@ __device__ inline double block_max_abs(double v, double* red) {
 // Persistent kernel: each CTA takes pairs from a global ticket until none is
 // left; blockIdx.x selects the CTA's scratch slot.
 template <class Est>
-__global__ void __launch_bounds__(GCR_BLOCK, 1) pair_kernel(Workspace ws, EngineParams prm) {
+__global__ void __launch_bounds__(GCR_BLOCK, GCR_MIN_BLOCKS) pair_kernel(Workspace ws, EngineParams prm) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Shared<Est>& sh = *reinterpret_cast<Shared<Est>*>(smem_raw);
   __shared__ int s_pair;

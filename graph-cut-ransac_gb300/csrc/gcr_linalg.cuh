@@ -25,21 +25,31 @@ __host__ __device__ __forceinline__ void matmul3(const double* a, const double* 
 // a bubble pre-pass that swaps rows on the diagonal column entries, then
 // elimination without pivoting and back substitution.
 __device__ __forceinline__ void gauss_elimination8(double a[8][9], double x[8]) {
+  // every loop is unrolled so that the system stays in registers
+#pragma unroll
   for (int i = 0; i < 8; i++)
-    for (int k = i + 1; k < 8; k++)
-      if (fabs(a[i][i]) < fabs(a[k][i]))
-        for (int j = 0; j <= 8; j++) {
-          const double t = a[i][j];
-          a[i][j] = a[k][j];
-          a[k][j] = t;
-        }
+#pragma unroll
+    for (int k = i + 1; k < 8; k++) {
+      const bool sw = fabs(a[i][i]) < fabs(a[k][i]);
+#pragma unroll
+      for (int j = 0; j <= 8; j++) {
+        const double t = a[i][j], u = a[k][j];
+        a[i][j] = sw ? u : t;
+        a[k][j] = sw ? t : u;
+      }
+    }
+#pragma unroll
   for (int i = 0; i < 7; i++)
+#pragma unroll
     for (int k = i + 1; k < 8; k++) {
       const double t = a[k][i] / a[i][i];
+#pragma unroll
       for (int j = 0; j <= 8; j++) a[k][j] = a[k][j] - t * a[i][j];
     }
+#pragma unroll
   for (int i = 7; i >= 0; i--) {
     double s = a[i][8];
+#pragma unroll
     for (int j = i + 1; j < 8; j++) s = s - a[i][j] * x[j];
     x[i] = s / a[i][i];
   }
@@ -48,31 +58,40 @@ __device__ __forceinline__ void gauss_elimination8(double a[8][9], double x[8]) 
 // Solves the symmetric positive definite system A x = b in place (x holds b on
 // entry). Returns false when A is not numerically positive definite.
 template <int N>
-__device__ bool cholesky_solve(double A[N][N], double* x) {
+__device__ __forceinline__ bool cholesky_solve(double A[N][N], double* x) {
+  bool ok = true;
+#pragma unroll
   for (int j = 0; j < N; ++j) {
     double d = A[j][j];
+#pragma unroll
     for (int k = 0; k < j; ++k) d -= A[j][k] * A[j][k];
-    if (!(d > 0)) return false;
+    ok = ok && (d > 0);
     const double l = sqrt(d);
     A[j][j] = l;
     const double il = 1.0 / l;
+#pragma unroll
     for (int i = j + 1; i < N; ++i) {
       double s = A[i][j];
+#pragma unroll
       for (int k = 0; k < j; ++k) s -= A[i][k] * A[j][k];
       A[i][j] = s * il;
     }
   }
+#pragma unroll
   for (int i = 0; i < N; ++i) {
     double s = x[i];
+#pragma unroll
     for (int k = 0; k < i; ++k) s -= A[i][k] * x[k];
     x[i] = s / A[i][i];
   }
+#pragma unroll
   for (int i = N - 1; i >= 0; --i) {
     double s = x[i];
+#pragma unroll
     for (int k = i + 1; k < N; ++k) s -= A[k][i] * x[k];
     x[i] = s / A[i][i];
   }
-  return true;
+  return ok;
 }
 
 }  // namespace gcr

@@ -67,6 +67,7 @@ class Stats(ctypes.Structure):
         ("score", ctypes.c_double),
         ("status", ctypes.c_int32),
         ("flags", ctypes.c_int32),
+        ("models_scored", ctypes.c_int64),
     ]
 
 
@@ -74,11 +75,11 @@ class Stats(ctypes.Structure):
 STATS_DTYPE = np.dtype([
     ("iteration_number", np.int64), ("graph_cut_number", np.int64),
     ("local_optimization_number", np.int64), ("inlier_number", np.int64),
-    ("score", np.float64), ("status", np.int32), ("flags", np.int32),
+    ("score", np.float64), ("status", np.int32), ("flags", np.int32), ("models_scored", np.int64),
 ])
 SIZE_DTYPE = np.dtype([("h1", np.int32), ("w1", np.int32), ("h2", np.int32), ("w2", np.int32)])
 
-assert ctypes.sizeof(Stats) == STATS_DTYPE.itemsize == 48
+assert ctypes.sizeof(Stats) == STATS_DTYPE.itemsize == 56
 assert ctypes.sizeof(Params) == 80
 
 _P = ctypes.c_void_p

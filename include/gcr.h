@@ -87,6 +87,8 @@ typedef struct gcr_stats {
   double score;
   int32_t status;                  /* gcr_status of this pair */
   int32_t flags;                   /* GCR_FLAG_* */
+  int64_t models_scored;           /* models the sequential algorithm scores against all
+                                      correspondences (main loop + local optimisation) */
 } gcr_stats;
 
 enum {

@@ -86,6 +86,7 @@ static int run_generic(const Mat& run_pts, const Mat& pixel_pts, const Est& est,
     st->score = g.statistics.score;
     st->flags = (g.statistics.local_optimization_number ? GCR_FLAG_LO_APPLIED : 0) |
                 (g.statistics.irls_applied ? GCR_FLAG_IRLS_APPLIED : 0);
+    st->models_scored = (int64_t)g.models_scored;
   }
   if (!ok) return GCR_NO_MODEL;
   inliers = g.statistics.inliers;

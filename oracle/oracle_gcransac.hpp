@@ -165,6 +165,7 @@ struct GCRansac {
   Scoring scoring;
   double truncated_threshold = 0, squared_truncated_threshold = 0, log_probability = 0;
   const Grid* graph = nullptr;
+  size_t models_scored = 0;  // main-loop models + LO trials + IRLS fits
   Sampler* main_sampler = nullptr;
   Sampler* lo_sampler = nullptr;
 
@@ -234,6 +235,7 @@ struct GCRansac {
           break;
         for (Model& m : models) {
           tmp.clear();
+          ++models_scored;
           const Score s = scoring.get(pts, m, est, &tmp);
           if (max_score < s) {
             updated = true;
@@ -275,6 +277,7 @@ struct GCRansac {
       if (models.empty()) break;
       if (models.size() == 1) {
         tmp.clear();
+        ++models_scored;
         const Score s = scoring.get(pts, models[0], est, &tmp);
         if (tmp.size() < m) break;
         if (s.inlier_number <= inliers.size()) break;
@@ -284,6 +287,7 @@ struct GCRansac {
         bool updated = false;
         for (Model& mm : models) {
           tmp.clear();
+          ++models_scored;
           const Score s = scoring.get(pts, mm, est, &tmp);
           if (tmp.size() < m) continue;
           if (s.inlier_number <= inliers.size()) continue;
@@ -303,6 +307,7 @@ struct GCRansac {
   // Returns true when a model was found.
   bool run(const Mat& pts, const Est& est, Sampler* main_s, Sampler* lo_s, const Grid* g, Model& out) {
     statistics = Statistics();
+    models_scored = 0;
     main_sampler = main_s;
     lo_sampler = lo_s;
     graph = g;
@@ -335,6 +340,7 @@ struct GCRansac {
       }
       statistics.iteration_number += unsuccessful;
       for (Model& model : models) {
+        ++models_scored;
         current_score = scoring.get(pts, model, est, &cont[off]);
         bool updated_model = false;
         if (best_score < current_score &&

