@@ -248,10 +248,14 @@ gcr_status gcr_batch_run_device(gcr_context* c, gcr_model_kind kind, int64_t num
     d.n_div = (int32_t)params->neighborhood_size;
     if (d.n_div < 1) d.n_div = 1;
     const double nd = (double)d.n_div;
-    d.cell[0] = (z.w1 + eps) / nd;
-    d.cell[1] = (z.h1 + eps) / nd;
-    d.cell[2] = (z.w2 + eps) / nd;
-    d.cell[3] = (z.h2 + eps) / nd;
+    // the homography driver pads the image size by machine epsilon
+    // (gcransac_python.cpp:4290-4297), the fundamental/essential ones do not
+    // (1670-1677)
+    const double pad = kind == GCR_HOMOGRAPHY ? eps : 0.0;
+    d.cell[0] = (z.w1 + pad) / nd;
+    d.cell[1] = (z.h1 + pad) / nd;
+    d.cell[2] = (z.w2 + pad) / nd;
+    d.cell[3] = (z.h2 + pad) / nd;
     d.threshold = params->threshold;
     d.centre[0] = 0.5 * z.w1;
     d.centre[1] = 0.5 * z.h1;
@@ -286,6 +290,9 @@ gcr_status gcr_batch_run_device(gcr_context* c, gcr_model_kind kind, int64_t num
   gcr::EngineParams prm;
   prm.confidence = params->confidence;
   prm.lambda = params->spatial_coherence_weight;
+  // the fundamental/essential drivers build no neighbourhood for a weight at
+  // or below machine epsilon (gcransac_python.cpp:1658-1667)
+  if (kind != GCR_HOMOGRAPHY && prm.lambda <= eps) prm.lambda = 0.0;
   prm.max_iters = params->max_iterations;
   prm.min_iters = params->min_iterations;
   prm.lo_number = params->lo_number;

@@ -23,6 +23,8 @@
 #pragma once
 
 #include "gcr_device.cuh"
+#include "gcr_fundamental.cuh"
+#include "gcr_homography.cuh"
 #include "gcr_linalg.cuh"
 
 namespace gcr {
@@ -76,7 +78,8 @@ struct StatsOut {
 struct Slot {
   double* models64;     // [kModels][9]
   float* models32;      // [kModels][12]
-  int* samples;         // [GCR_BLOCK][kSampleCap]
+  int* samples;         // [GCR_BLOCK][SAMPLE_CAP] local-optimisation samples
+  int* bsamples;        // [GCR_BLOCK][M] minimal samples of the current batch
   int* list0;           // [max_n]
   int* list1;           // [max_n]
   int* list2;           // [max_n]
@@ -89,6 +92,7 @@ struct Slot {
   double* flow;         // [GCR_WARPS][kMaxFlowCap^2]
   double* node_d;       // [GCR_WARPS][3 * kMaxFlowCap]  excess, sink residual, scratch
   int* node_i;          // [GCR_WARPS][3 * kMaxFlowCap]  height, queue, mark
+  double* red;          // [GCR_WARPS * 64 + 64] reduction partials
 };
 
 struct Workspace {
@@ -137,6 +141,13 @@ struct Shared {
   float s_sum[GCR_BLOCK];
   float s_err[GCR_BLOCK];
   int lo_ok[GCR_BLOCK];
+  double lm_f[19];                // factorised F (U, V, sigma) of the CTA-wide LM
+  double lm_fn[19];
+  double lm_G[9];
+  double lm_D[63];
+  double lm_acc[35];
+  double degen_H[9];
+  int lm_flag;
   int fit_ok;
   int flow_status;
 };
@@ -642,21 +653,31 @@ struct Engine {
   }
 
   // ------------------------------------------------------------------
-  // CTA-wide normalised weighted least squares over the rows list[0..n).
-  // weight_mode 0: unit weights; 1: the iterated-least-squares weights of the
-  // reference, where packed row k gets weights[k] of the point INDEX k
-  // (GCRANSAC.h:657-675 with homography_estimator.h:161-165 and
-  // solver_homography_four_point.h:211-224): Tukey^2 of point k under
-  // sh.work_model when point k is in the set (slot.flag), else 0.
-  // Result in sh.fit_model; returns success (uniform).
-  __device__ bool fit_cta(const int* list, int n, int weight_mode) {
-    if (n < Est::NONMIN) return false;
+  // CTA-wide non-minimal fits over the rows list[0..n).
+  // Row weights (weight_mode): 0 unit; 1 the iterated-least-squares weights of
+  // the reference, where packed row k gets weights[k] of the point INDEX k
+  // (GCRANSAC.h:657-675 with the solvers reading weights_[i] for packed row i,
+  // e.g. solver_homography_four_point.h:211-224): Tukey^2 of point k under
+  // sh.work_model when point k is in the set (slot.flag), else 0; 2 explicit
+  // weights slot.dres[k]. Result in sh.fit_model; returns success (uniform).
+  __device__ __forceinline__ double row_weight(int k, int weight_mode, const double* wm) const {
+    if (weight_mode == 0) return 1.0;
+    if (weight_mode == 2) return slot.dres[k];
+    if (k < N && slot.flag[k]) {
+      const double r2 = Est::r2_f64(pts64 + 4 * k, wm);
+      const double wt = fmax(0.0, 1.0 - r2 / t2);
+      return wt * wt;
+    }
+    return 0.0;
+  }
+
+  // Hartley normalisation of the rows (normalizePoints semantics), CTA-wide.
+  __device__ void cta_norm(const int* list, int n, HomographyModel::Norm& nm) {
     double s[4] = {0, 0, 0, 0};
     for (int k = threadIdx.x; k < n; k += GCR_BLOCK) {
       const double* p = pts64 + 4 * list[k];
       s[0] += p[0]; s[1] += p[1]; s[2] += p[2]; s[3] += p[3];
     }
-    typename Est::Norm nm;
     nm.ms0 = block_sum(s[0], sh.red_d) / n;
     nm.ms1 = block_sum(s[1], sh.red_d) / n;
     nm.md0 = block_sum(s[2], sh.red_d) / n;
@@ -670,46 +691,178 @@ struct Engine {
     }
     nm.rs = M_SQRT2 / (block_sum(a, sh.red_d) / n);
     nm.rd = M_SQRT2 / (block_sum(b, sh.red_d) / n);
-    constexpr int NA = Est::NACC;
-    double acc[NA];
-#pragma unroll
-    for (int q = 0; q < NA; ++q) acc[q] = 0;
-    double wm[9];
-    if (weight_mode == 1) {
-#pragma unroll
-      for (int q = 0; q < 9; ++q) wm[q] = sh.work_model[q];
-    }
-    for (int k = threadIdx.x; k < n; k += GCR_BLOCK) {
-      double w = 1.0;
-      if (weight_mode == 1) {
-        w = 0.0;
-        if (k < N && slot.flag[k]) {
-          const double r2 = Est::r2_f64(pts64 + 4 * k, wm);
-          const double wt = fmax(0.0, 1.0 - r2 / t2);
-          w = wt * wt;
-        }
-      }
-      Est::accumulate(nm, pts64 + 4 * list[k], w, acc);
-    }
-    // deterministic reduction: warp trees, then warp partials in order
+  }
+
+  // Deterministic CTA reduction of NA per-thread partial sums into tot (thread 0).
+  template <int NA>
+  __device__ void cta_reduce(const double* acc, double* tot) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int q = 0; q < NA; ++q) {
       const double v = warp_sum(acc[q]);
-      if (lane == 0) sh.red_d[warp * 48 + q] = v;
+      if (lane == 0) slot.red[warp * 64 + q] = v;
     }
     sync();
-    if (threadIdx.x == 0) {
-      double tot[NA];
-      for (int q = 0; q < NA; ++q) {
-        double t = 0;
-        for (int w = 0; w < GCR_WARPS; ++w) t += sh.red_d[w * 48 + q];
-        tot[q] = t;
-      }
-      sh.fit_ok = Est::solve_normal(nm, tot, sh.fit_model) ? 1 : 0;
+    if (threadIdx.x < NA) {
+      double t = 0;
+      for (int w = 0; w < GCR_WARPS; ++w) t += slot.red[w * 64 + threadIdx.x];
+      tot[threadIdx.x] = t;
     }
+    sync();
+  }
+
+  // Homography least squares (normalised, 23-sum normal equations).
+  __device__ bool fit_cta_h(const int* list, int n, int weight_mode) {
+    using H = HomographyModel;
+    if (n < H::NONMIN) return false;
+    H::Norm nm;
+    cta_norm(list, n, nm);
+    double acc[H::NACC];
+#pragma unroll
+    for (int q = 0; q < H::NACC; ++q) acc[q] = 0;
+    double wm[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) wm[q] = sh.work_model[q];
+    for (int k = threadIdx.x; k < n; k += GCR_BLOCK) H::accumulate(nm, pts64 + 4 * list[k], row_weight(k, weight_mode, wm), acc);
+    cta_reduce<H::NACC>(acc, sh.lm_acc);
+    if (threadIdx.x == 0) sh.fit_ok = H::solve_normal(nm, sh.lm_acc, sh.fit_model) ? 1 : 0;
     sync();
     return sh.fit_ok != 0;
+  }
+
+  // Fundamental matrix: FundamentalMatrixBundleAdjustmentSolver on the rows
+  // (8-point start, 25 LM iterations on the factorised F), optionally inside
+  // the estimator's normalisation (estimateModelNonminimal) or on the raw rows
+  // (the driver's final bundle adjustment).
+  __device__ double fit_f_cost(const double* f19, int n, int weight_mode, const HomographyModel::Norm& nm,
+                               const double* wm) {
+    using F = FundamentalModel;
+    double G[9];
+    if (threadIdx.x == 0) {
+      F::FactF ff;
+      for (int q = 0; q < 9; ++q) { ff.U[q] = f19[q]; ff.V[q] = f19[9 + q]; }
+      ff.sigma = f19[18];
+      F::factf_F(ff, sh.lm_G);
+    }
+    sync();
+#pragma unroll
+    for (int q = 0; q < 9; ++q) G[q] = sh.lm_G[q];
+    double c = 0;
+    for (int k = threadIdx.x; k < n; k += GCR_BLOCK) {
+      const double* p = pts64 + 4 * slot_list_[k];
+      const double w = row_weight(k, weight_mode, wm);
+      const double l = F::lm_cost_point(G, (p[0] - nm.ms0) * nm.rs, (p[1] - nm.ms1) * nm.rs, (p[2] - nm.md0) * nm.rd,
+                                        (p[3] - nm.md1) * nm.rd);
+      c += weight_mode == 0 ? l : w * l;
+    }
+    return block_sum(c, sh.red_d);
+  }
+
+  const int* slot_list_ = nullptr;
+
+  __device__ bool fit_cta_f(const int* list, int n, int weight_mode, bool normalise) {
+    using F = FundamentalModel;
+    if (n < 8) return false;  // 7 rows never reach the non-minimal solver in the loop
+    slot_list_ = list;
+    HomographyModel::Norm nm;
+    if (normalise) cta_norm(list, n, nm);
+    else { nm.ms0 = nm.ms1 = nm.md0 = nm.md1 = 0.0; nm.rs = nm.rd = 1.0; }
+    double wm[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) wm[q] = sh.work_model[q];
+    {
+      double acc[F::NATA];
+#pragma unroll
+      for (int q = 0; q < F::NATA; ++q) acc[q] = 0;
+      for (int k = threadIdx.x; k < n; k += GCR_BLOCK)
+        F::accumulate_ata(nm, pts64 + 4 * list[k], row_weight(k, weight_mode, wm), acc);
+      cta_reduce<F::NATA>(acc, slot.red + GCR_WARPS * 64);
+    }
+    if (threadIdx.x == 0) {
+      double F0[9];
+      F::eight_point_from_ata(slot.red + GCR_WARPS * 64, F0);
+      F::FactF ff;
+      F::factf_from(F0, ff);
+      for (int q = 0; q < 9; ++q) { sh.lm_f[q] = ff.U[q]; sh.lm_f[9 + q] = ff.V[q]; }
+      sh.lm_f[18] = ff.sigma;
+    }
+    sync();
+    double lambda = 1e-3;
+    double cost = fit_f_cost(sh.lm_f, n, weight_mode, nm, wm);
+    bool recompute = true;
+    for (int iter = 0; iter < 25; ++iter) {
+      if (recompute) {
+        if (threadIdx.x == 0) {
+          F::FactF ff;
+          for (int q = 0; q < 9; ++q) { ff.U[q] = sh.lm_f[q]; ff.V[q] = sh.lm_f[9 + q]; }
+          ff.sigma = sh.lm_f[18];
+          F::factf_F(ff, sh.lm_G);
+          double D[9][7];
+          F::lm_dparams(ff, sh.lm_G, D);
+          for (int r = 0; r < 9; ++r)
+            for (int c = 0; c < 7; ++c) sh.lm_D[r * 7 + c] = D[r][c];
+        }
+        sync();
+        double G[9], D[9][7];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) G[q] = sh.lm_G[q];
+#pragma unroll
+        for (int r = 0; r < 9; ++r)
+#pragma unroll
+          for (int c = 0; c < 7; ++c) D[r][c] = sh.lm_D[r * 7 + c];
+        double acc[F::NLM];
+#pragma unroll
+        for (int q = 0; q < F::NLM; ++q) acc[q] = 0;
+        for (int k = threadIdx.x; k < n; k += GCR_BLOCK) {
+          const double* p = pts64 + 4 * list[k];
+          F::lm_accumulate_point(G, D, (p[0] - nm.ms0) * nm.rs, (p[1] - nm.ms1) * nm.rs, (p[2] - nm.md0) * nm.rd,
+                                 (p[3] - nm.md1) * nm.rd, row_weight(k, weight_mode, wm), n, acc);
+        }
+        cta_reduce<F::NLM>(acc, sh.lm_acc);
+        double gn = 0;
+        for (int a = 0; a < 7; ++a) gn += sh.lm_acc[28 + a] * sh.lm_acc[28 + a];
+        if (sqrt(gn) < 1e-8) break;
+      }
+      if (threadIdx.x == 0) {
+        F::FactF ff, fn;
+        for (int q = 0; q < 9; ++q) { ff.U[q] = sh.lm_f[q]; ff.V[q] = sh.lm_f[9 + q]; }
+        ff.sigma = sh.lm_f[18];
+        sh.lm_flag = F::lm_step(sh.lm_acc, lambda, ff, fn) ? 1 : 0;
+        for (int q = 0; q < 9; ++q) { sh.lm_fn[q] = fn.U[q]; sh.lm_fn[9 + q] = fn.V[q]; }
+        sh.lm_fn[18] = fn.sigma;
+      }
+      sync();
+      if (!sh.lm_flag) break;
+      const double cn = fit_f_cost(sh.lm_fn, n, weight_mode, nm, wm);
+      if (cn < cost) {
+        sync();
+        if (threadIdx.x < 19) sh.lm_f[threadIdx.x] = sh.lm_fn[threadIdx.x];
+        sync();
+        lambda /= 10;
+        cost = cn;
+        recompute = true;
+      } else {
+        lambda *= 10;
+        recompute = false;
+      }
+    }
+    if (threadIdx.x == 0) {
+      F::FactF ff;
+      for (int q = 0; q < 9; ++q) { ff.U[q] = sh.lm_f[q]; ff.V[q] = sh.lm_f[9 + q]; }
+      ff.sigma = sh.lm_f[18];
+      double Fn[9];
+      F::factf_F(ff, Fn);
+      if (normalise) F::denormalise(nm, Fn, sh.fit_model);
+      else
+        for (int q = 0; q < 9; ++q) sh.fit_model[q] = Fn[q];
+    }
+    sync();
+    return true;
+  }
+
+  __device__ bool fit_cta(const int* list, int n, int weight_mode) {
+    if constexpr (Est::KIND == 1) return fit_cta_f(list, n, weight_mode, true);
+    return fit_cta_h(list, n, weight_mode);
   }
 
   // ------------------------------------------------------------------
@@ -795,6 +948,40 @@ struct Engine {
         copy_model(sh.lo_best_model, slot.models64 + 9 * k);
       }
     }
+  }
+
+  // ------------------------------------------------------------------
+  // FundamentalMatrixEstimator::isValidModel (fundamental_estimator.h:287-338)
+  // on the model's inlier list: at least max(7, 0.5 |I|) inliers under the
+  // symmetric epipolar distance, then DEGENSAC (341-572). Returns validity;
+  // `updated` reports a model replaced by the DEGENSAC inner run.
+  __device__ bool valid_model_cta(const double* model, const int* sample, const int* list, int cnt, bool& updated) {
+    updated = false;
+    double F[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) F[q] = model[q];
+    const int min_n = max(Est::M, (int)((double)cnt * 0.5));
+    int c = 0;
+    for (int k = threadIdx.x; k < cnt; k += GCR_BLOCK)
+      if (FundamentalModel::symepi2_f64(pts64 + 4 * list[k], F) < t2) ++c;
+    c = block_sum(c, sh.red_i);
+    if (c < min_n) return false;
+    if (threadIdx.x == 0) sh.lm_flag = FundamentalModel::degenerate_sample(F, pts64, sample, sh.degen_H) ? 1 : 0;
+    sync();
+    if (!sh.lm_flag) return true;
+    // H-degenerate sample: the plane's inliers among the model's inliers
+    double H[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) H[q] = sh.degen_H[q];
+    int hc = 0;
+    for (int k = threadIdx.x; k < cnt; k += GCR_BLOCK)
+      if (HomographyModel::r2_f64(pts64 + 4 * list[k], H) < 4.0) ++hc;
+    hc = block_sum(hc, sh.red_i);
+    if (hc < HomographyModel::NONMIN) return false;
+    // The plane-and-parallax inner GC-RANSAC of the reference runs here; this
+    // build keeps the model unchanged and reports it in the statistics flags.
+    flags |= 4;
+    return true;
   }
 
   // ------------------------------------------------------------------
@@ -886,6 +1073,8 @@ struct Engine {
     double mloc[9 * Est::MAXSOL];
     int nm = 0;
     if (ok && Est::valid_sample(pts64, s)) nm = Est::minimal(pts64, s, mloc);
+#pragma unroll
+    for (int q = 0; q < Est::M; ++q) slot.bsamples[j * Est::M + q] = s[q];
     int total;
     const int base = block_exclusive_scan(nm, sh.red_i, &total);
     sh.n_ok[j] = nm;
@@ -952,10 +1141,18 @@ struct Engine {
           cont[off] = {mk, sh.mcount[k]};
           if (sh.mcount[k] == 0 || !maybe_better(k, best.value)) continue;
           t0 = tick();
-          const Score sc = exact_score(mk, nullptr, slot.models32 + 12 * k);
+          const Score sc = exact_score(mk, Est::CTA_VALIDITY ? slot.list1 : nullptr, slot.models32 + 12 * k);
           tock(3, t0);
           tock(9, 0, 1);
-          if (best.value < sc.value && Est::valid_model(mk)) {
+          bool updated = false;
+          bool valid = false;
+          if (best.value < sc.value) {
+            if constexpr (Est::CTA_VALIDITY)
+              valid = valid_model_cta(mk, slot.bsamples + j * Est::M, slot.list1, sc.count, updated);
+            else
+              valid = Est::valid_model(mk);
+          }
+          if (valid) {
             off ^= 1;
             copy_model(sh.best_model, mk);
             best = sc;
@@ -1055,7 +1252,37 @@ struct Engine {
     if (irls_applied) flags |= 2;
     if (lo_number > 0) flags |= 1;
     // output: model and the inliers of the final container
-    const int cnt = materialise(cont[off], list);
+    int cnt = materialise(cont[off], list);
+    double final_score = best.value;
+    if constexpr (Est::KIND == 1) {
+      // findFundamentalMatrix_ epilogue (gcransac_python.cpp:1833-1889):
+      // weighted bundle adjustment of the final inliers on the raw
+      // coordinates, kept when its MSAC score beats the run's score; at most 7
+      // inliers give the identity.
+      if (cnt > 7) {
+        double Fb[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) Fb[q] = sh.best_model[q];
+        for (int k = threadIdx.x; k < cnt; k += GCR_BLOCK)
+          slot.dres[k] = fmax(0.0, 1.0 - Est::r2_f64(pts64 + 4 * list[k], Fb) / t2);
+        sync();
+        if (fit_cta_f(list, cnt, 2, false)) {
+          const Score sc = exact_score(sh.fit_model, spare);
+          if (final_score < sc.value) {
+            final_score = sc.value;
+            copy_model(sh.best_model, sh.fit_model);
+            int* t = list;
+            list = spare;
+            spare = t;
+            cnt = sc.count;
+          }
+        }
+      } else {
+        sync();
+        if (threadIdx.x < 9) sh.best_model[threadIdx.x] = (threadIdx.x % 4 == 0) ? 1.0 : 0.0;
+        sync();
+      }
+    }
     for (int i = threadIdx.x; i < N; i += GCR_BLOCK) mask[i] = 0;
     sync();
     for (int k = threadIdx.x; k < cnt; k += GCR_BLOCK) mask[list[k]] = 1;
@@ -1065,7 +1292,7 @@ struct Engine {
       so->graph_cut_number = gc_number;
       so->local_optimization_number = lo_number;
       so->inlier_number = cnt;
-      so->score = best.value;
+      so->score = final_score;
       so->status = status;
       so->flags = flags;
       so->models_scored = models_scored;

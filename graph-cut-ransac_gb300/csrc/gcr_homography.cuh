@@ -13,6 +13,8 @@
 namespace gcr {
 
 struct HomographyModel {
+  static constexpr int KIND = 0;
+  static constexpr bool CTA_VALIDITY = false;
   static constexpr int M = 4;          // minimal sample size
   static constexpr int MAXSOL = 1;     // models per minimal sample
   static constexpr int NONMIN = 4;     // smallest non-minimal sample

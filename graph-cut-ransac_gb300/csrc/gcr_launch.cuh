@@ -74,6 +74,8 @@ size_t slot_bytes(int max_n, int sort_cap) {
   s += al(sizeof(double) * 9 * Shared<Est>::kModels);
   s += al(sizeof(float) * 12 * Shared<Est>::kModels);
   s += al(sizeof(int) * GCR_BLOCK * Est::SAMPLE_CAP);
+  s += al(sizeof(int) * GCR_BLOCK * Est::M);
+  s += al(sizeof(double) * (GCR_WARPS * 64 + 64));
   s += 3 * al(sizeof(int) * max_n);
   s += al((size_t)max_n);
   s += 2 * al(sizeof(double) * max_n);
@@ -95,6 +97,8 @@ Slot carve_slot(unsigned char* base, int max_n, int sort_cap) {
   s.models64 = (double*)take(sizeof(double) * 9 * Shared<Est>::kModels);
   s.models32 = (float*)take(sizeof(float) * 12 * Shared<Est>::kModels);
   s.samples = (int*)take(sizeof(int) * GCR_BLOCK * Est::SAMPLE_CAP);
+  s.bsamples = (int*)take(sizeof(int) * GCR_BLOCK * Est::M);
+  s.red = (double*)take(sizeof(double) * (GCR_WARPS * 64 + 64));
   s.list0 = (int*)take(sizeof(int) * max_n);
   s.list1 = (int*)take(sizeof(int) * max_n);
   s.list2 = (int*)take(sizeof(int) * max_n);

@@ -94,7 +94,9 @@ typedef struct gcr_stats {
 enum {
   GCR_FLAG_LO_APPLIED = 1,         /* at least one graph-cut local optimisation ran */
   GCR_FLAG_IRLS_APPLIED = 2,       /* the final iterated least-squares model was kept */
-  GCR_FLAG_DEGENSAC_SKIPPED = 4    /* an H-degenerate F sample took the plain path */
+  GCR_FLAG_DEGENSAC_SKIPPED = 4,   /* an H-degenerate F sample kept its model without the
+                                      plane-and-parallax inner run */
+  GCR_FLAG_DEGENSAC_RAN = 8        /* the plane-and-parallax inner run of DEGENSAC ran */
 };
 
 /* Fills *p with the defaults of the reference python entry point of `kind`

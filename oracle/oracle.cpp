@@ -116,6 +116,71 @@ static int find_homography(const double* corr, int64_t n, const gcr_image_size& 
   return rc;
 }
 
+// findFundamentalMatrix_ (gcransac_python.cpp:1600-1923): grid only when the
+// spatial weight is positive (cells w / n, 1658-1677), the default estimator
+// (0.5 validity ratio, DEGENSAC), GC-RANSAC, then a weighted bundle adjustment
+// of the final inliers kept when it raises the MSAC score (1833-1887); with at
+// most 7 inliers the model is the identity (1889).
+static int find_fundamental(const double* corr, int64_t n, const gcr_image_size& sz, const gcr_params& p,
+                            uint64_t seed, double* model_out, uint8_t* mask, gcr_stats* st) {
+  if (n < 7) return GCR_TOO_FEW_POINTS;
+  const Mat pts{corr, n, 4};
+  std::unique_ptr<Grid> grid;
+  if (p.spatial_coherence_weight > std::numeric_limits<double>::epsilon()) {
+    const size_t nd = (size_t)p.neighborhood_size;
+    const double cs[4] = {sz.w1 / (double)nd, sz.h1 / (double)nd, sz.w2 / (double)nd, sz.h2 / (double)nd};
+    grid = std::make_unique<Grid>(pts, cs, nd);
+  }
+  FundamentalEstimator est;
+  est.seed = seed;
+  Model model{};
+  std::vector<size_t> inl;
+  int rc;
+  if (p.scoring == GCR_SCORING_MAGSAC)
+    rc = run_generic<FundamentalEstimator, MAGSACScoring>(pts, pts, est, p, sz, seed, grid.get(), p.threshold,
+                                                          model, inl, st, p.threshold);
+  else
+    rc = run_generic<FundamentalEstimator, MSACScoring>(pts, pts, est, p, sz, seed, grid.get(), p.threshold, model,
+                                                        inl, st, p.threshold);
+  if (est.degensac_ran && st) st->flags |= 8;
+  if (rc == GCR_OK) {
+    if (inl.size() > 7) {
+      const double tt = 1.5 * p.threshold, sq = tt * tt;
+      std::vector<double> w(inl.size());
+      for (size_t k = 0; k < inl.size(); ++k)
+        w[k] = std::max(0.0, 1.0 - f_sampson2(pts.row(inl[k]), model) / sq);
+      // FundamentalMatrixBundleAdjustmentSolver on the raw inliers: 8-point
+      // start then LM; the weights are taken by inlier position for both steps
+      std::vector<const double*> rows(inl.size());
+      for (size_t k = 0; k < inl.size(); ++k) rows[k] = pts.row(inl[k]);
+      std::vector<Model> models;
+      f_eight_point(rows.data(), (int)rows.size(), w.data(), models);
+      for (Model& F : models) f_refine_lm(rows.data(), (int)rows.size(), w.data(), F);
+      MSACScoring<FundamentalEstimator> sc;
+      sc.initialize(sq, n);
+      double best = st ? st->score : 0.0;
+      for (Model& F : models) {
+        std::vector<size_t> cur;
+        const Score s = sc.get(pts, F, est, &cur);
+        if (best < s.value) {
+          model = F;
+          best = s.value;
+          inl.swap(cur);
+        }
+      }
+      if (st) st->score = best;
+    } else {
+      model = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    }
+  }
+  std::memset(mask, 0, (size_t)n);
+  for (size_t i : inl) mask[i] = 1;
+  if (st) st->inlier_number = (int64_t)inl.size();
+  if (rc == GCR_OK) std::memcpy(model_out, model.data(), 9 * sizeof(double));
+  else std::memset(model_out, 0, 9 * sizeof(double));
+  return rc;
+}
+
 }  // namespace oracle
 
 using namespace oracle;
@@ -225,7 +290,6 @@ int oracle_minimal(int kind, const double* corr, int64_t n, const int64_t* sampl
   } else if (kind == GCR_FUNDAMENTAL) {
     FundamentalEstimator e;
     s.assign(sample, sample + 7);
-    if (!e.is_valid_sample(pts, s.data())) return -1;
     e.estimate_minimal(pts, s.data(), models);
   } else {
     EssentialEstimator e;

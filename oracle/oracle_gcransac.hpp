@@ -229,7 +229,7 @@ struct GCRansac {
         if (ss < inliers.size()) {
           lo_sampler->sample(inliers, sample.data(), ss);
           if (!est.estimate_nonminimal(pts, sample.data(), ss, models, nullptr)) continue;
-        } else if (Est::sample_size() < inliers.size()) {
+        } else if (est.sample_size_rt() < inliers.size()) {
           if (!est.estimate_nonminimal(pts, inliers.data(), inliers.size(), models, nullptr)) break;
         } else
           break;
@@ -258,7 +258,7 @@ struct GCRansac {
   }
 
   bool irls(const Mat& pts, const Est& est, std::vector<size_t>& inliers, Model& model) {
-    const size_t m = Est::sample_size();
+    const size_t m = est.sample_size_rt();
     if (inliers.size() <= m) return false;
     size_t iterations = 0;
     std::vector<size_t> tmp;
@@ -312,7 +312,7 @@ struct GCRansac {
     lo_sampler = lo_s;
     graph = g;
     statistics.neighbor_number = g ? g->neighbor_number : 0;
-    const size_t m = Est::sample_size();
+    const size_t m = est.sample_size_rt();
     log_probability = std::log(1.0 - settings.confidence);
     size_t max_iteration = iteration_number_for(1, pts.rows, m, log_probability);
     std::vector<size_t> sample(m);
