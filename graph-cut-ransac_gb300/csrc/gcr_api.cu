@@ -91,9 +91,9 @@ gcr_status check_params(gcr_model_kind kind, const gcr_params* p) {
   if (p->max_iterations < 0 || p->min_iterations < 0) return fail(GCR_INVALID_ARG, "negative iteration limit");
   if (p->lo_number < 0 || p->lo_number > GCR_BLOCK)
     return fail(GCR_UNSUPPORTED, "lo_number must be in [0, %d]", GCR_BLOCK);
-  if (p->sampler != GCR_SAMPLER_UNIFORM && p->sampler != GCR_SAMPLER_PROSAC)
-    return fail(GCR_UNSUPPORTED, "sampler %d is not provided by the device engine (0 uniform, 1 PROSAC)",
-                p->sampler);
+  if (p->sampler != GCR_SAMPLER_UNIFORM && p->sampler != GCR_SAMPLER_PROSAC && p->sampler != GCR_SAMPLER_PNAPSAC)
+    return fail(GCR_UNSUPPORTED,
+                "sampler %d is not provided by the device engine (0 uniform, 1 PROSAC, 2 P-NAPSAC)", p->sampler);
   if (p->scoring != GCR_SCORING_MSAC) return fail(GCR_UNSUPPORTED, "scoring %d is not provided", p->scoring);
   const bool pairwise = p->spatial_coherence_weight > 0;
   if (p->neighborhood != GCR_NEIGHBORHOOD_GRID && pairwise)

@@ -37,7 +37,7 @@ constexpr int kLoRegion = GCR_BLOCK;    // model slots reserved for local optimi
 
 enum PairStatus { ST_OK = 0, ST_NO_MODEL = 3, ST_TIMEOUT = 5, ST_CAPACITY = 6, ST_UNSUPPORTED = 7 };
 
-enum { SAMPLER_UNIFORM = 0, SAMPLER_PROSAC = 1 };
+enum { SAMPLER_UNIFORM = 0, SAMPLER_PROSAC = 1, SAMPLER_PNAPSAC = 2 };
 
 struct EngineParams {
   double confidence;
@@ -93,6 +93,8 @@ struct Slot {
   double* node_d;       // [GCR_WARPS][3 * kMaxFlowCap]  excess, sink residual, scratch
   int* node_i;          // [GCR_WARPS][3 * kMaxFlowCap]  height, queue, mark
   double* red;          // [GCR_WARPS * 64 + 64] reduction partials
+  int* napsac;          // [16][max_n] P-NAPSAC layers (sorted points, cell start, cell size per point)
+                        // x4, hits, subset sizes, layers, growth table
 };
 
 struct Workspace {
@@ -370,10 +372,13 @@ struct Engine {
   // ------------------------------------------------------------------
   // Grid neighbourhood: points sorted by (cell key, index); cell_start holds
   // the cell boundaries. Returns the number of cells.
-  __device__ int build_grid() {
+  // Points sorted by (cell key, index) for a grid of the given cell sizes and
+  // radix (GridNeighborhoodGraph<4>::initialize, grid_neighborhood_graph.h:230-292:
+  // idx_d = floor(coord_d / cell_d), key = sum_d idx_d * nd^d). Writes the
+  // sorted point list and the cell boundaries; returns the number of cells.
+  __device__ int sort_cells(const double* cell, uint64_t nd, int* sorted, int* starts) {
     unsigned long long* a = slot.sortbuf;
     const double* pix = ws.pix64 + 4 * pd.offset;
-    const uint64_t nd = (uint64_t)pd.n_div;
     int sort_n = 1;
     while (sort_n < N) sort_n <<= 1;
     for (int i = threadIdx.x; i < sort_n; i += GCR_BLOCK) {
@@ -381,7 +386,7 @@ struct Engine {
         const double* p = pix + 4 * i;
         uint64_t key = 0, o = 1;
         for (int d = 0; d < 4; ++d) {
-          const uint64_t idx = (uint64_t)(int64_t)floor(p[d] / pd.cell[d]);
+          const uint64_t idx = (uint64_t)(int64_t)floor(p[d] / cell[d]);
           key += o * idx;
           o *= nd;
         }
@@ -397,17 +402,199 @@ struct Engine {
       const int i = base + threadIdx.x;
       int f = 0;
       if (i < N) {
-        slot.cell_pts[i] = (int)(a[i] & 0xFFFFFFull);
+        sorted[i] = (int)(a[i] & 0xFFFFFFull);
         f = (i == 0) || ((a[i] >> 24) != (a[i - 1] >> 24));
       }
       int tot;
       const int pos = block_exclusive_scan(f, sh.red_i, &tot);
-      if (f) slot.cell_start[ncells + pos] = i;
+      if (f) starts[ncells + pos] = i;
       ncells += tot;
     }
-    if (threadIdx.x == 0) slot.cell_start[ncells] = N;
+    if (threadIdx.x == 0) starts[ncells] = N;
     sync();
     return ncells;
+  }
+
+  __device__ int build_grid() { return sort_cells(pd.cell, (uint64_t)pd.n_div, slot.cell_pts, slot.cell_start); }
+
+  // ------------------------------------------------------------------
+  // ProgressiveNapsacSampler<4> (samplers/progressive_napsac_sampler.h:50-326)
+  // with the driver's layers {16, 8, 4, 2} and length 0.5 N
+  // (gcransac_python.cpp:4333-4343). Its state evolves call by call (hit
+  // counters of the points), so thread 0 draws a batch sequentially.
+  struct Napsac {
+    long long kth = 0, max_iters = 0;
+    long long local_calls = 0, global_calls = 0;
+    // lazily extended P-NAPSAC growth table
+    int growth_n = 0;
+    double T_n = 0;
+    unsigned int T_prime = 1;
+    // global PROSAC (sample size m, convergence N)
+    long long g_kth = 1, g_subset = 0, g_hi = 0, g_growth = 1;
+    double g_Tn = 0;
+  };
+  Napsac ns;
+
+  __device__ int* nl_sorted(int l) const { return slot.napsac + (size_t)(3 * l) * N; }
+  __device__ int* nl_start(int l) const { return slot.napsac + (size_t)(3 * l + 1) * N; }
+  __device__ int* nl_size(int l) const { return slot.napsac + (size_t)(3 * l + 2) * N; }
+  __device__ int* n_hits() const { return slot.napsac + (size_t)12 * N; }
+  __device__ int* n_subset() const { return slot.napsac + (size_t)13 * N; }
+  __device__ int* n_layer() const { return slot.napsac + (size_t)14 * N; }
+  __device__ unsigned int* n_growth() const { return (unsigned int*)(slot.napsac + (size_t)15 * N); }
+
+  __device__ void napsac_setup() {
+    const int divs[4] = {16, 8, 4, 2};
+    for (int l = 0; l < 4; ++l) {
+      double cs[4];
+      for (int d = 0; d < 4; ++d) cs[d] = 2.0 * pd.centre[d] / (double)divs[l];
+      const int nc = sort_cells(cs, (uint64_t)divs[l], nl_sorted(l), slot.cell_start);
+      // per point: start and size of its cell in the sorted list
+      for (int c = threadIdx.x; c < nc; c += GCR_BLOCK) {
+        const int s0 = slot.cell_start[c], s1 = slot.cell_start[c + 1];
+        for (int i = s0; i < s1; ++i) {
+          const int p = nl_sorted(l)[i];
+          nl_start(l)[p] = s0;
+          nl_size(l)[p] = s1 - s0;
+        }
+      }
+      sync();
+    }
+    for (int i = threadIdx.x; i < N; i += GCR_BLOCK) {
+      n_hits()[i] = 0;
+      n_subset()[i] = m;
+      n_layer()[i] = 0;
+    }
+    ns.kth = 0;
+    ns.max_iters = (long long)(0.5 * (double)N);
+    ns.local_calls = ns.global_calls = 0;
+    // P-NAPSAC growth function: local sample size m - 1
+    const int ls = m - 1;
+    double T = (double)ns.max_iters;
+    for (int i = 0; i < ls; ++i) T *= (double)(ls - i) / (double)(N - i);
+    ns.T_n = T;
+    ns.T_prime = 1;
+    ns.growth_n = 0;
+    // global PROSAC
+    ns.g_kth = 1;
+    ns.g_subset = m;
+    ns.g_hi = m - 1;
+    ns.g_growth = 1;
+    double Tg = (double)N;
+    for (int i = 0; i < m; ++i) Tg *= (double)(m - i) / (double)(N - i);
+    ns.g_Tn = Tg;
+    sync();
+  }
+
+  // growth_function_progressive_napsac[i], extended on demand (thread 0)
+  __device__ unsigned int napsac_growth(int i) {
+    const int ls = m - 1;
+    unsigned int* g = n_growth();
+    while (ns.growth_n <= i) {
+      const int k = ns.growth_n;
+      if (k + 1 <= ls) {
+        g[k] = ns.T_prime;
+      } else {
+        const double Tn1 = (double)(k + 1) * ns.T_n / (double)(k + 1 - ls);
+        g[k] = ns.T_prime + (unsigned int)(size_t)ceil(Tn1 - ns.T_n);
+        ns.T_n = Tn1;
+        ns.T_prime = g[k];
+      }
+      ++ns.growth_n;
+    }
+    return g[i];
+  }
+
+  // global ProsacSampler(sample size m, convergence N): setSampleNumber(k)
+  // then sample (prosac_sampler.h:177-236); thread 0
+  __device__ bool napsac_global(long long k, int* s) {
+    // growth[subset - 1] of this sampler is tracked in g_growth
+    auto grow = [&]() {
+      const long long before = ns.g_subset;
+      ++ns.g_subset;
+      if (ns.g_subset > N) ns.g_subset = N;
+      ns.g_hi = ns.g_subset - 2;
+      if (ns.g_subset != before) {
+        const long long i = ns.g_subset - 1;
+        if (i + 1 > m) {
+          const double Tn1 = (double)(i + 1) * ns.g_Tn / (double)(i + 1 - m);
+          ns.g_growth = ns.g_growth + (long long)(unsigned int)ceil(Tn1 - ns.g_Tn);
+          ns.g_Tn = Tn1;
+        }
+      }
+    };
+    ns.g_kth = k;
+    bool global = false;
+    if (ns.g_kth > N) {
+      global = true;
+    } else {
+      while (ns.g_kth > ns.g_growth && ns.g_subset != N) grow();
+    }
+    DrawStream ds(pd.seed, STREAM_NAPSAC_GLOBAL, (uint64_t)(ns.global_calls++));
+    bool ok;
+    if (global) {
+      ok = unique_set(ds, s, m, 0, (uint32_t)(N - 1));
+    } else {
+      ok = unique_set(ds, s, m - 1, 0, (uint32_t)ns.g_hi);
+      s[m - 1] = (int)(ns.g_subset - 1);
+      // incrementIterationNumber
+      ++ns.g_kth;
+      if (!(ns.g_kth > N) && ns.g_kth > ns.g_growth) grow();
+    }
+    return ok;
+  }
+
+  // One P-NAPSAC call (thread 0). Returns false when the sampler fails.
+  __device__ bool napsac_call(int* s) {
+    ++ns.kth;
+    if (ns.kth > ns.max_iters) return napsac_global(ns.kth, s);
+    // one-point PROSAC of sample size 1 and convergence N: the k-th call
+    // returns point k - 1 (its range is empty until convergence)
+    const int initial = (int)(ns.kth - 1);
+    int* hits = n_hits();
+    const int h = ++hits[initial];
+    int ss = n_subset()[initial];
+    while ((unsigned int)h > napsac_growth(ss - 1) && ss < N) ss = min(ss + 1, N);
+    n_subset()[initial] = ss;
+    int layer = n_layer()[initial];
+    bool last = false;
+    for (;;) {
+      if (layer >= 4) {
+        last = true;
+        break;
+      }
+      if (nl_size(layer)[initial] < ss) {
+        ++layer;
+        continue;
+      }
+      break;
+    }
+    n_layer()[initial] = layer;
+    if (last) {
+      const bool ok = napsac_global(ns.kth, s);
+      s[m - 1] = initial;
+      return ok;
+    }
+    const int* nb = nl_sorted(layer) + nl_start(layer)[initial];
+    s[m - 1] = initial;
+    s[m - 2] = nb[ss - 1];
+    // generateUniqueRandomSet(subset, m - 2, ss - 2, initial): the local
+    // index is compared with the point index `initial`, as in the reference
+    DrawStream ds(pd.seed, STREAM_NAPSAC_LOCAL, (uint64_t)(ns.local_calls++));
+    const uint32_t hi = (uint32_t)(ss - 2);
+    for (int i = 0; i < m - 2; ++i) {
+      s[i] = (int)ds.next_in(0, hi);
+      if (s[i] == initial) { --i; continue; }
+      for (int j = i - 1; j >= 0; --j)
+        if (s[i] == s[j]) { --i; break; }
+      if (ds.d > (1u << 20)) return false;
+    }
+    for (int i = 0; i < m - 2; ++i) {
+      s[i] = nb[s[i]];
+      ++hits[s[i]];
+    }
+    ++hits[s[m - 2]];
+    return true;
   }
 
   // ------------------------------------------------------------------
@@ -627,6 +814,10 @@ struct Engine {
     const bool pairwise = prm.lambda > 0;
     for (int c = warp; c < ncells; c += GCR_WARPS) {
       const int c0 = slot.cell_start[c], n = slot.cell_start[c + 1] - c0;
+      if (c0 < 0 || n < 1 || c0 + n > N) {  // inconsistent cell table: skip, report
+        if (lane == 0) atomicMax(&sh.flow_status, ST_CAPACITY);
+        continue;
+      }
       if (n == 1 || !pairwise) {
         for (int k = lane; k < n; k += 32) {
           const int p = slot.cell_pts[c0 + k];
@@ -1026,7 +1217,20 @@ struct Engine {
     const int j = threadIdx.x;
     int s[Est::M];
     bool ok = false;
-    if (prm.sampler == SAMPLER_UNIFORM) {
+    if (prm.sampler == SAMPLER_PNAPSAC) {
+      if (threadIdx.x == 0)
+        for (int c = 0; c < GCR_BLOCK; ++c) {
+          int t[Est::M];
+          const bool o = napsac_call(t);
+          for (int q = 0; q < Est::M; ++q) slot.bsamples[c * Est::M + q] = t[q];
+          sh.s_cnt[c] = o ? 1 : 0;
+        }
+      sync();
+      ok = sh.s_cnt[j] != 0;
+#pragma unroll
+      for (int q = 0; q < Est::M; ++q) s[q] = slot.bsamples[j * Est::M + q];
+      sync();
+    } else if (prm.sampler == SAMPLER_UNIFORM) {
       DrawStream ds(pd.seed, STREAM_MAIN, (uint64_t)(a0 + j));
       ok = unique_set(ds, s, m, 0, (uint32_t)(N - 1));
     } else {
@@ -1092,6 +1296,9 @@ struct Engine {
   // ------------------------------------------------------------------
   __device__ void run() {
     long long t0 = tick();
+    // the sampler's layer grids use cell_start as scratch, so they come
+    // before the neighbourhood grid that keeps it
+    if (prm.sampler == SAMPLER_PNAPSAC) napsac_setup();
     const int ncells = build_grid();
     tock(0, t0);
     max_iter = iteration_number_for(1, N, m, log_prob);

@@ -70,3 +70,9 @@ def test_fundamental_drop_in_defaults(gcr):
     F, mask = gcr.findFundamentalMatrix(pr["corr"], 480, 640, 480, 640, threshold=0.75, seed=1)
     assert F is not None
     assert S.fundamental_error(F, pr) < 0.5
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_fundamental_pnapsac(oracle, gcr, seed):
+    pr = S.two_view_pair(20 + seed, n=1500, inlier_ratio=0.4)
+    compare(oracle, gcr, pr, f_params(sampler=2), seed)

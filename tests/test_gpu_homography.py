@@ -89,3 +89,8 @@ def test_drop_in_entry_point(oracle, gcr):
                                   h_params(spatial_coherence_weight=0.975), seed=9)
     assert H is not None and np.array_equal(mask, m_o)
     assert S.homography_error(H, pr["H_gt"]) < 1.0
+
+
+def test_homography_pnapsac(oracle, gcr):
+    pr = S.homography_pair(23)
+    compare(oracle, gcr, pr["corr"], pr["size"], h_params(sampler=2), 6)
