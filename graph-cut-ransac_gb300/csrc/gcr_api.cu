@@ -224,13 +224,17 @@ gcr_status gcr_batch_run_device(gcr_context* c, gcr_model_kind kind, int64_t num
     const int want_cnt = std::max(grid, c->slot_kind == (int)kind ? c->slot_count : 0);
     const int want_sort = pow2_at_least(want_n);
     const size_t per = ops->slot_bytes(want_n, want_sort);
+    const size_t per_nested = ops->nested_slot_bytes ? ops->nested_slot_bytes(want_n) : 0;
     CUDA_TRY(cudaStreamSynchronize(s));
-    CUDA_TRY(c->slot_mem.ensure(per * (size_t)want_cnt));
-    CUDA_TRY(c->slots_meta.ensure(sizeof(gcr::Slot) * want_cnt));
-    std::vector<gcr::Slot> meta(want_cnt);
-    for (int i = 0; i < want_cnt; ++i)
-      ops->carve((unsigned char*)c->slot_mem.p + per * (size_t)i, want_n, want_sort, &meta[i]);
-    CUDA_TRY(cudaMemcpy(c->slots_meta.p, meta.data(), sizeof(gcr::Slot) * want_cnt, cudaMemcpyHostToDevice));
+    CUDA_TRY(c->slot_mem.ensure((per + per_nested) * (size_t)want_cnt));
+    CUDA_TRY(c->slots_meta.ensure(sizeof(gcr::Slot) * 2 * want_cnt));
+    std::vector<gcr::Slot> meta(2 * (size_t)want_cnt);
+    for (int i = 0; i < want_cnt; ++i) {
+      unsigned char* b = (unsigned char*)c->slot_mem.p + (per + per_nested) * (size_t)i;
+      ops->carve(b, want_n, want_sort, &meta[i]);
+      if (ops->carve_nested) ops->carve_nested(b + per, want_n, &meta[want_cnt + i]);
+    }
+    CUDA_TRY(cudaMemcpy(c->slots_meta.p, meta.data(), sizeof(gcr::Slot) * 2 * want_cnt, cudaMemcpyHostToDevice));
     c->slot_kind = (int)kind;
     c->slot_max_n = want_n;
     c->slot_count = want_cnt;
@@ -275,6 +279,7 @@ gcr_status gcr_batch_run_device(gcr_context* c, gcr_model_kind kind, int64_t num
   ws.pts32 = (float4*)c->pts32.p;
   ws.pairs = (const gcr::PairDesc*)c->pairs.p;
   ws.slots = (gcr::Slot*)c->slots_meta.p;
+  ws.nested_slots = (gcr::Slot*)c->slots_meta.p + c->slot_count;
   ws.ticket = (int*)c->ticket.p;
   ws.models_out = d_models_out;
   ws.masks_out = d_masks_out;
@@ -300,6 +305,10 @@ gcr_status gcr_batch_run_device(gcr_context* c, gcr_model_kind kind, int64_t num
   prm.scoring = params->scoring;
   prm.num_pairs = (int32_t)num_pairs;
   prm.max_n = max_n;
+  prm.nested = 0;
+  prm.stream_main = 1;  // STREAM_MAIN
+  prm.stream_lo = 2;    // STREAM_LO
+  prm.pp_h = nullptr;
   CUDA_TRY(ops->launch(grid, s, ws, prm));
   g_last_launches = 1;
   return GCR_OK;

@@ -49,6 +49,13 @@ struct EngineParams {
   int32_t scoring;
   int32_t num_pairs;
   int32_t max_n;
+  // nested runs (DEGENSAC's plane-and-parallax GC-RANSAC): one sampler stream
+  // shared by the main loop and the local optimisation, results kept in
+  // shared memory instead of the outputs
+  int32_t nested;
+  uint32_t stream_main;
+  uint32_t stream_lo;
+  const double* pp_h;   // homography of the plane-and-parallax solver (nested runs)
 };
 
 // Per-pair inputs prepared on the device.
@@ -103,6 +110,7 @@ struct Workspace {
   float4* pts32;        // [total] centred FP32 copy of pts64 (pairs too large for shared memory)
   const PairDesc* pairs;
   Slot* slots;
+  Slot* nested_slots;   // light slots of DEGENSAC's inner run (fundamental matrices)
   int* ticket;
   double* models_out;   // [P][9]
   uint8_t* masks_out;   // [total]
@@ -125,7 +133,6 @@ struct Container {
 template <class Est>
 struct Shared {
   static constexpr int kModels = GCR_BLOCK * Est::MAXSOL + kLoRegion;
-  float4 pts[kSmemPoints];
   double best_model[9];
   double cont_model[2][9];
   double lo_best_model[9];
@@ -149,6 +156,9 @@ struct Shared {
   double lm_D[63];
   double lm_acc[35];
   double degen_H[9];
+  double pp_H[9];                 // homography of the plane-and-parallax solver
+  double result_model[9];         // model of a nested run
+  int result_count;               // inlier count of a nested run
   int lm_flag;
   int fit_ok;
   int flow_status;
@@ -189,6 +199,9 @@ struct Engine {
   // sequential state (identical in every thread)
   long long iter = 0, max_iter = 0, gc_number = 0, lo_number = 0, lo_calls = 0;
   long long models_scored = 0;  // models the sequential algorithm scores in full
+  long long degensac_calls = 0;  // DEGENSAC inner runs so far (their sampler streams)
+  Shared<PlaneParallaxModel>* nsh = nullptr;  // state of DEGENSAC's inner run
+  Slot nslot{};
   Score best{0, 0.0};
   Container cont[2];
   int off = 0;
@@ -812,7 +825,11 @@ struct Engine {
     if (threadIdx.x == 0) sh.flow_status = 0;
     sync();
     const bool pairwise = prm.lambda > 0;
-    for (int c = warp; c < ncells; c += GCR_WARPS) {
+    if (!pairwise) {
+      // unary terms only: SINK iff the sink capacity is positive
+      for (int i = threadIdx.x; i < N; i += GCR_BLOCK) slot.flag[i] = (uint8_t)(slot.tr[i] < -kResidualEps ? 1 : 0);
+    }
+    for (int c = warp; pairwise && c < ncells; c += GCR_WARPS) {
       const int c0 = slot.cell_start[c], n = slot.cell_start[c + 1] - c0;
       if (c0 < 0 || n < 1 || c0 + n > N) {  // inconsistent cell table: skip, report
         if (lane == 0) atomicMax(&sh.flow_status, ST_CAPACITY);
@@ -951,7 +968,7 @@ struct Engine {
 
   const int* slot_list_ = nullptr;
 
-  __device__ bool fit_cta_f(const int* list, int n, int weight_mode, bool normalise) {
+  __device__ bool fit_cta_f(const int* list, int n, int weight_mode, bool normalise, bool lm = true) {
     using F = FundamentalModel;
     if (n < 8) return false;  // 7 rows never reach the non-minimal solver in the loop
     slot_list_ = list;
@@ -978,6 +995,16 @@ struct Engine {
       sh.lm_f[18] = ff.sigma;
     }
     sync();
+    if (!lm) {
+      // plain normalised 8-point solver (the inner DEGENSAC estimator)
+      if (threadIdx.x == 0) {
+        double F0[9];
+        F::eight_point_from_ata(slot.red + GCR_WARPS * 64, F0);
+        F::denormalise(nm, F0, sh.fit_model);
+      }
+      sync();
+      return true;
+    }
     double lambda = 1e-3;
     double cost = fit_f_cost(sh.lm_f, n, weight_mode, nm, wm);
     bool recompute = true;
@@ -1053,6 +1080,7 @@ struct Engine {
 
   __device__ bool fit_cta(const int* list, int n, int weight_mode) {
     if constexpr (Est::KIND == 1) return fit_cta_f(list, n, weight_mode, true);
+    if constexpr (Est::KIND == 2) return fit_cta_f(list, n, weight_mode, true, false);
     return fit_cta_h(list, n, weight_mode);
   }
 
@@ -1079,7 +1107,7 @@ struct Engine {
         if (threadIdx.x < trials) {
           long long c0 = tick();
           int* smp = slot.samples + threadIdx.x * Est::SAMPLE_CAP;
-          DrawStream ds(pd.seed, STREAM_LO, (uint64_t)(lo_calls + threadIdx.x));
+          DrawStream ds(pd.seed, prm.stream_lo, (uint64_t)(lo_calls + threadIdx.x));
           bool ok = unique_set(ds, smp, ss, 0, (uint32_t)(nL - 1));
           tock(12, c0);
           c0 = tick();
@@ -1151,12 +1179,14 @@ struct Engine {
     double F[9];
 #pragma unroll
     for (int q = 0; q < 9; ++q) F[q] = model[q];
-    const int min_n = max(Est::M, (int)((double)cnt * 0.5));
+    const double ratio = Est::KIND == 1 ? 0.5 : 0.0;
+    const int min_n = max(Est::M, (int)((double)cnt * ratio));
     int c = 0;
     for (int k = threadIdx.x; k < cnt; k += GCR_BLOCK)
       if (FundamentalModel::symepi2_f64(pts64 + 4 * list[k], F) < t2) ++c;
     c = block_sum(c, sh.red_i);
     if (c < min_n) return false;
+    if constexpr (Est::KIND != 1) return true;
     if (threadIdx.x == 0) sh.lm_flag = FundamentalModel::degenerate_sample(F, pts64, sample, sh.degen_H) ? 1 : 0;
     sync();
     if (!sh.lm_flag) return true;
@@ -1164,14 +1194,51 @@ struct Engine {
     double H[9];
 #pragma unroll
     for (int q = 0; q < 9; ++q) H[q] = sh.degen_H[q];
-    int hc = 0;
-    for (int k = threadIdx.x; k < cnt; k += GCR_BLOCK)
-      if (HomographyModel::r2_f64(pts64 + 4 * list[k], H) < 4.0) ++hc;
-    hc = block_sum(hc, sh.red_i);
-    if (hc < HomographyModel::NONMIN) return false;
-    // The plane-and-parallax inner GC-RANSAC of the reference runs here; this
-    // build keeps the model unchanged and reports it in the statistics flags.
-    flags |= 4;
+    int total = 0;
+    for (int base = 0; base < cnt; base += GCR_BLOCK) {
+      const int k = base + threadIdx.x;
+      const int f = (k < cnt && HomographyModel::r2_f64(pts64 + 4 * list[k], H) < 4.0) ? 1 : 0;
+      int tot;
+      const int pos = block_exclusive_scan(f, sh.red_i, &tot);
+      if (f) slot.list2[total + pos] = list[k];
+      total += tot;
+    }
+    if (total < HomographyModel::NONMIN) return false;
+    // plane homography from its inliers, then the plane-and-parallax GC-RANSAC
+    if (!fit_cta_h(slot.list2, total, 0)) return false;
+    if constexpr (Est::KIND == 1) {
+      if (nsh == nullptr) {
+        flags |= 4;
+        return true;
+      }
+      flags |= 8;
+      Shared<PlaneParallaxModel>& ish = *nsh;
+      sync();
+      if (threadIdx.x < 9) ish.pp_H[threadIdx.x] = sh.fit_model[threadIdx.x];
+      sync();
+      EngineParams p2 = prm;
+      p2.confidence = 0.99;
+      p2.lambda = 0.0;
+      p2.max_iters = 1LL << 40;
+      p2.min_iters = 20;
+      p2.lo_number = 10;
+      p2.sampler = SAMPLER_UNIFORM;
+      p2.nested = 1;
+      p2.stream_main = p2.stream_lo = 16u + (uint32_t)(degensac_calls++);
+      p2.pp_h = ish.pp_H;
+      PairDesc pd2 = pd;
+      pd2.threshold = 1.5 * pd.threshold;  // the run's truncated threshold
+      Engine<PlaneParallaxModel> inner(ish, ws, p2, pd2, nslot, pair);
+      inner.pts32 = pts32;
+      inner.scale = scale;
+      inner.run();
+      if (ish.result_count > cnt) {
+        updated = true;
+        sync();
+        if (threadIdx.x < 9) sh.degen_H[threadIdx.x] = ish.result_model[threadIdx.x];
+        sync();
+      }
+    }
     return true;
   }
 
@@ -1231,7 +1298,7 @@ struct Engine {
       for (int q = 0; q < Est::M; ++q) s[q] = slot.bsamples[j * Est::M + q];
       sync();
     } else if (prm.sampler == SAMPLER_UNIFORM) {
-      DrawStream ds(pd.seed, STREAM_MAIN, (uint64_t)(a0 + j));
+      DrawStream ds(pd.seed, prm.stream_main, (uint64_t)(a0 + j));
       ok = unique_set(ds, s, m, 0, (uint32_t)(N - 1));
     } else {
       // PROSAC (samplers/prosac_sampler.h:51-237): every thread replays the
@@ -1266,7 +1333,7 @@ struct Engine {
           }
         }
       }
-      DrawStream ds(pd.seed, STREAM_MAIN, (uint64_t)(a0 + j));
+      DrawStream ds(pd.seed, prm.stream_main, (uint64_t)(a0 + j));
       if (my_global) {
         ok = unique_set(ds, s, m, 0, (uint32_t)(N - 1));
       } else {
@@ -1276,7 +1343,7 @@ struct Engine {
     }
     double mloc[9 * Est::MAXSOL];
     int nm = 0;
-    if (ok && Est::valid_sample(pts64, s)) nm = Est::minimal(pts64, s, mloc);
+    if (ok && Est::valid_sample(pts64, s)) nm = Est::minimal(pts64, s, mloc, prm.pp_h);
 #pragma unroll
     for (int q = 0; q < Est::M; ++q) slot.bsamples[j * Est::M + q] = s[q];
     int total;
@@ -1299,7 +1366,7 @@ struct Engine {
     // the sampler's layer grids use cell_start as scratch, so they come
     // before the neighbourhood grid that keeps it
     if (prm.sampler == SAMPLER_PNAPSAC) napsac_setup();
-    const int ncells = build_grid();
+    const int ncells = prm.nested ? 0 : build_grid();
     tock(0, t0);
     max_iter = iteration_number_for(1, N, m, log_prob);
     const long long max_iters = prm.max_iters, min_iters = prm.min_iters;
@@ -1319,11 +1386,14 @@ struct Engine {
       const int K = sh.mbase[GCR_BLOCK - 1] + sh.n_ok[GCR_BLOCK - 1];
       score_models_f32(0, K);
       tock(2, t0);
+      bool restart = false;
+      long long next_attempt = attempt + GCR_BLOCK;
       for (int j = 0; j < GCR_BLOCK; ++j) {
         if (!in_iter) {
           const long long lim = max_iter < max_iters ? max_iter : max_iters;
           if (!(min_iters > iter || iter < lim)) {
             done = true;
+            if (prm.nested) lo_calls = attempt + j;  // one stream: the next call follows
             break;
           }
           ++iter;
@@ -1360,22 +1430,39 @@ struct Engine {
               valid = Est::valid_model(mk);
           }
           if (valid) {
+            Score scb = sc;
+            const double* mb = mk;
+            if (updated) {
+              // DEGENSAC replaced the model: rescore it into the container
+              copy_model(sh.cont_model[off], sh.degen_H);
+              scb = exact_score(sh.cont_model[off], nullptr);
+              cont[off] = {sh.cont_model[off], scb.count};
+              mb = sh.cont_model[off];
+            }
             off ^= 1;
-            copy_model(sh.best_model, mk);
-            best = sc;
+            copy_model(sh.best_model, mb);
+            best = scb;
             do_lo = iter > 20 && best.count > m;
             max_iter = iteration_number_for(best.count, N, m, log_prob);
           }
         }
         if (do_lo) {
           ++lo_number;
+          if (prm.nested) lo_calls = attempt + j + 1;  // one stream: LO draws follow this attempt
           t0 = tick();
           local_optimization(ncells);
           tock(11, t0);
           max_iter = iteration_number_for(best.count, N, m, log_prob);
+          if (prm.nested) {
+            // later attempts of this batch used call indices the LO consumed
+            next_attempt = lo_calls;
+            restart = true;
+            break;
+          }
         }
       }
-      attempt += GCR_BLOCK;
+      attempt = next_attempt;
+      (void)restart;
       // containers that point into the batch table are copied out before reuse
       for (int c = 0; c < 2; ++c) {
         if (cont[c].model != nullptr && cont[c].model >= slot.models64 &&
@@ -1397,6 +1484,11 @@ struct Engine {
   __device__ void finish(int ncells) {
     StatsOut* so = ws.stats_out + pair;
     uint8_t* mask = ws.masks_out + pd.offset;
+    if (prm.nested && best.count <= m) {
+      if (threadIdx.x == 0) sh.result_count = 0;
+      sync();
+      return;
+    }
     if (best.count <= m) {
       for (int i = threadIdx.x; i < N; i += GCR_BLOCK) mask[i] = 0;
       if (threadIdx.x < 9) ws.models_out[9 * pair + threadIdx.x] = 0.0;
@@ -1489,6 +1581,13 @@ struct Engine {
         if (threadIdx.x < 9) sh.best_model[threadIdx.x] = (threadIdx.x % 4 == 0) ? 1.0 : 0.0;
         sync();
       }
+    }
+    if (prm.nested) {
+      sync();
+      if (threadIdx.x < 9) sh.result_model[threadIdx.x] = sh.best_model[threadIdx.x];
+      if (threadIdx.x == 0) sh.result_count = cnt;
+      sync();
+      return;
     }
     for (int i = threadIdx.x; i < N; i += GCR_BLOCK) mask[i] = 0;
     sync();

@@ -198,7 +198,7 @@ struct FundamentalModel {
     return nm;
   }
 
-  __device__ static int minimal(const double* pts, const int* s, double* out) {
+  __device__ static int minimal(const double* pts, const int* s, double* out, const double* = nullptr) {
     const double* rows[7];
     for (int i = 0; i < 7; ++i) rows[i] = pts + 4 * s[i];
     double tmp[27];
@@ -581,6 +581,71 @@ struct FundamentalModel {
     double Fn[9];
     factf_F(f, Fn);
     denormalise(N, Fn, out);
+    return true;
+  }
+};
+
+// The estimator of DEGENSAC's inner run: FundamentalMatrixEstimator with the
+// plane-and-parallax minimal solver (2 points and a fixed homography,
+// solver_fundamental_matrix_plane_and_parallax.h:102-165), the 8-point
+// non-minimal solver, validity ratio 0 and no DEGENSAC
+// (fundamental_estimator.h:519-553).
+struct PlaneParallaxModel {
+  static constexpr int KIND = 2;
+  static constexpr int M = 2;
+  static constexpr int MAXSOL = 1;
+  static constexpr int NONMIN = 8;
+  static constexpr int INLIER_LIMIT = 7 * M;
+  static constexpr int SAMPLE_CAP = INLIER_LIMIT;
+  static constexpr bool CTA_VALIDITY = true;
+  using Norm = HomographyModel::Norm;
+
+  __device__ static bool valid_sample(const double*, const int*) { return true; }
+
+  __device__ static int minimal(const double* pts, const int* s, double* out, const double* H) {
+    const double* p1 = pts + 4 * s[0];
+    const double* p2 = pts + 4 * s[1];
+    double q1[3], q2[3];
+    for (int i = 0; i < 3; ++i) {
+      q1[i] = H[i * 3] * p1[0] + H[i * 3 + 1] * p1[1] + H[i * 3 + 2];
+      q2[i] = H[i * 3] * p2[0] + H[i * 3 + 1] * p2[1] + H[i * 3 + 2];
+    }
+    const double d1[3] = {p1[2], p1[3], 1}, d2[3] = {p2[2], p2[3], 1};
+    double l1[3], l2[3], e[3];
+    dcross3(q1, d1, l1);
+    dcross3(q2, d2, l2);
+    dcross3(l1, l2, e);
+    if (fabs(e[2]) < 2.220446049250313e-16) return 0;
+    const double ex[9] = {0, -e[2], e[1], e[2], 0, -e[0], -e[1], e[0], 0};
+    double F[9];
+    matmul3(ex, H, F);
+    if (!FundamentalModel::orientation_valid(F, pts, s, 2)) return 0;
+    for (int i = 0; i < 9; ++i) out[i] = F[i];
+    return 1;
+  }
+
+  __device__ __forceinline__ static double r2_f64(const double* p, const double* F) {
+    return FundamentalModel::r2_f64(p, F);
+  }
+  __device__ __forceinline__ static float r2_f32(const float4 p, const float* F, float& it) {
+    return FundamentalModel::r2_f32(p, F, it);
+  }
+  __device__ static void prepare_f32(const double* F, const double* c, double S, float* out) {
+    FundamentalModel::prepare_f32(F, c, S, out);
+  }
+
+  // normalised 8-point fit, unit weights, one thread
+  __device__ static bool fit_thread(const double* pts, const int* idx, int n, double* out) {
+    if (n < NONMIN) return false;
+    Norm N;
+    HomographyModel::normalise(pts, idx, n, N);
+    double ata[FundamentalModel::NATA];
+#pragma unroll
+    for (int k = 0; k < FundamentalModel::NATA; ++k) ata[k] = 0;
+    for (int i = 0; i < n; ++i) FundamentalModel::accumulate_ata(N, pts + 4 * idx[i], 1.0, ata);
+    double F[9];
+    FundamentalModel::eight_point_from_ata(ata, F);
+    FundamentalModel::denormalise(N, F, out);
     return true;
   }
 };

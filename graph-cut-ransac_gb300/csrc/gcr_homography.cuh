@@ -70,7 +70,7 @@ struct HomographyModel {
     return true;
   }
 
-  __device__ static int minimal(const double* pts, const int* s, double* out) {
+  __device__ static int minimal(const double* pts, const int* s, double* out, const double* = nullptr) {
     const double* rows[4] = {pts + 4 * s[0], pts + 4 * s[1], pts + 4 * s[2], pts + 4 * s[3]};
     return solve_four(rows, nullptr, out) ? 1 : 0;
   }

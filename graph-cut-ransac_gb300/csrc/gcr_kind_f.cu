@@ -11,6 +11,8 @@ using Est = FundamentalModel;
 size_t f_shared() { return shared_bytes<Est>(); }
 size_t f_slot(int n, int s) { return slot_bytes<Est>(n, s); }
 void f_carve(unsigned char* b, int n, int s, Slot* o) { *o = carve_slot<Est>(b, n, s); }
+size_t f_nested_slot(int n) { return slot_bytes<PlaneParallaxModel>(n, 1, true); }
+void f_carve_nested(unsigned char* b, int n, Slot* o) { *o = carve_slot<PlaneParallaxModel>(b, n, 1, true); }
 cudaError_t f_prepare() {
   return cudaFuncSetAttribute(pair_kernel<Est>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shared_bytes<Est>());
 }
@@ -22,7 +24,7 @@ cudaError_t f_launch(int grid, cudaStream_t st, const Workspace& ws, const Engin
   return cudaGetLastError();
 }
 
-const KindOps kOps = {Est::M, f_shared, f_slot, f_carve, f_prepare, f_occupancy, f_launch};
+const KindOps kOps = {Est::M, f_shared, f_slot, f_carve, f_nested_slot, f_carve_nested, f_prepare, f_occupancy, f_launch};
 
 }  // namespace
 

@@ -22,7 +22,7 @@ cudaError_t h_launch(int grid, cudaStream_t st, const Workspace& ws, const Engin
   return cudaGetLastError();
 }
 
-const KindOps kOps = {Est::M, h_shared, h_slot, h_carve, h_prepare, h_occupancy, h_launch};
+const KindOps kOps = {Est::M, h_shared, h_slot, h_carve, nullptr, nullptr, h_prepare, h_occupancy, h_launch};
 
 }  // namespace
 

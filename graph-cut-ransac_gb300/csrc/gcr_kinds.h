@@ -18,6 +18,8 @@ struct KindOps {
   size_t (*shared_bytes)();
   size_t (*slot_bytes)(int max_n, int sort_cap);
   void (*carve)(unsigned char* base, int max_n, int sort_cap, Slot* out);
+  size_t (*nested_slot_bytes)(int max_n);                        // nullptr: no inner runs
+  void (*carve_nested)(unsigned char* base, int max_n, Slot* out);
   cudaError_t (*prepare)();  // one-time kernel attribute setup
   cudaError_t (*occupancy)(int* blocks_per_sm);
   cudaError_t (*launch)(int grid, cudaStream_t stream, const Workspace& ws, const EngineParams& prm);

@@ -29,10 +29,28 @@ __device__ inline double block_max_abs(double v, double* red) {
 
 // Persistent kernel: each CTA takes pairs from a global ticket until none is
 // left; blockIdx.x selects the CTA's scratch slot.
+// Dynamic shared memory: the FP32 correspondence tile, the engine state and,
+// for fundamental matrices, the state of DEGENSAC's inner run.
+constexpr size_t kTileBytes = sizeof(float4) * kSmemPoints;
+__host__ __device__ constexpr size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+template <class Est>
+__host__ __device__ constexpr size_t nested_bytes() {
+  return Est::KIND == 1 ? align256(sizeof(Shared<PlaneParallaxModel>)) : 0;
+}
+
+template <class Est>
+__host__ __device__ constexpr size_t shared_total() {
+  return kTileBytes + align256(sizeof(Shared<Est>)) + nested_bytes<Est>();
+}
+
+// Persistent kernel: each CTA takes pairs from a global ticket until none is
+// left; blockIdx.x selects the CTA's scratch slot.
 template <class Est>
 __global__ void __launch_bounds__(GCR_BLOCK, GCR_MIN_BLOCKS) pair_kernel(Workspace ws, EngineParams prm) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  Shared<Est>& sh = *reinterpret_cast<Shared<Est>*>(smem_raw);
+  float4* tile = reinterpret_cast<float4*>(smem_raw);
+  Shared<Est>& sh = *reinterpret_cast<Shared<Est>*>(smem_raw + kTileBytes);
   __shared__ int s_pair;
   const Slot slot = ws.slots[blockIdx.x];
   for (;;) {
@@ -43,10 +61,14 @@ __global__ void __launch_bounds__(GCR_BLOCK, GCR_MIN_BLOCKS) pair_kernel(Workspa
     if (pair >= prm.num_pairs) break;
     const PairDesc pd = ws.pairs[pair];
     Engine<Est> eng(sh, ws, prm, pd, slot, pair);
+    if constexpr (Est::KIND == 1) {
+      eng.nsh = reinterpret_cast<Shared<PlaneParallaxModel>*>(smem_raw + kTileBytes + align256(sizeof(Shared<Est>)));
+      eng.nslot = ws.nested_slots[blockIdx.x];
+    }
     // centred FP32 copy of the correspondences: shared memory when it fits
     const double* p64 = ws.pts64 + 4 * pd.offset;
     const bool in_smem = pd.n <= kSmemPoints;
-    float4* dst = in_smem ? sh.pts : ws.pts32 + pd.offset;
+    float4* dst = in_smem ? tile : ws.pts32 + pd.offset;
     double mx = 0.0;
     for (int i = threadIdx.x; i < pd.n; i += GCR_BLOCK) {
       const double a = p64[4 * i] - pd.centre[0], b = p64[4 * i + 1] - pd.centre[1];
@@ -63,12 +85,13 @@ __global__ void __launch_bounds__(GCR_BLOCK, GCR_MIN_BLOCKS) pair_kernel(Workspa
 
 template <class Est>
 size_t shared_bytes() {
-  return sizeof(Shared<Est>);
+  return shared_total<Est>();
 }
 
 // Scratch bytes of one slot for pairs of at most max_n correspondences.
+// Light slots (DEGENSAC's inner run) have no graph-cut or sampler-grid scratch.
 template <class Est>
-size_t slot_bytes(int max_n, int sort_cap) {
+size_t slot_bytes(int max_n, int sort_cap, bool light = false) {
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   size_t s = 0;
   s += al(sizeof(double) * 9 * Shared<Est>::kModels);
@@ -76,23 +99,25 @@ size_t slot_bytes(int max_n, int sort_cap) {
   s += al(sizeof(int) * GCR_BLOCK * Est::SAMPLE_CAP);
   s += al(sizeof(int) * GCR_BLOCK * Est::M);
   s += al(sizeof(double) * (GCR_WARPS * 64 + 64));
-  s += al(sizeof(int) * 16 * (size_t)max_n);
   s += 3 * al(sizeof(int) * max_n);
   s += al((size_t)max_n);
   s += 2 * al(sizeof(double) * max_n);
-  s += al(sizeof(unsigned long long) * sort_cap);
-  s += al(sizeof(int) * max_n);
-  s += al(sizeof(int) * (max_n + 1));
-  s += al(sizeof(double) * GCR_WARPS * kMaxFlowCap * kMaxFlowCap);
-  s += al(sizeof(double) * GCR_WARPS * 3 * kMaxFlowCap);
-  s += al(sizeof(int) * GCR_WARPS * 3 * kMaxFlowCap);
+  if (!light) {
+    s += al(sizeof(int) * 16 * (size_t)max_n);
+    s += al(sizeof(unsigned long long) * sort_cap);
+    s += al(sizeof(int) * max_n);
+    s += al(sizeof(int) * (max_n + 1));
+    s += al(sizeof(double) * GCR_WARPS * kMaxFlowCap * kMaxFlowCap);
+    s += al(sizeof(double) * GCR_WARPS * 3 * kMaxFlowCap);
+    s += al(sizeof(int) * GCR_WARPS * 3 * kMaxFlowCap);
+  }
   return s;
 }
 
 template <class Est>
-Slot carve_slot(unsigned char* base, int max_n, int sort_cap) {
+Slot carve_slot(unsigned char* base, int max_n, int sort_cap, bool light = false) {
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-  Slot s;
+  Slot s{};
   unsigned char* p = base;
   auto take = [&](size_t b) { unsigned char* r = p; p += al(b); return r; };
   s.models64 = (double*)take(sizeof(double) * 9 * Shared<Est>::kModels);
@@ -100,19 +125,21 @@ Slot carve_slot(unsigned char* base, int max_n, int sort_cap) {
   s.samples = (int*)take(sizeof(int) * GCR_BLOCK * Est::SAMPLE_CAP);
   s.bsamples = (int*)take(sizeof(int) * GCR_BLOCK * Est::M);
   s.red = (double*)take(sizeof(double) * (GCR_WARPS * 64 + 64));
-  s.napsac = (int*)take(sizeof(int) * 16 * (size_t)max_n);
   s.list0 = (int*)take(sizeof(int) * max_n);
   s.list1 = (int*)take(sizeof(int) * max_n);
   s.list2 = (int*)take(sizeof(int) * max_n);
   s.flag = (uint8_t*)take((size_t)max_n);
   s.dres = (double*)take(sizeof(double) * max_n);
   s.tr = (double*)take(sizeof(double) * max_n);
-  s.sortbuf = (unsigned long long*)take(sizeof(unsigned long long) * sort_cap);
-  s.cell_pts = (int*)take(sizeof(int) * max_n);
-  s.cell_start = (int*)take(sizeof(int) * (max_n + 1));
-  s.flow = (double*)take(sizeof(double) * GCR_WARPS * kMaxFlowCap * kMaxFlowCap);
-  s.node_d = (double*)take(sizeof(double) * GCR_WARPS * 3 * kMaxFlowCap);
-  s.node_i = (int*)take(sizeof(int) * GCR_WARPS * 3 * kMaxFlowCap);
+  if (!light) {
+    s.napsac = (int*)take(sizeof(int) * 16 * (size_t)max_n);
+    s.sortbuf = (unsigned long long*)take(sizeof(unsigned long long) * sort_cap);
+    s.cell_pts = (int*)take(sizeof(int) * max_n);
+    s.cell_start = (int*)take(sizeof(int) * (max_n + 1));
+    s.flow = (double*)take(sizeof(double) * GCR_WARPS * kMaxFlowCap * kMaxFlowCap);
+    s.node_d = (double*)take(sizeof(double) * GCR_WARPS * 3 * kMaxFlowCap);
+    s.node_i = (int*)take(sizeof(int) * GCR_WARPS * 3 * kMaxFlowCap);
+  }
   return s;
 }
 

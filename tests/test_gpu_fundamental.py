@@ -30,11 +30,7 @@ def compare(oracle, gcr, pr, p, seed):
     rc_o, F_o, m_o, st_o = oracle.find(_abi.GCR_FUNDAMENTAL, pr["corr"], oracle.make_size(*pr["size"]), p,
                                        seed=seed)
     models, masks, stats = gcr.find_batch(_abi.GCR_FUNDAMENTAL, [pr["corr"]], [pr["size"]], p, seeds=[seed])
-    if st_o.flags & 8:
-        # the oracle ran DEGENSAC's plane-and-parallax inner run; the device
-        # engine must at least have detected the same degenerate sample
-        assert stats["flags"][0] & 4
-        pytest.skip("DEGENSAC inner run is not executed by the device engine")
+    assert (stats["flags"][0] & 8) == (st_o.flags & 8), "DEGENSAC inner runs differ"
     assert stats["status"][0] == rc_o
     assert np.array_equal(masks[0], m_o), f"mask differs at {np.nonzero(masks[0] != m_o)[0][:10]}"
     if rc_o == 0:
