@@ -39,6 +39,12 @@ WORKLOADS = {
     # confidence 0.99, uniform sampler, 4^4 grid, lambda 0.975, 50 LO trials
     "homography": dict(kind=_abi.GCR_HOMOGRAPHY, n=2000, ratio=0.4, threshold=3.0, sampler=0, grid=4,
                        lam=0.975, pairs=1216),
+    # 5000 correspondences of a two-view scene (depth 2-10 m, f = 800 px,
+    # rotation up to 30 deg, unit baseline), 25 % inliers (sigma 0.5 px),
+    # threshold 0.75 px, P-NAPSAC sampler, 8^4 grid, lambda 0.975, 7-point
+    # solver + graph-cut LO, DEGENSAC on
+    "fundamental": dict(kind=_abi.GCR_FUNDAMENTAL, n=5000, ratio=0.25, threshold=0.75, sampler=2, grid=8,
+                        lam=0.975, pairs=608),
 }
 
 
@@ -49,6 +55,9 @@ def build_pairs(workload, pairs, seed0):
         if workload == "homography":
             pr = S.homography_pair(seed0 + i, n=w["n"], inlier_ratio=w["ratio"])
             gts.append(pr["H_gt"])
+        else:
+            pr = S.two_view_pair(seed0 + i, n=w["n"], inlier_ratio=w["ratio"])
+            gts.append(pr)
         corr.append(pr["corr"])
         sizes.append(pr["size"])
     offsets = np.zeros(pairs + 1, np.int64)
@@ -69,9 +78,13 @@ def size_array(sizes):
     return z
 
 
-def model_errors(workload, models, gts):
+def model_errors(workload, models, gts, limit=64):
+    """Median-ready model errors against ground truth on the first `limit` pairs
+    (H: RMS transfer px; F: mean Sampson px of clean correspondences)."""
     if workload == "homography":
         return [S.homography_error(m / m[2, 2] if abs(m[2, 2]) > 1e-12 else m, g) for m, g in zip(models, gts)]
+    if workload == "fundamental":
+        return [S.fundamental_error(m, g, n=200) for m, g in list(zip(models, gts))[:limit]]
     return []
 
 
@@ -175,7 +188,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gcr", choices=["gcr", "reference"])
-    ap.add_argument("--workload", default="homography", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="fundamental", choices=sorted(WORKLOADS))
     ap.add_argument("--pairs", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

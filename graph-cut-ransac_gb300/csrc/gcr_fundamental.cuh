@@ -34,50 +34,91 @@ __device__ __forceinline__ long long dabs_bits(double x) { return __double_as_lo
 // basis Eigen's FullPivLU::kernel() returns (free pivoted columns set to 1).
 // Returns the kernel dimension (the solver needs 2).
 __device__ inline int lu_kernel_7x9(double A[7][9], double f1[9], double f2[9]) {
+  // Every index is a compile-time constant after unrolling (row and column
+  // swaps are selects), so the 7x9 system stays in registers.
   int cp[9];
 #pragma unroll
   for (int j = 0; j < 9; ++j) cp[j] = j;
   long long maxpivot = 0;
   int nonzero = 7;
+  bool stopped = false;
+#pragma unroll
   for (int k = 0; k < 7; ++k) {
     int bi = k, bj = k;
     long long best = -1;
+#pragma unroll
     for (int i = k; i < 7; ++i)
+#pragma unroll
       for (int j = k; j < 9; ++j) {
         const long long v = dabs_bits(A[i][j]);
         if (v > best) { best = v; bi = i; bj = j; }
       }
-    if (best == 0) { nonzero = k; break; }
-    if (best > maxpivot) maxpivot = best;
-    if (bi != k)
-      for (int j = 0; j < 9; ++j) { const double t = A[k][j]; A[k][j] = A[bi][j]; A[bi][j] = t; }
-    if (bj != k) {
-      for (int i = 0; i < 7; ++i) { const double t = A[i][k]; A[i][k] = A[i][bj]; A[i][bj] = t; }
-      const int t = cp[k]; cp[k] = cp[bj]; cp[bj] = t;
+    if (!stopped && best == 0) {
+      nonzero = k;
+      stopped = true;
     }
-    const double inv = 1.0 / A[k][k];
-    for (int i = k + 1; i < 7; ++i) {
-      const double f = A[i][k] * inv;
-      A[i][k] = f;
-      for (int j = k + 1; j < 9; ++j) A[i][j] -= f * A[k][j];
+    if (!stopped) {
+      if (best > maxpivot) maxpivot = best;
+#pragma unroll
+      for (int i = k + 1; i < 7; ++i) {
+        const bool s = (i == bi);
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+          const double t = A[k][j], u = A[i][j];
+          A[k][j] = s ? u : t;
+          A[i][j] = s ? t : u;
+        }
+      }
+#pragma unroll
+      for (int j = k + 1; j < 9; ++j) {
+        const bool s = (j == bj);
+#pragma unroll
+        for (int i = 0; i < 7; ++i) {
+          const double t = A[i][k], u = A[i][j];
+          A[i][k] = s ? u : t;
+          A[i][j] = s ? t : u;
+        }
+        const int t = cp[k], u = cp[j];
+        cp[k] = s ? u : t;
+        cp[j] = s ? t : u;
+      }
+      const double inv = 1.0 / A[k][k];
+#pragma unroll
+      for (int i = k + 1; i < 7; ++i) {
+        const double f = A[i][k] * inv;
+        A[i][k] = f;
+#pragma unroll
+        for (int j = k + 1; j < 9; ++j) A[i][j] -= f * A[k][j];
+      }
     }
   }
   const double thr = 2.220446049250313e-16 * 7.0 * __longlong_as_double(maxpivot);
   int rank = 0;
-  for (int i = 0; i < nonzero; ++i)
-    if (fabs(A[i][i]) > thr) ++rank;
+#pragma unroll
+  for (int i = 0; i < 7; ++i)
+    if (i < nonzero && fabs(A[i][i]) > thr) ++rank;
   if (rank != 7) return 9 - rank;
-  double* out[2] = {f1, f2};
+#pragma unroll
   for (int j = 0; j < 2; ++j) {
     double x[7];
+#pragma unroll
     for (int i = 6; i >= 0; --i) {
       double s = -A[i][7 + j];
+#pragma unroll
       for (int q = i + 1; q < 7; ++q) s -= A[i][q] * x[q];
       x[i] = s / A[i][i];
     }
-    for (int i = 0; i < 9; ++i) out[j][i] = 0.0;
-    for (int i = 0; i < 7; ++i) out[j][cp[i]] = x[i];
-    out[j][cp[7 + j]] = 1.0;
+    double* o = j == 0 ? f1 : f2;
+    // o[cp[i]] = x[i] (i < 7), o[cp[7 + j]] = 1, others 0: selects over the
+    // static output index
+#pragma unroll
+    for (int t = 0; t < 9; ++t) {
+      double v = 0.0;
+#pragma unroll
+      for (int i = 0; i < 7; ++i) v = (cp[i] == t) ? x[i] : v;
+      v = (cp[7 + j] == t) ? 1.0 : v;
+      o[t] = v;
+    }
   }
   return 2;
 }
