@@ -70,6 +70,10 @@ const gcr::KindOps* ops_for(gcr_model_kind kind) {
 
 }  // namespace
 
+namespace gcr {
+void set_last_error(const char* msg) { g_last_error = msg; }
+}  // namespace gcr
+
 struct gcr_context {
   int device = 0;
   int num_sms = 0;

@@ -93,6 +93,8 @@ _EXPORTS = {
     "gcr_context_destroy": (ctypes.c_int, [_P]),
     "gcr_batch_run_device": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int64, _P, _P, _P, _P, _P, _P, _P,
                                             _P, _P, _P]),
+    "gcr_find_homography_device_noalloc": (ctypes.c_int, [_P, ctypes.c_int64, _P, _P, ctypes.c_uint64, _P, _P, _P,
+                                                          _P]),
     "gcr_last_launch_count": (ctypes.c_int64, []),
     "gcr_last_error_string": (ctypes.c_char_p, []),
 }

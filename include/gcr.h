@@ -156,6 +156,30 @@ gcr_status gcr_batch_run_device(gcr_context* ctx, gcr_model_kind kind, int64_t n
                                 const uint64_t* h_seeds, double* d_models_out,
                                 uint8_t* d_masks_out, gcr_stats* d_stats_out, void* stream);
 
+/* Allocation-free homography search on one image pair (no counterpart in the
+ * reference, whose C++ and Python entry points allocate on the host as they
+ * go). For callers that must not allocate device memory while they run: a
+ * process whose device memory is reserved up front by another allocator, or
+ * a real-time loop where the device-wide synchronisation of cudaMalloc and
+ * cudaFree would stall other streams. All scratch lives in one fixed 5 MiB
+ * array per device compiled into the library; the call makes no cudaMalloc,
+ * cudaFree or other allocating call and queues one kernel on `stream`.
+ *   d_corr        n x 4 row-major doubles on the current device, n <= 4096
+ *                 (larger n returns GCR_CAPACITY: use gcr_batch_run_device)
+ *   size, params  host structs, as for gcr_find_homography
+ *   seed          the pair's sampler seed
+ *   d_model_out9, d_mask_out (n bytes), d_stats_out: device pointers, fully
+ *                 written by the kernel; nothing needs to be cleared first
+ * The first call on a device does a one-time set-up with that device current;
+ * make it before any stream capture begins. Calls on the same device share
+ * the scratch: calls that overlap in time (two host threads, or two streams
+ * that run concurrently) race, so queue them on one stream or serialise them.
+ * Returns when the kernel is queued; the per-pair outcome is d_stats_out->status. */
+gcr_status gcr_find_homography_device_noalloc(const double* d_corr, int64_t n,
+                                              const gcr_image_size* size, const gcr_params* params,
+                                              uint64_t seed, double* d_model_out9, uint8_t* d_mask_out,
+                                              gcr_stats* d_stats_out, void* stream);
+
 /* Number of kernels the last gcr_batch_run_device / gcr_find_* call launched. */
 int64_t gcr_last_launch_count(void);
 
