@@ -37,7 +37,6 @@ constexpr double kResidualEps = 1e-12;  // residual capacity treated as saturate
 #endif
 constexpr int kSmemPoints = GCR_TILE_POINTS;  // correspondences kept resident in shared memory
 constexpr int kLoRegion = GCR_BLOCK;    // model slots reserved for local optimisation
-constexpr int kLmScratch = 512;         // doubles of per-warp fit scratch
 
 enum PairStatus { ST_OK = 0, ST_NO_MODEL = 3, ST_TIMEOUT = 5, ST_CAPACITY = 6, ST_UNSUPPORTED = 7 };
 
@@ -104,7 +103,6 @@ struct Slot {
   double* node_d;       // [GCR_WARPS][3 * kMaxFlowCap]  excess, sink residual, scratch
   int* node_i;          // [GCR_WARPS][3 * kMaxFlowCap]  height, queue, mark
   double* red;          // [GCR_WARPS * 64 + 64] reduction partials
-  double* lmws;         // [GCR_WARPS][kLmScratch] per-warp scratch of the warp-level fits
   int* napsac;          // [16][max_n] P-NAPSAC layers (sorted points, cell start, cell size per point)
                         // x4, hits, subset sizes, layers, growth table
 };
@@ -1083,151 +1081,6 @@ struct Engine {
     return true;
   }
 
-  // Fundamental-matrix non-minimal fit of one local-optimisation trial by one
-  // warp (lanes share the rows; sequential steps run on lane 0 in the warp's
-  // scratch, which stays in L1): normalisation, 8-point start, 25 LM
-  // iterations, denormalisation. Same arithmetic as fit_cta_f.
-  __device__ bool fit_warp_f(const int* idx, int n, double* out, int warp) {
-    using F = FundamentalModel;
-    const int lane = threadIdx.x & 31;
-    if (n < 8) return false;
-    double* W = slot.lmws + (size_t)warp * kLmScratch;
-    double* P = W;            // [n][4] normalised rows (n <= 49)
-    double* M = W + 200;      // [81] A^T A / QR workspace
-    double* fF = W + 281;     // [19] factorised F
-    double* fN = W + 300;     // [19] candidate
-    double* G = W + 319;      // [9]
-    double* D = W + 328;      // [63]
-    double* A = W + 391;      // [49] damped system
-    double* flag = W + 440;   // [2]
-    HomographyModel::Norm nm;
-    {
-      double a = 0, b = 0, c = 0, d = 0;
-      for (int i = lane; i < n; i += 32) {
-        const double* p = pts64 + 4 * idx[i];
-        a += p[0]; b += p[1]; c += p[2]; d += p[3];
-      }
-      nm.ms0 = warp_sum(a) / n; nm.ms1 = warp_sum(b) / n; nm.md0 = warp_sum(c) / n; nm.md1 = warp_sum(d) / n;
-      double ds = 0, dd = 0;
-      for (int i = lane; i < n; i += 32) {
-        const double* p = pts64 + 4 * idx[i];
-        const double dx1 = nm.ms0 - p[0], dy1 = nm.ms1 - p[1], dx2 = nm.md0 - p[2], dy2 = nm.md1 - p[3];
-        ds += sqrt(dx1 * dx1 + dy1 * dy1);
-        dd += sqrt(dx2 * dx2 + dy2 * dy2);
-      }
-      nm.rs = M_SQRT2 / (warp_sum(ds) / n);
-      nm.rd = M_SQRT2 / (warp_sum(dd) / n);
-    }
-    for (int i = lane; i < n; i += 32) {
-      const double* p = pts64 + 4 * idx[i];
-      P[4 * i] = (p[0] - nm.ms0) * nm.rs;
-      P[4 * i + 1] = (p[1] - nm.ms1) * nm.rs;
-      P[4 * i + 2] = (p[2] - nm.md0) * nm.rd;
-      P[4 * i + 3] = (p[3] - nm.md1) * nm.rd;
-    }
-    __syncwarp();
-    // A^T A of the design rows: lane e owns entries e and e + 32 of the packed
-    // lower triangle (45), summed over the rows in order
-    for (int e = lane; e < 45; e += 32) {
-      int a = 0, b = e;
-      while (b > a) { b -= a + 1; ++a; }  // e = a (a + 1) / 2 + b, b <= a
-      double s = 0;
-      for (int i = 0; i < n; ++i) {
-        const double x0 = P[4 * i], y0 = P[4 * i + 1], x1 = P[4 * i + 2], y1 = P[4 * i + 3];
-        const double r[9] = {x1 * x0, x1 * y0, x1, y1 * x0, y1 * y0, y1, x0, y0, 1.0};
-        s += r[a] * r[b];
-      }
-      M[a * 9 + b] = s;
-      M[b * 9 + a] = s;
-    }
-    __syncwarp();
-    if (lane == 0) {
-      double F0[9];
-      fullpiv_qr_lastcol9(M, F0);
-      F::FactF ff;
-      F::factf_from(F0, ff);
-      for (int q = 0; q < 9; ++q) { fF[q] = ff.U[q]; fF[9 + q] = ff.V[q]; }
-      fF[18] = ff.sigma;
-      F::factf_F(ff, G);
-    }
-    __syncwarp();
-    auto cost_of = [&]() {  // cost of the model in G
-      double c = 0;
-      for (int i = lane; i < n; i += 32) c += F::lm_cost_point(G, P[4 * i], P[4 * i + 1], P[4 * i + 2], P[4 * i + 3]);
-      return warp_sum(c);
-    };
-    double cost = cost_of();
-    double lambda = 1e-3;
-    bool recompute = true;
-    double acc[F::NLM];
-    for (int iter = 0; iter < 25; ++iter) {
-      if (recompute) {
-        if (lane == 0) {
-          F::FactF ff;
-          for (int q = 0; q < 9; ++q) { ff.U[q] = fF[q]; ff.V[q] = fF[9 + q]; }
-          ff.sigma = fF[18];
-          F::factf_F(ff, G);
-          double Dl[9][7];
-          F::lm_dparams(ff, G, Dl);
-          for (int r = 0; r < 9; ++r)
-            for (int c = 0; c < 7; ++c) D[r * 7 + c] = Dl[r][c];
-        }
-        __syncwarp();
-        double Gr[9], Dr[9][7];
-#pragma unroll
-        for (int q = 0; q < 9; ++q) Gr[q] = G[q];
-#pragma unroll
-        for (int r = 0; r < 9; ++r)
-#pragma unroll
-          for (int c = 0; c < 7; ++c) Dr[r][c] = D[r * 7 + c];
-#pragma unroll
-        for (int q = 0; q < F::NLM; ++q) acc[q] = 0;
-        for (int i = lane; i < n; i += 32)
-          F::lm_accumulate_point(Gr, Dr, P[4 * i], P[4 * i + 1], P[4 * i + 2], P[4 * i + 3], 1.0, n, acc);
-#pragma unroll
-        for (int q = 0; q < F::NLM; ++q) acc[q] = warp_sum(acc[q]);
-        double gn = 0;
-#pragma unroll
-        for (int a = 0; a < 7; ++a) gn += acc[28 + a] * acc[28 + a];
-        if (sqrt(gn) < 1e-8) break;
-      }
-      if (lane == 0) {
-        F::FactF ff, fn;
-        for (int q = 0; q < 9; ++q) { ff.U[q] = fF[q]; ff.V[q] = fF[9 + q]; }
-        ff.sigma = fF[18];
-        const bool st = F::lm_step(acc, lambda, ff, fn);
-        flag[0] = st ? 1.0 : 0.0;
-        for (int q = 0; q < 9; ++q) { fN[q] = fn.U[q]; fN[9 + q] = fn.V[q]; }
-        fN[18] = fn.sigma;
-        F::factf_F(fn, G);
-      }
-      __syncwarp();
-      if (flag[0] == 0.0) break;
-      const double cn = cost_of();
-      __syncwarp();
-      if (cn < cost) {
-        if (lane < 19) fF[lane] = fN[lane];
-        lambda /= 10;
-        cost = cn;
-        recompute = true;
-      } else {
-        lambda *= 10;
-        recompute = false;
-      }
-      __syncwarp();
-    }
-    if (lane == 0) {
-      F::FactF ff;
-      for (int q = 0; q < 9; ++q) { ff.U[q] = fF[q]; ff.V[q] = fF[9 + q]; }
-      ff.sigma = fF[18];
-      double Fn[9];
-      F::factf_F(ff, Fn);
-      F::denormalise(nm, Fn, out);
-    }
-    __syncwarp();
-    return true;
-  }
-
   __device__ bool fit_cta(const int* list, int n, int weight_mode) {
     if constexpr (Est::KIND == 1) return fit_cta_f(list, n, weight_mode, true);
     if constexpr (Est::KIND == 2) return fit_cta_f(list, n, weight_mode, true, false);
@@ -1255,28 +1108,7 @@ struct Engine {
         // the LO sampler stream; the fit runs per thread (linear solvers) or
         // per warp (the fundamental-matrix LM)
         const int kb = kBatchModels;
-        if constexpr (Est::KIND == 1) {
-          if (threadIdx.x < trials) {
-            int* smp = slot.samples + threadIdx.x * Est::SAMPLE_CAP;
-            DrawStream ds(pd.seed, prm.stream_lo, (uint64_t)(lo_calls + threadIdx.x));
-            const bool ok = unique_set(ds, smp, ss, 0, (uint32_t)(nL - 1));
-            if (ok)
-              for (int q = 0; q < ss; ++q) smp[q] = L[smp[q]];
-            sh.lo_ok[threadIdx.x] = ok ? 1 : 0;
-          }
-          sync();
-          const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-          for (int t = warp; t < trials; t += GCR_WARPS) {
-            bool ok = sh.lo_ok[t] != 0;
-            if (ok) ok = fit_warp_f(slot.samples + t * Est::SAMPLE_CAP, ss, slot.models64 + 9 * (kb + t), warp);
-            __syncwarp();
-            if (lane == 0) {
-              sh.lo_ok[t] = ok ? 1 : 0;
-              if (ok) put_f32(kb + t);
-            }
-            __syncwarp();
-          }
-        } else if (threadIdx.x < trials) {
+        if (threadIdx.x < trials) {
           long long c0 = tick();
           int* smp = slot.samples + threadIdx.x * Est::SAMPLE_CAP;
           DrawStream ds(pd.seed, prm.stream_lo, (uint64_t)(lo_calls + threadIdx.x));

@@ -502,6 +502,67 @@ struct FundamentalModel {
     for (int a = 0; a < 7; ++a) acc[28 + a] += weight * C * inv * J[a];
   }
 
+  // lm_accumulate_point with J = dF^T D formed from the structure of D
+  // (lm_dparams): the six rotation columns hold signed entries of F, the
+  // sigma column the products ds = U[:,1] V[:,1]^T; the nonzero terms are
+  // summed in row order like the dense product. kDcode[r][c] = +-(k + 1)
+  // for the entry +-F[k], 0 for a structural zero.
+  __device__ __forceinline__ static void lm_accumulate_point_s(const double* F, const double* ds, double p0,
+                                                               double p1, double q0, double q1, int n, double* acc) {
+    constexpr signed char kDcode[9][6] = {{0, 7, -4, 0, 3, -2}, {-7, 0, 1, 0, 6, -5}, {4, -1, 0, 0, 9, -8},
+                                          {0, 8, -5, -3, 0, 1},  {-8, 0, 2, -6, 0, 4}, {5, -2, 0, -9, 0, 7},
+                                          {0, 9, -6, 2, -1, 0},  {-9, 0, 3, 5, -4, 0}, {6, -3, 0, 8, -7, 0}};
+    constexpr int kDs[9] = {0, 3, 6, 1, 4, 7, 2, 5, 8};
+    const double Fx0 = F[0] * p0 + F[1] * p1 + F[2], Fx1 = F[3] * p0 + F[4] * p1 + F[5],
+                 Fx2 = F[6] * p0 + F[7] * p1 + F[8];
+    const double C = q0 * Fx0 + q1 * Fx1 + Fx2;
+    const double J0 = F[0] * q0 + F[3] * q1 + F[6], J1 = F[1] * q0 + F[4] * q1 + F[7];
+    const double J2 = Fx0, J3 = Fx1;
+    const double nJ = sqrt(J0 * J0 + J1 * J1 + J2 * J2 + J3 * J3);
+    const double inv = 1.0 / nJ;
+    const double r = C * inv;
+    if (!((r * r) < 1.0)) return;
+    const double weight = 1.0 / n;
+    double dF[9] = {p0 * q0, p0 * q1, p0, p1 * q0, p1 * q1, p1, q0, q1, 1.0};
+    const double s = C * inv * inv;
+    dF[0] -= s * (J2 * p0 + J0 * q0);
+    dF[1] -= s * (J3 * p0 + J0 * q1);
+    dF[2] -= s * (J0);
+    dF[3] -= s * (J2 * p1 + J1 * q0);
+    dF[4] -= s * (J3 * p1 + J1 * q1);
+    dF[5] -= s * (J1);
+    dF[6] -= s * (J2);
+    dF[7] -= s * (J3);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) dF[k] *= inv;
+    double J[7];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      double t = 0;
+#pragma unroll
+      for (int rr = 0; rr < 9; ++rr) {
+        const int code = kDcode[rr][c];
+        if (code > 0) t += dF[rr] * F[code - 1];
+        if (code < 0) t += dF[rr] * (-F[-code - 1]);
+      }
+      J[c] = t;
+    }
+    {
+      double t = 0;
+#pragma unroll
+      for (int rr = 0; rr < 9; ++rr) t += dF[rr] * ds[kDs[rr]];
+      J[6] = t;
+    }
+    int k = 0;
+#pragma unroll
+    for (int a = 0; a < 7; ++a) {
+#pragma unroll
+      for (int b = 0; b <= a; ++b) acc[k++] += weight * (J[a] * J[b]);
+    }
+#pragma unroll
+    for (int a = 0; a < 7; ++a) acc[28 + a] += weight * C * inv * J[a];
+  }
+
   // one LM step from the accumulated system: sol = -(JtJ + lambda I)^-1 Jtr,
   // then the rotated factorisation (bundle.cpp:285-320). Returns false when
   // the step is below the tolerance.
@@ -562,22 +623,26 @@ struct FundamentalModel {
     for (int i = 0; i < 9; ++i) out[i] = sgn * (G[i] / nrm);
   }
 
-  // Per-thread non-minimal fit with unit weights (local-optimisation trials).
+  // Per-thread non-minimal fit with unit weights (the local-optimisation
+  // trials run one per thread): normalisation, 8-point start, 25 LM
+  // iterations on the factorised F, denormalisation. The model of the
+  // current factorisation and its cost are carried between iterations; the
+  // Jacobian uses the structure of dF/dparams instead of a dense 9x7 matrix.
   __device__ static bool fit_thread(const double* pts, const int* idx, int n, double* out) {
     if (n < 8) return false;  // the 7-row case cannot occur in the loop (see the engine)
     Norm N;
     HomographyModel::normalise(pts, idx, n, N);
-    double ata[NATA];
-#pragma unroll
-    for (int k = 0; k < NATA; ++k) ata[k] = 0;
-    for (int i = 0; i < n; ++i) accumulate_ata(N, pts + 4 * idx[i], 1.0, ata);
     double F[9];
-    eight_point_from_ata(ata, F);
+    {
+      double ata[NATA];
+#pragma unroll
+      for (int k = 0; k < NATA; ++k) ata[k] = 0;
+      for (int i = 0; i < n; ++i) accumulate_ata(N, pts + 4 * idx[i], 1.0, ata);
+      eight_point_from_ata(ata, F);
+    }
     FactF f;
     factf_from(F, f);
-    auto cost_of = [&](const FactF& ff) {
-      double G[9];
-      factf_F(ff, G);
+    auto cost_of = [&](const double* G) {
       double c = 0;
       for (int i = 0; i < n; ++i) {
         const double* p = pts + 4 * idx[i];
@@ -586,31 +651,40 @@ struct FundamentalModel {
       }
       return c;
     };
+    double G[9];
+    factf_F(f, G);
     double lambda = 1e-3;
-    double cost = cost_of(f);
+    double cost = cost_of(G);
     bool recompute = true;
     double acc[NLM];
     for (int iter = 0; iter < 25; ++iter) {
       if (recompute) {
 #pragma unroll
         for (int k = 0; k < NLM; ++k) acc[k] = 0;
-        double G[9], D[9][7];
-        factf_F(f, G);
-        lm_dparams(f, G, D);
+        double ds[9];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) ds[i * 3 + j] = f.U[i * 3 + 1] * f.V[j * 3 + 1];
         for (int i = 0; i < n; ++i) {
           const double* p = pts + 4 * idx[i];
-          lm_accumulate_point(G, D, (p[0] - N.ms0) * N.rs, (p[1] - N.ms1) * N.rs, (p[2] - N.md0) * N.rd,
-                              (p[3] - N.md1) * N.rd, 1.0, n, acc);
+          lm_accumulate_point_s(G, ds, (p[0] - N.ms0) * N.rs, (p[1] - N.ms1) * N.rs, (p[2] - N.md0) * N.rd,
+                                (p[3] - N.md1) * N.rd, n, acc);
         }
         double gn = 0;
+#pragma unroll
         for (int a = 0; a < 7; ++a) gn += acc[28 + a] * acc[28 + a];
         if (sqrt(gn) < 1e-8) break;
       }
       FactF fn;
       if (!lm_step(acc, lambda, f, fn)) break;
-      const double cn = cost_of(fn);
+      double Gn[9];
+      factf_F(fn, Gn);
+      const double cn = cost_of(Gn);
       if (cn < cost) {
         f = fn;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) G[k] = Gn[k];
         lambda /= 10;
         cost = cn;
         recompute = true;
@@ -619,9 +693,7 @@ struct FundamentalModel {
         recompute = false;
       }
     }
-    double Fn[9];
-    factf_F(f, Fn);
-    denormalise(N, Fn, out);
+    denormalise(N, G, out);
     return true;
   }
 };

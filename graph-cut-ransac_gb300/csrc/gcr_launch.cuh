@@ -99,7 +99,6 @@ size_t slot_bytes(int max_n, int sort_cap, bool light = false) {
   s += al(sizeof(int) * GCR_BLOCK * Est::SAMPLE_CAP);
   s += al(sizeof(int) * GCR_BLOCK * Est::M);
   s += al(sizeof(double) * (GCR_WARPS * 64 + 64));
-  s += al(sizeof(double) * GCR_WARPS * kLmScratch);
   s += 3 * al(sizeof(int) * max_n);
   s += al((size_t)max_n);
   s += 2 * al(sizeof(double) * max_n);
@@ -126,7 +125,6 @@ Slot carve_slot(unsigned char* base, int max_n, int sort_cap, bool light = false
   s.samples = (int*)take(sizeof(int) * GCR_BLOCK * Est::SAMPLE_CAP);
   s.bsamples = (int*)take(sizeof(int) * GCR_BLOCK * Est::M);
   s.red = (double*)take(sizeof(double) * (GCR_WARPS * 64 + 64));
-  s.lmws = (double*)take(sizeof(double) * GCR_WARPS * kLmScratch);
   s.list0 = (int*)take(sizeof(int) * max_n);
   s.list1 = (int*)take(sizeof(int) * max_n);
   s.list2 = (int*)take(sizeof(int) * max_n);

@@ -39,51 +39,67 @@ __host__ __device__ __forceinline__ bool inverse3(const double* m, double* out) 
 }
 
 // Symmetric 3x3 eigen decomposition by cyclic Jacobi rotations; eigenvalues
-// in descending order, eigenvectors in the columns of V (row-major).
+// in descending order, eigenvectors in the columns of V (row-major). Every
+// index is a compile-time constant so that the matrices stay in registers.
 __device__ inline void sym3_eigen(const double* S_in, double* w, double* V) {
   double S[9];
+#pragma unroll
   for (int i = 0; i < 9; ++i) S[i] = S_in[i];
+#pragma unroll
   for (int i = 0; i < 9; ++i) V[i] = (i % 4 == 0) ? 1.0 : 0.0;
   for (int sweep = 0; sweep < 50; ++sweep) {
     const double off = S[1] * S[1] + S[2] * S[2] + S[5] * S[5];
     if (off < 1e-300) break;
-    for (int p = 0; p < 2; ++p)
-      for (int q = p + 1; q < 3; ++q) {
-        const double apq = S[p * 3 + q];
-        if (fabs(apq) < 1e-300) continue;
+#pragma unroll
+    for (int pq = 0; pq < 3; ++pq) {
+      const int p = pq == 2 ? 1 : 0;
+      const int q = pq == 0 ? 1 : 2;
+      const double apq = S[p * 3 + q];
+      if (!(fabs(apq) < 1e-300)) {
         const double app = S[p * 3 + p], aqq = S[q * 3 + q];
         const double theta = (aqq - app) / (2 * apq);
         const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1));
         const double cs = 1 / sqrt(t * t + 1), sn = t * cs;
+#pragma unroll
         for (int k = 0; k < 3; ++k) {
           const double skp = S[k * 3 + p], skq = S[k * 3 + q];
           S[k * 3 + p] = cs * skp - sn * skq;
           S[k * 3 + q] = sn * skp + cs * skq;
         }
+#pragma unroll
         for (int k = 0; k < 3; ++k) {
           const double spk = S[p * 3 + k], sqk = S[q * 3 + k];
           S[p * 3 + k] = cs * spk - sn * sqk;
           S[q * 3 + k] = sn * spk + cs * sqk;
         }
+#pragma unroll
         for (int k = 0; k < 3; ++k) {
           const double vkp = V[k * 3 + p], vkq = V[k * 3 + q];
           V[k * 3 + p] = cs * vkp - sn * vkq;
           V[k * 3 + q] = sn * vkp + cs * vkq;
         }
       }
+    }
   }
-  int i0 = 0, i1 = 1, i2 = 2;
-  auto sw = [](int& a, int& b) { const int t = a; a = b; b = t; };
-  if (S[i0 * 4] < S[i1 * 4]) sw(i0, i1);
-  if (S[i1 * 4] < S[i2 * 4]) sw(i1, i2);
-  if (S[i0 * 4] < S[i1 * 4]) sw(i0, i1);
-  const int idx[3] = {i0, i1, i2};
-  double Vs[9];
-  for (int j = 0; j < 3; ++j) {
-    w[j] = S[idx[j] * 4];
-    for (int i = 0; i < 3; ++i) Vs[i * 3 + j] = V[i * 3 + idx[j]];
-  }
-  for (int i = 0; i < 9; ++i) V[i] = Vs[i];
+  // descending order by three compare-and-swap steps on (eigenvalue, column)
+  double d[3] = {S[0], S[4], S[8]};
+  auto cswap = [&](int a, int b) {
+    const bool sw = d[a] < d[b];
+    const double da = d[a], db = d[b];
+    d[a] = sw ? db : da;
+    d[b] = sw ? da : db;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const double va = V[i * 3 + a], vb = V[i * 3 + b];
+      V[i * 3 + a] = sw ? vb : va;
+      V[i * 3 + b] = sw ? va : vb;
+    }
+  };
+  cswap(0, 1);
+  cswap(1, 2);
+  cswap(0, 1);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) w[j] = d[j];
 }
 
 // SVD A = U diag(s) V^T of a 3x3 matrix (s descending): V from the
