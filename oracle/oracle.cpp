@@ -181,6 +181,87 @@ static int find_fundamental(const double* corr, int64_t n, const gcr_image_size&
   return rc;
 }
 
+// findEssentialMatrix_ (gcransac_python.cpp:2519-2856): correspondences
+// normalised by the inverse intrinsics (utils.h:65-103), threshold divided by
+// the mean focal length (2601-2603), grid and P-NAPSAC on the pixel
+// coordinates (cells w / n), GC-RANSAC on the normalised ones, then the
+// weighted essential-matrix bundle adjustment of the final inliers kept when
+// it raises the MSAC score (2770-2826); with at most 5 inliers the model is
+// the identity (2828). The bundle adjustment's Stewenius start reads the
+// weights by point index (the reference indexes an inlier-sized array by
+// point index there); the weights are placed at the inliers' point indices,
+// so both steps see the weight of each inlier.
+static int find_essential(const double* corr, int64_t n, const double* K1, const double* K2,
+                          const gcr_image_size& sz, const gcr_params& p, uint64_t seed, double* model_out,
+                          uint8_t* mask, gcr_stats* st) {
+  if (n < 5) return GCR_TOO_FEW_POINTS;
+  if (!K1 || !K2) return GCR_INVALID_ARG;
+  const Mat pix{corr, n, 4};
+  double Ki1[9], Ki2[9];
+  inverse3(K1, Ki1);
+  inverse3(K2, Ki2);
+  std::vector<double> nrm((size_t)n * 4);
+  for (int64_t i = 0; i < n; ++i) {
+    const double* q = corr + 4 * i;
+    nrm[4 * i] = Ki1[0] * q[0] + Ki1[1] * q[1] + Ki1[2];
+    nrm[4 * i + 1] = Ki1[3] * q[0] + Ki1[4] * q[1] + Ki1[5];
+    nrm[4 * i + 2] = Ki2[0] * q[2] + Ki2[1] * q[3] + Ki2[2];
+    nrm[4 * i + 3] = Ki2[3] * q[2] + Ki2[4] * q[3] + Ki2[5];
+  }
+  const Mat pts{nrm.data(), n, 4};
+  const double normalizer = 0.25 * (K1[0] + K1[4] + K2[0] + K2[4]);
+  const double thr = p.threshold / normalizer;
+  std::unique_ptr<Grid> grid;
+  if (p.spatial_coherence_weight > std::numeric_limits<double>::epsilon()) {
+    const size_t nd = (size_t)p.neighborhood_size;
+    const double cs[4] = {sz.w1 / (double)nd, sz.h1 / (double)nd, sz.w2 / (double)nd, sz.h2 / (double)nd};
+    grid = std::make_unique<Grid>(pix, cs, nd);
+  }
+  EssentialEstimator est;
+  Model model{};
+  std::vector<size_t> inl;
+  int rc;
+  if (p.scoring == GCR_SCORING_MAGSAC)
+    rc = run_generic<EssentialEstimator, MAGSACScoring>(pts, pix, est, p, sz, seed, grid.get(), thr, model, inl,
+                                                        st, thr);
+  else
+    rc = run_generic<EssentialEstimator, MSACScoring>(pts, pix, est, p, sz, seed, grid.get(), thr, model, inl, st,
+                                                      thr);
+  if (rc == GCR_OK) {
+    if (inl.size() > 5) {
+      const double tt = 1.5 * thr, sq = tt * tt;
+      std::vector<double> w_pos(inl.size()), w_pt((size_t)n, 0.0);
+      for (size_t k = 0; k < inl.size(); ++k) {
+        w_pos[k] = std::max(0.0, 1.0 - e_sampson2(pts.row(inl[k]), model) / sq);
+        w_pt[inl[k]] = w_pos[k];
+      }
+      std::vector<Model> models;
+      e_bundle_adjust(pts, inl.data(), inl.size(), w_pt.data(), w_pos.data(), models);
+      MSACScoring<EssentialEstimator> sc;
+      sc.initialize(sq, n);
+      double best = st ? st->score : 0.0;
+      for (Model& E : models) {
+        std::vector<size_t> cur;
+        const Score s = sc.get(pts, E, est, &cur);
+        if (best < s.value) {
+          model = E;
+          best = s.value;
+          inl.swap(cur);
+        }
+      }
+      if (st) st->score = best;
+    } else {
+      model = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    }
+  }
+  std::memset(mask, 0, (size_t)n);
+  for (size_t i : inl) mask[i] = 1;
+  if (st) st->inlier_number = (int64_t)inl.size();
+  if (rc == GCR_OK) std::memcpy(model_out, model.data(), 9 * sizeof(double));
+  else std::memset(model_out, 0, 9 * sizeof(double));
+  return rc;
+}
+
 }  // namespace oracle
 
 using namespace oracle;
@@ -268,10 +349,14 @@ double oracle_msac_score(int kind, const double* corr, int64_t n, const double* 
     MSACScoring<HomographyEstimator> sc;
     sc.initialize(sq, n);
     s = sc.get(pts, m, HomographyEstimator(), nullptr);
-  } else {
+  } else if (kind == GCR_FUNDAMENTAL) {
     MSACScoring<FundamentalEstimator> sc;
     sc.initialize(sq, n);
     s = sc.get(pts, m, FundamentalEstimator(), nullptr);
+  } else {
+    MSACScoring<EssentialEstimator> sc;
+    sc.initialize(sq, n);
+    s = sc.get(pts, m, EssentialEstimator(), nullptr);
   }
   *count = (int64_t)s.inlier_number;
   return s.value;
@@ -299,6 +384,26 @@ int oracle_minimal(int kind, const double* corr, int64_t n, const int64_t* sampl
   }
   for (size_t i = 0; i < models.size() && i < 10; ++i) std::memcpy(models_out + 9 * i, models[i].data(), 72);
   return (int)models.size();
+}
+
+// Non-minimal essential-matrix solve (Stewenius) for tests: weights by point
+// index or NULL; writes up to 10 normalised models, returns their count.
+int oracle_nonminimal_essential(const double* corr, int64_t n, const int64_t* sample, int64_t ns,
+                                const double* weights, double* models_out) {
+  const Mat pts{corr, n, 4};
+  std::vector<size_t> s(sample, sample + ns);
+  std::vector<Model> models;
+  EssentialEstimator e;
+  if (!e.estimate_nonminimal(pts, s.data(), s.size(), models, weights)) return 0;
+  for (size_t i = 0; i < models.size() && i < 10; ++i) std::memcpy(models_out + 9 * i, models[i].data(), 72);
+  return (int)models.size();
+}
+
+// Real roots of a degree-10 polynomial (ascending coefficients) by the Sturm
+// bracketing of the five-point solver; returns their count.
+int oracle_sturm10(const double* coeffs, double* roots) {
+  Sturm st;
+  return st.solve(coeffs, roots);
 }
 
 // Draw sequence of the main sampler for tests of the device sampler.

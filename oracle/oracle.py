@@ -45,6 +45,10 @@ def load():
         lib.oracle_msac_score.argtypes = [ctypes.c_int, P, ctypes.c_int64, P, ctypes.c_double, P]
         lib.oracle_minimal.restype = ctypes.c_int
         lib.oracle_minimal.argtypes = [ctypes.c_int, P, ctypes.c_int64, P, P]
+        lib.oracle_nonminimal_essential.restype = ctypes.c_int
+        lib.oracle_nonminimal_essential.argtypes = [P, ctypes.c_int64, P, ctypes.c_int64, P, P]
+        lib.oracle_sturm10.restype = ctypes.c_int
+        lib.oracle_sturm10.argtypes = [P, P]
         lib.oracle_sample_sequence.restype = ctypes.c_int
         lib.oracle_sample_sequence.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.c_int, ctypes.c_uint64,
                                                ctypes.c_int64, P, P, P, P]
@@ -149,3 +153,23 @@ def philox(ctr, key):
 
 def draw_u32(seed, stream, call, draw):
     return load().oracle_draw_u32(seed, stream, call, draw)
+
+
+def nonminimal_essential(corr, sample, weights=None):
+    """Stewenius fit of normalised correspondences; returns a list of 3x3 models."""
+    lib = load()
+    corr = np.ascontiguousarray(corr, dtype=np.float64)
+    s = np.ascontiguousarray(sample, dtype=np.int64)
+    w = None if weights is None else np.ascontiguousarray(weights, np.float64)
+    out = np.zeros(90)
+    k = lib.oracle_nonminimal_essential(_p(corr), corr.shape[0], _p(s), len(s), _p(w), _p(out))
+    return [out[9 * i:9 * i + 9].reshape(3, 3) for i in range(k)]
+
+
+def sturm10(coeffs):
+    """Real roots of sum coeffs[i] x^i (degree 10) by Sturm bracketing."""
+    lib = load()
+    c = np.ascontiguousarray(coeffs, dtype=np.float64)
+    r = np.zeros(10)
+    k = lib.oracle_sturm10(_p(c), _p(r))
+    return np.sort(r[:k])
