@@ -16,7 +16,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 SOURCES = ["gcr_api.cu", "gcr_kind_h.cu", "gcr_kind_f.cu", "gcr_kind_e.cu", "gcr_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+         "--expt-relaxed-constexpr",
          "-Xptxas", "-warn-spills"]
 
 

@@ -260,6 +260,7 @@ gcr_status gcr_batch_run_device(gcr_context* c, gcr_model_kind kind, int64_t num
     // (gcransac_python.cpp:4290-4297), the fundamental/essential ones do not
     // (1670-1677)
     const double pad = kind == GCR_HOMOGRAPHY ? eps : 0.0;
+    const bool essential = kind == GCR_ESSENTIAL;
     d.cell[0] = (z.w1 + pad) / nd;
     d.cell[1] = (z.h1 + pad) / nd;
     d.cell[2] = (z.w2 + pad) / nd;
@@ -269,16 +270,46 @@ gcr_status gcr_batch_run_device(gcr_context* c, gcr_model_kind kind, int64_t num
     d.centre[1] = 0.5 * z.h1;
     d.centre[2] = 0.5 * z.w2;
     d.centre[3] = 0.5 * z.h2;
+    if (essential) {
+      // findEssentialMatrix_ (gcransac_python.cpp:2598-2603, 2655): the run
+      // works on K^-1-normalised coordinates with the threshold divided by
+      // the mean focal length; those coordinates need no centring
+      const double* K1 = h_K + 18 * i;
+      const double* K2 = K1 + 9;
+      const double normalizer = 0.25 * (K1[0] + K1[4] + K2[0] + K2[4]);
+      d.threshold = params->threshold / normalizer;
+      for (int q = 0; q < 4; ++q) d.centre[q] = 0.0;
+    }
+    d.img[0] = z.w1;
+    d.img[1] = z.h1;
+    d.img[2] = z.w2;
+    d.img[3] = z.h2;
     d.seed = h_seeds ? h_seeds[i] : params->seed + (uint64_t)i;
   }
   CUDA_TRY(c->pairs.ensure(sizeof(gcr::PairDesc) * num_pairs));
   CUDA_TRY(cudaMemcpyAsync(c->pairs.p, pd.data(), sizeof(gcr::PairDesc) * num_pairs, cudaMemcpyHostToDevice, s));
+  const double* run_pts = d_corr;
+  if (kind == GCR_ESSENTIAL) {
+    // K^-1 of both cameras per pair (a singular K is rejected)
+    std::vector<double> kinv(18 * (size_t)num_pairs);
+    for (int64_t i = 0; i < num_pairs; ++i)
+      for (int cam = 0; cam < 2; ++cam)
+        if (!gcr::inverse3(h_K + 18 * i + 9 * cam, kinv.data() + 18 * i + 9 * cam))
+          return fail(GCR_INVALID_ARG, "intrinsics of pair %lld camera %d are singular", (long long)i, cam + 1);
+    CUDA_TRY(c->kinv.ensure(sizeof(double) * kinv.size()));
+    // (a copy from pageable memory is staged before the call returns)
+    CUDA_TRY(cudaMemcpyAsync(c->kinv.p, kinv.data(), sizeof(double) * kinv.size(), cudaMemcpyHostToDevice, s));
+    CUDA_TRY(c->norm_pts.ensure(sizeof(double) * 4 * (size_t)std::max<int64_t>(total, 1)));
+    CUDA_TRY(gcr::launch_normalise_essential(d_corr, (const double*)c->kinv.p, (const gcr::PairDesc*)c->pairs.p,
+                                             (int)num_pairs, (double*)c->norm_pts.p, s));
+    run_pts = (const double*)c->norm_pts.p;
+  }
   if (max_n > gcr::kSmemPoints) CUDA_TRY(c->pts32.ensure(sizeof(float4) * (size_t)total));
   CUDA_TRY(c->ticket.ensure(sizeof(int)));
   CUDA_TRY(cudaMemsetAsync(c->ticket.p, 0, sizeof(int), s));
 
   gcr::Workspace ws;
-  ws.pts64 = d_corr;
+  ws.pts64 = run_pts;
   ws.pix64 = d_corr;
   ws.pts32 = (float4*)c->pts32.p;
   ws.pairs = (const gcr::PairDesc*)c->pairs.p;
@@ -314,7 +345,7 @@ gcr_status gcr_batch_run_device(gcr_context* c, gcr_model_kind kind, int64_t num
   prm.stream_lo = 2;    // STREAM_LO
   prm.pp_h = nullptr;
   CUDA_TRY(ops->launch(grid, s, ws, prm));
-  g_last_launches = 1;
+  g_last_launches = kind == GCR_ESSENTIAL ? 2 : 1;
   return GCR_OK;
 }
 

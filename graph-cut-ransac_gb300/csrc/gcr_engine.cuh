@@ -23,6 +23,7 @@
 #pragma once
 
 #include "gcr_device.cuh"
+#include "gcr_essential.cuh"
 #include "gcr_fundamental.cuh"
 #include "gcr_homography.cuh"
 #include "gcr_linalg.cuh"
@@ -69,6 +70,7 @@ struct PairDesc {
   double threshold;     // threshold in the coordinates the model is fitted in
   double cell[4];       // grid cell sizes (pixel coordinates)
   double centre[4];     // centring of the FP32 copy
+  double img[4];        // image sizes w1, h1, w2, h2 (P-NAPSAC grids)
   uint64_t seed;
 };
 
@@ -136,6 +138,9 @@ struct Container {
 template <class Est>
 struct Shared {
   static constexpr int kModels = GCR_BLOCK * Est::MAXSOL + kLoRegion;
+  // staging of per-trial model lists of multi-model non-minimal fits (global only)
+  static constexpr int kStage = Est::LO_MAXSOL > 1 ? GCR_BLOCK : 0;
+  static constexpr int kMulti = Est::LO_MAXSOL;
   double best_model[9];
   double cont_model[2][9];
   double lo_best_model[9];
@@ -153,6 +158,9 @@ struct Shared {
   float s_sum[GCR_BLOCK];
   float s_err[GCR_BLOCK];
   int lo_ok[GCR_BLOCK];
+  int lo_base[GCR_BLOCK];
+  double multi_models[9 * kMulti];  // models of the last CTA-wide multi-model fit
+  int multi_count;
   double lm_f[19];                // factorised F (U, V, sigma) of the CTA-wide LM
   double lm_fn[19];
   double lm_G[9];
@@ -463,7 +471,7 @@ struct Engine {
     const int divs[4] = {16, 8, 4, 2};
     for (int l = 0; l < 4; ++l) {
       double cs[4];
-      for (int d = 0; d < 4; ++d) cs[d] = 2.0 * pd.centre[d] / (double)divs[l];
+      for (int d = 0; d < 4; ++d) cs[d] = pd.img[d] / (double)divs[l];
       const int nc = sort_cells(cs, (uint64_t)divs[l], nl_sorted(l), slot.cell_start);
       // per point: start and size of its cell in the sorted list
       for (int c = threadIdx.x; c < nc; c += GCR_BLOCK) {
@@ -1082,9 +1090,224 @@ struct Engine {
   }
 
   __device__ bool fit_cta(const int* list, int n, int weight_mode) {
+    if constexpr (Est::LO_MAXSOL > 1) return false;  // multi-model estimators use fit_cta_multi
     if constexpr (Est::KIND == 1) return fit_cta_f(list, n, weight_mode, true);
     if constexpr (Est::KIND == 2) return fit_cta_f(list, n, weight_mode, true, false);
     return fit_cta_h(list, n, weight_mode);
+  }
+
+  // ------------------------------------------------------------------
+  // Essential matrices: the non-minimal solver returns up to ten models.
+
+  // Weighted Stewenius fit of the rows list[0..n) by the CTA: the weighted
+  // normal matrix is reduced across the CTA, thread 0 solves. weight_mode 0:
+  // unit weights; 2: slot.dres[k] by row position; 3: the squared Tukey
+  // weight of point list[k] under sh.work_model (weights by point index, as
+  // the Stewenius solver reads them). With `normalise` each model gets unit
+  // norm and E33 >= 0 (estimateModelNonminimal). Models go to
+  // sh.multi_models; returns their number.
+  __device__ int fit_cta_multi(const int* list, int n, int weight_mode, bool normalise) {
+    if constexpr (Est::LO_MAXSOL > 1) {
+      if (n < Est::NONMIN) return 0;
+      double wm[9];
+#pragma unroll
+      for (int q = 0; q < 9; ++q) wm[q] = sh.work_model[q];
+      auto weight = [&](int k) -> double {
+        if (weight_mode == 0) return 1.0;
+        if (weight_mode == 2) return slot.dres[k];
+        const double r2 = Est::r2_f64(pts64 + 4 * list[k], wm);
+        const double w = fmax(0.0, 1.0 - r2 / t2);
+        return w * w;
+      };
+      if (n == 5) {
+        if (threadIdx.x == 0) {
+          double rows[5][9];
+          for (int k = 0; k < 5; ++k) ess::design_row(pts64 + 4 * list[k], weight(k), rows[k]);
+          sh.multi_count = ess::stewenius_five(rows, sh.multi_models);
+        }
+      } else {
+        double acc[45];
+#pragma unroll
+        for (int q = 0; q < 45; ++q) acc[q] = 0;
+        for (int k = threadIdx.x; k < n; k += GCR_BLOCK) {
+          double r[9];
+          ess::design_row(pts64 + 4 * list[k], weight(k), r);
+          int q = 0;
+#pragma unroll
+          for (int a = 0; a < 9; ++a)
+#pragma unroll
+            for (int b = 0; b <= a; ++b) acc[q++] += r[a] * r[b];
+        }
+        cta_reduce<45>(acc, slot.red + GCR_WARPS * 64);
+        if (threadIdx.x == 0) {
+          const double* t = slot.red + GCR_WARPS * 64;
+          double full[81];
+          int q = 0;
+          for (int a = 0; a < 9; ++a)
+            for (int b = 0; b <= a; ++b) {
+              full[a * 9 + b] = t[q];
+              full[b * 9 + a] = t[q];
+              ++q;
+            }
+          sh.multi_count = ess::stewenius_from_ata(full, sh.multi_models);
+        }
+      }
+      if (threadIdx.x == 0 && normalise)
+        for (int q = 0; q < sh.multi_count; ++q) ess::normalise_sign(sh.multi_models + 9 * q);
+      sync();
+      return sh.multi_count;
+    } else {
+      return 0;
+    }
+  }
+
+  // Local-optimisation trials whose fits return several models: trials run
+  // one per thread in chunks of kLoRegion / LO_MAXSOL; each chunk's models are
+  // compacted in trial order into the local-optimisation region, scored in
+  // FP32 and replayed in order.
+  __device__ void lo_trials_multi(int nL, int ss, const int* L, int trials, Score& max_score, bool& updated) {
+    if constexpr (Est::LO_MAXSOL > 1) {
+      constexpr int chunk_cap = kLoRegion / Est::LO_MAXSOL;
+      constexpr int kstage = kBatchModels + kLoRegion;
+      const int kb = kBatchModels;
+      for (int t0 = 0; t0 < trials; t0 += chunk_cap) {
+        const int nt = min(chunk_cap, trials - t0);
+        int cnt = 0;
+        if (threadIdx.x < nt) {
+          int* smp = slot.samples + threadIdx.x * Est::SAMPLE_CAP;
+          DrawStream ds(pd.seed, prm.stream_lo, (uint64_t)(lo_calls + t0 + threadIdx.x));
+          if (unique_set(ds, smp, ss, 0, (uint32_t)(nL - 1))) {
+            for (int q = 0; q < ss; ++q) smp[q] = L[smp[q]];
+            cnt = Est::fit_thread_multi(pts64, smp, ss, slot.models64 + 9 * (kstage + threadIdx.x * Est::LO_MAXSOL));
+          }
+        }
+        int total;
+        const int base = block_exclusive_scan(cnt, sh.red_i, &total);
+        if (threadIdx.x < nt) {
+          sh.lo_ok[threadIdx.x] = cnt;
+          sh.lo_base[threadIdx.x] = base;
+        }
+        for (int q = 0; q < cnt; ++q) {
+          const double* src = slot.models64 + 9 * (kstage + threadIdx.x * Est::LO_MAXSOL + q);
+          double* dst = slot.models64 + 9 * (kb + base + q);
+#pragma unroll
+          for (int e = 0; e < 9; ++e) dst[e] = src[e];
+          put_f32(kb + base + q);
+        }
+        sync();
+        score_models_f32(kb, total);
+        for (int u = 0; u < nt; ++u) {
+          const int nm = sh.lo_ok[u], b0 = sh.lo_base[u];
+          for (int q = 0; q < nm; ++q) {
+            ++models_scored;
+            const int k = kb + b0 + q;
+            if (sh.mcount[k] == 0 || !maybe_better(k, max_score.value)) continue;
+            const Score sc = exact_score(slot.models64 + 9 * k, nullptr, slot.models32 + 12 * k);
+            if (max_score.value < sc.value) {
+              updated = true;
+              max_score = sc;
+              copy_model(sh.lo_best_model, slot.models64 + 9 * k);
+            }
+          }
+        }
+        sync();
+      }
+      lo_calls += trials;
+    }
+  }
+
+  // iteratedLeastSquaresFitting (GCRANSAC.h:629-758) with several models per
+  // fit: one model replaces the current set when it has more inliers; with
+  // several, every model with more inliers than the current set and at least
+  // as many as the best so far does, in order.
+  __device__ bool irls_multi(int*& list, int& n, int*& spare) {
+    if (n <= m) return false;
+    int iterations = 0;
+    int best_count = 0;
+    while (++iterations < 10) {
+      const int nm = fit_cta_multi(list, n, 3, true);
+      if (nm == 0) break;
+      if (nm == 1) {
+        const Score sc = exact_score(sh.multi_models, spare);
+        ++models_scored;
+        if (sc.count < m) break;
+        if (sc.count <= n) break;
+        copy_model(sh.work_model, sh.multi_models);
+        int* t = list;
+        list = spare;
+        spare = t;
+        n = sc.count;
+      } else {
+        bool upd = false;
+        for (int q = 0; q < nm; ++q) {
+          const Score sc = exact_score(sh.multi_models + 9 * q, spare);
+          ++models_scored;
+          if (sc.count < m) continue;
+          if (sc.count <= n) continue;
+          if (sc.count >= best_count) {
+            upd = true;
+            best_count = sc.count;
+            copy_model(sh.work_model, sh.multi_models + 9 * q);
+            int* t = list;
+            list = spare;
+            spare = t;
+            n = sc.count;
+          }
+        }
+        if (!upd) break;
+      }
+    }
+    return iterations > 1;
+  }
+
+  // refine_relpose (bundle.cpp:412-452 + 176-250) of the pose in sh over the
+  // rows list[0..n) with the position weights in slot.dres; every thread
+  // carries the same LM state, the sums are CTA reductions.
+  __device__ void refine_relpose_cta(const int* list, int n, ess::Pose& P) {
+    auto residual = [&](const ess::Pose& Q) {
+      double E[9];
+      ess::essential_from_pose(Q, E);
+      double c = 0;
+      for (int k = threadIdx.x; k < n; k += GCR_BLOCK) c += slot.dres[k] * ess::relpose_loss(E, pts64 + 4 * list[k]);
+      return block_sum(c, sh.red_d);
+    };
+    double lambda = 1e-3;
+    double cost = residual(P);
+    bool recompute = true;
+    double tot[20];
+    ess::PoseJac J;
+    for (int iter = 0; iter < 25; ++iter) {
+      if (recompute) {
+        ess::pose_jacobians(P, J);
+        double acc[20];
+#pragma unroll
+        for (int q = 0; q < 20; ++q) acc[q] = 0;
+        for (int k = threadIdx.x; k < n; k += GCR_BLOCK)
+          ess::relpose_accumulate(J, pts64 + 4 * list[k], slot.dres[k], n, acc);
+        cta_reduce<20>(acc, slot.red + GCR_WARPS * 64);
+#pragma unroll
+        for (int q = 0; q < 20; ++q) tot[q] = slot.red[GCR_WARPS * 64 + q];
+        sync();
+        double gn = 0;
+        for (int a = 0; a < 5; ++a) gn += tot[15 + a] * tot[15 + a];
+        if (sqrt(gn) < 1e-8) break;
+      }
+      constexpr int diag[5] = {0, 2, 5, 9, 14};
+      for (int a = 0; a < 5; ++a) tot[diag[a]] += lambda;
+      ess::Pose Pn;
+      if (!ess::relpose_step(tot, tot + 15, J, P, Pn)) break;
+      const double cn = residual(Pn);
+      if (cn < cost) {
+        P = Pn;
+        lambda /= 10;
+        cost = cn;
+        recompute = true;
+      } else {
+        for (int a = 0; a < 5; ++a) tot[diag[a]] -= lambda;
+        lambda *= 10;
+        recompute = false;
+      }
+    }
   }
 
   // ------------------------------------------------------------------
@@ -1103,44 +1326,65 @@ struct Engine {
       tock(4, t0);
       t0 = tick();
       const int ss = min(inlier_limit, nL);
-      if (ss < nL) {
-        // one thread per trial draws the sample from the labelled inliers with
-        // the LO sampler stream; the fit runs per thread (linear solvers) or
-        // per warp (the fundamental-matrix LM)
-        const int kb = kBatchModels;
-        if (threadIdx.x < trials) {
-          long long c0 = tick();
-          int* smp = slot.samples + threadIdx.x * Est::SAMPLE_CAP;
-          DrawStream ds(pd.seed, prm.stream_lo, (uint64_t)(lo_calls + threadIdx.x));
-          bool ok = unique_set(ds, smp, ss, 0, (uint32_t)(nL - 1));
-          tock(12, c0);
-          c0 = tick();
-          if (ok) {
-            for (int q = 0; q < ss; ++q) smp[q] = L[smp[q]];
-            ok = Est::fit_thread(pts64, smp, ss, slot.models64 + 9 * (kb + threadIdx.x));
+      if constexpr (Est::LO_MAXSOL > 1) {
+        if (ss < nL) {
+          lo_trials_multi(nL, ss, L, trials, max_score, updated);
+          tock(5, t0);
+        } else if (m < nL) {
+          // every trial fits all labelled inliers: the same models each time, so
+          // only the first trial can improve; the rest are counted
+          const int nm = fit_cta_multi(L, nL, 0, true);
+          if (nm > 0) {
+            models_scored += (long long)trials * nm;
+            for (int q = 0; q < nm && trials > 0; ++q) {
+              const Score sc = exact_score(sh.multi_models + 9 * q, nullptr);
+              if (max_score.value < sc.value) {
+                updated = true;
+                max_score = sc;
+                copy_model(sh.lo_best_model, sh.multi_models + 9 * q);
+              }
+            }
           }
-          tock(13, c0);
-          c0 = tick();
-          sh.lo_ok[threadIdx.x] = ok ? 1 : 0;
-          if (ok) put_f32(kb + threadIdx.x);
-          tock(14, c0);
         }
-        sync();
-        tock(5, t0);
-        lo_calls += trials;
-        t0 = tick();
-        score_lo_trials(kb, trials, max_score, updated);
-        tock(6, t0);
-      } else if (m < nL) {
-        if (!fit_cta(L, nL, 0)) {
-          // the reference breaks out of the trial loop; nothing was updated
-        } else {
-          const Score sc = exact_score(sh.fit_model, nullptr);
-          models_scored += trials;
-          if (max_score.value < sc.value) {
-            updated = true;
-            max_score = sc;
-            copy_model(sh.lo_best_model, sh.fit_model);
+      } else {
+        if (ss < nL) {
+          // one thread per trial draws the sample from the labelled inliers with
+          // the LO sampler stream and fits it
+          const int kb = kBatchModels;
+          if (threadIdx.x < trials) {
+            long long c0 = tick();
+            int* smp = slot.samples + threadIdx.x * Est::SAMPLE_CAP;
+            DrawStream ds(pd.seed, prm.stream_lo, (uint64_t)(lo_calls + threadIdx.x));
+            bool ok = unique_set(ds, smp, ss, 0, (uint32_t)(nL - 1));
+            tock(12, c0);
+            c0 = tick();
+            if (ok) {
+              for (int q = 0; q < ss; ++q) smp[q] = L[smp[q]];
+              ok = Est::fit_thread(pts64, smp, ss, slot.models64 + 9 * (kb + threadIdx.x));
+            }
+            tock(13, c0);
+            c0 = tick();
+            sh.lo_ok[threadIdx.x] = ok ? 1 : 0;
+            if (ok) put_f32(kb + threadIdx.x);
+            tock(14, c0);
+          }
+          sync();
+          tock(5, t0);
+          lo_calls += trials;
+          t0 = tick();
+          score_lo_trials(kb, trials, max_score, updated);
+          tock(6, t0);
+        } else if (m < nL) {
+          if (!fit_cta(L, nL, 0)) {
+            // the reference breaks out of the trial loop; nothing was updated
+          } else {
+            const Score sc = exact_score(sh.fit_model, nullptr);
+            models_scored += trials;
+            if (max_score.value < sc.value) {
+              updated = true;
+              max_score = sc;
+              copy_model(sh.lo_best_model, sh.fit_model);
+            }
           }
         }
       }
@@ -1183,7 +1427,7 @@ struct Engine {
     double F[9];
 #pragma unroll
     for (int q = 0; q < 9; ++q) F[q] = model[q];
-    const double ratio = Est::KIND == 1 ? 0.5 : 0.0;
+    const double ratio = Est::KIND == 1 ? 0.5 : (Est::KIND == 3 ? 0.1 : 0.0);
     const int min_n = max(Est::M, (int)((double)cnt * ratio));
     int c = 0;
     for (int k = threadIdx.x; k < cnt; k += GCR_BLOCK)
@@ -1524,7 +1768,9 @@ struct Engine {
     int n = materialise(cont[off], list);
     copy_model(sh.work_model, sh.best_model);
     bool irls_applied = false;
-    const bool ok = irls(list, n, spare);
+    bool ok;
+    if constexpr (Est::LO_MAXSOL > 1) ok = irls_multi(list, n, spare);
+    else ok = irls(list, n, spare);
     if (ok) {
       // the container now holds the inliers of the IRLS model
       copy_model(sh.cont_model[off], sh.work_model);
@@ -1539,7 +1785,21 @@ struct Engine {
         off = idx;
       }
     }
-    if (!irls_applied) {
+    if (Est::LO_MAXSOL > 1 && !irls_applied) {
+      // one fit on the first best.count points of the container; every model
+      // better than the run's best takes the other container
+      const int nm = fit_cta_multi(list, best.count < n ? best.count : n, 0, true);
+      for (int q = 0; q < nm; ++q) {
+        const int idx = off ^ 1;
+        const Score sc = exact_score(sh.multi_models + 9 * q, nullptr);
+        copy_model(sh.cont_model[idx], sh.multi_models + 9 * q);
+        cont[idx] = {sh.cont_model[idx], sc.count};
+        if (best.value < sc.value) {
+          copy_model(sh.best_model, sh.multi_models + 9 * q);
+          off = idx;
+        }
+      }
+    } else if (!irls_applied) {
       // one least-squares fit on the first best.count points of the container
       if (fit_cta(list, best.count < n ? best.count : n, 0)) {
         const int idx = off ^ 1;
@@ -1580,6 +1840,70 @@ struct Engine {
             cnt = sc.count;
           }
         }
+      } else {
+        sync();
+        if (threadIdx.x < 9) sh.best_model[threadIdx.x] = (threadIdx.x % 4 == 0) ? 1.0 : 0.0;
+        sync();
+      }
+    }
+    if constexpr (Est::KIND == 3) {
+      // findEssentialMatrix_ epilogue (gcransac_python.cpp:2770-2828): the
+      // essential-matrix bundle adjustment of the final inliers (Stewenius
+      // start, every cheirality-consistent pose refined), each result kept
+      // when its MSAC score beats the best so far; at most 5 inliers give
+      // the identity. Weights by inlier position.
+      if (cnt > 5) {
+        double Eb[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) Eb[q] = sh.best_model[q];
+        for (int k = threadIdx.x; k < cnt; k += GCR_BLOCK)
+          slot.dres[k] = fmax(0.0, 1.0 - Est::r2_f64(pts64 + 4 * list[k], Eb) / t2);
+        sync();
+        const int nm = fit_cta_multi(list, cnt, 2, false);
+        double x1[3], x2[3];
+        {
+          const double* p0 = pts64 + 4 * list[0];
+          x1[0] = p0[0]; x1[1] = p0[1]; x1[2] = 1.0;
+          x2[0] = p0[2]; x2[1] = p0[3]; x2[2] = 1.0;
+          const double n1 = sqrt(x1[0] * x1[0] + x1[1] * x1[1] + 1.0);
+          const double n2 = sqrt(x2[0] * x2[0] + x2[1] * x2[1] + 1.0);
+          for (int i = 0; i < 3; ++i) {
+            x1[i] /= n1;
+            x2[i] /= n2;
+          }
+        }
+        // the bundle adjustment reads the original inliers (ba, ba_n) while
+        // accepted results go to the two other lists
+        const int* ba = list;
+        const int ba_n = cnt;
+        int* cur = list;
+        int* tmp = spare;
+        double Em[9 * Shared<Est>::kMulti];
+        for (int q = 0; q < 9 * nm; ++q) Em[q] = sh.multi_models[q];
+        for (int q = 0; q < nm; ++q) {
+          double Eq[9];
+#pragma unroll
+          for (int e = 0; e < 9; ++e) Eq[e] = Em[9 * q + e];
+          ess::Pose poses[4];
+          const int np = ess::poses_from_essential(Eq, x1, x2, poses);
+          for (int v = 0; v < np; ++v) {
+            ess::Pose P = poses[v];
+            refine_relpose_cta(ba, ba_n, P);
+            ess::essential_from_pose(P, Eq);
+            sync();
+            if (threadIdx.x < 9) sh.fit_model[threadIdx.x] = Eq[threadIdx.x];
+            sync();
+            const Score sc = exact_score(sh.fit_model, tmp);
+            if (final_score < sc.value) {
+              final_score = sc.value;
+              copy_model(sh.best_model, sh.fit_model);
+              cur = tmp;
+              tmp = (tmp == spare) ? slot.list0 : spare;
+              cnt = sc.count;
+            }
+          }
+        }
+        list = cur;
       } else {
         sync();
         if (threadIdx.x < 9) sh.best_model[threadIdx.x] = (threadIdx.x % 4 == 0) ? 1.0 : 0.0;

@@ -167,6 +167,7 @@ struct FundamentalModel {
   static constexpr int KIND = 1;
   static constexpr int M = 7;
   static constexpr int MAXSOL = 3;
+  static constexpr int LO_MAXSOL = 1;
   static constexpr int NONMIN = 7;
   static constexpr int INLIER_LIMIT = 7 * M;
   static constexpr int SAMPLE_CAP = INLIER_LIMIT;
@@ -707,6 +708,7 @@ struct PlaneParallaxModel {
   static constexpr int KIND = 2;
   static constexpr int M = 2;
   static constexpr int MAXSOL = 1;
+  static constexpr int LO_MAXSOL = 1;
   static constexpr int NONMIN = 8;
   static constexpr int INLIER_LIMIT = 7 * M;
   static constexpr int SAMPLE_CAP = INLIER_LIMIT;

@@ -17,6 +17,7 @@ struct HomographyModel {
   static constexpr bool CTA_VALIDITY = false;
   static constexpr int M = 4;          // minimal sample size
   static constexpr int MAXSOL = 1;     // models per minimal sample
+  static constexpr int LO_MAXSOL = 1;  // models per non-minimal fit
   static constexpr int NONMIN = 4;     // smallest non-minimal sample
   static constexpr int INLIER_LIMIT = 7 * M;
   static constexpr bool WEIGHTED = true;

@@ -29,9 +29,12 @@ const KindOps* homography_ops();
 const KindOps* fundamental_ops();
 const KindOps* essential_ops();
 
+struct PairDesc;
+
 // K^-1 normalisation of essential-matrix correspondences (utils.h:65-103 of
-// the reference), one thread per correspondence.
-cudaError_t launch_normalise_essential(const double* corr, const double* kinv, const long long* pair_of_row,
-                                       long long rows, double* out, cudaStream_t stream);
+// the reference): kinv holds K1^-1 then K2^-1 (row-major) per pair; one CTA
+// per pair.
+cudaError_t launch_normalise_essential(const double* corr, const double* kinv, const PairDesc* pairs, int num_pairs,
+                                       double* out, cudaStream_t stream);
 
 }  // namespace gcr

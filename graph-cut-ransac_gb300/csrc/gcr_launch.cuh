@@ -94,7 +94,7 @@ template <class Est>
 size_t slot_bytes(int max_n, int sort_cap, bool light = false) {
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   size_t s = 0;
-  s += al(sizeof(double) * 9 * Shared<Est>::kModels);
+  s += al(sizeof(double) * 9 * (Shared<Est>::kModels + Shared<Est>::kStage));
   s += al(sizeof(float) * 12 * Shared<Est>::kModels);
   s += al(sizeof(int) * GCR_BLOCK * Est::SAMPLE_CAP);
   s += al(sizeof(int) * GCR_BLOCK * Est::M);
@@ -120,7 +120,7 @@ Slot carve_slot(unsigned char* base, int max_n, int sort_cap, bool light = false
   Slot s{};
   unsigned char* p = base;
   auto take = [&](size_t b) { unsigned char* r = p; p += al(b); return r; };
-  s.models64 = (double*)take(sizeof(double) * 9 * Shared<Est>::kModels);
+  s.models64 = (double*)take(sizeof(double) * 9 * (Shared<Est>::kModels + Shared<Est>::kStage));
   s.models32 = (float*)take(sizeof(float) * 12 * Shared<Est>::kModels);
   s.samples = (int*)take(sizeof(int) * GCR_BLOCK * Est::SAMPLE_CAP);
   s.bsamples = (int*)take(sizeof(int) * GCR_BLOCK * Est::M);

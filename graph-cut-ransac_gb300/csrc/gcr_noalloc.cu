@@ -171,6 +171,10 @@ extern "C" gcr_status gcr_find_homography_device_noalloc(const double* d_corr, i
   pd.centre[1] = 0.5 * size->h1;
   pd.centre[2] = 0.5 * size->w2;
   pd.centre[3] = 0.5 * size->h2;
+  pd.img[0] = size->w1;
+  pd.img[1] = size->h1;
+  pd.img[2] = size->w2;
+  pd.img[3] = size->h2;
   pd.seed = seed;
 
   gcr::Workspace ws{};

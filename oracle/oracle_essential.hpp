@@ -137,22 +137,17 @@ inline const MonoList& mono_cubic_grevlex() {
   return m;
 }
 
-// c (over lc) += sign * (a (over la) * b (over lb)): for every output monomial
-// the products are summed in the order of a's monomials, then b's, and the
-// sum is added to c once.
+// c (over lc) += sign * (a (over la) * b (over lb)): the terms are added one
+// by one in the order of a's monomials, then b's.
 inline void poly_mul_acc(const double* a, const MonoList& la, const double* b, const MonoList& lb, double* c,
                          const MonoList& lc, double sign = 1.0) {
-  double sum[20];
-  int cnt[20];
-  for (int k = 0; k < lc.n; ++k) cnt[k] = 0;
-  for (int i = 0; i < la.n; ++i)
+  for (int i = 0; i < la.n; ++i) {
+    const double ai = sign * a[i];
     for (int j = 0; j < lb.n; ++j) {
       const int k = lc.index(la.e[i][0] + lb.e[j][0], la.e[i][1] + lb.e[j][1], la.e[i][2] + lb.e[j][2]);
-      if (cnt[k]++ == 0) sum[k] = a[i] * b[j];
-      else sum[k] += a[i] * b[j];
+      c[k] += ai * b[j];
     }
-  for (int k = 0; k < lc.n; ++k)
-    if (cnt[k]) c[k] += sign * sum[k];
+  }
 }
 
 // ---------------------------------------------------------------------------
