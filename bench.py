@@ -45,16 +45,31 @@ WORKLOADS = {
     # solver + graph-cut LO, DEGENSAC on
     "fundamental": dict(kind=_abi.GCR_FUNDAMENTAL, n=5000, ratio=0.25, threshold=0.75, sampler=2, grid=8,
                         lam=0.975, pairs=608),
+    # calibrated pairs (f = 800 px, scene as above) with log-uniform 200-8000
+    # correspondences and inlier ratio uniform in 10-70 % (sigma 0.5 px),
+    # threshold 0.75 px (divided by the focal length), uniform sampler, 8^4
+    # grid, lambda 0.1, 5-point solver + graph-cut LO, MSAC scoring
+    "essential": dict(kind=_abi.GCR_ESSENTIAL, n=(200, 8000), ratio=(0.1, 0.7), threshold=0.75, sampler=0, grid=8,
+                      lam=0.1, pairs=1024),
 }
 
 
 def build_pairs(workload, pairs, seed0):
+    """Returns (corr, offsets, sizes, ground truths, K [P, 18] or None)."""
     w = WORKLOADS[workload]
-    corr, sizes, gts = [], [], []
+    corr, sizes, gts, Ks = [], [], [], []
+    if workload == "essential":
+        rng = np.random.Generator(np.random.PCG64(seed0 + 7919))
+        ns = np.exp(rng.uniform(np.log(w["n"][0]), np.log(w["n"][1]), pairs)).astype(int)
+        ratios = rng.uniform(w["ratio"][0], w["ratio"][1], pairs)
     for i in range(pairs):
         if workload == "homography":
             pr = S.homography_pair(seed0 + i, n=w["n"], inlier_ratio=w["ratio"])
             gts.append(pr["H_gt"])
+        elif workload == "essential":
+            pr = S.two_view_pair(seed0 + i, n=int(ns[i]), inlier_ratio=float(ratios[i]))
+            gts.append(pr)
+            Ks.append(np.concatenate([pr["K"].ravel(), pr["K"].ravel()]))
         else:
             pr = S.two_view_pair(seed0 + i, n=w["n"], inlier_ratio=w["ratio"])
             gts.append(pr)
@@ -62,7 +77,8 @@ def build_pairs(workload, pairs, seed0):
         sizes.append(pr["size"])
     offsets = np.zeros(pairs + 1, np.int64)
     offsets[1:] = np.cumsum([len(c) for c in corr])
-    return np.ascontiguousarray(np.concatenate(corr), np.float64), offsets, np.array(sizes), gts
+    K = np.ascontiguousarray(np.array(Ks), np.float64) if Ks else None
+    return np.ascontiguousarray(np.concatenate(corr), np.float64), offsets, np.array(sizes), gts, K
 
 
 def params_for(workload, seed=0):
@@ -85,6 +101,8 @@ def model_errors(workload, models, gts, limit=64):
         return [S.homography_error(m / m[2, 2] if abs(m[2, 2]) > 1e-12 else m, g) for m, g in zip(models, gts)]
     if workload == "fundamental":
         return [S.fundamental_error(m, g, n=200) for m, g in list(zip(models, gts))[:limit]]
+    if workload == "essential":
+        return [S.essential_error(m, g) for m, g in zip(models, gts)]
     return []
 
 
@@ -154,7 +172,7 @@ def fp32_peak_tflops(torch):
     return best
 
 
-def cpu_baseline(workload, corr, offsets, sizes, p, target_s=10.0, max_pairs=1 << 30):
+def cpu_baseline(workload, corr, offsets, sizes, p, K=None, target_s=10.0, max_pairs=1 << 30):
     """The oracle (CPU restatement of the reference path) on all host cores,
     on a bounded sample of the same workload. Returns (pairs/s, cores, sample)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -170,8 +188,8 @@ def cpu_baseline(workload, corr, offsets, sizes, p, target_s=10.0, max_pairs=1 <
         off = np.zeros(k + 1, np.int64)
         off[1:] = np.cumsum(lens)
         c = np.concatenate([corr[offsets[i]:offsets[i + 1]] for i in idx])
-        _, _, _, t = oracle.find_batch(kind, c, off, size_array(sizes[idx]), p,
-                                       seeds=idx.astype(np.uint64), threads=threads)
+        _, _, _, t = oracle.find_batch(kind, c, off, size_array(sizes[idx]), p, seeds=idx.astype(np.uint64),
+                                       K=None if K is None else np.ascontiguousarray(K[idx]), threads=threads)
         return k, t
 
     k, t = run(max(2 * threads, 8))
@@ -198,7 +216,12 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     w = WORKLOADS[args.workload]
     P = args.pairs or w["pairs"]
-    cfg = {"workload": f"{args.workload}: {P} pairs/step x {w['n']} correspondences, {int(w['ratio']*100)}% inliers",
+    if args.workload == "essential":
+        desc = (f"{args.workload}: {P} calibrated pairs/step x {w['n'][0]}-{w['n'][1]} (log-uniform) correspondences, "
+                f"{int(w['ratio'][0]*100)}-{int(w['ratio'][1]*100)}% inliers, MSAC")
+    else:
+        desc = f"{args.workload}: {P} pairs/step x {w['n']} correspondences, {int(w['ratio']*100)}% inliers"
+    cfg = {"workload": desc,
            "pairs_per_step": P, "correspondences": w["n"], "threshold": w["threshold"], "sampler": w["sampler"],
            "grid": w["grid"], "spatial_coherence_weight": w["lam"], "l2": "flushed between steps (256 MiB write)",
            "parallelism": f"replicas x{world}"}
@@ -206,13 +229,13 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        corr, offsets, sizes, gts = build_pairs(args.workload, P, 0)
+        corr, offsets, sizes, gts, K = build_pairs(args.workload, P, 0)
         p = params_for(args.workload)
         for _ in range(args.warmup):
-            cpu_baseline(args.workload, corr, offsets, sizes, p, target_s=1.0, max_pairs=64)
+            cpu_baseline(args.workload, corr, offsets, sizes, p, K, target_s=1.0, max_pairs=64)
         vals = []
         for _ in range(args.steps):
-            v, cores, sample = cpu_baseline(args.workload, corr, offsets, sizes, p, target_s=8.0)
+            v, cores, sample = cpu_baseline(args.workload, corr, offsets, sizes, p, K, target_s=8.0)
             vals.append(v)
         v = float(np.median(vals))
         print(json.dumps({"metric": METRIC, "value": v, "unit": "pairs/s", "n_gpus": args.gpus,
@@ -232,7 +255,7 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
 
     lib = _abi.load()
-    corr, offsets, sizes, gts = build_pairs(args.workload, P, 1000003 * rank)
+    corr, offsets, sizes, gts, K = build_pairs(args.workload, P, 1000003 * rank)
     p = params_for(args.workload)
     kind = w["kind"]
     seeds = np.arange(P, dtype=np.uint64) + np.uint64(P * rank)
@@ -247,7 +270,7 @@ def main():
     stream = torch.cuda.current_stream()
 
     def step():
-        rc = lib.gcr_batch_run_device(ctx, kind, P, ctypes.c_void_p(d_corr.data_ptr()), _abi.ptr(offsets), None,
+        rc = lib.gcr_batch_run_device(ctx, kind, P, ctypes.c_void_p(d_corr.data_ptr()), _abi.ptr(offsets), _abi.ptr(K),
                                       _abi.ptr(szs), ctypes.byref(p), _abi.ptr(seeds),
                                       ctypes.c_void_p(d_models.data_ptr()), ctypes.c_void_p(d_masks.data_ptr()),
                                       ctypes.c_void_p(d_stats.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
@@ -294,7 +317,7 @@ def main():
     h_stats = torch.zeros(P * _abi.STATS_DTYPE.itemsize, dtype=torch.uint8).pin_memory()
 
     def e2e_step():
-        rc = lib.gcr_find_batch(kind, P, ctypes.c_void_p(h_corr.data_ptr()), _abi.ptr(offsets), None,
+        rc = lib.gcr_find_batch(kind, P, ctypes.c_void_p(h_corr.data_ptr()), _abi.ptr(offsets), _abi.ptr(K),
                                 _abi.ptr(szs), ctypes.byref(p), _abi.ptr(seeds),
                                 ctypes.c_void_p(h_models.data_ptr()), ctypes.c_void_p(h_masks.data_ptr()),
                                 ctypes.c_void_p(h_stats.data_ptr()))
@@ -341,7 +364,7 @@ def main():
         "clocks": clk,
     }
     if not args.no_cpu_baseline and world == 1:
-        v, cores, sample = cpu_baseline(args.workload, corr, offsets, sizes, p)
+        v, cores, sample = cpu_baseline(args.workload, corr, offsets, sizes, p, K)
         line["cpu_baseline"] = {"value": v, "unit": "pairs/s", "cores": cores, "kind": "port", "sample": sample}
     print(json.dumps(line))
     lib.gcr_context_destroy(ctx)

@@ -137,7 +137,11 @@ struct Container {
 
 template <class Est>
 struct Shared {
-  static constexpr int kModels = GCR_BLOCK * Est::MAXSOL + kLoRegion;
+  // local-optimisation region: one model per trial, or the models of 25
+  // trials when a non-minimal fit returns up to ten (a larger region would
+  // leave room for only one CTA per SM)
+  static constexpr int kLo = kLoRegion;
+  static constexpr int kModels = GCR_BLOCK * Est::MAXSOL + kLo;
   // staging of per-trial model lists of multi-model non-minimal fits (global only)
   static constexpr int kStage = Est::LO_MAXSOL > 1 ? GCR_BLOCK : 0;
   static constexpr int kMulti = Est::LO_MAXSOL;
@@ -1162,42 +1166,53 @@ struct Engine {
   }
 
   // Local-optimisation trials whose fits return several models: trials run
-  // one per thread in chunks of kLoRegion / LO_MAXSOL; each chunk's models are
+  // one per thread (trial u on thread u), in chunks of kLo / LO_MAXSOL; each
+  // chunk's models are
   // compacted in trial order into the local-optimisation region, scored in
   // FP32 and replayed in order.
   __device__ void lo_trials_multi(int nL, int ss, const int* L, int trials, Score& max_score, bool& updated) {
     if constexpr (Est::LO_MAXSOL > 1) {
-      constexpr int chunk_cap = kLoRegion / Est::LO_MAXSOL;
-      constexpr int kstage = kBatchModels + kLoRegion;
+      constexpr int chunk_cap = Shared<Est>::kLo / Est::LO_MAXSOL;
+      constexpr int kstage = kBatchModels + Shared<Est>::kLo;
       const int kb = kBatchModels;
+      const int u = threadIdx.x;  // this thread's trial within the chunk
       for (int t0 = 0; t0 < trials; t0 += chunk_cap) {
         const int nt = min(chunk_cap, trials - t0);
         int cnt = 0;
-        if (threadIdx.x < nt) {
-          int* smp = slot.samples + threadIdx.x * Est::SAMPLE_CAP;
-          DrawStream ds(pd.seed, prm.stream_lo, (uint64_t)(lo_calls + t0 + threadIdx.x));
+        if (u < nt) {
+          int* smp = slot.samples + u * Est::SAMPLE_CAP;
+          DrawStream ds(pd.seed, prm.stream_lo, (uint64_t)(lo_calls + t0 + u));
           if (unique_set(ds, smp, ss, 0, (uint32_t)(nL - 1))) {
             for (int q = 0; q < ss; ++q) smp[q] = L[smp[q]];
-            cnt = Est::fit_thread_multi(pts64, smp, ss, slot.models64 + 9 * (kstage + threadIdx.x * Est::LO_MAXSOL));
+            cnt = Est::fit_thread_multi(pts64, smp, ss, slot.models64 + 9 * (kstage + u * Est::LO_MAXSOL));
           }
+          sh.lo_ok[u] = cnt;
         }
-        int total;
-        const int base = block_exclusive_scan(cnt, sh.red_i, &total);
-        if (threadIdx.x < nt) {
-          sh.lo_ok[threadIdx.x] = cnt;
-          sh.lo_base[threadIdx.x] = base;
+        sync();
+        if (threadIdx.x == 0) {
+          int acc = 0;
+          for (int v = 0; v < nt; ++v) {
+            sh.lo_base[v] = acc;
+            acc += sh.lo_ok[v];
+          }
+          sh.multi_count = acc;
         }
-        for (int q = 0; q < cnt; ++q) {
-          const double* src = slot.models64 + 9 * (kstage + threadIdx.x * Est::LO_MAXSOL + q);
-          double* dst = slot.models64 + 9 * (kb + base + q);
+        sync();
+        const int total = sh.multi_count;
+        if (u < nt) {
+          const int base = sh.lo_base[u];
+          for (int q = 0; q < cnt; ++q) {
+            const double* src = slot.models64 + 9 * (kstage + u * Est::LO_MAXSOL + q);
+            double* dst = slot.models64 + 9 * (kb + base + q);
 #pragma unroll
-          for (int e = 0; e < 9; ++e) dst[e] = src[e];
-          put_f32(kb + base + q);
+            for (int e = 0; e < 9; ++e) dst[e] = src[e];
+            put_f32(kb + base + q);
+          }
         }
         sync();
         score_models_f32(kb, total);
-        for (int u = 0; u < nt; ++u) {
-          const int nm = sh.lo_ok[u], b0 = sh.lo_base[u];
+        for (int v = 0; v < nt; ++v) {
+          const int nm = sh.lo_ok[v], b0 = sh.lo_base[v];
           for (int q = 0; q < nm; ++q) {
             ++models_scored;
             const int k = kb + b0 + q;
