@@ -48,9 +48,9 @@ WORKLOADS = {
     # calibrated pairs (f = 800 px, scene as above) with log-uniform 200-8000
     # correspondences and inlier ratio uniform in 10-70 % (sigma 0.5 px),
     # threshold 0.75 px (divided by the focal length), uniform sampler, 8^4
-    # grid, lambda 0.1, 5-point solver + graph-cut LO, MSAC scoring
+    # grid, lambda 0.1, 5-point solver + graph-cut LO, MAGSAC++ scoring
     "essential": dict(kind=_abi.GCR_ESSENTIAL, n=(200, 8000), ratio=(0.1, 0.7), threshold=0.75, sampler=0, grid=8,
-                      lam=0.1, pairs=1024),
+                      lam=0.1, pairs=1024, scoring=_abi.GCR_SCORING_MAGSAC),
 }
 
 
@@ -85,7 +85,8 @@ def params_for(workload, seed=0):
     w = WORKLOADS[workload]
     return _abi.Params(threshold=w["threshold"], confidence=0.99, spatial_coherence_weight=w["lam"],
                        neighborhood_size=w["grid"], max_iterations=10000, min_iterations=50,
-                       sampler=w["sampler"], neighborhood=0, lo_number=50, seed=seed)
+                       sampler=w["sampler"], neighborhood=0, lo_number=50, seed=seed,
+                       scoring=w.get("scoring", _abi.GCR_SCORING_MSAC))
 
 
 def size_array(sizes):
@@ -218,12 +219,14 @@ def main():
     P = args.pairs or w["pairs"]
     if args.workload == "essential":
         desc = (f"{args.workload}: {P} calibrated pairs/step x {w['n'][0]}-{w['n'][1]} (log-uniform) correspondences, "
-                f"{int(w['ratio'][0]*100)}-{int(w['ratio'][1]*100)}% inliers, MSAC")
+                f"{int(w['ratio'][0]*100)}-{int(w['ratio'][1]*100)}% inliers, MAGSAC++")
     else:
         desc = f"{args.workload}: {P} pairs/step x {w['n']} correspondences, {int(w['ratio']*100)}% inliers"
     cfg = {"workload": desc,
            "pairs_per_step": P, "correspondences": w["n"], "threshold": w["threshold"], "sampler": w["sampler"],
-           "grid": w["grid"], "spatial_coherence_weight": w["lam"], "l2": "flushed between steps (256 MiB write)",
+           "grid": w["grid"], "spatial_coherence_weight": w["lam"],
+           "scoring": "MAGSAC++" if w.get("scoring") == _abi.GCR_SCORING_MAGSAC else "MSAC",
+           "l2": "flushed between steps (256 MiB write)",
            "parallelism": f"replicas x{world}"}
 
     if args.impl == "reference":

@@ -80,6 +80,7 @@ struct gcr_context {
   DevBuf pairs, slots_meta, slot_mem, pts32, ticket, norm_pts, kinv, row_pair, phase;
   // staging of the host-buffer entry points
   DevBuf corr, models, masks, stats;
+  DevBuf magsac;  // the MAGSAC++ weight table, uploaded on first use
   int slot_kind = -1, slot_max_n = 0, slot_count = 0;
   bool prepared[3] = {false, false, false};
 };
@@ -98,7 +99,8 @@ gcr_status check_params(gcr_model_kind kind, const gcr_params* p) {
   if (p->sampler != GCR_SAMPLER_UNIFORM && p->sampler != GCR_SAMPLER_PROSAC && p->sampler != GCR_SAMPLER_PNAPSAC)
     return fail(GCR_UNSUPPORTED,
                 "sampler %d is not provided by the device engine (0 uniform, 1 PROSAC, 2 P-NAPSAC)", p->sampler);
-  if (p->scoring != GCR_SCORING_MSAC) return fail(GCR_UNSUPPORTED, "scoring %d is not provided", p->scoring);
+  if (p->scoring != GCR_SCORING_MSAC && p->scoring != GCR_SCORING_MAGSAC)
+    return fail(GCR_UNSUPPORTED, "scoring %d is not provided (0 MSAC, 1 MAGSAC++)", p->scoring);
   const bool pairwise = p->spatial_coherence_weight > 0;
   if (p->neighborhood != GCR_NEIGHBORHOOD_GRID && pairwise)
     return fail(GCR_UNSUPPORTED, "only the grid neighbourhood (0) is provided with a spatial coherence term");
@@ -106,6 +108,21 @@ gcr_status check_params(gcr_model_kind kind, const gcr_params* p) {
     return fail(GCR_INVALID_ARG, "neighborhood_size must be >= 1 for the grid");
   (void)kind;
   return GCR_OK;
+}
+
+// MAGSAC++ weight table (MAGSACScoringFunction, scoring_function.h:263-334):
+// the upper incomplete gamma function Gamma(1.5, x / 1000) for x = 0..36000,
+// which equals sqrt(pi)/2 erfc(sqrt(x/1000)) + sqrt(x/1000) exp(-x/1000).
+const std::vector<double>& magsac_table() {
+  static const std::vector<double> g = [] {
+    std::vector<double> t(36001);
+    for (int i = 0; i <= 36000; ++i) {
+      const double x = i / 1000.0;
+      t[i] = std::sqrt(M_PI) * 0.5 * std::erfc(std::sqrt(x)) + std::sqrt(x) * std::exp(-x);
+    }
+    return t;
+  }();
+  return g;
 }
 
 int pow2_at_least(int n) {
@@ -174,7 +191,7 @@ gcr_status gcr_context_create(gcr_context** ctx) {
 gcr_status gcr_context_destroy(gcr_context* c) {
   if (!c) return GCR_OK;
   for (DevBuf* b : {&c->pairs, &c->slots_meta, &c->slot_mem, &c->pts32, &c->ticket, &c->norm_pts, &c->kinv,
-                    &c->row_pair, &c->corr, &c->models, &c->masks, &c->stats})
+                    &c->row_pair, &c->corr, &c->models, &c->masks, &c->stats, &c->magsac})
     b->release();
   delete c;
   return GCR_OK;
@@ -344,6 +361,18 @@ gcr_status gcr_batch_run_device(gcr_context* c, gcr_model_kind kind, int64_t num
   prm.stream_main = 1;  // STREAM_MAIN
   prm.stream_lo = 2;    // STREAM_LO
   prm.pp_h = nullptr;
+  prm.mag_table = nullptr;
+  prm.mag_c2dof = 0.25 * std::pow(2.0, 1.5);
+  prm.mag_gamma_k = 0.0036572608340910764;
+  prm.mag_gamma_diff = std::tgamma(1.5) - prm.mag_gamma_k;
+  if (params->scoring == GCR_SCORING_MAGSAC) {
+    if (c->magsac.cap == 0) {
+      const std::vector<double>& g = magsac_table();
+      CUDA_TRY(c->magsac.ensure(sizeof(double) * g.size()));
+      CUDA_TRY(cudaMemcpy(c->magsac.p, g.data(), sizeof(double) * g.size(), cudaMemcpyHostToDevice));
+    }
+    prm.mag_table = (const double*)c->magsac.p;
+  }
   CUDA_TRY(ops->launch(grid, s, ws, prm));
   g_last_launches = kind == GCR_ESSENTIAL ? 2 : 1;
   return GCR_OK;

@@ -42,6 +42,7 @@ constexpr int kLoRegion = GCR_BLOCK;    // model slots reserved for local optimi
 enum PairStatus { ST_OK = 0, ST_NO_MODEL = 3, ST_TIMEOUT = 5, ST_CAPACITY = 6, ST_UNSUPPORTED = 7 };
 
 enum { SAMPLER_UNIFORM = 0, SAMPLER_PROSAC = 1, SAMPLER_PNAPSAC = 2 };
+enum { SCORING_MSAC = 0, SCORING_MAGSAC = 1 };
 
 struct EngineParams {
   double confidence;
@@ -60,6 +61,13 @@ struct EngineParams {
   uint32_t stream_main;
   uint32_t stream_lo;
   const double* pp_h;   // homography of the plane-and-parallax solver (nested runs)
+  // MAGSAC++ scoring (scoring == 1): the weight table Gamma(1.5, x / 1000),
+  // x = 0..36000, and the constants C 2^1.5, Gamma(1.5) - gamma_k, gamma_k,
+  // all evaluated on the host
+  const double* mag_table;
+  double mag_c2dof;
+  double mag_gamma_diff;
+  double mag_gamma_k;
 };
 
 // Per-pair inputs prepared on the device.
@@ -208,6 +216,10 @@ struct Engine {
   int N;
   double t2;
   double log_prob;
+  // MAGSAC++ scoring (MAGSACScoringFunction::getScore, scoring_function.h:
+  // 237-348): inlier iff r <= threshold, weight from the gamma table
+  bool mag = false;
+  double mag_thr = 0, mag_thr2 = 0, mag_sq2 = 0, mag_oos = 0, mag_w0 = 0;
   int status = ST_OK;
   int flags = 0;
 
@@ -229,6 +241,14 @@ struct Engine {
     const double tt = 1.5 * pd.threshold;
     t2 = tt * tt;
     log_prob = log(1.0 - prm.confidence);
+    if (prm.scoring == SCORING_MAGSAC && prm.mag_table != nullptr) {
+      mag = true;
+      mag_thr = pd.threshold;
+      mag_thr2 = mag_thr * mag_thr;
+      mag_sq2 = mag_thr * mag_thr * 2.0;
+      mag_oos = prm.mag_c2dof / mag_thr;
+      mag_w0 = mag_oos * prm.mag_gamma_diff;
+    }
     cont[0] = {nullptr, 0};
     cont[1] = {nullptr, 0};
   }
@@ -265,6 +285,8 @@ struct Engine {
   __device__ void score_models_f32(int k0, int K) {
     const float tf = (float)sqrt(t2);
     const float t2f = (float)t2;
+    // the FP32 thresholds are rounded: widen every band by their rounding
+    const float slack = 1.2e-7f * (mag ? (float)mag_thr2 : t2f);
     const int tid = threadIdx.x;
     for (int base = 0; base < K; base += GCR_BLOCK) {
       const int Kb = min(GCR_BLOCK, K - base);
@@ -285,31 +307,67 @@ struct Engine {
         const int i0 = slice * chunk, i1 = min(N, i0 + chunk);
         float inner = 0.f;
         int inner_n = 0;
-        for (int i = i0; i < i1; ++i) {
-          const float4 p = pts32[i];
-          float it;
-          const float r2 = Est::r2_f32(p, h, it);
-          const float e = fmaf(cm, fabsf(it), cm);
-          const float eb = fmaf(e, e, 2.f * tf * e);
-          const float dlt = r2 - t2f;
-          if (dlt < -eb) {
-            ++cnt;
-            inner += r2;
-            err += eb;
-          } else if (!(dlt > eb)) {  // inside the band, or NaN
-            const double r2d = Est::r2_f64(pts64 + 4 * i, m64);
-            if (r2d < t2) {
+        if (!mag) {
+          for (int i = i0; i < i1; ++i) {
+            const float4 p = pts32[i];
+            float it;
+            const float r2 = Est::r2_f32(p, h, it);
+            const float e = fmaf(cm, fabsf(it), cm);
+            const float eb = fmaf(e, e, 2.f * tf * e) + slack;
+            const float dlt = r2 - t2f;
+            if (dlt < -eb) {
               ++cnt;
-              inner += (float)r2d;
+              inner += r2;
+              err += eb;
+            } else if (!(dlt > eb)) {  // inside the band, or NaN
+              const double r2d = Est::r2_f64(pts64 + 4 * i, m64);
+              if (r2d < t2) {
+                ++cnt;
+                inner += (float)r2d;
+              }
+            }
+            if (++inner_n == 64) {
+              sum += inner;
+              inner = 0.f;
+              inner_n = 0;
             }
           }
-          if (++inner_n == 64) {
-            sum += inner;
-            inner = 0.f;
-            inner_n = 0;
+          sum += inner;
+        } else {
+          // MAGSAC++: sum of normalised weights; the FP32 residual may move the
+          // table index by 1e4 eb / (2 thr^2) + 1 bins, each worth at most
+          // 5e-4 of normalised weight
+          const float mt = (float)mag_thr, mt2 = (float)mag_thr2;
+          const float xs = (float)(1e4 / mag_sq2);
+          const float gk = (float)prm.mag_gamma_k, gdi = (float)(1.0 / prm.mag_gamma_diff);
+          for (int i = i0; i < i1; ++i) {
+            const float4 p = pts32[i];
+            float it;
+            const float r2 = Est::r2_f32(p, h, it);
+            const float e = fmaf(cm, fabsf(it), cm);
+            const float eb = fmaf(e, e, 2.f * mt * e) + slack;
+            const float dlt = r2 - mt2;
+            if (dlt < -eb) {
+              ++cnt;
+              const int x = min(36000, (int)roundf(r2 * xs));
+              inner += ((float)prm.mag_table[x] - gk) * gdi;
+              err += fmaf(eb, xs, 1.f) * 5e-4f;
+            } else if (!(dlt > eb)) {
+              const double r2d = Est::r2_f64(pts64 + 4 * i, m64);
+              const double r = sqrt(r2d);
+              if (!(r > mag_thr)) {
+                ++cnt;
+                inner += (float)mag_weight(r);
+              }
+            }
+            if (++inner_n == 64) {
+              sum += inner;
+              inner = 0.f;
+              inner_n = 0;
+            }
           }
+          sum += inner;
         }
-        sum += inner;
       }
       sh.s_cnt[tid] = cnt;
       sh.s_sum[tid] = sum;
@@ -325,9 +383,14 @@ struct Engine {
         }
         const int k = k0 + base + tid;
         sh.mcount[k] = c;
-        sh.mscore[k] = c == 0 ? 0.f : (c * t2f - s) / t2f;
-        // per-point residual error + FP32 summation error + the final division
-        sh.mbound[k] = (e + 2.f * s * (64.f + (float)N / 64.f) * 5.97e-8f) / t2f + 4e-7f * c + 1e-6f;
+        if (!mag) {
+          sh.mscore[k] = c == 0 ? 0.f : (c * t2f - s) / t2f;
+          // per-point residual error + FP32 summation error + the final division
+          sh.mbound[k] = (e + 2.f * s * (64.f + (float)N / 64.f) * 5.97e-8f) / t2f + 4e-7f * c + 1e-6f;
+        } else {
+          sh.mscore[k] = s;
+          sh.mbound[k] = e + 2.f * s * (64.f + (float)N / 64.f) * 5.97e-8f + 1e-5f * c + 1e-6f;
+        }
       }
       sync();
     }
@@ -344,7 +407,22 @@ struct Engine {
   // writes the inlier list in index order. Points whose FP32 residual lies
   // above the threshold by more than its error bound are outliers without an
   // FP64 evaluation; all others are decided and summed in FP64.
-  __device__ Score exact_score(const double* model, int* list, const float* m32 = nullptr) {
+  // MAGSAC++ weight of a correspondence at residual r <= threshold, divided by
+  // the weight at zero residual.
+  __device__ __forceinline__ double mag_weight(double r) const {
+    double w;
+    if (r < 2.220446049250313e-16) {
+      w = mag_w0;
+    } else {
+      long long x = (long long)round(1e4 * (r * r) / mag_sq2);
+      if (36000 < x) x = 36000;
+      w = mag_oos * (prm.mag_table[x] - prm.mag_gamma_k);
+    }
+    return w / mag_w0;
+  }
+
+  __device__ Score exact_score(const double* model, int* list, const float* m32 = nullptr, bool msac = false) {
+    if (mag && !msac) return exact_score_magsac(model, list, m32);
     if (m32 == nullptr) {
       prepare_shared_f32(model);
       m32 = sh.mf32;
@@ -367,7 +445,7 @@ struct Engine {
         float it;
         const float r2f = Est::r2_f32(pts32[i], hf, it);
         const float e = fmaf(cm, fabsf(it), cm);
-        const float eb = fmaf(e, e, 2.f * tf * e);
+        const float eb = fmaf(e, e, 2.f * tf * e) + 1.2e-7f * t2f;
         if (!(r2f - t2f > eb)) {
           const double r2 = Est::r2_f64(pts64 + 4 * i, h);
           if (r2 < t2) {
@@ -385,6 +463,52 @@ struct Engine {
     Score sc;
     sc.count = total;
     sc.value = total == 0 ? 0.0 : (s + total * t2) / t2;
+    return sc;
+  }
+
+  // MAGSACScoringFunction::getScore: inlier iff r <= threshold, value = sum
+  // of normalised weights (points whose FP32 residual lies above the
+  // threshold by more than its error bound are skipped).
+  __device__ Score exact_score_magsac(const double* model, int* list, const float* m32) {
+    if (m32 == nullptr) {
+      prepare_shared_f32(model);
+      m32 = sh.mf32;
+    }
+    double h[9];
+    float hf[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      h[q] = model[q];
+      hf[q] = m32[q];
+    }
+    const float cm = m32[9];
+    const float mt = (float)mag_thr, mt2 = (float)mag_thr2;
+    double acc = 0.0;
+    int total = 0;
+    for (int base = 0; base < N; base += GCR_BLOCK) {
+      const int i = base + threadIdx.x;
+      int f = 0;
+      if (i < N) {
+        float it;
+        const float r2f = Est::r2_f32(pts32[i], hf, it);
+        const float e = fmaf(cm, fabsf(it), cm);
+        const float eb = fmaf(e, e, 2.f * mt * e) + 1.2e-7f * mt2;
+        if (!(r2f - mt2 > eb)) {
+          const double r = sqrt(Est::r2_f64(pts64 + 4 * i, h));
+          if (!(r > mag_thr)) {
+            f = 1;
+            acc += mag_weight(r);
+          }
+        }
+      }
+      int tot;
+      const int pos = block_exclusive_scan(f, sh.red_i, &tot);
+      if (list && f) list[total + pos] = i;
+      total += tot;
+    }
+    Score sc;
+    sc.count = total;
+    sc.value = block_sum(acc, sh.red_d);
     return sc;
   }
 
@@ -1486,6 +1610,7 @@ struct Engine {
       p2.min_iters = 20;
       p2.lo_number = 10;
       p2.sampler = SAMPLER_UNIFORM;
+      p2.scoring = SCORING_MSAC;
       p2.nested = 1;
       p2.stream_main = p2.stream_lo = 16u + (uint32_t)(degensac_calls++);
       p2.pp_h = ish.pp_H;
@@ -1845,7 +1970,7 @@ struct Engine {
           slot.dres[k] = fmax(0.0, 1.0 - Est::r2_f64(pts64 + 4 * list[k], Fb) / t2);
         sync();
         if (fit_cta_f(list, cnt, 2, false)) {
-          const Score sc = exact_score(sh.fit_model, spare);
+          const Score sc = exact_score(sh.fit_model, spare, nullptr, true);
           if (final_score < sc.value) {
             final_score = sc.value;
             copy_model(sh.best_model, sh.fit_model);
@@ -1908,7 +2033,7 @@ struct Engine {
             sync();
             if (threadIdx.x < 9) sh.fit_model[threadIdx.x] = Eq[threadIdx.x];
             sync();
-            const Score sc = exact_score(sh.fit_model, tmp);
+            const Score sc = exact_score(sh.fit_model, tmp, nullptr, true);
             if (final_score < sc.value) {
               final_score = sc.value;
               copy_model(sh.best_model, sh.fit_model);

@@ -26,6 +26,9 @@ STATUS_NAMES = {
     4: "DEVICE_ERROR", 5: "TIMEOUT", 6: "CAPACITY", 7: "UNSUPPORTED",
 }
 
+GCR_SCORING_MSAC = 0
+GCR_SCORING_MAGSAC = 1
+
 GCR_HOMOGRAPHY = 0
 GCR_FUNDAMENTAL = 1
 GCR_ESSENTIAL = 2
