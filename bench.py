@@ -173,6 +173,24 @@ def fp32_peak_tflops(torch):
     return best
 
 
+def fp64_peak_tflops(torch):
+    """Measured FP64 peak: cuBLAS DGEMM 4096^3."""
+    a = torch.randn(4096, 4096, device="cuda", dtype=torch.float64)
+    b = torch.randn(4096, 4096, device="cuda", dtype=torch.float64)
+    a @ b
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        a @ b
+        e1.record()
+        e1.synchronize()
+        best = max(best, 2 * 4096 ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    del a, b
+    return best
+
+
 def cpu_baseline(workload, corr, offsets, sizes, p, K=None, target_s=10.0, max_pairs=1 << 30):
     """The oracle (CPU restatement of the reference path) on all host cores,
     on a bounded sample of the same workload. Returns (pairs/s, cores, sample)."""
@@ -347,10 +365,13 @@ def main():
     peak = fp32_peak_tflops(torch)
     achieved = flops / (total_ms / args.steps / 1e3) / 1e12
     traffic = None
+    fp64_work = None
     tp = os.path.join(ROOT, "profiles", f"traffic_{args.workload}.json")
     if os.path.exists(tp):
         t = json.load(open(tp))
         traffic = t["bytes_per_pair"] * P
+        fp64_work = t["fp64_flop_per_pair"] * P
+    peak64 = fp64_peak_tflops(torch)
     line = {
         "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -361,6 +382,14 @@ def main():
                      "frac": achieved / peak if peak else None, "traffic": traffic,
                      "peak_source": "cuBLAS SGEMM 8192^3, TF32 off, measured in this run",
                      "work": f"{FLOP_PER_RESIDUAL[args.workload]} FLOP x models_scored x N per pair"},
+        # the FP64 pipe is the unit the kernel keeps busiest (solvers, LO fits):
+        # executed FP64 FLOP per pair from the ncu capture in profiles/, over the
+        # live DGEMM peak
+        "roofline_fp64": None if fp64_work is None else {
+            "bound": "fp64", "achieved": fp64_work / (total_ms / args.steps / 1e3) / 1e12, "peak": peak64,
+            "unit": "TFLOP/s", "frac": fp64_work / (total_ms / args.steps / 1e3) / 1e12 / peak64,
+            "peak_source": "cuBLAS DGEMM 4096^3, measured in this run",
+            "work": "FP64 FLOP per pair executed by the kernel (ncu SASS counts, FMA = 2) x pairs"},
         "e2e": {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": int(corr.nbytes),
                 "d2h_bytes_per_step": int(P * 9 * 8 + offsets[-1] + P * _abi.STATS_DTYPE.itemsize)},
         "gpu_launches": int(launches),
