@@ -101,6 +101,8 @@ gcr_status check_params(gcr_model_kind kind, const gcr_params* p) {
                 "sampler %d is not provided by the device engine (0 uniform, 1 PROSAC, 2 P-NAPSAC)", p->sampler);
   if (p->scoring != GCR_SCORING_MSAC && p->scoring != GCR_SCORING_MAGSAC)
     return fail(GCR_UNSUPPORTED, "scoring %d is not provided (0 MSAC, 1 MAGSAC++)", p->scoring);
+  if (p->use_sprt && !(p->min_inlier_ratio_for_sprt > 0 && p->min_inlier_ratio_for_sprt < 1))
+    return fail(GCR_INVALID_ARG, "min_inlier_ratio_for_sprt must be in (0, 1) when use_sprt is set");
   const bool pairwise = p->spatial_coherence_weight > 0;
   if (p->neighborhood != GCR_NEIGHBORHOOD_GRID && pairwise)
     return fail(GCR_UNSUPPORTED, "only the grid neighbourhood (0) is provided with a spatial coherence term");
@@ -147,6 +149,7 @@ void gcr_default_params(gcr_model_kind kind, gcr_params* p) {
   p->scoring = GCR_SCORING_MSAC;
   p->use_sprt = 1;
   p->seed = 0;
+  p->min_inlier_ratio_for_sprt = kind == GCR_ESSENTIAL ? 0.01 : 0.00001;
   switch (kind) {
     case GCR_HOMOGRAPHY:  // bindings.cpp:1158-1178
       p->spatial_coherence_weight = 0.975;
@@ -361,6 +364,8 @@ gcr_status gcr_batch_run_device(gcr_context* c, gcr_model_kind kind, int64_t num
   prm.stream_main = 1;  // STREAM_MAIN
   prm.stream_lo = 2;    // STREAM_LO
   prm.pp_h = nullptr;
+  prm.use_sprt = params->use_sprt ? 1 : 0;
+  prm.sprt_min_ratio = params->min_inlier_ratio_for_sprt;
   prm.mag_table = nullptr;
   prm.mag_c2dof = 0.25 * std::pow(2.0, 1.5);
   prm.mag_gamma_k = 0.0036572608340910764;

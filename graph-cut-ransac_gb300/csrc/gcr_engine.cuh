@@ -68,6 +68,9 @@ struct EngineParams {
   double mag_c2dof;
   double mag_gamma_diff;
   double mag_gamma_k;
+  // SPRT preemptive verification of main-loop models
+  int32_t use_sprt;
+  double sprt_min_ratio;
 };
 
 // Per-pair inputs prepared on the device.
@@ -114,6 +117,8 @@ struct Slot {
   int* node_i;          // [GCR_WARPS][3 * kMaxFlowCap]  height, queue, mark
   double* red;          // [GCR_WARPS * 64 + 64] reduction partials
   int* napsac;          // [16][max_n] P-NAPSAC layers (sorted points, cell start, cell size per point)
+  int* sprt_pool;       // [max_n] SPRT's point order
+  double* sprt_buf;     // [GCR_BLOCK] squared residual of a chunk's inliers, -1 for outliers
                         // x4, hits, subset sizes, layers, growth table
 };
 
@@ -141,6 +146,10 @@ struct Score {
 struct Container {
   const double* model;
   int count;
+  // SPRT containers list the inliers among SPRT-pool positions
+  // [start, start + len) in pool order; start < 0: all points, index order
+  int start = -1;
+  int len = 0;
 };
 
 template <class Est>
@@ -220,6 +229,10 @@ struct Engine {
   // 237-348): inlier iff r <= threshold, weight from the gamma table
   bool mag = false;
   double mag_thr = 0, mag_thr2 = 0, mag_sq2 = 0, mag_oos = 0, mag_w0 = 0;
+  // SPRT state (identical in every thread)
+  bool sprt = false;
+  int sprt_cursor = 0;
+  double sprt_eps = 0, sprt_delta = 0, sprt_A = 0, sprt_tM = 1, sprt_mS = 1;
   int status = ST_OK;
   int flags = 0;
 
@@ -1611,6 +1624,7 @@ struct Engine {
       p2.lo_number = 10;
       p2.sampler = SAMPLER_UNIFORM;
       p2.scoring = SCORING_MSAC;
+      p2.use_sprt = 0;
       p2.nested = 1;
       p2.stream_main = p2.stream_lo = 16u + (uint32_t)(degensac_calls++);
       p2.pp_h = ish.pp_H;
@@ -1631,9 +1645,200 @@ struct Engine {
   }
 
   // ------------------------------------------------------------------
+  // SPRTPreemptiveVerfication (preemption/preemption_sprt.h:50-380): models
+  // are tested on the points in a fixed random order, continuing from where
+  // the previous model stopped, and rejected as soon as the likelihood ratio
+  // exceeds the decision threshold A. Two inputs of the reference are not
+  // reproducible and are replaced: the point order is a Fisher-Yates
+  // permutation with the reference's loop structure whose draws come from
+  // Philox stream 3 instead of rand(), and t_M is 1/m (what the reference gets
+  // whenever its first-sample estimate returns a model).
+
+  // estimateThresholdA (preemption_sprt.h:361-379)
+  __device__ double sprt_threshold_A(double eps, double del) const {
+    const double C = (1 - del) * log((1 - del) / (1 - eps)) + del * (log(del / eps));
+    const double K = (sprt_tM * C) / sprt_mS + 1;
+    double An_1 = K, An = K;
+    for (int i = 0; i < 10; ++i) {
+      An = K + log(An_1);
+      if (fabs(An - An_1) < 1.5e-8) break;
+      An_1 = An;
+    }
+    return An;
+  }
+
+  __device__ void sprt_init() {
+    if (threadIdx.x == 0) {
+      int* pool = slot.sprt_pool;
+      for (int i = 0; i < N; ++i) pool[i] = i;
+      DrawStream ds(pd.seed, 3u, 0);
+      int max = N;
+      for (int i = 0; i < N; ++i) {
+        const int idx = (int)(ds.next_u32() % (uint32_t)max);
+        const int t = pool[idx];
+        --max;
+        pool[idx] = pool[max];
+        pool[max] = t;
+      }
+    }
+    sync();
+    sprt = true;
+    sprt_cursor = 0;
+    sprt_tM = 1.0 / (double)m;
+    sprt_mS = (double)Est::MAXSOL;
+    sprt_delta = prm.sprt_min_ratio / 10.0;
+    sprt_eps = prm.sprt_min_ratio;
+    sprt_A = sprt_threshold_A(sprt_eps, sprt_delta);
+  }
+
+  // Inlier decisions (r^2 < t^2, FP32 filter + FP64 decision) of the points at
+  // SPRT-pool positions pos0 .. pos0 + cnt - 1 (mod N): sprt_buf[j] receives
+  // the squared residual of an inlier, -1 otherwise.
+  __device__ void sprt_flags(const double* h, const float* hf, float cm, int pos0, int cnt) {
+    const float tf = (float)sqrt(t2), t2f = (float)t2;
+    const int j = threadIdx.x;
+    if (j < cnt) {
+      int pos = pos0 + j;
+      if (pos >= N) pos -= N;
+      const int p = slot.sprt_pool[pos];
+      float it;
+      const float r2f = Est::r2_f32(pts32[p], hf, it);
+      const float e = fmaf(cm, fabsf(it), cm);
+      const float eb = fmaf(e, e, 2.f * tf * e) + 1.2e-7f * t2f;
+      double v = -1.0;
+      if (!(r2f - t2f > eb)) {
+        const double r2 = Est::r2_f64(pts64 + 4 * p, h);
+        if (r2 < t2) v = r2;
+      }
+      slot.sprt_buf[j] = v;
+    }
+    sync();
+  }
+
+  // verifyModel (preemption_sprt.h:232-347): returns whether the model
+  // passed; sc is its truncated-quadratic score over the tested points, list
+  // (optional) receives their inliers in pool order, [start, start + len) are
+  // the pool positions tested.
+  __device__ bool sprt_verify(const double* model, const float* m32, Score& sc, int* list, int& start, int& len) {
+    double h[9];
+    float hf[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      h[q] = model[q];
+      hf[q] = m32[q];
+    }
+    const float cm = m32[9];
+    start = sprt_cursor;
+    const double eps = sprt_eps, del = sprt_delta, A = sprt_A;
+    double lambda = 1.0, val = 0.0;
+    int cnt = 0, tested = 0;
+    bool valid = true;
+    while (valid && tested < N) {
+      const int chunk = min(GCR_BLOCK, N - tested);
+      sprt_flags(h, hf, cm, sprt_cursor, chunk);
+      if (threadIdx.x == 0) {
+        double lam = lambda, vl = val;
+        int c = cnt, used = 0;
+        bool ok = true;
+        for (int j = 0; j < chunk; ++j) {
+          const double r2 = slot.sprt_buf[j];
+          double ln;
+          if (r2 >= 0) {
+            ln = lam * (del / eps);
+            ++c;
+            vl += 1.0 - r2 / t2;
+          } else {
+            ln = lam * ((1 - del) / (1 - eps));
+          }
+          ++used;
+          if (ln > A * 1.0) {
+            ok = false;
+            break;
+          }
+          lam = ln;
+        }
+        sh.red_d[0] = lam;
+        sh.red_d[1] = vl;
+        sh.red_i[0] = c;
+        sh.red_i[1] = used;
+        sh.red_i[2] = ok ? 1 : 0;
+      }
+      sync();
+      lambda = sh.red_d[0];
+      val = sh.red_d[1];
+      const int cnew = sh.red_i[0], used = sh.red_i[1];
+      valid = sh.red_i[2] != 0;
+      sync();
+      const int j = threadIdx.x;
+      const int f = (j < used && slot.sprt_buf[j] >= 0) ? 1 : 0;
+      int tot;
+      const int pos = block_exclusive_scan(f, sh.red_i, &tot);
+      if (list && f) {
+        int pp = sprt_cursor + j;
+        if (pp >= N) pp -= N;
+        list[cnt + pos] = slot.sprt_pool[pp];
+      }
+      cnt = cnew;
+      tested += used;
+      sprt_cursor += used;
+      if (sprt_cursor >= N) sprt_cursor -= N;
+      sync();
+    }
+    len = tested;
+    sc.count = cnt;
+    sc.value = val;
+    if (valid) {
+      if (val > best.value) {
+        sprt_eps = (double)cnt / N;
+        sprt_A = sprt_threshold_A(sprt_eps, sprt_delta);
+      }
+    } else {
+      const double de = (double)cnt / N;
+      if (de > 0 && fabs(del - de) / del > 0.05) {
+        sprt_delta = de;
+        sprt_A = sprt_threshold_A(sprt_eps, de);
+      }
+    }
+    return valid;
+  }
+
+  // Inliers of `model` at pool positions [start, start + len), in pool order.
+  __device__ int sprt_list(const double* model, int start, int len, int* list) {
+    prepare_shared_f32(model);
+    double h[9];
+    float hf[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      h[q] = model[q];
+      hf[q] = sh.mf32[q];
+    }
+    const float cm = sh.mf32[9];
+    int total = 0;
+    for (int done = 0; done < len; done += GCR_BLOCK) {
+      const int chunk = min(GCR_BLOCK, len - done);
+      int p0 = start + done;
+      if (p0 >= N) p0 -= N;
+      sprt_flags(h, hf, cm, p0, chunk);
+      const int j = threadIdx.x;
+      const int f = (j < chunk && slot.sprt_buf[j] >= 0) ? 1 : 0;
+      int tot;
+      const int pos = block_exclusive_scan(f, sh.red_i, &tot);
+      if (list && f) {
+        int pp = p0 + j;
+        if (pp >= N) pp -= N;
+        list[total + pos] = slot.sprt_pool[pp];
+      }
+      total += tot;
+      sync();
+    }
+    return total;
+  }
+
+  // ------------------------------------------------------------------
   // Materialises the inlier list of a container's model into `list`.
   __device__ int materialise(const Container& c, int* list) {
     if (c.model == nullptr) return 0;
+    if (c.start >= 0) return sprt_list(c.model, c.start, c.len, list);
     return exact_score(c.model, list).count;
   }
 
@@ -1755,6 +1960,7 @@ struct Engine {
     // before the neighbourhood grid that keeps it
     if (prm.sampler == SAMPLER_PNAPSAC) napsac_setup();
     const int ncells = prm.nested ? 0 : build_grid();
+    if (prm.use_sprt && !prm.nested) sprt_init();
     tock(0, t0);
     max_iter = iteration_number_for(1, N, m, log_prob);
     const long long max_iters = prm.max_iters, min_iters = prm.min_iters;
@@ -1772,7 +1978,7 @@ struct Engine {
       tock(1, t0);
       t0 = tick();
       const int K = sh.mbase[GCR_BLOCK - 1] + sh.n_ok[GCR_BLOCK - 1];
-      score_models_f32(0, K);
+      if (!sprt) score_models_f32(0, K);
       tock(2, t0);
       bool restart = false;
       long long next_attempt = attempt + GCR_BLOCK;
@@ -1803,12 +2009,29 @@ struct Engine {
           const int k = sh.mbase[j] + q;
           const double* mk = slot.models64 + 9 * k;
           ++models_scored;
-          cont[off] = {mk, sh.mcount[k]};
-          if (sh.mcount[k] == 0 || !maybe_better(k, best.value)) continue;
-          t0 = tick();
-          const Score sc = exact_score(mk, Est::CTA_VALIDITY ? slot.list1 : nullptr, slot.models32 + 12 * k);
-          tock(3, t0);
-          tock(9, 0, 1);
+          Score sc;
+          if (sprt) {
+            // SPRT provides the score (GCRANSAC.h:370-431)
+            int st0 = 0, ln = 0;
+            t0 = tick();
+            const bool passed = sprt_verify(mk, slot.models32 + 12 * k, sc, Est::CTA_VALIDITY ? slot.list1 : nullptr,
+                                            st0, ln);
+            tock(3, t0);
+            Container ct;
+            ct.model = mk;
+            ct.count = sc.count;
+            ct.start = st0;
+            ct.len = ln;
+            cont[off] = ct;
+            if (!passed) continue;
+          } else {
+            cont[off] = {mk, sh.mcount[k]};
+            if (sh.mcount[k] == 0 || !maybe_better(k, best.value)) continue;
+            t0 = tick();
+            sc = exact_score(mk, Est::CTA_VALIDITY ? slot.list1 : nullptr, slot.models32 + 12 * k);
+            tock(3, t0);
+            tock(9, 0, 1);
+          }
           bool updated = false;
           bool valid = false;
           if (best.value < sc.value) {

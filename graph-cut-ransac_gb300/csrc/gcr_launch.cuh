@@ -104,6 +104,8 @@ size_t slot_bytes(int max_n, int sort_cap, bool light = false) {
   s += 2 * al(sizeof(double) * max_n);
   if (!light) {
     s += al(sizeof(int) * 16 * (size_t)max_n);
+    s += al(sizeof(int) * (size_t)max_n);
+    s += al(sizeof(double) * GCR_BLOCK);
     s += al(sizeof(unsigned long long) * sort_cap);
     s += al(sizeof(int) * max_n);
     s += al(sizeof(int) * (max_n + 1));
@@ -133,6 +135,8 @@ Slot carve_slot(unsigned char* base, int max_n, int sort_cap, bool light = false
   s.tr = (double*)take(sizeof(double) * max_n);
   if (!light) {
     s.napsac = (int*)take(sizeof(int) * 16 * (size_t)max_n);
+    s.sprt_pool = (int*)take(sizeof(int) * (size_t)max_n);
+    s.sprt_buf = (double*)take(sizeof(double) * GCR_BLOCK);
     s.sortbuf = (unsigned long long*)take(sizeof(unsigned long long) * sort_cap);
     s.cell_pts = (int*)take(sizeof(int) * max_n);
     s.cell_start = (int*)take(sizeof(int) * (max_n + 1));

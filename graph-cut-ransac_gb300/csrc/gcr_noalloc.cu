@@ -140,6 +140,8 @@ extern "C" gcr_status gcr_find_homography_device_noalloc(const double* d_corr, i
   if (p.sampler != GCR_SAMPLER_UNIFORM && p.sampler != GCR_SAMPLER_PROSAC && p.sampler != GCR_SAMPLER_PNAPSAC)
     return fail(GCR_UNSUPPORTED, "sampler %d is not provided (0 uniform, 1 PROSAC, 2 P-NAPSAC)", p.sampler);
   if (p.scoring != GCR_SCORING_MSAC) return fail(GCR_UNSUPPORTED, "scoring %d is not provided", p.scoring);
+  if (p.use_sprt && !(p.min_inlier_ratio_for_sprt > 0 && p.min_inlier_ratio_for_sprt < 1))
+    return fail(GCR_INVALID_ARG, "min_inlier_ratio_for_sprt must be in (0, 1) when use_sprt is set");
   if (p.spatial_coherence_weight > 0 && p.neighborhood != GCR_NEIGHBORHOOD_GRID)
     return fail(GCR_UNSUPPORTED, "only the grid neighbourhood (0) is provided with a spatial coherence term");
   if (p.neighborhood == GCR_NEIGHBORHOOD_GRID && !(p.neighborhood_size >= 1))
@@ -204,6 +206,8 @@ extern "C" gcr_status gcr_find_homography_device_noalloc(const double* d_corr, i
   prm.stream_main = 1;
   prm.stream_lo = 2;
   prm.pp_h = nullptr;
+  prm.use_sprt = p.use_sprt ? 1 : 0;
+  prm.sprt_min_ratio = p.min_inlier_ratio_for_sprt;
 
   single_pair_kernel<<<1, GCR_BLOCK, gcr::shared_bytes<Est>(), (cudaStream_t)stream>>>(ws, prm, pd, slot);
   e = cudaGetLastError();

@@ -33,7 +33,8 @@ def default_params(kind):
 
 
 def _params(kind, threshold, conf, spatial_coherence_weight, max_iters, min_iters, use_sprt, sampler,
-            neighborhood, neighborhood_size, lo_number, use_space_partitioning=False, seed=0, scoring=0):
+            neighborhood, neighborhood_size, lo_number, use_space_partitioning=False, seed=0, scoring=0,
+            min_inlier_ratio_for_sprt=0.00001):
     p = _abi.Params()
     p.threshold = float(threshold)
     p.confidence = float(conf)
@@ -48,6 +49,7 @@ def _params(kind, threshold, conf, spatial_coherence_weight, max_iters, min_iter
     p.use_sprt = int(bool(use_sprt))
     p.use_space_partitioning = int(bool(use_space_partitioning))
     p.seed = int(seed)
+    p.min_inlier_ratio_for_sprt = float(min_inlier_ratio_for_sprt)
     return p
 
 
@@ -106,7 +108,8 @@ def findHomography(correspondences, h1, w1, h2, w2, probabilities=None, threshol
         raise NotImplementedError("only point correspondences (solver=0) are provided")
     c = _check_corr(correspondences, 4, "homography")
     p = _params(_abi.GCR_HOMOGRAPHY, threshold, conf, spatial_coherence_weight, max_iters, min_iters, use_sprt,
-                sampler, neighborhood, neighborhood_size, lo_number, use_space_partitioning, seed)
+                sampler, neighborhood, neighborhood_size, lo_number, use_space_partitioning, seed,
+                min_inlier_ratio_for_sprt=min_inlier_ratio_for_sprt)
     return _run_one(_abi.GCR_HOMOGRAPHY, c, (h1, w1, h2, w2), p, return_stats=return_stats)
 
 
@@ -119,7 +122,8 @@ def findFundamentalMatrix(correspondences, h1, w1, h2, w2, probabilities=None, t
         raise NotImplementedError("only point correspondences (solver=0) are provided")
     c = _check_corr(correspondences, 7, "fundamental")
     p = _params(_abi.GCR_FUNDAMENTAL, threshold, conf, spatial_coherence_weight, max_iters, min_iters, use_sprt,
-                sampler, neighborhood, neighborhood_size, lo_number, False, seed)
+                sampler, neighborhood, neighborhood_size, lo_number, False, seed,
+                min_inlier_ratio_for_sprt=min_inlier_ratio_for_sprt)
     return _run_one(_abi.GCR_FUNDAMENTAL, c, (h1, w1, h2, w2), p, return_stats=return_stats)
 
 
@@ -132,7 +136,8 @@ def findEssentialMatrix(correspondences, K1, K2, h1, w1, h2, w2, probabilities=N
         raise NotImplementedError("only point correspondences (solver=0) are provided")
     c = _check_corr(correspondences, 5, "essential")
     p = _params(_abi.GCR_ESSENTIAL, threshold, conf, spatial_coherence_weight, max_iters, min_iters, use_sprt,
-                sampler, neighborhood, neighborhood_size, lo_number, False, seed)
+                sampler, neighborhood, neighborhood_size, lo_number, False, seed,
+                min_inlier_ratio_for_sprt=min_inlier_ratio_for_sprt)
     return _run_one(_abi.GCR_ESSENTIAL, c, (h1, w1, h2, w2), p, K1=K1, K2=K2, return_stats=return_stats)
 
 

@@ -58,6 +58,7 @@ class Params(ctypes.Structure):
         ("use_sprt", ctypes.c_int32),
         ("use_space_partitioning", ctypes.c_int32),
         ("seed", ctypes.c_uint64),
+        ("min_inlier_ratio_for_sprt", ctypes.c_double),
     ]
 
 
@@ -83,7 +84,7 @@ STATS_DTYPE = np.dtype([
 SIZE_DTYPE = np.dtype([("h1", np.int32), ("w1", np.int32), ("h2", np.int32), ("w2", np.int32)])
 
 assert ctypes.sizeof(Stats) == STATS_DTYPE.itemsize == 56
-assert ctypes.sizeof(Params) == 80
+assert ctypes.sizeof(Params) == 88
 
 _P = ctypes.c_void_p
 _EXPORTS = {

@@ -74,9 +74,10 @@ typedef struct gcr_params {
   int32_t neighborhood;            /* GCR_NEIGHBORHOOD_GRID only */
   int32_t lo_number;               /* inner-RANSAC trials per graph-cut */
   int32_t scoring;                 /* GCR_SCORING_* */
-  int32_t use_sprt;                /* accepted; the engine verifies every model in full */
+  int32_t use_sprt;                /* SPRT preemptive verification of main-loop models */
   int32_t use_space_partitioning;  /* accepted; the engine scores every point */
   uint64_t seed;                   /* seed of the counter-based sampler streams */
+  double min_inlier_ratio_for_sprt; /* SPRT's initial inlier-ratio guess (epsilon) */
 } gcr_params;
 
 typedef struct gcr_stats {

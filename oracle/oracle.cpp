@@ -42,6 +42,8 @@ static void fill_settings(Settings& s, const gcr_params& p) {
   s.max_local_optimization_number = (size_t)p.lo_number;
   s.max_iteration_number = (size_t)p.max_iterations;
   s.min_iteration_number = (size_t)p.min_iterations;
+  s.use_sprt = p.use_sprt != 0;
+  s.sprt_min_inlier_ratio = p.min_inlier_ratio_for_sprt;
 }
 
 static std::unique_ptr<Sampler> make_main_sampler(const gcr_params& p, const Mat& pts, size_t m,
@@ -76,6 +78,7 @@ static int run_generic(const Mat& run_pts, const Mat& pixel_pts, const Est& est,
   UniformSampler lo_s(seed, STREAM_LO);
   GCRansac<Est, Scoring<Est>> g;
   fill_settings(g.settings, p);
+  g.sprt_seed = seed;
   g.settings.threshold = threshold;
   if constexpr (std::is_same<Scoring<Est>, MAGSACScoring<Est>>::value) g.scoring.threshold = mag_threshold;
   const bool ok = g.run(run_pts, est, main_s.get(), &lo_s, grid, model);

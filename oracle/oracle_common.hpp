@@ -51,6 +51,10 @@ struct Settings {
   double spatial_coherence_weight = 0.14;
   double threshold = 2.0;
   double confidence = 0.95;
+  // SPRT preemptive verification (the drivers' use_sprt and
+  // min_inlier_ratio_for_sprt arguments)
+  bool use_sprt = false;
+  double sprt_min_inlier_ratio = 0.01;
 };
 
 struct Statistics {
@@ -94,6 +98,7 @@ inline uint32_t draw_u32(uint64_t seed, uint32_t stream, uint64_t call, uint32_t
 enum : uint32_t {
   STREAM_MAIN = 1,
   STREAM_LO = 2,
+  STREAM_SPRT = 3,
   STREAM_NAPSAC_LOCAL = 3,
   STREAM_NAPSAC_CENTER = 4,
   STREAM_NAPSAC_GLOBAL = 5,

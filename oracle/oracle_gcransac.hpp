@@ -155,6 +155,99 @@ struct MAGSACScoring {
 };
 
 // ---------------------------------------------------------------------------
+// SPRTPreemptiveVerfication (preemption/preemption_sprt.h:50-380). Two inputs
+// of the reference are not reproducible and are replaced: the point order is a
+// Fisher-Yates permutation with the reference's loop structure whose draws
+// come from Philox stream 3 instead of rand(), and t_M is 1/m (the reference
+// gets 1/m whenever its first-sample estimate returns a model, because the
+// timer it divides by is not restarted; otherwise it uses a wall-clock time).
+struct Sprt {
+  std::vector<size_t> pool;
+  size_t cursor = 0;
+  double epsilon = 0, delta = 0, A = 0;
+  size_t last_update = 0;
+  double t_M = 1, m_S = 1, amp = 1.0;
+
+  void init(size_t N, size_t m, size_t max_solutions, double min_ratio, uint64_t seed) {
+    pool.resize(N);
+    for (size_t i = 0; i < N; ++i) pool[i] = i;
+    size_t max = N;
+    for (size_t i = 0; i < N; ++i) {
+      const size_t idx = draw_u32(seed, STREAM_SPRT, 0, (uint32_t)i) % max;
+      const size_t t = pool[idx];
+      --max;
+      pool[idx] = pool[max];
+      pool[max] = t;
+    }
+    cursor = 0;
+    t_M = 1.0 / (double)m;
+    m_S = (double)max_solutions;
+    delta = min_ratio / 10.0;
+    epsilon = min_ratio;
+    A = threshold_A(epsilon, delta);
+    last_update = 0;
+  }
+  // estimateThresholdA (preemption_sprt.h:361-379)
+  double threshold_A(double eps, double del) const {
+    const double C = (1 - del) * std::log((1 - del) / (1 - eps)) + del * (std::log(del / eps));
+    const double K = (t_M * C) / m_S + 1;
+    double An_1 = K, An = K;
+    for (unsigned i = 0; i < 10; ++i) {
+      An = K + std::log(An_1);
+      if (std::fabs(An - An_1) < 1.5e-8) break;
+      An_1 = An;
+    }
+    return An;
+  }
+  // verifyModel (preemption_sprt.h:232-347) without pre-selected index sets.
+  // Writes the tested inliers in pool order; returns whether the model passed.
+  template <class Est>
+  bool verify(const Mat& pts, const Model& model, const Est& est, double threshold, size_t iteration,
+              const Score& best, std::vector<size_t>& inliers, Score& score) {
+    inliers.clear();
+    const size_t N = (size_t)pts.rows;
+    const double sq = threshold * threshold;
+    const double eps = epsilon, del = delta, a = A;
+    double lambda = 1, lambda_new;
+    score = Score();
+    bool valid = true;
+    for (size_t t = 0; t < N; ++t) {
+      const size_t idx = pool[cursor];
+      const double r2 = est.squared_residual(pts.row(idx), model);
+      if (r2 < sq) {
+        lambda_new = lambda * (del / eps);
+        ++score.inlier_number;
+        score.value += 1.0 - r2 / sq;
+        inliers.push_back(idx);
+      } else {
+        lambda_new = lambda * ((1 - del) / (1 - eps));
+      }
+      if (++cursor >= N) cursor = 0;
+      if (lambda_new > a * amp) {
+        valid = false;
+        break;
+      }
+      lambda = lambda_new;
+    }
+    if (valid) {
+      if (score.value > best.value) {
+        epsilon = (double)score.inlier_number / N;
+        A = threshold_A(epsilon, del);
+        last_update = iteration;
+      }
+    } else {
+      const double de = (double)score.inlier_number / N;
+      if (de > 0 && std::fabs(del - de) / del > 0.05) {
+        delta = de;
+        A = threshold_A(eps, de);
+        last_update = iteration;
+      }
+    }
+    return valid;
+  }
+};
+
+// ---------------------------------------------------------------------------
 // GCRANSAC<Estimator, GridNeighborhoodGraph<4>, Scoring>::run, restated from
 // GCRANSAC.h:200-627 together with graphCutLocalOptimization (779-910),
 // labeling (912-1021) and iteratedLeastSquaresFitting (629-758).
@@ -166,6 +259,7 @@ struct GCRansac {
   double truncated_threshold = 0, squared_truncated_threshold = 0, log_probability = 0;
   const Grid* graph = nullptr;
   size_t models_scored = 0;  // main-loop models + LO trials + IRLS fits
+  uint64_t sprt_seed = 0;    // seed of the SPRT point permutation
   Sampler* main_sampler = nullptr;
   Sampler* lo_sampler = nullptr;
 
@@ -327,6 +421,8 @@ struct GCRansac {
     std::vector<size_t> pool(N);
     for (size_t i = 0; i < N; ++i) pool[i] = i;
     std::vector<Model> models;
+    Sprt sprt;
+    if (settings.use_sprt) sprt.init(N, m, Est::max_solutions(), settings.sprt_min_inlier_ratio, sprt_seed);
     while (settings.min_iteration_number > statistics.iteration_number ||
            statistics.iteration_number < std::min(max_iteration, settings.max_iteration_number)) {
       bool do_lo = false;
@@ -341,7 +437,14 @@ struct GCRansac {
       statistics.iteration_number += unsuccessful;
       for (Model& model : models) {
         ++models_scored;
-        current_score = scoring.get(pts, model, est, &cont[off]);
+        if (settings.use_sprt) {
+          // SPRT provides the score (GCRANSAC.h:370-431)
+          if (!sprt.verify(pts, model, est, truncated_threshold, statistics.iteration_number, best_score, cont[off],
+                           current_score))
+            continue;
+        } else {
+          current_score = scoring.get(pts, model, est, &cont[off]);
+        }
         bool updated_model = false;
         if (best_score < current_score &&
             est.is_valid_model(model, pts, cont[off], sample.data(), truncated_threshold, updated_model)) {
