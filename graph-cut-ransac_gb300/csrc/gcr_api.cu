@@ -365,6 +365,7 @@ gcr_status gcr_batch_run_device(gcr_context* c, gcr_model_kind kind, int64_t num
   prm.stream_lo = 2;    // STREAM_LO
   prm.pp_h = nullptr;
   prm.use_sprt = params->use_sprt ? 1 : 0;
+  prm.use_sp = (kind == GCR_HOMOGRAPHY && params->use_space_partitioning) ? 1 : 0;
   prm.sprt_min_ratio = params->min_inlier_ratio_for_sprt;
   prm.mag_table = nullptr;
   prm.mag_c2dof = 0.25 * std::pow(2.0, 1.5);

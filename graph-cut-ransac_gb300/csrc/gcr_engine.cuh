@@ -71,6 +71,8 @@ struct EngineParams {
   // SPRT preemptive verification of main-loop models
   int32_t use_sprt;
   double sprt_min_ratio;
+  // space-partitioning pre-selection of homography models
+  int32_t use_sp;
 };
 
 // Per-pair inputs prepared on the device.
@@ -119,6 +121,9 @@ struct Slot {
   int* napsac;          // [16][max_n] P-NAPSAC layers (sorted points, cell start, cell size per point)
   int* sprt_pool;       // [max_n] SPRT's point order
   double* sprt_buf;     // [GCR_BLOCK] squared residual of a chunk's inliers, -1 for outliers
+  int* sp_cell;         // [max_n] grid cell of each sorted position
+  int* sp_flag;         // [max_n] cell kept by the space partitioning of the current model
+  int* sp_sel;          // [max_n] points of the kept cells, cell by cell
                         // x4, hits, subset sizes, layers, growth table
 };
 
@@ -229,6 +234,10 @@ struct Engine {
   // 237-348): inlier iff r <= threshold, weight from the gamma table
   bool mag = false;
   double mag_thr = 0, mag_thr2 = 0, mag_sq2 = 0, mag_oos = 0, mag_w0 = 0;
+  // space partitioning (homographies): cells of the grid kept for a model
+  bool sp = false;
+  int sp_ncells = 0;
+  int sp_count = 0;  // points in the kept cells of the last selection
   // SPRT state (identical in every thread)
   bool sprt = false;
   int sprt_cursor = 0;
@@ -1802,6 +1811,236 @@ struct Engine {
     return valid;
   }
 
+  // ------------------------------------------------------------------
+  // SpacePartitioningRANSAC::runHomography (inlier_selectors/
+  // space_partitioning_ransac.h:341-505) on the neighbourhood grid: a cell with
+  // fewer than four points is always kept; otherwise its four source-image
+  // corners are mapped by H and the cell is kept when one lands in the cell's
+  // destination indices, or when the threshold-grown box of the mapped corners
+  // 00 and 11 overlaps the destination cell. Cells are visited by ascending
+  // key (the reference visits them in std::unordered_map order, which is
+  // library-specific). A mapped coordinate outside the int range (or NaN)
+  // converts to INT_MIN.
+  __device__ static int sp_trunc_int(double v) {
+    if (!(v > -2147483649.0 && v < 2147483648.0)) return (int)0x80000000;
+    return (int)v;
+  }
+
+  __device__ void sp_init(int ncells) {
+    sp = true;
+    sp_ncells = ncells;
+    for (int c = threadIdx.x; c < ncells; c += GCR_BLOCK)
+      for (int j = slot.cell_start[c]; j < slot.cell_start[c + 1]; ++j) slot.sp_cell[j] = c;
+    sync();
+  }
+
+  // Keeps the cells of `model`: sp_flag per cell, sp_sel the points of the
+  // kept cells in cell order, sp_count their number.
+  __device__ void sp_select(const double* model) {
+    double H[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) H[q] = model[q];
+    const bool degenerate = fabs(det3(H)) < 1e-3;
+    const double cs1 = pd.cell[0], cs2 = pd.cell[1], cs3 = pd.cell[2], cs4 = pd.cell[3];
+    const uint64_t n = (uint64_t)pd.n_div;
+    const double thr = 1.5 * pd.threshold;
+    const double* pix = ws.pix64 + 4 * pd.offset;
+    auto proj = [&](uint64_t hx, uint64_t vy, double& x, double& y) {
+      const double X1 = (double)hx * cs1, Y1 = (double)vy * cs2;
+      double x2p = X1 * H[0] + Y1 * H[1] + H[2], y2p = X1 * H[3] + Y1 * H[4] + H[5],
+             h2p = X1 * H[6] + Y1 * H[7] + H[8];
+      x2p /= h2p;
+      y2p /= h2p;
+      x = x2p;
+      y = y2p;
+    };
+    for (int c = threadIdx.x; c < sp_ncells; c += GCR_BLOCK) {
+      int keep = 0;
+      const int c0 = slot.cell_start[c], sz = slot.cell_start[c + 1] - c0;
+      if (!degenerate) {
+        if (sz < 4) {
+          keep = 1;
+        } else {
+          const double* p = pix + 4 * slot.cell_pts[c0];
+          uint64_t ci[4];
+          for (int d = 0; d < 4; ++d) ci[d] = (uint64_t)(int64_t)floor(p[d] / pd.cell[d]);
+          double c00x = 0, c00y = 0, c11x = 0, c11y = 0;
+          for (int st = 0; st < 4 && !keep; ++st) {
+            const uint64_t hx = ci[0] + (uint64_t)(st >> 1);
+            if (hx >= n) continue;
+            const uint64_t vy = ci[1] + (uint64_t)(st & 1);
+            if (vy >= n) continue;
+            double x, y;
+            proj(hx, vy, x, y);
+            if (st == 0) { c00x = x; c00y = y; }
+            if (st == 3) { c11x = x; c11y = y; }
+            const int ix = sp_trunc_int(x / cs3), iy = sp_trunc_int(y / cs4);
+            if ((uint64_t)(int64_t)ix == ci[2] && (uint64_t)(int64_t)iy == ci[3]) keep = 1;
+          }
+          if (!keep) {
+            const uint64_t hx11 = ci[0] + 1, vy11 = ci[1] + 1;
+            if (vy11 >= n || hx11 >= n) proj(hx11, vy11, c11x, c11y);
+            const double l1x = c00x - thr, l1y = c00y - thr, r1x = c11x + thr, r1y = c11y + thr;
+            const double l2x = cs3 * (double)ci[2], l2y = cs4 * (double)ci[3];
+            const double r2x = l2x + cs3, r2y = l2y + cs4;
+            if ((l1x <= r2x && l2x <= r1x) || (r1y <= l2y && r2y <= l1y)) keep = 1;
+          }
+        }
+      }
+      slot.sp_flag[c] = keep;
+    }
+    sync();
+    int total = 0;
+    for (int base = 0; base < N; base += GCR_BLOCK) {
+      const int j = base + threadIdx.x;
+      const int f = (j < N && slot.sp_flag[slot.sp_cell[j]]) ? 1 : 0;
+      int tot;
+      const int pos = block_exclusive_scan(f, sh.red_i, &tot);
+      if (f) slot.sp_sel[total + pos] = slot.cell_pts[j];
+      total += tot;
+    }
+    sp_count = total;
+    sync();
+  }
+
+  // getScore over the kept points (scoring_function.h:186-230): MSAC in cell
+  // order; the first `len` kept points when len >= 0.
+  __device__ Score exact_score_sp(const double* model, int* list, int len = -1) {
+    prepare_shared_f32(model);
+    double h[9];
+    float hf[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      h[q] = model[q];
+      hf[q] = sh.mf32[q];
+    }
+    const float cm = sh.mf32[9];
+    const float tf = (float)sqrt(t2), t2f = (float)t2;
+    const int S = len >= 0 ? len : sp_count;
+    double acc = 0.0;
+    int total = 0;
+    for (int base = 0; base < S; base += GCR_BLOCK) {
+      const int j = base + threadIdx.x;
+      int f = 0, p = 0;
+      if (j < S) {
+        p = slot.sp_sel[j];
+        float it;
+        const float r2f = Est::r2_f32(pts32[p], hf, it);
+        const float e = fmaf(cm, fabsf(it), cm);
+        const float eb = fmaf(e, e, 2.f * tf * e) + 1.2e-7f * t2f;
+        if (!(r2f - t2f > eb)) {
+          const double r2 = Est::r2_f64(pts64 + 4 * p, h);
+          if (r2 < t2) {
+            f = 1;
+            acc -= r2;
+          }
+        }
+      }
+      int tot;
+      const int pos = block_exclusive_scan(f, sh.red_i, &tot);
+      if (list && f) list[total + pos] = p;
+      total += tot;
+    }
+    const double s = block_sum(acc, sh.red_d);
+    Score sc;
+    sc.count = total;
+    sc.value = total == 0 ? 0.0 : (s + total * t2) / t2;
+    return sc;
+  }
+
+  // verifyModel with index sets (preemption_sprt.h:268-296): the kept points
+  // in cell order, the pool cursor untouched.
+  __device__ bool sprt_verify_sp(const double* model, const float* m32, Score& sc, int* list, int& len) {
+    double h[9];
+    float hf[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      h[q] = model[q];
+      hf[q] = m32[q];
+    }
+    const float cm = m32[9];
+    const float tf = (float)sqrt(t2), t2f = (float)t2;
+    const double eps = sprt_eps, del = sprt_delta, A = sprt_A;
+    double lambda = 1.0, val = 0.0;
+    int cnt = 0, tested = 0;
+    bool valid = true;
+    const int S = sp_count;
+    while (valid && tested < S) {
+      const int chunk = min(GCR_BLOCK, S - tested);
+      const int j = threadIdx.x;
+      if (j < chunk) {
+        const int p = slot.sp_sel[tested + j];
+        float it;
+        const float r2f = Est::r2_f32(pts32[p], hf, it);
+        const float e = fmaf(cm, fabsf(it), cm);
+        const float eb = fmaf(e, e, 2.f * tf * e) + 1.2e-7f * t2f;
+        double v = -1.0;
+        if (!(r2f - t2f > eb)) {
+          const double r2 = Est::r2_f64(pts64 + 4 * p, h);
+          if (r2 < t2) v = r2;
+        }
+        slot.sprt_buf[j] = v;
+      }
+      sync();
+      if (threadIdx.x == 0) {
+        double lam = lambda, vl = val;
+        int c = cnt, used = 0;
+        bool ok = true;
+        for (int q = 0; q < chunk; ++q) {
+          const double r2 = slot.sprt_buf[q];
+          double ln;
+          if (r2 >= 0) {
+            ln = lam * (del / eps);
+            ++c;
+            vl += 1.0 - r2 / t2;
+          } else {
+            ln = lam * ((1 - del) / (1 - eps));
+          }
+          ++used;
+          if (ln > A * 1.0) {
+            ok = false;
+            break;
+          }
+          lam = ln;
+        }
+        sh.red_d[0] = lam;
+        sh.red_d[1] = vl;
+        sh.red_i[0] = c;
+        sh.red_i[1] = used;
+        sh.red_i[2] = ok ? 1 : 0;
+      }
+      sync();
+      lambda = sh.red_d[0];
+      val = sh.red_d[1];
+      const int cnew = sh.red_i[0], used = sh.red_i[1];
+      valid = sh.red_i[2] != 0;
+      sync();
+      const int f = (j < used && slot.sprt_buf[j] >= 0) ? 1 : 0;
+      int tot;
+      const int pos = block_exclusive_scan(f, sh.red_i, &tot);
+      if (list && f) list[cnt + pos] = slot.sp_sel[tested + j];
+      cnt = cnew;
+      tested += used;
+      sync();
+    }
+    len = tested;
+    sc.count = cnt;
+    sc.value = val;
+    if (valid) {
+      if (val > best.value) {
+        sprt_eps = (double)cnt / N;
+        sprt_A = sprt_threshold_A(sprt_eps, sprt_delta);
+      }
+    } else {
+      const double de = (double)cnt / N;
+      if (de > 0 && fabs(del - de) / del > 0.05) {
+        sprt_delta = de;
+        sprt_A = sprt_threshold_A(sprt_eps, de);
+      }
+    }
+    return valid;
+  }
+
   // Inliers of `model` at pool positions [start, start + len), in pool order.
   __device__ int sprt_list(const double* model, int start, int len, int* list) {
     prepare_shared_f32(model);
@@ -1838,6 +2077,11 @@ struct Engine {
   // Materialises the inlier list of a container's model into `list`.
   __device__ int materialise(const Container& c, int* list) {
     if (c.model == nullptr) return 0;
+    if (c.start == -2) {
+      // the first `len` kept points of the model's space partitioning
+      sp_select(c.model);
+      return exact_score_sp(c.model, list, c.len).count;
+    }
     if (c.start >= 0) return sprt_list(c.model, c.start, c.len, list);
     return exact_score(c.model, list).count;
   }
@@ -1961,6 +2205,8 @@ struct Engine {
     if (prm.sampler == SAMPLER_PNAPSAC) napsac_setup();
     const int ncells = prm.nested ? 0 : build_grid();
     if (prm.use_sprt && !prm.nested) sprt_init();
+    if constexpr (Est::KIND == 0)
+      if (prm.use_sp && !prm.nested && ncells > 0) sp_init(ncells);
     tock(0, t0);
     max_iter = iteration_number_for(1, N, m, log_prob);
     const long long max_iters = prm.max_iters, min_iters = prm.min_iters;
@@ -1978,7 +2224,7 @@ struct Engine {
       tock(1, t0);
       t0 = tick();
       const int K = sh.mbase[GCR_BLOCK - 1] + sh.n_ok[GCR_BLOCK - 1];
-      if (!sprt) score_models_f32(0, K);
+      if (!sprt && !(sp && !mag)) score_models_f32(0, K);
       tock(2, t0);
       bool restart = false;
       long long next_attempt = attempt + GCR_BLOCK;
@@ -2010,12 +2256,23 @@ struct Engine {
           const double* mk = slot.models64 + 9 * k;
           ++models_scored;
           Score sc;
+          if (sp) {
+            // GCRANSAC.h:343-366: rejected when the kept cells hold fewer
+            // points than the best model has inliers
+            sp_select(mk);
+            if (sp_count < best.count) continue;
+          }
           if (sprt) {
             // SPRT provides the score (GCRANSAC.h:370-431)
             int st0 = 0, ln = 0;
             t0 = tick();
-            const bool passed = sprt_verify(mk, slot.models32 + 12 * k, sc, Est::CTA_VALIDITY ? slot.list1 : nullptr,
-                                            st0, ln);
+            bool passed;
+            if (sp) {
+              passed = sprt_verify_sp(mk, slot.models32 + 12 * k, sc, Est::CTA_VALIDITY ? slot.list1 : nullptr, ln);
+              st0 = -2;
+            } else {
+              passed = sprt_verify(mk, slot.models32 + 12 * k, sc, Est::CTA_VALIDITY ? slot.list1 : nullptr, st0, ln);
+            }
             tock(3, t0);
             Container ct;
             ct.model = mk;
@@ -2024,6 +2281,16 @@ struct Engine {
             ct.len = ln;
             cont[off] = ct;
             if (!passed) continue;
+          } else if (sp && !mag) {
+            // MSAC over the kept points, cell by cell
+            sc = exact_score_sp(mk, Est::CTA_VALIDITY ? slot.list1 : nullptr);
+            Container ct;
+            ct.model = mk;
+            ct.count = sc.count;
+            ct.start = -2;
+            ct.len = sp_count;
+            cont[off] = ct;
+            if (sc.count == 0) continue;
           } else {
             cont[off] = {mk, sh.mcount[k]};
             if (sh.mcount[k] == 0 || !maybe_better(k, best.value)) continue;

@@ -106,6 +106,7 @@ size_t slot_bytes(int max_n, int sort_cap, bool light = false) {
     s += al(sizeof(int) * 16 * (size_t)max_n);
     s += al(sizeof(int) * (size_t)max_n);
     s += al(sizeof(double) * GCR_BLOCK);
+    s += 3 * al(sizeof(int) * (size_t)max_n);
     s += al(sizeof(unsigned long long) * sort_cap);
     s += al(sizeof(int) * max_n);
     s += al(sizeof(int) * (max_n + 1));
@@ -137,6 +138,9 @@ Slot carve_slot(unsigned char* base, int max_n, int sort_cap, bool light = false
     s.napsac = (int*)take(sizeof(int) * 16 * (size_t)max_n);
     s.sprt_pool = (int*)take(sizeof(int) * (size_t)max_n);
     s.sprt_buf = (double*)take(sizeof(double) * GCR_BLOCK);
+    s.sp_cell = (int*)take(sizeof(int) * (size_t)max_n);
+    s.sp_flag = (int*)take(sizeof(int) * (size_t)max_n);
+    s.sp_sel = (int*)take(sizeof(int) * (size_t)max_n);
     s.sortbuf = (unsigned long long*)take(sizeof(unsigned long long) * sort_cap);
     s.cell_pts = (int*)take(sizeof(int) * max_n);
     s.cell_start = (int*)take(sizeof(int) * (max_n + 1));

@@ -75,7 +75,7 @@ typedef struct gcr_params {
   int32_t lo_number;               /* inner-RANSAC trials per graph-cut */
   int32_t scoring;                 /* GCR_SCORING_* */
   int32_t use_sprt;                /* SPRT preemptive verification of main-loop models */
-  int32_t use_space_partitioning;  /* accepted; the engine scores every point */
+  int32_t use_space_partitioning;  /* homographies: space-partitioning pre-selection of models */
   uint64_t seed;                   /* seed of the counter-based sampler streams */
   double min_inlier_ratio_for_sprt; /* SPRT's initial inlier-ratio guess (epsilon) */
 } gcr_params;

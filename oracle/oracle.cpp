@@ -43,6 +43,7 @@ static void fill_settings(Settings& s, const gcr_params& p) {
   s.max_iteration_number = (size_t)p.max_iterations;
   s.min_iteration_number = (size_t)p.min_iterations;
   s.use_sprt = p.use_sprt != 0;
+  s.use_space_partitioning = p.use_space_partitioning != 0;
   s.sprt_min_inlier_ratio = p.min_inlier_ratio_for_sprt;
 }
 

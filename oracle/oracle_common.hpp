@@ -55,6 +55,7 @@ struct Settings {
   // min_inlier_ratio_for_sprt arguments)
   bool use_sprt = false;
   double sprt_min_inlier_ratio = 0.01;
+  bool use_space_partitioning = false;
 };
 
 struct Statistics {
@@ -230,17 +231,26 @@ struct ProsacSampler : Sampler {
 struct Grid {
   std::vector<std::vector<size_t>> cells;  // point lists, first-occurrence order
   std::vector<int64_t> cell_of_point;      // index into cells
+  std::vector<uint64_t> keys;              // key of each cell
+  std::vector<std::array<uint64_t, 4>> idx;  // cell indices along the four axes
+  std::vector<size_t> key_order;           // cells by ascending key
+  double cs[4] = {0, 0, 0, 0};
+  size_t nd = 0;
   size_t neighbor_number = 0;
   Grid() = default;
   Grid(const Mat& pts, const double cell_sizes[4], size_t n_div) {
     std::unordered_map<uint64_t, size_t> index;
     cell_of_point.assign(pts.rows, -1);
+    nd = n_div;
+    for (int dd = 0; dd < 4; ++dd) cs[dd] = cell_sizes[dd];
     for (int64_t r = 0; r < pts.rows; ++r) {
       const double* p = pts.row(r);
       uint64_t key = 0, off = 1;
+      std::array<uint64_t, 4> ci;
       for (int dd = 0; dd < 4; ++dd) {
-        const uint64_t idx = (uint64_t)(int64_t)std::floor(p[dd] / cell_sizes[dd]);
-        key += off * idx;
+        const uint64_t id = (uint64_t)(int64_t)std::floor(p[dd] / cell_sizes[dd]);
+        ci[dd] = id;
+        key += off * id;
         off *= (uint64_t)n_div;
       }
       auto it = index.find(key);
@@ -249,11 +259,16 @@ struct Grid {
         c = cells.size();
         index.emplace(key, c);
         cells.emplace_back();
+        keys.push_back(key);
+        idx.push_back(ci);
       } else c = it->second;
       cells[c].push_back((size_t)r);
       cell_of_point[r] = (int64_t)c;
     }
     for (auto& c : cells) neighbor_number += c.size() * (c.size() - 1) / 2;
+    key_order.resize(cells.size());
+    for (size_t c = 0; c < cells.size(); ++c) key_order[c] = c;
+    std::sort(key_order.begin(), key_order.end(), [&](size_t a, size_t b) { return keys[a] < keys[b]; });
   }
   const std::vector<size_t>& neighbors(size_t i) const { return cells[cell_of_point[i]]; }
   bool empty() const { return cells.empty(); }

@@ -1180,6 +1180,7 @@ inline void e_bundle_adjust(const Mat& pts, const size_t* s, size_t n, const dou
 // EssentialMatrixEstimator<Nister, Stewenius> (essential_estimator.h:57-402).
 struct EssentialEstimator {
   static constexpr size_t sample_size() { return 5; }
+  static constexpr bool space_partitioning = false;  // SpacePartitioningRANSAC applies
   static constexpr size_t max_solutions() { return 10; }  // maximumMinimalSolutions
   size_t sample_size_rt() const { return 5; }
   size_t inlier_limit() const { return 7 * sample_size(); }

@@ -295,6 +295,7 @@ struct FundamentalEstimator {
   static constexpr size_t kSample = 7;
   size_t sample_size_rt() const { return plane_parallax ? 2 : 7; }
   static constexpr size_t sample_size() { return 7; }
+  static constexpr bool space_partitioning = false;  // SpacePartitioningRANSAC applies
   static constexpr size_t max_solutions() { return 3; }  // maximumMinimalSolutions
   size_t inlier_limit() const { return 7 * sample_size_rt(); }
   size_t non_minimal_sample_size() const { return plane_parallax ? 8 : 7; }

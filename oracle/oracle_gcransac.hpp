@@ -103,6 +103,24 @@ struct MSACScoring {
     s.value = (s.value + (double)s.inlier_number * sq_trunc) / sq_trunc;
     return s;
   }
+  // getScore over index sets (scoring_function.h:186-218): the listed points
+  // in order
+  Score get_subset(const Mat& pts, const Model& m, const Est& est, const std::vector<size_t>& idx,
+                   std::vector<size_t>* inliers) const {
+    Score s;
+    if (inliers) inliers->clear();
+    for (size_t i : idx) {
+      const double r2 = est.squared_residual(pts.row(i), m);
+      if (r2 < sq_trunc) {
+        if (inliers) inliers->push_back(i);
+        ++s.inlier_number;
+        s.value -= r2;
+      }
+    }
+    if (s.inlier_number == 0) return Score();
+    s.value = (s.value + (double)s.inlier_number * sq_trunc) / sq_trunc;
+    return s;
+  }
 };
 
 // MAGSACScoringFunction::getScore (scoring_function.h:237-348). The weight
@@ -120,6 +138,12 @@ template <class Est>
 struct MAGSACScoring {
   double threshold = 0;  // settings.threshold (not the 1.5x truncated one)
   void initialize(double, size_t) {}
+  // MAGSAC++ scores every point even when index sets are given
+  // (scoring_function.h:253-304)
+  template <class Idx>
+  Score get_subset(const Mat& pts, const Model& m, const Est& est, const Idx&, std::vector<size_t>* inliers) const {
+    return get(pts, m, est, inliers);
+  }
   Score get(const Mat& pts, const Model& m, const Est& est, std::vector<size_t>* inliers) const {
     constexpr double k = 3.64;
     constexpr double C = 0.25;
@@ -153,6 +177,77 @@ struct MAGSACScoring {
     return s;
   }
 };
+
+// ---------------------------------------------------------------------------
+// SpacePartitioningRANSAC::runHomography (inlier_selectors/
+// space_partitioning_ransac.h:341-505): a cell with fewer than four points is
+// always kept; otherwise its four source-image corners are mapped by H and
+// the cell is kept when one lands in the cell's destination indices or when
+// the threshold-grown box of the mapped corners 00 and 11 overlaps the
+// destination cell. Cells are visited by ascending key (the reference visits
+// them in std::unordered_map order, which is library-specific). A mapped
+// coordinate outside the int range (or NaN) converts to INT_MIN.
+inline int sp_trunc_int(double v) {
+  if (!(v > -2147483649.0 && v < 2147483648.0)) return std::numeric_limits<int>::min();
+  return (int)v;
+}
+
+inline void sp_select(const Grid& g, const Model& H, double thr, std::vector<size_t>& sel, size_t& point_number) {
+  sel.clear();
+  point_number = 0;
+  if (std::fabs(det3(H)) < 1e-3) return;
+  const double cs1 = g.cs[0], cs2 = g.cs[1], cs3 = g.cs[2], cs4 = g.cs[3];
+  const uint64_t n = (uint64_t)g.nd;
+  auto proj = [&](uint64_t hx, uint64_t vy, double& x, double& y) {
+    const double X1 = (double)hx * cs1, Y1 = (double)vy * cs2;
+    double x2p = X1 * H[0] + Y1 * H[1] + H[2], y2p = X1 * H[3] + Y1 * H[4] + H[5],
+           h2p = X1 * H[6] + Y1 * H[7] + H[8];
+    x2p /= h2p;
+    y2p /= h2p;
+    x = x2p;
+    y = y2p;
+  };
+  const int steps[8] = {0, 0, 0, 1, 1, 0, 1, 1};
+  for (size_t c : g.key_order) {
+    const std::vector<size_t>& points = g.cells[c];
+    if (points.size() < 4) {
+      sel.push_back(c);
+      point_number += points.size();
+      continue;
+    }
+    const std::array<uint64_t, 4>& ci = g.idx[c];
+    bool overlaps = false;
+    double c00x = 0, c00y = 0, c11x = 0, c11y = 0;
+    for (int st = 0; st < 8; st += 2) {
+      const uint64_t hx = ci[0] + (uint64_t)steps[st];
+      if (hx >= n) continue;
+      const uint64_t vy = ci[1] + (uint64_t)steps[st + 1];
+      if (vy >= n) continue;
+      double x, y;
+      proj(hx, vy, x, y);
+      if (st == 0) { c00x = x; c00y = y; }
+      if (st == 6) { c11x = x; c11y = y; }
+      const int ix = sp_trunc_int(x / cs3), iy = sp_trunc_int(y / cs4);
+      if ((uint64_t)(int64_t)ix == ci[2] && (uint64_t)(int64_t)iy == ci[3]) {
+        sel.push_back(c);
+        point_number += points.size();
+        overlaps = true;
+        break;
+      }
+    }
+    if (!overlaps) {
+      const uint64_t hx11 = ci[0] + 1, vy11 = ci[1] + 1;
+      if (vy11 >= n || hx11 >= n) proj(hx11, vy11, c11x, c11y);
+      const double l1x = c00x - thr, l1y = c00y - thr, r1x = c11x + thr, r1y = c11y + thr;
+      const double l2x = cs3 * (double)ci[2], l2y = cs4 * (double)ci[3];
+      const double r2x = l2x + cs3, r2y = l2y + cs4;
+      if ((l1x <= r2x && l2x <= r1x) || (r1y <= l2y && r2y <= l1y)) {
+        sel.push_back(c);
+        point_number += points.size();
+      }
+    }
+  }
+}
 
 // ---------------------------------------------------------------------------
 // SPRTPreemptiveVerfication (preemption/preemption_sprt.h:50-380). Two inputs
@@ -199,11 +294,14 @@ struct Sprt {
     }
     return An;
   }
-  // verifyModel (preemption_sprt.h:232-347) without pre-selected index sets.
-  // Writes the tested inliers in pool order; returns whether the model passed.
+  // verifyModel (preemption_sprt.h:232-347). Without index sets the points
+  // are taken from the pool, continuing at the cursor; with index sets (space
+  // partitioning) the listed points are walked in order and the cursor stays.
+  // Writes the tested inliers in walk order; returns whether the model passed.
   template <class Est>
   bool verify(const Mat& pts, const Model& model, const Est& est, double threshold, size_t iteration,
-              const Score& best, std::vector<size_t>& inliers, Score& score) {
+              const Score& best, std::vector<size_t>& inliers, Score& score,
+              const std::vector<size_t>* index_set = nullptr) {
     inliers.clear();
     const size_t N = (size_t)pts.rows;
     const double sq = threshold * threshold;
@@ -211,7 +309,25 @@ struct Sprt {
     double lambda = 1, lambda_new;
     score = Score();
     bool valid = true;
-    for (size_t t = 0; t < N; ++t) {
+    if (index_set) {
+      for (size_t idx : *index_set) {
+        const double r2 = est.squared_residual(pts.row(idx), model);
+        if (r2 < sq) {
+          lambda_new = lambda * (del / eps);
+          ++score.inlier_number;
+          score.value += 1.0 - r2 / sq;
+          inliers.push_back(idx);
+        } else {
+          lambda_new = lambda * ((1 - del) / (1 - eps));
+        }
+        if (lambda_new > a * amp) {
+          valid = false;
+          break;
+        }
+        lambda = lambda_new;
+      }
+    }
+    for (size_t t = 0; t < N && !index_set; ++t) {
       const size_t idx = pool[cursor];
       const double r2 = est.squared_residual(pts.row(idx), model);
       if (r2 < sq) {
@@ -423,6 +539,8 @@ struct GCRansac {
     std::vector<Model> models;
     Sprt sprt;
     if (settings.use_sprt) sprt.init(N, m, Est::max_solutions(), settings.sprt_min_inlier_ratio, sprt_seed);
+    const bool use_sp = settings.use_space_partitioning && Est::space_partitioning && graph != nullptr;
+    std::vector<size_t> sp_cells, sp_points;
     while (settings.min_iteration_number > statistics.iteration_number ||
            statistics.iteration_number < std::min(max_iteration, settings.max_iteration_number)) {
       bool do_lo = false;
@@ -437,11 +555,25 @@ struct GCRansac {
       statistics.iteration_number += unsuccessful;
       for (Model& model : models) {
         ++models_scored;
+        const std::vector<size_t>* sel_pts = nullptr;
+        if (use_sp) {
+          // GCRANSAC.h:343-366: reject when the selected cells hold fewer
+          // points than the best model has inliers
+          size_t sel_n = 0;
+          sp_select(*graph, model, truncated_threshold, sp_cells, sel_n);
+          if (sel_n < best_score.inlier_number) continue;
+          sp_points.clear();
+          for (size_t c : sp_cells)
+            for (size_t p : graph->cells[c]) sp_points.push_back(p);
+          sel_pts = &sp_points;
+        }
         if (settings.use_sprt) {
           // SPRT provides the score (GCRANSAC.h:370-431)
           if (!sprt.verify(pts, model, est, truncated_threshold, statistics.iteration_number, best_score, cont[off],
-                           current_score))
+                           current_score, sel_pts))
             continue;
+        } else if (sel_pts) {
+          current_score = scoring.get_subset(pts, model, est, *sel_pts, &cont[off]);
         } else {
           current_score = scoring.get(pts, model, est, &cont[off]);
         }

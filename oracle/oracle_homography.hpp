@@ -10,6 +10,7 @@ namespace oracle {
 
 struct HomographyEstimator {
   static constexpr size_t sample_size() { return 4; }
+  static constexpr bool space_partitioning = true;  // SpacePartitioningRANSAC applies
   static constexpr size_t max_solutions() { return 1; }  // maximumMinimalSolutions
   size_t sample_size_rt() const { return 4; }
   static constexpr size_t non_minimal_sample_size() { return 4; }
