@@ -3,8 +3,9 @@
 
 One step = one batch of synthetic image pairs run to completion by the pair
 engine (one persistent launch). `value` is pairs/s with the correspondences
-resident in HBM (device-pointer C-ABI entry, CUDA events on the launching
-stream, L2 flushed between steps by a 256 MiB write); `e2e` is the same metric
+resident in HBM (device-pointer C-ABI entry: gcr_batch_prepare once, then each
+step replays the recorded gcr_batch_launch from a CUDA graph; CUDA events on the
+launching stream, L2 flushed between steps by a 256 MiB write); `e2e` is the same metric
 through the host-buffer C-ABI entry gcr_find_batch, host<->device copies
 included. `--impl reference` times the CPU restatement of the reference's
 path (the oracle) on all host cores instead.
@@ -244,6 +245,7 @@ def main():
            "pairs_per_step": P, "correspondences": w["n"], "threshold": w["threshold"], "sampler": w["sampler"],
            "grid": w["grid"], "spatial_coherence_weight": w["lam"],
            "scoring": "MAGSAC++" if w.get("scoring") == _abi.GCR_SCORING_MAGSAC else "MSAC",
+           "launch": "one persistent engine launch per step, replayed from a CUDA graph",
            "l2": "flushed between steps (256 MiB write)",
            "parallelism": f"replicas x{world}"}
 
@@ -290,13 +292,23 @@ def main():
     assert lib.gcr_context_create(ctypes.byref(ctx)) == 0, _abi.last_error()
     stream = torch.cuda.current_stream()
 
+    # one persistent launch per batch (plus the K^-1 normalisation for E),
+    # prepared once and recorded into a CUDA graph; a step is one replay
+    rc = lib.gcr_batch_prepare(ctx, kind, P, ctypes.c_void_p(d_corr.data_ptr()), _abi.ptr(offsets), _abi.ptr(K),
+                               _abi.ptr(szs), ctypes.byref(p), _abi.ptr(seeds), ctypes.c_void_p(d_models.data_ptr()),
+                               ctypes.c_void_p(d_masks.data_ptr()), ctypes.c_void_p(d_stats.data_ptr()))
+    assert rc == 0, _abi.last_error()
+    graph = torch.cuda.CUDAGraph()
+    cap = torch.cuda.Stream()
+    with torch.cuda.stream(cap):
+        with torch.cuda.graph(graph, stream=cap):
+            rc = lib.gcr_batch_launch(ctx, ctypes.c_void_p(cap.cuda_stream))
+    assert rc == 0, _abi.last_error()
+    launches_per_step = int(lib.gcr_last_launch_count())
+
     def step():
-        rc = lib.gcr_batch_run_device(ctx, kind, P, ctypes.c_void_p(d_corr.data_ptr()), _abi.ptr(offsets), _abi.ptr(K),
-                                      _abi.ptr(szs), ctypes.byref(p), _abi.ptr(seeds),
-                                      ctypes.c_void_p(d_models.data_ptr()), ctypes.c_void_p(d_masks.data_ptr()),
-                                      ctypes.c_void_p(d_stats.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
-        assert rc == 0, _abi.last_error()
-        return lib.gcr_last_launch_count()
+        graph.replay()
+        return launches_per_step
 
     for _ in range(args.warmup):
         step()

@@ -81,6 +81,17 @@ struct gcr_context {
   // staging of the host-buffer entry points
   DevBuf corr, models, masks, stats;
   DevBuf magsac;  // the MAGSAC++ weight table, uploaded on first use
+  // the device work of the last prepared batch (see gcr_batch_prepare)
+  struct Pending {
+    bool valid = false;
+    const gcr::KindOps* ops = nullptr;
+    int grid = 0;
+    gcr::Workspace ws{};
+    gcr::EngineParams prm{};
+    bool normalise = false;
+    const double* d_corr = nullptr;
+    int num_pairs = 0;
+  } pending;
   int slot_kind = -1, slot_max_n = 0, slot_count = 0;
   bool prepared[3] = {false, false, false};
 };
@@ -202,11 +213,18 @@ gcr_status gcr_context_destroy(gcr_context* c) {
 
 // Device-resident batch: bulk arrays are device pointers, per-pair metadata
 // (offsets, intrinsics, image sizes, seeds) are host arrays.
-gcr_status gcr_batch_run_device(gcr_context* c, gcr_model_kind kind, int64_t num_pairs, const double* d_corr,
-                                const int64_t* h_offsets, const double* h_K,
-                                const gcr_image_size* h_sizes, const gcr_params* params, const uint64_t* h_seeds,
-                                double* d_models_out, uint8_t* d_masks_out, gcr_stats* d_stats_out, void* stream) {
-  g_last_launches = 0;
+}  // extern "C"
+
+// Host side of a batch: argument checks, scratch growth, descriptor and
+// intrinsics uploads (queued on s). The device work it describes (ticket
+// reset, K^-1 normalisation, engine launch) is recorded in *L and queued by
+// launch_batch.
+static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num_pairs, const double* d_corr,
+                                const int64_t* h_offsets, const double* h_K, const gcr_image_size* h_sizes,
+                                const gcr_params* params, const uint64_t* h_seeds, double* d_models_out,
+                                uint8_t* d_masks_out, gcr_stats* d_stats_out, cudaStream_t s,
+                                gcr_context::Pending* L) {
+  L->valid = false;
   if (!c) return fail(GCR_INVALID_ARG, "context is NULL");
   const gcr::KindOps* ops = ops_for(kind);
   if (!ops) return fail(GCR_UNSUPPORTED, "model kind %d is not provided by this build", (int)kind);
@@ -229,7 +247,6 @@ gcr_status gcr_batch_run_device(gcr_context* c, gcr_model_kind kind, int64_t num
   }
   const int64_t total = h_offsets[num_pairs] - h_offsets[0];
   if (h_offsets[0] != 0) return fail(GCR_INVALID_ARG, "offsets[0] must be 0");
-  cudaStream_t s = (cudaStream_t)stream;
 
   if (!c->prepared[kind]) {
     CUDA_TRY(ops->prepare());
@@ -320,13 +337,10 @@ gcr_status gcr_batch_run_device(gcr_context* c, gcr_model_kind kind, int64_t num
     // (a copy from pageable memory is staged before the call returns)
     CUDA_TRY(cudaMemcpyAsync(c->kinv.p, kinv.data(), sizeof(double) * kinv.size(), cudaMemcpyHostToDevice, s));
     CUDA_TRY(c->norm_pts.ensure(sizeof(double) * 4 * (size_t)std::max<int64_t>(total, 1)));
-    CUDA_TRY(gcr::launch_normalise_essential(d_corr, (const double*)c->kinv.p, (const gcr::PairDesc*)c->pairs.p,
-                                             (int)num_pairs, (double*)c->norm_pts.p, s));
     run_pts = (const double*)c->norm_pts.p;
   }
   if (max_n > gcr::kSmemPoints) CUDA_TRY(c->pts32.ensure(sizeof(float4) * (size_t)total));
   CUDA_TRY(c->ticket.ensure(sizeof(int)));
-  CUDA_TRY(cudaMemsetAsync(c->ticket.p, 0, sizeof(int), s));
 
   gcr::Workspace ws;
   ws.pts64 = run_pts;
@@ -379,9 +393,70 @@ gcr_status gcr_batch_run_device(gcr_context* c, gcr_model_kind kind, int64_t num
     }
     prm.mag_table = (const double*)c->magsac.p;
   }
-  CUDA_TRY(ops->launch(grid, s, ws, prm));
-  g_last_launches = kind == GCR_ESSENTIAL ? 2 : 1;
+  L->ops = ops;
+  L->grid = grid;
+  L->ws = ws;
+  L->prm = prm;
+  L->normalise = kind == GCR_ESSENTIAL;
+  L->d_corr = d_corr;
+  L->num_pairs = (int)num_pairs;
+  L->valid = true;
   return GCR_OK;
+}
+
+// Device side of a prepared batch: only stream work (a memset and kernel
+// launches), so it can be recorded into a CUDA graph.
+static gcr_status launch_batch(gcr_context* c, const gcr_context::Pending& L, cudaStream_t s) {
+  CUDA_TRY(cudaMemsetAsync(c->ticket.p, 0, sizeof(int), s));
+  int launches = 1;
+  if (L.normalise) {
+    CUDA_TRY(gcr::launch_normalise_essential(L.d_corr, (const double*)c->kinv.p, (const gcr::PairDesc*)c->pairs.p,
+                                             L.num_pairs, (double*)c->norm_pts.p, s));
+    ++launches;
+  }
+  CUDA_TRY(L.ops->launch(L.grid, s, L.ws, L.prm));
+  g_last_launches = launches;
+  return GCR_OK;
+}
+
+extern "C" {
+
+gcr_status gcr_batch_run_device(gcr_context* c, gcr_model_kind kind, int64_t num_pairs, const double* d_corr,
+                                const int64_t* h_offsets, const double* h_K,
+                                const gcr_image_size* h_sizes, const gcr_params* params, const uint64_t* h_seeds,
+                                double* d_models_out, uint8_t* d_masks_out, gcr_stats* d_stats_out, void* stream) {
+  g_last_launches = 0;
+  if (!c) return fail(GCR_INVALID_ARG, "context is NULL");
+  if (num_pairs <= 0) return GCR_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  c->pending.valid = false;  // the scratch a prepared batch refers to may move
+  gcr_context::Pending L;
+  gcr_status st = prepare_batch(c, kind, num_pairs, d_corr, h_offsets, h_K, h_sizes, params, h_seeds, d_models_out,
+                                d_masks_out, d_stats_out, s, &L);
+  if (st != GCR_OK || !L.valid) return st;
+  return launch_batch(c, L, s);
+}
+
+gcr_status gcr_batch_prepare(gcr_context* c, gcr_model_kind kind, int64_t num_pairs, const double* d_corr,
+                             const int64_t* h_offsets, const double* h_K, const gcr_image_size* h_sizes,
+                             const gcr_params* params, const uint64_t* h_seeds, double* d_models_out,
+                             uint8_t* d_masks_out, gcr_stats* d_stats_out) {
+  g_last_launches = 0;
+  if (!c) return fail(GCR_INVALID_ARG, "context is NULL");
+  c->pending.valid = false;
+  if (num_pairs <= 0) return fail(GCR_INVALID_ARG, "num_pairs must be positive");
+  gcr_status st = prepare_batch(c, kind, num_pairs, d_corr, h_offsets, h_K, h_sizes, params, h_seeds, d_models_out,
+                                d_masks_out, d_stats_out, 0, &c->pending);
+  if (st != GCR_OK) return st;
+  CUDA_TRY(cudaStreamSynchronize(0));
+  return GCR_OK;
+}
+
+gcr_status gcr_batch_launch(gcr_context* c, void* stream) {
+  g_last_launches = 0;
+  if (!c) return fail(GCR_INVALID_ARG, "context is NULL");
+  if (!c->pending.valid) return fail(GCR_INVALID_ARG, "no prepared batch on this context (call gcr_batch_prepare)");
+  return launch_batch(c, c->pending, (cudaStream_t)stream);
 }
 
 gcr_status gcr_find_batch(gcr_model_kind kind, int64_t num_pairs, const double* corr, const int64_t* offsets,

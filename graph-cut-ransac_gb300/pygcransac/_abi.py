@@ -99,6 +99,8 @@ _EXPORTS = {
                                             _P, _P, _P]),
     "gcr_find_homography_device_noalloc": (ctypes.c_int, [_P, ctypes.c_int64, _P, _P, ctypes.c_uint64, _P, _P, _P,
                                                           _P]),
+    "gcr_batch_prepare": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int64, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "gcr_batch_launch": (ctypes.c_int, [_P, _P]),
     "gcr_last_launch_count": (ctypes.c_int64, []),
     "gcr_last_error_string": (ctypes.c_char_p, []),
 }

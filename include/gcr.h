@@ -181,7 +181,24 @@ gcr_status gcr_find_homography_device_noalloc(const double* d_corr, int64_t n,
                                               uint64_t seed, double* d_model_out9, uint8_t* d_mask_out,
                                               gcr_stats* d_stats_out, void* stream);
 
-/* Number of kernels the last gcr_batch_run_device / gcr_find_* call launched. */
+/* gcr_batch_run_device split in two, for CUDA-graph capture. gcr_batch_prepare
+ * does the host side (argument checks, scratch growth, per-pair descriptor and
+ * intrinsics uploads; it returns after those copies complete) and records the
+ * batch's device work in ctx. gcr_batch_launch queues that device work on
+ * `stream`: a memset and kernel launches only, no allocation and no host
+ * copies, so it can be recorded into a CUDA graph and replayed; each replay
+ * re-runs the batch on the current contents of the device buffers given to
+ * gcr_batch_prepare (new correspondences of the same sizes may be written there
+ * between replays). A prepared batch stays valid until the next
+ * gcr_batch_prepare or gcr_batch_run_device on the same context. */
+gcr_status gcr_batch_prepare(gcr_context* ctx, gcr_model_kind kind, int64_t num_pairs,
+                             const double* d_corr, const int64_t* h_offsets, const double* h_K,
+                             const gcr_image_size* h_sizes, const gcr_params* params,
+                             const uint64_t* h_seeds, double* d_models_out, uint8_t* d_masks_out,
+                             gcr_stats* d_stats_out);
+gcr_status gcr_batch_launch(gcr_context* ctx, void* stream);
+
+/* Number of kernels the last gcr_batch_run_device / gcr_batch_launch / gcr_find_* call launched. */
 int64_t gcr_last_launch_count(void);
 
 /* Message of the last failing call on this host thread. */

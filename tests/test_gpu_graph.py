@@ -1,0 +1,80 @@
+"""GPU test of the prepared batch launch recorded into a CUDA graph:
+gcr_batch_prepare + gcr_batch_launch captured with torch.cuda.graph and
+replayed must give the results of gcr_batch_run_device, also after new
+correspondences are written into the same device buffer."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from pygcransac import _abi, synthetic as S
+
+pytestmark = pytest.mark.gpu
+
+
+def run_kind(kind, pairs, p, K=None):
+    torch = pytest.importorskip("torch")
+    lib = _abi.load()
+    corr = np.concatenate([pr["corr"] for pr in pairs])
+    offsets = np.zeros(len(pairs) + 1, np.int64)
+    offsets[1:] = np.cumsum([len(pr["corr"]) for pr in pairs])
+    sizes = np.zeros(len(pairs), _abi.SIZE_DTYPE)
+    for i, pr in enumerate(pairs):
+        sizes[i] = pr["size"]
+    P = len(pairs)
+    seeds = np.arange(P, dtype=np.uint64) + np.uint64(5)
+    d_corr = torch.from_numpy(np.ascontiguousarray(corr)).cuda()
+    outs = []
+    for _ in range(2):
+        outs.append((torch.zeros(P * 9, dtype=torch.float64, device="cuda"),
+                     torch.zeros(len(corr), dtype=torch.uint8, device="cuda"),
+                     torch.zeros(P * _abi.STATS_DTYPE.itemsize, dtype=torch.uint8, device="cuda")))
+    ctx = ctypes.c_void_p()
+    assert lib.gcr_context_create(ctypes.byref(ctx)) == 0
+    ptr = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    Kp = _abi.ptr(K)
+    # reference: the one-call form
+    rc = lib.gcr_batch_run_device(ctx, kind, P, ptr(d_corr), _abi.ptr(offsets), Kp, _abi.ptr(sizes),
+                                  ctypes.byref(p), _abi.ptr(seeds), ptr(outs[0][0]), ptr(outs[0][1]),
+                                  ptr(outs[0][2]), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == 0, _abi.last_error()
+    torch.cuda.synchronize()
+    # prepared + captured
+    rc = lib.gcr_batch_prepare(ctx, kind, P, ptr(d_corr), _abi.ptr(offsets), Kp, _abi.ptr(sizes), ctypes.byref(p),
+                               _abi.ptr(seeds), ptr(outs[1][0]), ptr(outs[1][1]), ptr(outs[1][2]))
+    assert rc == 0, _abi.last_error()
+    g = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s):
+            rc = lib.gcr_batch_launch(ctx, ctypes.c_void_p(s.cuda_stream))
+    assert rc == 0, _abi.last_error()
+    for _ in range(2):
+        outs[1][2].zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        assert torch.equal(outs[0][1], outs[1][1])
+        assert torch.equal(outs[0][2], outs[1][2])
+        assert torch.allclose(outs[0][0], outs[1][0], rtol=0, atol=1e-12)
+    # new correspondences in the same buffer: the replay follows them
+    d_corr.copy_(torch.from_numpy(np.ascontiguousarray(corr[::-1].copy())))
+    g.replay()
+    torch.cuda.synchronize()
+    assert not torch.equal(outs[0][1], outs[1][1])
+    lib.gcr_context_destroy(ctx)
+
+
+def test_graph_replay_homography():
+    pairs = [S.homography_pair(s, n=1000 + 200 * s) for s in range(6)]
+    p = _abi.Params(threshold=3.0, confidence=0.99, spatial_coherence_weight=0.975, neighborhood_size=4,
+                    max_iterations=2000, min_iterations=50, sampler=0, neighborhood=0, lo_number=50, seed=0)
+    run_kind(_abi.GCR_HOMOGRAPHY, pairs, p)
+
+
+def test_graph_replay_essential():
+    pairs = [S.two_view_pair(s, n=600 + 100 * s, inlier_ratio=0.5) for s in range(4)]
+    K = np.stack([np.concatenate([pr["K"].ravel(), pr["K"].ravel()]) for pr in pairs])
+    p = _abi.Params(threshold=0.75, confidence=0.99, spatial_coherence_weight=0.1, neighborhood_size=8,
+                    max_iterations=500, min_iterations=50, sampler=0, neighborhood=0, lo_number=20, seed=0,
+                    scoring=_abi.GCR_SCORING_MAGSAC)
+    run_kind(_abi.GCR_ESSENTIAL, pairs, p, K=K)
