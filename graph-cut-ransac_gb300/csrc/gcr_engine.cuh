@@ -1508,7 +1508,40 @@ struct Engine {
           }
         }
       } else {
-        if (ss < nL) {
+        if (Est::KIND == 1 && ss < nL) {
+          // fundamental matrices: each trial on a group of four lanes; lane 0
+          // of the group draws the sample with the LO sampler stream
+          const int kb = kBatchModels;
+          const int q = threadIdx.x & 3;
+          const unsigned gmask = 0xFu << (threadIdx.x & 28);
+          for (int u0 = 0; u0 < trials; u0 += GCR_BLOCK / 4) {
+            const int u = u0 + (threadIdx.x >> 2);
+            if (u < trials) {
+              int* smp = slot.samples + u * Est::SAMPLE_CAP;
+              if (q == 0) {
+                DrawStream ds(pd.seed, prm.stream_lo, (uint64_t)(lo_calls + u));
+                const bool ok = unique_set(ds, smp, ss, 0, (uint32_t)(nL - 1));
+                if (ok)
+                  for (int k = 0; k < ss; ++k) smp[k] = L[smp[k]];
+                sh.lo_ok[u] = ok ? 1 : 0;
+              }
+              __syncwarp(gmask);
+              bool ok = sh.lo_ok[u] != 0;
+              if (ok) ok = FundamentalModel::fit_group(pts64, smp, ss, slot.models64 + 9 * (kb + u), q, gmask);
+              __syncwarp(gmask);
+              if (q == 0) {
+                sh.lo_ok[u] = ok ? 1 : 0;
+                if (ok) put_f32(kb + u);
+              }
+            }
+          }
+          sync();
+          tock(5, t0);
+          lo_calls += trials;
+          t0 = tick();
+          score_lo_trials(kb, trials, max_score, updated);
+          tock(6, t0);
+        } else if (ss < nL) {
           // one thread per trial draws the sample from the labelled inliers with
           // the LO sampler stream and fits it
           const int kb = kBatchModels;

@@ -624,6 +624,109 @@ struct FundamentalModel {
     for (int i = 0; i < 9; ++i) out[i] = sgn * (G[i] / nrm);
   }
 
+  // The same fit by a group of four lanes of one warp (lane q of the group
+  // takes rows q, q + 4, ...; `mask` selects the group's lanes): every sum
+  // over the rows is formed per lane and combined by two butterfly steps,
+  // ((s0 + s1) + (s2 + s3)) in every lane, and the small solves run in all
+  // four lanes in lockstep. The rows' work per lane is a quarter of the
+  // one-thread fit, which shortens the dependent chain of each LM iteration.
+  __device__ static double sum4(double v, unsigned mask) {
+    v += __shfl_xor_sync(mask, v, 1);
+    v += __shfl_xor_sync(mask, v, 2);
+    return v;
+  }
+  __device__ static bool fit_group(const double* pts, const int* idx, int n, double* out, int q, unsigned mask) {
+    if (n < 8) return false;
+    Norm N;
+    {
+      double a = 0, b = 0, c = 0, d = 0;
+      for (int i = q; i < n; i += 4) {
+        const double* p = pts + 4 * idx[i];
+        a += p[0]; b += p[1]; c += p[2]; d += p[3];
+      }
+      a = sum4(a, mask); b = sum4(b, mask); c = sum4(c, mask); d = sum4(d, mask);
+      N.ms0 = a / n; N.ms1 = b / n; N.md0 = c / n; N.md1 = d / n;
+      double ads = 0, add = 0;
+      for (int i = q; i < n; i += 4) {
+        const double* p = pts + 4 * idx[i];
+        const double dx1 = N.ms0 - p[0], dy1 = N.ms1 - p[1], dx2 = N.md0 - p[2], dy2 = N.md1 - p[3];
+        ads += sqrt(dx1 * dx1 + dy1 * dy1);
+        add += sqrt(dx2 * dx2 + dy2 * dy2);
+      }
+      ads = sum4(ads, mask);
+      add = sum4(add, mask);
+      N.rs = M_SQRT2 / (ads / n);
+      N.rd = M_SQRT2 / (add / n);
+    }
+    double F[9];
+    {
+      double ata[NATA];
+#pragma unroll
+      for (int k = 0; k < NATA; ++k) ata[k] = 0;
+      for (int i = q; i < n; i += 4) accumulate_ata(N, pts + 4 * idx[i], 1.0, ata);
+#pragma unroll
+      for (int k = 0; k < NATA; ++k) ata[k] = sum4(ata[k], mask);
+      eight_point_from_ata(ata, F);
+    }
+    FactF f;
+    factf_from(F, f);
+    auto cost_of = [&](const double* G) {
+      double c = 0;
+      for (int i = q; i < n; i += 4) {
+        const double* p = pts + 4 * idx[i];
+        c += lm_cost_point(G, (p[0] - N.ms0) * N.rs, (p[1] - N.ms1) * N.rs, (p[2] - N.md0) * N.rd,
+                           (p[3] - N.md1) * N.rd);
+      }
+      return sum4(c, mask);
+    };
+    double G[9];
+    factf_F(f, G);
+    double lambda = 1e-3;
+    double cost = cost_of(G);
+    bool recompute = true;
+    double acc[NLM];
+    for (int iter = 0; iter < 25; ++iter) {
+      if (recompute) {
+#pragma unroll
+        for (int k = 0; k < NLM; ++k) acc[k] = 0;
+        double ds[9];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) ds[i * 3 + j] = f.U[i * 3 + 1] * f.V[j * 3 + 1];
+        for (int i = q; i < n; i += 4) {
+          const double* p = pts + 4 * idx[i];
+          lm_accumulate_point_s(G, ds, (p[0] - N.ms0) * N.rs, (p[1] - N.ms1) * N.rs, (p[2] - N.md0) * N.rd,
+                                (p[3] - N.md1) * N.rd, n, acc);
+        }
+#pragma unroll
+        for (int k = 0; k < NLM; ++k) acc[k] = sum4(acc[k], mask);
+        double gn = 0;
+#pragma unroll
+        for (int a = 0; a < 7; ++a) gn += acc[28 + a] * acc[28 + a];
+        if (sqrt(gn) < 1e-8) break;
+      }
+      FactF fn;
+      if (!lm_step(acc, lambda, f, fn)) break;
+      double Gn[9];
+      factf_F(fn, Gn);
+      const double cn = cost_of(Gn);
+      if (cn < cost) {
+        f = fn;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) G[k] = Gn[k];
+        lambda /= 10;
+        cost = cn;
+        recompute = true;
+      } else {
+        lambda *= 10;
+        recompute = false;
+      }
+    }
+    if (q == 0) denormalise(N, G, out);
+    return true;
+  }
+
   // Per-thread non-minimal fit with unit weights (the local-optimisation
   // trials run one per thread): normalisation, 8-point start, 25 LM
   // iterations on the factorised F, denormalisation. The model of the
