@@ -174,6 +174,26 @@ def fp32_peak_tflops(torch):
     return best
 
 
+def replica_shard(workload, pairs, rank):
+    """The batch and sampler seeds of one replica: every rank runs its own
+    independent pairs (weak scaling, no collective on the data path)."""
+    corr, offsets, sizes, gts, K = build_pairs(workload, pairs, 1000003 * rank)
+    seeds = np.arange(pairs, dtype=np.uint64) + np.uint64(pairs * rank)
+    return corr, offsets, sizes, gts, K, seeds
+
+
+def aggregate_rate(units_per_rank, seconds, world, dist=None, device="cpu"):
+    """Whole-job rate over replicas: units of all ranks divided by the slowest
+    rank's time (max over ranks)."""
+    t = seconds
+    if dist is not None:
+        import torch
+        tt = torch.tensor([seconds], device=device, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    return units_per_rank * world / t, t
+
+
 def fp64_peak_tflops(torch):
     """Measured FP64 peak: cuBLAS DGEMM 4096^3."""
     a = torch.randn(4096, 4096, device="cuda", dtype=torch.float64)
@@ -278,10 +298,9 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
 
     lib = _abi.load()
-    corr, offsets, sizes, gts, K = build_pairs(args.workload, P, 1000003 * rank)
+    corr, offsets, sizes, gts, K, seeds = replica_shard(args.workload, P, rank)
     p = params_for(args.workload)
     kind = w["kind"]
-    seeds = np.arange(P, dtype=np.uint64) + np.uint64(P * rank)
     szs = size_array(sizes)
     d_corr = torch.from_numpy(corr).cuda()
     d_models = torch.zeros(P * 9, dtype=torch.float64, device="cuda")
@@ -329,13 +348,9 @@ def main():
         total_ms += e0.elapsed_time(e1)
     torch.cuda.synchronize()
     clk = clocks.stop()
-    t_rank = total_ms / 1e3
+    value, t_rank = aggregate_rate(P * args.steps, total_ms / 1e3, world, dist, "cuda")
     if dist:
-        t = torch.tensor([t_rank], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_rank = float(t.item())
         dist.barrier()
-    value = P * world * args.steps / t_rank
 
     stats = np.frombuffer(d_stats.cpu().numpy().tobytes(), _abi.STATS_DTYPE)
     models = d_models.cpu().numpy().reshape(P, 3, 3)
@@ -364,11 +379,7 @@ def main():
         t0 = time.perf_counter()
         e2e_step()
         e2e_t += time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_t], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_t = float(t.item())
-    e2e_value = P * world * args.steps / e2e_t
+    e2e_value, e2e_t = aggregate_rate(P * args.steps, e2e_t, world, dist, "cuda")
 
     if rank != 0:
         if dist:
