@@ -1,0 +1,525 @@
+// Learned inlier-probability proposal: per-correspondence features, a small
+// MLP (BF16 weights, FP32 accumulation) and its training kernels. The
+// predicted probabilities order the correspondences for the PROSAC sampler.
+//
+// Features of correspondence i of a pair (kFeat = 20 values, padded to 32):
+//   (x1/w1 - 0.5, y1/h1 - 0.5, x2/w2 - 0.5, y2/h2 - 0.5) and, for each of the
+//   k = 8 nearest neighbours j of i in the first image (FP32 squared
+//   distance, ties by index), the pair
+//     (|d_j - d_i|^(1/2) / 4, |x1_j - x1_i|^(1/2) / 4)
+//   with d = x2 - x1 the displacement in pixels, the k pairs ordered by the
+//   first value (a missing neighbour gives (4, 4) and sorts last). Inliers of
+//   a coherent motion have near neighbours that move alike; a random match
+//   does not.
+// Network: 32 -> 128 -> 128 -> 128 -> 1, ReLU between layers, the last output
+// is a logit. Parameters are kept as FP32 master copies (Adam) and BF16 copies
+// used by the forward and backward passes.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+
+#include "../../include/gcr.h"
+
+namespace gcr {
+void set_last_error(const char* msg);
+}
+
+namespace {
+
+constexpr int kK = 8;          // neighbours
+constexpr int kFeat = 20;      // real features
+constexpr int kIn = 32;        // padded input width
+constexpr int kH = 128;        // hidden width
+constexpr int kRows = 16;      // rows (correspondences) per CTA of the MLP passes
+constexpr int kTile = 128;     // query rows per CTA of the neighbour search and the ordering
+constexpr int kCand = 2048;    // candidates staged in shared memory per round
+constexpr double kMissing = 65536.0;  // squared length standing in for a missing neighbour (feature 4.0)
+// parameter layout (floats): W1 [kIn][kH], b1 [kH], W2 [kH][kH], b2, W3, b3, W4 [kH], b4 [1]
+constexpr int kOffW1 = 0;
+constexpr int kOffB1 = kOffW1 + kIn * kH;
+constexpr int kOffW2 = kOffB1 + kH;
+constexpr int kOffB2 = kOffW2 + kH * kH;
+constexpr int kOffW3 = kOffB2 + kH;
+constexpr int kOffB3 = kOffW3 + kH * kH;
+constexpr int kOffW4 = kOffB3 + kH;
+constexpr int kOffB4 = kOffW4 + kH;
+constexpr int kParams = kOffB4 + 1;
+
+gcr_status fail(gcr_status s, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  gcr::set_last_error(buf);
+  return s;
+}
+
+#define CUDA_TRY(expr)                                                                    \
+  do {                                                                                    \
+    cudaError_t e_ = (expr);                                                              \
+    if (e_ != cudaSuccess) return fail(GCR_DEVICE_ERROR, "%s failed: %s", #expr, cudaGetErrorString(e_)); \
+  } while (0)
+
+// Features: grid (tile of kTile rows, pair). Each thread holds one query
+// correspondence; the pair's first-image points are staged through shared
+// memory in rounds of kCand and scanned with FP32 squared distances (each
+// operation rounded on its own, so the selection is reproducible on any
+// IEEE host), keeping the k nearest in registers (ascending distance, ties by
+// index).
+__global__ void __launch_bounds__(kTile) features_kernel(const double* corr, const int64_t* offsets,
+                                                         const gcr_image_size* sizes, float* feat) {
+  __shared__ float2 cand[kCand];
+  const int pair = blockIdx.y;
+  const int64_t o0 = offsets[pair];
+  const int n = (int)(offsets[pair + 1] - o0);
+  if ((int)blockIdx.x * kTile >= n) return;  // uniform over the CTA
+  const int i = (int)blockIdx.x * kTile + threadIdx.x;
+  const bool active = i < n;
+  float px = 0.f, py = 0.f;
+  if (active) {
+    px = (float)corr[4 * (o0 + i)];
+    py = (float)corr[4 * (o0 + i) + 1];
+  }
+  float bd[kK];
+  int bi[kK];
+#pragma unroll
+  for (int k = 0; k < kK; ++k) {
+    bd[k] = INFINITY;
+    bi[k] = -1;
+  }
+  for (int c0 = 0; c0 < n; c0 += kCand) {
+    const int m = min(kCand, n - c0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < m; t += kTile) {
+      const double* q = corr + 4 * (o0 + c0 + t);
+      cand[t] = make_float2((float)q[0], (float)q[1]);
+    }
+    __syncthreads();
+    if (!active) continue;
+    for (int t = 0; t < m; ++t) {
+      const float2 q = cand[t];
+      const float ex = __fsub_rn(q.x, px), ey = __fsub_rn(q.y, py);
+      const float d = __fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey));
+      if (d < bd[kK - 1] && c0 + t != i) {
+        bd[kK - 1] = d;
+        bi[kK - 1] = c0 + t;
+#pragma unroll
+        for (int k = kK - 1; k > 0; --k) {
+          if (bd[k] < bd[k - 1]) {
+            const float tf = bd[k];
+            bd[k] = bd[k - 1];
+            bd[k - 1] = tf;
+            const int ti = bi[k];
+            bi[k] = bi[k - 1];
+            bi[k - 1] = ti;
+          }
+        }
+      }
+    }
+  }
+  if (!active) return;
+  const gcr_image_size z = sizes[pair];
+  const double* p = corr + 4 * (o0 + i);
+  float* f = feat + (int64_t)kIn * (o0 + i);
+  f[0] = (float)(p[0] / z.w1 - 0.5);
+  f[1] = (float)(p[1] / z.h1 - 0.5);
+  f[2] = (float)(p[2] / z.w2 - 0.5);
+  f[3] = (float)(p[3] / z.h2 - 0.5);
+  // per neighbour: squared length of the displacement difference (pixels)
+  // and squared first-image distance, ordered by the former (ascending,
+  // stable), so the first entry is the best-agreeing neighbour; missing
+  // neighbours sort last
+  const double dx = p[2] - p[0], dy = p[3] - p[1];
+  double dm[kK], dd[kK];
+#pragma unroll
+  for (int k = 0; k < kK; ++k) {
+    double mag = kMissing, dist = kMissing;
+    if (bi[k] >= 0) {
+      const double* q = corr + 4 * (o0 + bi[k]);
+      const double a = (q[2] - q[0]) - dx, b = (q[3] - q[1]) - dy;
+      const double ex = q[0] - p[0], ey = q[1] - p[1];
+      mag = __dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b));
+      dist = __dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey));
+    }
+    dm[k] = mag;
+    dd[k] = dist;
+#pragma unroll
+    for (int t = k; t > 0; --t) {
+      if (dm[t] < dm[t - 1]) {
+        double x = dm[t]; dm[t] = dm[t - 1]; dm[t - 1] = x;
+        x = dd[t]; dd[t] = dd[t - 1]; dd[t - 1] = x;
+      }
+    }
+  }
+  // fourth roots (square roots of lengths) compress the pixel range: an
+  // agreeing inlier neighbour gives about 1, a random one about 17
+#pragma unroll
+  for (int k = 0; k < kK; ++k) {
+    f[4 + 2 * k] = (float)(0.25 * sqrt(sqrt(dm[k])));
+    f[5 + 2 * k] = (float)(0.25 * sqrt(sqrt(dd[k])));
+  }
+#pragma unroll
+  for (int c = kFeat; c < kIn; ++c) f[c] = 0.f;
+}
+
+__device__ __forceinline__ float bf(const __nv_bfloat16* w, int i) { return __bfloat162float(w[i]); }
+
+__device__ __forceinline__ float4 bf4(const __nv_bfloat16* w, int i) {
+  const uint2 u = *reinterpret_cast<const uint2*>(w + i);
+  const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.x));
+  const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.y));
+  return make_float4(a.x, a.y, b.x, b.y);
+}
+
+// One dense layer on kRows rows: out[r][j] = b[j] + sum_k in[r][k] W[k][j]
+// (FP32 accumulation in k order), ReLU when `relu`. Thread j of the CTA
+// (kH threads) owns output column j; the inputs are read four columns at a
+// time (one 16-byte shared load feeds four FMAs).
+__device__ void dense(const float* in, int width, const __nv_bfloat16* W, const __nv_bfloat16* b, bool relu,
+                      float* out_s) {
+  const int j = threadIdx.x;
+  float acc[kRows];
+  const float bj = bf(b, j);
+#pragma unroll
+  for (int r = 0; r < kRows; ++r) acc[r] = bj;
+  for (int k = 0; k < width; k += 4) {
+    const float w0 = bf(W, k * kH + j), w1 = bf(W, (k + 1) * kH + j);
+    const float w2 = bf(W, (k + 2) * kH + j), w3 = bf(W, (k + 3) * kH + j);
+#pragma unroll
+    for (int r = 0; r < kRows; ++r) {
+      const float4 v = *reinterpret_cast<const float4*>(in + r * width + k);
+      acc[r] = fmaf(v.x, w0, acc[r]);
+      acc[r] = fmaf(v.y, w1, acc[r]);
+      acc[r] = fmaf(v.z, w2, acc[r]);
+      acc[r] = fmaf(v.w, w3, acc[r]);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < kRows; ++r) out_s[r * kH + j] = relu ? fmaxf(acc[r], 0.f) : acc[r];
+  __syncthreads();
+}
+
+// Forward pass on kRows rows per CTA. Writes the three hidden activations (for
+// the backward pass, optional) and the logits.
+__global__ void __launch_bounds__(kH) forward_kernel(const float* feat, int64_t n, const __nv_bfloat16* P,
+                                                     float* A1, float* A2, float* A3, float* logits) {
+  __shared__ __align__(16) float xin[kRows * kIn];
+  __shared__ __align__(16) float h0[kRows * kH];
+  __shared__ __align__(16) float h1[kRows * kH];
+  const int64_t r0 = (int64_t)blockIdx.x * kRows;
+  const int rows = (int)min((int64_t)kRows, n - r0);
+  for (int t = threadIdx.x; t < kRows * kIn; t += kH) {
+    const int r = t / kIn;
+    xin[t] = r < rows ? feat[(r0 + r) * kIn + (t % kIn)] : 0.f;
+  }
+  __syncthreads();
+  dense(xin, kIn, P + kOffW1, P + kOffB1, true, h0);
+  if (A1)
+    for (int t = threadIdx.x; t < rows * kH; t += kH) A1[r0 * kH + t] = h0[t];
+  dense(h0, kH, P + kOffW2, P + kOffB2, true, h1);
+  if (A2)
+    for (int t = threadIdx.x; t < rows * kH; t += kH) A2[r0 * kH + t] = h1[t];
+  dense(h1, kH, P + kOffW3, P + kOffB3, true, h0);
+  if (A3)
+    for (int t = threadIdx.x; t < rows * kH; t += kH) A3[r0 * kH + t] = h0[t];
+  // output logit: one warp per row, reduction over the 128 hidden units
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int r = warp; r < rows; r += kH / 32) {
+    float s = 0.f;
+    for (int k = lane; k < kH; k += 32) s = fmaf(h0[r * kH + k], bf(P, kOffW4 + k), s);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) logits[r0 + r] = s + bf(P, kOffB4);
+  }
+}
+
+// Backward pass of the weighted binary cross-entropy with logits,
+// loss = sum_i w_i [max(z,0) - z y + log(1 + exp(-|z|))] / sum_i w_i.
+// Persistent: each CTA walks chunks of kRows rows and accumulates the
+// parameter gradient in shared memory (thread j owns column j of every weight
+// matrix, so the accumulation needs no atomics); at the end each CTA adds its
+// partial gradient to G once.
+constexpr int kParamsPad = (kParams + 3) & ~3;
+constexpr size_t kBackwardSmem = sizeof(float) * (kParamsPad + 2 * kRows * kH + kRows);
+
+__global__ void __launch_bounds__(kH) backward_kernel(const float* feat, int64_t n, const __nv_bfloat16* P,
+                                                      const float* A1, const float* A2, const float* A3,
+                                                      const float* logits, const float* labels,
+                                                      const float* weights, float inv_wsum, float* G) {
+  extern __shared__ __align__(16) float smem[];
+  float* acc = smem;                // kParamsPad, parameter layout
+  float* dz = acc + kParamsPad;     // [kRows][kH] gradient w.r.t. the current pre-activation
+  float* act = dz + kRows * kH;     // [kRows][width] the current layer's input
+  float* g4 = act + kRows * kH;     // [kRows] gradient w.r.t. the logits
+  const int j = threadIdx.x;
+  for (int t = j; t < kParamsPad; t += kH) acc[t] = 0.f;
+  const int64_t chunks = (n + kRows - 1) / kRows;
+  const float* prevs[3] = {A2, A1, feat};
+  const int widths[3] = {kH, kH, kIn};
+  const int offW[3] = {kOffW3, kOffW2, kOffW1};
+  const int offB[3] = {kOffB3, kOffB2, kOffB1};
+  for (int64_t chunk = blockIdx.x; chunk < chunks; chunk += gridDim.x) {
+    const int64_t r0 = chunk * kRows;
+    const int rows = (int)min((int64_t)kRows, n - r0);
+    __syncthreads();
+    if (j < kRows) {
+      float g = 0.f;
+      if (j < rows) {
+        const float z = logits[r0 + j];
+        const float s = 1.f / (1.f + expf(-z));
+        g = (s - labels[r0 + j]) * weights[r0 + j] * inv_wsum;
+      }
+      g4[j] = g;
+    }
+    for (int t = j; t < kRows * kH; t += kH) act[t] = t / kH < rows ? A3[r0 * kH + t] : 0.f;
+    __syncthreads();
+    // layer 4: dW4[k] = sum_r A3[r][k] g4[r], db4 = sum_r g4[r], dz3 = g4 W4^T relu'(A3)
+    {
+      float s = 0.f;
+#pragma unroll
+      for (int r = 0; r < kRows; ++r) s = fmaf(act[r * kH + j], g4[r], s);
+      acc[kOffW4 + j] += s;
+      if (j == 0) {
+        float sb = 0.f;
+        for (int r = 0; r < kRows; ++r) sb += g4[r];
+        acc[kOffB4] += sb;
+      }
+      const float w4 = bf(P, kOffW4 + j);
+#pragma unroll
+      for (int r = 0; r < kRows; ++r) dz[r * kH + j] = act[r * kH + j] > 0.f ? g4[r] * w4 : 0.f;
+    }
+    // layers 3, 2, 1: dW[k][j] += sum_r in[r][k] dz[r][j], db[j] += sum_r dz[r][j],
+    // then dz_prev[r][k] = (sum_j dz[r][j] W[k][j]) relu'(in[r][k])
+#pragma unroll
+    for (int L = 0; L < 3; ++L) {
+      const int width = widths[L];
+      __syncthreads();
+      for (int t = j; t < kRows * width; t += kH) act[t] = t / width < rows ? prevs[L][r0 * width + t] : 0.f;
+      __syncthreads();
+      float dzr[kRows];
+      float sb = 0.f;
+#pragma unroll
+      for (int r = 0; r < kRows; ++r) {
+        dzr[r] = dz[r * kH + j];
+        sb += dzr[r];
+      }
+      acc[offB[L] + j] += sb;
+      float* aw = acc + offW[L];
+      for (int k = 0; k < width; k += 4) {
+        float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+#pragma unroll
+        for (int r = 0; r < kRows; ++r) {
+          const float4 a = *reinterpret_cast<const float4*>(act + r * width + k);
+          s0 = fmaf(a.x, dzr[r], s0);
+          s1 = fmaf(a.y, dzr[r], s1);
+          s2 = fmaf(a.z, dzr[r], s2);
+          s3 = fmaf(a.w, dzr[r], s3);
+        }
+        aw[k * kH + j] += s0;
+        aw[(k + 1) * kH + j] += s1;
+        aw[(k + 2) * kH + j] += s2;
+        aw[(k + 3) * kH + j] += s3;
+      }
+      if (L < 2) {
+        const __nv_bfloat16* W = P + offW[L];
+        float dp[kRows];
+#pragma unroll
+        for (int r = 0; r < kRows; ++r) dp[r] = 0.f;
+        for (int c = 0; c < kH; c += 4) {
+          const float4 w = bf4(W, j * kH + c);
+#pragma unroll
+          for (int r = 0; r < kRows; ++r) {
+            const float4 d = *reinterpret_cast<const float4*>(dz + r * kH + c);
+            dp[r] = fmaf(d.x, w.x, dp[r]);
+            dp[r] = fmaf(d.y, w.y, dp[r]);
+            dp[r] = fmaf(d.z, w.z, dp[r]);
+            dp[r] = fmaf(d.w, w.w, dp[r]);
+          }
+        }
+        __syncthreads();  // every thread has read dz
+#pragma unroll
+        for (int r = 0; r < kRows; ++r) dz[r * kH + j] = act[r * kH + j] > 0.f ? dp[r] : 0.f;
+      }
+    }
+  }
+  __syncthreads();
+  for (int t = j; t < kParams; t += kH)
+    if (acc[t] != 0.f) atomicAdd(G + t, acc[t]);
+}
+
+// Descending order of the logits within each pair (ties by index, NaN last):
+// grid (tile of kTile rows, pair). Row i's rank is the number of rows of its
+// pair that precede it; the row is copied to that position of the sorted
+// correspondences and its local index recorded in perm.
+__device__ __forceinline__ float order_key(float z) { return isnan(z) ? -INFINITY : z; }
+
+__global__ void __launch_bounds__(kTile) order_kernel(const double* corr, const int64_t* offsets, const float* logits,
+                                                      double* sorted, int* perm) {
+  __shared__ float cz[kCand];
+  const int pair = blockIdx.y;
+  const int64_t o0 = offsets[pair];
+  const int n = (int)(offsets[pair + 1] - o0);
+  if ((int)blockIdx.x * kTile >= n) return;  // uniform over the CTA
+  const int i = (int)blockIdx.x * kTile + threadIdx.x;
+  const bool active = i < n;
+  const float zi = active ? order_key(logits[o0 + i]) : 0.f;
+  int rank = 0;
+  for (int c0 = 0; c0 < n; c0 += kCand) {
+    const int m = min(kCand, n - c0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < m; t += kTile) cz[t] = order_key(logits[o0 + c0 + t]);
+    __syncthreads();
+    if (!active) continue;
+    for (int t = 0; t < m; ++t) {
+      const float zt = cz[t];
+      rank += (zt > zi) | ((zt == zi) & (c0 + t < i));
+    }
+  }
+  if (!active) return;
+  const int64_t dst = o0 + rank;
+  const double4 v = *reinterpret_cast<const double4*>(corr + 4 * (o0 + i));
+  *reinterpret_cast<double4*>(sorted + 4 * dst) = v;
+  perm[dst] = i;
+}
+
+// mask[offsets[pair] + perm[r]] = sorted_mask[r]
+__global__ void unpermute_kernel(const uint8_t* sorted_mask, const int* perm, const int64_t* offsets,
+                                 const int* pair_of_row, int64_t total, uint8_t* mask) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= total) return;
+  mask[offsets[pair_of_row[r]] + perm[r]] = sorted_mask[r];
+}
+
+// Adam step on the FP32 master parameters; refreshes the BF16 copies.
+__global__ void adam_kernel(float* M, float* V, float* Pm, __nv_bfloat16* P, const float* G, int count, float lr,
+                            float b1, float b2, float eps, float c1, float c2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const float g = G[i];
+  const float m = b1 * M[i] + (1.f - b1) * g;
+  const float v = b2 * V[i] + (1.f - b2) * g * g;
+  M[i] = m;
+  V[i] = v;
+  const float p = Pm[i] - lr * (m / c1) / (sqrtf(v / c2) + eps);
+  Pm[i] = p;
+  P[i] = __float2bfloat16(p);
+}
+
+__global__ void to_bf16_kernel(const float* Pm, __nv_bfloat16* P, int count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) P[i] = __float2bfloat16(Pm[i]);
+}
+
+}  // namespace
+
+extern "C" {
+
+int64_t gcr_learned_param_count(void) { return kParams; }
+int32_t gcr_learned_feature_width(void) { return kIn; }
+
+static gcr_status check_pairs(int64_t num_pairs, int64_t max_n) {
+  if (num_pairs < 0 || num_pairs > 65535) return fail(GCR_INVALID_ARG, "num_pairs %lld outside [0, 65535]", (long long)num_pairs);
+  if (max_n < 0 || max_n > (int64_t)1 << 30) return fail(GCR_INVALID_ARG, "max_n %lld outside [0, 2^30]", (long long)max_n);
+  return GCR_OK;
+}
+
+gcr_status gcr_learned_features(const double* d_corr, const int64_t* d_offsets, const gcr_image_size* d_sizes,
+                                int64_t num_pairs, int64_t max_n, float* d_feat, void* stream) {
+  if (!d_corr || !d_offsets || !d_sizes || !d_feat) return fail(GCR_INVALID_ARG, "NULL buffer");
+  const gcr_status st = check_pairs(num_pairs, max_n);
+  if (st != GCR_OK) return st;
+  if (num_pairs == 0 || max_n == 0) return GCR_OK;
+  const dim3 grid((unsigned)((max_n + kTile - 1) / kTile), (unsigned)num_pairs);
+  features_kernel<<<grid, kTile, 0, (cudaStream_t)stream>>>(d_corr, d_offsets, d_sizes, d_feat);
+  CUDA_TRY(cudaGetLastError());
+  return GCR_OK;
+}
+
+gcr_status gcr_learned_params_to_bf16(const float* d_master, void* d_bf16, void* stream) {
+  if (!d_master || !d_bf16) return fail(GCR_INVALID_ARG, "NULL buffer");
+  to_bf16_kernel<<<(kParams + 255) / 256, 256, 0, (cudaStream_t)stream>>>(d_master, (__nv_bfloat16*)d_bf16, kParams);
+  CUDA_TRY(cudaGetLastError());
+  return GCR_OK;
+}
+
+gcr_status gcr_learned_forward(const float* d_feat, int64_t n, const void* d_bf16, float* d_a1, float* d_a2,
+                               float* d_a3, float* d_logits, void* stream) {
+  if (!d_feat || !d_bf16 || !d_logits) return fail(GCR_INVALID_ARG, "NULL buffer");
+  if (n <= 0) return GCR_OK;
+  forward_kernel<<<(unsigned)((n + kRows - 1) / kRows), kH, 0, (cudaStream_t)stream>>>(
+      d_feat, n, (const __nv_bfloat16*)d_bf16, d_a1, d_a2, d_a3, d_logits);
+  CUDA_TRY(cudaGetLastError());
+  return GCR_OK;
+}
+
+gcr_status gcr_learned_backward(const float* d_feat, int64_t n, const void* d_bf16, const float* d_a1,
+                                const float* d_a2, const float* d_a3, const float* d_logits, const float* d_labels,
+                                const float* d_weights, float inv_weight_sum, float* d_grad, void* stream) {
+  if (!d_feat || !d_bf16 || !d_a1 || !d_a2 || !d_a3 || !d_logits || !d_labels || !d_weights || !d_grad)
+    return fail(GCR_INVALID_ARG, "NULL buffer");
+  if (n <= 0) return GCR_OK;
+  int dev = 0, sms = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  CUDA_TRY(cudaFuncSetAttribute(backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBackwardSmem));
+  const int64_t chunks = (n + kRows - 1) / kRows;
+  const unsigned grid = (unsigned)(chunks < sms ? chunks : sms);
+  backward_kernel<<<grid, kH, kBackwardSmem, (cudaStream_t)stream>>>(
+      d_feat, n, (const __nv_bfloat16*)d_bf16, d_a1, d_a2, d_a3, d_logits, d_labels, d_weights, inv_weight_sum,
+      d_grad);
+  CUDA_TRY(cudaGetLastError());
+  return GCR_OK;
+}
+
+gcr_status gcr_learned_adam(float* d_m, float* d_v, float* d_master, void* d_bf16, const float* d_grad, float lr,
+                            int64_t step, void* stream) {
+  if (!d_m || !d_v || !d_master || !d_bf16 || !d_grad) return fail(GCR_INVALID_ARG, "NULL buffer");
+  if (step < 1) return fail(GCR_INVALID_ARG, "Adam step counts from 1");
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+  adam_kernel<<<(kParams + 255) / 256, 256, 0, (cudaStream_t)stream>>>(d_m, d_v, d_master, (__nv_bfloat16*)d_bf16,
+                                                                      d_grad, kParams, lr, b1, b2, eps, c1, c2);
+  CUDA_TRY(cudaGetLastError());
+  return GCR_OK;
+}
+
+gcr_status gcr_learned_order(const double* d_corr, const int64_t* d_offsets, int64_t num_pairs, int64_t max_n,
+                             const float* d_logits, double* d_sorted_corr, int32_t* d_perm, void* stream) {
+  if (!d_corr || !d_offsets || !d_logits || !d_sorted_corr || !d_perm) return fail(GCR_INVALID_ARG, "NULL buffer");
+  if (((uintptr_t)d_corr | (uintptr_t)d_sorted_corr) & 31)
+    return fail(GCR_INVALID_ARG, "correspondence buffers must be 32-byte aligned");
+  const gcr_status st = check_pairs(num_pairs, max_n);
+  if (st != GCR_OK) return st;
+  if (num_pairs == 0 || max_n == 0) return GCR_OK;
+  const dim3 grid((unsigned)((max_n + kTile - 1) / kTile), (unsigned)num_pairs);
+  order_kernel<<<grid, kTile, 0, (cudaStream_t)stream>>>(d_corr, d_offsets, d_logits, d_sorted_corr, d_perm);
+  CUDA_TRY(cudaGetLastError());
+  return GCR_OK;
+}
+
+gcr_status gcr_learned_propose(const double* d_corr, const int64_t* d_offsets, const gcr_image_size* d_sizes,
+                               int64_t num_pairs, int64_t max_n, int64_t total, const void* d_bf16, float* d_feat,
+                               float* d_logits, double* d_sorted_corr, int32_t* d_perm, void* stream) {
+  gcr_status st = gcr_learned_features(d_corr, d_offsets, d_sizes, num_pairs, max_n, d_feat, stream);
+  if (st == GCR_OK) st = gcr_learned_forward(d_feat, total, d_bf16, nullptr, nullptr, nullptr, d_logits, stream);
+  if (st == GCR_OK) st = gcr_learned_order(d_corr, d_offsets, num_pairs, max_n, d_logits, d_sorted_corr, d_perm, stream);
+  return st;
+}
+
+gcr_status gcr_learned_unpermute_mask(const uint8_t* d_sorted_mask, const int32_t* d_perm, const int64_t* d_offsets,
+                                      const int32_t* d_pair_of_row, int64_t total, uint8_t* d_mask, void* stream) {
+  if (!d_sorted_mask || !d_perm || !d_offsets || !d_pair_of_row || !d_mask) return fail(GCR_INVALID_ARG, "NULL buffer");
+  if (total <= 0) return GCR_OK;
+  unpermute_kernel<<<(unsigned)((total + 255) / 256), 256, 0, (cudaStream_t)stream>>>(d_sorted_mask, d_perm, d_offsets,
+                                                                                    d_pair_of_row, total, d_mask);
+  CUDA_TRY(cudaGetLastError());
+  return GCR_OK;
+}
+
+}  // extern "C"

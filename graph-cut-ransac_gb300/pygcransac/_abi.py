@@ -101,6 +101,18 @@ _EXPORTS = {
                                                           _P]),
     "gcr_batch_prepare": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int64, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "gcr_batch_launch": (ctypes.c_int, [_P, _P]),
+    "gcr_learned_param_count": (ctypes.c_int64, []),
+    "gcr_learned_feature_width": (ctypes.c_int32, []),
+    "gcr_learned_features": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_int64, _P, _P]),
+    "gcr_learned_params_to_bf16": (ctypes.c_int, [_P, _P, _P]),
+    "gcr_learned_forward": (ctypes.c_int, [_P, ctypes.c_int64, _P, _P, _P, _P, _P, _P]),
+    "gcr_learned_backward": (ctypes.c_int, [_P, ctypes.c_int64, _P, _P, _P, _P, _P, _P, _P, ctypes.c_float, _P,
+                                            _P]),
+    "gcr_learned_adam": (ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.c_float, ctypes.c_int64, _P]),
+    "gcr_learned_order": (ctypes.c_int, [_P, _P, ctypes.c_int64, ctypes.c_int64, _P, _P, _P, _P]),
+    "gcr_learned_propose": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, _P, _P, _P,
+                                           _P, _P, _P]),
+    "gcr_learned_unpermute_mask": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int64, _P, _P]),
     "gcr_last_launch_count": (ctypes.c_int64, []),
     "gcr_last_error_string": (ctypes.c_char_p, []),
 }

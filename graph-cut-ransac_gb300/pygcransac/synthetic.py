@@ -11,7 +11,11 @@ workloads of this engine:
   focal 800 px, 640x480, camera 2 rotated by U(+-30 deg) about a random axis
   and translated by a unit vector; inliers with sigma = 0.5 px, uniform
   outliers. Used for both the fundamental (pixels) and essential (K known)
-  workloads.
+  workloads. With ``smooth_depth=True`` the inliers' depth is a smooth field
+  over the first image (three random plane waves, 0.5-2 cycles per image,
+  2-10 m) instead of independent per point: the piecewise-smooth scenes real
+  image pairs show, in which neighbouring inliers move alike (the hard
+  fundamental-matrix workload of the learned proposal, 5-10 % inliers).
 
 All generators use numpy ``Generator(PCG64(seed))``.
 """
@@ -81,9 +85,28 @@ def skew(t):
     return np.array([[0, -t[2], t[1]], [t[2], 0, -t[0]], [-t[1], t[0], 0]])
 
 
-def two_view_pair(seed, n=5000, inlier_ratio=0.25, sigma=0.5, f=800.0, w=W, h=H, max_angle_deg=30.0):
+def depth_field(rng, w=W, h=H):
+    """Smooth depth (2-10 m) over the first image: 6 + 4 * (0.5 s1 + 0.3 s2 +
+    0.2 s3) with s_i = sin(2 pi f_i (cos a_i u/w + sin a_i v/h) + phi_i),
+    f_i ~ U(0.5, 2) cycles per image, a_i, phi_i ~ U(0, 2 pi)."""
+    fr = rng.uniform(0.5, 2.0, 3)
+    ang = rng.uniform(0, 2 * np.pi, 3)
+    ph = rng.uniform(0, 2 * np.pi, 3)
+    amp = np.array([0.5, 0.3, 0.2])
+
+    def Z(uv):
+        u, v = uv[:, 0] / w, uv[:, 1] / h
+        s = sum(amp[i] * np.sin(2 * np.pi * fr[i] * (np.cos(ang[i]) * u + np.sin(ang[i]) * v) + ph[i])
+                for i in range(3))
+        return 6.0 + 4.0 * s
+    return Z
+
+
+def two_view_pair(seed, n=5000, inlier_ratio=0.25, sigma=0.5, f=800.0, w=W, h=H, max_angle_deg=30.0,
+                  smooth_depth=False):
     """Returns dict(corr [n,4] pixels, K, R, t, F_gt, E_gt, inlier_gt, size)."""
     rng = _rng(seed)
+    Zf = depth_field(rng, w, h) if smooth_depth else None
     K = intrinsics(f, w, h)
     Ki = np.linalg.inv(K)
     ni = int(round(n * inlier_ratio))
@@ -98,7 +121,7 @@ def two_view_pair(seed, n=5000, inlier_ratio=0.25, sigma=0.5, f=800.0, w=W, h=H,
             tries += 1
             m = 4 * ni
             uv = rng.uniform([0, 0], [w, h], size=(m, 2))
-            depth = rng.uniform(2, 10, size=m)
+            depth = rng.uniform(2, 10, size=m) if Zf is None else Zf(uv)
             X = (np.c_[uv, np.ones(m)] @ Ki.T) * depth[:, None]
             X2 = X @ R.T + t
             front = X2[:, 2] > 0.1

@@ -198,6 +198,56 @@ gcr_status gcr_batch_prepare(gcr_context* ctx, gcr_model_kind kind, int64_t num_
                              gcr_stats* d_stats_out);
 gcr_status gcr_batch_launch(gcr_context* ctx, void* stream);
 
+/* Learned inlier-probability proposal (no counterpart in the reference, which
+ * takes externally computed probabilities for its samplers 3 and 4): a
+ * per-correspondence MLP whose scores order the correspondences for PROSAC
+ * (sampler 1). All buffers are device pointers; work is queued on `stream`.
+ * Pairs are laid out as in gcr_batch_run_device (d_offsets [num_pairs + 1],
+ * max_n = the largest pair size, num_pairs <= 65535).
+ *   gcr_learned_features    k = 8 nearest-neighbour displacement features,
+ *                           d_feat [total][gcr_learned_feature_width()] floats
+ *   gcr_learned_forward     logits [n]; the hidden activations d_a1..d_a3
+ *                           ([n][128] floats) are written when not NULL
+ *   gcr_learned_backward    adds the gradient of the weighted binary
+ *                           cross-entropy (labels, weights [n]; the loss is
+ *                           divided by the weight sum) to d_grad
+ *   gcr_learned_adam        one Adam step (step counts from 1) on the FP32
+ *                           master parameters, refreshing the BF16 copies
+ *   gcr_learned_order       per pair, copies the correspondences in
+ *                           descending logit order (ties by index) to
+ *                           d_sorted_corr and records each sorted row's
+ *                           original in-pair index in d_perm [total];
+ *                           correspondence buffers 32-byte aligned
+ *   gcr_learned_propose     features + forward + order in one call (d_feat,
+ *                           d_logits: workspaces of total rows)
+ *   gcr_learned_unpermute_mask
+ *                           maps an inlier mask of the sorted order back to
+ *                           the caller's order (d_pair_of_row [total])
+ * Parameters: gcr_learned_param_count() floats (master, Adam moments,
+ * gradient) or BF16 values (the copy the passes read). */
+int64_t gcr_learned_param_count(void);
+int32_t gcr_learned_feature_width(void);
+gcr_status gcr_learned_features(const double* d_corr, const int64_t* d_offsets, const gcr_image_size* d_sizes,
+                                int64_t num_pairs, int64_t max_n, float* d_feat, void* stream);
+gcr_status gcr_learned_params_to_bf16(const float* d_master, void* d_bf16, void* stream);
+gcr_status gcr_learned_forward(const float* d_feat, int64_t n, const void* d_bf16, float* d_a1, float* d_a2,
+                               float* d_a3, float* d_logits, void* stream);
+gcr_status gcr_learned_backward(const float* d_feat, int64_t n, const void* d_bf16, const float* d_a1,
+                                const float* d_a2, const float* d_a3, const float* d_logits,
+                                const float* d_labels, const float* d_weights, float inv_weight_sum,
+                                float* d_grad, void* stream);
+gcr_status gcr_learned_adam(float* d_m, float* d_v, float* d_master, void* d_bf16, const float* d_grad,
+                            float lr, int64_t step, void* stream);
+gcr_status gcr_learned_order(const double* d_corr, const int64_t* d_offsets, int64_t num_pairs, int64_t max_n,
+                             const float* d_logits, double* d_sorted_corr, int32_t* d_perm, void* stream);
+gcr_status gcr_learned_propose(const double* d_corr, const int64_t* d_offsets, const gcr_image_size* d_sizes,
+                               int64_t num_pairs, int64_t max_n, int64_t total, const void* d_bf16,
+                               float* d_feat, float* d_logits, double* d_sorted_corr, int32_t* d_perm,
+                               void* stream);
+gcr_status gcr_learned_unpermute_mask(const uint8_t* d_sorted_mask, const int32_t* d_perm,
+                                      const int64_t* d_offsets, const int32_t* d_pair_of_row, int64_t total,
+                                      uint8_t* d_mask, void* stream);
+
 /* Number of kernels the last gcr_batch_run_device / gcr_batch_launch / gcr_find_* call launched. */
 int64_t gcr_last_launch_count(void);
 
