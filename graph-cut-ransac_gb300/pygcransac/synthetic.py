@@ -171,10 +171,12 @@ def sampson_sq(F, corr):
 
 def fundamental_error(F_est, pair, n=1000, seed=12345):
     """Mean Sampson distance (px) of noise-free ground-truth correspondences."""
-    if F_est is None:
+    if F_est is None or not np.any(F_est):
         return np.inf
     clean = two_view_pair_clean(pair, n, seed)
-    return float(np.mean(np.sqrt(sampson_sq(F_est, clean))))
+    with np.errstate(invalid="ignore", divide="ignore"):
+        e = float(np.mean(np.sqrt(sampson_sq(F_est, clean))))
+    return e if np.isfinite(e) else np.inf
 
 
 def two_view_pair_clean(pair, n, seed):
