@@ -219,11 +219,20 @@ gcr_status gcr_context_destroy(gcr_context* c) {
 // intrinsics uploads (queued on s). The device work it describes (ticket
 // reset, K^-1 normalisation, engine launch) is recorded in *L and queued by
 // launch_batch.
+// GCRANSAC::run without the drivers (gcr_run): the caller's grid, the
+// neighbourhood coordinates apart from the fitting ones, the threshold in the
+// fitting coordinates' units, no epilogue.
+struct RunOnly {
+  const double* d_pixels;
+  double cell[4];
+  int divisions;
+};
+
 static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num_pairs, const double* d_corr,
                                 const int64_t* h_offsets, const double* h_K, const gcr_image_size* h_sizes,
                                 const gcr_params* params, const uint64_t* h_seeds, double* d_models_out,
                                 uint8_t* d_masks_out, gcr_stats* d_stats_out, cudaStream_t s,
-                                gcr_context::Pending* L) {
+                                gcr_context::Pending* L, const RunOnly* run_only = nullptr) {
   L->valid = false;
   if (!c) return fail(GCR_INVALID_ARG, "context is NULL");
   const gcr::KindOps* ops = ops_for(kind);
@@ -234,7 +243,7 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
   if (num_pairs > (1 << 30)) return fail(GCR_CAPACITY, "too many pairs");
   if (!d_corr || !h_offsets || !h_sizes || !d_models_out || !d_masks_out || !d_stats_out)
     return fail(GCR_INVALID_ARG, "NULL buffer");
-  if (kind == GCR_ESSENTIAL && !h_K) return fail(GCR_INVALID_ARG, "essential matrices need intrinsics");
+  if (kind == GCR_ESSENTIAL && !h_K && !run_only) return fail(GCR_INVALID_ARG, "essential matrices need intrinsics");
   const int m = ops->sample_size;
   int max_n = 0;
   for (int64_t i = 0; i < num_pairs; ++i) {
@@ -307,7 +316,7 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
     d.centre[1] = 0.5 * z.h1;
     d.centre[2] = 0.5 * z.w2;
     d.centre[3] = 0.5 * z.h2;
-    if (essential) {
+    if (essential && !run_only) {
       // findEssentialMatrix_ (gcransac_python.cpp:2598-2603, 2655): the run
       // works on K^-1-normalised coordinates with the threshold divided by
       // the mean focal length; those coordinates need no centring
@@ -316,6 +325,13 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
       const double normalizer = 0.25 * (K1[0] + K1[4] + K2[0] + K2[4]);
       d.threshold = params->threshold / normalizer;
       for (int q = 0; q < 4; ++q) d.centre[q] = 0.0;
+    }
+    if (run_only) {
+      d.n_div = run_only->divisions;
+      for (int q = 0; q < 4; ++q) d.cell[q] = run_only->cell[q];
+      d.threshold = params->threshold;
+      if (essential)
+        for (int q = 0; q < 4; ++q) d.centre[q] = 0.0;
     }
     d.img[0] = z.w1;
     d.img[1] = z.h1;
@@ -326,7 +342,7 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
   CUDA_TRY(c->pairs.ensure(sizeof(gcr::PairDesc) * num_pairs));
   CUDA_TRY(cudaMemcpyAsync(c->pairs.p, pd.data(), sizeof(gcr::PairDesc) * num_pairs, cudaMemcpyHostToDevice, s));
   const double* run_pts = d_corr;
-  if (kind == GCR_ESSENTIAL) {
+  if (kind == GCR_ESSENTIAL && !run_only) {
     // K^-1 of both cameras per pair (a singular K is rejected)
     std::vector<double> kinv(18 * (size_t)num_pairs);
     for (int64_t i = 0; i < num_pairs; ++i)
@@ -344,7 +360,7 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
 
   gcr::Workspace ws;
   ws.pts64 = run_pts;
-  ws.pix64 = d_corr;
+  ws.pix64 = run_only ? run_only->d_pixels : d_corr;
   ws.pts32 = (float4*)c->pts32.p;
   ws.pairs = (const gcr::PairDesc*)c->pairs.p;
   ws.slots = (gcr::Slot*)c->slots_meta.p;
@@ -366,7 +382,7 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
   prm.lambda = params->spatial_coherence_weight;
   // the fundamental/essential drivers build no neighbourhood for a weight at
   // or below machine epsilon (gcransac_python.cpp:1658-1667)
-  if (kind != GCR_HOMOGRAPHY && prm.lambda <= eps) prm.lambda = 0.0;
+  if (kind != GCR_HOMOGRAPHY && prm.lambda <= eps && !run_only) prm.lambda = 0.0;
   prm.max_iters = params->max_iterations;
   prm.min_iters = params->min_iterations;
   prm.lo_number = params->lo_number;
@@ -381,6 +397,7 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
   prm.use_sprt = params->use_sprt ? 1 : 0;
   prm.use_sp = (kind == GCR_HOMOGRAPHY && params->use_space_partitioning) ? 1 : 0;
   prm.sprt_min_ratio = params->min_inlier_ratio_for_sprt;
+  prm.epilogue = run_only ? 0 : 1;
   prm.mag_table = nullptr;
   prm.mag_c2dof = 0.25 * std::pow(2.0, 1.5);
   prm.mag_gamma_k = 0.0036572608340910764;
@@ -397,7 +414,7 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
   L->grid = grid;
   L->ws = ws;
   L->prm = prm;
-  L->normalise = kind == GCR_ESSENTIAL;
+  L->normalise = kind == GCR_ESSENTIAL && !run_only;
   L->d_corr = d_corr;
   L->num_pairs = (int)num_pairs;
   L->valid = true;
@@ -533,6 +550,59 @@ gcr_status gcr_find_essential(const double* corr, int64_t n, const double* K1, c
                               double* model_out9, uint8_t* mask_out, gcr_stats* stats_out) {
   (void)probabilities;
   return find_one(GCR_ESSENTIAL, corr, n, K1, K2, size, params, model_out9, mask_out, stats_out);
+}
+
+gcr_status gcr_run(gcr_model_kind kind, const double* points, const double* pixels, int64_t n,
+                   const double* cell_sizes, int32_t divisions, const gcr_image_size* size,
+                   const gcr_params* params, double* model_out9, uint8_t* mask_out, gcr_stats* stats_out) {
+  static thread_local gcr_context* ctx = nullptr;
+  g_last_launches = 0;
+  if (!points || !cell_sizes || !size || !params || !model_out9 || !mask_out)
+    return fail(GCR_INVALID_ARG, "NULL argument");
+  const int m = kind == GCR_HOMOGRAPHY ? 4 : (kind == GCR_FUNDAMENTAL ? 7 : 5);
+  if (n < m) return fail(GCR_TOO_FEW_POINTS, "%lld points, needs >= %d", (long long)n, m);
+  if (divisions < 1) return fail(GCR_INVALID_ARG, "the grid needs at least one division per axis");
+  for (int q = 0; q < 4; ++q)
+    if (!(cell_sizes[q] > 0)) return fail(GCR_INVALID_ARG, "grid cell sizes must be positive");
+  if (!ctx) {
+    gcr_status s0 = gcr_context_create(&ctx);
+    if (s0 != GCR_OK) return s0;
+  }
+  cudaStream_t s = 0;
+  const size_t bytes = sizeof(double) * 4 * (size_t)n;
+  // points and pixels share one staging buffer: [points | pixels]
+  CUDA_TRY(ctx->corr.ensure(2 * bytes));
+  CUDA_TRY(ctx->models.ensure(sizeof(double) * 9));
+  CUDA_TRY(ctx->masks.ensure((size_t)n));
+  CUDA_TRY(ctx->stats.ensure(sizeof(gcr_stats)));
+  double* d_pts = (double*)ctx->corr.p;
+  double* d_pix = d_pts + 4 * n;
+  CUDA_TRY(cudaMemcpyAsync(d_pts, points, bytes, cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(d_pix, pixels ? pixels : points, bytes, cudaMemcpyHostToDevice, s));
+  RunOnly ro;
+  ro.d_pixels = d_pix;
+  for (int q = 0; q < 4; ++q) ro.cell[q] = cell_sizes[q];
+  ro.divisions = divisions;
+  const int64_t offsets[2] = {0, n};
+  const uint64_t seed = params->seed;
+  ctx->pending.valid = false;
+  gcr_context::Pending L;
+  gcr_status st = prepare_batch(ctx, kind, 1, d_pts, offsets, nullptr, size, params, &seed, (double*)ctx->models.p,
+                                (uint8_t*)ctx->masks.p, (gcr_stats*)ctx->stats.p, s, &L, &ro);
+  if (st != GCR_OK) return st;
+  st = launch_batch(ctx, L, s);
+  if (st != GCR_OK) return st;
+  gcr_stats so{};
+  CUDA_TRY(cudaMemcpyAsync(model_out9, ctx->models.p, sizeof(double) * 9, cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaMemcpyAsync(mask_out, ctx->masks.p, (size_t)n, cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaMemcpyAsync(&so, ctx->stats.p, sizeof(gcr_stats), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  if (stats_out) *stats_out = so;
+  if (so.status != GCR_OK) {
+    if (so.status == GCR_NO_MODEL) return fail(GCR_NO_MODEL, "no model with more than %d inliers", m);
+    return fail((gcr_status)so.status, "device engine reported status %d", so.status);
+  }
+  return GCR_OK;
 }
 
 }  // extern "C"

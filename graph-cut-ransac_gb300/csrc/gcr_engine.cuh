@@ -73,6 +73,9 @@ struct EngineParams {
   double sprt_min_ratio;
   // space-partitioning pre-selection of homography models
   int32_t use_sp;
+  // 1: the Python drivers' epilogue after the run (bundle adjustment of the
+  // final inliers for F and E); 0: GCRANSAC::run alone
+  int32_t epilogue;
 };
 
 // Per-pair inputs prepared on the device.
@@ -2480,7 +2483,7 @@ struct Engine {
     // output: model and the inliers of the final container
     int cnt = materialise(cont[off], list);
     double final_score = best.value;
-    if constexpr (Est::KIND == 1) {
+    if constexpr (Est::KIND == 1) if (prm.epilogue) {
       // findFundamentalMatrix_ epilogue (gcransac_python.cpp:1833-1889):
       // weighted bundle adjustment of the final inliers on the raw
       // coordinates, kept when its MSAC score beats the run's score; at most 7
@@ -2509,7 +2512,7 @@ struct Engine {
         sync();
       }
     }
-    if constexpr (Est::KIND == 3) {
+    if constexpr (Est::KIND == 3) if (prm.epilogue) {
       // findEssentialMatrix_ epilogue (gcransac_python.cpp:2770-2828): the
       // essential-matrix bundle adjustment of the final inliers (Stewenius
       // start, every cheirality-consistent pose refined), each result kept

@@ -198,6 +198,21 @@ gcr_status gcr_batch_prepare(gcr_context* ctx, gcr_model_kind kind, int64_t num_
                              gcr_stats* d_stats_out);
 gcr_status gcr_batch_launch(gcr_context* ctx, void* stream);
 
+/* GCRANSAC::run on one pair (GCRANSAC.h:200-627) without the Python drivers'
+ * pre- and post-processing; the entry behind the C++ plugin surface
+ * include/gcransac/GCRANSAC.h. `points` [n][4] are the coordinates the model
+ * is fitted in (K^-1-normalised for essential matrices, as the reference's
+ * essential driver passes them to run), `pixels` [n][4] (NULL = points) the
+ * coordinates of the grid neighbourhood and of the P-NAPSAC sampler;
+ * `cell_sizes` [4] and `divisions` describe the grid (GridNeighborhoodGraph<4>,
+ * neighborhood/grid_neighborhood_graph.h:163); `size` gives the image extents
+ * P-NAPSAC uses; params->threshold is in the units of `points`. Host buffers;
+ * the inlier mask and statistics are those of the run, with no bundle
+ * adjustment epilogue (gcransac_python.cpp:1833-1889, 2770-2828). */
+gcr_status gcr_run(gcr_model_kind kind, const double* points, const double* pixels, int64_t n,
+                   const double* cell_sizes, int32_t divisions, const gcr_image_size* size,
+                   const gcr_params* params, double* model_out9, uint8_t* mask_out, gcr_stats* stats_out);
+
 /* Learned inlier-probability proposal (no counterpart in the reference, which
  * takes externally computed probabilities for its samplers 3 and 4): a
  * per-correspondence MLP whose scores order the correspondences for PROSAC

@@ -289,6 +289,57 @@ int oracle_find(int kind, const double* corr, int64_t n, const double* K1, const
   return rc;
 }
 
+// GCRANSAC::run alone (GCRANSAC.h:200-627) on caller-given fitting
+// coordinates `points`, neighbourhood coordinates `pixels` and grid cells:
+// the counterpart of gcr_run; no driver epilogue, threshold in the units of
+// `points`.
+int oracle_run(int kind, const double* points, const double* pixels, int64_t n, const double* cell_sizes,
+               int32_t divisions, const gcr_image_size* sz, const gcr_params* p, uint64_t seed, double* model_out,
+               uint8_t* mask, gcr_stats* st) {
+  gcr_stats local{};
+  gcr_stats* s = st ? st : &local;
+  std::memset(s, 0, sizeof(*s));
+  const Mat pts{points, n, 4};
+  const Mat pix{pixels ? pixels : points, n, 4};
+  const Grid grid(pix, cell_sizes, (size_t)divisions);
+  Model model{};
+  std::vector<size_t> inl;
+  int rc = GCR_INVALID_ARG;
+  const bool mag = p->scoring == GCR_SCORING_MAGSAC;
+  const double t = p->threshold;
+  if (kind == GCR_HOMOGRAPHY) {
+    if (n < 4) rc = GCR_TOO_FEW_POINTS;
+    else {
+      HomographyEstimator est;
+      rc = mag ? run_generic<HomographyEstimator, MAGSACScoring>(pts, pix, est, *p, *sz, seed, &grid, t, model, inl, s, t)
+               : run_generic<HomographyEstimator, MSACScoring>(pts, pix, est, *p, *sz, seed, &grid, t, model, inl, s, t);
+    }
+  } else if (kind == GCR_FUNDAMENTAL) {
+    if (n < 7) rc = GCR_TOO_FEW_POINTS;
+    else {
+      FundamentalEstimator est;
+      est.seed = seed;
+      rc = mag ? run_generic<FundamentalEstimator, MAGSACScoring>(pts, pix, est, *p, *sz, seed, &grid, t, model, inl, s, t)
+               : run_generic<FundamentalEstimator, MSACScoring>(pts, pix, est, *p, *sz, seed, &grid, t, model, inl, s, t);
+      if (est.degensac_ran) s->flags |= 8;
+    }
+  } else if (kind == GCR_ESSENTIAL) {
+    if (n < 5) rc = GCR_TOO_FEW_POINTS;
+    else {
+      EssentialEstimator est;
+      rc = mag ? run_generic<EssentialEstimator, MAGSACScoring>(pts, pix, est, *p, *sz, seed, &grid, t, model, inl, s, t)
+               : run_generic<EssentialEstimator, MSACScoring>(pts, pix, est, *p, *sz, seed, &grid, t, model, inl, s, t);
+    }
+  }
+  std::memset(mask, 0, (size_t)n);
+  for (size_t i : inl) mask[i] = 1;
+  s->inlier_number = (int64_t)inl.size();
+  if (rc == GCR_OK) std::memcpy(model_out, model.data(), 9 * sizeof(double));
+  else std::memset(model_out, 0, 9 * sizeof(double));
+  s->status = rc;
+  return rc;
+}
+
 // Pair-parallel batch over `threads` host threads (one pair per thread at a
 // time, each pair single-threaded like the reference). Returns wall seconds.
 double oracle_find_batch(int kind, int64_t num_pairs, const double* corr, const int64_t* offsets, const double* K,

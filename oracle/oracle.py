@@ -37,6 +37,9 @@ def load():
         lib.oracle_find.argtypes = [ctypes.c_int, P, ctypes.c_int64, P, P, P, P, ctypes.c_uint64, P, P, P]
         lib.oracle_find_batch.restype = ctypes.c_double
         lib.oracle_find_batch.argtypes = [ctypes.c_int, ctypes.c_int64, P, P, P, P, P, P, P, P, P, ctypes.c_int]
+        lib.oracle_run.restype = ctypes.c_int
+        lib.oracle_run.argtypes = [ctypes.c_int, P, P, ctypes.c_int64, P, ctypes.c_int32, P, P, ctypes.c_uint64, P,
+                                   P, P]
         lib.oracle_magsac_gamma.restype = ctypes.c_double
         lib.oracle_magsac_gamma.argtypes = [ctypes.c_int]
         lib.oracle_labeling.restype = ctypes.c_int
@@ -81,6 +84,21 @@ def find(kind, corr, size, params, seed=None, K1=None, K2=None):
     seed = params.seed if seed is None else seed
     rc = lib.oracle_find(kind, _p(corr), n, _p(K1), _p(K2), ctypes.byref(size), ctypes.byref(params),
                          seed, _p(model), _p(mask), ctypes.byref(st))
+    return rc, model.reshape(3, 3), mask.astype(bool), st
+
+
+def run(kind, points, pixels, cell_sizes, divisions, size, params, seed=0):
+    """GCRANSAC::run alone (oracle_run): (status, model [3, 3], mask, stats)."""
+    lib = load()
+    points = np.ascontiguousarray(points, np.float64)
+    pixels = None if pixels is None else np.ascontiguousarray(pixels, np.float64)
+    cs = np.ascontiguousarray(cell_sizes, np.float64)
+    n = len(points)
+    model = np.zeros(9)
+    mask = np.zeros(n, np.uint8)
+    st = _abi.Stats()
+    rc = lib.oracle_run(kind, _p(points), _p(pixels), n, _p(cs), int(divisions), ctypes.byref(size),
+                        ctypes.byref(params), int(seed), _p(model), _p(mask), ctypes.byref(st))
     return rc, model.reshape(3, 3), mask.astype(bool), st
 
 
