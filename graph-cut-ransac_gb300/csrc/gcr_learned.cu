@@ -12,8 +12,10 @@
 //   a coherent motion have near neighbours that move alike; a random match
 //   does not.
 // Network: 32 -> 128 -> 128 -> 128 -> 1, ReLU between layers, the last output
-// is a logit. Parameters are kept as FP32 master copies (Adam) and BF16 copies
-// used by the forward and backward passes.
+// is a logit; the inputs of the first three layers are rounded to BF16 and
+// multiplied on the tensor cores with FP32 accumulation. Parameters are kept
+// as FP32 master copies (Adam) and BF16 copies used by the forward and
+// backward passes.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -176,66 +178,155 @@ __device__ __forceinline__ float4 bf4(const __nv_bfloat16* w, int i) {
   return make_float4(a.x, a.y, b.x, b.y);
 }
 
-// One dense layer on kRows rows: out[r][j] = b[j] + sum_k in[r][k] W[k][j]
-// (FP32 accumulation in k order), ReLU when `relu`. Thread j of the CTA
-// (kH threads) owns output column j; the inputs are read four columns at a
-// time (one 16-byte shared load feeds four FMAs).
-__device__ void dense(const float* in, int width, const __nv_bfloat16* W, const __nv_bfloat16* b, bool relu,
-                      float* out_s) {
-  const int j = threadIdx.x;
-  float acc[kRows];
-  const float bj = bf(b, j);
-#pragma unroll
-  for (int r = 0; r < kRows; ++r) acc[r] = bj;
-  for (int k = 0; k < width; k += 4) {
-    const float w0 = bf(W, k * kH + j), w1 = bf(W, (k + 1) * kH + j);
-    const float w2 = bf(W, (k + 2) * kH + j), w3 = bf(W, (k + 3) * kH + j);
-#pragma unroll
-    for (int r = 0; r < kRows; ++r) {
-      const float4 v = *reinterpret_cast<const float4*>(in + r * width + k);
-      acc[r] = fmaf(v.x, w0, acc[r]);
-      acc[r] = fmaf(v.y, w1, acc[r]);
-      acc[r] = fmaf(v.z, w2, acc[r]);
-      acc[r] = fmaf(v.w, w3, acc[r]);
-    }
-  }
-  __syncthreads();
-#pragma unroll
-  for (int r = 0; r < kRows; ++r) out_s[r * kH + j] = relu ? fmaxf(acc[r], 0.f) : acc[r];
-  __syncthreads();
+// ---- Forward pass on the tensor cores: mma.sync m16n8k16, BF16 x BF16 ->
+// FP32. Each warp owns 16 rows; a layer is 16 n-tiles of 8 columns x K/16
+// k-steps. The FP32 accumulator fragment of n-tiles (2j, 2j+1) has exactly
+// the layout of the next layer's A fragment for k-step j (rows g and g + 8,
+// columns 2t, 2t + 1 and 8 + 2t, 9 + 2t of the 16), so activations stay in
+// registers between layers: bias, ReLU, rounding to BF16, next layer. The
+// weights sit in shared memory transposed ([n][k], rows padded by 8 so the
+// warp's B-fragment loads hit 32 distinct banks) and are loaded once per
+// persistent CTA. The output layer (128 -> 1) is an FP32 dot product of the
+// third layer's FP32 activations, reduced over the four lanes of each row.
+// Activations: layer inputs are rounded to BF16 (the features included); A1
+// and A2 are stored rounded (what the next layer read), A3 in FP32.
+constexpr int kMmaWarps = 4;
+constexpr int kTileRows = 16 * kMmaWarps;
+constexpr int kLd1 = kIn + 8;
+constexpr int kLdH = kH + 8;
+constexpr size_t kForwardSmem =
+    sizeof(__nv_bfloat16) * (size_t)(kH * kLd1 + 2 * kH * kLdH) + sizeof(float) * (size_t)(4 * kH + 4);
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+__device__ __forceinline__ float round_bf16(float v) { return __bfloat162float(__float2bfloat16_rn(v)); }
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-// Forward pass on kRows rows per CTA. Writes the three hidden activations (for
-// the backward pass, optional) and the logits.
-__global__ void __launch_bounds__(kH) forward_kernel(const float* feat, int64_t n, const __nv_bfloat16* P,
-                                                     float* A1, float* A2, float* A3, float* logits) {
-  __shared__ __align__(16) float xin[kRows * kIn];
-  __shared__ __align__(16) float h0[kRows * kH];
-  __shared__ __align__(16) float h1[kRows * kH];
-  const int64_t r0 = (int64_t)blockIdx.x * kRows;
-  const int rows = (int)min((int64_t)kRows, n - r0);
-  for (int t = threadIdx.x; t < kRows * kIn; t += kH) {
-    const int r = t / kIn;
-    xin[t] = r < rows ? feat[(r0 + r) * kIn + (t % kIn)] : 0.f;
-  }
-  __syncthreads();
-  dense(xin, kIn, P + kOffW1, P + kOffB1, true, h0);
-  if (A1)
-    for (int t = threadIdx.x; t < rows * kH; t += kH) A1[r0 * kH + t] = h0[t];
-  dense(h0, kH, P + kOffW2, P + kOffB2, true, h1);
-  if (A2)
-    for (int t = threadIdx.x; t < rows * kH; t += kH) A2[r0 * kH + t] = h1[t];
-  dense(h1, kH, P + kOffW3, P + kOffB3, true, h0);
-  if (A3)
-    for (int t = threadIdx.x; t < rows * kH; t += kH) A3[r0 * kH + t] = h0[t];
-  // output logit: one warp per row, reduction over the 128 hidden units
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int r = warp; r < rows; r += kH / 32) {
-    float s = 0.f;
-    for (int k = lane; k < kH; k += 32) s = fmaf(h0[r * kH + k], bf(P, kOffW4 + k), s);
+// c = bias + A W for one warp's 16 rows; Wt is [kH][ld] (n-major), K the layer width
+template <int K>
+__device__ __forceinline__ void mma_layer(const uint32_t (&a)[K / 16][4], const __nv_bfloat16* Wt, int ld,
+                                          const float* bias, float (&c)[kH / 8][4], int g, int t) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) logits[r0 + r] = s + bf(P, kOffB4);
+  for (int nt = 0; nt < kH / 8; ++nt) {
+    const float b0 = bias[8 * nt + 2 * t], b1 = bias[8 * nt + 2 * t + 1];
+    c[nt][0] = b0;
+    c[nt][1] = b1;
+    c[nt][2] = b0;
+    c[nt][3] = b1;
+    const __nv_bfloat16* w = Wt + (8 * nt + g) * ld + 2 * t;
+#pragma unroll
+    for (int ks = 0; ks < K / 16; ++ks) {
+      const uint32_t w0 = *reinterpret_cast<const uint32_t*>(w + 16 * ks);
+      const uint32_t w1 = *reinterpret_cast<const uint32_t*>(w + 16 * ks + 8);
+      mma_bf16(c[nt], a[ks], w0, w1);
+    }
+  }
+}
+
+// ReLU of the accumulators, packed as the next layer's A fragments; the
+// rounded activations are stored to out (when not NULL) for rows ra, rb
+__device__ __forceinline__ void relu_pack(float (&c)[kH / 8][4], uint32_t (&a)[kH / 16][4], float* out, int64_t ra,
+                                          int64_t rb, int64_t n, int t) {
+#pragma unroll
+  for (int nt = 0; nt < kH / 8; ++nt) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) c[nt][q] = round_bf16(fmaxf(c[nt][q], 0.f));
+    if (out) {
+      const int col = 8 * nt + 2 * t;
+      if (ra < n) *reinterpret_cast<float2*>(out + ra * kH + col) = make_float2(c[nt][0], c[nt][1]);
+      if (rb < n) *reinterpret_cast<float2*>(out + rb * kH + col) = make_float2(c[nt][2], c[nt][3]);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < kH / 16; ++j) {
+    a[j][0] = pack_bf16(c[2 * j][0], c[2 * j][1]);
+    a[j][1] = pack_bf16(c[2 * j][2], c[2 * j][3]);
+    a[j][2] = pack_bf16(c[2 * j + 1][0], c[2 * j + 1][1]);
+    a[j][3] = pack_bf16(c[2 * j + 1][2], c[2 * j + 1][3]);
+  }
+}
+
+__global__ void __launch_bounds__(32 * kMmaWarps, 2) forward_kernel(const float* feat, int64_t n,
+                                                                    const __nv_bfloat16* P, float* A1, float* A2,
+                                                                    float* A3, float* logits) {
+  extern __shared__ __align__(16) unsigned char fsm[];
+  __nv_bfloat16* W1t = reinterpret_cast<__nv_bfloat16*>(fsm);
+  __nv_bfloat16* W2t = W1t + kH * kLd1;
+  __nv_bfloat16* W3t = W2t + kH * kLdH;
+  float* vec = reinterpret_cast<float*>(W3t + kH * kLdH);  // b1, b2, b3, w4, b4
+  for (int i = threadIdx.x; i < kIn * kH; i += blockDim.x) W1t[(i % kH) * kLd1 + i / kH] = P[kOffW1 + i];
+  for (int i = threadIdx.x; i < kH * kH; i += blockDim.x) {
+    W2t[(i % kH) * kLdH + i / kH] = P[kOffW2 + i];
+    W3t[(i % kH) * kLdH + i / kH] = P[kOffW3 + i];
+  }
+  for (int i = threadIdx.x; i < kH; i += blockDim.x) {
+    vec[i] = __bfloat162float(P[kOffB1 + i]);
+    vec[kH + i] = __bfloat162float(P[kOffB2 + i]);
+    vec[2 * kH + i] = __bfloat162float(P[kOffB3 + i]);
+    vec[3 * kH + i] = __bfloat162float(P[kOffW4 + i]);
+  }
+  if (threadIdx.x == 0) vec[4 * kH] = __bfloat162float(P[kOffB4]);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int g = lane >> 2, t = lane & 3;
+  const int64_t tiles = (n + kTileRows - 1) / kTileRows;
+  for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const int64_t ra = tile * kTileRows + 16 * warp + g, rb = ra + 8;
+    uint32_t a1[kIn / 16][4];
+#pragma unroll
+    for (int ks = 0; ks < kIn / 16; ++ks) {
+      const int c0 = 16 * ks + 2 * t;
+      float2 x00 = make_float2(0.f, 0.f), x01 = x00, x10 = x00, x11 = x00;
+      if (ra < n) {
+        x00 = *reinterpret_cast<const float2*>(feat + ra * kIn + c0);
+        x01 = *reinterpret_cast<const float2*>(feat + ra * kIn + c0 + 8);
+      }
+      if (rb < n) {
+        x10 = *reinterpret_cast<const float2*>(feat + rb * kIn + c0);
+        x11 = *reinterpret_cast<const float2*>(feat + rb * kIn + c0 + 8);
+      }
+      a1[ks][0] = pack_bf16(x00.x, x00.y);
+      a1[ks][1] = pack_bf16(x10.x, x10.y);
+      a1[ks][2] = pack_bf16(x01.x, x01.y);
+      a1[ks][3] = pack_bf16(x11.x, x11.y);
+    }
+    float c[kH / 8][4];
+    uint32_t a[kH / 16][4];
+    mma_layer<kIn>(a1, W1t, kLd1, vec, c, g, t);
+    relu_pack(c, a, A1, ra, rb, n, t);
+    mma_layer<kH>(a, W2t, kLdH, vec + kH, c, g, t);
+    relu_pack(c, a, A2, ra, rb, n, t);
+    mma_layer<kH>(a, W3t, kLdH, vec + 2 * kH, c, g, t);
+    float sa = 0.f, sb = 0.f;
+#pragma unroll
+    for (int nt = 0; nt < kH / 8; ++nt) {
+      const int col = 8 * nt + 2 * t;
+      const float h0 = fmaxf(c[nt][0], 0.f), h1 = fmaxf(c[nt][1], 0.f);
+      const float h2 = fmaxf(c[nt][2], 0.f), h3 = fmaxf(c[nt][3], 0.f);
+      sa = fmaf(h0, vec[3 * kH + col], fmaf(h1, vec[3 * kH + col + 1], sa));
+      sb = fmaf(h2, vec[3 * kH + col], fmaf(h3, vec[3 * kH + col + 1], sb));
+      if (A3) {
+        if (ra < n) *reinterpret_cast<float2*>(A3 + ra * kH + col) = make_float2(h0, h1);
+        if (rb < n) *reinterpret_cast<float2*>(A3 + rb * kH + col) = make_float2(h2, h3);
+      }
+    }
+    sa += __shfl_xor_sync(0xffffffffu, sa, 1);
+    sa += __shfl_xor_sync(0xffffffffu, sa, 2);
+    sb += __shfl_xor_sync(0xffffffffu, sb, 1);
+    sb += __shfl_xor_sync(0xffffffffu, sb, 2);
+    if (t == 0) {
+      if (ra < n) logits[ra] = sa + vec[4 * kH];
+      if (rb < n) logits[rb] = sb + vec[4 * kH];
+    }
   }
 }
 
@@ -300,7 +391,9 @@ __global__ void __launch_bounds__(kH) backward_kernel(const float* feat, int64_t
     for (int L = 0; L < 3; ++L) {
       const int width = widths[L];
       __syncthreads();
-      for (int t = j; t < kRows * width; t += kH) act[t] = t / width < rows ? prevs[L][r0 * width + t] : 0.f;
+      // the first layer read the features rounded to BF16
+      for (int t = j; t < kRows * width; t += kH)
+        act[t] = t / width < rows ? (L == 2 ? round_bf16(prevs[L][r0 * width + t]) : prevs[L][r0 * width + t]) : 0.f;
       __syncthreads();
       float dzr[kRows];
       float sb = 0.f;
@@ -452,7 +545,13 @@ gcr_status gcr_learned_forward(const float* d_feat, int64_t n, const void* d_bf1
                                float* d_a3, float* d_logits, void* stream) {
   if (!d_feat || !d_bf16 || !d_logits) return fail(GCR_INVALID_ARG, "NULL buffer");
   if (n <= 0) return GCR_OK;
-  forward_kernel<<<(unsigned)((n + kRows - 1) / kRows), kH, 0, (cudaStream_t)stream>>>(
+  int dev = 0, sms = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  CUDA_TRY(cudaFuncSetAttribute(forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kForwardSmem));
+  const int64_t tiles = (n + kTileRows - 1) / kTileRows;
+  const unsigned grid = (unsigned)(tiles < 2 * sms ? tiles : 2 * sms);
+  forward_kernel<<<grid, 32 * kMmaWarps, kForwardSmem, (cudaStream_t)stream>>>(
       d_feat, n, (const __nv_bfloat16*)d_bf16, d_a1, d_a2, d_a3, d_logits);
   CUDA_TRY(cudaGetLastError());
   return GCR_OK;

@@ -100,21 +100,25 @@ def adam(m, v, P, g, lr, step, b1=0.9, b2=0.999, eps=1e-8):
     return m, v, P
 
 
-def forward(X, P):
+def forward(X, P, rounding=True):
+    """(A1, A2, A3, z): the device forward (gcr_learned.cu, forward_kernel) in
+    FP64. With rounding, the inputs of the first three layers are rounded to
+    BF16 (the features, and A1, A2 as stored); A3 stays unrounded."""
     W1, b1, W2, b2, W3, b3, W4, b4 = unpack(P)
-    X = np.asarray(X, np.float64)
-    A1 = np.maximum(X @ W1 + b1, 0)
-    A2 = np.maximum(A1 @ W2 + b2, 0)
+    r = bf16_round if rounding else (lambda v: np.asarray(v, np.float64))
+    Xb = r(X)
+    A1 = r(np.maximum(Xb @ W1 + b1, 0))
+    A2 = r(np.maximum(A1 @ W2 + b2, 0))
     A3 = np.maximum(A2 @ W3 + b3, 0)
     z = A3 @ W4 + b4
     return A1, A2, A3, z
 
 
-def loss_and_grad(X, P, y, w):
-    """Weighted BCE with logits divided by sum(w), and its gradient."""
+def grad_from(Xin, A1, A2, A3, z, P, y, w):
+    """Weighted BCE with logits divided by sum(w), and its gradient, from the
+    layer inputs of a forward pass (Xin: the first layer's input)."""
     W1, b1, W2, b2, W3, b3, W4, b4 = unpack(P)
-    X = np.asarray(X, np.float64)
-    A1, A2, A3, z = forward(X, P)
+    Xin, A1, A2, A3, z = (np.asarray(v, np.float64) for v in (Xin, A1, A2, A3, z))
     ws = np.sum(w)
     loss = np.sum(w * (np.maximum(z, 0) - z * y + np.log1p(np.exp(-np.abs(z))))) / ws
     g4 = (1 / (1 + np.exp(-z)) - y) * w / ws
@@ -128,6 +132,14 @@ def loss_and_grad(X, P, y, w):
     G[OFF["W2"]:OFF["b2"]] = (A1.T @ dz2).ravel()
     G[OFF["b2"]:OFF["W3"]] = dz2.sum(0)
     dz1 = (dz2 @ W2.T) * (A1 > 0)
-    G[OFF["W1"]:OFF["b1"]] = (X.T @ dz1).ravel()
+    G[OFF["W1"]:OFF["b1"]] = (Xin.T @ dz1).ravel()
     G[OFF["b1"]:OFF["W2"]] = dz1.sum(0)
     return loss, G
+
+
+def loss_and_grad(X, P, y, w, rounding=True):
+    """Loss and gradient through forward(X, P, rounding); the BF16 roundings
+    pass gradients straight through."""
+    A1, A2, A3, z = forward(X, P, rounding)
+    Xin = bf16_round(X) if rounding else np.asarray(X, np.float64)
+    return grad_from(Xin, A1, A2, A3, z, P, y, w)

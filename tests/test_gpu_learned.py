@@ -1,7 +1,7 @@
 """GPU checks of the learned proposal (csrc/gcr_learned.cu) against the NumPy
-oracle (oracle/oracle_mlp.py): neighbour features bit-exact, forward logits
-and the backward gradient within FP32-accumulation tolerance of the FP64
-restatement on the same BF16 weights, the Adam step, the per-pair ordering and
+oracle (oracle/oracle_mlp.py): neighbour features bit-exact, tensor-core
+forward logits and the backward gradient within FP32-accumulation tolerance of
+the FP64 restatement on the same BF16 weights and roundings, the Adam step, the per-pair ordering and
 mask mapping exact; the learned batch equals the plain engine run on the same
 order; and a trained network's gain over the uniform sampler on hard pairs."""
 import numpy as np
@@ -13,7 +13,7 @@ from pygcransac import _abi, synthetic as S
 pytestmark = pytest.mark.gpu
 
 # FP32 accumulation of BF16-weighted sums over <= 128 terms against FP64
-LOGIT_RTOL = 1e-4
+LOGIT_RTOL = 1e-3
 GRAD_RTOL = 2e-4
 
 
@@ -52,17 +52,41 @@ def test_features_bit_exact(net):
         assert np.array_equal(got, ref), f"pair {i} (n={len(c)}): rows {np.nonzero((got != ref).any(1))[0][:8]}"
 
 
+def _device_forward(torch, net, X):
+    n = len(X)
+    a = [torch.empty((n, 128), dtype=torch.float32, device="cuda") for _ in range(3)]
+    z = torch.empty(n, dtype=torch.float32, device="cuda")
+    d_x = torch.from_numpy(X).cuda()
+    import ctypes
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    assert net.lib.gcr_learned_forward(vp(d_x), n, vp(net.bf16), vp(a[0]), vp(a[1]), vp(a[2]), vp(z), None) == 0
+    return d_x, [t.cpu().numpy().astype(np.float64) for t in a], z
+
+
 def test_forward_matches_oracle(torch, net):
-    c, z = _pairs([700], 11)[0]
+    """Tensor-core forward vs the FP64 restatement with the same BF16
+    roundings: the two accumulate in different orders, so an activation close
+    to a BF16 rounding boundary can round to the neighbouring value (one BF16
+    ulp); such flips are rare and move a logit by far less than its scale."""
+    c, z = _pairs([3000], 11)[0]
     X = M.features(c, z)
     Pb = net.bf16_parameters()
-    got = net.logits(torch.from_numpy(X).cuda()).cpu().numpy()
-    _, _, _, ref = M.forward(X, Pb)
+    _, (a1, a2, a3), zd = _device_forward(torch, net, X)
+    A1, A2, A3, ref = M.forward(X, Pb)
+    got = zd.cpu().numpy()
     scale = np.abs(ref).max()
-    np.testing.assert_allclose(got, ref, rtol=LOGIT_RTOL, atol=LOGIT_RTOL * scale)
+    d = np.abs(got - ref)
+    assert np.percentile(d, 99) <= LOGIT_RTOL * scale, (np.percentile(d, 99), scale)
+    assert d.max() <= 1e-2 * scale
+    for dev, orc in ((a1, A1), (a2, A2)):
+        assert np.mean(dev != orc) < 2e-3  # BF16 values: equal unless a rounding flipped
+    np.testing.assert_allclose(a3, A3, rtol=1e-2, atol=1e-2 * np.abs(A3).max())
 
 
 def test_backward_matches_oracle(torch, net):
+    """Gradient of the device backward pass vs the FP64 restatement on the
+    device forward's own layer inputs (so only the backward arithmetic is
+    compared)."""
     c, z = _pairs([1000], 12)[0]
     X = M.features(c, z)
     rng = np.random.Generator(np.random.PCG64(5))
@@ -70,7 +94,9 @@ def test_backward_matches_oracle(torch, net):
     w = np.where(y > 0, 2.5, 1.0).astype(np.float32)
     loss, G = net.loss_and_grad(torch.from_numpy(X).cuda(), torch.from_numpy(y).cuda(), torch.from_numpy(w).cuda())
     G = G.cpu().numpy().astype(np.float64)
-    loss_ref, G_ref = M.loss_and_grad(X, net.bf16_parameters(), y.astype(np.float64), w.astype(np.float64))
+    _, (a1, a2, a3), zd = _device_forward(torch, net, X)
+    loss_ref, G_ref = M.grad_from(M.bf16_round(X), a1, a2, a3, zd.cpu().numpy(), net.bf16_parameters(),
+                                  y.astype(np.float64), w.astype(np.float64))
     assert abs(loss - loss_ref) <= 1e-5 * max(1.0, abs(loss_ref))
     for name, a, b in [("W1", "W1", "b1"), ("b1", "b1", "W2"), ("W2", "W2", "b2"), ("b2", "b2", "W3"),
                        ("W3", "W3", "b3"), ("b3", "b3", "W4"), ("W4", "W4", "b4")]:

@@ -17,14 +17,14 @@ def test_gradient_matches_finite_differences():
     X[:, M.FEAT:] = 0
     y = (rng.uniform(size=12) < 0.5).astype(float)
     w = rng.uniform(0.5, 2.0, 12)
-    _, G = M.loss_and_grad(X, P, y, w)
+    _, G = M.loss_and_grad(X, P, y, w, rounding=False)
     idx = np.r_[rng.integers(0, M.OFF["count"], 200), M.OFF["b4"], M.OFF["W4"] + 3]
     h = 1e-6
     for i in idx:
         Pp, Pm = P.copy(), P.copy()
         Pp[i] += h
         Pm[i] -= h
-        fd = (M.loss_and_grad(X, Pp, y, w)[0] - M.loss_and_grad(X, Pm, y, w)[0]) / (2 * h)
+        fd = (M.loss_and_grad(X, Pp, y, w, rounding=False)[0] - M.loss_and_grad(X, Pm, y, w, rounding=False)[0]) / (2 * h)
         assert abs(fd - G[i]) <= 1e-6 + 1e-5 * abs(fd), (i, fd, G[i])
 
 
