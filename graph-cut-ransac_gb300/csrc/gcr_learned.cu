@@ -40,6 +40,9 @@ constexpr int kRows = 16;      // rows (correspondences) per CTA of the MLP pass
 constexpr int kTile = 128;     // query rows per CTA of the neighbour search and the ordering
 constexpr int kCand = 2048;    // candidates staged in shared memory per round
 constexpr double kMissing = 65536.0;  // squared length standing in for a missing neighbour (feature 4.0)
+constexpr int kGridMax = 8192;      // pairs up to this size use the shared-memory grid search
+constexpr int kGridMaxSide = 64;    // at most 64 x 64 cells (G^2 <= kGridMax / 2)
+constexpr int kGridThreads = 256;
 // parameter layout (floats): W1 [kIn][kH], b1 [kH], W2 [kH][kH], b2, W3, b3, W4 [kH], b4 [1]
 constexpr int kOffW1 = 0;
 constexpr int kOffB1 = kOffW1 + kIn * kH;
@@ -67,65 +70,48 @@ gcr_status fail(gcr_status s, const char* fmt, ...) {
     if (e_ != cudaSuccess) return fail(GCR_DEVICE_ERROR, "%s failed: %s", #expr, cudaGetErrorString(e_)); \
   } while (0)
 
-// Features: grid (tile of kTile rows, pair). Each thread holds one query
-// correspondence; the pair's first-image points are staged through shared
-// memory in rounds of kCand and scanned with FP32 squared distances (each
-// operation rounded on its own, so the selection is reproducible on any
-// IEEE host), keeping the k nearest in registers (ascending distance, ties by
-// index).
-__global__ void __launch_bounds__(kTile) features_kernel(const double* corr, const int64_t* offsets,
-                                                         const gcr_image_size* sizes, float* feat) {
-  __shared__ float2 cand[kCand];
-  const int pair = blockIdx.y;
-  const int64_t o0 = offsets[pair];
-  const int n = (int)(offsets[pair + 1] - o0);
-  if ((int)blockIdx.x * kTile >= n) return;  // uniform over the CTA
-  const int i = (int)blockIdx.x * kTile + threadIdx.x;
-  const bool active = i < n;
-  float px = 0.f, py = 0.f;
-  if (active) {
-    px = (float)corr[4 * (o0 + i)];
-    py = (float)corr[4 * (o0 + i) + 1];
-  }
-  float bd[kK];
-  int bi[kK];
+// k nearest neighbours in registers, ascending by (squared distance, index);
+// a candidate enters when it precedes the current k-th. The order is the same
+// whatever the order the candidates arrive in.
+struct Knn {
+  float d[kK];
+  int j[kK];
+  __device__ __forceinline__ void init() {
 #pragma unroll
-  for (int k = 0; k < kK; ++k) {
-    bd[k] = INFINITY;
-    bi[k] = -1;
-  }
-  for (int c0 = 0; c0 < n; c0 += kCand) {
-    const int m = min(kCand, n - c0);
-    __syncthreads();
-    for (int t = threadIdx.x; t < m; t += kTile) {
-      const double* q = corr + 4 * (o0 + c0 + t);
-      cand[t] = make_float2((float)q[0], (float)q[1]);
+    for (int k = 0; k < kK; ++k) {
+      d[k] = INFINITY;
+      j[k] = -1;
     }
-    __syncthreads();
-    if (!active) continue;
-    for (int t = 0; t < m; ++t) {
-      const float2 q = cand[t];
-      const float ex = __fsub_rn(q.x, px), ey = __fsub_rn(q.y, py);
-      const float d = __fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey));
-      if (d < bd[kK - 1] && c0 + t != i) {
-        bd[kK - 1] = d;
-        bi[kK - 1] = c0 + t;
+  }
+  __device__ __forceinline__ void offer(float dist, int idx) {
+    if (dist < d[kK - 1] || (dist == d[kK - 1] && idx < j[kK - 1])) {
+      d[kK - 1] = dist;
+      j[kK - 1] = idx;
 #pragma unroll
-        for (int k = kK - 1; k > 0; --k) {
-          if (bd[k] < bd[k - 1]) {
-            const float tf = bd[k];
-            bd[k] = bd[k - 1];
-            bd[k - 1] = tf;
-            const int ti = bi[k];
-            bi[k] = bi[k - 1];
-            bi[k - 1] = ti;
-          }
+      for (int k = kK - 1; k > 0; --k) {
+        if (d[k] < d[k - 1] || (d[k] == d[k - 1] && j[k] < j[k - 1])) {
+          const float tf = d[k];
+          d[k] = d[k - 1];
+          d[k - 1] = tf;
+          const int ti = j[k];
+          j[k] = j[k - 1];
+          j[k - 1] = ti;
         }
       }
     }
   }
-  if (!active) return;
-  const gcr_image_size z = sizes[pair];
+};
+
+// FP32 squared distance, each operation rounded on its own (reproducible on
+// any IEEE host)
+__device__ __forceinline__ float sqdist(float qx, float qy, float px, float py) {
+  const float ex = __fsub_rn(qx, px), ey = __fsub_rn(qy, py);
+  return __fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey));
+}
+
+// Features of row i of a pair from its neighbours (local indices, -1 missing)
+__device__ void write_features(const double* corr, int64_t o0, int i, const int* nb, const gcr_image_size& z,
+                               float* feat) {
   const double* p = corr + 4 * (o0 + i);
   float* f = feat + (int64_t)kIn * (o0 + i);
   f[0] = (float)(p[0] / z.w1 - 0.5);
@@ -141,8 +127,8 @@ __global__ void __launch_bounds__(kTile) features_kernel(const double* corr, con
 #pragma unroll
   for (int k = 0; k < kK; ++k) {
     double mag = kMissing, dist = kMissing;
-    if (bi[k] >= 0) {
-      const double* q = corr + 4 * (o0 + bi[k]);
+    if (nb[k] >= 0) {
+      const double* q = corr + 4 * (o0 + nb[k]);
       const double a = (q[2] - q[0]) - dx, b = (q[3] - q[1]) - dy;
       const double ex = q[0] - p[0], ey = q[1] - p[1];
       mag = __dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b));
@@ -167,6 +153,168 @@ __global__ void __launch_bounds__(kTile) features_kernel(const double* corr, con
   }
 #pragma unroll
   for (int c = kFeat; c < kIn; ++c) f[c] = 0.f;
+}
+
+// Features of the pairs with more than kGridMax correspondences: grid (tile of
+// kTile rows, pair). Each thread holds one query; the pair's first-image
+// points stream through shared memory in rounds of kCand.
+__global__ void __launch_bounds__(kTile) features_scan_kernel(const double* corr, const int64_t* offsets,
+                                                              const gcr_image_size* sizes, float* feat) {
+  __shared__ float2 cand[kCand];
+  const int pair = blockIdx.y;
+  const int64_t o0 = offsets[pair];
+  const int n = (int)(offsets[pair + 1] - o0);
+  if (n <= kGridMax || (int)blockIdx.x * kTile >= n) return;  // uniform over the CTA
+  const int i = (int)blockIdx.x * kTile + threadIdx.x;
+  const bool active = i < n;
+  float px = 0.f, py = 0.f;
+  if (active) {
+    px = (float)corr[4 * (o0 + i)];
+    py = (float)corr[4 * (o0 + i) + 1];
+  }
+  Knn nn;
+  nn.init();
+  for (int c0 = 0; c0 < n; c0 += kCand) {
+    const int m = min(kCand, n - c0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < m; t += kTile) {
+      const double* q = corr + 4 * (o0 + c0 + t);
+      cand[t] = make_float2((float)q[0], (float)q[1]);
+    }
+    __syncthreads();
+    if (!active) continue;
+    for (int t = 0; t < m; ++t)
+      if (c0 + t != i) nn.offer(sqdist(cand[t].x, cand[t].y, px, py), c0 + t);
+  }
+  if (active) write_features(corr, o0, i, nn.j, sizes[pair], feat);
+}
+
+// Features of the pairs with at most kGridMax correspondences: one CTA per
+// pair. The first-image points are bucketed into a G x G grid over their
+// bounding box (G^2 about n / 2 cells) by a counting sort in shared memory;
+// each query then visits rings of cells around its own until its k-th
+// distance lies below the distance to every unvisited cell (with a margin of
+// 1e-3 cell for the rounding of cell boundaries). Exact: the same neighbours
+// as the all-pairs scan.
+__host__ __device__ constexpr size_t grid_smem_bytes(int max_n) {
+  return sizeof(float2) * (size_t)max_n + sizeof(int) * (size_t)max_n + 2 * sizeof(int) * (size_t)(max_n / 2 + 2);
+}
+
+__global__ void __launch_bounds__(kGridThreads) features_grid_kernel(const double* corr, const int64_t* offsets,
+                                                                     const gcr_image_size* sizes, float* feat) {
+  extern __shared__ __align__(16) unsigned char gsm[];
+  __shared__ float bbox[4];
+  __shared__ float red[4][kGridThreads / 32];
+  const int pair = blockIdx.x;
+  const int64_t o0 = offsets[pair];
+  const int n = (int)(offsets[pair + 1] - o0);
+  if (n > kGridMax || n <= 0) return;  // uniform over the CTA
+  float2* pts = reinterpret_cast<float2*>(gsm);
+  int* sorted = reinterpret_cast<int*>(pts + n);
+  const int G = max(1, min(kGridMaxSide, (int)sqrtf(0.5f * (float)n)));
+  const int cells = G * G;
+  int* start = sorted + n;        // [cells + 1]
+  int* cursor = start + cells + 1;  // [cells]
+  float mnx = INFINITY, mny = INFINITY, mxx = -INFINITY, mxy = -INFINITY;
+  for (int i = threadIdx.x; i < n; i += kGridThreads) {
+    const double* q = corr + 4 * (o0 + i);
+    const float2 v = make_float2((float)q[0], (float)q[1]);
+    pts[i] = v;
+    mnx = fminf(mnx, v.x);
+    mny = fminf(mny, v.y);
+    mxx = fmaxf(mxx, v.x);
+    mxy = fmaxf(mxy, v.y);
+  }
+  for (int c = threadIdx.x; c < cells; c += kGridThreads) cursor[c] = 0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+    mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+    mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+    mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    red[0][warp] = mnx;
+    red[1][warp] = mny;
+    red[2][warp] = mxx;
+    red[3][warp] = mxy;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float a = INFINITY, b = INFINITY, c = -INFINITY, d = -INFINITY;
+    for (int w = 0; w < kGridThreads / 32; ++w) {
+      a = fminf(a, red[0][w]);
+      b = fminf(b, red[1][w]);
+      c = fmaxf(c, red[2][w]);
+      d = fmaxf(d, red[3][w]);
+    }
+    bbox[0] = a;
+    bbox[1] = b;
+    bbox[2] = (c - a) > 0.f ? (c - a) / (float)G : 1.f;  // cell width
+    bbox[3] = (d - b) > 0.f ? (d - b) / (float)G : 1.f;  // cell height
+  }
+  __syncthreads();
+  const float x0 = bbox[0], y0 = bbox[1], cw = bbox[2], ch = bbox[3];
+  auto cell_of = [&](float2 v, int& cx, int& cy) {
+    cx = min(G - 1, max(0, (int)((v.x - x0) / cw)));
+    cy = min(G - 1, max(0, (int)((v.y - y0) / ch)));
+  };
+  for (int i = threadIdx.x; i < n; i += kGridThreads) {
+    int cx, cy;
+    cell_of(pts[i], cx, cy);
+    atomicAdd(&cursor[cy * G + cx], 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int c = 0; c < cells; ++c) {
+      start[c] = acc;
+      acc += cursor[c];
+      cursor[c] = start[c];
+    }
+    start[cells] = acc;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += kGridThreads) {
+    int cx, cy;
+    cell_of(pts[i], cx, cy);
+    sorted[atomicAdd(&cursor[cy * G + cx], 1)] = i;
+  }
+  __syncthreads();
+  const float mx = 1e-3f * cw, my = 1e-3f * ch;
+  for (int i = threadIdx.x; i < n; i += kGridThreads) {
+    const float2 q = pts[i];
+    int cx, cy;
+    cell_of(q, cx, cy);
+    Knn nn;
+    nn.init();
+    for (int r = 0;; ++r) {
+      for (int dy = -r; dy <= r; ++dy) {
+        const int y = cy + dy;
+        if (y < 0 || y >= G) continue;
+        const int step = (dy == -r || dy == r) ? 1 : 2 * r;
+        for (int dx = -r; dx <= r; dx += max(step, 1)) {
+          const int x = cx + dx;
+          if (x < 0 || x >= G) continue;
+          const int c = y * G + x;
+          for (int s = start[c]; s < start[c + 1]; ++s) {
+            const int j = sorted[s];
+            if (j != i) nn.offer(sqdist(pts[j].x, pts[j].y, q.x, q.y), j);
+          }
+        }
+      }
+      // distance to the nearest unvisited cell (sides still inside the grid)
+      float lb = INFINITY;
+      if (cx - r > 0) lb = fminf(lb, q.x - (x0 + (float)(cx - r) * cw) - mx);
+      if (cx + r < G - 1) lb = fminf(lb, (x0 + (float)(cx + r + 1) * cw) - q.x - mx);
+      if (cy - r > 0) lb = fminf(lb, q.y - (y0 + (float)(cy - r) * ch) - my);
+      if (cy + r < G - 1) lb = fminf(lb, (y0 + (float)(cy + r + 1) * ch) - q.y - my);
+      if (lb == INFINITY) break;  // the rings cover the grid
+      if (lb > 0.f && nn.d[kK - 1] < lb * lb) break;
+    }
+    write_features(corr, o0, i, nn.j, sizes[pair], feat);
+  }
 }
 
 __device__ __forceinline__ float bf(const __nv_bfloat16* w, int i) { return __bfloat162float(w[i]); }
@@ -446,8 +594,8 @@ __global__ void __launch_bounds__(kH) backward_kernel(const float* feat, int64_t
     if (acc[t] != 0.f) atomicAdd(G + t, acc[t]);
 }
 
-// Descending order of the logits within each pair (ties by index, NaN last):
-// grid (tile of kTile rows, pair). Row i's rank is the number of rows of its
+// Descending order of the logits within each pair (ties by index, NaN last),
+// for pairs of more than kGridMax rows: grid (tile of kTile rows, pair). Row i's rank is the number of rows of its
 // pair that precede it; the row is copied to that position of the sorted
 // correspondences and its local index recorded in perm.
 __device__ __forceinline__ float order_key(float z) { return isnan(z) ? -INFINITY : z; }
@@ -458,7 +606,7 @@ __global__ void __launch_bounds__(kTile) order_kernel(const double* corr, const 
   const int pair = blockIdx.y;
   const int64_t o0 = offsets[pair];
   const int n = (int)(offsets[pair + 1] - o0);
-  if ((int)blockIdx.x * kTile >= n) return;  // uniform over the CTA
+  if (n <= kGridMax || (int)blockIdx.x * kTile >= n) return;  // uniform over the CTA
   const int i = (int)blockIdx.x * kTile + threadIdx.x;
   const bool active = i < n;
   const float zi = active ? order_key(logits[o0 + i]) : 0.f;
@@ -476,9 +624,58 @@ __global__ void __launch_bounds__(kTile) order_kernel(const double* corr, const 
   }
   if (!active) return;
   const int64_t dst = o0 + rank;
-  const double4 v = *reinterpret_cast<const double4*>(corr + 4 * (o0 + i));
-  *reinterpret_cast<double4*>(sorted + 4 * dst) = v;
+  const double4_32a v = *reinterpret_cast<const double4_32a*>(corr + 4 * (o0 + i));
+  *reinterpret_cast<double4_32a*>(sorted + 4 * dst) = v;
   perm[dst] = i;
+}
+
+// The same order for pairs of at most kGridMax rows: one CTA per pair sorts
+// 64-bit keys (the logit mapped to an unsigned integer whose ascending order
+// is the logits' descending order, NaN last and -0 equal to +0, then the row)
+// with a bitonic network in shared memory.
+__device__ __forceinline__ uint64_t order_key64(float z, int i) {
+  float k = order_key(z);
+  if (k == 0.f) k = 0.f;  // -0 sorts with +0
+  const uint32_t u = __float_as_uint(-k);
+  const uint32_t asc = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+  return ((uint64_t)asc << 32) | (uint32_t)i;
+}
+
+constexpr int kSortThreads = 512;
+
+__global__ void __launch_bounds__(kSortThreads) order_sort_kernel(const double* corr, const int64_t* offsets,
+                                                                  const float* logits, double* sorted, int* perm) {
+  extern __shared__ __align__(16) unsigned long long keys[];
+  const int pair = blockIdx.x;
+  const int64_t o0 = offsets[pair];
+  const int n = (int)(offsets[pair + 1] - o0);
+  if (n > kGridMax || n <= 0) return;  // uniform over the CTA
+  int npad = 1;
+  while (npad < n) npad <<= 1;
+  for (int i = threadIdx.x; i < npad; i += kSortThreads)
+    keys[i] = i < n ? order_key64(logits[o0 + i], i) : ~0ull;
+  __syncthreads();
+  for (int k = 2; k <= npad; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < npad; i += kSortThreads) {
+        const int l = i ^ j;
+        if (l > i) {
+          const unsigned long long a = keys[i], b = keys[l];
+          if ((a > b) == ((i & k) == 0)) {
+            keys[i] = b;
+            keys[l] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (int s = threadIdx.x; s < n; s += kSortThreads) {
+    const int i = (int)(keys[s] & 0xffffffffull);
+    const double4_32a v = *reinterpret_cast<const double4_32a*>(corr + 4 * (o0 + i));
+    *reinterpret_cast<double4_32a*>(sorted + 4 * (o0 + s)) = v;
+    perm[o0 + s] = i;
+  }
 }
 
 // mask[offsets[pair] + perm[r]] = sorted_mask[r]
@@ -528,9 +725,17 @@ gcr_status gcr_learned_features(const double* d_corr, const int64_t* d_offsets, 
   const gcr_status st = check_pairs(num_pairs, max_n);
   if (st != GCR_OK) return st;
   if (num_pairs == 0 || max_n == 0) return GCR_OK;
-  const dim3 grid((unsigned)((max_n + kTile - 1) / kTile), (unsigned)num_pairs);
-  features_kernel<<<grid, kTile, 0, (cudaStream_t)stream>>>(d_corr, d_offsets, d_sizes, d_feat);
+  const int small_n = (int)(max_n < kGridMax ? max_n : kGridMax);
+  const size_t smem = grid_smem_bytes(small_n);
+  CUDA_TRY(cudaFuncSetAttribute(features_grid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  features_grid_kernel<<<(unsigned)num_pairs, kGridThreads, smem, (cudaStream_t)stream>>>(d_corr, d_offsets,
+                                                                                            d_sizes, d_feat);
   CUDA_TRY(cudaGetLastError());
+  if (max_n > kGridMax) {
+    const dim3 grid((unsigned)((max_n + kTile - 1) / kTile), (unsigned)num_pairs);
+    features_scan_kernel<<<grid, kTile, 0, (cudaStream_t)stream>>>(d_corr, d_offsets, d_sizes, d_feat);
+    CUDA_TRY(cudaGetLastError());
+  }
   return GCR_OK;
 }
 
@@ -596,9 +801,18 @@ gcr_status gcr_learned_order(const double* d_corr, const int64_t* d_offsets, int
   const gcr_status st = check_pairs(num_pairs, max_n);
   if (st != GCR_OK) return st;
   if (num_pairs == 0 || max_n == 0) return GCR_OK;
-  const dim3 grid((unsigned)((max_n + kTile - 1) / kTile), (unsigned)num_pairs);
-  order_kernel<<<grid, kTile, 0, (cudaStream_t)stream>>>(d_corr, d_offsets, d_logits, d_sorted_corr, d_perm);
+  int npad = 1;
+  while (npad < (max_n < kGridMax ? max_n : kGridMax)) npad <<= 1;
+  const size_t smem = sizeof(unsigned long long) * (size_t)npad;
+  CUDA_TRY(cudaFuncSetAttribute(order_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  order_sort_kernel<<<(unsigned)num_pairs, kSortThreads, smem, (cudaStream_t)stream>>>(d_corr, d_offsets, d_logits,
+                                                                                       d_sorted_corr, d_perm);
   CUDA_TRY(cudaGetLastError());
+  if (max_n > kGridMax) {
+    const dim3 grid((unsigned)((max_n + kTile - 1) / kTile), (unsigned)num_pairs);
+    order_kernel<<<grid, kTile, 0, (cudaStream_t)stream>>>(d_corr, d_offsets, d_logits, d_sorted_corr, d_perm);
+    CUDA_TRY(cudaGetLastError());
+  }
   return GCR_OK;
 }
 

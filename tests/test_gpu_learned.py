@@ -43,7 +43,16 @@ def _pairs(sizes_n, seed0=0):
 
 
 def test_features_bit_exact(net):
-    pairs = _pairs([300, 1, 2, 8, 9, 2500, 129])
+    """Grid search (pairs up to 8192) and all-pairs scan (larger pairs) give
+    the oracle's features bit for bit, including duplicate points (distance
+    ties broken by index), a zero-width bounding box and points outside the
+    image."""
+    pairs = _pairs([300, 1, 2, 8, 9, 2500, 129, 8500])
+    rng = np.random.Generator(np.random.PCG64(21))
+    dup = rng.integers(0, 12, (600, 4)).astype(np.float64)  # many identical first-image points
+    line = np.c_[np.full(300, 17.0), rng.uniform(0, 480, 300), rng.uniform(0, 640, (300, 2))]
+    outside = rng.uniform(-200, 900, (700, 4))
+    pairs += [(dup, (480, 640, 480, 640)), (line, (480, 640, 480, 640)), (outside, (480, 640, 480, 640))]
     feat, offsets = net.host_features([c for c, _ in pairs], [z for _, z in pairs])
     F = feat.cpu().numpy()
     for i, (c, z) in enumerate(pairs):
@@ -127,12 +136,13 @@ def test_order_and_unpermute_exact(torch, net):
     lib = _abi.load()
     from pygcransac.learned import layout
     rng = np.random.Generator(np.random.PCG64(4))
-    lens = [5, 1, 3000, 257, 64]
+    lens = [5, 1, 3000, 257, 64, 8500]  # the last uses the counting kernel, the others the bitonic sort
     corr = [rng.uniform(0, 640, (n, 4)) for n in lens]
     offsets, max_n, por = layout(lens)
     z = np.round(rng.normal(size=int(offsets[-1])), 1).astype(np.float32)  # many ties
-    z[[3, 10, 400]] = np.nan
-    z[[11, 12]] = -np.inf
+    z[[3, 10, 400, 4000]] = np.nan
+    z[[11, 12, 4001]] = -np.inf
+    z[[13, 14]] = [0.0, -0.0]
     d_corr = torch.from_numpy(np.concatenate(corr)).cuda()
     d_off = torch.from_numpy(offsets).cuda()
     d_z = torch.from_numpy(z).cuda()
