@@ -94,6 +94,7 @@ struct gcr_context {
   } pending;
   int slot_kind = -1, slot_max_n = 0, slot_count = 0;
   bool prepared[3] = {false, false, false};
+  unsigned long long* pair_times = nullptr;  // see gcr_context_set_pair_times
 };
 
 namespace {
@@ -370,6 +371,7 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
   ws.masks_out = d_masks_out;
   ws.stats_out = (gcr::StatsOut*)d_stats_out;
   ws.phase = nullptr;
+  ws.times = c->pair_times;
 #ifdef GCR_PHASE_PROFILE
   CUDA_TRY(c->phase.ensure(sizeof(long long) * 16 * num_pairs));
   CUDA_TRY(cudaMemsetAsync(c->phase.p, 0, sizeof(long long) * 16 * num_pairs, s));
@@ -466,6 +468,12 @@ gcr_status gcr_batch_prepare(gcr_context* c, gcr_model_kind kind, int64_t num_pa
                                 d_masks_out, d_stats_out, 0, &c->pending);
   if (st != GCR_OK) return st;
   CUDA_TRY(cudaStreamSynchronize(0));
+  return GCR_OK;
+}
+
+gcr_status gcr_context_set_pair_times(gcr_context* c, unsigned long long* d_times) {
+  if (!c) return fail(GCR_INVALID_ARG, "context is NULL");
+  c->pair_times = d_times;
   return GCR_OK;
 }
 

@@ -142,6 +142,7 @@ struct Workspace {
   uint8_t* masks_out;   // [total]
   StatsOut* stats_out;  // [P]
   long long* phase;     // [P][16] phase cycle counters (GCR_PHASE_PROFILE builds), else null
+  unsigned long long* times;  // [P][2] global timer (ns) when a CTA takes the pair and when it is done, or null
 };
 
 struct Score {

@@ -27,6 +27,13 @@ __device__ inline double block_max_abs(double v, double* red) {
   return r;
 }
 
+// The GPU's global nanosecond timer (per-pair service times).
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
 // Persistent kernel: each CTA takes pairs from a global ticket until none is
 // left; blockIdx.x selects the CTA's scratch slot.
 // Dynamic shared memory: the FP32 correspondence tile, the engine state and,
@@ -59,6 +66,7 @@ __global__ void __launch_bounds__(GCR_BLOCK, GCR_MIN_BLOCKS) pair_kernel(Workspa
     __syncthreads();
     const int pair = s_pair;
     if (pair >= prm.num_pairs) break;
+    if (ws.times && threadIdx.x == 0) ws.times[2 * pair] = global_ns();
     const PairDesc pd = ws.pairs[pair];
     Engine<Est> eng(sh, ws, prm, pd, slot, pair);
     if constexpr (Est::KIND == 1) {
@@ -80,6 +88,10 @@ __global__ void __launch_bounds__(GCR_BLOCK, GCR_MIN_BLOCKS) pair_kernel(Workspa
     eng.pts32 = dst;
     __syncthreads();
     eng.run();
+    if (ws.times) {
+      __syncthreads();
+      if (threadIdx.x == 0) ws.times[2 * pair + 1] = global_ns();
+    }
   }
 }
 

@@ -191,6 +191,7 @@ extern "C" gcr_status gcr_find_homography_device_noalloc(const double* d_corr, i
   ws.masks_out = d_mask_out;
   ws.stats_out = (gcr::StatsOut*)d_stats_out;
   ws.phase = nullptr;
+  ws.times = nullptr;
 
   gcr::EngineParams prm{};
   prm.confidence = p.confidence;

@@ -101,6 +101,7 @@ _EXPORTS = {
                                                           _P]),
     "gcr_batch_prepare": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int64, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "gcr_batch_launch": (ctypes.c_int, [_P, _P]),
+    "gcr_context_set_pair_times": (ctypes.c_int, [_P, _P]),
     "gcr_run": (ctypes.c_int, [ctypes.c_int, _P, _P, ctypes.c_int64, _P, ctypes.c_int32, _P, _P, _P, _P, _P]),
     "gcr_learned_param_count": (ctypes.c_int64, []),
     "gcr_learned_feature_width": (ctypes.c_int32, []),

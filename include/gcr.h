@@ -198,6 +198,12 @@ gcr_status gcr_batch_prepare(gcr_context* ctx, gcr_model_kind kind, int64_t num_
                              gcr_stats* d_stats_out);
 gcr_status gcr_batch_launch(gcr_context* ctx, void* stream);
 
+/* Per-pair timing of the batches prepared on `ctx` from now on (no counterpart
+ * in the reference, whose statistics hold one wall-clock time per call):
+ * d_times [P][2] receives the GPU global timer in nanoseconds when a CTA takes
+ * pair i and when its result is written. NULL switches it off. */
+gcr_status gcr_context_set_pair_times(gcr_context* ctx, unsigned long long* d_times);
+
 /* GCRANSAC::run on one pair (GCRANSAC.h:200-627) without the Python drivers'
  * pre- and post-processing; the entry behind the C++ plugin surface
  * include/gcransac/GCRANSAC.h. `points` [n][4] are the coordinates the model
