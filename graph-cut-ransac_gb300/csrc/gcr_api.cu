@@ -20,6 +20,8 @@ namespace {
 thread_local std::string g_last_error;
 thread_local long long g_last_launches = 0;
 thread_local long long* g_last_phase = nullptr;
+// host probabilities of the single-pair entries, staged by gcr_find_batch
+thread_local const double* g_batch_probs = nullptr;
 
 gcr_status fail(gcr_status s, const char* fmt, ...) {
   char buf[512];
@@ -89,12 +91,15 @@ struct gcr_context {
     gcr::Workspace ws{};
     gcr::EngineParams prm{};
     bool normalise = false;
+    const double* probs = nullptr;  // importance sampler: probabilities to tabulate
     const double* d_corr = nullptr;
     int num_pairs = 0;
   } pending;
   int slot_kind = -1, slot_max_n = 0, slot_count = 0;
   bool prepared[3] = {false, false, false};
   unsigned long long* pair_times = nullptr;  // see gcr_context_set_pair_times
+  const double* probs = nullptr;             // see gcr_context_set_probabilities
+  DevBuf cdf, probs_stage;                   // importance sampler tables, staged probabilities
 };
 
 namespace {
@@ -108,9 +113,11 @@ gcr_status check_params(gcr_model_kind kind, const gcr_params* p) {
   if (p->max_iterations < 0 || p->min_iterations < 0) return fail(GCR_INVALID_ARG, "negative iteration limit");
   if (p->lo_number < 0 || p->lo_number > GCR_BLOCK)
     return fail(GCR_UNSUPPORTED, "lo_number must be in [0, %d]", GCR_BLOCK);
-  if (p->sampler != GCR_SAMPLER_UNIFORM && p->sampler != GCR_SAMPLER_PROSAC && p->sampler != GCR_SAMPLER_PNAPSAC)
+  if (p->sampler != GCR_SAMPLER_UNIFORM && p->sampler != GCR_SAMPLER_PROSAC && p->sampler != GCR_SAMPLER_PNAPSAC &&
+      p->sampler != GCR_SAMPLER_IMPORTANCE)
     return fail(GCR_UNSUPPORTED,
-                "sampler %d is not provided by the device engine (0 uniform, 1 PROSAC, 2 P-NAPSAC)", p->sampler);
+                "sampler %d is not provided by the device engine (0 uniform, 1 PROSAC, 2 P-NAPSAC, 3 importance)",
+                p->sampler);
   if (p->scoring != GCR_SCORING_MSAC && p->scoring != GCR_SCORING_MAGSAC)
     return fail(GCR_UNSUPPORTED, "scoring %d is not provided (0 MSAC, 1 MAGSAC++)", p->scoring);
   if (p->use_sprt && !(p->min_inlier_ratio_for_sprt > 0 && p->min_inlier_ratio_for_sprt < 1))
@@ -400,6 +407,12 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
   prm.use_sp = (kind == GCR_HOMOGRAPHY && params->use_space_partitioning) ? 1 : 0;
   prm.sprt_min_ratio = params->min_inlier_ratio_for_sprt;
   prm.epilogue = run_only ? 0 : 1;
+  prm.cdf = nullptr;
+  if (params->sampler == GCR_SAMPLER_IMPORTANCE) {
+    if (!c->probs) return fail(GCR_INVALID_ARG, "the importance sampler (3) needs per-correspondence probabilities");
+    CUDA_TRY(c->cdf.ensure(sizeof(double) * (size_t)std::max<int64_t>(total, 1)));
+    prm.cdf = (const double*)c->cdf.p;
+  }
   prm.mag_table = nullptr;
   prm.mag_c2dof = 0.25 * std::pow(2.0, 1.5);
   prm.mag_gamma_k = 0.0036572608340910764;
@@ -417,6 +430,7 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
   L->ws = ws;
   L->prm = prm;
   L->normalise = kind == GCR_ESSENTIAL && !run_only;
+  L->probs = params->sampler == GCR_SAMPLER_IMPORTANCE ? c->probs : nullptr;
   L->d_corr = d_corr;
   L->num_pairs = (int)num_pairs;
   L->valid = true;
@@ -433,10 +447,43 @@ static gcr_status launch_batch(gcr_context* c, const gcr_context::Pending& L, cu
                                              L.num_pairs, (double*)c->norm_pts.p, s));
     ++launches;
   }
+  if (L.probs) {
+    CUDA_TRY(gcr::launch_importance_cdf(L.probs, (const gcr::PairDesc*)c->pairs.p, L.num_pairs, (double*)c->cdf.p, s));
+    ++launches;
+  }
   CUDA_TRY(L.ops->launch(L.grid, s, L.ws, L.prm));
   g_last_launches = launches;
   return GCR_OK;
 }
+
+namespace gcr {
+
+// std::discrete_distribution's table (the reference's ImportanceSampler,
+// samplers/importance_sampler.h:67-81): p_i / sum p, running sums, the last
+// entry 1. One thread per pair, sums in row order (the oracle's order).
+__global__ void importance_cdf_kernel(const double* probs, const PairDesc* pairs, int num_pairs, double* cdf) {
+  const int pair = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pair >= num_pairs) return;
+  const PairDesc pd = pairs[pair];
+  const double* p = probs + pd.offset;
+  double* c = cdf + pd.offset;
+  double sum = 0.0;
+  for (int i = 0; i < pd.n; ++i) sum += p[i];
+  double acc = 0.0;
+  for (int i = 0; i < pd.n; ++i) {
+    acc += p[i] / sum;
+    c[i] = acc;
+  }
+  if (pd.n > 0) c[pd.n - 1] = 1.0;
+}
+
+cudaError_t launch_importance_cdf(const double* probs, const PairDesc* pairs, int num_pairs, double* cdf,
+                                  cudaStream_t s) {
+  importance_cdf_kernel<<<(num_pairs + 127) / 128, 128, 0, s>>>(probs, pairs, num_pairs, cdf);
+  return cudaGetLastError();
+}
+
+}  // namespace gcr
 
 extern "C" {
 
@@ -471,6 +518,13 @@ gcr_status gcr_batch_prepare(gcr_context* c, gcr_model_kind kind, int64_t num_pa
   return GCR_OK;
 }
 
+gcr_status gcr_context_set_probabilities(gcr_context* c, const double* d_probabilities) {
+  if (!c) return fail(GCR_INVALID_ARG, "context is NULL");
+  c->probs = d_probabilities;
+  c->pending.valid = false;
+  return GCR_OK;
+}
+
 gcr_status gcr_context_set_pair_times(gcr_context* c, unsigned long long* d_times) {
   if (!c) return fail(GCR_INVALID_ARG, "context is NULL");
   c->pair_times = d_times;
@@ -502,6 +556,12 @@ gcr_status gcr_find_batch(gcr_model_kind kind, int64_t num_pairs, const double* 
   CUDA_TRY(ctx->stats.ensure(sizeof(gcr_stats) * num_pairs));
   cudaStream_t s = 0;
   CUDA_TRY(cudaMemcpyAsync(ctx->corr.p, corr, sizeof(double) * 4 * total, cudaMemcpyHostToDevice, s));
+  ctx->probs = nullptr;
+  if (g_batch_probs) {
+    CUDA_TRY(ctx->probs_stage.ensure(sizeof(double) * (size_t)std::max<int64_t>(total, 1)));
+    CUDA_TRY(cudaMemcpyAsync(ctx->probs_stage.p, g_batch_probs, sizeof(double) * total, cudaMemcpyHostToDevice, s));
+    ctx->probs = (const double*)ctx->probs_stage.p;
+  }
   gcr_status st = gcr_batch_run_device(ctx, kind, num_pairs, (const double*)ctx->corr.p, offsets, K, sizes,
                                        params, seeds, (double*)ctx->models.p, (uint8_t*)ctx->masks.p,
                                        (gcr_stats*)ctx->stats.p, s);
@@ -514,8 +574,8 @@ gcr_status gcr_find_batch(gcr_model_kind kind, int64_t num_pairs, const double* 
 }
 
 static gcr_status find_one(gcr_model_kind kind, const double* corr, int64_t n, const double* K1, const double* K2,
-                           const gcr_image_size* size, const gcr_params* params, double* model_out9,
-                           uint8_t* mask_out, gcr_stats* stats_out) {
+                           const gcr_image_size* size, const double* probabilities, const gcr_params* params,
+                           double* model_out9, uint8_t* mask_out, gcr_stats* stats_out) {
   if (!corr || !size || !params || !model_out9 || !mask_out) return fail(GCR_INVALID_ARG, "NULL argument");
   const int m = kind == GCR_HOMOGRAPHY ? 4 : (kind == GCR_FUNDAMENTAL ? 7 : 5);
   if (n < m) return fail(GCR_TOO_FEW_POINTS, "%lld correspondences, needs >= %d", (long long)n, m);
@@ -528,8 +588,12 @@ static gcr_status find_one(gcr_model_kind kind, const double* corr, int64_t n, c
   }
   gcr_stats st{};
   const uint64_t seed = params->seed;
+  if (params->sampler == GCR_SAMPLER_IMPORTANCE && !probabilities)
+    return fail(GCR_INVALID_ARG, "the importance sampler (3) needs per-correspondence probabilities");
+  g_batch_probs = params->sampler == GCR_SAMPLER_IMPORTANCE ? probabilities : nullptr;
   gcr_status rc = gcr_find_batch(kind, 1, corr, offsets, kind == GCR_ESSENTIAL ? K : nullptr, size, params, &seed,
                                  model_out9, mask_out, &st);
+  g_batch_probs = nullptr;
   if (rc != GCR_OK) return rc;
   if (stats_out) *stats_out = st;
   if (st.status != GCR_OK) {
@@ -542,22 +606,21 @@ static gcr_status find_one(gcr_model_kind kind, const double* corr, int64_t n, c
 gcr_status gcr_find_homography(const double* corr, int64_t n, const gcr_image_size* size, const double* probabilities,
                                const gcr_params* params, double* model_out9, uint8_t* mask_out,
                                gcr_stats* stats_out) {
-  (void)probabilities;
-  return find_one(GCR_HOMOGRAPHY, corr, n, nullptr, nullptr, size, params, model_out9, mask_out, stats_out);
+  return find_one(GCR_HOMOGRAPHY, corr, n, nullptr, nullptr, size, probabilities, params, model_out9, mask_out,
+                  stats_out);
 }
 
 gcr_status gcr_find_fundamental(const double* corr, int64_t n, const gcr_image_size* size,
                                 const double* probabilities, const gcr_params* params, double* model_out9,
                                 uint8_t* mask_out, gcr_stats* stats_out) {
-  (void)probabilities;
-  return find_one(GCR_FUNDAMENTAL, corr, n, nullptr, nullptr, size, params, model_out9, mask_out, stats_out);
+  return find_one(GCR_FUNDAMENTAL, corr, n, nullptr, nullptr, size, probabilities, params, model_out9, mask_out,
+                  stats_out);
 }
 
 gcr_status gcr_find_essential(const double* corr, int64_t n, const double* K1, const double* K2,
                               const gcr_image_size* size, const double* probabilities, const gcr_params* params,
                               double* model_out9, uint8_t* mask_out, gcr_stats* stats_out) {
-  (void)probabilities;
-  return find_one(GCR_ESSENTIAL, corr, n, K1, K2, size, params, model_out9, mask_out, stats_out);
+  return find_one(GCR_ESSENTIAL, corr, n, K1, K2, size, probabilities, params, model_out9, mask_out, stats_out);
 }
 
 gcr_status gcr_run(gcr_model_kind kind, const double* points, const double* pixels, int64_t n,

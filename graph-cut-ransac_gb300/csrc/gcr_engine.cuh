@@ -41,7 +41,7 @@ constexpr int kLoRegion = GCR_BLOCK;    // model slots reserved for local optimi
 
 enum PairStatus { ST_OK = 0, ST_NO_MODEL = 3, ST_TIMEOUT = 5, ST_CAPACITY = 6, ST_UNSUPPORTED = 7 };
 
-enum { SAMPLER_UNIFORM = 0, SAMPLER_PROSAC = 1, SAMPLER_PNAPSAC = 2 };
+enum { SAMPLER_UNIFORM = 0, SAMPLER_PROSAC = 1, SAMPLER_PNAPSAC = 2, SAMPLER_IMPORTANCE = 3 };
 enum { SCORING_MSAC = 0, SCORING_MAGSAC = 1 };
 
 struct EngineParams {
@@ -65,6 +65,8 @@ struct EngineParams {
   // x = 0..36000, and the constants C 2^1.5, Gamma(1.5) - gamma_k, gamma_k,
   // all evaluated on the host
   const double* mag_table;
+  // importance sampler: per-pair cumulative normalised probabilities [total]
+  const double* cdf;
   double mag_c2dof;
   double mag_gamma_diff;
   double mag_gamma_k;
@@ -2174,6 +2176,25 @@ struct Engine {
     } else if (prm.sampler == SAMPLER_UNIFORM) {
       DrawStream ds(pd.seed, prm.stream_main, (uint64_t)(a0 + j));
       ok = unique_set(ds, s, m, 0, (uint32_t)(N - 1));
+    } else if (prm.sampler == SAMPLER_IMPORTANCE) {
+      // ImportanceSampler::sample (samplers/importance_sampler.h:120-133):
+      // m independent multinomial draws (repeats allowed), each a 53-bit
+      // uniform u from two stream words and the first row whose cumulative
+      // probability is not below u
+      DrawStream ds(pd.seed, prm.stream_main, (uint64_t)(a0 + j));
+      const double* cdf = prm.cdf + pd.offset;
+      for (int q = 0; q < m; ++q) {
+        const uint32_t w0 = ds.next_u32(), w1 = ds.next_u32();
+        const double u = ((double)(w0 >> 5) * 67108864.0 + (double)(w1 >> 6)) * (1.0 / 9007199254740992.0);
+        int lo = 0, hi = N - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (cdf[mid] < u) lo = mid + 1;
+          else hi = mid;
+        }
+        s[q] = lo;
+      }
+      ok = true;
     } else {
       // PROSAC (samplers/prosac_sampler.h:51-237): every thread replays the
       // state machine for the whole batch and keeps its own call's draw range.

@@ -37,4 +37,9 @@ struct PairDesc;
 cudaError_t launch_normalise_essential(const double* corr, const double* kinv, const PairDesc* pairs, int num_pairs,
                                        double* out, cudaStream_t stream);
 
+// Cumulative normalised probabilities of the importance sampler, one table per
+// pair laid out like the correspondences.
+cudaError_t launch_importance_cdf(const double* probs, const PairDesc* pairs, int num_pairs, double* cdf,
+                                  cudaStream_t stream);
+
 }  // namespace gcr

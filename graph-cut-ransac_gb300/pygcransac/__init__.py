@@ -73,24 +73,40 @@ def _raise_for(rc, where):
     raise GCRError(rc, f"{where}: {msg}")
 
 
-def _run_one(kind, corr, size, params, K1=None, K2=None, return_stats=False):
+def _probabilities(probabilities, n, sampler):
+    """The importance sampler's weights (sampler 3), else None (the other
+    samplers ignore them, as in the reference)."""
+    if int(sampler) != _abi.GCR_SAMPLER_IMPORTANCE:
+        return None
+    if probabilities is None:
+        raise ValueError("the importance sampler (3) needs per-correspondence probabilities")
+    p = np.ascontiguousarray(probabilities, dtype=np.float64).reshape(-1)
+    if p.shape[0] != n:
+        raise ValueError(f"probabilities has {p.shape[0]} entries for {n} correspondences")
+    if not np.all(np.isfinite(p)) or np.any(p < 0) or not p.sum() > 0:
+        raise ValueError("probabilities must be finite, non-negative and not all zero")
+    return p
+
+
+def _run_one(kind, corr, size, params, K1=None, K2=None, return_stats=False, probabilities=None):
     import ctypes
     lib = _abi.load()
     n = corr.shape[0]
+    prob = _probabilities(probabilities, n, params.sampler)
     model = np.zeros(9)
     mask = np.zeros(n, np.uint8)
     st = _abi.Stats()
     sz = _abi.ImageSize(*[int(v) for v in size])
     if kind == _abi.GCR_HOMOGRAPHY:
-        rc = lib.gcr_find_homography(_abi.ptr(corr), n, ctypes.byref(sz), None, ctypes.byref(params),
+        rc = lib.gcr_find_homography(_abi.ptr(corr), n, ctypes.byref(sz), _abi.ptr(prob), ctypes.byref(params),
                                      _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
     elif kind == _abi.GCR_FUNDAMENTAL:
-        rc = lib.gcr_find_fundamental(_abi.ptr(corr), n, ctypes.byref(sz), None, ctypes.byref(params),
+        rc = lib.gcr_find_fundamental(_abi.ptr(corr), n, ctypes.byref(sz), _abi.ptr(prob), ctypes.byref(params),
                                       _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
     else:
         K1 = np.ascontiguousarray(K1, np.float64).reshape(9)
         K2 = np.ascontiguousarray(K2, np.float64).reshape(9)
-        rc = lib.gcr_find_essential(_abi.ptr(corr), n, _abi.ptr(K1), _abi.ptr(K2), ctypes.byref(sz), None,
+        rc = lib.gcr_find_essential(_abi.ptr(corr), n, _abi.ptr(K1), _abi.ptr(K2), ctypes.byref(sz), _abi.ptr(prob),
                                     ctypes.byref(params), _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
     _raise_for(rc, ["findHomography", "findFundamentalMatrix", "findEssentialMatrix"][kind])
     maskb = mask.astype(bool)
@@ -110,7 +126,8 @@ def findHomography(correspondences, h1, w1, h2, w2, probabilities=None, threshol
     p = _params(_abi.GCR_HOMOGRAPHY, threshold, conf, spatial_coherence_weight, max_iters, min_iters, use_sprt,
                 sampler, neighborhood, neighborhood_size, lo_number, use_space_partitioning, seed,
                 min_inlier_ratio_for_sprt=min_inlier_ratio_for_sprt)
-    return _run_one(_abi.GCR_HOMOGRAPHY, c, (h1, w1, h2, w2), p, return_stats=return_stats)
+    return _run_one(_abi.GCR_HOMOGRAPHY, c, (h1, w1, h2, w2), p, return_stats=return_stats,
+                    probabilities=probabilities)
 
 
 def findFundamentalMatrix(correspondences, h1, w1, h2, w2, probabilities=None, threshold=1.0, conf=0.99,
@@ -124,7 +141,8 @@ def findFundamentalMatrix(correspondences, h1, w1, h2, w2, probabilities=None, t
     p = _params(_abi.GCR_FUNDAMENTAL, threshold, conf, spatial_coherence_weight, max_iters, min_iters, use_sprt,
                 sampler, neighborhood, neighborhood_size, lo_number, False, seed,
                 min_inlier_ratio_for_sprt=min_inlier_ratio_for_sprt)
-    return _run_one(_abi.GCR_FUNDAMENTAL, c, (h1, w1, h2, w2), p, return_stats=return_stats)
+    return _run_one(_abi.GCR_FUNDAMENTAL, c, (h1, w1, h2, w2), p, return_stats=return_stats,
+                    probabilities=probabilities)
 
 
 def findEssentialMatrix(correspondences, K1, K2, h1, w1, h2, w2, probabilities=None, threshold=1.0, conf=0.99,
@@ -138,7 +156,8 @@ def findEssentialMatrix(correspondences, K1, K2, h1, w1, h2, w2, probabilities=N
     p = _params(_abi.GCR_ESSENTIAL, threshold, conf, spatial_coherence_weight, max_iters, min_iters, use_sprt,
                 sampler, neighborhood, neighborhood_size, lo_number, False, seed,
                 min_inlier_ratio_for_sprt=min_inlier_ratio_for_sprt)
-    return _run_one(_abi.GCR_ESSENTIAL, c, (h1, w1, h2, w2), p, K1=K1, K2=K2, return_stats=return_stats)
+    return _run_one(_abi.GCR_ESSENTIAL, c, (h1, w1, h2, w2), p, K1=K1, K2=K2, return_stats=return_stats,
+                    probabilities=probabilities)
 
 
 def find_batch(kind, correspondences, sizes, params, seeds=None, K=None):

@@ -29,6 +29,11 @@ STATUS_NAMES = {
 GCR_SCORING_MSAC = 0
 GCR_SCORING_MAGSAC = 1
 
+GCR_SAMPLER_UNIFORM = 0
+GCR_SAMPLER_PROSAC = 1
+GCR_SAMPLER_PNAPSAC = 2
+GCR_SAMPLER_IMPORTANCE = 3
+
 GCR_HOMOGRAPHY = 0
 GCR_FUNDAMENTAL = 1
 GCR_ESSENTIAL = 2
@@ -102,6 +107,7 @@ _EXPORTS = {
     "gcr_batch_prepare": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int64, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "gcr_batch_launch": (ctypes.c_int, [_P, _P]),
     "gcr_context_set_pair_times": (ctypes.c_int, [_P, _P]),
+    "gcr_context_set_probabilities": (ctypes.c_int, [_P, _P]),
     "gcr_run": (ctypes.c_int, [ctypes.c_int, _P, _P, ctypes.c_int64, _P, ctypes.c_int32, _P, _P, _P, _P, _P]),
     "gcr_learned_param_count": (ctypes.c_int64, []),
     "gcr_learned_feature_width": (ctypes.c_int32, []),

@@ -8,7 +8,8 @@ order, which draws from the most promising correspondences first. The inlier
 mask is mapped back to the caller's order. The reference has no such network:
 its samplers 3 and 4 take externally computed probabilities
 (src/pygcransac/src/bindings.cpp, `probabilities`); this module produces the
-order from the correspondences alone.
+order from the correspondences alone, and `predict` gives probabilities that
+the importance sampler (sampler 3) of the entry points accepts.
 
 The features, forward pass, backward pass, Adam update, ordering and mask
 mapping are the engine's own kernels (csrc/gcr_learned.cu, reached through the

@@ -52,7 +52,7 @@ enum {
   GCR_SAMPLER_UNIFORM = 0,
   GCR_SAMPLER_PROSAC = 1,
   GCR_SAMPLER_PNAPSAC = 2,
-  GCR_SAMPLER_IMPORTANCE = 3,
+  GCR_SAMPLER_IMPORTANCE = 3,     /* needs per-correspondence probabilities */
   GCR_SAMPLER_AR = 4
 };
 
@@ -106,7 +106,7 @@ void gcr_default_params(gcr_model_kind kind, gcr_params* p);
 
 /* Single image pair, host buffers.
  *   corr           n x 4 row-major doubles (x1, y1, x2, y2)
- *   probabilities  n doubles or NULL (read only by samplers 3 and 4)
+ *   probabilities  n doubles or NULL (read only by the importance sampler, 3)
  *   model_out9     3x3 row-major model
  *   mask_out       n bytes, 1 = inlier
  *   stats_out      may be NULL
@@ -197,6 +197,14 @@ gcr_status gcr_batch_prepare(gcr_context* ctx, gcr_model_kind kind, int64_t num_
                              const uint64_t* h_seeds, double* d_models_out, uint8_t* d_masks_out,
                              gcr_stats* d_stats_out);
 gcr_status gcr_batch_launch(gcr_context* ctx, void* stream);
+
+/* Probabilities of the importance sampler (sampler 3,
+ * samplers/importance_sampler.h:51-136) for the batches prepared on `ctx` from
+ * now on: d_probabilities [total] (device, non-negative, laid out like the
+ * correspondences); NULL switches it off. The single-pair entries take the
+ * same weights through their `probabilities` argument (host), which the other
+ * samplers ignore, as in the reference. */
+gcr_status gcr_context_set_probabilities(gcr_context* ctx, const double* d_probabilities);
 
 /* Per-pair timing of the batches prepared on `ctx` from now on (no counterpart
  * in the reference, whose statistics hold one wall-clock time per call):

@@ -47,9 +47,15 @@ static void fill_settings(Settings& s, const gcr_params& p) {
   s.sprt_min_inlier_ratio = p.min_inlier_ratio_for_sprt;
 }
 
+// point probabilities of the importance sampler for the current driver call
+static thread_local const double* g_probs = nullptr;
+
 static std::unique_ptr<Sampler> make_main_sampler(const gcr_params& p, const Mat& pts, size_t m,
                                                   const gcr_image_size& sz, uint64_t seed) {
   switch (p.sampler) {
+    case GCR_SAMPLER_IMPORTANCE:
+      if (!g_probs) return nullptr;
+      return std::make_unique<ImportanceSampler>(seed, STREAM_MAIN, g_probs, (size_t)pts.rows);
     case GCR_SAMPLER_UNIFORM: return std::make_unique<UniformSampler>(seed, STREAM_MAIN);
     case GCR_SAMPLER_PROSAC: return std::make_unique<ProsacSampler>(seed, STREAM_MAIN, m, (size_t)pts.rows);
     case GCR_SAMPLER_PNAPSAC: {
@@ -271,6 +277,20 @@ static int find_essential(const double* corr, int64_t n, const double* K1, const
 using namespace oracle;
 
 extern "C" {
+
+int oracle_find(int kind, const double* corr, int64_t n, const double* K1, const double* K2,
+                const gcr_image_size* sz, const gcr_params* p, uint64_t seed, double* model_out,
+                uint8_t* mask_out, gcr_stats* st);
+
+// oracle_find with the importance sampler's point probabilities
+int oracle_find_prob(int kind, const double* corr, int64_t n, const double* K1, const double* K2,
+                     const double* probabilities, const gcr_image_size* sz, const gcr_params* p, uint64_t seed,
+                     double* model_out, uint8_t* mask_out, gcr_stats* st) {
+  g_probs = probabilities;
+  const int rc = oracle_find(kind, corr, n, K1, K2, sz, p, seed, model_out, mask_out, st);
+  g_probs = nullptr;
+  return rc;
+}
 
 int oracle_find(int kind, const double* corr, int64_t n, const double* K1, const double* K2,
                 const gcr_image_size* sz, const gcr_params* p, uint64_t seed, double* model_out,

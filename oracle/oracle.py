@@ -37,6 +37,8 @@ def load():
         lib.oracle_find.argtypes = [ctypes.c_int, P, ctypes.c_int64, P, P, P, P, ctypes.c_uint64, P, P, P]
         lib.oracle_find_batch.restype = ctypes.c_double
         lib.oracle_find_batch.argtypes = [ctypes.c_int, ctypes.c_int64, P, P, P, P, P, P, P, P, P, ctypes.c_int]
+        lib.oracle_find_prob.restype = ctypes.c_int
+        lib.oracle_find_prob.argtypes = [ctypes.c_int, P, ctypes.c_int64, P, P, P, P, P, ctypes.c_uint64, P, P, P]
         lib.oracle_run.restype = ctypes.c_int
         lib.oracle_run.argtypes = [ctypes.c_int, P, P, ctypes.c_int64, P, ctypes.c_int32, P, P, ctypes.c_uint64, P,
                                    P, P]
@@ -71,8 +73,9 @@ def make_size(h1, w1, h2, w2):
     return _abi.ImageSize(int(h1), int(w1), int(h2), int(w2))
 
 
-def find(kind, corr, size, params, seed=None, K1=None, K2=None):
-    """Runs the oracle on one pair. Returns (status, model 3x3, mask bool[N], stats)."""
+def find(kind, corr, size, params, seed=None, K1=None, K2=None, probabilities=None):
+    """Runs the oracle on one pair. Returns (status, model 3x3, mask bool[N], stats).
+    `probabilities` feed the importance sampler (sampler 3)."""
     lib = load()
     corr = np.ascontiguousarray(corr, dtype=np.float64)
     n = corr.shape[0]
@@ -82,8 +85,13 @@ def find(kind, corr, size, params, seed=None, K1=None, K2=None):
     K1 = None if K1 is None else np.ascontiguousarray(K1, np.float64)
     K2 = None if K2 is None else np.ascontiguousarray(K2, np.float64)
     seed = params.seed if seed is None else seed
-    rc = lib.oracle_find(kind, _p(corr), n, _p(K1), _p(K2), ctypes.byref(size), ctypes.byref(params),
-                         seed, _p(model), _p(mask), ctypes.byref(st))
+    if probabilities is not None:
+        pr = np.ascontiguousarray(probabilities, np.float64)
+        rc = lib.oracle_find_prob(kind, _p(corr), n, _p(K1), _p(K2), _p(pr), ctypes.byref(size),
+                                  ctypes.byref(params), seed, _p(model), _p(mask), ctypes.byref(st))
+    else:
+        rc = lib.oracle_find(kind, _p(corr), n, _p(K1), _p(K2), ctypes.byref(size), ctypes.byref(params),
+                             seed, _p(model), _p(mask), ctypes.byref(st))
     return rc, model.reshape(3, 3), mask.astype(bool), st
 
 

@@ -170,6 +170,41 @@ struct UniformSampler : Sampler {
   }
 };
 
+// samplers/importance_sampler.h:51-136: m independent draws (repeats
+// allowed) from the multinomial of the point probabilities. The table is
+// std::discrete_distribution's (p_i / sum p, running sums in row order, the
+// last entry 1); a draw takes a 53-bit uniform u from stream words 2q and
+// 2q + 1 of the call (in place of mt19937) and the first entry not below u.
+// One call index per sample.
+struct ImportanceSampler : Sampler {
+  uint64_t seed;
+  uint32_t stream;
+  uint64_t calls = 0;
+  std::vector<double> cdf;
+  ImportanceSampler(uint64_t s, uint32_t st, const double* p, size_t n) : seed(s), stream(st), cdf(n) {
+    double sum = 0.0;
+    for (size_t i = 0; i < n; ++i) sum += p[i];
+    double acc = 0.0;
+    for (size_t i = 0; i < n; ++i) {
+      acc += p[i] / sum;
+      cdf[i] = acc;
+    }
+    if (n) cdf[n - 1] = 1.0;
+  }
+  bool sample(const std::vector<size_t>& pool, size_t* subset, size_t k) override {
+    (void)pool;
+    const uint64_t call = calls++;
+    for (size_t q = 0; q < k; ++q) {
+      const uint32_t w0 = draw_u32(seed, stream, call, (uint32_t)(2 * q));
+      const uint32_t w1 = draw_u32(seed, stream, call, (uint32_t)(2 * q + 1));
+      const double u = ((double)(w0 >> 5) * 67108864.0 + (double)(w1 >> 6)) * (1.0 / 9007199254740992.0);
+      size_t i = (size_t)(std::lower_bound(cdf.begin(), cdf.end(), u) - cdf.begin());
+      subset[q] = i < cdf.size() ? i : cdf.size() - 1;
+    }
+    return true;
+  }
+};
+
 // samplers/prosac_sampler.h:51-237
 struct ProsacSampler : Sampler {
   size_t sample_size, point_number, convergence, kth = 1, largest, subset_size;

@@ -62,6 +62,11 @@ def test_python_argument_checks(gcr):
         gcr.findFundamentalMatrix(np.zeros((6, 4)), 480, 640, 480, 640)
     with pytest.raises(ValueError):
         gcr.findEssentialMatrix(np.zeros((4, 4)), np.eye(3), np.eye(3), 480, 640, 480, 640)
+    # the importance sampler needs one finite, non-negative weight per correspondence
+    c = np.random.default_rng(0).uniform(0, 480, (50, 4))
+    for bad in (None, np.ones(49), -np.ones(50), np.zeros(50), np.full(50, np.nan)):
+        with pytest.raises(ValueError):
+            gcr.findHomography(c, 480, 640, 480, 640, bad, sampler=3)
 
 
 def test_default_params_follow_reference(gcr):
