@@ -98,6 +98,7 @@ struct gcr_context {
   int slot_kind = -1, slot_max_n = 0, slot_count = 0;
   bool prepared[3] = {false, false, false};
   unsigned long long* pair_times = nullptr;  // see gcr_context_set_pair_times
+  DevBuf rg_int, rg_dbl, rg_px;              // radius-graph scratch (one region per resident CTA)
   const double* probs = nullptr;             // see gcr_context_set_probabilities
   DevBuf cdf, probs_stage;                   // importance sampler tables, staged probabilities
 };
@@ -122,11 +123,12 @@ gcr_status check_params(gcr_model_kind kind, const gcr_params* p) {
     return fail(GCR_UNSUPPORTED, "scoring %d is not provided (0 MSAC, 1 MAGSAC++)", p->scoring);
   if (p->use_sprt && !(p->min_inlier_ratio_for_sprt > 0 && p->min_inlier_ratio_for_sprt < 1))
     return fail(GCR_INVALID_ARG, "min_inlier_ratio_for_sprt must be in (0, 1) when use_sprt is set");
-  const bool pairwise = p->spatial_coherence_weight > 0;
-  if (p->neighborhood != GCR_NEIGHBORHOOD_GRID && pairwise)
-    return fail(GCR_UNSUPPORTED, "only the grid neighbourhood (0) is provided with a spatial coherence term");
+  if (p->neighborhood != GCR_NEIGHBORHOOD_GRID && p->neighborhood != GCR_NEIGHBORHOOD_FLANN)
+    return fail(GCR_UNSUPPORTED, "neighbourhood %d is not provided (0 grid, 1 radius graph)", p->neighborhood);
   if (p->neighborhood == GCR_NEIGHBORHOOD_GRID && !(p->neighborhood_size >= 1))
     return fail(GCR_INVALID_ARG, "neighborhood_size must be >= 1 for the grid");
+  if (p->neighborhood == GCR_NEIGHBORHOOD_FLANN && !(p->neighborhood_size > 0))
+    return fail(GCR_INVALID_ARG, "neighborhood_size (the radius) must be > 0 for the radius graph");
   (void)kind;
   return GCR_OK;
 }
@@ -145,6 +147,10 @@ const std::vector<double>& magsac_table() {
   }();
   return g;
 }
+
+// radius graph: edges kept per correspondence (beyond this a pair reports
+// GCR_CAPACITY)
+constexpr int64_t kRadiusEdgesPerPoint = 32;
 
 int pow2_at_least(int n) {
   int s = 1;
@@ -264,6 +270,15 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
   }
   const int64_t total = h_offsets[num_pairs] - h_offsets[0];
   if (h_offsets[0] != 0) return fail(GCR_INVALID_ARG, "offsets[0] must be 0");
+  // the radius graph replaces the grid when asked for with a spatial term; the
+  // fundamental / essential drivers build no neighbourhood for a weight at or
+  // below machine epsilon, and the homography driver keeps the grid under space
+  // partitioning (gcransac_python.cpp:1658-1687, 4282-4286)
+  const double eps0 = std::numeric_limits<double>::epsilon();
+  const bool radius = params->neighborhood == GCR_NEIGHBORHOOD_FLANN &&
+                      (kind == GCR_HOMOGRAPHY ? params->spatial_coherence_weight > 0
+                                              : params->spatial_coherence_weight > eps0) &&
+                      !(kind == GCR_HOMOGRAPHY && params->use_space_partitioning);
 
   if (!c->prepared[kind]) {
     CUDA_TRY(ops->prepare());
@@ -308,7 +323,7 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
     d.offset = h_offsets[i];
     d.n = (int32_t)(h_offsets[i + 1] - h_offsets[i]);
     d.n_div = (int32_t)params->neighborhood_size;
-    if (d.n_div < 1) d.n_div = 1;
+    if (d.n_div < 1 || radius) d.n_div = 1;
     const double nd = (double)d.n_div;
     // the homography driver pads the image size by machine epsilon
     // (gcransac_python.cpp:4290-4297), the fundamental/essential ones do not
@@ -408,6 +423,31 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
   prm.sprt_min_ratio = params->min_inlier_ratio_for_sprt;
   prm.epilogue = run_only ? 0 : 1;
   prm.cdf = nullptr;
+  prm.neighborhood = 0;
+  prm.radius2 = 0.0;
+  prm.rg_cap = 0;
+  prm.rg_stride_n = 0;
+  prm.rg_int = nullptr;
+  prm.rg_dbl = nullptr;
+  prm.rg_px = nullptr;
+  if (radius) {
+    // the homography driver with space partitioning keeps the grid
+    // (gcransac_python.cpp:4282-4286); otherwise the radius graph, with room
+    // for kRadiusEdgesPerPoint edges per correspondence
+    const int64_t stride = (int64_t)max_n + 1;
+    const int64_t cap = (int64_t)max_n * kRadiusEdgesPerPoint;
+    if (cap > 0x7fffffffLL) return fail(GCR_CAPACITY, "radius graph capacity");
+    CUDA_TRY(c->rg_int.ensure(sizeof(int) * (size_t)grid * (size_t)(5 * stride + 3 * cap)));
+    CUDA_TRY(c->rg_dbl.ensure(sizeof(double) * (size_t)grid * (size_t)(2 * cap + 3 * stride)));
+    CUDA_TRY(c->rg_px.ensure(sizeof(float4) * (size_t)grid * (size_t)stride));
+    prm.neighborhood = 1;
+    prm.radius2 = params->neighborhood_size * params->neighborhood_size;
+    prm.rg_cap = (int32_t)cap;
+    prm.rg_stride_n = (int32_t)stride;
+    prm.rg_int = (int*)c->rg_int.p;
+    prm.rg_dbl = (double*)c->rg_dbl.p;
+    prm.rg_px = (float4*)c->rg_px.p;
+  }
   if (params->sampler == GCR_SAMPLER_IMPORTANCE) {
     if (!c->probs) return fail(GCR_INVALID_ARG, "the importance sampler (3) needs per-correspondence probabilities");
     CUDA_TRY(c->cdf.ensure(sizeof(double) * (size_t)std::max<int64_t>(total, 1)));

@@ -67,6 +67,17 @@ struct EngineParams {
   const double* mag_table;
   // importance sampler: per-pair cumulative normalised probabilities [total]
   const double* cdf;
+  // neighbourhood: 0 the grid; 1 the radius graph (FlannNeighborhoodGraph's
+  // ball of radius sqrt(radius2) in the four pixel coordinates), whose
+  // per-CTA scratch follows
+  int32_t neighborhood;
+  double radius2;
+  int32_t rg_cap;        // edge capacity per CTA
+  int32_t rg_stride_n;   // max_n + 1
+  int* rg_int;           // per CTA: nb_start, rev_start [rg_stride_n]; nb_idx, rev_edge, edge_src [rg_cap];
+                         // height, queue, mark [rg_stride_n]
+  double* rg_dbl;        // per CTA: cap_f, cap_b [rg_cap]; excess, cap_t, back_s [rg_stride_n]
+  float4* rg_px;         // per CTA: FP32 copy of the pixel coordinates [rg_stride_n]
   double mag_c2dof;
   double mag_gamma_diff;
   double mag_gamma_k;
@@ -956,6 +967,267 @@ struct Engine {
 
   // GCRANSAC::labeling (GCRANSAC.h:912-1021): writes the SINK points in index
   // order into `list` and returns their number.
+  // ------------------------------------------------------------------
+  // Radius neighbourhood (FlannNeighborhoodGraph, neighborhood/
+  // flann_neighborhood_graph.h:100-139, with an exact search): the edges
+  // {i, j}, j > i, whose squared 4-D pixel distance ((a^2 + b^2) + c^2) + d^2,
+  // every operation rounded, is at most radius2. An FP32 pass with a margin
+  // picks the candidates, FP64 decides. Edges are stored by i (ascending j) and
+  // indexed by j for the flow. Returns false when they exceed the capacity.
+  __device__ __forceinline__ int* rg_i(int k) const {
+    return prm.rg_int + (size_t)blockIdx.x * (2 * (size_t)prm.rg_stride_n * 1 + 3 * (size_t)prm.rg_cap +
+                                              3 * (size_t)prm.rg_stride_n) + k;
+  }
+  __device__ __forceinline__ int* rg_nb_start() const { return rg_i(0); }
+  __device__ __forceinline__ int* rg_rev_start() const { return rg_i(prm.rg_stride_n); }
+  __device__ __forceinline__ int* rg_nb_idx() const { return rg_i(2 * prm.rg_stride_n); }
+  __device__ __forceinline__ int* rg_rev_edge() const { return rg_i(2 * prm.rg_stride_n + prm.rg_cap); }
+  __device__ __forceinline__ int* rg_edge_src() const { return rg_i(2 * prm.rg_stride_n + 2 * prm.rg_cap); }
+  __device__ __forceinline__ int* rg_height() const { return rg_i(2 * prm.rg_stride_n + 3 * prm.rg_cap); }
+  __device__ __forceinline__ int* rg_queue() const { return rg_i(3 * prm.rg_stride_n + 3 * prm.rg_cap); }
+  __device__ __forceinline__ int* rg_mark() const { return rg_i(4 * prm.rg_stride_n + 3 * prm.rg_cap); }
+  __device__ __forceinline__ double* rg_d(int k) const {
+    return prm.rg_dbl + (size_t)blockIdx.x * (2 * (size_t)prm.rg_cap + 3 * (size_t)prm.rg_stride_n) + k;
+  }
+  __device__ __forceinline__ double* rg_cap_f() const { return rg_d(0); }
+  __device__ __forceinline__ double* rg_cap_b() const { return rg_d(prm.rg_cap); }
+  __device__ __forceinline__ double* rg_excess() const { return rg_d(2 * prm.rg_cap); }
+  __device__ __forceinline__ double* rg_cap_t() const { return rg_d(2 * prm.rg_cap + prm.rg_stride_n); }
+  __device__ __forceinline__ double* rg_back_s() const { return rg_d(2 * prm.rg_cap + 2 * prm.rg_stride_n); }
+
+  __device__ __forceinline__ bool rg_within(int i, int j, const float4& pi, const float4& pj, float r2f) const {
+    const float a = pj.x - pi.x, b = pj.y - pi.y, c = pj.z - pi.z, d = pj.w - pi.w;
+    const float d2f = a * a + b * b + c * c + d * d;
+    if (d2f > r2f) return false;
+    const double* pix = ws.pix64 + 4 * pd.offset;
+    const double* p = pix + 4 * i;
+    const double* q = pix + 4 * j;
+    const double da = q[0] - p[0], db = q[1] - p[1], dc = q[2] - p[2], dd = q[3] - p[3];
+    const double d2 =
+        __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(da, da), __dmul_rn(db, db)), __dmul_rn(dc, dc)), __dmul_rn(dd, dd));
+    return d2 <= prm.radius2;
+  }
+
+  bool rg_ok = false;  // the radius graph of this pair is built
+  __device__ bool build_radius_graph() {
+    float4* px = prm.rg_px + (size_t)blockIdx.x * prm.rg_stride_n;
+    const double* pix = ws.pix64 + 4 * pd.offset;
+    for (int i = threadIdx.x; i < N; i += GCR_BLOCK) {
+      const double* p = pix + 4 * i;
+      px[i] = make_float4((float)p[0], (float)p[1], (float)p[2], (float)p[3]);
+    }
+    sync();
+    // FP32 candidates: the FP32 distance of a pair within the radius is at
+    // most radius2 (1 + 1e-5) + 1e-3 (coordinates below 1e6 px)
+    const float r2f = (float)(prm.radius2 * (1.0 + 1e-5) + 1e-3);
+    int* start = rg_nb_start();
+    for (int i = threadIdx.x; i < N; i += GCR_BLOCK) {
+      const float4 pi = px[i];
+      int cnt = 0;
+      for (int j = i + 1; j < N; ++j)
+        if (rg_within(i, j, pi, px[j], r2f)) ++cnt;
+      start[i + 1] = cnt;
+    }
+    sync();
+    if (threadIdx.x == 0) {
+      start[0] = 0;
+      long long acc = 0;
+      for (int i = 1; i <= N; ++i) {
+        acc += start[i];
+        start[i] = acc > 0x7fffffff ? 0x7fffffff : (int)acc;
+      }
+      sh.flow_status = acc > prm.rg_cap ? 1 : 0;
+    }
+    sync();
+    if (sh.flow_status) return false;
+    const int E = start[N];
+    int* nb = rg_nb_idx();
+    int* src = rg_edge_src();
+    int* rstart = rg_rev_start();
+    for (int i = threadIdx.x; i <= N; i += GCR_BLOCK) rstart[i] = 0;
+    sync();
+    for (int i = threadIdx.x; i < N; i += GCR_BLOCK) {
+      const float4 pi = px[i];
+      int pos = start[i];
+      for (int j = i + 1; j < N; ++j)
+        if (rg_within(i, j, pi, px[j], r2f)) {
+          nb[pos] = j;
+          src[pos] = i;
+          ++pos;
+          atomicAdd(&rstart[j + 1], 1);
+        }
+    }
+    sync();
+    if (threadIdx.x == 0)
+      for (int i = 1; i <= N; ++i) rstart[i] += rstart[i - 1];
+    sync();
+    // edges by their second endpoint (order within a list does not matter)
+    int* cursor = rg_queue();
+    for (int i = threadIdx.x; i < N; i += GCR_BLOCK) cursor[i] = rstart[i];
+    sync();
+    int* rev = rg_rev_edge();
+    for (int e = threadIdx.x; e < E; e += GCR_BLOCK) rev[atomicAdd(&cursor[nb[e]], 1)] = e;
+    sync();
+    return true;
+  }
+
+  // Labelling on the radius graph (GCRANSAC.h:912-1021): the pairwise terms of
+  // the edges (capacities lambda - A forward, lambda backward, A taken from the
+  // first endpoint's terminal weight, in ascending neighbour order), then a
+  // FIFO push-relabel maximum flow on one thread and the nodes that still
+  // reach the sink through residuals above kResidualEps (the minimal sink
+  // side). Bounded: past 2^24 push / relabel steps the pair reports a timeout.
+  __device__ void radius_mincut() {
+    const int* start = rg_nb_start();
+    const int* nb = rg_nb_idx();
+    double* cf = rg_cap_f();
+    double* cb = rg_cap_b();
+    double* ex = rg_excess();
+    double* ct = rg_cap_t();
+    double* bs = rg_back_s();
+    const double lam = prm.lambda;
+    for (int i = threadIdx.x; i < N; i += GCR_BLOCK) {
+      double tri = slot.tr[i];
+      const double di = slot.dres[i];
+      for (int e = start[i]; e < start[i + 1]; ++e) {
+        const double A = 0.5 * (di + slot.dres[nb[e]]) * lam;
+        tri = tri - A;
+        cf[e] = lam - A;
+        cb[e] = lam;
+      }
+      ex[i] = tri > 0 ? tri : 0.0;   // source arc saturated by the preflow
+      bs[i] = ex[i];                 // residual back to the source
+      ct[i] = tri < 0 ? -tri : 0.0;  // sink arc
+    }
+    sync();
+    if (threadIdx.x == 0) {
+      const int* rstart = rg_rev_start();
+      const int* rev = rg_rev_edge();
+      const int* src = rg_edge_src();
+      int* h = rg_height();
+      int* q = rg_queue();
+      int* inq = rg_mark();
+      const int hs = N + 1;  // height of the source (nodes 0..N-1, sink at 0)
+      int qh = 0, qt = 0, qn = 0;
+      for (int i = 0; i < N; ++i) {
+        h[i] = 0;
+        inq[i] = 0;
+        if (ex[i] > 0) {
+          q[qt] = i;
+          qt = qt + 1 == N ? 0 : qt + 1;
+          ++qn;
+          inq[i] = 1;
+        }
+      }
+      long long steps = 0;
+      bool ok = true;
+      while (qn > 0) {
+        const int u = q[qh];
+        qh = qh + 1 == N ? 0 : qh + 1;
+        --qn;
+        inq[u] = 0;
+        while (ex[u] > 0) {
+          if (++steps > (1ll << 24) || h[u] > 2 * N + 2) {
+            ok = false;
+            break;
+          }
+          int hmin = 0x7fffffff;
+          // to the sink
+          if (ct[u] > 0) {
+            if (h[u] == 1) {
+              const double d = fmin(ex[u], ct[u]);
+              ct[u] -= d;
+              ex[u] -= d;
+              if (ex[u] <= 0) break;
+            } else hmin = min(hmin, 0);
+          }
+          // forward edges u -> v
+          for (int e = start[u]; e < start[u + 1] && ex[u] > 0; ++e) {
+            if (!(cf[e] > 0)) continue;
+            const int v = nb[e];
+            if (h[u] == h[v] + 1) {
+              const double d = fmin(ex[u], cf[e]);
+              cf[e] -= d;
+              cb[e] += d;
+              ex[u] -= d;
+              ex[v] += d;
+              if (!inq[v]) {
+                q[qt] = v;
+                qt = qt + 1 == N ? 0 : qt + 1;
+                ++qn;
+                inq[v] = 1;
+              }
+            } else hmin = min(hmin, h[v]);
+          }
+          // backward edges u -> w (edges (w, u), residual cap_b)
+          for (int k = rstart[u]; k < rstart[u + 1] && ex[u] > 0; ++k) {
+            const int e = rev[k];
+            if (!(cb[e] > 0)) continue;
+            const int w = src[e];
+            if (h[u] == h[w] + 1) {
+              const double d = fmin(ex[u], cb[e]);
+              cb[e] -= d;
+              cf[e] += d;
+              ex[u] -= d;
+              ex[w] += d;
+              if (!inq[w]) {
+                q[qt] = w;
+                qt = qt + 1 == N ? 0 : qt + 1;
+                ++qn;
+                inq[w] = 1;
+              }
+            } else hmin = min(hmin, h[w]);
+          }
+          // back to the source
+          if (ex[u] > 0 && bs[u] > 0) {
+            if (h[u] == hs + 1) {
+              const double d = fmin(ex[u], bs[u]);
+              bs[u] -= d;
+              ex[u] -= d;
+            } else hmin = min(hmin, hs);
+          }
+          if (ex[u] > 0) {
+            if (hmin == 0x7fffffff) {  // no residual arc: cannot happen for a preflow
+              ok = false;
+              break;
+            }
+            h[u] = hmin + 1;
+          }
+        }
+        if (!ok) break;
+      }
+      // minimal sink side: reverse search from the sink over residuals
+      for (int i = 0; i < N; ++i) inq[i] = 0;
+      qt = 0;
+      for (int i = 0; i < N; ++i)
+        if (ct[i] > kResidualEps) {
+          inq[i] = 1;
+          q[qt++] = i;
+        }
+      for (int k = 0; k < qt; ++k) {
+        const int v = q[k];
+        // u -> v residuals: forward edges (u, v) [cap_f], backward of (v, u) [cap_b]
+        for (int r = rstart[v]; r < rstart[v + 1]; ++r) {
+          const int e = rev[r];
+          const int u = src[e];
+          if (!inq[u] && cf[e] > kResidualEps) {
+            inq[u] = 1;
+            q[qt++] = u;
+          }
+        }
+        for (int e = start[v]; e < start[v + 1]; ++e) {
+          const int u = nb[e];
+          if (!inq[u] && cb[e] > kResidualEps) {
+            inq[u] = 1;
+            q[qt++] = u;
+          }
+        }
+      }
+      for (int i = 0; i < N; ++i) slot.flag[i] = (uint8_t)inq[i];
+      if (!ok) sh.flow_status = ST_TIMEOUT;
+    }
+  }
+
   __device__ int labeling(const double* model, int ncells, int* list) {
     const double sq = t2;  // thr^2 * 9 / 4
     const double oml = 1.0 - prm.lambda;
@@ -996,7 +1268,17 @@ struct Engine {
       // unary terms only: SINK iff the sink capacity is positive
       for (int i = threadIdx.x; i < N; i += GCR_BLOCK) slot.flag[i] = (uint8_t)(slot.tr[i] < -kResidualEps ? 1 : 0);
     }
-    for (int c = warp; pairwise && c < ncells; c += GCR_WARPS) {
+    if (pairwise && prm.neighborhood == 1) {
+      if (rg_ok) {
+        radius_mincut();
+      } else {
+        // no graph (capacity exceeded, reported): unary terms only
+        for (int i = threadIdx.x; i < N; i += GCR_BLOCK)
+          slot.flag[i] = (uint8_t)(slot.tr[i] < -kResidualEps ? 1 : 0);
+      }
+      sync();
+    }
+    for (int c = warp; pairwise && prm.neighborhood == 0 && c < ncells; c += GCR_WARPS) {
       const int c0 = slot.cell_start[c], n = slot.cell_start[c + 1] - c0;
       if (c0 < 0 || n < 1 || c0 + n > N) {  // inconsistent cell table: skip, report
         if (lane == 0) atomicMax(&sh.flow_status, ST_CAPACITY);
@@ -2262,6 +2544,10 @@ struct Engine {
     // before the neighbourhood grid that keeps it
     if (prm.sampler == SAMPLER_PNAPSAC) napsac_setup();
     const int ncells = prm.nested ? 0 : build_grid();
+    if (prm.neighborhood == 1 && prm.lambda > 0 && !prm.nested) {
+      rg_ok = build_radius_graph();
+      if (!rg_ok && status == ST_OK) status = ST_CAPACITY;
+    }
     if (prm.use_sprt && !prm.nested) sprt_init();
     if constexpr (Est::KIND == 0)
       if (prm.use_sp && !prm.nested && ncells > 0) sp_init(ncells);

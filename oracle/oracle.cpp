@@ -107,7 +107,11 @@ static int find_homography(const double* corr, int64_t n, const gcr_image_size& 
                            uint64_t seed, double* model_out, uint8_t* mask, gcr_stats* st) {
   if (n < 4) return GCR_TOO_FEW_POINTS;
   const Mat pts{corr, n, 4};
-  auto grid = make_grid(pts, sz, p.neighborhood_size);
+  // the homography driver keeps the grid under space partitioning
+  // (gcransac_python.cpp:4282-4286)
+  auto grid = p.neighborhood == GCR_NEIGHBORHOOD_FLANN && !p.use_space_partitioning
+                  ? std::make_unique<Grid>(Grid::radius_graph(pts, p.neighborhood_size))
+                  : make_grid(pts, sz, p.neighborhood_size);
   HomographyEstimator est;
   Model model{};
   std::vector<size_t> inl;
@@ -137,9 +141,13 @@ static int find_fundamental(const double* corr, int64_t n, const gcr_image_size&
   const Mat pts{corr, n, 4};
   std::unique_ptr<Grid> grid;
   if (p.spatial_coherence_weight > std::numeric_limits<double>::epsilon()) {
-    const size_t nd = (size_t)p.neighborhood_size;
-    const double cs[4] = {sz.w1 / (double)nd, sz.h1 / (double)nd, sz.w2 / (double)nd, sz.h2 / (double)nd};
-    grid = std::make_unique<Grid>(pts, cs, nd);
+    if (p.neighborhood == GCR_NEIGHBORHOOD_FLANN) {
+      grid = std::make_unique<Grid>(Grid::radius_graph(pts, p.neighborhood_size));
+    } else {
+      const size_t nd = (size_t)p.neighborhood_size;
+      const double cs[4] = {sz.w1 / (double)nd, sz.h1 / (double)nd, sz.w2 / (double)nd, sz.h2 / (double)nd};
+      grid = std::make_unique<Grid>(pts, cs, nd);
+    }
   }
   FundamentalEstimator est;
   est.seed = seed;
@@ -223,9 +231,13 @@ static int find_essential(const double* corr, int64_t n, const double* K1, const
   const double thr = p.threshold / normalizer;
   std::unique_ptr<Grid> grid;
   if (p.spatial_coherence_weight > std::numeric_limits<double>::epsilon()) {
-    const size_t nd = (size_t)p.neighborhood_size;
-    const double cs[4] = {sz.w1 / (double)nd, sz.h1 / (double)nd, sz.w2 / (double)nd, sz.h2 / (double)nd};
-    grid = std::make_unique<Grid>(pix, cs, nd);
+    if (p.neighborhood == GCR_NEIGHBORHOOD_FLANN) {
+      grid = std::make_unique<Grid>(Grid::radius_graph(pix, p.neighborhood_size));
+    } else {
+      const size_t nd = (size_t)p.neighborhood_size;
+      const double cs[4] = {sz.w1 / (double)nd, sz.h1 / (double)nd, sz.w2 / (double)nd, sz.h2 / (double)nd};
+      grid = std::make_unique<Grid>(pix, cs, nd);
+    }
   }
   EssentialEstimator est;
   Model model{};
@@ -358,6 +370,13 @@ int oracle_run(int kind, const double* points, const double* pixels, int64_t n, 
   else std::memset(model_out, 0, 9 * sizeof(double));
   s->status = rc;
   return rc;
+}
+
+// Neighbour counts of the radius graph (Grid::radius_graph) of n points.
+void oracle_radius_counts(const double* corr, int64_t n, double radius, int64_t* counts) {
+  const Mat pts{corr, n, 4};
+  const Grid g = Grid::radius_graph(pts, radius);
+  for (int64_t i = 0; i < n; ++i) counts[i] = (int64_t)g.neighbors((size_t)i).size();
 }
 
 // Pair-parallel batch over `threads` host threads (one pair per thread at a

@@ -39,6 +39,8 @@ def load():
         lib.oracle_find_batch.argtypes = [ctypes.c_int, ctypes.c_int64, P, P, P, P, P, P, P, P, P, ctypes.c_int]
         lib.oracle_find_prob.restype = ctypes.c_int
         lib.oracle_find_prob.argtypes = [ctypes.c_int, P, ctypes.c_int64, P, P, P, P, P, ctypes.c_uint64, P, P, P]
+        lib.oracle_radius_counts.restype = None
+        lib.oracle_radius_counts.argtypes = [P, ctypes.c_int64, ctypes.c_double, P]
         lib.oracle_run.restype = ctypes.c_int
         lib.oracle_run.argtypes = [ctypes.c_int, P, P, ctypes.c_int64, P, ctypes.c_int32, P, P, ctypes.c_uint64, P,
                                    P, P]
@@ -93,6 +95,15 @@ def find(kind, corr, size, params, seed=None, K1=None, K2=None, probabilities=No
         rc = lib.oracle_find(kind, _p(corr), n, _p(K1), _p(K2), ctypes.byref(size), ctypes.byref(params),
                              seed, _p(model), _p(mask), ctypes.byref(st))
     return rc, model.reshape(3, 3), mask.astype(bool), st
+
+
+def radius_counts(corr, radius):
+    """Neighbour count of every point in the radius graph."""
+    lib = load()
+    corr = np.ascontiguousarray(corr, np.float64)
+    out = np.zeros(len(corr), np.int64)
+    lib.oracle_radius_counts(_p(corr), len(corr), float(radius), _p(out))
+    return out
 
 
 def run(kind, points, pixels, cell_sizes, divisions, size, params, seed=0):

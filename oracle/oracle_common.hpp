@@ -305,8 +305,36 @@ struct Grid {
     for (size_t c = 0; c < cells.size(); ++c) key_order[c] = c;
     std::sort(key_order.begin(), key_order.end(), [&](size_t a, size_t b) { return keys[a] < keys[b]; });
   }
-  const std::vector<size_t>& neighbors(size_t i) const { return cells[cell_of_point[i]]; }
-  bool empty() const { return cells.empty(); }
+  const std::vector<size_t>& neighbors(size_t i) const {
+    return radius_mode ? radius_nb[i] : cells[cell_of_point[i]];
+  }
+  bool empty() const { return cells.empty() && radius_nb.empty(); }
+
+  // FlannNeighborhoodGraph (neighborhood/flann_neighborhood_graph.h:100-139)
+  // with an exact ball search in place of the approximate k-d tree: the
+  // neighbours of i are the j != i whose squared 4-D distance
+  // ((a^2 + b^2) + c^2) + d^2 is at most radius^2, in index order.
+  bool radius_mode = false;
+  std::vector<std::vector<size_t>> radius_nb;
+  static Grid radius_graph(const Mat& pts, double radius) {
+    Grid g;
+    g.radius_mode = true;
+    g.radius_nb.assign(pts.rows, {});
+    const double r2 = radius * radius;
+    for (int64_t i = 0; i < pts.rows; ++i) {
+      const double* p = pts.row(i);
+      for (int64_t j = 0; j < pts.rows; ++j) {
+        if (j == i) continue;
+        const double* q = pts.row(j);
+        const double a = q[0] - p[0], b = q[1] - p[1], c = q[2] - p[2], d = q[3] - p[3];
+        const double d2 = ((a * a + b * b) + c * c) + d * d;
+        if (d2 <= r2) g.radius_nb[i].push_back((size_t)j);
+      }
+      g.neighbor_number += g.radius_nb[i].size();
+    }
+    g.neighbor_number /= 2;
+    return g;
+  }
 };
 
 // samplers/progressive_napsac_sampler.h:50-326 with layers {16, 8, 4, 2} and

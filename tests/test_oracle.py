@@ -132,3 +132,17 @@ def test_labeling_is_minimal_sink_min_cut(oracle, seed):
             minimisers.append(L)
     inter = np.all(np.array(minimisers), axis=0)
     assert np.array_equal(lab, inter.astype(bool))
+
+
+def test_radius_graph_is_the_exact_ball(oracle):
+    """The oracle's radius neighbourhood (the FlannNeighborhoodGraph restated
+    with an exact search) against a NumPy ball search with the same operation
+    order: same neighbour counts, symmetric, no self-loops."""
+    from pygcransac import synthetic as S
+    pr = S.two_view_pair(77, n=400, inlier_ratio=0.5)
+    c = pr["corr"]
+    d = c[None, :, :] - c[:, None, :]
+    d2 = ((d[..., 0] * d[..., 0] + d[..., 1] * d[..., 1]) + d[..., 2] * d[..., 2]) + d[..., 3] * d[..., 3]
+    ref = (d2 <= 20.0 * 20.0) & ~np.eye(len(c), dtype=bool)
+    assert np.array_equal(ref, ref.T) and ref.sum() > 0
+    np.testing.assert_array_equal(oracle.radius_counts(c, 20.0), ref.sum(1))
