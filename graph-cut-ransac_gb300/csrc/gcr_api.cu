@@ -99,6 +99,7 @@ struct gcr_context {
   bool prepared[3] = {false, false, false};
   unsigned long long* pair_times = nullptr;  // see gcr_context_set_pair_times
   DevBuf rg_int, rg_dbl, rg_px;              // radius-graph scratch (one region per resident CTA)
+  DevBuf ar_p, ar_i, ar_ab, ar_cnt;          // AR sampler heaps and per-point state (per resident CTA)
   const double* probs = nullptr;             // see gcr_context_set_probabilities
   DevBuf cdf, probs_stage;                   // importance sampler tables, staged probabilities
 };
@@ -114,11 +115,11 @@ gcr_status check_params(gcr_model_kind kind, const gcr_params* p) {
   if (p->max_iterations < 0 || p->min_iterations < 0) return fail(GCR_INVALID_ARG, "negative iteration limit");
   if (p->lo_number < 0 || p->lo_number > GCR_BLOCK)
     return fail(GCR_UNSUPPORTED, "lo_number must be in [0, %d]", GCR_BLOCK);
-  if (p->sampler != GCR_SAMPLER_UNIFORM && p->sampler != GCR_SAMPLER_PROSAC && p->sampler != GCR_SAMPLER_PNAPSAC &&
-      p->sampler != GCR_SAMPLER_IMPORTANCE)
+  if (p->sampler < GCR_SAMPLER_UNIFORM || p->sampler > GCR_SAMPLER_AR)
     return fail(GCR_UNSUPPORTED,
-                "sampler %d is not provided by the device engine (0 uniform, 1 PROSAC, 2 P-NAPSAC, 3 importance)",
-                p->sampler);
+                "sampler %d is not provided (0 uniform, 1 PROSAC, 2 P-NAPSAC, 3 importance, 4 AR)", p->sampler);
+  if (p->sampler == GCR_SAMPLER_AR && !(p->sampler_variance > 0))
+    return fail(GCR_INVALID_ARG, "the AR sampler needs sampler_variance > 0");
   if (p->scoring != GCR_SCORING_MSAC && p->scoring != GCR_SCORING_MAGSAC)
     return fail(GCR_UNSUPPORTED, "scoring %d is not provided (0 MSAC, 1 MAGSAC++)", p->scoring);
   if (p->use_sprt && !(p->min_inlier_ratio_for_sprt > 0 && p->min_inlier_ratio_for_sprt < 1))
@@ -175,6 +176,7 @@ void gcr_default_params(gcr_model_kind kind, gcr_params* p) {
   p->use_sprt = 1;
   p->seed = 0;
   p->min_inlier_ratio_for_sprt = kind == GCR_ESSENTIAL ? 0.01 : 0.00001;
+  p->sampler_variance = 0.1;
   switch (kind) {
     case GCR_HOMOGRAPHY:  // bindings.cpp:1158-1178
       p->spatial_coherence_weight = 0.975;
@@ -448,6 +450,34 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
     prm.rg_dbl = (double*)c->rg_dbl.p;
     prm.rg_px = (float4*)c->rg_px.p;
   }
+  prm.probs = nullptr;
+  prm.sampler_variance = params->sampler_variance;
+  prm.ar_p = nullptr;
+  prm.ar_i = nullptr;
+  prm.ar_ab = nullptr;
+  prm.ar_cnt = nullptr;
+  prm.ar_cap = 0;
+  prm.ar_stride_n = 0;
+  if (params->sampler == GCR_SAMPLER_AR) {
+    if (!c->probs) return fail(GCR_INVALID_ARG, "the AR sampler (4) needs per-correspondence probabilities");
+    // a heap entry per point plus m per sampler call, for the iteration limit
+    // (at most 2^20) and two batches of calls beyond it
+    const int64_t calls = std::min<int64_t>(params->max_iterations, 1 << 20) + 2 * GCR_BLOCK;
+    const int64_t cap = (int64_t)max_n + (int64_t)ops->sample_size * calls;
+    if (cap > 0x7fffffffLL) return fail(GCR_CAPACITY, "AR sampler heap");
+    const int64_t stride = (int64_t)max_n + 1;
+    CUDA_TRY(c->ar_p.ensure(sizeof(double) * (size_t)grid * (size_t)cap));
+    CUDA_TRY(c->ar_i.ensure(sizeof(int) * (size_t)grid * (size_t)cap));
+    CUDA_TRY(c->ar_ab.ensure(sizeof(double) * 2 * (size_t)grid * (size_t)stride));
+    CUDA_TRY(c->ar_cnt.ensure(sizeof(int) * (size_t)grid * (size_t)stride));
+    prm.probs = c->probs;
+    prm.ar_p = (double*)c->ar_p.p;
+    prm.ar_i = (int*)c->ar_i.p;
+    prm.ar_ab = (double*)c->ar_ab.p;
+    prm.ar_cnt = (int*)c->ar_cnt.p;
+    prm.ar_cap = (int32_t)cap;
+    prm.ar_stride_n = (int32_t)stride;
+  }
   if (params->sampler == GCR_SAMPLER_IMPORTANCE) {
     if (!c->probs) return fail(GCR_INVALID_ARG, "the importance sampler (3) needs per-correspondence probabilities");
     CUDA_TRY(c->cdf.ensure(sizeof(double) * (size_t)std::max<int64_t>(total, 1)));
@@ -628,9 +658,10 @@ static gcr_status find_one(gcr_model_kind kind, const double* corr, int64_t n, c
   }
   gcr_stats st{};
   const uint64_t seed = params->seed;
-  if (params->sampler == GCR_SAMPLER_IMPORTANCE && !probabilities)
-    return fail(GCR_INVALID_ARG, "the importance sampler (3) needs per-correspondence probabilities");
-  g_batch_probs = params->sampler == GCR_SAMPLER_IMPORTANCE ? probabilities : nullptr;
+  const bool weighted = params->sampler == GCR_SAMPLER_IMPORTANCE || params->sampler == GCR_SAMPLER_AR;
+  if (weighted && !probabilities)
+    return fail(GCR_INVALID_ARG, "samplers 3 and 4 need per-correspondence probabilities");
+  g_batch_probs = weighted ? probabilities : nullptr;
   gcr_status rc = gcr_find_batch(kind, 1, corr, offsets, kind == GCR_ESSENTIAL ? K : nullptr, size, params, &seed,
                                  model_out9, mask_out, &st);
   g_batch_probs = nullptr;

@@ -41,7 +41,8 @@ constexpr int kLoRegion = GCR_BLOCK;    // model slots reserved for local optimi
 
 enum PairStatus { ST_OK = 0, ST_NO_MODEL = 3, ST_TIMEOUT = 5, ST_CAPACITY = 6, ST_UNSUPPORTED = 7 };
 
-enum { SAMPLER_UNIFORM = 0, SAMPLER_PROSAC = 1, SAMPLER_PNAPSAC = 2, SAMPLER_IMPORTANCE = 3 };
+enum { SAMPLER_UNIFORM = 0, SAMPLER_PROSAC = 1, SAMPLER_PNAPSAC = 2, SAMPLER_IMPORTANCE = 3, SAMPLER_AR = 4 };
+constexpr uint32_t kStreamAr = 6;  // jitter draws of the AR sampler
 enum { SCORING_MSAC = 0, SCORING_MAGSAC = 1 };
 
 struct EngineParams {
@@ -78,6 +79,17 @@ struct EngineParams {
                          // height, queue, mark [rg_stride_n]
   double* rg_dbl;        // per CTA: cap_f, cap_b [rg_cap]; excess, cap_t, back_s [rg_stride_n]
   float4* rg_px;         // per CTA: FP32 copy of the pixel coordinates [rg_stride_n]
+  // AR sampler: the caller's probabilities [total], the estimator variance
+  // and per CTA a max-heap of (probability, point) [ar_cap] plus the
+  // per-point a, b [2 * ar_stride_n] and appearance counts [ar_stride_n]
+  const double* probs;
+  double sampler_variance;
+  double* ar_p;
+  int* ar_i;
+  double* ar_ab;
+  int* ar_cnt;
+  int32_t ar_cap;
+  int32_t ar_stride_n;
   double mag_c2dof;
   double mag_gamma_diff;
   double mag_gamma_k;
@@ -216,6 +228,8 @@ struct Shared {
   int lm_flag;
   int fit_ok;
   int flow_status;
+  int ar_size;                    // entries in the AR sampler's heap
+  int ar_overflow;
 };
 
 // GCRANSAC::getIterationNumber (GCRANSAC.h:156-172)
@@ -2437,6 +2451,122 @@ struct Engine {
   // One batch of main-sampler calls [a0, a0 + GCR_BLOCK): thread j draws call
   // a0 + j, checks the sample, runs the minimal solver and writes its models
   // compacted into the slot table; sh.n_ok[j] / sh.mbase[j] describe them.
+  // ------------------------------------------------------------------
+  // AR sampler (samplers/adaptive_reordering_sampler.h:46-166). The driver
+  // divides the probabilities by their maximum (gcransac_python.cpp:1731-1736);
+  // each point enters a max-heap of (probability, index) with the estimator's
+  // a, b; a sample pops the m largest entries (stale ones included) and the
+  // update that follows every sample (GCRANSAC.h:304-335, 474-478) pushes each
+  // sampled point back with |a / (a + b + appearances)| + jitter, clamped to
+  // [0, 0.999]. The jitter, rand() in the reference, is
+  // 0.01 u / (2^32 - 1) - 0.005 with u word q of the call's kStreamAr stream.
+  // Probabilities that are not positive start at 1e-12 (the reference divides
+  // by zero there). The state depends only on the calls, so thread 0 replays
+  // a batch of calls ahead.
+  __device__ __forceinline__ bool ar_greater(double pa, int ia, double pb, int ib) const {
+    return pa > pb || (pa == pb && ia > ib);
+  }
+  __device__ void ar_sift_down(double* hp, int* hi, int n, int k) const {
+    for (int it = 0; it < 64; ++it) {
+      const int l = 2 * k + 1, r = l + 1;
+      int best = k;
+      if (l < n && ar_greater(hp[l], hi[l], hp[best], hi[best])) best = l;
+      if (r < n && ar_greater(hp[r], hi[r], hp[best], hi[best])) best = r;
+      if (best == k) return;
+      const double tp = hp[k]; hp[k] = hp[best]; hp[best] = tp;
+      const int ti = hi[k]; hi[k] = hi[best]; hi[best] = ti;
+      k = best;
+    }
+  }
+  __device__ void ar_push(double* hp, int* hi, int& n, double p, int i) const {
+    int k = n++;
+    hp[k] = p;
+    hi[k] = i;
+    for (int it = 0; it < 64 && k > 0; ++it) {
+      const int parent = (k - 1) >> 1;
+      if (!ar_greater(hp[k], hi[k], hp[parent], hi[parent])) break;
+      const double tp = hp[k]; hp[k] = hp[parent]; hp[parent] = tp;
+      const int ti = hi[k]; hi[k] = hi[parent]; hi[parent] = ti;
+      k = parent;
+    }
+  }
+  __device__ double* ar_hp() const { return prm.ar_p + (size_t)blockIdx.x * prm.ar_cap; }
+  __device__ int* ar_hi() const { return prm.ar_i + (size_t)blockIdx.x * prm.ar_cap; }
+  __device__ double* ar_a() const { return prm.ar_ab + (size_t)blockIdx.x * 2 * prm.ar_stride_n; }
+  __device__ double* ar_b() const { return ar_a() + prm.ar_stride_n; }
+  __device__ int* ar_c() const { return prm.ar_cnt + (size_t)blockIdx.x * prm.ar_stride_n; }
+
+  __device__ void ar_init() {
+    if (threadIdx.x == 0) {
+      const double* pr = prm.probs + pd.offset;
+      double mx = 0.0;
+      for (int i = 0; i < N; ++i) mx = pr[i] > mx ? pr[i] : mx;
+      double* hp = ar_hp();
+      int* hi = ar_hi();
+      double* A = ar_a();
+      double* B = ar_b();
+      int* C = ar_c();
+      const double var = prm.sampler_variance;
+      for (int i = 0; i < N; ++i) {
+        double p = pr[i] / mx;
+        if (p == 1.0) p -= 1e-6;
+        if (!(p > 1e-12)) p = 1e-12;
+        const double omp = 1.0 - p;
+        const double a = __dsub_rn(__ddiv_rn(__dmul_rn(__dmul_rn(p, p), omp), var), p);
+        A[i] = a;
+        B[i] = __ddiv_rn(__dmul_rn(a, omp), p);
+        C[i] = 0;
+        hp[i] = p;
+        hi[i] = i;
+      }
+      for (int k = N / 2 - 1; k >= 0; --k) ar_sift_down(hp, hi, N, k);
+      sh.ar_size = N;
+      sh.ar_overflow = 0;
+    }
+    sync();
+  }
+
+  // thread 0: the samples of calls a0 .. a0 + GCR_BLOCK - 1 into slot.bsamples
+  __device__ void ar_batch(long long a0) {
+    if (threadIdx.x == 0) {
+      double* hp = ar_hp();
+      int* hi = ar_hi();
+      const double* A = ar_a();
+      const double* B = ar_b();
+      int* C = ar_c();
+      int n = sh.ar_size;
+      for (int c = 0; c < GCR_BLOCK; ++c) {
+        if (sh.ar_overflow || n + m > prm.ar_cap || n < m) {
+          sh.ar_overflow = 1;
+          sh.s_cnt[c] = 0;
+          continue;
+        }
+        int* smp = slot.bsamples + c * Est::M;
+        for (int q = 0; q < m; ++q) {
+          smp[q] = hi[0];
+          --n;
+          hp[0] = hp[n];
+          hi[0] = hi[n];
+          ar_sift_down(hp, hi, n, 0);
+        }
+        DrawStream ds(pd.seed, kStreamAr, (uint64_t)(a0 + c));
+        for (int q = 0; q < m; ++q) {
+          const int idx = smp[q];
+          const int k = ++C[idx];
+          const double r = fabs(__ddiv_rn(A[idx], __dadd_rn(__dadd_rn(A[idx], B[idx]), (double)k)));
+          const double u = (double)ds.next_u32();
+          double v = __dsub_rn(__dadd_rn(r, __dmul_rn(0.01, __ddiv_rn(u, 4294967295.0))), 0.005);
+          v = v < 0.999 ? v : 0.999;
+          v = v > 0.0 ? v : 0.0;
+          ar_push(hp, hi, n, v, idx);
+        }
+        sh.s_cnt[c] = 1;
+      }
+      sh.ar_size = n;
+    }
+    sync();
+  }
+
   __device__ int generate_batch(long long a0, long long& p_kth, long long& p_subset, long long& p_hi,
                                 double& p_Tn, long long& p_Tprime) {
     const int j = threadIdx.x;
@@ -2458,6 +2588,13 @@ struct Engine {
     } else if (prm.sampler == SAMPLER_UNIFORM) {
       DrawStream ds(pd.seed, prm.stream_main, (uint64_t)(a0 + j));
       ok = unique_set(ds, s, m, 0, (uint32_t)(N - 1));
+    } else if (prm.sampler == SAMPLER_AR) {
+      ar_batch(a0);
+      if (sh.ar_overflow && status == ST_OK) status = ST_CAPACITY;
+      ok = sh.s_cnt[j] != 0;
+#pragma unroll
+      for (int q = 0; q < Est::M; ++q) s[q] = slot.bsamples[j * Est::M + q];
+      sync();
     } else if (prm.sampler == SAMPLER_IMPORTANCE) {
       // ImportanceSampler::sample (samplers/importance_sampler.h:120-133):
       // m independent multinomial draws (repeats allowed), each a 53-bit
@@ -2543,6 +2680,7 @@ struct Engine {
     // the sampler's layer grids use cell_start as scratch, so they come
     // before the neighbourhood grid that keeps it
     if (prm.sampler == SAMPLER_PNAPSAC) napsac_setup();
+    if (prm.sampler == SAMPLER_AR) ar_init();
     const int ncells = prm.nested ? 0 : build_grid();
     if (prm.neighborhood == 1 && prm.lambda > 0 && !prm.nested) {
       rg_ok = build_radius_graph();

@@ -34,7 +34,7 @@ def default_params(kind):
 
 def _params(kind, threshold, conf, spatial_coherence_weight, max_iters, min_iters, use_sprt, sampler,
             neighborhood, neighborhood_size, lo_number, use_space_partitioning=False, seed=0, scoring=0,
-            min_inlier_ratio_for_sprt=0.00001):
+            min_inlier_ratio_for_sprt=0.00001, sampler_variance=0.1):
     p = _abi.Params()
     p.threshold = float(threshold)
     p.confidence = float(conf)
@@ -50,6 +50,7 @@ def _params(kind, threshold, conf, spatial_coherence_weight, max_iters, min_iter
     p.use_space_partitioning = int(bool(use_space_partitioning))
     p.seed = int(seed)
     p.min_inlier_ratio_for_sprt = float(min_inlier_ratio_for_sprt)
+    p.sampler_variance = float(sampler_variance)
     return p
 
 
@@ -74,12 +75,12 @@ def _raise_for(rc, where):
 
 
 def _probabilities(probabilities, n, sampler):
-    """The importance sampler's weights (sampler 3), else None (the other
-    samplers ignore them, as in the reference)."""
-    if int(sampler) != _abi.GCR_SAMPLER_IMPORTANCE:
+    """The weights of the importance and AR samplers (3, 4), else None (the
+    other samplers ignore them, as in the reference)."""
+    if int(sampler) not in (_abi.GCR_SAMPLER_IMPORTANCE, _abi.GCR_SAMPLER_AR):
         return None
     if probabilities is None:
-        raise ValueError("the importance sampler (3) needs per-correspondence probabilities")
+        raise ValueError("samplers 3 and 4 need per-correspondence probabilities")
     p = np.ascontiguousarray(probabilities, dtype=np.float64).reshape(-1)
     if p.shape[0] != n:
         raise ValueError(f"probabilities has {p.shape[0]} entries for {n} correspondences")
@@ -125,7 +126,7 @@ def findHomography(correspondences, h1, w1, h2, w2, probabilities=None, threshol
     c = _check_corr(correspondences, 4, "homography")
     p = _params(_abi.GCR_HOMOGRAPHY, threshold, conf, spatial_coherence_weight, max_iters, min_iters, use_sprt,
                 sampler, neighborhood, neighborhood_size, lo_number, use_space_partitioning, seed,
-                min_inlier_ratio_for_sprt=min_inlier_ratio_for_sprt)
+                min_inlier_ratio_for_sprt=min_inlier_ratio_for_sprt, sampler_variance=sampler_variance)
     return _run_one(_abi.GCR_HOMOGRAPHY, c, (h1, w1, h2, w2), p, return_stats=return_stats,
                     probabilities=probabilities)
 
@@ -140,7 +141,7 @@ def findFundamentalMatrix(correspondences, h1, w1, h2, w2, probabilities=None, t
     c = _check_corr(correspondences, 7, "fundamental")
     p = _params(_abi.GCR_FUNDAMENTAL, threshold, conf, spatial_coherence_weight, max_iters, min_iters, use_sprt,
                 sampler, neighborhood, neighborhood_size, lo_number, False, seed,
-                min_inlier_ratio_for_sprt=min_inlier_ratio_for_sprt)
+                min_inlier_ratio_for_sprt=min_inlier_ratio_for_sprt, sampler_variance=sampler_variance)
     return _run_one(_abi.GCR_FUNDAMENTAL, c, (h1, w1, h2, w2), p, return_stats=return_stats,
                     probabilities=probabilities)
 
@@ -155,7 +156,7 @@ def findEssentialMatrix(correspondences, K1, K2, h1, w1, h2, w2, probabilities=N
     c = _check_corr(correspondences, 5, "essential")
     p = _params(_abi.GCR_ESSENTIAL, threshold, conf, spatial_coherence_weight, max_iters, min_iters, use_sprt,
                 sampler, neighborhood, neighborhood_size, lo_number, False, seed,
-                min_inlier_ratio_for_sprt=min_inlier_ratio_for_sprt)
+                min_inlier_ratio_for_sprt=min_inlier_ratio_for_sprt, sampler_variance=sampler_variance)
     return _run_one(_abi.GCR_ESSENTIAL, c, (h1, w1, h2, w2), p, K1=K1, K2=K2, return_stats=return_stats,
                     probabilities=probabilities)
 

@@ -33,6 +33,7 @@ GCR_SAMPLER_UNIFORM = 0
 GCR_SAMPLER_PROSAC = 1
 GCR_SAMPLER_PNAPSAC = 2
 GCR_SAMPLER_IMPORTANCE = 3
+GCR_SAMPLER_AR = 4
 
 GCR_HOMOGRAPHY = 0
 GCR_FUNDAMENTAL = 1
@@ -64,6 +65,7 @@ class Params(ctypes.Structure):
         ("use_space_partitioning", ctypes.c_int32),
         ("seed", ctypes.c_uint64),
         ("min_inlier_ratio_for_sprt", ctypes.c_double),
+        ("sampler_variance", ctypes.c_double),
     ]
 
 
@@ -89,7 +91,7 @@ STATS_DTYPE = np.dtype([
 SIZE_DTYPE = np.dtype([("h1", np.int32), ("w1", np.int32), ("h2", np.int32), ("w2", np.int32)])
 
 assert ctypes.sizeof(Stats) == STATS_DTYPE.itemsize == 56
-assert ctypes.sizeof(Params) == 88
+assert ctypes.sizeof(Params) == 96
 
 _P = ctypes.c_void_p
 _EXPORTS = {

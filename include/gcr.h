@@ -53,7 +53,7 @@ enum {
   GCR_SAMPLER_PROSAC = 1,
   GCR_SAMPLER_PNAPSAC = 2,
   GCR_SAMPLER_IMPORTANCE = 3,     /* needs per-correspondence probabilities */
-  GCR_SAMPLER_AR = 4
+  GCR_SAMPLER_AR = 4               /* needs per-correspondence probabilities */
 };
 
 enum { GCR_NEIGHBORHOOD_GRID = 0, GCR_NEIGHBORHOOD_FLANN = 1 };
@@ -78,6 +78,7 @@ typedef struct gcr_params {
   int32_t use_space_partitioning;  /* homographies: space-partitioning pre-selection of models */
   uint64_t seed;                   /* seed of the counter-based sampler streams */
   double min_inlier_ratio_for_sprt; /* SPRT's initial inlier-ratio guess (epsilon) */
+  double sampler_variance;         /* AR sampler (4): variance of the inlier-probability estimator */
 } gcr_params;
 
 typedef struct gcr_stats {
@@ -106,7 +107,7 @@ void gcr_default_params(gcr_model_kind kind, gcr_params* p);
 
 /* Single image pair, host buffers.
  *   corr           n x 4 row-major doubles (x1, y1, x2, y2)
- *   probabilities  n doubles or NULL (read only by the importance sampler, 3)
+ *   probabilities  n doubles or NULL (read only by the importance and AR samplers, 3 and 4)
  *   model_out9     3x3 row-major model
  *   mask_out       n bytes, 1 = inlier
  *   stats_out      may be NULL

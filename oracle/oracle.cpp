@@ -56,6 +56,9 @@ static std::unique_ptr<Sampler> make_main_sampler(const gcr_params& p, const Mat
     case GCR_SAMPLER_IMPORTANCE:
       if (!g_probs) return nullptr;
       return std::make_unique<ImportanceSampler>(seed, STREAM_MAIN, g_probs, (size_t)pts.rows);
+    case GCR_SAMPLER_AR:
+      if (!g_probs) return nullptr;
+      return std::make_unique<ARSampler>(seed, STREAM_AR, g_probs, (size_t)pts.rows, p.sampler_variance);
     case GCR_SAMPLER_UNIFORM: return std::make_unique<UniformSampler>(seed, STREAM_MAIN);
     case GCR_SAMPLER_PROSAC: return std::make_unique<ProsacSampler>(seed, STREAM_MAIN, m, (size_t)pts.rows);
     case GCR_SAMPLER_PNAPSAC: {

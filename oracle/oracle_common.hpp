@@ -16,6 +16,7 @@
 #include <limits>
 #include <memory>
 #include <unordered_map>
+#include <queue>
 #include <vector>
 
 namespace oracle {
@@ -103,6 +104,7 @@ enum : uint32_t {
   STREAM_NAPSAC_LOCAL = 3,
   STREAM_NAPSAC_CENTER = 4,
   STREAM_NAPSAC_GLOBAL = 5,
+  STREAM_AR = 6,
 };
 
 // Restates utils::UniformRandomGenerator (uniform_random_generator.h:44-124):
@@ -200,6 +202,56 @@ struct ImportanceSampler : Sampler {
       const double u = ((double)(w0 >> 5) * 67108864.0 + (double)(w1 >> 6)) * (1.0 / 9007199254740992.0);
       size_t i = (size_t)(std::lower_bound(cdf.begin(), cdf.end(), u) - cdf.begin());
       subset[q] = i < cdf.size() ? i : cdf.size() - 1;
+    }
+    return true;
+  }
+};
+
+// samplers/adaptive_reordering_sampler.h:46-166 with the driver's division
+// by the largest probability (gcransac_python.cpp:1731-1736): a max-heap of
+// (probability, index); a sample pops the m largest entries and the update
+// that follows every sample pushes each sampled point back with
+// |a / (a + b + appearances)| + jitter clamped to [0, 0.999]. The jitter,
+// rand() in the reference, is 0.01 u / (2^32 - 1) - 0.005 with u draw q of
+// the call on stream STREAM_AR; probabilities that are not positive start at
+// 1e-12 (the reference divides by zero there). std::priority_queue has the
+// reference's tie order (larger index first among equal probabilities).
+struct ARSampler : Sampler {
+  uint64_t seed;
+  uint32_t stream;
+  uint64_t calls = 0;
+  std::vector<double> a, b;
+  std::vector<size_t> cnt;
+  std::priority_queue<std::pair<double, size_t>> q;
+  ARSampler(uint64_t s, uint32_t st, const double* probs, size_t n, double variance)
+      : seed(s), stream(st), a(n), b(n), cnt(n, 0) {
+    double mx = 0.0;
+    for (size_t i = 0; i < n; ++i) mx = probs[i] > mx ? probs[i] : mx;
+    for (size_t i = 0; i < n; ++i) {
+      double p = probs[i] / mx;
+      if (p == 1.0) p -= 1e-6;
+      if (!(p > 1e-12)) p = 1e-12;
+      a[i] = p * p * (1.0 - p) / variance - p;
+      b[i] = a[i] * (1.0 - p) / p;
+      q.emplace(p, i);
+    }
+  }
+  bool sample(const std::vector<size_t>& pool, size_t* subset, size_t k) override {
+    (void)pool;
+    const uint64_t call = calls++;
+    for (size_t i = 0; i < k; ++i) {
+      subset[i] = q.top().second;
+      q.pop();
+    }
+    for (size_t i = 0; i < k; ++i) {
+      const size_t idx = subset[i];
+      ++cnt[idx];
+      const double r = std::fabs(a[idx] / (a[idx] + b[idx] + (double)cnt[idx]));
+      const double u = (double)draw_u32(seed, stream, call, (uint32_t)i);
+      double v = r + 0.01 * (u / 4294967295.0) - 0.005;
+      v = v < 0.999 ? v : 0.999;
+      v = v > 0.0 ? v : 0.0;
+      q.emplace(v, idx);
     }
     return true;
   }

@@ -1,9 +1,10 @@
-"""GPU parity of the importance sampler (sampler 3, samplers/importance_sampler.h)
-for the three model kinds: the device tabulates the same cumulative
-probabilities as the oracle and draws the same multinomial indices from the
-shared Philox streams, so masks, counts and models agree. Covers the
-single-pair entry points (host probabilities) and the device batch entry
-(gcr_context_set_probabilities)."""
+"""GPU parity of the samplers fed by per-correspondence probabilities for the
+three model kinds: the importance sampler (3, samplers/importance_sampler.h:
+the same cumulative table as the oracle and the same multinomial draws from
+the shared Philox streams) and the AR sampler (4, adaptive_reordering_sampler.h:
+the same heap replay and jitter draws), so masks, counts and models agree.
+Covers the single-pair entry points (host probabilities) and the device batch
+entry (gcr_context_set_probabilities)."""
 import ctypes
 
 import numpy as np
@@ -41,18 +42,20 @@ def make(name, seed):
     return S.two_view_pair(seed, n=1500, inlier_ratio=0.3)
 
 
+@pytest.mark.parametrize("sampler", [3, 4])
 @pytest.mark.parametrize("case", range(3))
-def test_importance_sampler_single_pair(oracle, gcr, case):
+def test_weighted_sampler_single_pair(oracle, gcr, case, sampler):
     name, kind, thr, lam, grid = CASES[case]
     pr = make(name, 300 + case)
     prob = weights(pr, case)
-    p = gcr._params(kind, thr, 0.99, lam, 2000, 50, False, 3, 0, grid, 50, False, 11)
+    p = gcr._params(kind, thr, 0.99, lam, 2000, 50, False, sampler, 0, grid, 50, False, 11, sampler_variance=0.1)
     K = pr.get("K")
     rc, M, mask, st = oracle.find(kind, pr["corr"], oracle.make_size(*pr["size"]), p, seed=11, K1=K, K2=K,
                                   probabilities=prob)
     h1, w1, h2, w2 = pr["size"]
     kw = dict(probabilities=prob, threshold=thr, spatial_coherence_weight=lam, max_iters=2000, min_iters=50,
-              use_sprt=False, sampler=3, neighborhood=0, neighborhood_size=grid, seed=11, return_stats=True)
+              use_sprt=False, sampler=sampler, neighborhood=0, neighborhood_size=grid, seed=11, return_stats=True,
+              sampler_variance=0.1)
     if kind == _abi.GCR_HOMOGRAPHY:
         model, m, sd = gcr.findHomography(pr["corr"], h1, w1, h2, w2, use_space_partitioning=False, **kw)
     elif kind == _abi.GCR_FUNDAMENTAL:
@@ -66,7 +69,8 @@ def test_importance_sampler_single_pair(oracle, gcr, case):
         assert rel_err(model, M) < MODEL_TOL
 
 
-def test_importance_sampler_device_batch(oracle):
+@pytest.mark.parametrize("sampler", [3, 4])
+def test_weighted_sampler_device_batch(oracle, sampler):
     import torch
     lib = _abi.load()
     prs = [S.two_view_pair(400 + k, n=n, inlier_ratio=0.35) for k, n in enumerate((900, 1700))]
@@ -77,7 +81,8 @@ def test_importance_sampler_device_batch(oracle):
     for i, pr in enumerate(prs):
         sizes[i] = tuple(pr["size"])
     p = _abi.Params(threshold=0.75, confidence=0.99, spatial_coherence_weight=0.975, neighborhood_size=8,
-                    max_iterations=1500, min_iterations=50, sampler=3, neighborhood=0, lo_number=50, seed=0)
+                    max_iterations=1500, min_iterations=50, sampler=sampler, neighborhood=0, lo_number=50, seed=0,
+                    sampler_variance=0.1)
     seeds = np.array([5, 6], np.uint64)
     d_corr = torch.from_numpy(corr).cuda()
     d_prob = torch.from_numpy(np.concatenate(probs)).cuda()
