@@ -29,6 +29,7 @@
  *   sampler::ProsacSampler           samplers/prosac_sampler.h:51-237
  *   sampler::ProgressiveNapsacSampler<4>  samplers/progressive_napsac_sampler.h:50-326
  *   neighborhood::GridNeighborhoodGraph<4> neighborhood/grid_neighborhood_graph.h:132-301
+ *   neighborhood::FlannNeighborhoodGraph   neighborhood/flann_neighborhood_graph.h:100-139 (exact ball)
  *   MSACScoringFunction, MAGSACScoringFunction  scoring_function.h:137-348
  *   preemption::EmptyPreemptiveVerfication, SPRTPreemptiveVerfication
  *                                    preemption/preemption_empty.h, preemption_sprt.h:50-380
@@ -224,6 +225,19 @@ class GridNeighborhoodGraph {
   size_t cell_number_along_all_axes;
 };
 
+// The radius graph (flann_neighborhood_graph.h:100-139) as an exact ball
+// search of radius matching_radius_ in the four pixel coordinates.
+class FlannNeighborhoodGraph {
+ public:
+  FlannNeighborhoodGraph(const MatView* container_, double matching_radius_)
+      : container(container_), matching_radius(matching_radius_) {
+    if (!(matching_radius_ > 0)) throw std::invalid_argument("the neighbourhood radius must be positive");
+  }
+  const std::string getName() const { return "FLANN neighborhood (radius)"; }
+  const MatView* container;
+  double matching_radius;
+};
+
 }  // namespace neighborhood
 
 template <class _ModelEstimator>
@@ -291,8 +305,9 @@ template <class _ModelEstimator, class _NeighborhoodGraph,
           class _PreemptiveModelVerification = preemption::EmptyPreemptiveVerfication<_ModelEstimator>,
           class _FastInlierSelector = inlier_selector::EmptyInlierSelector<_ModelEstimator, _NeighborhoodGraph>>
 class GCRANSAC {
-  static_assert(std::is_same<_NeighborhoodGraph, neighborhood::GridNeighborhoodGraph<4>>::value,
-                "the device engine provides the grid neighbourhood graph");
+  static constexpr bool kRadius = std::is_same<_NeighborhoodGraph, neighborhood::FlannNeighborhoodGraph>::value;
+  static_assert(std::is_same<_NeighborhoodGraph, neighborhood::GridNeighborhoodGraph<4>>::value || kRadius,
+                "the device engine provides the grid and the radius neighbourhood graphs");
 
  public:
   utils::Settings settings;
@@ -320,27 +335,45 @@ class GCRANSAC {
     p.threshold = settings.threshold;
     p.confidence = settings.confidence;
     p.spatial_coherence_weight = settings.spatial_coherence_weight;
-    p.neighborhood_size = (double)neighborhood_graph_->cell_number_along_all_axes;
+    double cells_[4] = {1.0, 1.0, 1.0, 1.0};
+    int32_t divisions_ = 1;
+    if constexpr (kRadius) {
+      p.neighborhood = GCR_NEIGHBORHOOD_FLANN;
+      p.neighborhood_size = neighborhood_graph_->matching_radius;
+    } else {
+      p.neighborhood = GCR_NEIGHBORHOOD_GRID;
+      p.neighborhood_size = (double)neighborhood_graph_->cell_number_along_all_axes;
+      for (int q = 0; q < 4; ++q) cells_[q] = neighborhood_graph_->cell_sizes[q];
+      divisions_ = (int32_t)neighborhood_graph_->cell_number_along_all_axes;
+    }
     p.max_iterations = settings.max_iteration_number > (size_t)std::numeric_limits<int64_t>::max()
                            ? std::numeric_limits<int64_t>::max()
                            : (int64_t)settings.max_iteration_number;
     p.min_iterations = (int64_t)settings.min_iteration_number;
     p.sampler = main_sampler_->deviceSamplerId();
-    p.neighborhood = GCR_NEIGHBORHOOD_GRID;
     p.lo_number = (int32_t)settings.max_local_optimization_number;
     p.scoring = _ScoringFunction::device_scoring;
     p.use_sprt = _PreemptiveModelVerification::device_sprt ? 1 : 0;
     p.min_inlier_ratio_for_sprt = preemptive_verification_.minimum_inlier_ratio();
     p.use_space_partitioning = _FastInlierSelector::device_space_partitioning ? 1 : 0;
     p.seed = seed;
-    const std::vector<double>& cs = neighborhood_graph_->cell_sizes;
-    const double div = (double)neighborhood_graph_->cell_number_along_all_axes;
-    // image extents: P-NAPSAC's sizes when given, else the grid's span
+    // image extents: P-NAPSAC's sizes when given, else the grid's span or the
+    // points' bounding box
     gcr_image_size size;
-    size.w1 = (int32_t)(cs[0] * div);
-    size.h1 = (int32_t)(cs[1] * div);
-    size.w2 = (int32_t)(cs[2] * div);
-    size.h2 = (int32_t)(cs[3] * div);
+    {
+      double mx[4] = {cells_[0] * divisions_, cells_[1] * divisions_, cells_[2] * divisions_,
+                      cells_[3] * divisions_};
+      if constexpr (kRadius) {
+        const MatView& px = *neighborhood_graph_->container;
+        for (int q = 0; q < 4; ++q) mx[q] = 1.0;
+        for (int r = 0; r < px.rows; ++r)
+          for (int q = 0; q < 4; ++q) mx[q] = px.at<double>(r, q) > mx[q] ? px.at<double>(r, q) : mx[q];
+      }
+      size.w1 = (int32_t)mx[0];
+      size.h1 = (int32_t)mx[1];
+      size.w2 = (int32_t)mx[2];
+      size.h2 = (int32_t)mx[3];
+    }
     if (auto* pn = dynamic_cast<const sampler::ProgressiveNapsacSampler<4>*>(main_sampler_)) {
       size.w1 = (int32_t)pn->sizes[0];
       size.h1 = (int32_t)pn->sizes[1];
@@ -352,9 +385,8 @@ class GCRANSAC {
     gcr_stats st{};
     Model out;
     const gcr_status rc =
-        gcr_run(_ModelEstimator::kind, points_.data, neighborhood_graph_->container->data, n, cs.data(),
-                (int32_t)neighborhood_graph_->cell_number_along_all_axes, &size, &p, out.descriptor.v, mask.data(),
-                &st);
+        gcr_run(_ModelEstimator::kind, points_.data, neighborhood_graph_->container->data, n, cells_, divisions_,
+                &size, &p, out.descriptor.v, mask.data(), &st);
     if (rc != GCR_OK && rc != GCR_NO_MODEL) throw std::runtime_error(gcr_last_error_string());
     statistics = utils::RANSACStatistics();
     statistics.main_sampler_name = main_sampler_->getName();

@@ -336,7 +336,8 @@ int oracle_run(int kind, const double* points, const double* pixels, int64_t n, 
   std::memset(s, 0, sizeof(*s));
   const Mat pts{points, n, 4};
   const Mat pix{pixels ? pixels : points, n, 4};
-  const Grid grid(pix, cell_sizes, (size_t)divisions);
+  const Grid grid = p->neighborhood == GCR_NEIGHBORHOOD_FLANN ? Grid::radius_graph(pix, p->neighborhood_size)
+                                                              : Grid(pix, cell_sizes, (size_t)divisions);
   Model model{};
   std::vector<size_t> inl;
   int rc = GCR_INVALID_ARG;

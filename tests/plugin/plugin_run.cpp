@@ -3,7 +3,8 @@
 // library's plugin types, writes the model, the inliers and the statistics.
 //   plugin_run IN OUT
 // IN  (little-endian): int32 kind, sampler, scoring, sprt, space_partitioning,
-//     divisions; int64 n; double threshold, confidence, lambda; int64
+//     divisions (0: the radius graph, radius cell[0]); int64 n; double
+//     threshold, confidence, lambda; int64
 //     max_iterations, min_iterations; int32 lo_number; uint64 seed; double
 //     sprt_ratio, cell[4], sizes[4]; double points[n][4], pixels[n][4],
 //     K1[9], K2[9]
@@ -37,15 +38,26 @@ static void rd(FILE* f, T* v, size_t k = 1) {
   }
 }
 
-template <class Est, template <class> class Scoring, bool SPRT, bool SP>
+template <class Graph>
+Graph make_graph(const Input& in, const MatView* pixels);
+template <>
+neighborhood::GridNeighborhoodGraph<4> make_graph(const Input& in, const MatView* pixels) {
+  return neighborhood::GridNeighborhoodGraph<4>(pixels, {in.cell[0], in.cell[1], in.cell[2], in.cell[3]},
+                                                (size_t)in.divisions);
+}
+template <>
+neighborhood::FlannNeighborhoodGraph make_graph(const Input& in, const MatView* pixels) {
+  return neighborhood::FlannNeighborhoodGraph(pixels, in.cell[0]);
+}
+
+template <class Est, template <class> class Scoring, bool SPRT, bool SP, class Graph>
 static int run_case(const Input& in, const Est& est, FILE* out) {
-  using Graph = neighborhood::GridNeighborhoodGraph<4>;
   using Pre = typename std::conditional<SPRT, preemption::SPRTPreemptiveVerfication<Est>,
                                         preemption::EmptyPreemptiveVerfication<Est>>::type;
   using Sel = typename std::conditional<SP, inlier_selector::SpacePartitioningRANSAC<Est, Graph>,
                                         inlier_selector::EmptyInlierSelector<Est, Graph>>::type;
   const MatView points(in.points.data(), (int)in.n, 4), pixels(in.pixels.data(), (int)in.n, 4);
-  Graph graph(&pixels, {in.cell[0], in.cell[1], in.cell[2], in.cell[3]}, (size_t)in.divisions);
+  Graph graph = make_graph<Graph>(in, &pixels);
   sampler::UniformSampler uniform(&pixels), lo_sampler(&pixels);
   sampler::ProsacSampler prosac(&pixels, Est::sampleSize());
   std::vector<double> sizes(in.sizes, in.sizes + 4);
@@ -90,14 +102,23 @@ static int run_case(const Input& in, const Est& est, FILE* out) {
   return 0;
 }
 
+template <class Est, bool SP, class Graph>
+static int dispatch_graph(const Input& in, const Est& est, FILE* out) {
+  if (in.scoring == GCR_SCORING_MAGSAC) {
+    if (in.sprt) return run_case<Est, MAGSACScoringFunction, true, SP, Graph>(in, est, out);
+    return run_case<Est, MAGSACScoringFunction, false, SP, Graph>(in, est, out);
+  }
+  if (in.sprt) return run_case<Est, MSACScoringFunction, true, SP, Graph>(in, est, out);
+  return run_case<Est, MSACScoringFunction, false, SP, Graph>(in, est, out);
+}
+
 template <class Est, bool SP>
 static int dispatch(const Input& in, const Est& est, FILE* out) {
-  if (in.scoring == GCR_SCORING_MAGSAC) {
-    if (in.sprt) return run_case<Est, MAGSACScoringFunction, true, SP>(in, est, out);
-    return run_case<Est, MAGSACScoringFunction, false, SP>(in, est, out);
+  if (in.divisions == 0) {
+    if constexpr (SP) return 2;  // space partitioning needs the grid
+    else return dispatch_graph<Est, false, neighborhood::FlannNeighborhoodGraph>(in, est, out);
   }
-  if (in.sprt) return run_case<Est, MSACScoringFunction, true, SP>(in, est, out);
-  return run_case<Est, MSACScoringFunction, false, SP>(in, est, out);
+  return dispatch_graph<Est, SP, neighborhood::GridNeighborhoodGraph<4>>(in, est, out);
 }
 
 int main(int argc, char** argv) {

@@ -90,11 +90,16 @@ def cases():
     out.append(("E normalised points, pixel grid, MAGSAC++", _abi.GCR_ESSENTIAL, nrm, c,
                 dict(fcfg, scoring=1, lam=0.1, thr=0.75 / 800.0, seed=7), K))
     out.append(("E SPRT", _abi.GCR_ESSENTIAL, nrm, c, dict(fcfg, sprt=1, lam=0.1, thr=0.75 / 800.0, seed=8), K))
+    # the radius graph (FlannNeighborhoodGraph): divisions 0, radius in cell[0]
+    out.append(("F radius graph", _abi.GCR_FUNDAMENTAL, pf["corr"], pf["corr"],
+                dict(fcfg, div=0, cell=[20.0, 1.0, 1.0, 1.0], seed=9), None))
+    out.append(("E radius graph", _abi.GCR_ESSENTIAL, nrm, c,
+                dict(fcfg, div=0, cell=[20.0, 1.0, 1.0, 1.0], lam=0.1, thr=0.75 / 800.0, seed=10), K))
     return out
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("idx", range(6))
+@pytest.mark.parametrize("idx", range(8))
 def test_plugin_run_matches_oracle_run(tmp_path, oracle, idx):
     name, kind, pts, pix, cfg, K = cases()[idx]
     exe = compile_driver(str(tmp_path))
@@ -103,13 +108,15 @@ def test_plugin_run_matches_oracle_run(tmp_path, oracle, idx):
     r = subprocess.run([exe, fin, fout], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     has, model, counts, score, inl = read_output(fout)
+    radius = cfg["div"] == 0
     p = _abi.Params(threshold=cfg["thr"], confidence=0.99, spatial_coherence_weight=cfg["lam"],
-                    neighborhood_size=cfg["div"], max_iterations=cfg["max_it"], min_iterations=cfg["min_it"],
-                    sampler=cfg["sampler"], neighborhood=0, lo_number=50, seed=cfg["seed"], scoring=cfg["scoring"],
+                    neighborhood_size=cfg["cell"][0] if radius else cfg["div"], max_iterations=cfg["max_it"],
+                    min_iterations=cfg["min_it"], sampler=cfg["sampler"], neighborhood=1 if radius else 0,
+                    lo_number=50, seed=cfg["seed"], scoring=cfg["scoring"],
                     use_sprt=cfg["sprt"], use_space_partitioning=cfg["sp"],
                     min_inlier_ratio_for_sprt=cfg.get("ratio", 0.01))
     z = cfg["sizes"]
-    rc, M, mask, st = oracle.run(kind, pts, pix, cfg["cell"], cfg["div"], oracle.make_size(int(z[1]), int(z[0]),
+    rc, M, mask, st = oracle.run(kind, pts, pix, cfg["cell"], max(cfg["div"], 1), oracle.make_size(int(z[1]), int(z[0]),
                                                                                             int(z[3]), int(z[2])),
                                  p, seed=cfg["seed"])
     assert has == (rc == 0), name
