@@ -8,8 +8,11 @@ learned-proposal batched form: each step replays two CUDA graphs, the proposal
 (one persistent PROSAC launch with a 50-iteration budget, plus the mask
 mapping); the plain form (uniform sampler, the reference's 10000-iteration
 budget, one persistent launch) is timed on the same pairs and reported under
-`plain`, with both median model errors. The other workloads (`homography`,
-`fundamental`, `essential`) time one persistent engine launch per step.
+`plain`, with both median model errors. `serving` is the mixed H / F / E
+batch (4096 pairs, 2k-40k correspondences, 5-60 % inliers; one launch per
+kind on three streams) with per-pair latency percentiles. The other workloads
+(`homography`, `fundamental`, `essential`) time one persistent engine launch
+per step.
 Correspondences are resident in HBM for `value` (CUDA events on the launching
 stream, L2 flushed between steps by a 256 MiB write); `e2e` is the same metric
 through the public API with host buffers, host<->device copies included.
@@ -69,7 +72,7 @@ WORKLOADS = {
     # 5-60 %, 16^4 grid (cells stay within the flow solver's 256 points), the
     # learned proposal for every kind; MSAC; plain form: uniform sampler, 10000
     # iterations; learned form: PROSAC on the learned order, 50 iterations
-    "serving": dict(kind=None, n=(2000, 40000), ratio=(0.05, 0.60), sampler=0, grid=16, pairs=1536, learned_iters=50,
+    "serving": dict(kind=None, n=(2000, 40000), ratio=(0.05, 0.60), sampler=0, grid=16, pairs=4096, learned_iters=50,
                     threshold=None, lam=None),
 }
 

@@ -78,3 +78,49 @@ def test_graph_replay_essential():
                     max_iterations=500, min_iterations=50, sampler=0, neighborhood=0, lo_number=20, seed=0,
                     scoring=_abi.GCR_SCORING_MAGSAC)
     run_kind(_abi.GCR_ESSENTIAL, pairs, p, K=K)
+
+
+def test_pair_times_stamp_every_pair():
+    """gcr_context_set_pair_times: every pair of a batch gets a start and an
+    end stamp from the GPU's global timer, end >= start, and the results are
+    those of a run without stamps."""
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    from pygcransac import _abi, synthetic as S
+    lib = _abi.load()
+    prs = [S.homography_pair(60 + k, n=500 + 100 * k) for k in range(5)]
+    corr = np.ascontiguousarray(np.concatenate([p["corr"] for p in prs]))
+    offsets = np.zeros(6, np.int64)
+    offsets[1:] = np.cumsum([len(p["corr"]) for p in prs])
+    sizes = np.zeros(5, _abi.SIZE_DTYPE)
+    for i, p in enumerate(prs):
+        sizes[i] = tuple(p["size"])
+    prm = _abi.Params(threshold=3.0, confidence=0.99, spatial_coherence_weight=0.975, neighborhood_size=4,
+                      max_iterations=1000, min_iterations=50, sampler=0, neighborhood=0, lo_number=50, seed=0)
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    d_corr = torch.from_numpy(corr).cuda()
+    outs = []
+    for stamped in (False, True):
+        d_models = torch.zeros(45, dtype=torch.float64, device="cuda")
+        d_masks = torch.zeros(int(offsets[-1]), dtype=torch.uint8, device="cuda")
+        d_stats = torch.zeros(5 * _abi.STATS_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+        times = torch.zeros(10, dtype=torch.int64, device="cuda")
+        ctx = ctypes.c_void_p()
+        assert lib.gcr_context_create(ctypes.byref(ctx)) == 0
+        try:
+            if stamped:
+                assert lib.gcr_context_set_pair_times(ctx, vp(times)) == 0
+            assert lib.gcr_batch_run_device(ctx, _abi.GCR_HOMOGRAPHY, 5, vp(d_corr), _abi.ptr(offsets), None,
+                                            _abi.ptr(sizes), ctypes.byref(prm), None, vp(d_models), vp(d_masks),
+                                            vp(d_stats), None) == 0, _abi.last_error()
+            torch.cuda.synchronize()
+        finally:
+            lib.gcr_context_destroy(ctx)
+        outs.append((d_models.cpu().numpy(), d_masks.cpu().numpy(), times.cpu().numpy().reshape(5, 2)))
+    (m0, k0, t0), (m1, k1, t1) = outs
+    assert np.array_equal(m0, m1) and np.array_equal(k0, k1)
+    assert np.all(t0 == 0)
+    assert np.all(t1 > 0) and np.all(t1[:, 1] >= t1[:, 0])
