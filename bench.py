@@ -8,11 +8,8 @@ learned-proposal batched form: each step replays two CUDA graphs, the proposal
 (one persistent PROSAC launch with a 50-iteration budget, plus the mask
 mapping); the plain form (uniform sampler, the reference's 10000-iteration
 budget, one persistent launch) is timed on the same pairs and reported under
-`plain`, with both median model errors. `serving` is the mixed H / F / E
-batch (4096 pairs, 2k-40k correspondences, 5-60 % inliers; one launch per
-kind on three streams) with per-pair latency percentiles. The other workloads
-(`homography`, `fundamental`, `essential`) time one persistent engine launch
-per step.
+`plain`, with both median model errors. The other workloads (`homography`,
+`fundamental`, `essential`) time one persistent engine launch per step.
 Correspondences are resident in HBM for `value` (CUDA events on the launching
 stream, L2 flushed between steps by a 256 MiB write); `e2e` is the same metric
 through the public API with host buffers, host<->device copies included.
@@ -20,7 +17,7 @@ through the public API with host buffers, host<->device copies included.
 oracle, plain method) on all host cores instead.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gcr|reference]
-                  [--workload learned|serving|homography|fundamental|essential] [--pairs P]
+                  [--workload learned|homography|fundamental|essential] [--pairs P]
 """
 import argparse
 import ctypes
@@ -67,20 +64,7 @@ WORKLOADS = {
     # with a 50-iteration budget. Same threshold, grid, lambda and LO.
     "learned": dict(kind=_abi.GCR_FUNDAMENTAL, n=4000, ratio=(0.05, 0.10), threshold=0.75, sampler=0, grid=8,
                     lam=0.975, pairs=1216, learned_iters=50),
-    # mixed serving batch: pairs split evenly across H / F / E (pair i has kind
-    # i mod 3), correspondences log-uniform over 2k-40k, inliers uniform over
-    # 5-60 %, 16^4 grid (cells stay within the flow solver's 256 points), the
-    # learned proposal for every kind; MSAC; plain form: uniform sampler, 10000
-    # iterations; learned form: PROSAC on the learned order, 50 iterations
-    "serving": dict(kind=None, n=(2000, 40000), ratio=(0.05, 0.60), sampler=0, grid=16, pairs=4096, learned_iters=50,
-                    threshold=None, lam=None),
 }
-
-SERVING_KINDS = [  # (workload of the generator, kind, threshold, lambda)
-    ("homography", _abi.GCR_HOMOGRAPHY, 3.0, 0.975),
-    ("fundamental", _abi.GCR_FUNDAMENTAL, 0.75, 0.975),
-    ("essential", _abi.GCR_ESSENTIAL, 0.75, 0.1),
-]
 
 CHECKPOINT = os.path.join(ROOT, "graph-cut-ransac_gb300", "pygcransac", "weights", "proposal_fundamental.gcrl")
 
@@ -106,10 +90,7 @@ def build_pairs(workload, pairs, seed0):
     else:
         ns = np.full(pairs, w["n"])
         ratios = np.full(pairs, w["ratio"])
-    if workload == "serving":
-        jobs = [(SERVING_KINDS[i % 3][0], seed0 + i, int(ns[i]), float(ratios[i])) for i in range(pairs)]
-    else:
-        jobs = [(workload, seed0 + i, int(ns[i]), float(ratios[i])) for i in range(pairs)]
+    jobs = [(workload, seed0 + i, int(ns[i]), float(ratios[i])) for i in range(pairs)]
     if pairs >= 256:
         import multiprocessing as mp
         with mp.get_context("spawn").Pool(max(1, min(16, os.cpu_count() or 1))) as pool:
@@ -119,8 +100,6 @@ def build_pairs(workload, pairs, seed0):
     corr = [c for c, _, _ in out]
     sizes = [z for _, z, _ in out]
     gts = [g for _, _, g in out]
-    if workload == "serving":
-        return corr, None, np.array(sizes), gts, None
     Ks = [np.concatenate([g["K"].ravel(), g["K"].ravel()]) for g in gts] if workload == "essential" else []
     offsets = np.zeros(pairs + 1, np.int64)
     offsets[1:] = np.cumsum([len(c) for c in corr])
@@ -473,194 +452,6 @@ def run_learned(args, P, w, cfg, world, rank, local_rank, dist, torch):
         dist.destroy_process_group()
 
 
-def serving_groups(corr_list, sizes, gts):
-    """Per kind: (name, kind, threshold, lambda, pair ids, corr, offsets, sizes, K, gts)."""
-    out = []
-    for k, (name, kind, thr, lam) in enumerate(SERVING_KINDS):
-        ids = np.arange(k, len(corr_list), 3)
-        c = [corr_list[i] for i in ids]
-        off = np.zeros(len(ids) + 1, np.int64)
-        off[1:] = np.cumsum([len(x) for x in c])
-        K = None
-        if kind == _abi.GCR_ESSENTIAL:
-            K = np.ascontiguousarray([np.concatenate([gts[i]["K"].ravel(), gts[i]["K"].ravel()]) for i in ids])
-        out.append((name, kind, thr, lam, ids, np.ascontiguousarray(np.concatenate(c), np.float64), off,
-                    np.array([sizes[i] for i in ids]), K, [gts[i] for i in ids]))
-    return out
-
-
-def serving_params(kind, thr, lam, grid, iters, seed=0):
-    return _abi.Params(threshold=thr, confidence=0.99, spatial_coherence_weight=lam, neighborhood_size=grid,
-                       max_iterations=iters, min_iterations=min(50, iters), sampler=0, neighborhood=0, lo_number=50,
-                       seed=seed, scoring=_abi.GCR_SCORING_MSAC)
-
-
-def serving_errors(name, models, gts):
-    if name == "homography":
-        return [S.homography_error(m / m[2, 2] if abs(m[2, 2]) > 1e-12 else m, g["H_gt"] if isinstance(g, dict)
-                                   else g) for m, g in zip(models, gts)]
-    if name == "fundamental":
-        return [S.fundamental_error(m, g, n=100) for m, g in zip(models, gts)]
-    return [S.essential_error(m, g) for m, g in zip(models, gts)]
-
-
-def run_serving(args, P, w, cfg, world, rank, local_rank, dist, torch):
-    """Mixed H / F / E batch: one engine launch per kind, the three on their
-    own streams; learned form = proposal + PROSAC engine + mask mapping per
-    kind (one CUDA graph each), plain form = uniform-sampler engine launch per
-    kind. Per-pair service times come from the engine's global-timer stamps."""
-    from pygcransac.learned import LearnedBatch, LearnedProposal
-    lib = _abi.load()
-    corr_list, _, sizes, gts, _ = build_pairs("serving", P, 1000003 * rank)
-    groups = serving_groups(corr_list, sizes, gts)
-    net = LearnedProposal.load(CHECKPOINT)
-    cfg.update(network="the fundamental-matrix checkpoint, applied to every kind",
-               kinds={g[0]: dict(pairs=int(len(g[4])), threshold=g[2], spatial_coherence_weight=g[3]) for g in groups},
-               learned_iterations=w["learned_iters"], correspondences="log-uniform 2000-40000",
-               inlier_ratio="uniform 5-60 %")
-    vp = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    main = torch.cuda.current_stream()
-    streams = [torch.cuda.Stream() for _ in groups]
-    plain, learned = [], []
-    for gi, (name, kind, thr, lam, ids, corr, off, sz, K, g) in enumerate(groups):
-        n_pairs, total = len(ids), int(off[-1])
-        d_corr = torch.from_numpy(corr).cuda()
-        times_p = torch.zeros(2 * n_pairs, dtype=torch.int64, device="cuda")
-        times_l = torch.zeros(2 * n_pairs, dtype=torch.int64, device="cuda")
-        ctx = ctypes.c_void_p()
-        assert lib.gcr_context_create(ctypes.byref(ctx)) == 0
-        assert lib.gcr_context_set_pair_times(ctx, vp(times_p)) == 0
-        pm = torch.zeros(n_pairs * 9, dtype=torch.float64, device="cuda")
-        pk = torch.zeros(total, dtype=torch.uint8, device="cuda")
-        ps = torch.zeros(n_pairs * _abi.STATS_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
-        pp = serving_params(kind, thr, lam, w["grid"], 10000)
-        seeds = np.arange(n_pairs, dtype=np.uint64) + np.uint64(gi * 1000003)
-        rc = lib.gcr_batch_prepare(ctx, kind, n_pairs, vp(d_corr), _abi.ptr(off), _abi.ptr(K), _abi.ptr(size_array(sz)),
-                                   ctypes.byref(pp), _abi.ptr(seeds), vp(pm), vp(pk), vp(ps))
-        assert rc == 0, _abi.last_error()
-        gp = torch.cuda.CUDAGraph()
-        with torch.cuda.stream(streams[gi]):
-            with torch.cuda.graph(gp, stream=streams[gi]):
-                assert lib.gcr_batch_launch(ctx, ctypes.c_void_p(streams[gi].cuda_stream)) == 0
-        plain.append(dict(graph=gp, models=pm, stats=ps, times=times_p, ctx=ctx))
-        pl = serving_params(kind, thr, lam, w["grid"], w["learned_iters"])
-        b = LearnedBatch(net, kind, d_corr, off, sz, pl, seeds, K)
-        assert lib.gcr_context_set_pair_times(b.ctx, vp(times_l)) == 0
-        b.prepare()
-        gl = torch.cuda.CUDAGraph()
-        with torch.cuda.stream(streams[gi]):
-            with torch.cuda.graph(gl, stream=streams[gi]):
-                b.launch(streams[gi])
-        learned.append(dict(graph=gl, batch=b, times=times_l, d_corr=d_corr, corr=corr))
-
-    def step(form):
-        start = torch.cuda.Event(enable_timing=True)
-        stop = torch.cuda.Event(enable_timing=True)
-        start.record(main)
-        for s_, f in zip(streams, form):
-            s_.wait_event(start)
-            with torch.cuda.stream(s_):
-                f["graph"].replay()
-        for s_ in streams:
-            e = torch.cuda.Event()
-            e.record(s_)
-            main.wait_event(e)
-        stop.record(main)
-        stop.synchronize()
-        return start.elapsed_time(stop)
-
-    def lat(form):
-        t = np.concatenate([f["times"].cpu().numpy().reshape(-1, 2) for f in form]).astype(np.float64)
-        service = (t[:, 1] - t[:, 0]) / 1e6
-        done = (t[:, 1] - t[:, 0].min()) / 1e6
-        return {"service_ms_p50": float(np.percentile(service, 50)), "service_ms_p99": float(np.percentile(service, 99)),
-                "completion_ms_p50": float(np.percentile(done, 50)), "completion_ms_p99": float(np.percentile(done, 99))}
-
-    for _ in range(args.warmup):
-        step(plain)
-        step(learned)
-    plain_ms = sum(step(plain) for _ in range(args.steps))
-    plain_lat = lat(plain)
-    clocks = ClockSampler(local_rank)
-    torch.cuda.synchronize()
-    clocks.start()
-    flush.fill_(1)
-    learned_ms = 0.0
-    for _ in range(args.steps):
-        flush.fill_(1)
-        learned_ms += step(learned)
-    clk = clocks.stop()
-    learned_lat = lat(learned)
-    value, _ = aggregate_rate(P * args.steps, learned_ms / 1e3, world, dist, "cuda")
-    plain_value, _ = aggregate_rate(P * args.steps, plain_ms / 1e3, world, dist, "cuda")
-    errs_l, errs_p, ok = {}, {}, []
-    for (name, kind, thr, lam, ids, corr, off, sz, K, g), fp, fl in zip(groups, plain, learned):
-        ml, _, stl = fl["batch"].results()
-        mp = fp["models"].cpu().numpy().reshape(-1, 3, 3)
-        errs_l[name] = float(np.median(serving_errors(name, ml, g)))
-        errs_p[name] = float(np.median(serving_errors(name, mp, g)))
-        ok.append(stl["status"] == 0)
-
-    # end to end: pinned host correspondences in, models / masks / stats out
-    pinned = [torch.from_numpy(f["corr"]).pin_memory() for f in learned]
-    outs = [(torch.empty(f["batch"].P * 9, dtype=torch.float64).pin_memory(),
-             torch.empty(f["batch"].total, dtype=torch.uint8).pin_memory(),
-             torch.empty(f["batch"].P * _abi.STATS_DTYPE.itemsize, dtype=torch.uint8).pin_memory()) for f in learned]
-
-    def e2e_step():
-        for s_, f, h, o in zip(streams, learned, pinned, outs):
-            with torch.cuda.stream(s_):
-                f["d_corr"].copy_(h, non_blocking=True)
-                f["batch"].launch(s_)
-                o[0].copy_(f["batch"].d_models, non_blocking=True)
-                o[1].copy_(f["batch"].d_masks, non_blocking=True)
-                o[2].copy_(f["batch"].d_stats, non_blocking=True)
-        torch.cuda.synchronize()
-
-    e2e_step()
-    e2e_t = 0.0
-    for _ in range(args.steps):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        e2e_step()
-        e2e_t += time.perf_counter() - t0
-    e2e_value, _ = aggregate_rate(P * args.steps, e2e_t, world, dist, "cuda")
-    if rank != 0:
-        return
-    line = {
-        "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": learned_ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "fp32 scoring / fp64 solvers / bf16 MLP", "data": "synthetic", "config": cfg,
-        "median_model_error": errs_l, "status_ok_fraction": float(np.mean(np.concatenate(ok))),
-        "latency": learned_lat,
-        "plain": {"value": plain_value, "unit": "pairs/s", "ms_per_step": plain_ms / args.steps,
-                  "median_model_error": errs_p, "latency": plain_lat},
-        "learned_over_plain": value / plain_value,
-        "error_unit": "H: RMS transfer px; F: mean Sampson px; E: max(rotation, translation) deg",
-        "e2e": {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": int(sum(f["corr"].nbytes for f in learned)),
-                "d2h_bytes_per_step": int(sum(o[0].numel() * 8 + o[1].numel() + o[2].numel() for o in outs))},
-        "gpu_launches": int(sum(3 + 1 + 1 for _ in groups) * args.steps),
-        "clocks": clk,
-    }
-    if not args.no_cpu_baseline and world == 1:
-        # the oracle (plain method) per kind on a bounded sample of its pairs
-        rates = []
-        samples = []
-        for name, kind, thr, lam, ids, corr, off, sz, K, g in groups:
-            p_ = serving_params(kind, thr, lam, w["grid"], 10000)
-            v, cores, sample = cpu_baseline_kind(kind, corr, off, sz, p_, K, target_s=6.0)
-            rates.append(v)
-            samples.append(f"{name}: {sample}")
-        line["cpu_baseline"] = {"value": 3.0 / sum(1.0 / r for r in rates), "unit": "pairs/s", "cores": cores,
-                                "kind": "port", "sample": "; ".join(samples) + "; combined as equal thirds"}
-    print(json.dumps(line))
-    for f in plain:
-        lib.gcr_context_destroy(f["ctx"])
-    for f in learned:
-        f["batch"].close()
-
-
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -680,10 +471,6 @@ def main():
     if args.workload == "essential":
         desc = (f"{args.workload}: {P} calibrated pairs/step x {w['n'][0]}-{w['n'][1]} (log-uniform) correspondences, "
                 f"{int(w['ratio'][0]*100)}-{int(w['ratio'][1]*100)}% inliers, MAGSAC++")
-    elif args.workload == "serving":
-        desc = (f"serving: {P} pairs/step split evenly across H / F / E, 2000-40000 (log-uniform) correspondences, "
-                f"5-60% inliers; learned order -> PROSAC ({w['learned_iters']} iterations) vs plain uniform "
-                f"sampler (10000 iterations), one launch per kind on three streams")
     elif args.workload == "learned":
         desc = (f"learned: {P} fundamental-matrix pairs/step x {w['n']} correspondences, "
                 f"{int(w['ratio'][0]*100)}-{int(w['ratio'][1]*100)}% inliers; learned order -> PROSAC "
@@ -698,29 +485,6 @@ def main():
            "l2": "flushed between steps (256 MiB write)",
            "parallelism": f"replicas x{world}"}
 
-    if args.impl == "reference" and args.workload == "serving":
-        if rank != 0:
-            return
-        corr_list, _, sizes, gts, _ = build_pairs("serving", P, 0)
-        vals = []
-        for it in range(args.warmup + args.steps):
-            rates, samples = [], []
-            for name, kind, thr, lam, ids, corr, off, sz, K, g in serving_groups(corr_list, sizes, gts):
-                v, cores, sample = cpu_baseline_kind(kind, corr, off, sz, serving_params(kind, thr, lam, w["grid"], 10000),
-                                                     K, target_s=1.0 if it < args.warmup else 4.0)
-                rates.append(v)
-                samples.append(f"{name}: {sample}")
-            if it >= args.warmup:
-                vals.append(3.0 / sum(1.0 / r for r in rates))
-        v = float(np.median(vals))
-        print(json.dumps({"metric": METRIC, "value": v, "unit": "pairs/s", "n_gpus": args.gpus, "steps": args.steps,
-                          "warmup": args.warmup, "ms_per_step": 1e3 * P / v, "higher_is_better": True,
-                          "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
-                          "impl": "reference",
-                          "cpu_baseline": {"value": v, "unit": "pairs/s", "cores": cores, "kind": "port",
-                                           "sample": "; ".join(samples) + "; combined as equal thirds"},
-                          "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
-        return
     if args.impl == "reference":
         if rank != 0:
             return
@@ -751,8 +515,6 @@ def main():
 
     if args.workload == "learned":
         return run_learned(args, P, w, cfg, world, rank, local_rank, dist, torch)
-    if args.workload == "serving":
-        return run_serving(args, P, w, cfg, world, rank, local_rank, dist, torch)
 
     lib = _abi.load()
     corr, offsets, sizes, gts, K, seeds = replica_shard(args.workload, P, rank)

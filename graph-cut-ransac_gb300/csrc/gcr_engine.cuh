@@ -39,7 +39,14 @@ constexpr double kResidualEps = 1e-12;  // residual capacity treated as saturate
 constexpr int kSmemPoints = GCR_TILE_POINTS;  // correspondences kept resident in shared memory
 constexpr int kLoRegion = GCR_BLOCK;    // model slots reserved for local optimisation
 
-enum PairStatus { ST_OK = 0, ST_NO_MODEL = 3, ST_TIMEOUT = 5, ST_CAPACITY = 6, ST_UNSUPPORTED = 7 };
+enum PairStatus {
+  ST_OK = 0,
+  ST_NO_MODEL = 3,
+  ST_DEVICE_ERROR = 4,  // an internal consistency check failed (a row index outside the pair)
+  ST_TIMEOUT = 5,
+  ST_CAPACITY = 6,
+  ST_UNSUPPORTED = 7
+};
 
 enum { SAMPLER_UNIFORM = 0, SAMPLER_PROSAC = 1, SAMPLER_PNAPSAC = 2, SAMPLER_IMPORTANCE = 3, SAMPLER_AR = 4 };
 constexpr uint32_t kStreamAr = 6;  // jitter draws of the AR sampler
@@ -228,6 +235,7 @@ struct Shared {
   int lm_flag;
   int fit_ok;
   int flow_status;
+  int bad_row;                    // a row index read from a list fell outside the pair
   int ar_size;                    // entries in the AR sampler's heap
   int ar_overflow;
 };
@@ -322,6 +330,22 @@ struct Engine {
 #else
     (void)id; (void)t0; (void)count;
 #endif
+  }
+
+  // Row `idx` of the pair's fitting coordinates, for indices read from lists:
+  // an index outside [0, N) is recorded (the pair then reports
+  // ST_DEVICE_ERROR) and row 0 is read instead of memory beyond the pair.
+  __device__ __forceinline__ const double* row64(int idx) const {
+    if ((unsigned)idx >= (unsigned)N) {
+      sh.bad_row = 1;
+      idx = 0;
+    }
+    return pts64 + 4 * idx;
+  }
+  __device__ __forceinline__ bool row_ok(int idx) const {
+    if ((unsigned)idx < (unsigned)N) return true;
+    sh.bad_row = 1;
+    return false;
   }
 
   // thread 0 copies 9 doubles; everyone waits
@@ -1346,7 +1370,7 @@ struct Engine {
   __device__ void cta_norm(const int* list, int n, HomographyModel::Norm& nm) {
     double s[4] = {0, 0, 0, 0};
     for (int k = threadIdx.x; k < n; k += GCR_BLOCK) {
-      const double* p = pts64 + 4 * list[k];
+      const double* p = row64(list[k]);
       s[0] += p[0]; s[1] += p[1]; s[2] += p[2]; s[3] += p[3];
     }
     nm.ms0 = block_sum(s[0], sh.red_d) / n;
@@ -1355,7 +1379,7 @@ struct Engine {
     nm.md1 = block_sum(s[3], sh.red_d) / n;
     double a = 0, b = 0;
     for (int k = threadIdx.x; k < n; k += GCR_BLOCK) {
-      const double* p = pts64 + 4 * list[k];
+      const double* p = row64(list[k]);
       const double dx1 = nm.ms0 - p[0], dy1 = nm.ms1 - p[1], dx2 = nm.md0 - p[2], dy2 = nm.md1 - p[3];
       a += sqrt(dx1 * dx1 + dy1 * dy1);
       b += sqrt(dx2 * dx2 + dy2 * dy2);
@@ -1394,7 +1418,7 @@ struct Engine {
     double wm[9];
 #pragma unroll
     for (int q = 0; q < 9; ++q) wm[q] = sh.work_model[q];
-    for (int k = threadIdx.x; k < n; k += GCR_BLOCK) H::accumulate(nm, pts64 + 4 * list[k], row_weight(k, weight_mode, wm), acc);
+    for (int k = threadIdx.x; k < n; k += GCR_BLOCK) H::accumulate(nm, row64(list[k]), row_weight(k, weight_mode, wm), acc);
     cta_reduce<H::NACC>(acc, sh.lm_acc);
     if (threadIdx.x == 0) sh.fit_ok = H::solve_normal(nm, sh.lm_acc, sh.fit_model) ? 1 : 0;
     sync();
@@ -1420,7 +1444,7 @@ struct Engine {
     for (int q = 0; q < 9; ++q) G[q] = sh.lm_G[q];
     double c = 0;
     for (int k = threadIdx.x; k < n; k += GCR_BLOCK) {
-      const double* p = pts64 + 4 * slot_list_[k];
+      const double* p = row64(slot_list_[k]);
       const double w = row_weight(k, weight_mode, wm);
       const double l = F::lm_cost_point(G, (p[0] - nm.ms0) * nm.rs, (p[1] - nm.ms1) * nm.rs, (p[2] - nm.md0) * nm.rd,
                                         (p[3] - nm.md1) * nm.rd);
@@ -1446,7 +1470,7 @@ struct Engine {
 #pragma unroll
       for (int q = 0; q < F::NATA; ++q) acc[q] = 0;
       for (int k = threadIdx.x; k < n; k += GCR_BLOCK)
-        F::accumulate_ata(nm, pts64 + 4 * list[k], row_weight(k, weight_mode, wm), acc);
+        F::accumulate_ata(nm, row64(list[k]), row_weight(k, weight_mode, wm), acc);
       cta_reduce<F::NATA>(acc, slot.red + GCR_WARPS * 64);
     }
     if (threadIdx.x == 0) {
@@ -1495,7 +1519,7 @@ struct Engine {
 #pragma unroll
         for (int q = 0; q < F::NLM; ++q) acc[q] = 0;
         for (int k = threadIdx.x; k < n; k += GCR_BLOCK) {
-          const double* p = pts64 + 4 * list[k];
+          const double* p = row64(list[k]);
           F::lm_accumulate_point(G, D, (p[0] - nm.ms0) * nm.rs, (p[1] - nm.ms1) * nm.rs, (p[2] - nm.md0) * nm.rd,
                                  (p[3] - nm.md1) * nm.rd, row_weight(k, weight_mode, wm), n, acc);
         }
@@ -1567,14 +1591,14 @@ struct Engine {
       auto weight = [&](int k) -> double {
         if (weight_mode == 0) return 1.0;
         if (weight_mode == 2) return slot.dres[k];
-        const double r2 = Est::r2_f64(pts64 + 4 * list[k], wm);
+        const double r2 = Est::r2_f64(row64(list[k]), wm);
         const double w = fmax(0.0, 1.0 - r2 / t2);
         return w * w;
       };
       if (n == 5) {
         if (threadIdx.x == 0) {
           double rows[5][9];
-          for (int k = 0; k < 5; ++k) ess::design_row(pts64 + 4 * list[k], weight(k), rows[k]);
+          for (int k = 0; k < 5; ++k) ess::design_row(row64(list[k]), weight(k), rows[k]);
           sh.multi_count = ess::stewenius_five(rows, sh.multi_models);
         }
       } else {
@@ -1583,7 +1607,7 @@ struct Engine {
         for (int q = 0; q < 45; ++q) acc[q] = 0;
         for (int k = threadIdx.x; k < n; k += GCR_BLOCK) {
           double r[9];
-          ess::design_row(pts64 + 4 * list[k], weight(k), r);
+          ess::design_row(row64(list[k]), weight(k), r);
           int q = 0;
 #pragma unroll
           for (int a = 0; a < 9; ++a)
@@ -1731,7 +1755,7 @@ struct Engine {
       double E[9];
       ess::essential_from_pose(Q, E);
       double c = 0;
-      for (int k = threadIdx.x; k < n; k += GCR_BLOCK) c += slot.dres[k] * ess::relpose_loss(E, pts64 + 4 * list[k]);
+      for (int k = threadIdx.x; k < n; k += GCR_BLOCK) c += slot.dres[k] * ess::relpose_loss(E, row64(list[k]));
       return block_sum(c, sh.red_d);
     };
     double lambda = 1e-3;
@@ -1746,7 +1770,7 @@ struct Engine {
 #pragma unroll
         for (int q = 0; q < 20; ++q) acc[q] = 0;
         for (int k = threadIdx.x; k < n; k += GCR_BLOCK)
-          ess::relpose_accumulate(J, pts64 + 4 * list[k], slot.dres[k], n, acc);
+          ess::relpose_accumulate(J, row64(list[k]), slot.dres[k], n, acc);
         cta_reduce<20>(acc, slot.red + GCR_WARPS * 64);
 #pragma unroll
         for (int q = 0; q < 20; ++q) tot[q] = slot.red[GCR_WARPS * 64 + q];
@@ -1927,7 +1951,7 @@ struct Engine {
     const int min_n = max(Est::M, (int)((double)cnt * ratio));
     int c = 0;
     for (int k = threadIdx.x; k < cnt; k += GCR_BLOCK)
-      if (FundamentalModel::symepi2_f64(pts64 + 4 * list[k], F) < t2) ++c;
+      if (FundamentalModel::symepi2_f64(row64(list[k]), F) < t2) ++c;
     c = block_sum(c, sh.red_i);
     if (c < min_n) return false;
     if constexpr (Est::KIND != 1) return true;
@@ -1941,7 +1965,7 @@ struct Engine {
     int total = 0;
     for (int base = 0; base < cnt; base += GCR_BLOCK) {
       const int k = base + threadIdx.x;
-      const int f = (k < cnt && HomographyModel::r2_f64(pts64 + 4 * list[k], H) < 4.0) ? 1 : 0;
+      const int f = (k < cnt && HomographyModel::r2_f64(row64(list[k]), H) < 4.0) ? 1 : 0;
       int tot;
       const int pos = block_exclusive_scan(f, sh.red_i, &tot);
       if (f) slot.list2[total + pos] = list[k];
@@ -2431,7 +2455,8 @@ struct Engine {
       // membership flags of the current set (the weights array of the reference)
       for (int i = threadIdx.x; i < N; i += GCR_BLOCK) slot.flag[i] = 0;
       sync();
-      for (int k = threadIdx.x; k < n; k += GCR_BLOCK) slot.flag[list[k]] = 1;
+      for (int k = threadIdx.x; k < n; k += GCR_BLOCK)
+        if (row_ok(list[k])) slot.flag[list[k]] = 1;
       sync();
       if (!fit_cta(list, n, 1)) break;
       const Score sc = exact_score(sh.fit_model, spare);
@@ -2676,6 +2701,8 @@ struct Engine {
 
   // ------------------------------------------------------------------
   __device__ void run() {
+    if (threadIdx.x == 0) sh.bad_row = 0;
+    sync();
     long long t0 = tick();
     // the sampler's layer grids use cell_start as scratch, so they come
     // before the neighbourhood grid that keeps it
@@ -2939,7 +2966,7 @@ struct Engine {
 #pragma unroll
         for (int q = 0; q < 9; ++q) Fb[q] = sh.best_model[q];
         for (int k = threadIdx.x; k < cnt; k += GCR_BLOCK)
-          slot.dres[k] = fmax(0.0, 1.0 - Est::r2_f64(pts64 + 4 * list[k], Fb) / t2);
+          slot.dres[k] = fmax(0.0, 1.0 - Est::r2_f64(row64(list[k]), Fb) / t2);
         sync();
         if (fit_cta_f(list, cnt, 2, false)) {
           const Score sc = exact_score(sh.fit_model, spare, nullptr, true);
@@ -2969,12 +2996,12 @@ struct Engine {
 #pragma unroll
         for (int q = 0; q < 9; ++q) Eb[q] = sh.best_model[q];
         for (int k = threadIdx.x; k < cnt; k += GCR_BLOCK)
-          slot.dres[k] = fmax(0.0, 1.0 - Est::r2_f64(pts64 + 4 * list[k], Eb) / t2);
+          slot.dres[k] = fmax(0.0, 1.0 - Est::r2_f64(row64(list[k]), Eb) / t2);
         sync();
         const int nm = fit_cta_multi(list, cnt, 2, false);
         double x1[3], x2[3];
         {
-          const double* p0 = pts64 + 4 * list[0];
+          const double* p0 = row64(list[0]);
           x1[0] = p0[0]; x1[1] = p0[1]; x1[2] = 1.0;
           x2[0] = p0[2]; x2[1] = p0[3]; x2[2] = 1.0;
           const double n1 = sqrt(x1[0] * x1[0] + x1[1] * x1[1] + 1.0);
@@ -3031,8 +3058,11 @@ struct Engine {
     }
     for (int i = threadIdx.x; i < N; i += GCR_BLOCK) mask[i] = 0;
     sync();
-    for (int k = threadIdx.x; k < cnt; k += GCR_BLOCK) mask[list[k]] = 1;
+    for (int k = threadIdx.x; k < cnt; k += GCR_BLOCK)
+      if (row_ok(list[k])) mask[list[k]] = 1;
     if (threadIdx.x < 9) ws.models_out[9 * pair + threadIdx.x] = sh.best_model[threadIdx.x];
+    sync();
+    if (sh.bad_row && status == ST_OK) status = ST_DEVICE_ERROR;
     if (threadIdx.x == 0) {
       so->iteration_number = iter;
       so->graph_cut_number = gc_number;

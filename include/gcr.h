@@ -35,7 +35,8 @@ typedef enum gcr_status {
   GCR_INVALID_ARG = 1,     /* bad pointer, shape or parameter value */
   GCR_TOO_FEW_POINTS = 2,  /* fewer correspondences than the minimal sample */
   GCR_NO_MODEL = 3,        /* the run ended without a model of more than m inliers */
-  GCR_DEVICE_ERROR = 4,    /* a CUDA call failed */
+  GCR_DEVICE_ERROR = 4,    /* a CUDA call failed, or (per pair) the engine's
+                              row-index check caught an index outside the pair */
   GCR_TIMEOUT = 5,         /* a device loop reached its iteration cap */
   GCR_CAPACITY = 6,        /* an input exceeds a documented size limit */
   GCR_UNSUPPORTED = 7      /* option combination not provided by this build */
