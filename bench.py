@@ -318,7 +318,8 @@ def run_learned(args, P, w, cfg, world, rank, local_rank, dist, torch):
     pk = torch.zeros(total, dtype=torch.uint8, device="cuda")
     ps = torch.zeros(P * _abi.STATS_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
     vp = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
-    rc = lib.gcr_batch_prepare(ctx_p, kind, P, vp(d_corr), _abi.ptr(offsets), None, _abi.ptr(size_array(sizes)),
+    sz = size_array(sizes)
+    rc = lib.gcr_batch_prepare(ctx_p, kind, P, vp(d_corr), _abi.ptr(offsets), None, _abi.ptr(sz),
                                ctypes.byref(p_plain), _abi.ptr(seeds), vp(pm), vp(pk), vp(ps))
     assert rc == 0, _abi.last_error()
     cap = torch.cuda.Stream()

@@ -221,7 +221,8 @@ gcr_status gcr_context_create(gcr_context** ctx) {
 gcr_status gcr_context_destroy(gcr_context* c) {
   if (!c) return GCR_OK;
   for (DevBuf* b : {&c->pairs, &c->slots_meta, &c->slot_mem, &c->pts32, &c->ticket, &c->norm_pts, &c->kinv,
-                    &c->row_pair, &c->corr, &c->models, &c->masks, &c->stats, &c->magsac})
+                    &c->row_pair, &c->phase, &c->corr, &c->models, &c->masks, &c->stats, &c->magsac, &c->rg_int,
+                    &c->rg_dbl, &c->rg_px, &c->ar_p, &c->ar_i, &c->ar_ab, &c->ar_cnt, &c->cdf, &c->probs_stage})
     b->release();
   delete c;
   return GCR_OK;
@@ -272,6 +273,13 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
   }
   const int64_t total = h_offsets[num_pairs] - h_offsets[0];
   if (h_offsets[0] != 0) return fail(GCR_INVALID_ARG, "offsets[0] must be 0");
+  // image sizes set the grid's cell sizes and the centring of the FP32 copies
+  for (int64_t i = 0; i < num_pairs; ++i) {
+    const gcr_image_size& z = h_sizes[i];
+    if (z.h1 <= 0 || z.w1 <= 0 || z.h2 <= 0 || z.w2 <= 0)
+      return fail(GCR_INVALID_ARG, "pair %lld: image sizes must be positive (got %d x %d, %d x %d)", (long long)i,
+                  z.h1, z.w1, z.h2, z.w2);
+  }
   // the radius graph replaces the grid when asked for with a spatial term; the
   // fundamental / essential drivers build no neighbourhood for a weight at or
   // below machine epsilon, and the homography driver keeps the grid under space

@@ -129,6 +129,8 @@ extern "C" gcr_status gcr_find_homography_device_noalloc(const double* d_corr, i
                 "%lld correspondences exceed the %d that the fixed scratch of the allocation-free entry point "
                 "holds; use gcr_batch_run_device for larger pairs",
                 (long long)n, kNoAllocMaxPoints);
+  if (size->h1 <= 0 || size->w1 <= 0 || size->h2 <= 0 || size->w2 <= 0)
+    return fail(GCR_INVALID_ARG, "image sizes must be positive");
   const gcr_params& p = *params;
   if (!(p.threshold > 0)) return fail(GCR_INVALID_ARG, "threshold must be > 0");
   if (!(p.confidence > 0 && p.confidence < 1)) return fail(GCR_INVALID_ARG, "confidence must be in (0, 1)");

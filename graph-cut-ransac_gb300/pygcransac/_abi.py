@@ -154,10 +154,12 @@ def exported_symbols():
 
 
 def ptr(a):
-    """Address of a numpy array's data (None -> NULL)."""
+    """Address of a numpy array's data (None -> NULL). The returned pointer
+    object holds a reference to the array, so a temporary passed straight into
+    a call stays alive until the call returns."""
     if a is None:
         return None
-    return ctypes.c_void_p(a.ctypes.data)
+    return a.ctypes.data_as(ctypes.c_void_p)
 
 
 def last_error():

@@ -68,7 +68,7 @@ def load():
 
 
 def _p(a):
-    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)  # keeps the array alive
 
 
 def make_size(h1, w1, h2, w2):

@@ -1,5 +1,6 @@
 """CPU checks of the C-ABI boundary: libgcr.so loads, exports every function
 that include/gcr.h declares, and the ctypes mirror matches the C layout."""
+import ctypes
 import os
 import re
 import subprocess
@@ -78,3 +79,24 @@ def test_default_params_follow_reference(gcr):
     assert (f.spatial_coherence_weight, f.neighborhood, f.neighborhood_size) == (0.0, 1, 20.0)
     e = gcr.default_params(_abi.GCR_ESSENTIAL)
     assert (e.spatial_coherence_weight, e.neighborhood) == (0.1, 1)
+
+
+def test_ptr_keeps_a_temporary_array_alive():
+    """_abi.ptr(f(x)) passed straight into a call: the pointer object holds
+    the array, so its memory is not freed before the call reads it."""
+    import gc
+    import weakref
+
+    class Arr(np.ndarray):
+        pass
+
+    a = np.arange(16, dtype=np.float64).view(Arr)
+    ref = weakref.ref(a)
+    p = _abi.ptr(a)
+    del a
+    gc.collect()
+    assert ref() is not None
+    assert ctypes.cast(p, ctypes.POINTER(ctypes.c_double))[5] == 5.0
+    del p
+    gc.collect()
+    assert ref() is None

@@ -124,3 +124,54 @@ def test_pair_times_stamp_every_pair():
     assert np.array_equal(m0, m1) and np.array_equal(k0, k1)
     assert np.all(t0 == 0)
     assert np.all(t1 > 0) and np.all(t1[:, 1] >= t1[:, 0])
+
+
+def test_non_positive_image_sizes_are_rejected(gcr):
+    pr = S.homography_pair(3, n=300)
+    p = gcr.default_params(_abi.GCR_HOMOGRAPHY)
+    for bad in [(0, 640, 480, 640), (480, -1, 480, 640), (480, 640, 480, 0)]:
+        with pytest.raises(ValueError, match="image sizes must be positive"):
+            gcr.find_batch(_abi.GCR_HOMOGRAPHY, [pr["corr"]], [bad], p, seeds=[1])
+
+
+def test_context_destroy_releases_every_scratch_buffer():
+    """Create / run / destroy with the radius graph and the AR sampler (their
+    per-CTA scratch is the largest) several times: free device memory returns
+    to where it started."""
+    torch = pytest.importorskip("torch")
+    lib = _abi.load()
+    pr = S.two_view_pair(41, n=1500, inlier_ratio=0.4)
+    corr = np.ascontiguousarray(pr["corr"])
+    n = len(corr)
+    offsets = np.array([0, n], np.int64)
+    sizes = np.zeros(1, _abi.SIZE_DTYPE)
+    sizes[0] = tuple(pr["size"])
+    prm = _abi.Params(threshold=0.75, confidence=0.99, spatial_coherence_weight=0.975, neighborhood_size=20.0,
+                      max_iterations=300, min_iterations=50, sampler=_abi.GCR_SAMPLER_AR, neighborhood=1,
+                      lo_number=50, seed=0, sampler_variance=0.1)
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    d_corr = torch.from_numpy(corr).cuda()
+    d_prob = torch.from_numpy(0.1 + pr["inlier_gt"].astype(np.float64)).cuda()
+    d_models = torch.zeros(9, dtype=torch.float64, device="cuda")
+    d_masks = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    d_stats = torch.zeros(_abi.STATS_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+
+    def cycle():
+        ctx = ctypes.c_void_p()
+        assert lib.gcr_context_create(ctypes.byref(ctx)) == 0
+        try:
+            assert lib.gcr_context_set_probabilities(ctx, vp(d_prob)) == 0
+            assert lib.gcr_batch_run_device(ctx, _abi.GCR_FUNDAMENTAL, 1, vp(d_corr), _abi.ptr(offsets), None,
+                                            _abi.ptr(sizes), ctypes.byref(prm), None, vp(d_models), vp(d_masks),
+                                            vp(d_stats), None) == 0, _abi.last_error()
+            torch.cuda.synchronize()
+        finally:
+            assert lib.gcr_context_destroy(ctx) == 0
+
+    cycle()  # first use: module loading and the runtime's own allocations
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(3):
+        cycle()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free0 - free1 < (64 << 20), f"{(free0 - free1) >> 20} MiB not returned"
