@@ -702,9 +702,14 @@ gcr_status gcr_find_essential(const double* corr, int64_t n, const double* K1, c
   return find_one(GCR_ESSENTIAL, corr, n, K1, K2, size, probabilities, params, model_out9, mask_out, stats_out);
 }
 
-gcr_status gcr_run(gcr_model_kind kind, const double* points, const double* pixels, int64_t n,
-                   const double* cell_sizes, int32_t divisions, const gcr_image_size* size,
-                   const gcr_params* params, double* model_out9, uint8_t* mask_out, gcr_stats* stats_out) {
+}  // extern "C"
+
+// GCRANSAC::run on one pair (gcr_run and gcr_run_with_probabilities):
+// `probabilities` [n] (host) or NULL feed the importance and AR samplers.
+static gcr_status run_single(gcr_model_kind kind, const double* points, const double* pixels, int64_t n,
+                             const double* cell_sizes, int32_t divisions, const gcr_image_size* size,
+                             const double* probabilities, const gcr_params* params, double* model_out9,
+                             uint8_t* mask_out, gcr_stats* stats_out) {
   static thread_local gcr_context* ctx = nullptr;
   g_last_launches = 0;
   if (!points || !cell_sizes || !size || !params || !model_out9 || !mask_out)
@@ -729,6 +734,12 @@ gcr_status gcr_run(gcr_model_kind kind, const double* points, const double* pixe
   double* d_pix = d_pts + 4 * n;
   CUDA_TRY(cudaMemcpyAsync(d_pts, points, bytes, cudaMemcpyHostToDevice, s));
   CUDA_TRY(cudaMemcpyAsync(d_pix, pixels ? pixels : points, bytes, cudaMemcpyHostToDevice, s));
+  ctx->probs = nullptr;
+  if (probabilities) {
+    CUDA_TRY(ctx->probs_stage.ensure(sizeof(double) * (size_t)n));
+    CUDA_TRY(cudaMemcpyAsync(ctx->probs_stage.p, probabilities, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    ctx->probs = (const double*)ctx->probs_stage.p;
+  }
   RunOnly ro;
   ro.d_pixels = d_pix;
   for (int q = 0; q < 4; ++q) ro.cell[q] = cell_sizes[q];
@@ -753,6 +764,29 @@ gcr_status gcr_run(gcr_model_kind kind, const double* points, const double* pixe
     return fail((gcr_status)so.status, "device engine reported status %d", so.status);
   }
   return GCR_OK;
+}
+
+extern "C" {
+
+gcr_status gcr_run(gcr_model_kind kind, const double* points, const double* pixels, int64_t n,
+                   const double* cell_sizes, int32_t divisions, const gcr_image_size* size,
+                   const gcr_params* params, double* model_out9, uint8_t* mask_out, gcr_stats* stats_out) {
+  if (params && (params->sampler == GCR_SAMPLER_IMPORTANCE || params->sampler == GCR_SAMPLER_AR))
+    return fail(GCR_INVALID_ARG, "samplers 3 and 4 need probabilities: use gcr_run_with_probabilities");
+  return run_single(kind, points, pixels, n, cell_sizes, divisions, size, nullptr, params, model_out9, mask_out,
+                    stats_out);
+}
+
+gcr_status gcr_run_with_probabilities(gcr_model_kind kind, const double* points, const double* pixels, int64_t n,
+                                      const double* cell_sizes, int32_t divisions, const gcr_image_size* size,
+                                      const double* probabilities, const gcr_params* params, double* model_out9,
+                                      uint8_t* mask_out, gcr_stats* stats_out) {
+  if (!probabilities) return fail(GCR_INVALID_ARG, "probabilities is NULL");
+  for (int64_t i = 0; i < n; ++i)
+    if (!(probabilities[i] >= 0.0) || !std::isfinite(probabilities[i]))
+      return fail(GCR_INVALID_ARG, "probability %lld is negative or not finite", (long long)i);
+  return run_single(kind, points, pixels, n, cell_sizes, divisions, size, probabilities, params, model_out9,
+                    mask_out, stats_out);
 }
 
 }  // extern "C"

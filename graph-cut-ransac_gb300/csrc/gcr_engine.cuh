@@ -1302,18 +1302,17 @@ struct Engine {
     if (threadIdx.x == 0) sh.flow_status = 0;
     sync();
     const bool pairwise = prm.lambda > 0;
-    if (!pairwise) {
-      // unary terms only: SINK iff the sink capacity is positive
-      for (int i = threadIdx.x; i < N; i += GCR_BLOCK) slot.flag[i] = (uint8_t)(slot.tr[i] < -kResidualEps ? 1 : 0);
-    }
+    // Every point starts with its unary decision (SINK iff the sink capacity
+    // is positive). That is the labelling without pairwise terms, and on the
+    // grid it stays the label of the points of single-point cells and of
+    // cells the flow solver does not take (more than kMaxFlowCap points, or an
+    // inconsistent cell table: status ST_CAPACITY), so no flag of this pair
+    // keeps a value from an earlier pair or from other uses of the slot.
+    for (int i = threadIdx.x; i < N; i += GCR_BLOCK) slot.flag[i] = (uint8_t)(slot.tr[i] < -kResidualEps ? 1 : 0);
+    sync();
     if (pairwise && prm.neighborhood == 1) {
-      if (rg_ok) {
-        radius_mincut();
-      } else {
-        // no graph (capacity exceeded, reported): unary terms only
-        for (int i = threadIdx.x; i < N; i += GCR_BLOCK)
-          slot.flag[i] = (uint8_t)(slot.tr[i] < -kResidualEps ? 1 : 0);
-      }
+      // without a graph (capacity exceeded, reported) the unary labels stand
+      if (rg_ok) radius_mincut();
       sync();
     }
     for (int c = warp; pairwise && prm.neighborhood == 0 && c < ncells; c += GCR_WARPS) {
@@ -1322,12 +1321,8 @@ struct Engine {
         if (lane == 0) atomicMax(&sh.flow_status, ST_CAPACITY);
         continue;
       }
-      if (n == 1 || !pairwise) {
-        for (int k = lane; k < n; k += 32) {
-          const int p = slot.cell_pts[c0 + k];
-          slot.flag[p] = (uint8_t)(slot.tr[p] < -kResidualEps ? 1 : 0);
-        }
-      } else if (n > kMaxFlowCap) {
+      if (n == 1) continue;  // unary label, set above
+      if (n > kMaxFlowCap) {
         if (lane == 0) atomicMax(&sh.flow_status, ST_CAPACITY);
       } else if (!mincut_cell(c0, n, warp)) {
         if (lane == 0) atomicMax(&sh.flow_status, ST_TIMEOUT);
@@ -1335,10 +1330,11 @@ struct Engine {
     }
     sync();
     if (sh.flow_status != 0 && status == ST_OK) status = sh.flow_status;
+    // flags are read as booleans, so the list never holds more than N points
     int total = 0;
     for (int base = 0; base < N; base += GCR_BLOCK) {
       const int i = base + threadIdx.x;
-      const int f = (i < N) ? slot.flag[i] : 0;
+      const int f = (i < N && slot.flag[i] != 0) ? 1 : 0;
       int tot;
       const int pos = block_exclusive_scan(f, sh.red_i, &tot);
       if (f) list[total + pos] = i;

@@ -111,6 +111,8 @@ _EXPORTS = {
     "gcr_context_set_pair_times": (ctypes.c_int, [_P, _P]),
     "gcr_context_set_probabilities": (ctypes.c_int, [_P, _P]),
     "gcr_run": (ctypes.c_int, [ctypes.c_int, _P, _P, ctypes.c_int64, _P, ctypes.c_int32, _P, _P, _P, _P, _P]),
+    "gcr_run_with_probabilities": (ctypes.c_int, [ctypes.c_int, _P, _P, ctypes.c_int64, _P, ctypes.c_int32, _P, _P,
+                                                  _P, _P, _P, _P]),
     "gcr_learned_param_count": (ctypes.c_int64, []),
     "gcr_learned_feature_width": (ctypes.c_int32, []),
     "gcr_learned_features": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_int64, _P, _P]),

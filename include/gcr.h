@@ -229,6 +229,19 @@ gcr_status gcr_run(gcr_model_kind kind, const double* points, const double* pixe
                    const double* cell_sizes, int32_t divisions, const gcr_image_size* size,
                    const gcr_params* params, double* model_out9, uint8_t* mask_out, gcr_stats* stats_out);
 
+/* gcr_run with a main sampler that reads per-correspondence probabilities:
+ * the ImportanceSampler (samplers/importance_sampler.h:67-80, sampler 3) and
+ * the AdaptiveReorderingSampler (samplers/adaptive_reordering_sampler.h:59-97,
+ * sampler 4), which the reference constructs from a probability vector and
+ * passes to GCRANSAC::run (GCRANSAC.h:200-627). `probabilities` [n] (host,
+ * finite, non-negative; the AR sampler divides them by their maximum as the
+ * reference's drivers do, gcransac_python.cpp:1730-1741). gcr_run rejects
+ * samplers 3 and 4. */
+gcr_status gcr_run_with_probabilities(gcr_model_kind kind, const double* points, const double* pixels, int64_t n,
+                                      const double* cell_sizes, int32_t divisions, const gcr_image_size* size,
+                                      const double* probabilities, const gcr_params* params, double* model_out9,
+                                      uint8_t* mask_out, gcr_stats* stats_out);
+
 /* Learned inlier-probability proposal (no counterpart in the reference, which
  * takes externally computed probabilities for its samplers 3 and 4): a
  * per-correspondence MLP whose scores order the correspondences for PROSAC

@@ -7,7 +7,8 @@
  * that interface compiles against this header and runs on the device.
  *
  * Correspondences are a gcransac::MatView (row-major doubles, 4 columns:
- * x1 y1 x2 y2) instead of cv::Mat. run() forwards to gcr_run (include/gcr.h):
+ * x1 y1 x2 y2) instead of cv::Mat. run() forwards to gcr_run (include/gcr.h;
+ * gcr_run_with_probabilities for the importance and AR samplers):
  * one pair, GCRANSAC::run semantics (no Python-driver pre- or post-processing),
  * the samplers' and graph's data points as the neighbourhood coordinates, the
  * points given to run() as the fitting coordinates (K^-1-normalised ones for
@@ -28,6 +29,8 @@
  *   sampler::UniformSampler          samplers/uniform_sampler.h:45-115
  *   sampler::ProsacSampler           samplers/prosac_sampler.h:51-237
  *   sampler::ProgressiveNapsacSampler<4>  samplers/progressive_napsac_sampler.h:50-326
+ *   sampler::ImportanceSampler       samplers/importance_sampler.h:51-136
+ *   sampler::AdaptiveReorderingSampler  samplers/adaptive_reordering_sampler.h:46-166
  *   neighborhood::GridNeighborhoodGraph<4> neighborhood/grid_neighborhood_graph.h:132-301
  *   neighborhood::FlannNeighborhoodGraph   neighborhood/flann_neighborhood_graph.h:100-139 (exact ball)
  *   MSACScoringFunction, MAGSACScoringFunction  scoring_function.h:137-348
@@ -160,6 +163,8 @@ class Sampler {
   bool isInitialized() const { return initialized; }
   /* the engine's sampler id (GCR_SAMPLER_*) */
   virtual int deviceSamplerId() const = 0;
+  /* the per-point probabilities the sampler draws from (samplers 3 and 4), else NULL */
+  virtual const std::vector<double>* deviceProbabilities() const { return nullptr; }
   const Container* container;
 
  protected:
@@ -204,6 +209,56 @@ class ProgressiveNapsacSampler : public Sampler<MatView, size_t> {
   size_t sample_size;
   std::vector<double> sizes;
   double sampler_length;
+};
+
+/* ImportanceSampler (samplers/importance_sampler.h:51-136): every sample is m
+   independent draws from the multinomial distribution of the given point
+   probabilities (std::discrete_distribution there, the engine's counter-based
+   streams here). */
+class ImportanceSampler : public Sampler<MatView, size_t> {
+ public:
+  ImportanceSampler(const MatView* container_, const std::vector<double>& probabilities_, size_t sample_size_)
+      : Sampler(container_), probabilities(probabilities_), sample_size(sample_size_) {
+    initialized = probabilities_.size() == (size_t)container_->rows;
+  }
+  const std::string getName() const override { return "Importance Sampler"; }
+  int deviceSamplerId() const override { return GCR_SAMPLER_IMPORTANCE; }
+  const std::vector<double>* deviceProbabilities() const override { return &probabilities; }
+  std::vector<double> probabilities;
+  size_t sample_size;
+};
+
+/* AdaptiveReorderingSampler (samplers/adaptive_reordering_sampler.h:46-166):
+   a max-heap of point probabilities; a sample takes the m most probable points
+   and pushes each back with its updated beta-posterior estimate plus a jitter
+   of +-randomness/2. The engine keeps the reference drivers' configuration:
+   randomness 0.01, not ordered, and probabilities divided by their maximum
+   (gcransac_python.cpp:1730-1741), so the vector given here must have maximum 1
+   for the run to equal the reference's sampler on the same vector. */
+class AdaptiveReorderingSampler : public Sampler<MatView, size_t> {
+ public:
+  AdaptiveReorderingSampler(const MatView* container_, const std::vector<double>& inlier_probabilities_,
+                            size_t sample_size_, double estimator_variance_ = 0.9765, double randomness_ = 0.01,
+                            bool ordered_ = false)
+      : Sampler(container_), probabilities(inlier_probabilities_), sample_size(sample_size_),
+        estimator_variance(estimator_variance_) {
+    if (randomness_ != 0.01 || ordered_)
+      throw std::invalid_argument("the device AR sampler has randomness 0.01 and no ordered mode");
+    if (!(estimator_variance_ > 0)) throw std::invalid_argument("the AR sampler needs estimator_variance > 0");
+    double mx = 0.0;
+    for (double v : inlier_probabilities_) mx = v > mx ? v : mx;
+    if (!inlier_probabilities_.empty() && mx != 1.0)
+      throw std::invalid_argument(
+          "the device AR sampler divides the probabilities by their maximum, as the reference's drivers do "
+          "before constructing it: pass probabilities whose maximum is 1");
+    initialized = inlier_probabilities_.size() == (size_t)container_->rows;
+  }
+  const std::string getName() const override { return "Probabilistic Reordering Sampler"; }
+  int deviceSamplerId() const override { return GCR_SAMPLER_AR; }
+  const std::vector<double>* deviceProbabilities() const override { return &probabilities; }
+  std::vector<double> probabilities;
+  size_t sample_size;
+  double estimator_variance;
 };
 
 }  // namespace sampler
@@ -351,6 +406,11 @@ class GCRANSAC {
                            : (int64_t)settings.max_iteration_number;
     p.min_iterations = (int64_t)settings.min_iteration_number;
     p.sampler = main_sampler_->deviceSamplerId();
+    const std::vector<double>* probs = main_sampler_->deviceProbabilities();
+    if (probs && (!main_sampler_->isInitialized() || probs->size() != (size_t)points_.rows))
+      throw std::invalid_argument("the sampler's probabilities must have one entry per correspondence");
+    if (auto* ar = dynamic_cast<const sampler::AdaptiveReorderingSampler*>(main_sampler_))
+      p.sampler_variance = ar->estimator_variance;
     p.lo_number = (int32_t)settings.max_local_optimization_number;
     p.scoring = _ScoringFunction::device_scoring;
     p.use_sprt = _PreemptiveModelVerification::device_sprt ? 1 : 0;
@@ -385,8 +445,11 @@ class GCRANSAC {
     gcr_stats st{};
     Model out;
     const gcr_status rc =
-        gcr_run(_ModelEstimator::kind, points_.data, neighborhood_graph_->container->data, n, cells_, divisions_,
-                &size, &p, out.descriptor.v, mask.data(), &st);
+        probs ? gcr_run_with_probabilities(_ModelEstimator::kind, points_.data, neighborhood_graph_->container->data,
+                                           n, cells_, divisions_, &size, probs->data(), &p, out.descriptor.v,
+                                           mask.data(), &st)
+              : gcr_run(_ModelEstimator::kind, points_.data, neighborhood_graph_->container->data, n, cells_,
+                        divisions_, &size, &p, out.descriptor.v, mask.data(), &st);
     if (rc != GCR_OK && rc != GCR_NO_MODEL) throw std::runtime_error(gcr_last_error_string());
     statistics = utils::RANSACStatistics();
     statistics.main_sampler_name = main_sampler_->getName();

@@ -376,6 +376,19 @@ int oracle_run(int kind, const double* points, const double* pixels, int64_t n, 
   return rc;
 }
 
+// oracle_run with the importance / AR samplers' point probabilities (the
+// probability vector the reference's ImportanceSampler and
+// AdaptiveReorderingSampler are constructed from,
+// samplers/importance_sampler.h:67-80, adaptive_reordering_sampler.h:59-97)
+int oracle_run_prob(int kind, const double* points, const double* pixels, int64_t n, const double* cell_sizes,
+                    int32_t divisions, const gcr_image_size* sz, const double* probabilities, const gcr_params* p,
+                    uint64_t seed, double* model_out, uint8_t* mask, gcr_stats* st) {
+  g_probs = probabilities;
+  const int rc = oracle_run(kind, points, pixels, n, cell_sizes, divisions, sz, p, seed, model_out, mask, st);
+  g_probs = nullptr;
+  return rc;
+}
+
 // Neighbour counts of the radius graph (Grid::radius_graph) of n points.
 void oracle_radius_counts(const double* corr, int64_t n, double radius, int64_t* counts) {
   const Mat pts{corr, n, 4};

@@ -44,6 +44,9 @@ def load():
         lib.oracle_run.restype = ctypes.c_int
         lib.oracle_run.argtypes = [ctypes.c_int, P, P, ctypes.c_int64, P, ctypes.c_int32, P, P, ctypes.c_uint64, P,
                                    P, P]
+        lib.oracle_run_prob.restype = ctypes.c_int
+        lib.oracle_run_prob.argtypes = [ctypes.c_int, P, P, ctypes.c_int64, P, ctypes.c_int32, P, P, P,
+                                        ctypes.c_uint64, P, P, P]
         lib.oracle_magsac_gamma.restype = ctypes.c_double
         lib.oracle_magsac_gamma.argtypes = [ctypes.c_int]
         lib.oracle_labeling.restype = ctypes.c_int
@@ -106,8 +109,9 @@ def radius_counts(corr, radius):
     return out
 
 
-def run(kind, points, pixels, cell_sizes, divisions, size, params, seed=0):
-    """GCRANSAC::run alone (oracle_run): (status, model [3, 3], mask, stats)."""
+def run(kind, points, pixels, cell_sizes, divisions, size, params, seed=0, probabilities=None):
+    """GCRANSAC::run alone (oracle_run): (status, model [3, 3], mask, stats).
+    `probabilities` feed the importance and AR samplers (samplers 3 and 4)."""
     lib = load()
     points = np.ascontiguousarray(points, np.float64)
     pixels = None if pixels is None else np.ascontiguousarray(pixels, np.float64)
@@ -116,8 +120,13 @@ def run(kind, points, pixels, cell_sizes, divisions, size, params, seed=0):
     model = np.zeros(9)
     mask = np.zeros(n, np.uint8)
     st = _abi.Stats()
-    rc = lib.oracle_run(kind, _p(points), _p(pixels), n, _p(cs), int(divisions), ctypes.byref(size),
-                        ctypes.byref(params), int(seed), _p(model), _p(mask), ctypes.byref(st))
+    if probabilities is not None:
+        pr = np.ascontiguousarray(probabilities, np.float64)
+        rc = lib.oracle_run_prob(kind, _p(points), _p(pixels), n, _p(cs), int(divisions), ctypes.byref(size),
+                                 _p(pr), ctypes.byref(params), int(seed), _p(model), _p(mask), ctypes.byref(st))
+    else:
+        rc = lib.oracle_run(kind, _p(points), _p(pixels), n, _p(cs), int(divisions), ctypes.byref(size),
+                            ctypes.byref(params), int(seed), _p(model), _p(mask), ctypes.byref(st))
     return rc, model.reshape(3, 3), mask.astype(bool), st
 
 

@@ -7,7 +7,8 @@
 //     threshold, confidence, lambda; int64
 //     max_iterations, min_iterations; int32 lo_number; uint64 seed; double
 //     sprt_ratio, cell[4], sizes[4]; double points[n][4], pixels[n][4],
-//     K1[9], K2[9]
+//     K1[9], K2[9]; double sampler_variance, probabilities[n] (read by samplers
+//     3 and 4)
 // OUT int32 has_model; double model[9]; int64 iterations, graph_cuts,
 //     local_optimisations; double score; int64 inlier count, inliers[]
 #include <cstdio>
@@ -28,6 +29,8 @@ struct Input {
   double sprt_ratio, cell[4], sizes[4];
   std::vector<double> points, pixels;
   double K1[9], K2[9];
+  double variance;
+  std::vector<double> probs;
 };
 
 template <class T>
@@ -64,10 +67,16 @@ static int run_case(const Input& in, const Est& est, FILE* out) {
   sampler::ProgressiveNapsacSampler<4>* pnapsac = nullptr;
   if (in.sampler == GCR_SAMPLER_PNAPSAC)
     pnapsac = new sampler::ProgressiveNapsacSampler<4>(&pixels, {16, 8, 4, 2}, Est::sampleSize(), sizes, 0.5);
+  sampler::ImportanceSampler importance(&pixels, in.probs, Est::sampleSize());
+  sampler::AdaptiveReorderingSampler* ar = nullptr;
+  if (in.sampler == GCR_SAMPLER_AR)
+    ar = new sampler::AdaptiveReorderingSampler(&pixels, in.probs, Est::sampleSize(), in.variance);
   sampler::Sampler<MatView, size_t>* main_sampler =
-      in.sampler == GCR_SAMPLER_UNIFORM ? (sampler::Sampler<MatView, size_t>*)&uniform
-      : in.sampler == GCR_SAMPLER_PROSAC ? (sampler::Sampler<MatView, size_t>*)&prosac
-                                         : (sampler::Sampler<MatView, size_t>*)pnapsac;
+      in.sampler == GCR_SAMPLER_UNIFORM      ? (sampler::Sampler<MatView, size_t>*)&uniform
+      : in.sampler == GCR_SAMPLER_PROSAC     ? (sampler::Sampler<MatView, size_t>*)&prosac
+      : in.sampler == GCR_SAMPLER_IMPORTANCE ? (sampler::Sampler<MatView, size_t>*)&importance
+      : in.sampler == GCR_SAMPLER_AR         ? (sampler::Sampler<MatView, size_t>*)ar
+                                             : (sampler::Sampler<MatView, size_t>*)pnapsac;
   GCRANSAC<Est, Graph, Scoring<Est>, Pre, Sel> g;
   g.settings.threshold = in.threshold;
   g.settings.confidence = in.confidence;
@@ -99,6 +108,7 @@ static int run_case(const Input& in, const Est& est, FILE* out) {
     fwrite(&v, 8, 1, out);
   }
   delete pnapsac;
+  delete ar;
   return 0;
 }
 
@@ -138,6 +148,9 @@ int main(int argc, char** argv) {
   rd(f, in.pixels.data(), in.pixels.size());
   rd(f, in.K1, 9);
   rd(f, in.K2, 9);
+  rd(f, &in.variance);
+  in.probs.resize((size_t)in.n);
+  rd(f, in.probs.data(), in.probs.size());
   fclose(f);
   FILE* out = fopen(argv[2], "wb");
   if (!out) return 2;

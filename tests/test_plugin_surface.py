@@ -49,6 +49,9 @@ def write_input(path, kind, pts, pix, cfg, K=None):
         f.write(np.ascontiguousarray(pix, "<f8").tobytes())
         Kf = np.eye(3) if K is None else K
         f.write(np.asarray(Kf, "<f8").tobytes() * 2)
+        f.write(struct.pack("<d", cfg.get("variance", 0.1)))
+        pr = cfg.get("probs")
+        f.write(np.ascontiguousarray(np.ones(n) if pr is None else pr, "<f8").tobytes())
 
 
 def read_output(path):
@@ -95,11 +98,37 @@ def cases():
                 dict(fcfg, div=0, cell=[20.0, 1.0, 1.0, 1.0], seed=9), None))
     out.append(("E radius graph", _abi.GCR_ESSENTIAL, nrm, c,
                 dict(fcfg, div=0, cell=[20.0, 1.0, 1.0, 1.0], lam=0.1, thr=0.75 / 800.0, seed=10), K))
+    # samplers reading per-point probabilities (largest 1, as the AR sampler
+    # wants them): a noisy inlier indicator
+    rng = np.random.default_rng(14)
+    ph = np.clip(np.where(pr["inlier_gt"], 0.8, 0.2) + rng.normal(0, 0.1, len(pr["corr"])), 0.01, 0.99)
+    ph /= ph.max()
+    out.append(("H importance sampler", _abi.GCR_HOMOGRAPHY, pr["corr"], pr["corr"],
+                dict(base, sampler=3, probs=ph, seed=11), None))
+    pq = np.clip(np.where(pf["inlier_gt"], 0.7, 0.3) + rng.normal(0, 0.1, len(pf["corr"])), 0.01, 0.99)
+    pq /= pq.max()
+    out.append(("F AR sampler", _abi.GCR_FUNDAMENTAL, pf["corr"], pf["corr"],
+                dict(fcfg, sampler=4, probs=pq, variance=0.1, seed=12), None))
     return out
 
 
+def test_ar_sampler_rejects_unscaled_probabilities(tmp_path):
+    """The AR sampler class throws (driver exit code 3) for probabilities
+    whose maximum is not 1; no device work is started."""
+    if not os.path.exists(os.path.join(LIBDIR, "libgcr.so")):
+        pytest.skip("libgcr.so not built")
+    exe = compile_driver(str(tmp_path))
+    pf = S.two_view_pair(15, n=300, inlier_ratio=0.5)
+    cfg = dict(sampler=4, scoring=0, sprt=0, sp=0, div=8, thr=0.75, lam=0.975, max_it=100, min_it=50, seed=1,
+               cell=[80.0, 60.0, 80.0, 60.0], sizes=[640.0, 480.0, 640.0, 480.0], probs=np.full(300, 0.5))
+    fin, fout = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
+    write_input(fin, _abi.GCR_FUNDAMENTAL, pf["corr"], pf["corr"], cfg)
+    r = subprocess.run([exe, fin, fout], capture_output=True, text=True)
+    assert r.returncode == 3 and "maximum is 1" in r.stderr
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("idx", range(8))
+@pytest.mark.parametrize("idx", range(10))
 def test_plugin_run_matches_oracle_run(tmp_path, oracle, idx):
     name, kind, pts, pix, cfg, K = cases()[idx]
     exe = compile_driver(str(tmp_path))
@@ -114,11 +143,11 @@ def test_plugin_run_matches_oracle_run(tmp_path, oracle, idx):
                     min_iterations=cfg["min_it"], sampler=cfg["sampler"], neighborhood=1 if radius else 0,
                     lo_number=50, seed=cfg["seed"], scoring=cfg["scoring"],
                     use_sprt=cfg["sprt"], use_space_partitioning=cfg["sp"],
-                    min_inlier_ratio_for_sprt=cfg.get("ratio", 0.01))
+                    min_inlier_ratio_for_sprt=cfg.get("ratio", 0.01), sampler_variance=cfg.get("variance", 0.1))
     z = cfg["sizes"]
     rc, M, mask, st = oracle.run(kind, pts, pix, cfg["cell"], max(cfg["div"], 1), oracle.make_size(int(z[1]), int(z[0]),
                                                                                             int(z[3]), int(z[2])),
-                                 p, seed=cfg["seed"])
+                                 p, seed=cfg["seed"], probabilities=cfg.get("probs"))
     assert has == (rc == 0), name
     ref = np.flatnonzero(mask)
     assert np.array_equal(inl, ref), f"{name}: inliers differ ({len(inl)} vs {len(ref)})"
