@@ -332,6 +332,8 @@ def run_learned(args, P, w, cfg, world, rank, local_rank, dist, torch):
     p_l = params_for(args.workload)
     p_l.max_iterations = w["learned_iters"]
     p_l.min_iterations = min(50, w["learned_iters"])
+    p_l.lo_number = args.learned_lo
+    cfg["learned_lo_number"] = args.learned_lo
     b = LearnedBatch(net, kind, d_corr, offsets, sizes, p_l, seeds)
     b.prepare()
     g_prop, g_eng = torch.cuda.CUDAGraph(), torch.cuda.CUDAGraph()
@@ -462,6 +464,8 @@ def main():
     ap.add_argument("--workload", default="learned", choices=sorted(WORKLOADS))
     ap.add_argument("--pairs", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--learned-lo", type=int, default=50,
+                    help="LO trials of the learned form (the reference's default is 50)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
