@@ -100,3 +100,28 @@ def test_ptr_keeps_a_temporary_array_alive():
     del p
     gc.collect()
     assert ref() is None
+
+
+def test_run_entries_check_probabilities_before_device_work():
+    """gcr_run rejects the samplers that read probabilities, and
+    gcr_run_with_probabilities rejects a missing, negative or non-finite
+    probability: both return GCR_INVALID_ARG before any device call."""
+    lib = _abi.load()
+    n = 40
+    pts = np.random.default_rng(1).uniform(0, 480, (n, 4))
+    cells = np.array([160.0, 120.0, 160.0, 120.0])
+    size = _abi.ImageSize(h1=480, w1=640, h2=480, w2=640)
+    model = np.zeros(9)
+    mask = np.zeros(n, np.uint8)
+    st = _abi.Stats()
+    for sampler in (_abi.GCR_SAMPLER_IMPORTANCE, _abi.GCR_SAMPLER_AR):
+        p = _abi.Params(threshold=3.0, confidence=0.99, spatial_coherence_weight=0.975, neighborhood_size=4,
+                        max_iterations=100, min_iterations=50, sampler=sampler, lo_number=50, sampler_variance=0.1)
+        rc = lib.gcr_run(_abi.GCR_HOMOGRAPHY, _abi.ptr(pts), None, n, _abi.ptr(cells), 4, ctypes.byref(size),
+                         ctypes.byref(p), _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
+        assert rc == _abi.GCR_INVALID_ARG and "gcr_run_with_probabilities" in _abi.last_error()
+        for bad in (None, np.r_[np.ones(n - 1), -1.0], np.r_[np.ones(n - 1), np.inf], np.r_[np.ones(n - 1), np.nan]):
+            rc = lib.gcr_run_with_probabilities(_abi.GCR_HOMOGRAPHY, _abi.ptr(pts), None, n, _abi.ptr(cells), 4,
+                                                ctypes.byref(size), _abi.ptr(bad), ctypes.byref(p), _abi.ptr(model),
+                                                _abi.ptr(mask), ctypes.byref(st))
+            assert rc == _abi.GCR_INVALID_ARG, bad
