@@ -1,4 +1,4 @@
-"""Parity on pairs above 8000 correspondences with a 16^4 grid: one batch per
+"""Parity on pairs of 9000-40000 correspondences with a 16^4 grid: one batch per
 model kind with pairs of different sizes (so a CTA's scratch may serve pairs
 of several sizes), every pair checked against the oracle on exact masks,
 statuses and iteration / graph-cut counts, models within 1e-6 relative
@@ -12,6 +12,9 @@ pytestmark = pytest.mark.gpu
 
 MODEL_TOL = 1e-6
 SIZES = [(12000, 0.45), (9000, 0.3), (10500, 0.55)]
+# the largest pairs of the mixed serving batch, inlier sets up to 12000 points
+SIZES_XL = [(40000, 0.25), (24000, 0.5)]
+CASES = [(SIZES, 0), (SIZES_XL, 100)]
 
 
 def params(threshold, lam):
@@ -41,16 +44,19 @@ def check_batch(oracle, gcr, kind, pairs, p, K=None):
         assert stats["graph_cut_number"][i] == st.graph_cut_number, i
 
 
-def test_homography_large_pairs(oracle, gcr):
-    pairs = [S.homography_pair(400 + i, n=n, inlier_ratio=r) for i, (n, r) in enumerate(SIZES)]
+@pytest.mark.parametrize("sizes,base", CASES)
+def test_homography_large_pairs(oracle, gcr, sizes, base):
+    pairs = [S.homography_pair(400 + base + i, n=n, inlier_ratio=r) for i, (n, r) in enumerate(sizes)]
     check_batch(oracle, gcr, _abi.GCR_HOMOGRAPHY, pairs, params(3.0, 0.975))
 
 
-def test_fundamental_large_pairs(oracle, gcr):
-    pairs = [S.two_view_pair(410 + i, n=n, inlier_ratio=r) for i, (n, r) in enumerate(SIZES)]
+@pytest.mark.parametrize("sizes,base", CASES)
+def test_fundamental_large_pairs(oracle, gcr, sizes, base):
+    pairs = [S.two_view_pair(410 + base + i, n=n, inlier_ratio=r) for i, (n, r) in enumerate(sizes)]
     check_batch(oracle, gcr, _abi.GCR_FUNDAMENTAL, pairs, params(0.75, 0.975))
 
 
-def test_essential_large_pairs(oracle, gcr):
-    pairs = [S.two_view_pair(420 + i, n=n, inlier_ratio=r) for i, (n, r) in enumerate(SIZES)]
+@pytest.mark.parametrize("sizes,base", CASES)
+def test_essential_large_pairs(oracle, gcr, sizes, base):
+    pairs = [S.two_view_pair(420 + base + i, n=n, inlier_ratio=r) for i, (n, r) in enumerate(sizes)]
     check_batch(oracle, gcr, _abi.GCR_ESSENTIAL, pairs, params(0.75, 0.1), K=[q["K"] for q in pairs])
