@@ -146,3 +146,25 @@ def test_radius_graph_is_the_exact_ball(oracle):
     ref = (d2 <= 20.0 * 20.0) & ~np.eye(len(c), dtype=bool)
     assert np.array_equal(ref, ref.T) and ref.sum() > 0
     np.testing.assert_array_equal(oracle.radius_counts(c, 20.0), ref.sum(1))
+
+
+@pytest.mark.parametrize("sampler", [3, 4])
+def test_oracle_run_with_probabilities(oracle, sampler):
+    """GCRANSAC::run alone with the importance (3) or AR (4) sampler on the
+    probabilities it is given (a noiseless inlier indicator scaled to maximum
+    1): the homography is recovered; without probabilities the run reports
+    GCR_UNSUPPORTED (the sampler cannot be built) instead of running."""
+    pr = S.homography_pair(11, n=1500)
+    ph = np.where(pr["inlier_gt"], 0.9, 0.1)
+    ph = ph / ph.max()
+    p = _abi.Params(threshold=3.0, confidence=0.99, spatial_coherence_weight=0.975, neighborhood_size=4,
+                    max_iterations=2000, min_iterations=50, sampler=sampler, lo_number=50, seed=3,
+                    sampler_variance=0.1)
+    cells = [160.0, 120.0, 160.0, 120.0]
+    size = oracle.make_size(480, 640, 480, 640)
+    rc, M, mask, st = oracle.run(_abi.GCR_HOMOGRAPHY, pr["corr"], pr["corr"], cells, 4, size, p, seed=3,
+                                 probabilities=ph)
+    assert rc == 0 and mask.sum() >= 0.9 * pr["inlier_gt"].sum()
+    assert S.homography_error(M / M[2, 2], pr["H_gt"]) < 1.0
+    rc2, _, _, _ = oracle.run(_abi.GCR_HOMOGRAPHY, pr["corr"], pr["corr"], cells, 4, size, p, seed=3)
+    assert rc2 == _abi.GCR_UNSUPPORTED
