@@ -43,6 +43,7 @@
 #ifndef GCRANSAC_GB300_GCRANSAC_H_
 #define GCRANSAC_GB300_GCRANSAC_H_
 
+#include <chrono>
 #include <cstddef>
 #include <cstdint>
 #include <limits>
@@ -444,6 +445,7 @@ class GCRANSAC {
     std::vector<uint8_t> mask((size_t)n);
     gcr_stats st{};
     Model out;
+    const auto t_start = std::chrono::steady_clock::now();
     const gcr_status rc =
         probs ? gcr_run_with_probabilities(_ModelEstimator::kind, points_.data, neighborhood_graph_->container->data,
                                            n, cells_, divisions_, &size, probs->data(), &p, out.descriptor.v,
@@ -452,6 +454,10 @@ class GCRANSAC {
                         divisions_, &size, &p, out.descriptor.v, mask.data(), &st);
     if (rc != GCR_OK && rc != GCR_NO_MODEL) throw std::runtime_error(gcr_last_error_string());
     statistics = utils::RANSACStatistics();
+    // wall-clock seconds of the run (GCRANSAC.h:263, 624-626); here the call
+    // includes the copies of the points to the device and of the results back
+    statistics.processing_time =
+        std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
     statistics.main_sampler_name = main_sampler_->getName();
     statistics.local_optimizer_sampler_name = local_optimization_sampler_->getName();
     statistics.iteration_number = (size_t)st.iteration_number;
