@@ -8,8 +8,18 @@ learned-proposal batched form: each step replays two CUDA graphs, the proposal
 (one persistent PROSAC launch with a 50-iteration budget, plus the mask
 mapping); the plain form (uniform sampler, the reference's 10000-iteration
 budget, one persistent launch) is timed on the same pairs and reported under
-`plain`, with both median model errors. The other workloads (`homography`,
-`fundamental`, `essential`) time one persistent engine launch per step.
+`plain`, with both median model errors. `equal_error` sweeps the plain form's
+iteration budget on a subset of the same pairs and compares the two forms at
+equal median model error.
+
+The default run also measures the other workloads with a few steps each and
+reports them under `workloads`: `homography` (2000 correspondences),
+`fundamental` (5000, P-NAPSAC), `essential` (batched, 200-8000, MAGSAC++) and
+`serving` (4096 pairs split across H / F / E, 2000-40000 correspondences,
+learned and plain forms on three streams, per-pair latency percentiles). Each
+carries its own `value`, `e2e`, `cpu_baseline` and median model error.
+`--workload X` makes X the headline instead.
+
 Correspondences are resident in HBM for `value` (CUDA events on the launching
 stream, L2 flushed between steps by a 256 MiB write); `e2e` is the same metric
 through the public API with host buffers, host<->device copies included.
@@ -17,7 +27,8 @@ through the public API with host buffers, host<->device copies included.
 oracle, plain method) on all host cores instead.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gcr|reference]
-                  [--workload learned|homography|fundamental|essential] [--pairs P]
+                  [--workload learned|serving|homography|fundamental|essential] [--pairs P]
+                  [--no-side] [--side-steps S] [--no-sweep]
 """
 import argparse
 import ctypes
@@ -33,7 +44,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "graph-cut-ransac_gb300"))
 
-from pygcransac import _abi, synthetic as S  # noqa: E402
+from pygcransac import _abi, autotune, synthetic as S  # noqa: E402
 
 METRIC = "image pairs/sec at equal model error; learned vs plain GC-RANSAC on 1 GB300"
 
@@ -64,7 +75,27 @@ WORKLOADS = {
     # with a 50-iteration budget. Same threshold, grid, lambda and LO.
     "learned": dict(kind=_abi.GCR_FUNDAMENTAL, n=4000, ratio=(0.05, 0.10), threshold=0.75, sampler=0, grid=8,
                     lam=0.975, pairs=1216, learned_iters=50),
+    # mixed serving batch: pairs split evenly across H / F / E (pair i has kind
+    # i mod 3), correspondences log-uniform over 2k-40k, inliers uniform over
+    # 5-60 %, 16^4 grid, the learned proposal for every kind; MSAC; plain
+    # form: uniform sampler, 10000 iterations; learned form: PROSAC on the
+    # learned order, 50 iterations
+    "serving": dict(kind=None, n=(2000, 40000), ratio=(0.05, 0.60), threshold=None, sampler=0, grid=16,
+                    lam=None, pairs=4096, learned_iters=50),
 }
+
+SERVING_KINDS = [  # (generator, kind, threshold, lambda)
+    ("homography", _abi.GCR_HOMOGRAPHY, 3.0, 0.975),
+    ("fundamental", _abi.GCR_FUNDAMENTAL, 0.75, 0.975),
+    ("essential", _abi.GCR_ESSENTIAL, 0.75, 0.1),
+]
+
+# launch shapes the serving mix's autotuning tries (a subset, to keep the
+# calibration of six batches short)
+SERVING_CANDIDATES = ((256, 2, 0), (256, 2, 1), (256, 1, 1), (64, 2, 1))
+
+# plain-form iteration budgets of the equal-error comparison
+SWEEP_BUDGETS = (10000, 30000, 100000, 300000, 1000000)
 
 CHECKPOINT = os.path.join(ROOT, "graph-cut-ransac_gb300", "pygcransac", "weights", "proposal_fundamental.gcrl")
 
@@ -79,9 +110,7 @@ def _gen_pair(job):
     return pr["corr"], pr["size"], pr
 
 
-def build_pairs(workload, pairs, seed0):
-    """Returns (corr, offsets, sizes, ground truths, K [P, 18] or None)."""
-    w = WORKLOADS[workload]
+def _draw_sizes(w, pairs, seed0):
     if isinstance(w["n"], tuple) or isinstance(w["ratio"], tuple):
         rng = np.random.Generator(np.random.PCG64(seed0 + 7919))
         ns = (np.exp(rng.uniform(np.log(w["n"][0]), np.log(w["n"][1]), pairs)).astype(int)
@@ -90,13 +119,22 @@ def build_pairs(workload, pairs, seed0):
     else:
         ns = np.full(pairs, w["n"])
         ratios = np.full(pairs, w["ratio"])
-    jobs = [(workload, seed0 + i, int(ns[i]), float(ratios[i])) for i in range(pairs)]
-    if pairs >= 256:
+    return ns, ratios
+
+
+def _generate(jobs):
+    if len(jobs) >= 256:
         import multiprocessing as mp
         with mp.get_context("spawn").Pool(max(1, min(16, os.cpu_count() or 1))) as pool:
-            out = pool.map(_gen_pair, jobs, chunksize=16)
-    else:
-        out = [_gen_pair(j) for j in jobs]
+            return pool.map(_gen_pair, jobs, chunksize=16)
+    return [_gen_pair(j) for j in jobs]
+
+
+def build_pairs(workload, pairs, seed0):
+    """Returns (corr, offsets, sizes, ground truths, K [P, 18] or None)."""
+    w = WORKLOADS[workload]
+    ns, ratios = _draw_sizes(w, pairs, seed0)
+    out = _generate([(workload, seed0 + i, int(ns[i]), float(ratios[i])) for i in range(pairs)])
     corr = [c for c, _, _ in out]
     sizes = [z for _, z, _ in out]
     gts = [g for _, _, g in out]
@@ -107,12 +145,40 @@ def build_pairs(workload, pairs, seed0):
     return np.ascontiguousarray(np.concatenate(corr), np.float64), offsets, np.array(sizes), gts, K
 
 
+def build_serving_groups(pairs, seed0):
+    """The serving mix, grouped by kind: a list of dicts (name, kind,
+    threshold, lam, ids, corr, offsets, sizes, K, gts); pair i has kind i mod 3."""
+    w = WORKLOADS["serving"]
+    ns, ratios = _draw_sizes(w, pairs, seed0)
+    out = _generate([(SERVING_KINDS[i % 3][0], seed0 + i, int(ns[i]), float(ratios[i])) for i in range(pairs)])
+    groups = []
+    for k, (name, kind, thr, lam) in enumerate(SERVING_KINDS):
+        ids = np.arange(k, pairs, 3)
+        c = [out[i][0] for i in ids]
+        off = np.zeros(len(ids) + 1, np.int64)
+        off[1:] = np.cumsum([len(x) for x in c])
+        gts = [out[i][2] for i in ids]
+        K = None
+        if kind == _abi.GCR_ESSENTIAL:
+            K = np.ascontiguousarray([np.concatenate([g["K"].ravel(), g["K"].ravel()]) for g in gts])
+        groups.append(dict(name=name, kind=kind, threshold=thr, lam=lam, ids=ids,
+                           corr=np.ascontiguousarray(np.concatenate(c), np.float64), offsets=off,
+                           sizes=np.array([out[i][1] for i in ids]), K=K, gts=gts))
+    return groups
+
+
 def params_for(workload, seed=0):
     w = WORKLOADS[workload]
     return _abi.Params(threshold=w["threshold"], confidence=0.99, spatial_coherence_weight=w["lam"],
                        neighborhood_size=w["grid"], max_iterations=10000, min_iterations=50,
                        sampler=w["sampler"], neighborhood=0, lo_number=50, seed=seed,
                        scoring=w.get("scoring", _abi.GCR_SCORING_MSAC))
+
+
+def serving_params(g, iters, grid=16):
+    return _abi.Params(threshold=g["threshold"], confidence=0.99, spatial_coherence_weight=g["lam"],
+                       neighborhood_size=grid, max_iterations=iters, min_iterations=min(50, iters), sampler=0,
+                       neighborhood=0, lo_number=50, seed=0, scoring=_abi.GCR_SCORING_MSAC)
 
 
 def size_array(sizes):
@@ -133,6 +199,21 @@ def model_errors(workload, models, gts, limit=64):
     if workload == "essential":
         return [S.essential_error(m, g) for m, g in zip(models, gts)]
     return []
+
+
+def serving_errors(name, models, gts):
+    if name == "homography":
+        return [S.homography_error(m / m[2, 2] if abs(m[2, 2]) > 1e-12 else m, g["H_gt"] if isinstance(g, dict)
+                                   else g) for m, g in zip(models, gts)]
+    if name == "fundamental":
+        return [S.fundamental_error(m, g, n=100) for m, g in zip(models, gts)]
+    return [S.essential_error(m, g) for m, g in zip(models, gts)]
+
+
+def equal_error(e_plain, e_learned):
+    """The plain form's median error is no worse than the learned form's, within
+    5 % relative or 0.05 absolute (px or deg)."""
+    return e_plain <= e_learned * 1.05 or e_plain <= e_learned + 0.05
 
 
 class ClockSampler:
@@ -245,15 +326,18 @@ def cpu_baseline(workload, corr, offsets, sizes, p, K=None, target_s=10.0, max_p
     return cpu_baseline_kind(WORKLOADS[workload]["kind"], corr, offsets, sizes, p, K, target_s, max_pairs)
 
 
-def cpu_baseline_kind(kind, corr, offsets, sizes, p, K=None, target_s=10.0, max_pairs=1 << 30):
+def cpu_baseline_kind(kind, corr, offsets, sizes, p, K=None, target_s=10.0, max_pairs=1 << 30, stride=1):
+    """`stride` > 1 samples every stride-th pair of the batch (a stratified
+    sample when the batch is in random size order)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     threads = os.cpu_count() or 1
     P = len(offsets) - 1
+    pool = np.arange(0, P, max(1, stride))
 
     def run(k):
-        # k pairs, cycling over the step's batch when k exceeds it
-        idx = np.arange(k) % P
+        # k pairs, cycling over the sampled pairs when k exceeds them
+        idx = pool[np.arange(k) % len(pool)]
         lens = np.diff(offsets)[idx]
         off = np.zeros(k + 1, np.int64)
         off[1:] = np.cumsum(lens)
@@ -267,7 +351,8 @@ def cpu_baseline_kind(kind, corr, offsets, sizes, p, K=None, target_s=10.0, max_
     k2 = int(min(max_pairs, max(k, rate * target_s)))
     if k2 > k:
         k, t = run(k2)
-    return k / t, threads, f"{k} pairs cycling over the step's batch ({t:.1f} s)"
+    what = "pairs cycling over the step's batch" if stride <= 1 else f"pairs cycling over every {stride}th pair"
+    return k / t, threads, f"{k} {what} ({t:.1f} s)"
 
 
 def timed_steps(torch, fns, steps, flush, stream):
@@ -285,6 +370,85 @@ def timed_steps(torch, fns, steps, flush, stream):
         for k in range(len(fns)):
             parts[k] += ev[k].elapsed_time(ev[k + 1])
     return parts
+
+
+def vp(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def tune_shape(torch, args, kind, d_corr, offsets, sizes, params, seeds, K=None, candidates=None):
+    """Autotunes the engine's launch shape on the first pairs of the batch
+    (results are identical for every shape) and records it in the tuning
+    cache. Returns the gcr_tuning table for the whole batch and a summary."""
+    P = len(offsets) - 1
+    n = min(P, args.tune_pairs)
+    max_n = int(np.diff(offsets).max())
+    if args.no_tune:
+        return [], {"shape": "defaults (256 calls per batch, CTAs per SM as the occupancy allows, caller's order)"}
+    best, timings = autotune.tune(kind, d_corr, offsets[:n + 1], sizes[:n], params, seeds[:n],
+                                  None if K is None else K[:n], candidates=candidates or autotune.CANDIDATES,
+                                  repeats=1)
+    gpu = autotune.gpu_name()
+    try:
+        autotune.save_cache(autotune.record(autotune.load_cache(), gpu, kind, max_n, best, timings))
+    except OSError:
+        pass
+    row = _abi.Tuning(kind=int(kind), max_n=max_n, batch_calls=best[0], ctas_per_sm=best[1], order=best[2],
+                      reserved=0)
+    summary = {"batch_calls": best[0], "ctas_per_sm": best[1], "order": ["caller", "largest first"][best[2]],
+               "calibration_pairs": n, "candidates": len(timings),
+               "calibration_ms": {f"{c[0]}/{c[1]}/{c[2]}": round(t, 3) for c, t in sorted(timings.items())}}
+    return [row], summary
+
+
+def plain_budget_sweep(torch, lib, d_corr, offsets, sizes, gts, seeds, P, budgets, flush, learned_eval):
+    """The plain form (uniform sampler) on the first P pairs at each iteration
+    budget: pairs/s of one launch and the median model error; the learned form
+    on the same pairs through `learned_eval(P) -> (pairs/s, median error)`."""
+    off = np.ascontiguousarray(offsets[:P + 1])
+    total = int(off[-1])
+    ctx = ctypes.c_void_p()
+    assert lib.gcr_context_create(ctypes.byref(ctx)) == 0, _abi.last_error()
+    pm = torch.zeros(P * 9, dtype=torch.float64, device="cuda")
+    pk = torch.zeros(total, dtype=torch.uint8, device="cuda")
+    ps = torch.zeros(P * _abi.STATS_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    sz = size_array(sizes[:P])
+    stream = torch.cuda.current_stream()
+    rows = []
+    for it in budgets:
+        p = params_for("learned")
+        p.max_iterations = int(it)
+        flush.fill_(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        rc = lib.gcr_batch_run_device(ctx, _abi.GCR_FUNDAMENTAL, P, vp(d_corr), _abi.ptr(off), None, _abi.ptr(sz),
+                                      ctypes.byref(p), _abi.ptr(seeds[:P]), vp(pm), vp(pk), vp(ps),
+                                      ctypes.c_void_p(stream.cuda_stream))
+        assert rc == 0, _abi.last_error()
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        st = np.frombuffer(ps.cpu().numpy().tobytes(), _abi.STATS_DTYPE)
+        err = model_errors("learned", pm.cpu().numpy().reshape(P, 3, 3), gts[:P])
+        rows.append({"max_iterations": int(it), "pairs_per_s": P / ms * 1e3, "median_model_error": float(np.median(err)),
+                     "iterations_mean": float(st["iteration_number"].mean())})
+    lib.gcr_context_destroy(ctx)
+    v_l, e_l = learned_eval(P)
+    reached = [r for r in rows if equal_error(r["median_model_error"], e_l)]
+    out = {"pairs": P, "plain": rows, "learned": {"pairs_per_s": v_l, "median_model_error": e_l},
+           "criterion": "plain median error <= learned median error x 1.05 or + 0.05 px"}
+    if reached:
+        r = reached[0]
+        out["plain_budget_at_equal_error"] = r["max_iterations"]
+        out["learned_over_plain_at_equal_error"] = v_l / r["pairs_per_s"]
+    else:
+        r = rows[-1]
+        out["plain_budget_at_equal_error"] = None
+        out["learned_over_plain_lower_bound"] = v_l / r["pairs_per_s"]
+        out["note"] = (f"plain did not reach equal error at <= {r['max_iterations']} iterations "
+                       f"(median {r['median_model_error']:.3g} px vs learned {e_l:.3g} px); the ratio to the "
+                       f"largest budget measured is a lower bound of the ratio at equal error")
+    return out
 
 
 def run_learned(args, P, w, cfg, world, rank, local_rank, dist, torch):
@@ -314,10 +478,11 @@ def run_learned(args, P, w, cfg, world, rank, local_rank, dist, torch):
     ctx_p = ctypes.c_void_p()
     assert lib.gcr_context_create(ctypes.byref(ctx_p)) == 0, _abi.last_error()
     p_plain = params_for(args.workload)
+    rows, cfg["tuning_plain"] = tune_shape(torch, args, kind, d_corr, offsets, sizes, p_plain, seeds)
+    autotune.set_table(ctx_p, rows)
     pm = torch.zeros(P * 9, dtype=torch.float64, device="cuda")
     pk = torch.zeros(total, dtype=torch.uint8, device="cuda")
     ps = torch.zeros(P * _abi.STATS_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
-    vp = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
     sz = size_array(sizes)
     rc = lib.gcr_batch_prepare(ctx_p, kind, P, vp(d_corr), _abi.ptr(offsets), None, _abi.ptr(sz),
                                ctypes.byref(p_plain), _abi.ptr(seeds), vp(pm), vp(pk), vp(ps))
@@ -335,6 +500,14 @@ def run_learned(args, P, w, cfg, world, rank, local_rank, dist, torch):
     p_l.lo_number = args.learned_lo
     cfg["learned_lo_number"] = args.learned_lo
     b = LearnedBatch(net, kind, d_corr, offsets, sizes, p_l, seeds)
+    # the learned engine's shape, tuned on the ordered correspondences
+    assert lib.gcr_learned_propose(vp(d_corr), vp(b.d_off), vp(b.d_sz), P, b.max_n, total, vp(net.bf16),
+                                   vp(b.d_feat), vp(b.d_logits), vp(b.d_sorted), vp(b.d_perm), None) == 0
+    torch.cuda.synchronize()
+    p_tune = _abi.Params(**{f: getattr(p_l, f) for f, _ in p_l._fields_})
+    p_tune.sampler = 1
+    rows, cfg["tuning"] = tune_shape(torch, args, kind, b.d_sorted, offsets, sizes, p_tune, seeds)
+    autotune.set_table(b.ctx, rows)
     b.prepare()
     g_prop, g_eng = torch.cuda.CUDAGraph(), torch.cuda.CUDAGraph()
     sp = ctypes.c_void_p(cap.cuda_stream)
@@ -397,24 +570,44 @@ def run_learned(args, P, w, cfg, world, rank, local_rank, dist, torch):
         e2e_step()
         e2e_t += time.perf_counter() - t0
     e2e_value, _ = aggregate_rate(P * args.steps, e2e_t, world, dist, "cuda")
+
+    # equal model error: plain budgets against the learned form on one wave of pairs
+    sweep = None
+    if not args.no_sweep:
+        def learned_eval(n):
+            bl = LearnedBatch(net, kind, d_corr, offsets[:n + 1], sizes[:n], p_l, seeds[:n])
+            autotune.set_table(bl.ctx, rows)
+            bl.prepare()
+            bl.launch()
+            torch.cuda.synchronize()
+            flush.fill_(1)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            bl.launch()
+            e1.record(stream)
+            e1.synchronize()
+            ml, _, _ = bl.results()
+            bl.close()
+            return n / e0.elapsed_time(e1) * 1e3, float(np.median(model_errors(args.workload, ml, gts[:n])))
+        sweep = plain_budget_sweep(torch, lib, d_corr, offsets, sizes, gts, seeds, min(P, args.sweep_pairs),
+                                   args.sweep_budgets, flush, learned_eval)
     if rank != 0:
         b.close()
         lib.gcr_context_destroy(ctx_p)
-        if dist:
-            dist.destroy_process_group()
-        return
+        return None
     n_per = np.diff(offsets)
     peak = fp32_peak_tflops(torch)
     eng_s = eng_ms / args.steps / 1e3
     flops = float(np.sum(stats["models_scored"] * n_per)) * FLOP_PER_RESIDUAL[args.workload]
     mlp_flops = 2.0 * total * (32 * 128 + 2 * 128 * 128 + 128)
     achieved = flops / eng_s / 1e12
-    traffic = fp64_work = None
+    traffic = fp64_work = traffic_note = None
     tp = os.path.join(ROOT, "profiles", "traffic_learned.json")
     if os.path.exists(tp):
         t = json.load(open(tp))
         traffic = t["bytes_per_pair"] * P
         fp64_work = t["fp64_flop_per_pair"] * P
+        traffic_note = f"ncu capture of a {t.get('pairs', 152)}-pair launch, scaled to {P} pairs by the pair count"
     peak64 = fp64_peak_tflops(torch)
     line = {
         "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
@@ -427,10 +620,11 @@ def run_learned(args, P, w, cfg, world, rank, local_rank, dist, torch):
                   "median_model_error": float(np.median(err_p)),
                   "iterations_mean": float(np.mean(plain_stats["iteration_number"]))},
         "learned_over_plain": value / plain_value,
+        "equal_error": sweep,
         "error_unit": "px, mean Sampson distance of 100 noise-free ground-truth correspondences per pair",
         "proposal_ms_per_step": prop_ms / args.steps, "engine_ms_per_step": eng_ms / args.steps,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak if peak else None, "traffic": traffic,
+                     "frac": achieved / peak if peak else None, "traffic": traffic, "traffic_source": traffic_note,
                      "peak_source": "cuBLAS SGEMM 8192^3, TF32 off, measured in this run",
                      "kernel": "pair engine (PROSAC, learned order)",
                      "work": f"{FLOP_PER_RESIDUAL[args.workload]} FLOP x models_scored x N per pair"},
@@ -448,11 +642,371 @@ def run_learned(args, P, w, cfg, world, rank, local_rank, dist, torch):
         v, cores, sample = cpu_baseline(args.workload, corr, offsets, sizes, p_plain, None)
         line["cpu_baseline"] = {"value": v, "unit": "pairs/s", "cores": cores, "kind": "port",
                                 "sample": sample + "; plain method (uniform sampler, 10000 iterations)"}
-    print(json.dumps(line))
     b.close()
     lib.gcr_context_destroy(ctx_p)
+    return line
+
+
+def run_kind(args, workload, P, steps, warmup, world, rank, local_rank, dist, torch, clocks_on=True):
+    """One persistent engine launch per step (single model kind), replayed from
+    a CUDA graph; `e2e` through gcr_find_batch with pinned host buffers."""
+    w = WORKLOADS[workload]
+    lib = _abi.load()
+    corr, offsets, sizes, gts, K, seeds = replica_shard(workload, P, rank)
+    p = params_for(workload)
+    kind = w["kind"]
+    szs = size_array(sizes)
+    d_corr = torch.from_numpy(corr).cuda()
+    d_models = torch.zeros(P * 9, dtype=torch.float64, device="cuda")
+    d_masks = torch.zeros(int(offsets[-1]), dtype=torch.uint8, device="cuda")
+    d_stats = torch.zeros(P * _abi.STATS_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    ctx = ctypes.c_void_p()
+    assert lib.gcr_context_create(ctypes.byref(ctx)) == 0, _abi.last_error()
+    stream = torch.cuda.current_stream()
+    rows, tuning = tune_shape(torch, args, kind, d_corr, offsets, sizes, p, seeds, K)
+    autotune.set_table(ctx, rows)
+
+    # one persistent launch per batch (plus the K^-1 normalisation for E),
+    # prepared once and recorded into a CUDA graph; a step is one replay
+    rc = lib.gcr_batch_prepare(ctx, kind, P, vp(d_corr), _abi.ptr(offsets), _abi.ptr(K), _abi.ptr(szs),
+                               ctypes.byref(p), _abi.ptr(seeds), vp(d_models), vp(d_masks), vp(d_stats))
+    assert rc == 0, _abi.last_error()
+    graph = torch.cuda.CUDAGraph()
+    cap = torch.cuda.Stream()
+    with torch.cuda.stream(cap):
+        with torch.cuda.graph(graph, stream=cap):
+            rc = lib.gcr_batch_launch(ctx, ctypes.c_void_p(cap.cuda_stream))
+    assert rc == 0, _abi.last_error()
+    launches_per_step = int(lib.gcr_last_launch_count())
+
+    for _ in range(warmup):
+        graph.replay()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local_rank) if clocks_on else None
     if dist:
-        dist.destroy_process_group()
+        dist.barrier()
+    torch.cuda.synchronize()
+    if clocks:
+        clocks.start()
+    total_ms = sum(timed_steps(torch, [graph.replay], steps, flush, stream))
+    torch.cuda.synchronize()
+    clk = clocks.stop() if clocks else None
+    value, _ = aggregate_rate(P * steps, total_ms / 1e3, world, dist, "cuda")
+    if dist:
+        dist.barrier()
+
+    stats = np.frombuffer(d_stats.cpu().numpy().tobytes(), _abi.STATS_DTYPE)
+    models = d_models.cpu().numpy().reshape(P, 3, 3)
+    n_per = np.diff(offsets)
+    flops = float(np.sum(stats["models_scored"] * n_per)) * FLOP_PER_RESIDUAL[workload]
+    errs = model_errors(workload, models, gts)
+
+    # end to end through the host-buffer entry: pinned inputs, copies timed
+    h_corr = torch.from_numpy(corr).pin_memory()
+    h_models = torch.zeros(P * 9, dtype=torch.float64).pin_memory()
+    h_masks = torch.zeros(int(offsets[-1]), dtype=torch.uint8).pin_memory()
+    h_stats = torch.zeros(P * _abi.STATS_DTYPE.itemsize, dtype=torch.uint8).pin_memory()
+
+    def e2e_step():
+        rc = lib.gcr_find_batch(kind, P, vp(h_corr), _abi.ptr(offsets), _abi.ptr(K), _abi.ptr(szs),
+                                ctypes.byref(p), _abi.ptr(seeds), vp(h_models), vp(h_masks), vp(h_stats))
+        assert rc == 0, _abi.last_error()
+
+    e2e_step()
+    e2e_t = 0.0
+    for _ in range(steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_t += time.perf_counter() - t0
+    e2e_value, e2e_t = aggregate_rate(P * steps, e2e_t, world, dist, "cuda")
+    lib.gcr_context_destroy(ctx)
+    if rank != 0:
+        return None
+    peak = fp32_peak_tflops(torch)
+    achieved = flops / (total_ms / steps / 1e3) / 1e12
+    traffic = fp64_work = traffic_note = None
+    tp = os.path.join(ROOT, "profiles", f"traffic_{workload}.json")
+    if os.path.exists(tp):
+        t = json.load(open(tp))
+        traffic = t["bytes_per_pair"] * P
+        fp64_work = t["fp64_flop_per_pair"] * P
+        traffic_note = f"ncu capture of a {t.get('pairs', 152)}-pair launch, scaled to {P} pairs by the pair count"
+    peak64 = fp64_peak_tflops(torch)
+    line = {
+        "value": value, "unit": "pairs/s", "steps": steps, "warmup": warmup, "ms_per_step": total_ms / steps,
+        "pairs_per_step": P, "config": {"tuning": tuning},
+        "median_model_error": float(np.median(errs)) if errs else None,
+        "status_ok_fraction": float(np.mean(stats["status"] == 0)),
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak if peak else None, "traffic": traffic, "traffic_source": traffic_note,
+                     "peak_source": "cuBLAS SGEMM 8192^3, TF32 off, measured in this run",
+                     "work": f"{FLOP_PER_RESIDUAL[workload]} FLOP x models_scored x N per pair"},
+        # the FP64 pipe is the unit the kernel keeps busiest (solvers, LO fits):
+        # executed FP64 FLOP per pair from the ncu capture in profiles/, over the
+        # live DGEMM peak
+        "roofline_fp64": None if fp64_work is None else {
+            "bound": "fp64", "achieved": fp64_work / (total_ms / steps / 1e3) / 1e12, "peak": peak64,
+            "unit": "TFLOP/s", "frac": fp64_work / (total_ms / steps / 1e3) / 1e12 / peak64,
+            "peak_source": "cuBLAS DGEMM 4096^3, measured in this run",
+            "work": "FP64 FLOP per pair executed by the kernel (ncu SASS counts, FMA = 2) x pairs"},
+        "e2e": {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": int(corr.nbytes),
+                "d2h_bytes_per_step": int(P * 9 * 8 + offsets[-1] + P * _abi.STATS_DTYPE.itemsize)},
+        "gpu_launches": int(launches_per_step * steps),
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline and world == 1:
+        v, cores, sample = cpu_baseline(workload, corr, offsets, sizes, p, K,
+                                        target_s=10.0 if workload == args.workload else 6.0)
+        line["cpu_baseline"] = {"value": v, "unit": "pairs/s", "cores": cores, "kind": "port", "sample": sample}
+    return line
+
+
+def run_serving(args, P, steps, warmup, world, rank, local_rank, dist, torch, clocks_on=True):
+    """Mixed H / F / E batch: one engine launch per kind, the three kinds on
+    their own streams. Learned form = proposal + PROSAC engine + mask mapping
+    per kind (one CUDA graph each); plain form = uniform-sampler engine launch
+    per kind (one CUDA graph each). Per-pair service times come from the
+    engine's global-timer stamps.
+
+    Every device buffer a captured graph reads or writes is owned by the
+    kind's record below for the whole run: a graph keeps raw addresses, so a
+    buffer released to the caching allocator (and returned to the driver by
+    the empty_cache() that graph capture performs) would leave the replay
+    writing into freed memory."""
+    from pygcransac.learned import LearnedBatch, LearnedProposal
+    lib = _abi.load()
+    w = WORKLOADS["serving"]
+    groups = build_serving_groups(P, 1000003 * rank)
+    net = LearnedProposal.load(CHECKPOINT)
+    cfg = dict(network="the fundamental-matrix checkpoint, applied to every kind",
+               kinds={g["name"]: dict(pairs=int(len(g["ids"])), threshold=g["threshold"],
+                                      spatial_coherence_weight=g["lam"]) for g in groups},
+               learned_iterations=w["learned_iters"], correspondences="log-uniform 2000-40000",
+               inlier_ratio="uniform 5-60 %", grid=w["grid"])
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    main = torch.cuda.current_stream()
+    streams = [torch.cuda.Stream() for _ in groups]
+    recs = []
+    for gi, g in enumerate(groups):
+        n_pairs, total = len(g["ids"]), int(g["offsets"][-1])
+        rec = dict(group=g, stream=streams[gi])
+        rec["d_corr"] = torch.from_numpy(g["corr"]).cuda()
+        rec["times_p"] = torch.zeros(2 * n_pairs, dtype=torch.int64, device="cuda")
+        rec["times_l"] = torch.zeros(2 * n_pairs, dtype=torch.int64, device="cuda")
+        rec["pm"] = torch.zeros(n_pairs * 9, dtype=torch.float64, device="cuda")
+        rec["pk"] = torch.zeros(total, dtype=torch.uint8, device="cuda")
+        rec["ps"] = torch.zeros(n_pairs * _abi.STATS_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+        rec["seeds"] = np.arange(n_pairs, dtype=np.uint64) + np.uint64(gi * 1000003)
+        ctx = ctypes.c_void_p()
+        assert lib.gcr_context_create(ctypes.byref(ctx)) == 0
+        rec["ctx"] = ctx
+        assert lib.gcr_context_set_pair_times(ctx, vp(rec["times_p"])) == 0
+        pp = serving_params(g, 10000, w["grid"])
+        rows, cfg.setdefault("tuning_plain", {})[g["name"]] = tune_shape(
+            torch, args, g["kind"], rec["d_corr"], g["offsets"], g["sizes"], pp, rec["seeds"], g["K"],
+            candidates=SERVING_CANDIDATES)
+        autotune.set_table(ctx, rows)
+        rc = lib.gcr_batch_prepare(ctx, g["kind"], n_pairs, vp(rec["d_corr"]), _abi.ptr(g["offsets"]),
+                                   _abi.ptr(g["K"]), _abi.ptr(size_array(g["sizes"])), ctypes.byref(pp),
+                                   _abi.ptr(rec["seeds"]), vp(rec["pm"]), vp(rec["pk"]), vp(rec["ps"]))
+        assert rc == 0, _abi.last_error()
+        rec["g_plain"] = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(streams[gi]):
+            with torch.cuda.graph(rec["g_plain"], stream=streams[gi]):
+                assert lib.gcr_batch_launch(ctx, ctypes.c_void_p(streams[gi].cuda_stream)) == 0
+        pl = serving_params(g, w["learned_iters"], w["grid"])
+        b = LearnedBatch(net, g["kind"], rec["d_corr"], g["offsets"], g["sizes"], pl, rec["seeds"], g["K"])
+        assert lib.gcr_context_set_pair_times(b.ctx, vp(rec["times_l"])) == 0
+        assert lib.gcr_learned_propose(vp(rec["d_corr"]), vp(b.d_off), vp(b.d_sz), b.P, b.max_n, b.total,
+                                       vp(net.bf16), vp(b.d_feat), vp(b.d_logits), vp(b.d_sorted), vp(b.d_perm),
+                                       None) == 0
+        torch.cuda.synchronize()
+        pt = _abi.Params(**{f: getattr(pl, f) for f, _ in pl._fields_})
+        pt.sampler = 1
+        rows, cfg.setdefault("tuning", {})[g["name"]] = tune_shape(
+            torch, args, g["kind"], b.d_sorted, g["offsets"], g["sizes"], pt, rec["seeds"], g["K"],
+            candidates=SERVING_CANDIDATES)
+        autotune.set_table(b.ctx, rows)
+        b.prepare()
+        rec["batch"] = b
+        rec["g_learned"] = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(streams[gi]):
+            with torch.cuda.graph(rec["g_learned"], stream=streams[gi]):
+                rec["launches_learned"] = b.launch(streams[gi])
+        recs.append(rec)
+
+    def step(key):
+        start = torch.cuda.Event(enable_timing=True)
+        stop = torch.cuda.Event(enable_timing=True)
+        flush.fill_(1)
+        start.record(main)
+        for r in recs:
+            r["stream"].wait_event(start)
+            with torch.cuda.stream(r["stream"]):
+                r[key].replay()
+        for r in recs:
+            e = torch.cuda.Event()
+            e.record(r["stream"])
+            main.wait_event(e)
+        stop.record(main)
+        stop.synchronize()
+        return start.elapsed_time(stop)
+
+    def lat(key):
+        t = np.concatenate([r[key].cpu().numpy().reshape(-1, 2) for r in recs]).astype(np.float64)
+        service = (t[:, 1] - t[:, 0]) / 1e6
+        done = (t[:, 1] - t[:, 0].min()) / 1e6
+        return {"service_ms_p50": float(np.percentile(service, 50)), "service_ms_p99": float(np.percentile(service, 99)),
+                "completion_ms_p50": float(np.percentile(done, 50)), "completion_ms_p99": float(np.percentile(done, 99))}
+
+    for _ in range(warmup):
+        step("g_plain")
+        step("g_learned")
+    plain_ms = sum(step("g_plain") for _ in range(steps))
+    plain_lat = lat("times_p")
+    clocks = ClockSampler(local_rank) if clocks_on else None
+    torch.cuda.synchronize()
+    if clocks:
+        clocks.start()
+    learned_ms = sum(step("g_learned") for _ in range(steps))
+    clk = clocks.stop() if clocks else None
+    learned_lat = lat("times_l")
+    value, _ = aggregate_rate(P * steps, learned_ms / 1e3, world, dist, "cuda")
+    plain_value, _ = aggregate_rate(P * steps, plain_ms / 1e3, world, dist, "cuda")
+    errs_l, errs_p, ok_l, ok_p = {}, {}, [], []
+    for r in recs:
+        g = r["group"]
+        ml, _, stl = r["batch"].results()
+        mp = r["pm"].cpu().numpy().reshape(-1, 3, 3)
+        stp = np.frombuffer(r["ps"].cpu().numpy().tobytes(), _abi.STATS_DTYPE)
+        errs_l[g["name"]] = float(np.median(serving_errors(g["name"], ml, g["gts"])))
+        errs_p[g["name"]] = float(np.median(serving_errors(g["name"], mp, g["gts"])))
+        ok_l.append(stl["status"] == 0)
+        ok_p.append(stp["status"] == 0)
+
+    # end to end: pinned host correspondences in, models / masks / stats out
+    for r in recs:
+        b = r["batch"]
+        r["h_corr"] = torch.from_numpy(r["group"]["corr"]).pin_memory()
+        r["h_out"] = (torch.empty(b.P * 9, dtype=torch.float64).pin_memory(),
+                      torch.empty(b.total, dtype=torch.uint8).pin_memory(),
+                      torch.empty(b.P * _abi.STATS_DTYPE.itemsize, dtype=torch.uint8).pin_memory())
+
+    def e2e_step():
+        for r in recs:
+            b, o = r["batch"], r["h_out"]
+            with torch.cuda.stream(r["stream"]):
+                r["d_corr"].copy_(r["h_corr"], non_blocking=True)
+                b.launch(r["stream"])
+                o[0].copy_(b.d_models, non_blocking=True)
+                o[1].copy_(b.d_masks, non_blocking=True)
+                o[2].copy_(b.d_stats, non_blocking=True)
+        torch.cuda.synchronize()
+
+    e2e_step()
+    e2e_t = 0.0
+    for _ in range(steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_t += time.perf_counter() - t0
+    e2e_value, _ = aggregate_rate(P * steps, e2e_t, world, dist, "cuda")
+    line = None
+    if rank == 0:
+        line = {
+            "value": value, "unit": "pairs/s", "steps": steps, "warmup": warmup, "ms_per_step": learned_ms / steps,
+            "pairs_per_step": P, "config": cfg,
+            "median_model_error": errs_l, "status_ok_fraction": float(np.mean(np.concatenate(ok_l))),
+            "latency": learned_lat,
+            "plain": {"value": plain_value, "unit": "pairs/s", "ms_per_step": plain_ms / steps,
+                      "median_model_error": errs_p, "status_ok_fraction": float(np.mean(np.concatenate(ok_p))),
+                      "latency": plain_lat},
+            "learned_over_plain": value / plain_value,
+            "error_unit": "H: RMS transfer px; F: mean Sampson px; E: max(rotation, translation) deg",
+            "e2e": {"value": e2e_value, "unit": "pairs/s",
+                    "h2d_bytes_per_step": int(sum(r["group"]["corr"].nbytes for r in recs)),
+                    "d2h_bytes_per_step": int(sum(o.numel() * o.element_size() for r in recs for o in r["h_out"]))},
+            "gpu_launches": int(sum(r["launches_learned"] for r in recs) * steps),
+            "clocks": clk,
+        }
+        if not args.no_cpu_baseline and world == 1:
+            # the oracle (plain method) per kind on a bounded sample of its pairs
+            rates, samples, cores = [], [], 1
+            for r in recs:
+                g = r["group"]
+                v, cores, sample = cpu_baseline_kind(g["kind"], g["corr"], g["offsets"], g["sizes"],
+                                                     serving_params(g, 10000, w["grid"]), g["K"], target_s=6.0,
+                                                     stride=7)
+                rates.append(v)
+                samples.append(f"{g['name']}: {sample}")
+            line["cpu_baseline"] = {"value": 3.0 / sum(1.0 / v for v in rates), "unit": "pairs/s", "cores": cores,
+                                    "kind": "port", "sample": "; ".join(samples) + "; combined as equal thirds"}
+    for r in recs:
+        lib.gcr_context_destroy(r["ctx"])
+        r["batch"].close()
+    return line
+
+
+def describe(workload, P, world):
+    w = WORKLOADS[workload]
+    if workload == "essential":
+        desc = (f"{workload}: {P} calibrated pairs/step x {w['n'][0]}-{w['n'][1]} (log-uniform) correspondences, "
+                f"{int(w['ratio'][0]*100)}-{int(w['ratio'][1]*100)}% inliers, MAGSAC++")
+    elif workload == "learned":
+        desc = (f"learned: {P} fundamental-matrix pairs/step x {w['n']} correspondences, "
+                f"{int(w['ratio'][0]*100)}-{int(w['ratio'][1]*100)}% inliers; learned order -> PROSAC "
+                f"({w['learned_iters']} iterations) vs plain uniform sampler (10000 iterations)")
+    elif workload == "serving":
+        desc = (f"serving: {P} pairs/step split evenly across H / F / E, 2000-40000 (log-uniform) correspondences, "
+                f"5-60% inliers; learned order -> PROSAC ({w['learned_iters']} iterations) vs plain uniform "
+                f"sampler (10000 iterations), one launch per kind on three streams")
+    else:
+        desc = f"{workload}: {P} pairs/step x {w['n']} correspondences, {int(w['ratio']*100)}% inliers"
+    cfg = {"workload": desc, "pairs_per_step": P, "correspondences": w["n"], "threshold": w["threshold"],
+           "sampler": w["sampler"], "grid": w["grid"], "spatial_coherence_weight": w["lam"],
+           "scoring": "MAGSAC++" if w.get("scoring") == _abi.GCR_SCORING_MAGSAC else "MSAC",
+           "launch": "one persistent engine launch per step, replayed from a CUDA graph",
+           "l2": "flushed between steps (256 MiB write)",
+           "parallelism": f"replicas x{world}"}
+    return cfg
+
+
+def reference_arm(args, P, cfg):
+    """The CPU restatement of the reference path (plain method) on all host
+    cores, on bounded samples of the workload."""
+    w = WORKLOADS[args.workload]
+    vals = []
+    if args.workload == "serving":
+        groups = build_serving_groups(P, 0)
+        for it in range(args.warmup + args.steps):
+            rates, samples = [], []
+            for g in groups:
+                v, cores, sample = cpu_baseline_kind(g["kind"], g["corr"], g["offsets"], g["sizes"],
+                                                     serving_params(g, 10000, w["grid"]), g["K"],
+                                                     target_s=1.0 if it < args.warmup else 4.0, stride=7)
+                rates.append(v)
+                samples.append(f"{g['name']}: {sample}")
+            if it >= args.warmup:
+                vals.append(3.0 / sum(1.0 / r for r in rates))
+        sample = "; ".join(samples) + "; combined as equal thirds"
+    else:
+        corr, offsets, sizes, gts, K = build_pairs(args.workload, P, 0)
+        p = params_for(args.workload)
+        for _ in range(args.warmup):
+            cpu_baseline(args.workload, corr, offsets, sizes, p, K, target_s=1.0, max_pairs=64)
+        for _ in range(args.steps):
+            v, cores, sample = cpu_baseline(args.workload, corr, offsets, sizes, p, K, target_s=8.0)
+            vals.append(v)
+    v = float(np.median(vals))
+    return {"metric": METRIC, "value": v, "unit": "pairs/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * P / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg, "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "pairs/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
 def main():
@@ -466,49 +1020,26 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--learned-lo", type=int, default=50,
                     help="LO trials of the learned form (the reference's default is 50)")
+    ap.add_argument("--no-side", action="store_true", help="skip the other workloads")
+    ap.add_argument("--side-steps", type=int, default=3, help="timed steps of each other workload")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the plain-budget sweep of the learned workload")
+    ap.add_argument("--sweep-pairs", type=int, default=304)
+    ap.add_argument("--sweep-budgets", default=",".join(str(b) for b in SWEEP_BUDGETS))
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape (no autotuning)")
+    ap.add_argument("--tune-pairs", type=int, default=304, help="calibration pairs of the autotuner")
     args = ap.parse_args()
+    args.sweep_budgets = [int(float(x)) for x in args.sweep_budgets.split(",") if x]
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     w = WORKLOADS[args.workload]
     P = args.pairs or w["pairs"]
-    if args.workload == "essential":
-        desc = (f"{args.workload}: {P} calibrated pairs/step x {w['n'][0]}-{w['n'][1]} (log-uniform) correspondences, "
-                f"{int(w['ratio'][0]*100)}-{int(w['ratio'][1]*100)}% inliers, MAGSAC++")
-    elif args.workload == "learned":
-        desc = (f"learned: {P} fundamental-matrix pairs/step x {w['n']} correspondences, "
-                f"{int(w['ratio'][0]*100)}-{int(w['ratio'][1]*100)}% inliers; learned order -> PROSAC "
-                f"({w['learned_iters']} iterations) vs plain uniform sampler (10000 iterations)")
-    else:
-        desc = f"{args.workload}: {P} pairs/step x {w['n']} correspondences, {int(w['ratio']*100)}% inliers"
-    cfg = {"workload": desc,
-           "pairs_per_step": P, "correspondences": w["n"], "threshold": w["threshold"], "sampler": w["sampler"],
-           "grid": w["grid"], "spatial_coherence_weight": w["lam"],
-           "scoring": "MAGSAC++" if w.get("scoring") == _abi.GCR_SCORING_MAGSAC else "MSAC",
-           "launch": "one persistent engine launch per step, replayed from a CUDA graph",
-           "l2": "flushed between steps (256 MiB write)",
-           "parallelism": f"replicas x{world}"}
+    cfg = describe(args.workload, P, world)
 
     if args.impl == "reference":
-        if rank != 0:
-            return
-        corr, offsets, sizes, gts, K = build_pairs(args.workload, P, 0)
-        p = params_for(args.workload)
-        for _ in range(args.warmup):
-            cpu_baseline(args.workload, corr, offsets, sizes, p, K, target_s=1.0, max_pairs=64)
-        vals = []
-        for _ in range(args.steps):
-            v, cores, sample = cpu_baseline(args.workload, corr, offsets, sizes, p, K, target_s=8.0)
-            vals.append(v)
-        v = float(np.median(vals))
-        print(json.dumps({"metric": METRIC, "value": v, "unit": "pairs/s", "n_gpus": args.gpus,
-                          "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * P / v,
-                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                          "data": "synthetic", "config": cfg, "impl": "reference",
-                          "cpu_baseline": {"value": v, "unit": "pairs/s", "cores": cores, "kind": "port",
-                                           "sample": sample},
-                          "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        if rank == 0:
+            print(json.dumps(reference_arm(args, P, cfg)))
         return
 
     import torch
@@ -519,134 +1050,41 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
 
     if args.workload == "learned":
-        return run_learned(args, P, w, cfg, world, rank, local_rank, dist, torch)
+        line = run_learned(args, P, w, cfg, world, rank, local_rank, dist, torch)
+    elif args.workload == "serving":
+        sub = run_serving(args, P, args.steps, args.warmup, world, rank, local_rank, dist, torch)
+        line = None if sub is None else {"metric": METRIC, **sub}
+    else:
+        sub = run_kind(args, args.workload, P, args.steps, args.warmup, world, rank, local_rank, dist, torch)
+        line = None if sub is None else {"metric": METRIC, **sub}
+    if line is not None:
+        line.update({"n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                     "scaling": "weak", "vs_baseline": None, "data": "synthetic"})
+        line.setdefault("dtype", "fp32 scoring / fp64 solvers" +
+                        (" / bf16 weights, fp32 accumulation (MLP)" if args.workload == "serving" else ""))
+        if args.workload != "learned":
+            line["config"] = {**cfg, **line.get("config", {})}
 
-    lib = _abi.load()
-    corr, offsets, sizes, gts, K, seeds = replica_shard(args.workload, P, rank)
-    p = params_for(args.workload)
-    kind = w["kind"]
-    szs = size_array(sizes)
-    d_corr = torch.from_numpy(corr).cuda()
-    d_models = torch.zeros(P * 9, dtype=torch.float64, device="cuda")
-    d_masks = torch.zeros(int(offsets[-1]), dtype=torch.uint8, device="cuda")
-    d_stats = torch.zeros(P * _abi.STATS_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    ctx = ctypes.c_void_p()
-    assert lib.gcr_context_create(ctypes.byref(ctx)) == 0, _abi.last_error()
-    stream = torch.cuda.current_stream()
-
-    # one persistent launch per batch (plus the K^-1 normalisation for E),
-    # prepared once and recorded into a CUDA graph; a step is one replay
-    rc = lib.gcr_batch_prepare(ctx, kind, P, ctypes.c_void_p(d_corr.data_ptr()), _abi.ptr(offsets), _abi.ptr(K),
-                               _abi.ptr(szs), ctypes.byref(p), _abi.ptr(seeds), ctypes.c_void_p(d_models.data_ptr()),
-                               ctypes.c_void_p(d_masks.data_ptr()), ctypes.c_void_p(d_stats.data_ptr()))
-    assert rc == 0, _abi.last_error()
-    graph = torch.cuda.CUDAGraph()
-    cap = torch.cuda.Stream()
-    with torch.cuda.stream(cap):
-        with torch.cuda.graph(graph, stream=cap):
-            rc = lib.gcr_batch_launch(ctx, ctypes.c_void_p(cap.cuda_stream))
-    assert rc == 0, _abi.last_error()
-    launches_per_step = int(lib.gcr_last_launch_count())
-
-    def step():
-        graph.replay()
-        return launches_per_step
-
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    clocks = ClockSampler(local_rank)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    clocks.start()
-    total_ms, launches = 0.0, 0
-    for _ in range(args.steps):
-        flush.fill_(1)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        launches += step()
-        e1.record(stream)
-        e1.synchronize()
-        total_ms += e0.elapsed_time(e1)
-    torch.cuda.synchronize()
-    clk = clocks.stop()
-    value, t_rank = aggregate_rate(P * args.steps, total_ms / 1e3, world, dist, "cuda")
-    if dist:
-        dist.barrier()
-
-    stats = np.frombuffer(d_stats.cpu().numpy().tobytes(), _abi.STATS_DTYPE)
-    models = d_models.cpu().numpy().reshape(P, 3, 3)
-    n_per = np.diff(offsets)
-    flops = float(np.sum(stats["models_scored"] * n_per)) * FLOP_PER_RESIDUAL[args.workload]
-    errs = model_errors(args.workload, models, gts)
-
-    # end to end through the host-buffer entry: pinned inputs, copies timed
-    h_corr = torch.from_numpy(corr).pin_memory()
-    h_models = torch.zeros(P * 9, dtype=torch.float64).pin_memory()
-    h_masks = torch.zeros(int(offsets[-1]), dtype=torch.uint8).pin_memory()
-    h_stats = torch.zeros(P * _abi.STATS_DTYPE.itemsize, dtype=torch.uint8).pin_memory()
-
-    def e2e_step():
-        rc = lib.gcr_find_batch(kind, P, ctypes.c_void_p(h_corr.data_ptr()), _abi.ptr(offsets), _abi.ptr(K),
-                                _abi.ptr(szs), ctypes.byref(p), _abi.ptr(seeds),
-                                ctypes.c_void_p(h_models.data_ptr()), ctypes.c_void_p(h_masks.data_ptr()),
-                                ctypes.c_void_p(h_stats.data_ptr()))
-        assert rc == 0, _abi.last_error()
-
-    e2e_step()
-    e2e_t = 0.0
-    for _ in range(args.steps):
-        flush.fill_(1)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        e2e_step()
-        e2e_t += time.perf_counter() - t0
-    e2e_value, e2e_t = aggregate_rate(P * args.steps, e2e_t, world, dist, "cuda")
-
-    if rank != 0:
-        if dist:
-            dist.destroy_process_group()
-        return
-    peak = fp32_peak_tflops(torch)
-    achieved = flops / (total_ms / args.steps / 1e3) / 1e12
-    traffic = None
-    fp64_work = None
-    tp = os.path.join(ROOT, "profiles", f"traffic_{args.workload}.json")
-    if os.path.exists(tp):
-        t = json.load(open(tp))
-        traffic = t["bytes_per_pair"] * P
-        fp64_work = t["fp64_flop_per_pair"] * P
-    peak64 = fp64_peak_tflops(torch)
-    line = {
-        "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "fp32 scoring / fp64 solvers", "data": "synthetic", "config": cfg,
-        "median_model_error": float(np.median(errs)) if errs else None,
-        "status_ok_fraction": float(np.mean(stats["status"] == 0)),
-        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak if peak else None, "traffic": traffic,
-                     "peak_source": "cuBLAS SGEMM 8192^3, TF32 off, measured in this run",
-                     "work": f"{FLOP_PER_RESIDUAL[args.workload]} FLOP x models_scored x N per pair"},
-        # the FP64 pipe is the unit the kernel keeps busiest (solvers, LO fits):
-        # executed FP64 FLOP per pair from the ncu capture in profiles/, over the
-        # live DGEMM peak
-        "roofline_fp64": None if fp64_work is None else {
-            "bound": "fp64", "achieved": fp64_work / (total_ms / args.steps / 1e3) / 1e12, "peak": peak64,
-            "unit": "TFLOP/s", "frac": fp64_work / (total_ms / args.steps / 1e3) / 1e12 / peak64,
-            "peak_source": "cuBLAS DGEMM 4096^3, measured in this run",
-            "work": "FP64 FLOP per pair executed by the kernel (ncu SASS counts, FMA = 2) x pairs"},
-        "e2e": {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": int(corr.nbytes),
-                "d2h_bytes_per_step": int(P * 9 * 8 + offsets[-1] + P * _abi.STATS_DTYPE.itemsize)},
-        "gpu_launches": int(launches),
-        "clocks": clk,
-    }
-    if not args.no_cpu_baseline and world == 1:
-        v, cores, sample = cpu_baseline(args.workload, corr, offsets, sizes, p, K)
-        line["cpu_baseline"] = {"value": v, "unit": "pairs/s", "cores": cores, "kind": "port", "sample": sample}
-    print(json.dumps(line))
-    lib.gcr_context_destroy(ctx)
+    # the other workloads, a few steps each (same replicas and timing rules)
+    if not args.no_side:
+        side = {}
+        for name in ("homography", "fundamental", "essential", "serving"):
+            if name == args.workload:
+                continue
+            sw = WORKLOADS[name]
+            if name == "serving":
+                sub = run_serving(args, sw["pairs"], args.side_steps, 1, world, rank, local_rank, dist, torch,
+                                  clocks_on=False)
+            else:
+                sub = run_kind(args, name, sw["pairs"], args.side_steps, 1, world, rank, local_rank, dist, torch,
+                               clocks_on=False)
+            if sub is not None:
+                sub["config"] = {**describe(name, sw["pairs"], world), **sub.get("config", {})}
+                side[name] = sub
+        if line is not None:
+            line["workloads"] = side
+    if line is not None:
+        print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
 

@@ -22,6 +22,9 @@ thread_local long long g_last_launches = 0;
 thread_local long long* g_last_phase = nullptr;
 // host probabilities of the single-pair entries, staged by gcr_find_batch
 thread_local const double* g_batch_probs = nullptr;
+// host sample tape of the host-buffer entries (gcr_set_sample_tape)
+thread_local const int32_t* g_host_tape = nullptr;
+thread_local long long g_host_tape_calls = 0;
 
 gcr_status fail(gcr_status s, const char* fmt, ...) {
   char buf[512];
@@ -102,10 +105,18 @@ struct gcr_context {
   DevBuf ar_p, ar_i, ar_ab, ar_cnt;          // AR sampler heaps and per-point state (per resident CTA)
   const double* probs = nullptr;             // see gcr_context_set_probabilities
   DevBuf cdf, probs_stage;                   // importance sampler tables, staged probabilities
+  long long flow_cap = 0;                    // see gcr_context_set_flow_step_limit
+  const int32_t* tape = nullptr;             // see gcr_context_set_sample_tape
+  long long tape_calls = 0;
+  DevBuf tape_stage;                         // the host tape of the host-buffer entries, staged
+  std::vector<gcr_tuning> tuning;            // see gcr_context_set_tuning
+  DevBuf order;                              // pair of each work ticket (largest first)
+  gcr_tuning last_tuning{};                  // the entry the last prepared batch used
 };
 
-namespace {
+namespace gcr {
 
+// Argument checks shared by every entry point that takes gcr_params.
 gcr_status check_params(gcr_model_kind kind, const gcr_params* p) {
   if (!p) return fail(GCR_INVALID_ARG, "params is NULL");
   if (!(p->threshold > 0)) return fail(GCR_INVALID_ARG, "threshold must be > 0");
@@ -128,11 +139,28 @@ gcr_status check_params(gcr_model_kind kind, const gcr_params* p) {
     return fail(GCR_UNSUPPORTED, "neighbourhood %d is not provided (0 grid, 1 radius graph)", p->neighborhood);
   if (p->neighborhood == GCR_NEIGHBORHOOD_GRID && !(p->neighborhood_size >= 1))
     return fail(GCR_INVALID_ARG, "neighborhood_size must be >= 1 for the grid");
-  if (p->neighborhood == GCR_NEIGHBORHOOD_FLANN && !(p->neighborhood_size > 0))
-    return fail(GCR_INVALID_ARG, "neighborhood_size (the radius) must be > 0 for the radius graph");
+  // cell keys hold 10 bits per axis (40 bits for the four axes)
+  if (p->neighborhood == GCR_NEIGHBORHOOD_GRID && !(p->neighborhood_size < 1025))
+    return fail(GCR_UNSUPPORTED, "neighborhood_size must be at most 1024 grid divisions");
+  if (p->neighborhood == GCR_NEIGHBORHOOD_FLANN && !(p->neighborhood_size > 0 && std::isfinite(p->neighborhood_size)))
+    return fail(GCR_INVALID_ARG, "neighborhood_size (the radius) must be > 0 and finite for the radius graph");
   (void)kind;
   return GCR_OK;
 }
+
+// Grid divisions per axis: neighborhood_size truncated (as the drivers'
+// size_t conversion does), within [1, 1024]; one cell when the radius graph
+// replaces the grid.
+int32_t grid_divisions(double neighborhood_size, bool radius_graph) {
+  if (radius_graph || !(neighborhood_size >= 1)) return 1;
+  return neighborhood_size >= 1024 ? 1024 : (int32_t)neighborhood_size;
+}
+
+}  // namespace gcr
+
+namespace {
+
+using gcr::check_params;
 
 // MAGSAC++ weight table (MAGSACScoringFunction, scoring_function.h:263-334):
 // the upper incomplete gamma function Gamma(1.5, x / 1000) for x = 0..36000,
@@ -222,7 +250,7 @@ gcr_status gcr_context_destroy(gcr_context* c) {
   if (!c) return GCR_OK;
   for (DevBuf* b : {&c->pairs, &c->slots_meta, &c->slot_mem, &c->pts32, &c->ticket, &c->norm_pts, &c->kinv,
                     &c->row_pair, &c->phase, &c->corr, &c->models, &c->masks, &c->stats, &c->magsac, &c->rg_int,
-                    &c->rg_dbl, &c->rg_px, &c->ar_p, &c->ar_i, &c->ar_ab, &c->ar_cnt, &c->cdf, &c->probs_stage})
+                    &c->rg_dbl, &c->rg_px, &c->ar_p, &c->ar_i, &c->ar_ab, &c->ar_cnt, &c->cdf, &c->probs_stage, &c->tape_stage, &c->order})
     b->release();
   delete c;
   return GCR_OK;
@@ -297,7 +325,27 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
   int per_sm = 0;
   CUDA_TRY(ops->occupancy(&per_sm));
   if (per_sm < 1) return fail(GCR_DEVICE_ERROR, "engine kernel does not fit on an SM");
-  const int resident = per_sm * c->num_sms;
+  // launch shape from the context's tuning table: the entry of this kind
+  // with the smallest max_n that covers the batch's largest pair
+  gcr_tuning tune{};
+  tune.kind = (int32_t)kind;
+  tune.max_n = max_n;
+  tune.batch_calls = GCR_BLOCK;
+  tune.ctas_per_sm = per_sm;
+  tune.order = 0;
+  {
+    const gcr_tuning* best = nullptr;
+    for (const gcr_tuning& e : c->tuning)
+      if (e.kind == (int32_t)kind && e.max_n >= max_n && (!best || e.max_n < best->max_n)) best = &e;
+    if (best) {
+      if (best->batch_calls > 0) tune.batch_calls = std::min(best->batch_calls, (int32_t)GCR_BLOCK);
+      if (best->ctas_per_sm > 0) tune.ctas_per_sm = std::min(best->ctas_per_sm, (int32_t)per_sm);
+      tune.order = best->order;
+      tune.max_n = best->max_n;
+    }
+  }
+  c->last_tuning = tune;
+  const int resident = tune.ctas_per_sm * c->num_sms;
   const int grid = (int)std::min<int64_t>(num_pairs, resident);
   const int sort_cap = pow2_at_least(max_n);
 
@@ -332,8 +380,7 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
     const gcr_image_size& z = h_sizes[i];
     d.offset = h_offsets[i];
     d.n = (int32_t)(h_offsets[i + 1] - h_offsets[i]);
-    d.n_div = (int32_t)params->neighborhood_size;
-    if (d.n_div < 1 || radius) d.n_div = 1;
+    d.n_div = gcr::grid_divisions(params->neighborhood_size, radius);
     const double nd = (double)d.n_div;
     // the homography driver pads the image size by machine epsilon
     // (gcransac_python.cpp:4290-4297), the fundamental/essential ones do not
@@ -390,6 +437,19 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
   }
   if (max_n > gcr::kSmemPoints) CUDA_TRY(c->pts32.ensure(sizeof(float4) * (size_t)total));
   CUDA_TRY(c->ticket.ensure(sizeof(int)));
+  // largest pairs first: a persistent CTA that takes a big pair late would
+  // otherwise finish long after the others (stable order among equal sizes)
+  const int* d_order = nullptr;
+  if (tune.order == 1 && num_pairs > 1) {
+    std::vector<int> ord((size_t)num_pairs);
+    for (int64_t i = 0; i < num_pairs; ++i) ord[i] = (int)i;
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+      return h_offsets[a + 1] - h_offsets[a] > h_offsets[b + 1] - h_offsets[b];
+    });
+    CUDA_TRY(c->order.ensure(sizeof(int) * (size_t)num_pairs));
+    CUDA_TRY(cudaMemcpy(c->order.p, ord.data(), sizeof(int) * (size_t)num_pairs, cudaMemcpyHostToDevice));
+    d_order = (const int*)c->order.p;
+  }
 
   gcr::Workspace ws;
   ws.pts64 = run_pts;
@@ -404,6 +464,7 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
   ws.stats_out = (gcr::StatsOut*)d_stats_out;
   ws.phase = nullptr;
   ws.times = c->pair_times;
+  ws.order = d_order;
 #ifdef GCR_PHASE_PROFILE
   CUDA_TRY(c->phase.ensure(sizeof(long long) * 16 * num_pairs));
   CUDA_TRY(cudaMemsetAsync(c->phase.p, 0, sizeof(long long) * 16 * num_pairs, s));
@@ -432,6 +493,10 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
   prm.use_sp = (kind == GCR_HOMOGRAPHY && params->use_space_partitioning) ? 1 : 0;
   prm.sprt_min_ratio = params->min_inlier_ratio_for_sprt;
   prm.epilogue = run_only ? 0 : 1;
+  prm.flow_cap = c->flow_cap;
+  prm.tape = c->tape;
+  prm.tape_calls = c->tape ? c->tape_calls : 0;
+  prm.batch_calls = tune.batch_calls;
   prm.cdf = nullptr;
   prm.neighborhood = 0;
   prm.radius2 = 0.0;
@@ -609,6 +674,52 @@ gcr_status gcr_context_set_pair_times(gcr_context* c, unsigned long long* d_time
   return GCR_OK;
 }
 
+gcr_status gcr_context_set_flow_step_limit(gcr_context* c, int64_t steps) {
+  if (!c) return fail(GCR_INVALID_ARG, "context is NULL");
+  if (steps < 0) return fail(GCR_INVALID_ARG, "the step limit must be >= 0 (0 restores the defaults)");
+  c->flow_cap = steps;
+  c->pending.valid = false;
+  return GCR_OK;
+}
+
+gcr_status gcr_context_set_sample_tape(gcr_context* c, const int32_t* d_tape, int64_t calls_per_pair) {
+  if (!c) return fail(GCR_INVALID_ARG, "context is NULL");
+  if (calls_per_pair < 0) return fail(GCR_INVALID_ARG, "calls_per_pair must be >= 0");
+  c->tape = calls_per_pair > 0 ? d_tape : nullptr;
+  c->tape_calls = c->tape ? calls_per_pair : 0;
+  c->pending.valid = false;
+  return GCR_OK;
+}
+
+gcr_status gcr_context_set_tuning(gcr_context* c, const gcr_tuning* entries, int32_t count) {
+  if (!c) return fail(GCR_INVALID_ARG, "context is NULL");
+  if (count < 0 || (count > 0 && !entries)) return fail(GCR_INVALID_ARG, "bad tuning table");
+  for (int32_t i = 0; i < count; ++i) {
+    const gcr_tuning& e = entries[i];
+    if (!ops_for((gcr_model_kind)e.kind)) return fail(GCR_INVALID_ARG, "tuning entry %d: unknown kind %d", i, e.kind);
+    if (e.batch_calls < 0 || e.batch_calls > GCR_BLOCK)
+      return fail(GCR_INVALID_ARG, "tuning entry %d: batch_calls must be in [0, %d]", i, GCR_BLOCK);
+    if (e.ctas_per_sm < 0 || e.order < 0 || e.order > 1 || e.max_n < 0)
+      return fail(GCR_INVALID_ARG, "tuning entry %d: bad ctas_per_sm, order or max_n", i);
+  }
+  c->tuning.assign(entries, entries + count);
+  c->pending.valid = false;
+  return GCR_OK;
+}
+
+gcr_status gcr_context_last_tuning(const gcr_context* c, gcr_tuning* out) {
+  if (!c || !out) return fail(GCR_INVALID_ARG, "NULL argument");
+  *out = c->last_tuning;
+  return GCR_OK;
+}
+
+gcr_status gcr_set_sample_tape(const int32_t* h_tape, int64_t calls_per_pair) {
+  if (calls_per_pair < 0) return fail(GCR_INVALID_ARG, "calls_per_pair must be >= 0");
+  g_host_tape = calls_per_pair > 0 ? h_tape : nullptr;
+  g_host_tape_calls = g_host_tape ? calls_per_pair : 0;
+  return GCR_OK;
+}
+
 gcr_status gcr_batch_launch(gcr_context* c, void* stream) {
   g_last_launches = 0;
   if (!c) return fail(GCR_INVALID_ARG, "context is NULL");
@@ -620,13 +731,17 @@ gcr_status gcr_find_batch(gcr_model_kind kind, int64_t num_pairs, const double* 
                           const double* K, const gcr_image_size* sizes, const gcr_params* params,
                           const uint64_t* seeds, double* models_out, uint8_t* masks_out, gcr_stats* stats_out) {
   static thread_local gcr_context* ctx = nullptr;
+  // arguments first: a bad call returns its status before any device work
+  if (!ops_for(kind)) return fail(GCR_UNSUPPORTED, "model kind %d is not provided by this build", (int)kind);
+  gcr_status chk = check_params(kind, params);
+  if (chk != GCR_OK) return chk;
+  if (num_pairs <= 0) return GCR_OK;
+  if (!corr || !offsets || !sizes || !models_out || !masks_out || !stats_out)
+    return fail(GCR_INVALID_ARG, "NULL buffer");
   if (!ctx) {
     gcr_status s = gcr_context_create(&ctx);
     if (s != GCR_OK) return s;
   }
-  if (num_pairs <= 0) return GCR_OK;
-  if (!corr || !offsets || !sizes || !models_out || !masks_out || !stats_out)
-    return fail(GCR_INVALID_ARG, "NULL buffer");
   const int64_t total = offsets[num_pairs];
   CUDA_TRY(ctx->corr.ensure(sizeof(double) * 4 * (size_t)std::max<int64_t>(total, 1)));
   CUDA_TRY(ctx->models.ensure(sizeof(double) * 9 * num_pairs));
@@ -640,9 +755,21 @@ gcr_status gcr_find_batch(gcr_model_kind kind, int64_t num_pairs, const double* 
     CUDA_TRY(cudaMemcpyAsync(ctx->probs_stage.p, g_batch_probs, sizeof(double) * total, cudaMemcpyHostToDevice, s));
     ctx->probs = (const double*)ctx->probs_stage.p;
   }
+  ctx->tape = nullptr;
+  ctx->tape_calls = 0;
+  if (g_host_tape) {
+    const int m = ops_for(kind)->sample_size;
+    const size_t tb = sizeof(int32_t) * (size_t)m * (size_t)g_host_tape_calls * (size_t)num_pairs;
+    CUDA_TRY(ctx->tape_stage.ensure(tb));
+    CUDA_TRY(cudaMemcpyAsync(ctx->tape_stage.p, g_host_tape, tb, cudaMemcpyHostToDevice, s));
+    ctx->tape = (const int32_t*)ctx->tape_stage.p;
+    ctx->tape_calls = g_host_tape_calls;
+  }
   gcr_status st = gcr_batch_run_device(ctx, kind, num_pairs, (const double*)ctx->corr.p, offsets, K, sizes,
                                        params, seeds, (double*)ctx->models.p, (uint8_t*)ctx->masks.p,
                                        (gcr_stats*)ctx->stats.p, s);
+  ctx->tape = nullptr;
+  ctx->tape_calls = 0;
   if (st != GCR_OK) return st;
   CUDA_TRY(cudaMemcpyAsync(models_out, ctx->models.p, sizeof(double) * 9 * num_pairs, cudaMemcpyDeviceToHost, s));
   CUDA_TRY(cudaMemcpyAsync(masks_out, ctx->masks.p, (size_t)total, cudaMemcpyDeviceToHost, s));
@@ -740,6 +867,15 @@ static gcr_status run_single(gcr_model_kind kind, const double* points, const do
     CUDA_TRY(cudaMemcpyAsync(ctx->probs_stage.p, probabilities, sizeof(double) * n, cudaMemcpyHostToDevice, s));
     ctx->probs = (const double*)ctx->probs_stage.p;
   }
+  ctx->tape = nullptr;
+  ctx->tape_calls = 0;
+  if (g_host_tape) {
+    const size_t tb = sizeof(int32_t) * (size_t)m * (size_t)g_host_tape_calls;
+    CUDA_TRY(ctx->tape_stage.ensure(tb));
+    CUDA_TRY(cudaMemcpyAsync(ctx->tape_stage.p, g_host_tape, tb, cudaMemcpyHostToDevice, s));
+    ctx->tape = (const int32_t*)ctx->tape_stage.p;
+    ctx->tape_calls = g_host_tape_calls;
+  }
   RunOnly ro;
   ro.d_pixels = d_pix;
   for (int q = 0; q < 4; ++q) ro.cell[q] = cell_sizes[q];
@@ -751,6 +887,8 @@ static gcr_status run_single(gcr_model_kind kind, const double* points, const do
   gcr_status st = prepare_batch(ctx, kind, 1, d_pts, offsets, nullptr, size, params, &seed, (double*)ctx->models.p,
                                 (uint8_t*)ctx->masks.p, (gcr_stats*)ctx->stats.p, s, &L, &ro);
   if (st != GCR_OK) return st;
+  ctx->tape = nullptr;
+  ctx->tape_calls = 0;
   st = launch_batch(ctx, L, s);
   if (st != GCR_OK) return st;
   gcr_stats so{};

@@ -41,6 +41,7 @@ constexpr int kLoRegion = GCR_BLOCK;    // model slots reserved for local optimi
 
 enum PairStatus {
   ST_OK = 0,
+  ST_INVALID_ARG = 1,   // a coordinate of the pair is not finite
   ST_NO_MODEL = 3,
   ST_DEVICE_ERROR = 4,  // an internal consistency check failed (a row index outside the pair)
   ST_TIMEOUT = 5,
@@ -108,6 +109,18 @@ struct EngineParams {
   // 1: the Python drivers' epilogue after the run (bundle adjustment of the
   // final inliers for F and E); 0: GCRANSAC::run alone
   int32_t epilogue;
+  // push / relabel steps of one labelling flow problem before the pair
+  // reports ST_TIMEOUT; 0 for the defaults (kFlowOpsCap per grid cell, 2^24
+  // on the radius graph)
+  long long flow_cap;
+  // recorded main-sampler samples replacing the sampler's draws (null: the
+  // sampler draws): [num_pairs][tape_calls][M] point indices
+  const int32_t* tape;
+  long long tape_calls;
+  // sampler calls (hypotheses) drawn, solved and scored per batch, 1..GCR_BLOCK;
+  // calls are counter-based and replayed in call order, so any batch size
+  // gives the same results (a tuning knob)
+  int32_t batch_calls;
 };
 
 // Per-pair inputs prepared on the device.
@@ -175,6 +188,7 @@ struct Workspace {
   StatsOut* stats_out;  // [P]
   long long* phase;     // [P][16] phase cycle counters (GCR_PHASE_PROFILE builds), else null
   unsigned long long* times;  // [P][2] global timer (ns) when a CTA takes the pair and when it is done, or null
+  const int* order;     // [P] pair of each work ticket (largest pairs first), or null for ticket order
 };
 
 struct Score {
@@ -911,6 +925,7 @@ struct Engine {
     }
     __syncwarp();
     long long ops = 0;
+    const long long ops_cap = prm.flow_cap > 0 ? prm.flow_cap : kFlowOpsCap;
     bool ok = true;
     while (qh != qt) {
       const int u = q[qh % kMaxFlowCap];
@@ -919,7 +934,7 @@ struct Engine {
       if (lane == 0) mark[u] = 0;
       __syncwarp();
       for (;;) {
-        if (++ops > kFlowOpsCap) { ok = false; break; }
+        if (++ops > ops_cap) { ok = false; break; }
         double e = ex[u];
         const int hu = h[u];
         if (!dpos(e) || hu >= dead) break;
@@ -1158,6 +1173,7 @@ struct Engine {
         }
       }
       long long steps = 0;
+      const long long steps_cap = prm.flow_cap > 0 ? prm.flow_cap : (1ll << 24);
       bool ok = true;
       while (qn > 0) {
         const int u = q[qh];
@@ -1165,7 +1181,7 @@ struct Engine {
         --qn;
         inq[u] = 0;
         while (ex[u] > 0) {
-          if (++steps > (1ll << 24) || h[u] > 2 * N + 2) {
+          if (++steps > steps_cap || h[u] > 2 * N + 2) {
             ok = false;
             break;
           }
@@ -2547,8 +2563,8 @@ struct Engine {
     sync();
   }
 
-  // thread 0: the samples of calls a0 .. a0 + GCR_BLOCK - 1 into slot.bsamples
-  __device__ void ar_batch(long long a0) {
+  // thread 0: the samples of calls a0 .. a0 + calls - 1 into slot.bsamples
+  __device__ void ar_batch(long long a0, int calls) {
     if (threadIdx.x == 0) {
       double* hp = ar_hp();
       int* hi = ar_hi();
@@ -2556,7 +2572,7 @@ struct Engine {
       const double* B = ar_b();
       int* C = ar_c();
       int n = sh.ar_size;
-      for (int c = 0; c < GCR_BLOCK; ++c) {
+      for (int c = 0; c < calls; ++c) {
         if (sh.ar_overflow || n + m > prm.ar_cap || n < m) {
           sh.ar_overflow = 1;
           sh.s_cnt[c] = 0;
@@ -2591,28 +2607,47 @@ struct Engine {
   __device__ int generate_batch(long long a0, long long& p_kth, long long& p_subset, long long& p_hi,
                                 double& p_Tn, long long& p_Tprime) {
     const int j = threadIdx.x;
+    const int B = prm.batch_calls;  // calls of this batch: a0 .. a0 + B - 1, one per thread j < B
     int s[Est::M];
+#pragma unroll
+    for (int q = 0; q < Est::M; ++q) s[q] = 0;
     bool ok = false;
-    if (prm.sampler == SAMPLER_PNAPSAC) {
+    if (prm.tape != nullptr && !prm.nested) {
+      // a recorded sample sequence replaces the sampler (the reference's
+      // Sampler* plugin of GCRANSAC::run, GCRANSAC.h:69-76): call c reads row
+      // c of the pair's tape; a call past its end or a row with an index
+      // outside [0, N) is an unsuccessful sampler call
+      const long long c = a0 + j;
+      ok = j < B && c < prm.tape_calls;
+      const int32_t* row = prm.tape + ((size_t)pair * (size_t)prm.tape_calls + (size_t)(ok ? c : 0)) * Est::M;
+#pragma unroll
+      for (int q = 0; q < Est::M; ++q) {
+        const int v = ok ? row[q] : 0;
+        if ((unsigned)v >= (unsigned)N) ok = false;
+        s[q] = (unsigned)v < (unsigned)N ? v : 0;
+      }
+    } else if (prm.sampler == SAMPLER_PNAPSAC) {
       if (threadIdx.x == 0)
-        for (int c = 0; c < GCR_BLOCK; ++c) {
+        for (int c = 0; c < B; ++c) {
           int t[Est::M];
           const bool o = napsac_call(t);
           for (int q = 0; q < Est::M; ++q) slot.bsamples[c * Est::M + q] = t[q];
           sh.s_cnt[c] = o ? 1 : 0;
         }
       sync();
-      ok = sh.s_cnt[j] != 0;
+      ok = j < B && sh.s_cnt[j] != 0;
 #pragma unroll
       for (int q = 0; q < Est::M; ++q) s[q] = slot.bsamples[j * Est::M + q];
       sync();
     } else if (prm.sampler == SAMPLER_UNIFORM) {
-      DrawStream ds(pd.seed, prm.stream_main, (uint64_t)(a0 + j));
-      ok = unique_set(ds, s, m, 0, (uint32_t)(N - 1));
+      if (j < B) {
+        DrawStream ds(pd.seed, prm.stream_main, (uint64_t)(a0 + j));
+        ok = unique_set(ds, s, m, 0, (uint32_t)(N - 1));
+      }
     } else if (prm.sampler == SAMPLER_AR) {
-      ar_batch(a0);
+      ar_batch(a0, B);
       if (sh.ar_overflow && status == ST_OK) status = ST_CAPACITY;
-      ok = sh.s_cnt[j] != 0;
+      ok = j < B && sh.s_cnt[j] != 0;
 #pragma unroll
       for (int q = 0; q < Est::M; ++q) s[q] = slot.bsamples[j * Est::M + q];
       sync();
@@ -2623,7 +2658,7 @@ struct Engine {
       // probability is not below u
       DrawStream ds(pd.seed, prm.stream_main, (uint64_t)(a0 + j));
       const double* cdf = prm.cdf + pd.offset;
-      for (int q = 0; q < m; ++q) {
+      for (int q = 0; q < m && j < B; ++q) {
         const uint32_t w0 = ds.next_u32(), w1 = ds.next_u32();
         const double u = ((double)(w0 >> 5) * 67108864.0 + (double)(w1 >> 6)) * (1.0 / 9007199254740992.0);
         int lo = 0, hi = N - 1;
@@ -2634,14 +2669,14 @@ struct Engine {
         }
         s[q] = lo;
       }
-      ok = true;
+      ok = j < B;
     } else {
       // PROSAC (samplers/prosac_sampler.h:51-237): every thread replays the
       // state machine for the whole batch and keeps its own call's draw range.
       const long long conv = 100000;
       long long my_hi = 0, my_last = 0;
       bool my_global = false;
-      for (int c = 0; c < GCR_BLOCK; ++c) {
+      for (int c = 0; c < B; ++c) {
         if (c == j) {
           my_global = p_kth > conv;
           my_hi = p_hi;
@@ -2669,7 +2704,9 @@ struct Engine {
         }
       }
       DrawStream ds(pd.seed, prm.stream_main, (uint64_t)(a0 + j));
-      if (my_global) {
+      if (j >= B) {
+        ok = false;
+      } else if (my_global) {
         ok = unique_set(ds, s, m, 0, (uint32_t)(N - 1));
       } else {
         ok = unique_set(ds, s, m - 1, 0, (uint32_t)my_hi);
@@ -2732,8 +2769,8 @@ struct Engine {
       if (!sprt && !(sp && !mag)) score_models_f32(0, K);
       tock(2, t0);
       bool restart = false;
-      long long next_attempt = attempt + GCR_BLOCK;
-      for (int j = 0; j < GCR_BLOCK; ++j) {
+      long long next_attempt = attempt + prm.batch_calls;
+      for (int j = 0; j < prm.batch_calls; ++j) {
         if (!in_iter) {
           const long long lim = max_iter < max_iters ? max_iter : max_iters;
           if (!(min_iters > iter || iter < lim)) {
@@ -2862,6 +2899,26 @@ struct Engine {
     t0 = tick();
     finish(ncells);
     tock(8, t0);
+  }
+
+  // A pair the engine does not run: status st, a zero model, an empty mask
+  // and zero counts.
+  __device__ void reject(int st) {
+    StatsOut* so = ws.stats_out + pair;
+    uint8_t* mask = ws.masks_out + pd.offset;
+    for (int i = threadIdx.x; i < N; i += GCR_BLOCK) mask[i] = 0;
+    if (threadIdx.x < 9) ws.models_out[9 * pair + threadIdx.x] = 0.0;
+    if (threadIdx.x == 0) {
+      so->iteration_number = 0;
+      so->graph_cut_number = 0;
+      so->local_optimization_number = 0;
+      so->inlier_number = 0;
+      so->score = 0.0;
+      so->status = st;
+      so->flags = 0;
+      so->models_scored = 0;
+    }
+    sync();
   }
 
   __device__ void finish(int ncells) {

@@ -51,6 +51,27 @@ __host__ __device__ constexpr size_t shared_total() {
   return kTileBytes + align256(sizeof(Shared<Est>)) + nested_bytes<Est>();
 }
 
+// Centred FP32 copy of a pair's correspondences into dst (shared memory or
+// global), the largest centred magnitude into mx (per thread); returns
+// nonzero when this thread saw a coordinate (fitting or pixel) that is not
+// finite.
+__device__ inline int load_pair_tile(const Workspace& ws, const PairDesc& pd, const double* p64, float4* dst,
+                                     double& mx) {
+  int bad = 0;
+  for (int i = threadIdx.x; i < pd.n; i += GCR_BLOCK) {
+    const double a = p64[4 * i] - pd.centre[0], b = p64[4 * i + 1] - pd.centre[1];
+    const double c = p64[4 * i + 2] - pd.centre[2], d = p64[4 * i + 3] - pd.centre[3];
+    dst[i] = make_float4((float)a, (float)b, (float)c, (float)d);
+    mx = fmax(mx, fmax(fmax(fabs(a), fabs(b)), fmax(fabs(c), fabs(d))));
+    bad |= !(isfinite(a) && isfinite(b) && isfinite(c) && isfinite(d));
+  }
+  if (ws.pix64 != ws.pts64) {
+    const double* px = ws.pix64 + 4 * pd.offset;
+    for (int i = threadIdx.x; i < 4 * pd.n; i += GCR_BLOCK) bad |= !isfinite(px[i]);
+  }
+  return bad;
+}
+
 // Persistent kernel: each CTA takes pairs from a global ticket until none is
 // left; blockIdx.x selects the CTA's scratch slot.
 template <class Est>
@@ -64,8 +85,9 @@ __global__ void __launch_bounds__(GCR_BLOCK, GCR_MIN_BLOCKS) pair_kernel(Workspa
     __syncthreads();
     if (threadIdx.x == 0) s_pair = atomicAdd(ws.ticket, 1);
     __syncthreads();
-    const int pair = s_pair;
-    if (pair >= prm.num_pairs) break;
+    const int ticket = s_pair;
+    if (ticket >= prm.num_pairs) break;
+    const int pair = ws.order ? ws.order[ticket] : ticket;
     if (ws.times && threadIdx.x == 0) ws.times[2 * pair] = global_ns();
     const PairDesc pd = ws.pairs[pair];
     Engine<Est> eng(sh, ws, prm, pd, slot, pair);
@@ -78,16 +100,13 @@ __global__ void __launch_bounds__(GCR_BLOCK, GCR_MIN_BLOCKS) pair_kernel(Workspa
     const bool in_smem = pd.n <= kSmemPoints;
     float4* dst = in_smem ? tile : ws.pts32 + pd.offset;
     double mx = 0.0;
-    for (int i = threadIdx.x; i < pd.n; i += GCR_BLOCK) {
-      const double a = p64[4 * i] - pd.centre[0], b = p64[4 * i + 1] - pd.centre[1];
-      const double c = p64[4 * i + 2] - pd.centre[2], d = p64[4 * i + 3] - pd.centre[3];
-      dst[i] = make_float4((float)a, (float)b, (float)c, (float)d);
-      mx = fmax(mx, fmax(fmax(fabs(a), fabs(b)), fmax(fabs(c), fabs(d))));
-    }
+    int bad = load_pair_tile(ws, pd, p64, dst, mx);
     eng.scale = block_max_abs(mx, sh.red_d);
     eng.pts32 = dst;
-    __syncthreads();
-    eng.run();
+    // a pair with a coordinate that is not finite is not run (status
+    // GCR_INVALID_ARG, no model, empty mask)
+    if (__syncthreads_or(bad)) eng.reject(ST_INVALID_ARG);
+    else eng.run();
     if (ws.times) {
       __syncthreads();
       if (threadIdx.x == 0) ws.times[2 * pair + 1] = global_ns();

@@ -34,6 +34,10 @@
 namespace gcr {
 // Records the message returned by gcr_last_error_string (gcr_api.cu).
 void set_last_error(const char* msg);
+// The argument checks of every gcr_params entry point (gcr_api.cu).
+gcr_status check_params(gcr_model_kind kind, const gcr_params* p);
+// Grid divisions per axis for neighborhood_size (gcr_api.cu).
+int32_t grid_divisions(double neighborhood_size, bool radius_graph);
 }  // namespace gcr
 
 namespace {
@@ -50,7 +54,6 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 
 struct DeviceSetup {
   bool done = false;
-  cudaError_t err = cudaSuccess;
   gcr::Slot slot{};
 };
 DeviceSetup g_setup[kMaxDevices];
@@ -75,41 +78,35 @@ __global__ void __launch_bounds__(GCR_BLOCK, 1)
   float4* tile = reinterpret_cast<float4*>(smem_raw);
   gcr::Shared<Est>& sh = *reinterpret_cast<gcr::Shared<Est>*>(smem_raw + gcr::kTileBytes);
   gcr::Engine<Est> eng(sh, ws, prm, pd, slot, 0);
-  const double* p64 = ws.pts64;
   double mx = 0.0;
-  for (int i = threadIdx.x; i < pd.n; i += GCR_BLOCK) {
-    const double a = p64[4 * i] - pd.centre[0], b = p64[4 * i + 1] - pd.centre[1];
-    const double c = p64[4 * i + 2] - pd.centre[2], d = p64[4 * i + 3] - pd.centre[3];
-    tile[i] = make_float4((float)a, (float)b, (float)c, (float)d);
-    mx = fmax(mx, fmax(fmax(fabs(a), fabs(b)), fmax(fabs(c), fabs(d))));
-  }
+  const int bad = gcr::load_pair_tile(ws, pd, ws.pts64, tile, mx);
   eng.scale = gcr::block_max_abs(mx, sh.red_d);
   eng.pts32 = tile;
-  __syncthreads();
-  eng.run();
+  if (__syncthreads_or(bad)) eng.reject(gcr::ST_INVALID_ARG);
+  else eng.run();
 }
 
-// One-time set-up of the current device; returns its scratch slot.
+// One-time set-up of the current device; returns its scratch slot. A device
+// counts as set up only once both steps succeeded, so a call that failed here
+// (for instance one made during a stream capture) leaves the next call to try
+// again.
 gcr_status setup_device(int dev, gcr::Slot* out) {
   std::lock_guard<std::mutex> lock(g_setup_mutex);
   DeviceSetup& s = g_setup[dev];
   if (!s.done) {
-    s.done = true;
     unsigned char* base = nullptr;
-    s.err = cudaGetSymbolAddress((void**)&base, g_noalloc_scratch);
-    if (s.err == cudaSuccess)
-      s.err = cudaFuncSetAttribute(single_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)gcr::shared_bytes<Est>());
-    if (s.err == cudaSuccess) {
-      if (gcr::slot_bytes<Est>(kNoAllocMaxPoints, kNoAllocMaxPoints) > kNoAllocScratchBytes)
-        s.err = cudaErrorInvalidValue;  // cannot happen for the sizes above
-      else
-        s.slot = gcr::carve_slot<Est>(base, kNoAllocMaxPoints, kNoAllocMaxPoints);
-    }
+    cudaError_t err = cudaGetSymbolAddress((void**)&base, g_noalloc_scratch);
+    if (err == cudaSuccess)
+      err = cudaFuncSetAttribute(single_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)gcr::shared_bytes<Est>());
+    if (err == cudaSuccess && gcr::slot_bytes<Est>(kNoAllocMaxPoints, kNoAllocMaxPoints) > kNoAllocScratchBytes)
+      err = cudaErrorInvalidValue;  // cannot happen for the sizes above
+    if (err != cudaSuccess)
+      return fail(GCR_DEVICE_ERROR, "set-up of the allocation-free scratch on device %d failed: %s", dev,
+                  cudaGetErrorString(err));
+    s.slot = gcr::carve_slot<Est>(base, kNoAllocMaxPoints, kNoAllocMaxPoints);
+    s.done = true;
   }
-  if (s.err != cudaSuccess)
-    return fail(GCR_DEVICE_ERROR, "set-up of the allocation-free scratch on device %d failed: %s", dev,
-                cudaGetErrorString(s.err));
   *out = s.slot;
   return GCR_OK;
 }
@@ -131,23 +128,15 @@ extern "C" gcr_status gcr_find_homography_device_noalloc(const double* d_corr, i
                 (long long)n, kNoAllocMaxPoints);
   if (size->h1 <= 0 || size->w1 <= 0 || size->h2 <= 0 || size->w2 <= 0)
     return fail(GCR_INVALID_ARG, "image sizes must be positive");
+  gcr_status chk = gcr::check_params(GCR_HOMOGRAPHY, params);
+  if (chk != GCR_OK) return chk;
+  // the limits of this entry point beyond the shared checks
   const gcr_params& p = *params;
-  if (!(p.threshold > 0)) return fail(GCR_INVALID_ARG, "threshold must be > 0");
-  if (!(p.confidence > 0 && p.confidence < 1)) return fail(GCR_INVALID_ARG, "confidence must be in (0, 1)");
-  if (!(p.spatial_coherence_weight >= 0 && p.spatial_coherence_weight <= 1))
-    return fail(GCR_INVALID_ARG, "spatial_coherence_weight must be in [0, 1]");
-  if (p.max_iterations < 0 || p.min_iterations < 0) return fail(GCR_INVALID_ARG, "negative iteration limit");
-  if (p.lo_number < 0 || p.lo_number > GCR_BLOCK)
-    return fail(GCR_UNSUPPORTED, "lo_number must be in [0, %d]", GCR_BLOCK);
   if (p.sampler != GCR_SAMPLER_UNIFORM && p.sampler != GCR_SAMPLER_PROSAC && p.sampler != GCR_SAMPLER_PNAPSAC)
-    return fail(GCR_UNSUPPORTED, "sampler %d is not provided (0 uniform, 1 PROSAC, 2 P-NAPSAC)", p.sampler);
-  if (p.scoring != GCR_SCORING_MSAC) return fail(GCR_UNSUPPORTED, "scoring %d is not provided", p.scoring);
-  if (p.use_sprt && !(p.min_inlier_ratio_for_sprt > 0 && p.min_inlier_ratio_for_sprt < 1))
-    return fail(GCR_INVALID_ARG, "min_inlier_ratio_for_sprt must be in (0, 1) when use_sprt is set");
+    return fail(GCR_UNSUPPORTED, "sampler %d is not provided here (0 uniform, 1 PROSAC, 2 P-NAPSAC)", p.sampler);
+  if (p.scoring != GCR_SCORING_MSAC) return fail(GCR_UNSUPPORTED, "scoring %d is not provided here", p.scoring);
   if (p.spatial_coherence_weight > 0 && p.neighborhood != GCR_NEIGHBORHOOD_GRID)
-    return fail(GCR_UNSUPPORTED, "only the grid neighbourhood (0) is provided with a spatial coherence term");
-  if (p.neighborhood == GCR_NEIGHBORHOOD_GRID && !(p.neighborhood_size >= 1))
-    return fail(GCR_INVALID_ARG, "neighborhood_size must be >= 1 for the grid");
+    return fail(GCR_UNSUPPORTED, "only the grid neighbourhood (0) is provided here with a spatial coherence term");
 
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -162,8 +151,9 @@ extern "C" gcr_status gcr_find_homography_device_noalloc(const double* d_corr, i
   gcr::PairDesc pd{};
   pd.offset = 0;
   pd.n = (int32_t)n;
-  pd.n_div = (int32_t)p.neighborhood_size;
-  if (pd.n_div < 1) pd.n_div = 1;
+  // the grid's divisions, as gcr_batch_run_device sets them (the radius
+  // graph is not taken here, so the size is a division count)
+  pd.n_div = gcr::grid_divisions(p.neighborhood_size, false);
   const double nd = (double)pd.n_div;
   const double eps = std::numeric_limits<double>::epsilon();
   pd.cell[0] = (size->w1 + eps) / nd;
@@ -212,6 +202,7 @@ extern "C" gcr_status gcr_find_homography_device_noalloc(const double* d_corr, i
   prm.use_sprt = p.use_sprt ? 1 : 0;
   prm.use_sp = p.use_space_partitioning ? 1 : 0;
   prm.epilogue = 1;
+  prm.batch_calls = GCR_BLOCK;
   prm.sprt_min_ratio = p.min_inlier_ratio_for_sprt;
 
   single_pair_kernel<<<1, GCR_BLOCK, gcr::shared_bytes<Est>(), (cudaStream_t)stream>>>(ws, prm, pd, slot);

@@ -89,7 +89,42 @@ def _probabilities(probabilities, n, sampler):
     return p
 
 
-def _run_one(kind, corr, size, params, K1=None, K2=None, return_stats=False, probabilities=None):
+class _SampleTape:
+    """Sets the host sample tape of this thread's entry calls inside the block
+    (gcr_set_sample_tape): `tape` [calls, m] for one pair or [P, calls, m]
+    for a batch, int point indices, -1 for a failed call; None leaves the
+    sampler alone."""
+
+    def __init__(self, tape, m, pairs=None):
+        self.tape = None
+        if tape is not None:
+            t = np.ascontiguousarray(tape, np.int32)
+            want = 2 if pairs is None else 3
+            if t.ndim != want or t.shape[-1] != m or (pairs is not None and t.shape[0] != pairs):
+                raise ValueError(f"sample_tape must have shape {'[calls, m]' if pairs is None else '[P, calls, m]'}"
+                                 f" with m = {m}")
+            self.tape = t
+
+    def __enter__(self):
+        if self.tape is not None:
+            _raise_for(_abi.load().gcr_set_sample_tape(_abi.ptr(self.tape), int(self.tape.shape[-2])), "sample_tape")
+        return self
+
+    def __exit__(self, *exc):
+        if self.tape is not None:
+            _abi.load().gcr_set_sample_tape(None, 0)
+        return False
+
+
+_SAMPLE_SIZE = {_abi.GCR_HOMOGRAPHY: 4, _abi.GCR_FUNDAMENTAL: 7, _abi.GCR_ESSENTIAL: 5}
+
+
+def _run_one(kind, corr, size, params, K1=None, K2=None, return_stats=False, probabilities=None, sample_tape=None):
+    with _SampleTape(sample_tape, _SAMPLE_SIZE[kind]):
+        return _run_one_(kind, corr, size, params, K1, K2, return_stats, probabilities)
+
+
+def _run_one_(kind, corr, size, params, K1=None, K2=None, return_stats=False, probabilities=None):
     import ctypes
     lib = _abi.load()
     n = corr.shape[0]
@@ -119,8 +154,10 @@ def findHomography(correspondences, h1, w1, h2, w2, probabilities=None, threshol
                    spatial_coherence_weight=0.975, max_iters=10000, min_iters=50, use_sprt=True,
                    min_inlier_ratio_for_sprt=0.00001, sampler=1, neighborhood=0, neighborhood_size=4.0,
                    use_space_partitioning=True, lo_number=50, sampler_variance=0.1, solver=0, seed=0,
-                   return_stats=False):
-    """Robust homography by Graph-Cut RANSAC (reference: bindings.cpp:859-983)."""
+                   return_stats=False, sample_tape=None):
+    """Robust homography by Graph-Cut RANSAC (reference: bindings.cpp:859-983).
+    `sample_tape` [calls, 4] replays recorded minimal samples in place of the
+    main sampler's draws (gcr_set_sample_tape)."""
     if solver != 0:
         raise NotImplementedError("only point correspondences (solver=0) are provided")
     c = _check_corr(correspondences, 4, "homography")
@@ -128,14 +165,16 @@ def findHomography(correspondences, h1, w1, h2, w2, probabilities=None, threshol
                 sampler, neighborhood, neighborhood_size, lo_number, use_space_partitioning, seed,
                 min_inlier_ratio_for_sprt=min_inlier_ratio_for_sprt, sampler_variance=sampler_variance)
     return _run_one(_abi.GCR_HOMOGRAPHY, c, (h1, w1, h2, w2), p, return_stats=return_stats,
-                    probabilities=probabilities)
+                    probabilities=probabilities, sample_tape=sample_tape)
 
 
 def findFundamentalMatrix(correspondences, h1, w1, h2, w2, probabilities=None, threshold=1.0, conf=0.99,
                           spatial_coherence_weight=0.0, max_iters=10000, min_iters=50, use_sprt=True,
                           min_inlier_ratio_for_sprt=0.00001, sampler=1, neighborhood=1, neighborhood_size=20.0,
-                          lo_number=50, sampler_variance=0.1, solver=0, seed=0, return_stats=False):
-    """Robust fundamental matrix by Graph-Cut RANSAC (reference: bindings.cpp:279-401)."""
+                          lo_number=50, sampler_variance=0.1, solver=0, seed=0, return_stats=False,
+                          sample_tape=None):
+    """Robust fundamental matrix by Graph-Cut RANSAC (reference: bindings.cpp:279-401).
+    `sample_tape` [calls, 7] replays recorded minimal samples."""
     if solver != 0:
         raise NotImplementedError("only point correspondences (solver=0) are provided")
     c = _check_corr(correspondences, 7, "fundamental")
@@ -143,14 +182,16 @@ def findFundamentalMatrix(correspondences, h1, w1, h2, w2, probabilities=None, t
                 sampler, neighborhood, neighborhood_size, lo_number, False, seed,
                 min_inlier_ratio_for_sprt=min_inlier_ratio_for_sprt, sampler_variance=sampler_variance)
     return _run_one(_abi.GCR_FUNDAMENTAL, c, (h1, w1, h2, w2), p, return_stats=return_stats,
-                    probabilities=probabilities)
+                    probabilities=probabilities, sample_tape=sample_tape)
 
 
 def findEssentialMatrix(correspondences, K1, K2, h1, w1, h2, w2, probabilities=None, threshold=1.0, conf=0.99,
                         spatial_coherence_weight=0.1, max_iters=10000, min_iters=50, use_sprt=True,
                         min_inlier_ratio_for_sprt=0.01, sampler=1, neighborhood=1, neighborhood_size=20.0,
-                        lo_number=50, sampler_variance=0.1, solver=0, seed=0, return_stats=False):
-    """Robust essential matrix by Graph-Cut RANSAC (reference: bindings.cpp:710-857)."""
+                        lo_number=50, sampler_variance=0.1, solver=0, seed=0, return_stats=False,
+                        sample_tape=None):
+    """Robust essential matrix by Graph-Cut RANSAC (reference: bindings.cpp:710-857).
+    `sample_tape` [calls, 5] replays recorded minimal samples."""
     if solver != 0:
         raise NotImplementedError("only point correspondences (solver=0) are provided")
     c = _check_corr(correspondences, 5, "essential")
@@ -158,16 +199,23 @@ def findEssentialMatrix(correspondences, K1, K2, h1, w1, h2, w2, probabilities=N
                 sampler, neighborhood, neighborhood_size, lo_number, False, seed,
                 min_inlier_ratio_for_sprt=min_inlier_ratio_for_sprt, sampler_variance=sampler_variance)
     return _run_one(_abi.GCR_ESSENTIAL, c, (h1, w1, h2, w2), p, K1=K1, K2=K2, return_stats=return_stats,
-                    probabilities=probabilities)
+                    probabilities=probabilities, sample_tape=sample_tape)
 
 
-def find_batch(kind, correspondences, sizes, params, seeds=None, K=None):
+def find_batch(kind, correspondences, sizes, params, seeds=None, K=None, sample_tape=None):
     """Many pairs of one model kind in one device launch (host buffers).
 
     correspondences: list of [n_i, 4] arrays or (concatenated [sum n_i, 4], offsets [P+1]).
     sizes: [P, 4] (h1, w1, h2, w2); params: an _abi.Params; K: [P, 18] for essential matrices.
+    sample_tape: [P, calls, m] recorded minimal samples replacing the main sampler's draws.
     Returns (models [P, 3, 3], masks list of bool arrays, stats structured array).
     """
+    P = len(correspondences[1]) - 1 if isinstance(correspondences, tuple) else len(correspondences)
+    with _SampleTape(sample_tape, _SAMPLE_SIZE[kind], pairs=P):
+        return _find_batch(kind, correspondences, sizes, params, seeds, K)
+
+
+def _find_batch(kind, correspondences, sizes, params, seeds=None, K=None):
     lib = _abi.load()
     if isinstance(correspondences, tuple):
         corr, offsets = correspondences

@@ -69,6 +69,11 @@ class Params(ctypes.Structure):
     ]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("max_n", ctypes.c_int32), ("batch_calls", ctypes.c_int32),
+                ("ctas_per_sm", ctypes.c_int32), ("order", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
 class Stats(ctypes.Structure):
     _fields_ = [
         ("iteration_number", ctypes.c_int64),
@@ -110,6 +115,11 @@ _EXPORTS = {
     "gcr_batch_launch": (ctypes.c_int, [_P, _P]),
     "gcr_context_set_pair_times": (ctypes.c_int, [_P, _P]),
     "gcr_context_set_probabilities": (ctypes.c_int, [_P, _P]),
+    "gcr_context_set_flow_step_limit": (ctypes.c_int, [_P, ctypes.c_int64]),
+    "gcr_context_set_sample_tape": (ctypes.c_int, [_P, _P, ctypes.c_int64]),
+    "gcr_set_sample_tape": (ctypes.c_int, [_P, ctypes.c_int64]),
+    "gcr_context_set_tuning": (ctypes.c_int, [_P, _P, ctypes.c_int32]),
+    "gcr_context_last_tuning": (ctypes.c_int, [_P, _P]),
     "gcr_run": (ctypes.c_int, [ctypes.c_int, _P, _P, ctypes.c_int64, _P, ctypes.c_int32, _P, _P, _P, _P, _P]),
     "gcr_run_with_probabilities": (ctypes.c_int, [ctypes.c_int, _P, _P, ctypes.c_int64, _P, ctypes.c_int32, _P, _P,
                                                   _P, _P, _P, _P]),

@@ -32,7 +32,8 @@ extern "C" {
 
 typedef enum gcr_status {
   GCR_OK = 0,
-  GCR_INVALID_ARG = 1,     /* bad pointer, shape or parameter value */
+  GCR_INVALID_ARG = 1,     /* bad pointer, shape or parameter value; per pair: a
+                              coordinate that is not finite (the pair is not run) */
   GCR_TOO_FEW_POINTS = 2,  /* fewer correspondences than the minimal sample */
   GCR_NO_MODEL = 3,        /* the run ended without a model of more than m inliers */
   GCR_DEVICE_ERROR = 4,    /* a CUDA call failed, or (per pair) the engine's
@@ -213,6 +214,63 @@ gcr_status gcr_context_set_probabilities(gcr_context* ctx, const double* d_proba
  * d_times [P][2] receives the GPU global timer in nanoseconds when a CTA takes
  * pair i and when its result is written. NULL switches it off. */
 gcr_status gcr_context_set_pair_times(gcr_context* ctx, unsigned long long* d_times);
+
+/* Step limit of the labelling's maximum-flow solvers for the batches prepared
+ * on `ctx` from now on (no counterpart in the reference, whose Boykov-Kolmogorov
+ * solver, maxflow.cpp:471-607, runs unbounded): a flow problem that needs more
+ * than `steps` push / relabel steps stops, keeps the labels found so far and
+ * the pair reports GCR_TIMEOUT; the kernel returns normally. 0 restores the
+ * defaults (20,000,000 steps per grid cell, 2^24 on the radius graph). A
+ * failure-detection hook: tests set a tiny limit to check that a runaway flow
+ * ends with a status instead of a hung kernel. */
+gcr_status gcr_context_set_flow_step_limit(gcr_context* ctx, int64_t steps);
+
+/* Launch shape of the engine (no counterpart in the reference, which runs one
+ * pair per call on one thread). None of these changes a result: sampler calls
+ * are counter-based and replayed in call order, and each pair runs on one CTA
+ * whatever its place in the launch.
+ *   batch_calls  sampler calls (hypotheses) drawn, solved and scored together
+ *                per CTA, 1..256 (0: 256)
+ *   ctas_per_sm  resident engine CTAs per SM, at most what fits (0: that many)
+ *   order        0: pairs in the caller's order; 1: largest pairs first
+ * gcr_context_set_tuning installs a table for the batches prepared on ctx from
+ * now on: gcr_batch_prepare / gcr_batch_run_device use the entry of the
+ * batch's model kind with the smallest max_n at or above the batch's largest
+ * pair (no entry: the defaults). The table is what pygcransac.autotune writes:
+ * the fastest shape per kind and size bucket on a calibration batch, cached
+ * per GPU name. gcr_context_last_tuning reports the entry the last prepared
+ * batch used (max_n: the entry's bound, or the batch's largest pair). */
+typedef struct gcr_tuning {
+  int32_t kind;         /* gcr_model_kind */
+  int32_t max_n;        /* applies to batches whose largest pair has at most max_n correspondences */
+  int32_t batch_calls;
+  int32_t ctas_per_sm;
+  int32_t order;
+  int32_t reserved;     /* 0 */
+} gcr_tuning;
+
+gcr_status gcr_context_set_tuning(gcr_context* ctx, const gcr_tuning* entries, int32_t count);
+gcr_status gcr_context_last_tuning(const gcr_context* ctx, gcr_tuning* out);
+
+/* Sample tape: recorded main-sampler samples that replace the sampler's draws,
+ * so a run can replay the sample indices of another implementation — e.g. the
+ * reference's own run, recorded through the Sampler* argument of
+ * GCRANSAC::run (src/pygcransac/include/GCRANSAC.h:69-76, samplers/sampler.h:44-87).
+ * Layout: [num_pairs][calls_per_pair][m] int32 point indices (m = 4 H, 7 F,
+ * 5 E). Sampler call c of pair i (the c-th minimal sample the run asks for,
+ * counting unsuccessful ones, from 0) reads row c of block i; a call past
+ * calls_per_pair, or a row holding an index outside [0, n) (write -1 for a
+ * call on which the recording sampler failed), is an unsuccessful sampler
+ * call. Only the main sampler is replaced: the local optimisation's sampler
+ * and DEGENSAC's inner run draw as before.
+ *   gcr_context_set_sample_tape  device tape for the batches prepared on ctx
+ *                                from now on (NULL or 0 calls: draw again)
+ *   gcr_set_sample_tape          host tape read by this thread's host-buffer
+ *                                entries (gcr_find_*, gcr_find_batch, gcr_run,
+ *                                gcr_run_with_probabilities) from now on; the
+ *                                single-pair entries read block 0 */
+gcr_status gcr_context_set_sample_tape(gcr_context* ctx, const int32_t* d_tape, int64_t calls_per_pair);
+gcr_status gcr_set_sample_tape(const int32_t* h_tape, int64_t calls_per_pair);
 
 /* GCRANSAC::run on one pair (GCRANSAC.h:200-627) without the Python drivers'
  * pre- and post-processing; the entry behind the C++ plugin surface

@@ -49,9 +49,15 @@ static void fill_settings(Settings& s, const gcr_params& p) {
 
 // point probabilities of the importance sampler for the current driver call
 static thread_local const double* g_probs = nullptr;
+// sample tape of the driver calls from now on ([pairs][calls][m], see
+// oracle_set_sample_tape) and the current pair's rows
+static const int32_t* g_tape = nullptr;
+static int64_t g_tape_calls = 0;
+static thread_local const int32_t* t_tape = nullptr;
 
 static std::unique_ptr<Sampler> make_main_sampler(const gcr_params& p, const Mat& pts, size_t m,
                                                   const gcr_image_size& sz, uint64_t seed) {
+  if (t_tape) return std::make_unique<TapeSampler>(t_tape, g_tape_calls, (size_t)pts.rows);
   switch (p.sampler) {
     case GCR_SAMPLER_IMPORTANCE:
       if (!g_probs) return nullptr;
@@ -287,6 +293,26 @@ static int find_essential(const double* corr, int64_t n, const double* K1, const
   return rc;
 }
 
+// One driver call; `tape` (or NULL) holds this pair's rows of the sample tape.
+static int find_pair(int kind, const double* corr, int64_t n, const double* K1, const double* K2,
+                     const gcr_image_size* sz, const gcr_params* p, uint64_t seed, double* model_out,
+                     uint8_t* mask_out, gcr_stats* st, const int32_t* tape) {
+  gcr_stats local{};
+  gcr_stats* s = st ? st : &local;
+  std::memset(s, 0, sizeof(*s));
+  t_tape = tape;
+  int rc;
+  switch (kind) {
+    case GCR_HOMOGRAPHY: rc = find_homography(corr, n, *sz, *p, seed, model_out, mask_out, s); break;
+    case GCR_FUNDAMENTAL: rc = find_fundamental(corr, n, *sz, *p, seed, model_out, mask_out, s); break;
+    case GCR_ESSENTIAL: rc = find_essential(corr, n, K1, K2, *sz, *p, seed, model_out, mask_out, s); break;
+    default: rc = GCR_INVALID_ARG;
+  }
+  t_tape = nullptr;
+  s->status = rc;
+  return rc;
+}
+
 }  // namespace oracle
 
 using namespace oracle;
@@ -310,18 +336,7 @@ int oracle_find_prob(int kind, const double* corr, int64_t n, const double* K1, 
 int oracle_find(int kind, const double* corr, int64_t n, const double* K1, const double* K2,
                 const gcr_image_size* sz, const gcr_params* p, uint64_t seed, double* model_out,
                 uint8_t* mask_out, gcr_stats* st) {
-  gcr_stats local{};
-  gcr_stats* s = st ? st : &local;
-  std::memset(s, 0, sizeof(*s));
-  int rc;
-  switch (kind) {
-    case GCR_HOMOGRAPHY: rc = find_homography(corr, n, *sz, *p, seed, model_out, mask_out, s); break;
-    case GCR_FUNDAMENTAL: rc = find_fundamental(corr, n, *sz, *p, seed, model_out, mask_out, s); break;
-    case GCR_ESSENTIAL: rc = find_essential(corr, n, K1, K2, *sz, *p, seed, model_out, mask_out, s); break;
-    default: rc = GCR_INVALID_ARG;
-  }
-  s->status = rc;
-  return rc;
+  return find_pair(kind, corr, n, K1, K2, sz, p, seed, model_out, mask_out, st, g_tape);
 }
 
 // GCRANSAC::run alone (GCRANSAC.h:200-627) on caller-given fitting
@@ -334,6 +349,7 @@ int oracle_run(int kind, const double* points, const double* pixels, int64_t n, 
   gcr_stats local{};
   gcr_stats* s = st ? st : &local;
   std::memset(s, 0, sizeof(*s));
+  t_tape = g_tape;
   const Mat pts{points, n, 4};
   const Mat pix{pixels ? pixels : points, n, 4};
   const Grid grid = p->neighborhood == GCR_NEIGHBORHOOD_FLANN ? Grid::radius_graph(pix, p->neighborhood_size)
@@ -367,6 +383,7 @@ int oracle_run(int kind, const double* points, const double* pixels, int64_t n, 
                : run_generic<EssentialEstimator, MSACScoring>(pts, pix, est, *p, *sz, seed, &grid, t, model, inl, s, t);
     }
   }
+  t_tape = nullptr;
   std::memset(mask, 0, (size_t)n);
   for (size_t i : inl) mask[i] = 1;
   s->inlier_number = (int64_t)inl.size();
@@ -398,6 +415,15 @@ void oracle_radius_counts(const double* corr, int64_t n, double radius, int64_t*
 
 // Pair-parallel batch over `threads` host threads (one pair per thread at a
 // time, each pair single-threaded like the reference). Returns wall seconds.
+// The main sampler of the driver calls from now on reads `tape` ([pairs]
+// [calls][m] point indices, m the kind's sample size; -1 marks a failed call)
+// instead of drawing: pair i of oracle_find_batch reads block i, oracle_find
+// and oracle_run block 0. NULL switches it off.
+void oracle_set_sample_tape(const int32_t* tape, int64_t calls) {
+  g_tape = calls > 0 ? tape : nullptr;
+  g_tape_calls = g_tape ? calls : 0;
+}
+
 double oracle_find_batch(int kind, int64_t num_pairs, const double* corr, const int64_t* offsets, const double* K,
                          const gcr_image_size* sizes, const gcr_params* p, const uint64_t* seeds,
                          double* models_out, uint8_t* masks_out, gcr_stats* stats_out, int threads) {
@@ -408,8 +434,10 @@ double oracle_find_batch(int kind, int64_t num_pairs, const double* corr, const 
       if (i >= num_pairs) return;
       const int64_t o = offsets[i], n = offsets[i + 1] - offsets[i];
       const uint64_t seed = seeds ? seeds[i] : p->seed + (uint64_t)i;
-      oracle_find(kind, corr + o * 4, n, K ? K + 18 * i : nullptr, K ? K + 18 * i + 9 : nullptr, &sizes[i], p,
-                  seed, models_out + 9 * i, masks_out + o, stats_out ? stats_out + i : nullptr);
+      const int m = kind == GCR_HOMOGRAPHY ? 4 : (kind == GCR_FUNDAMENTAL ? 7 : 5);
+      const int32_t* tape = g_tape ? g_tape + (size_t)i * (size_t)g_tape_calls * m : nullptr;
+      find_pair(kind, corr + o * 4, n, K ? K + 18 * i : nullptr, K ? K + 18 * i + 9 : nullptr, &sizes[i], p,
+                seed, models_out + 9 * i, masks_out + o, stats_out ? stats_out + i : nullptr, tape);
     }
   };
   const auto t0 = std::chrono::steady_clock::now();

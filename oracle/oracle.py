@@ -64,6 +64,8 @@ def load():
                                                ctypes.c_int64, P, P, P, P]
         lib.oracle_philox.restype = None
         lib.oracle_philox.argtypes = [P, P, P]
+        lib.oracle_set_sample_tape.restype = None
+        lib.oracle_set_sample_tape.argtypes = [P, ctypes.c_int64]
         lib.oracle_draw_u32.restype = ctypes.c_uint32
         lib.oracle_draw_u32.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32]
         _lib = lib
@@ -78,9 +80,34 @@ def make_size(h1, w1, h2, w2):
     return _abi.ImageSize(int(h1), int(w1), int(h2), int(w2))
 
 
-def find(kind, corr, size, params, seed=None, K1=None, K2=None, probabilities=None):
+class _Tape:
+    """The main sampler reads `tape` ([calls, m] or [pairs, calls, m] point
+    indices, -1 for a failed call) for the calls inside the block; None
+    leaves the sampler alone."""
+
+    def __init__(self, tape):
+        self.tape = None if tape is None else np.ascontiguousarray(tape, np.int32)
+
+    def __enter__(self):
+        if self.tape is not None:
+            load().oracle_set_sample_tape(_p(self.tape), int(self.tape.shape[-2]))
+        return self
+
+    def __exit__(self, *exc):
+        if self.tape is not None:
+            load().oracle_set_sample_tape(None, 0)
+        return False
+
+
+def find(kind, corr, size, params, seed=None, K1=None, K2=None, probabilities=None, sample_tape=None):
     """Runs the oracle on one pair. Returns (status, model 3x3, mask bool[N], stats).
-    `probabilities` feed the importance sampler (sampler 3)."""
+    `probabilities` feed the importance sampler (sampler 3); `sample_tape`
+    [calls, m] replaces the main sampler's draws."""
+    with _Tape(sample_tape):
+        return _find(kind, corr, size, params, seed, K1, K2, probabilities)
+
+
+def _find(kind, corr, size, params, seed=None, K1=None, K2=None, probabilities=None):
     lib = load()
     corr = np.ascontiguousarray(corr, dtype=np.float64)
     n = corr.shape[0]
@@ -109,9 +136,15 @@ def radius_counts(corr, radius):
     return out
 
 
-def run(kind, points, pixels, cell_sizes, divisions, size, params, seed=0, probabilities=None):
+def run(kind, points, pixels, cell_sizes, divisions, size, params, seed=0, probabilities=None, sample_tape=None):
     """GCRANSAC::run alone (oracle_run): (status, model [3, 3], mask, stats).
-    `probabilities` feed the importance and AR samplers (samplers 3 and 4)."""
+    `probabilities` feed the importance and AR samplers (samplers 3 and 4);
+    `sample_tape` [calls, m] replaces the main sampler's draws."""
+    with _Tape(sample_tape):
+        return _run(kind, points, pixels, cell_sizes, divisions, size, params, seed, probabilities)
+
+
+def _run(kind, points, pixels, cell_sizes, divisions, size, params, seed=0, probabilities=None):
     lib = load()
     points = np.ascontiguousarray(points, np.float64)
     pixels = None if pixels is None else np.ascontiguousarray(pixels, np.float64)
@@ -130,8 +163,14 @@ def run(kind, points, pixels, cell_sizes, divisions, size, params, seed=0, proba
     return rc, model.reshape(3, 3), mask.astype(bool), st
 
 
-def find_batch(kind, corr, offsets, sizes, params, seeds=None, K=None, threads=1):
-    """Pair-parallel oracle batch. Returns (models [P,9], masks, stats, wall seconds)."""
+def find_batch(kind, corr, offsets, sizes, params, seeds=None, K=None, threads=1, sample_tape=None):
+    """Pair-parallel oracle batch. Returns (models [P,9], masks, stats, wall seconds).
+    `sample_tape` [P, calls, m] replaces the main sampler's draws of each pair."""
+    with _Tape(sample_tape):
+        return _find_batch(kind, corr, offsets, sizes, params, seeds, K, threads)
+
+
+def _find_batch(kind, corr, offsets, sizes, params, seeds=None, K=None, threads=1):
     lib = load()
     corr = np.ascontiguousarray(corr, np.float64)
     offsets = np.ascontiguousarray(offsets, np.int64)

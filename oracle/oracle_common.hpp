@@ -160,6 +160,31 @@ struct Sampler {
   virtual bool sample(const std::vector<size_t>& pool, size_t* subset, size_t k) = 0;
 };
 
+// A recorded sample sequence in place of the main sampler: call c returns
+// row c of the tape ([calls][k] point indices). A call past the end of the
+// tape, or a row holding an index outside [0, n) (a failed call of the
+// recording sampler is written as -1), is an unsuccessful sampler call. The
+// reference's hook for this is the Sampler* argument of GCRANSAC::run
+// (GCRANSAC.h:69-76, samplers/sampler.h:44-87).
+struct TapeSampler : Sampler {
+  const int32_t* tape;
+  int64_t calls;
+  size_t n;
+  int64_t next = 0;
+  TapeSampler(const int32_t* t, int64_t c, size_t n_) : tape(t), calls(c), n(n_) {}
+  bool sample(const std::vector<size_t>& pool, size_t* subset, size_t k) override {
+    (void)pool;
+    const int64_t c = next++;
+    if (c >= calls) return false;
+    const int32_t* row = tape + (size_t)c * k;
+    for (size_t q = 0; q < k; ++q) {
+      if (row[q] < 0 || (size_t)row[q] >= n) return false;
+      subset[q] = (size_t)row[q];
+    }
+    return true;
+  }
+};
+
 // samplers/uniform_sampler.h:97-115
 struct UniformSampler : Sampler {
   Generator gen;

@@ -3,14 +3,17 @@
 Reads stored_gamma_values from the reference checkout
 (src/pygcransac/include/gamma_values.cpp:2012) as text and writes every 100th
 entry to magsac_gamma_subset.json next to this script. Run from the repository
-root: python tests/golden/make_magsac_gamma.py [/path/to/reference]
+root with the reference checkout's path:
+python tests/golden/make_magsac_gamma.py <path to the graph-cut-ransac checkout>
 """
 import json
 import os
 import re
 import sys
 
-ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: make_magsac_gamma.py <path to the graph-cut-ransac checkout>")
+ref = sys.argv[1]
 path = os.path.join(ref, "src/pygcransac/include/gamma_values.cpp")
 text = open(path).read()
 start = text.index("stored_gamma_values[]")

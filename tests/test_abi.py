@@ -36,9 +36,9 @@ def test_struct_layout_matches_header():
 #include <stddef.h>
 #include "gcr.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(gcr_params), sizeof(gcr_stats), sizeof(gcr_image_size),
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(gcr_params), sizeof(gcr_stats), sizeof(gcr_image_size),
          offsetof(gcr_params, seed), offsetof(gcr_params, sampler), offsetof(gcr_stats, status),
-         offsetof(gcr_params, use_space_partitioning));
+         offsetof(gcr_params, use_space_partitioning), sizeof(gcr_tuning), offsetof(gcr_tuning, order));
   return 0;
 }
 '''
@@ -50,8 +50,9 @@ int main(void) {
         out = [int(v) for v in subprocess.check_output([exe]).split()]
     P, S, Z = _abi.Params, _abi.Stats, _abi.ImageSize
     import ctypes
+    T = _abi.Tuning
     assert out == [ctypes.sizeof(P), ctypes.sizeof(S), ctypes.sizeof(Z), P.seed.offset, P.sampler.offset,
-                   S.status.offset, P.use_space_partitioning.offset]
+                   S.status.offset, P.use_space_partitioning.offset, ctypes.sizeof(T), T.order.offset]
 
 
 def test_python_argument_checks(gcr):
@@ -125,3 +126,52 @@ def test_run_entries_check_probabilities_before_device_work():
                                                 ctypes.byref(size), _abi.ptr(bad), ctypes.byref(p), _abi.ptr(model),
                                                 _abi.ptr(mask), ctypes.byref(st))
             assert rc == _abi.GCR_INVALID_ARG, bad
+
+
+def test_noalloc_entry_checks_arguments_before_device_work():
+    """The allocation-free entry point applies the shared argument checks (a
+    neighbourhood other than 0 or 1 is unsupported, a grid size that is not a
+    number or above 1024 divisions is refused) and its own limits (samplers
+    0-2, MSAC, the grid with a spatial term) before any device call; the
+    dummy device pointers are never dereferenced."""
+    lib = _abi.load()
+    size = _abi.ImageSize(h1=480, w1=640, h2=480, w2=640)
+    dummy = ctypes.c_void_p(16)
+
+    def call(**kw):
+        base = dict(threshold=3.0, confidence=0.99, spatial_coherence_weight=0.975, neighborhood_size=4,
+                    max_iterations=100, min_iterations=50, sampler=0, neighborhood=0, lo_number=50)
+        base.update(kw)
+        p = _abi.Params(**base)
+        return lib.gcr_find_homography_device_noalloc(dummy, 1000, ctypes.byref(size), ctypes.byref(p), 0, dummy,
+                                                      dummy, dummy, None)
+
+    assert call(spatial_coherence_weight=0.0, neighborhood=7) == _abi.GCR_UNSUPPORTED
+    assert call(neighborhood=7) == _abi.GCR_UNSUPPORTED
+    assert call(neighborhood_size=float("nan")) == _abi.GCR_INVALID_ARG
+    assert call(neighborhood_size=0.5) == _abi.GCR_INVALID_ARG
+    assert call(neighborhood_size=1e12) == _abi.GCR_UNSUPPORTED
+    assert call(spatial_coherence_weight=0.0, neighborhood=1, neighborhood_size=float("inf")) == _abi.GCR_INVALID_ARG
+    assert call(spatial_coherence_weight=0.5, neighborhood=1, neighborhood_size=20) == _abi.GCR_UNSUPPORTED
+    assert call(sampler=3) == _abi.GCR_UNSUPPORTED
+    assert call(scoring=_abi.GCR_SCORING_MAGSAC) == _abi.GCR_UNSUPPORTED
+    assert call(threshold=-1.0) == _abi.GCR_INVALID_ARG
+
+
+def test_batch_entry_refuses_grid_sizes_beyond_the_cell_key():
+    """The batch entry refuses a grid of more than 1024 divisions per axis
+    (cell keys hold 10 bits per axis) before any device work."""
+    lib = _abi.load()
+    n = 40
+    pts = np.random.default_rng(2).uniform(0, 480, (n, 4))
+    offsets = np.array([0, n], np.int64)
+    sz = np.zeros(1, _abi.SIZE_DTYPE)
+    sz[0] = (480, 640, 480, 640)
+    p = _abi.Params(threshold=3.0, confidence=0.99, spatial_coherence_weight=0.975, neighborhood_size=5000,
+                    max_iterations=100, min_iterations=50, sampler=0, neighborhood=0, lo_number=50)
+    models = np.zeros(9)
+    masks = np.zeros(n, np.uint8)
+    stats = np.zeros(1, _abi.STATS_DTYPE)
+    rc = lib.gcr_find_batch(_abi.GCR_HOMOGRAPHY, 1, _abi.ptr(pts), _abi.ptr(offsets), None, _abi.ptr(sz),
+                            ctypes.byref(p), None, _abi.ptr(models), _abi.ptr(masks), _abi.ptr(stats))
+    assert rc == _abi.GCR_UNSUPPORTED and "1024" in _abi.last_error()

@@ -168,3 +168,29 @@ def test_oracle_run_with_probabilities(oracle, sampler):
     assert S.homography_error(M / M[2, 2], pr["H_gt"]) < 1.0
     rc2, _, _, _ = oracle.run(_abi.GCR_HOMOGRAPHY, pr["corr"], pr["corr"], cells, 4, size, p, seed=3)
     assert rc2 == _abi.GCR_UNSUPPORTED
+
+
+def test_oracle_sample_tape_replays_its_own_draws(oracle):
+    """The oracle's main sampler replaced by a tape of its own draws runs the
+    same search (every count and the mask); a tape of other draws changes the
+    run; a tape that ends early or holds -1 rows fails those calls."""
+    from pygcransac import synthetic as S
+    pr = S.homography_pair(3, n=600)
+    sz = oracle.make_size(*pr["size"])
+    p = _abi.Params(threshold=3.0, confidence=0.99, spatial_coherence_weight=0.975, neighborhood_size=4,
+                    max_iterations=10000, min_iterations=50, sampler=0, neighborhood=0, lo_number=50, seed=0)
+    rc, H, mask, st = oracle.find(0, pr["corr"], sz, p, seed=11)
+    own, ok = oracle.sample_sequence(0, pr["corr"], 4, 11, 5000, sz)
+    assert ok.all()
+    rc2, H2, mask2, st2 = oracle.find(0, pr["corr"], sz, p, seed=11, sample_tape=own)
+    assert rc == rc2 == 0 and np.array_equal(mask, mask2) and np.array_equal(H, H2)
+    assert (st.iteration_number, st.graph_cut_number, st.models_scored) == \
+        (st2.iteration_number, st2.graph_cut_number, st2.models_scored)
+    other, _ = oracle.sample_sequence(0, pr["corr"], 4, 99, 5000, sz)
+    _, _, _, st3 = oracle.find(0, pr["corr"], sz, p, seed=11, sample_tape=other)
+    assert (st3.iteration_number, st3.models_scored) != (st.iteration_number, st.models_scored)
+    # no usable call at all: 100 failed calls per iteration until the budget ends
+    dead = np.full((300, 4), -1, np.int32)
+    p.max_iterations = 200
+    rc4, _, mask4, st4 = oracle.find(0, pr["corr"], sz, p, seed=11, sample_tape=dead)
+    assert rc4 == _abi.GCR_NO_MODEL and not mask4.any() and st4.iteration_number >= 200

@@ -1,7 +1,9 @@
 """GPU test of gcr_find_homography_device_noalloc, the allocation-free
 single-pair entry point, through the C-ABI: two calls in a row on one stream
 must give the masks, statistics and (within 1e-6 relative Frobenius error)
-the models of the allocating entry point gcr_find_batch on the same pairs.
+the models of the allocating entry point gcr_find_batch on the same pairs,
+for each sampler the entry point provides (uniform, PROSAC, P-NAPSAC) and with
+SPRT and space partitioning, alone and together.
 The file name sorts last so that the test also runs after every other test."""
 import ctypes
 
@@ -15,9 +17,22 @@ pytestmark = pytest.mark.gpu
 MODEL_TOL = 1e-6
 
 
-def h_params():
-    return _abi.Params(threshold=3.0, confidence=0.99, spatial_coherence_weight=0.975, neighborhood_size=4,
-                       max_iterations=10000, min_iterations=50, sampler=0, neighborhood=0, lo_number=50, seed=0)
+def h_params(**kw):
+    base = dict(threshold=3.0, confidence=0.99, spatial_coherence_weight=0.975, neighborhood_size=4,
+                max_iterations=10000, min_iterations=50, sampler=0, neighborhood=0, lo_number=50, seed=0,
+                min_inlier_ratio_for_sprt=1e-5)
+    base.update(kw)
+    return _abi.Params(**base)
+
+
+CONFIGS = {
+    "uniform": {},
+    "prosac": dict(sampler=1),
+    "pnapsac": dict(sampler=2),
+    "sprt": dict(use_sprt=1),
+    "space_partitioning": dict(use_space_partitioning=1),
+    "sprt_and_space_partitioning": dict(sampler=1, use_sprt=1, use_space_partitioning=1),
+}
 
 
 def rel_model_err(a, b):
@@ -26,10 +41,11 @@ def rel_model_err(a, b):
     return min(np.linalg.norm(a - b), np.linalg.norm(a + b))
 
 
-def test_noalloc_matches_allocating_entry(gcr):
+@pytest.mark.parametrize("config", sorted(CONFIGS))
+def test_noalloc_matches_allocating_entry(gcr, config):
     torch = pytest.importorskip("torch")
     lib = _abi.load()
-    p = h_params()
+    p = h_params(**CONFIGS[config])
     cases = [(S.homography_pair(5, n=2000), 7), (S.homography_pair(6, n=4096, inlier_ratio=0.3), 8)]
     stream = torch.cuda.current_stream()
     outs = []
