@@ -37,10 +37,11 @@ def compile_one(src, extra, out=OUT):
     return obj, r.stderr
 
 
-def build(jobs=4, verbose=False, extra=(), out=OUT):
-    """Compiles every source with `extra` nvcc flags into `out`/libgcr.so."""
+def build(jobs=4, verbose=False, extra=(), out=OUT, sources=None):
+    """Compiles every source (or `sources`) with `extra` nvcc flags into
+    `out`/libgcr.so."""
     os.makedirs(out, exist_ok=True)
-    srcs = [s for s in SOURCES if os.path.exists(os.path.join(CSRC, s))]
+    srcs = [s for s in (sources or SOURCES) if os.path.exists(os.path.join(CSRC, s))]
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
         results = list(ex.map(lambda s: compile_one(s, list(extra), out), srcs))
     objs = [o for o, _ in results]

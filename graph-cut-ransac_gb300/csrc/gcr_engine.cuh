@@ -2604,10 +2604,13 @@ struct Engine {
     sync();
   }
 
+  // sampler calls per batch, within [1, GCR_BLOCK] whatever the parameter holds
+  __device__ __forceinline__ int calls_per_batch() const { return max(1, min(GCR_BLOCK, prm.batch_calls)); }
+
   __device__ int generate_batch(long long a0, long long& p_kth, long long& p_subset, long long& p_hi,
                                 double& p_Tn, long long& p_Tprime) {
     const int j = threadIdx.x;
-    const int B = prm.batch_calls;  // calls of this batch: a0 .. a0 + B - 1, one per thread j < B
+    const int B = calls_per_batch();  // calls of this batch: a0 .. a0 + B - 1, one per thread j < B
     int s[Est::M];
 #pragma unroll
     for (int q = 0; q < Est::M; ++q) s[q] = 0;
@@ -2769,8 +2772,8 @@ struct Engine {
       if (!sprt && !(sp && !mag)) score_models_f32(0, K);
       tock(2, t0);
       bool restart = false;
-      long long next_attempt = attempt + prm.batch_calls;
-      for (int j = 0; j < prm.batch_calls; ++j) {
+      long long next_attempt = attempt + calls_per_batch();
+      for (int j = 0; j < calls_per_batch(); ++j) {
         if (!in_iter) {
           const long long lim = max_iter < max_iters ? max_iter : max_iters;
           if (!(min_iters > iter || iter < lim)) {
