@@ -112,6 +112,7 @@ struct gcr_context {
   std::vector<gcr_tuning> tuning;            // see gcr_context_set_tuning
   DevBuf order;                              // pair of each work ticket (largest first)
   gcr_tuning last_tuning{};                  // the entry the last prepared batch used
+  int32_t lo_fp32 = 0;                       // see gcr_context_set_lo_precision
 };
 
 namespace gcr {
@@ -497,6 +498,7 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
   prm.tape = c->tape;
   prm.tape_calls = c->tape ? c->tape_calls : 0;
   prm.batch_calls = tune.batch_calls;
+  prm.lo_fp32 = c->lo_fp32;
   prm.cdf = nullptr;
   prm.neighborhood = 0;
   prm.radius2 = 0.0;
@@ -703,6 +705,15 @@ gcr_status gcr_context_set_tuning(gcr_context* c, const gcr_tuning* entries, int
       return fail(GCR_INVALID_ARG, "tuning entry %d: bad ctas_per_sm, order or max_n", i);
   }
   c->tuning.assign(entries, entries + count);
+  c->pending.valid = false;
+  return GCR_OK;
+}
+
+gcr_status gcr_context_set_lo_precision(gcr_context* c, int32_t precision) {
+  if (!c) return fail(GCR_INVALID_ARG, "context is NULL");
+  if (precision != GCR_LO_FP64 && precision != GCR_LO_FP32)
+    return fail(GCR_INVALID_ARG, "precision must be GCR_LO_FP64 (0) or GCR_LO_FP32 (1)");
+  c->lo_fp32 = precision == GCR_LO_FP32 ? 1 : 0;
   c->pending.valid = false;
   return GCR_OK;
 }

@@ -27,6 +27,7 @@
 #include "gcr_fundamental.cuh"
 #include "gcr_homography.cuh"
 #include "gcr_linalg.cuh"
+#include "gcr_lo_f32.cuh"
 
 namespace gcr {
 
@@ -121,6 +122,9 @@ struct EngineParams {
   // calls are counter-based and replayed in call order, so any batch size
   // gives the same results (a tuning knob)
   int32_t batch_calls;
+  // 1: the local optimisation's fundamental-matrix fits in FP32 (lo32::
+  // fit_fundamental); 0: in FP64, the oracle's arithmetic (parity)
+  int32_t lo_fp32;
 };
 
 // Per-pair inputs prepared on the device.
@@ -252,6 +256,7 @@ struct Shared {
   int bad_row;                    // a row index read from a list fell outside the pair
   int ar_size;                    // entries in the AR sampler's heap
   int ar_overflow;
+  int big_cells;                  // grid cells of the current labelling above kMaxFlowCap points
 };
 
 // GCRANSAC::getIterationNumber (GCRANSAC.h:156-172)
@@ -1282,6 +1287,160 @@ struct Engine {
     }
   }
 
+  // ------------------------------------------------------------------
+  // Minimum cut of one grid cell of n > kMaxFlowCap points by its closed form
+  // (the whole CTA; `scratch` holds n ints and is free during the cut).
+  //
+  // A cell is a clique. With label 1 = SINK (inlier), 0 = SOURCE, the unary
+  // energies of GCRANSAC::labeling (GCRANSAC.h:945-961; a point's terminal
+  // capacity tr_i = E1_i - E0_i) and the pairwise terms of every pair of the
+  // cell (add_term2(i, j, lambda (d_i + d_j) / 2, lambda, lambda, 0),
+  // GCRANSAC.h:965-1007), the energy of a source set T of t points is
+  //   E(T) = sum_i E1_i + sum_{i in T} (a_i + c_t d_i) + lambda t (n - t),
+  //   a_i = -tr_i,  c_t = lambda (t - 1) / 2,
+  // because the pairs inside T cost lambda (d_i + d_j) / 2 each and the
+  // mixed pairs lambda. For a fixed t the best T is the t points of smallest
+  // key a_i + c_t d_i, and the keys have a simple order: every point beyond the
+  // threshold has d = 1 and a = -(1 - lambda) (one shared key), and every
+  // point within it has a = (1 - lambda)(1 - d), a key monotone in d. So after
+  // one sort of the inliers by d, the minimum over all T of each size t is a
+  // prefix sum, and the cut is the size of lowest energy. The maximum flow's
+  // SINK side (what_segment, graph.h:478-483) is the smallest minimising sink
+  // set, i.e. the largest minimising T: the largest t whose energy is within
+  // rounding of the minimum. Writes slot.flag for the cell's points.
+  __device__ void clique_cut_cta(int c0, int n, int* scratch) {
+    const double lam = prm.lambda;
+    const double oml = 1.0 - lam;
+    const int* gp = slot.cell_pts + c0;
+    const int tid = threadIdx.x;
+    // inliers (tr <= 0) of the cell: keys = (d bits, cell position); the d
+    // bits of d in [0, 1] order like d, their two top bits are zero, and the
+    // low bits the position needs are dropped
+    const int ib = 32 - __clz(n);
+    const unsigned long long low = (1ull << ib) - 1ull;
+    unsigned long long* keys = slot.sortbuf;
+    int m = 0;
+    for (int base = 0; base < n; base += GCR_BLOCK) {
+      const int k = base + tid;
+      int f = 0;
+      if (k < n) f = slot.tr[gp[k]] > 0 ? 0 : 1;
+      int tot;
+      const int pos = block_exclusive_scan(f, sh.red_i, &tot);
+      if (f) {
+        const unsigned long long db = (unsigned long long)__double_as_longlong(slot.dres[gp[k]]);
+        keys[m + pos] = ((db << 2) & ~low) | (unsigned long long)k;
+      }
+      m += tot;
+    }
+    const int n_out = n - m;
+    int sn = 1;
+    while (sn < m) sn <<= 1;
+    for (int i = m + tid; i < sn; i += GCR_BLOCK) keys[i] = ~0ull;
+    sync();
+    if (m > 1) block_bitonic_sort(keys, sn);
+    // sorted inliers: the point of each rank (ascending d) into scratch, then
+    // the exclusive prefix sums of d over that order into the key array
+    for (int j = tid; j < m; j += GCR_BLOCK) scratch[j] = gp[(int)(keys[j] & low)];
+    sync();
+    double* D = reinterpret_cast<double*>(keys);
+    double carry = 0.0;
+    for (int base = 0; base < m; base += GCR_BLOCK) {
+      const int j = base + tid;
+      const double v = j < m ? slot.dres[scratch[j]] : 0.0;
+      double x = v;
+      const int lane = tid & 31, w = tid >> 5;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const double y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+      }
+      sync();
+      if (lane == 31) sh.red_d[w] = x;
+      sync();
+      double wb = 0.0, tot = 0.0;
+      for (int q = 0; q < GCR_WARPS; ++q) {
+        if (q < w) wb += sh.red_d[q];
+        tot += sh.red_d[q];
+      }
+      if (j < m) D[j] = carry + wb + (x - v);
+      carry += tot;
+      sync();
+    }
+    const double Dm = carry;
+    // r-th smallest inlier key at slope s = c - (1 - lambda): ascending d for
+    // s >= 0, descending d otherwise
+    auto d_at = [&](int j) { return slot.dres[scratch[j]]; };
+    auto pref = [&](int j) { return j >= m ? Dm : D[j]; };
+    auto inl_sum = [&](int j, double sl) {  // the j smallest inlier keys
+      return sl >= 0 ? oml * j + sl * pref(j) : oml * j + sl * (Dm - pref(m - j));
+    };
+    auto count_le = [&](double sl, double ko) {  // inliers with key <= ko
+      int lo = 0, hi = m;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        const double d = d_at(sl >= 0 ? mid : m - 1 - mid);
+        if (oml + sl * d <= ko) lo = mid + 1;
+        else hi = mid;
+      }
+      return lo;
+    };
+    auto energy = [&](int t) -> double {  // E(T) - sum_i E1_i of the best T of size t
+      if (t == 0) return 0.0;
+      const double c = 0.5 * lam * (double)(t - 1);
+      const double sl = c - oml, ko = c - oml;
+      const int J = count_le(sl, ko);
+      double S;
+      if (t <= J) S = inl_sum(t, sl);
+      else if (t <= J + n_out) S = inl_sum(J, sl) + (double)(t - J) * ko;
+      else S = inl_sum(t - n_out, sl) + (double)n_out * ko;
+      return S + lam * (double)t * (double)(n - t);
+    };
+    double fmin = 0.0;
+    for (int t = tid; t <= n; t += GCR_BLOCK) {
+      const double e = energy(t);
+      fmin = e < fmin ? e : fmin;
+    }
+    fmin = warp_min(fmin);
+    sync();
+    if ((tid & 31) == 0) sh.red_d[tid >> 5] = fmin;
+    sync();
+    for (int q = 0; q < GCR_WARPS; ++q) fmin = sh.red_d[q] < fmin ? sh.red_d[q] : fmin;
+    // rounding bound of the energies: |terms| <= (1 - lambda) n + lambda (n - 1) / 2 Dm + lambda n^2 / 4
+    const double tol = 1e-12 * (1.0 + oml * n + 0.5 * lam * (double)(n - 1) * Dm + 0.25 * lam * (double)n * n);
+    int tmax = 0;
+    for (int t = tid; t <= n; t += GCR_BLOCK)
+      if (energy(t) <= fmin + tol) tmax = t > tmax ? t : tmax;
+    tmax = -warp_min(-tmax);
+    sync();
+    if ((tid & 31) == 0) sh.red_i[tid >> 5] = tmax;
+    sync();
+    for (int q = 0; q < GCR_WARPS; ++q) tmax = sh.red_i[q] > tmax ? sh.red_i[q] : tmax;
+    sync();
+    // the source set of size tmax: its inliers by key rank, its outliers by index
+    const double c = 0.5 * lam * (double)(tmax - 1);
+    const double sl = c - oml;
+    int in_T = 0;
+    if (tmax > 0) {
+      const int J = count_le(sl, sl);
+      in_T = tmax <= J ? tmax : (tmax <= J + n_out ? J : tmax - n_out);
+    }
+    const int out_T = tmax - in_T;
+    for (int j = tid; j < m; j += GCR_BLOCK) {
+      const int r = sl >= 0 ? j : m - 1 - j;
+      slot.flag[scratch[j]] = r < in_T ? 0 : 1;
+    }
+    int seen = 0;
+    for (int base = 0; base < n; base += GCR_BLOCK) {
+      const int k = base + tid;
+      const int f = (k < n && slot.tr[gp[k]] > 0) ? 1 : 0;
+      int tot;
+      const int pos = block_exclusive_scan(f, sh.red_i, &tot);
+      if (f) slot.flag[gp[k]] = seen + pos < out_T ? 0 : 1;
+      seen += tot;
+    }
+    sync();
+  }
+
   __device__ int labeling(const double* model, int ncells, int* list) {
     const double sq = t2;  // thr^2 * 9 / 4
     const double oml = 1.0 - prm.lambda;
@@ -1331,6 +1490,8 @@ struct Engine {
       if (rg_ok) radius_mincut();
       sync();
     }
+    if (threadIdx.x == 0) sh.big_cells = 0;
+    sync();
     for (int c = warp; pairwise && prm.neighborhood == 0 && c < ncells; c += GCR_WARPS) {
       const int c0 = slot.cell_start[c], n = slot.cell_start[c + 1] - c0;
       if (c0 < 0 || n < 1 || c0 + n > N) {  // inconsistent cell table: skip, report
@@ -1339,12 +1500,34 @@ struct Engine {
       }
       if (n == 1) continue;  // unary label, set above
       if (n > kMaxFlowCap) {
-        if (lane == 0) atomicMax(&sh.flow_status, ST_CAPACITY);
+        if (lane == 0) atomicAdd(&sh.big_cells, 1);  // cut below by the whole CTA
       } else if (!mincut_cell(c0, n, warp)) {
         if (lane == 0) atomicMax(&sh.flow_status, ST_TIMEOUT);
       }
     }
     sync();
+    // cells above the warp solver's capacity: one at a time by the CTA, in
+    // cell order, with the list scratch that the labelled inliers fill later
+    if (sh.big_cells > 0) {
+      for (int base = 0; base < ncells; base += GCR_BLOCK) {
+        const int c = base + threadIdx.x;
+        int f = 0;
+        if (c < ncells) {
+          const int c0 = slot.cell_start[c], n = slot.cell_start[c + 1] - c0;
+          f = (c0 >= 0 && n > kMaxFlowCap && c0 + n <= N) ? 1 : 0;
+        }
+        int tot;
+        const int pos = block_exclusive_scan(f, sh.red_i, &tot);
+        if (f) sh.s_cnt[pos] = c;
+        sync();
+        for (int q = 0; q < tot; ++q) {
+          const int cc = sh.s_cnt[q];
+          const int c0 = slot.cell_start[cc];
+          clique_cut_cta(c0, slot.cell_start[cc + 1] - c0, list);
+        }
+        sync();
+      }
+    }
     if (sh.flow_status != 0 && status == ST_OK) status = sh.flow_status;
     // flags are read as booleans, so the list never holds more than N points
     int total = 0;
@@ -1865,7 +2048,10 @@ struct Engine {
               }
               __syncwarp(gmask);
               bool ok = sh.lo_ok[u] != 0;
-              if (ok) ok = FundamentalModel::fit_group(pts64, smp, ss, slot.models64 + 9 * (kb + u), q, gmask);
+              if (ok)
+                ok = prm.lo_fp32 ? lo32::fit_fundamental(pts32, pd.centre, smp, ss, slot.models64 + 9 * (kb + u), q,
+                                                         gmask, 4)
+                                 : FundamentalModel::fit_group(pts64, smp, ss, slot.models64 + 9 * (kb + u), q, gmask);
               __syncwarp(gmask);
               if (q == 0) {
                 sh.lo_ok[u] = ok ? 1 : 0;

@@ -203,6 +203,7 @@ extern "C" gcr_status gcr_find_homography_device_noalloc(const double* d_corr, i
   prm.use_sp = p.use_space_partitioning ? 1 : 0;
   prm.epilogue = 1;
   prm.batch_calls = GCR_BLOCK;
+  prm.lo_fp32 = 0;
   prm.sprt_min_ratio = p.min_inlier_ratio_for_sprt;
 
   single_pair_kernel<<<1, GCR_BLOCK, gcr::shared_bytes<Est>(), (cudaStream_t)stream>>>(ws, prm, pd, slot);

@@ -35,6 +35,9 @@ GCR_SAMPLER_PNAPSAC = 2
 GCR_SAMPLER_IMPORTANCE = 3
 GCR_SAMPLER_AR = 4
 
+GCR_LO_FP64 = 0
+GCR_LO_FP32 = 1
+
 GCR_HOMOGRAPHY = 0
 GCR_FUNDAMENTAL = 1
 GCR_ESSENTIAL = 2
@@ -120,6 +123,7 @@ _EXPORTS = {
     "gcr_set_sample_tape": (ctypes.c_int, [_P, ctypes.c_int64]),
     "gcr_context_set_tuning": (ctypes.c_int, [_P, _P, ctypes.c_int32]),
     "gcr_context_last_tuning": (ctypes.c_int, [_P, _P]),
+    "gcr_context_set_lo_precision": (ctypes.c_int, [_P, ctypes.c_int32]),
     "gcr_run": (ctypes.c_int, [ctypes.c_int, _P, _P, ctypes.c_int64, _P, ctypes.c_int32, _P, _P, _P, _P, _P]),
     "gcr_run_with_probabilities": (ctypes.c_int, [ctypes.c_int, _P, _P, ctypes.c_int64, _P, ctypes.c_int32, _P, _P,
                                                   _P, _P, _P, _P]),

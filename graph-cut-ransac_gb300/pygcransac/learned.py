@@ -229,7 +229,8 @@ class LearnedBatch:
     kernels (no host work, no allocation), so it can be recorded into a CUDA
     graph after `prepare`."""
 
-    def __init__(self, proposal, kind, d_corr, offsets, sizes, params, seeds=None, K=None, ctx=None):
+    def __init__(self, proposal, kind, d_corr, offsets, sizes, params, seeds=None, K=None, ctx=None,
+                 lo_precision=_abi.GCR_LO_FP64):
         torch = _torch()
         self.lib = _abi.load()
         self.proposal = proposal
@@ -256,6 +257,9 @@ class LearnedBatch:
         self.ctx = ctypes.c_void_p() if ctx is None else ctx
         if self.own_ctx:
             _check(self.lib.gcr_context_create(ctypes.byref(self.ctx)), "context_create")
+        # GCR_LO_FP32: the local optimisation's F fits in FP32 (the engine's
+        # fast mode for throughput forms; GCR_LO_FP64 keeps the oracle's arithmetic)
+        _check(self.lib.gcr_context_set_lo_precision(self.ctx, int(lo_precision)), "set_lo_precision")
         self.params = _abi.Params(**{f: getattr(params, f) for f, _ in params._fields_})
         self.params.sampler = 1
         self.seeds = None if seeds is None else np.ascontiguousarray(seeds, np.uint64)
@@ -298,17 +302,19 @@ class LearnedBatch:
             self.ctx = None
 
 
-def find_batch_learned(kind, correspondences, sizes, params, proposal, seeds=None, K=None):
+def find_batch_learned(kind, correspondences, sizes, params, proposal, seeds=None, K=None,
+                       lo_precision=_abi.GCR_LO_FP64):
     """`find_batch` with the learned order driving PROSAC (params.sampler is
     set to 1). Same arguments and returns as pygcransac.find_batch, plus the
-    trained `proposal`."""
+    trained `proposal` and the local optimisation's arithmetic
+    (`lo_precision`, GCR_LO_FP64 or GCR_LO_FP32)."""
     torch = _torch()
     lens = [len(c) for c in correspondences]
     offsets = np.zeros(len(lens) + 1, np.int64)
     offsets[1:] = np.cumsum(lens)
     d_corr = torch.from_numpy(np.ascontiguousarray(np.concatenate(correspondences, 0), np.float64)).to(
         proposal.device)
-    b = LearnedBatch(proposal, kind, d_corr, offsets, sizes, params, seeds, K)
+    b = LearnedBatch(proposal, kind, d_corr, offsets, sizes, params, seeds, K, lo_precision=lo_precision)
     try:
         b.prepare()
         b.launch()

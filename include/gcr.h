@@ -252,6 +252,22 @@ typedef struct gcr_tuning {
 gcr_status gcr_context_set_tuning(gcr_context* ctx, const gcr_tuning* entries, int32_t count);
 gcr_status gcr_context_last_tuning(const gcr_context* ctx, gcr_tuning* out);
 
+/* Arithmetic of the local optimisation's fundamental-matrix fits for the
+ * batches prepared on `ctx` from now on (no counterpart in the reference, which
+ * computes in double throughout):
+ *   GCR_LO_FP64  (default) the reference's arithmetic: masks and counts equal
+ *                the FP64 oracle's
+ *   GCR_LO_FP32  the fits of the graph-cut local optimisation (8-point start
+ *                and Levenberg-Marquardt on the factorised F) run in FP32 from
+ *                the FP32 correspondence tile; each fit is still scored with
+ *                exact inlier decisions, and the final iteratively reweighted
+ *                fits and the drivers' bundle adjustment stay FP64. Models
+ *                agree with the FP64 fits to model tolerance, masks can differ
+ *                in borderline points. For throughput forms (the learned
+ *                proposal), not for parity runs. */
+enum { GCR_LO_FP64 = 0, GCR_LO_FP32 = 1 };
+gcr_status gcr_context_set_lo_precision(gcr_context* ctx, int32_t precision);
+
 /* Sample tape: recorded main-sampler samples that replace the sampler's draws,
  * so a run can replay the sample indices of another implementation — e.g. the
  * reference's own run, recorded through the Sampler* argument of
