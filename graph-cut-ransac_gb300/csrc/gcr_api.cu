@@ -14,6 +14,7 @@
 #include "../../include/gcr.h"
 #include "gcr_engine.cuh"
 #include "gcr_kinds.h"
+#include "gcr_launch.cuh"
 
 namespace {
 
@@ -82,7 +83,7 @@ void set_last_error(const char* msg) { g_last_error = msg; }
 struct gcr_context {
   int device = 0;
   int num_sms = 0;
-  DevBuf pairs, slots_meta, slot_mem, pts32, ticket, norm_pts, kinv, row_pair, phase;
+  DevBuf pairs, slots_meta, slot_mem, pts32, ticket, norm_pts, kinv, row_pair, phase, aux;
   // staging of the host-buffer entry points
   DevBuf corr, models, masks, stats;
   DevBuf magsac;  // the MAGSAC++ weight table, uploaded on first use
@@ -249,7 +250,7 @@ gcr_status gcr_context_create(gcr_context** ctx) {
 
 gcr_status gcr_context_destroy(gcr_context* c) {
   if (!c) return GCR_OK;
-  for (DevBuf* b : {&c->pairs, &c->slots_meta, &c->slot_mem, &c->pts32, &c->ticket, &c->norm_pts, &c->kinv,
+  for (DevBuf* b : {&c->pairs, &c->slots_meta, &c->slot_mem, &c->pts32, &c->aux, &c->ticket, &c->norm_pts, &c->kinv,
                     &c->row_pair, &c->phase, &c->corr, &c->models, &c->masks, &c->stats, &c->magsac, &c->rg_int,
                     &c->rg_dbl, &c->rg_px, &c->ar_p, &c->ar_i, &c->ar_ab, &c->ar_cnt, &c->cdf, &c->probs_stage, &c->tape_stage, &c->order})
     b->release();
@@ -436,7 +437,9 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
     CUDA_TRY(c->norm_pts.ensure(sizeof(double) * 4 * (size_t)std::max<int64_t>(total, 1)));
     run_pts = (const double*)c->norm_pts.p;
   }
-  if (max_n > gcr::kSmemPoints) CUDA_TRY(c->pts32.ensure(sizeof(float4) * (size_t)total));
+  // the centred FP32 copy of every pair (staging kernel) and its per-pair results
+  CUDA_TRY(c->pts32.ensure(sizeof(float4) * (size_t)std::max<int64_t>(total, 1)));
+  CUDA_TRY(c->aux.ensure(sizeof(gcr::PairAux) * (size_t)num_pairs));
   CUDA_TRY(c->ticket.ensure(sizeof(int)));
   // largest pairs first: a persistent CTA that takes a big pair late would
   // otherwise finish long after the others (stable order among equal sizes)
@@ -466,6 +469,7 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
   ws.phase = nullptr;
   ws.times = c->pair_times;
   ws.order = d_order;
+  ws.aux = (const gcr::PairAux*)c->aux.p;
 #ifdef GCR_PHASE_PROFILE
   CUDA_TRY(c->phase.ensure(sizeof(long long) * 16 * num_pairs));
   CUDA_TRY(cudaMemsetAsync(c->phase.p, 0, sizeof(long long) * 16 * num_pairs, s));
@@ -596,6 +600,8 @@ static gcr_status launch_batch(gcr_context* c, const gcr_context::Pending& L, cu
     CUDA_TRY(gcr::launch_importance_cdf(L.probs, (const gcr::PairDesc*)c->pairs.p, L.num_pairs, (double*)c->cdf.p, s));
     ++launches;
   }
+  CUDA_TRY(gcr::launch_centre(L.ws, (gcr::PairAux*)c->aux.p, L.num_pairs, s));
+  ++launches;
   CUDA_TRY(L.ops->launch(L.grid, s, L.ws, L.prm));
   g_last_launches = launches;
   return GCR_OK;
@@ -620,6 +626,33 @@ __global__ void importance_cdf_kernel(const double* probs, const PairDesc* pairs
     c[i] = acc;
   }
   if (pd.n > 0) c[pd.n - 1] = 1.0;
+}
+
+// Staging kernel, one CTA per pair (grid-stride over pairs): the centred FP32
+// copy of the pair's fitting coordinates into ws.pts32, its largest centred
+// magnitude and its non-finite flag into aux.
+__global__ void __launch_bounds__(GCR_BLOCK) centre_kernel(Workspace ws, PairAux* aux, int num_pairs) {
+  __shared__ double red[GCR_WARPS];
+  for (int pair = blockIdx.x; pair < num_pairs; pair += gridDim.x) {
+    const PairDesc pd = ws.pairs[pair];
+    double mx = 0.0;
+    const int bad = load_pair_tile(ws, pd, ws.pts64 + 4 * pd.offset, ws.pts32 + pd.offset, mx);
+    const double scale = block_max_abs(mx, red);
+    const int any_bad = __syncthreads_or(bad);
+    if (threadIdx.x == 0) {
+      PairAux a;
+      a.scale = scale;
+      a.bad = any_bad ? 1 : 0;
+      a.pad = 0;
+      aux[pair] = a;
+    }
+  }
+}
+
+cudaError_t launch_centre(const Workspace& ws, PairAux* aux, int num_pairs, cudaStream_t s) {
+  const int grid = std::min(num_pairs, 65535);
+  centre_kernel<<<grid, GCR_BLOCK, 0, s>>>(ws, aux, num_pairs);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_importance_cdf(const double* probs, const PairDesc* pairs, int num_pairs, double* cdf,

@@ -179,10 +179,19 @@ struct Slot {
                         // x4, hits, subset sizes, layers, growth table
 };
 
+// Per-pair results of the staging kernel (centre_kernel): the largest
+// centred magnitude of the pair's coordinates (the FP32 error bounds scale
+// with it) and whether a coordinate is not finite.
+struct PairAux {
+  double scale;
+  int32_t bad;
+  int32_t pad;
+};
+
 struct Workspace {
   const double* pts64;  // [total][4] coordinates the model is fitted in
   const double* pix64;  // [total][4] pixel coordinates for the grid
-  float4* pts32;        // [total] centred FP32 copy of pts64 (pairs too large for shared memory)
+  float4* pts32;        // [total] centred FP32 copy of pts64, written by centre_kernel before the engine runs
   const PairDesc* pairs;
   Slot* slots;
   Slot* nested_slots;   // light slots of DEGENSAC's inner run (fundamental matrices)
@@ -193,6 +202,7 @@ struct Workspace {
   long long* phase;     // [P][16] phase cycle counters (GCR_PHASE_PROFILE builds), else null
   unsigned long long* times;  // [P][2] global timer (ns) when a CTA takes the pair and when it is done, or null
   const int* order;     // [P] pair of each work ticket (largest pairs first), or null for ticket order
+  const PairAux* aux;   // [P] staging results (centre_kernel)
 };
 
 struct Score {

@@ -30,6 +30,11 @@ const KindOps* fundamental_ops();
 const KindOps* essential_ops();
 
 struct PairDesc;
+struct PairAux;
+
+// Staging of every pair of a batch: the centred FP32 copy into ws.pts32 and
+// the per-pair scale and non-finite flag into aux (one CTA per pair).
+cudaError_t launch_centre(const Workspace& ws, PairAux* aux, int num_pairs, cudaStream_t stream);
 
 // K^-1 normalisation of essential-matrix correspondences (utils.h:65-103 of
 // the reference): kinv holds K1^-1 then K2^-1 (row-major) per pair; one CTA
