@@ -690,6 +690,10 @@ struct Engine {
     // global PROSAC (sample size m, convergence N)
     long long g_kth = 1, g_subset = 0, g_hi = 0, g_growth = 1;
     double g_Tn = 0;
+    // one-point PROSAC of the centre points (sample size 1, convergence N):
+    // call index, subset size, growth[subset - 1] and T_n of the recurrence
+    long long op_kth = 1, op_subset = 1, op_growth = 1;
+    double op_Tn = 0;
   };
   Napsac ns;
 
@@ -741,6 +745,15 @@ struct Engine {
     double Tg = (double)N;
     for (int i = 0; i < m; ++i) Tg *= (double)(m - i) / (double)(N - i);
     ns.g_Tn = Tg;
+    // the centre sampler's growth recurrence starts from N * (1 / N), which
+    // rounds below 1 for many N: its growth function then steps by 2 once and
+    // a centre point is returned twice, so it is followed exactly
+    ns.op_kth = 1;
+    ns.op_subset = 1;
+    ns.op_growth = 1;
+    double To = (double)N;
+    To *= 1.0 / (double)N;
+    ns.op_Tn = To;
     sync();
   }
 
@@ -806,9 +819,19 @@ struct Engine {
   __device__ bool napsac_call(int* s) {
     ++ns.kth;
     if (ns.kth > ns.max_iters) return napsac_global(ns.kth, s);
-    // one-point PROSAC of sample size 1 and convergence N: the k-th call
-    // returns point k - 1 (its range is empty until convergence)
-    const int initial = (int)(ns.kth - 1);
+    // one-point PROSAC of sample size 1 and convergence N
+    // (prosac_sampler.h:65-87, 199-236; its random range is empty before
+    // convergence, which the local phase never reaches): the call returns
+    // point subset - 1, then the subset grows past growth[subset - 1]
+    const int initial = (int)(ns.op_subset - 1);
+    ++ns.op_kth;
+    if (ns.op_kth > ns.op_growth && ns.op_subset < N) {
+      ++ns.op_subset;
+      const long long i = ns.op_subset - 1;  // >= 1: past the sample size
+      const double Tn1 = (double)(i + 1) * ns.op_Tn / (double)i;
+      ns.op_growth = ns.op_growth + (long long)(unsigned int)ceil(Tn1 - ns.op_Tn);
+      ns.op_Tn = Tn1;
+    }
     int* hits = n_hits();
     const int h = ++hits[initial];
     int ss = n_subset()[initial];

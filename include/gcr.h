@@ -192,7 +192,11 @@ gcr_status gcr_find_homography_device_noalloc(const double* d_corr, int64_t n,
  * copies, so it can be recorded into a CUDA graph and replayed; each replay
  * re-runs the batch on the current contents of the device buffers given to
  * gcr_batch_prepare (new correspondences of the same sizes may be written there
- * between replays). A prepared batch stays valid until the next
+ * between replays). The prepared batch keeps the addresses of the device
+ * buffers given here: they must stay allocated for as long as a launch or a
+ * captured graph of the batch may run (a caching allocator that hands a
+ * released buffer back to the driver turns a later replay into writes to
+ * freed memory). A prepared batch stays valid until the next
  * gcr_batch_prepare or gcr_batch_run_device on the same context. */
 gcr_status gcr_batch_prepare(gcr_context* ctx, gcr_model_kind kind, int64_t num_pairs,
                              const double* d_corr, const int64_t* h_offsets, const double* h_K,
