@@ -1683,9 +1683,175 @@ struct Engine {
 
   const int* slot_list_ = nullptr;
 
+  // fit_cta_f with the per-correspondence terms in FP32 (the fast precision
+  // mode, prm.lo_fp32): each thread forms its rows' 8-point products, weights,
+  // Jacobian terms and costs in FP32 from the FP32 tile, its partial sums go
+  // to FP64 for the CTA reductions, and the normal equations are solved in
+  // FP64 (the 8-point null vector, the damped 7x7 LM steps). The
+  // normalisation is FP64 (cta_norm).
+  __device__ bool fit_cta_f_fast(const int* list, int n, int weight_mode, bool normalise) {
+    using F = FundamentalModel;
+    HomographyModel::Norm nm;
+    if (normalise) cta_norm(list, n, nm);
+    else { nm.ms0 = nm.ms1 = nm.md0 = nm.md1 = 0.0; nm.rs = nm.rd = 1.0; }
+    // the tile is centred: x_n = (x_c - (ms - c)) rs
+    const float a0 = (float)(nm.ms0 - pd.centre[0]), a1 = (float)(nm.ms1 - pd.centre[1]);
+    const float b0 = (float)(nm.md0 - pd.centre[2]), b1 = (float)(nm.md1 - pd.centre[3]);
+    const float rs = (float)nm.rs, rd = (float)nm.rd;
+    // row weights: 0 unit; 1 Tukey^2 of point k (the row index, as the
+    // reference's weights array) under sh.work_model when k is in the set; 2 slot.dres[k]
+    float wf[10];
+    if (weight_mode == 1) {
+      prepare_shared_f32(sh.work_model);
+#pragma unroll
+      for (int q = 0; q < 10; ++q) wf[q] = sh.mf32[q];
+    }
+    const float t2f = (float)t2;
+    auto weight = [&](int k) -> float {
+      if (weight_mode == 0) return 1.f;
+      if (weight_mode == 2) return (float)slot.dres[k];
+      if (k < N && slot.flag[k]) {
+        float it;
+        const float r2 = Est::r2_f32(pts32[k], wf, it);
+        const float w = fmaxf(0.f, 1.f - r2 / t2f);
+        return w * w;
+      }
+      return 0.f;
+    };
+    auto row = [&](int k, float& p0, float& p1, float& q0, float& q1) {
+      const float4 p = pts32[row_ok(list[k]) ? list[k] : 0];
+      p0 = (p.x - a0) * rs;
+      p1 = (p.y - a1) * rs;
+      q0 = (p.z - b0) * rd;
+      q1 = (p.w - b1) * rd;
+    };
+    {
+      float af[F::NATA];
+#pragma unroll
+      for (int q = 0; q < F::NATA; ++q) af[q] = 0.f;
+      for (int k = threadIdx.x; k < n; k += GCR_BLOCK) {
+        float x0, y0, x1, y1;
+        row(k, x0, y0, x1, y1);
+        const float w = weight(k);
+        const float r[9] = {w * x1 * x0, w * x1 * y0, w * x1, w * y1 * x0, w * y1 * y0, w * y1, w * x0, w * y0, w};
+        int q = 0;
+#pragma unroll
+        for (int a = 0; a < 9; ++a)
+#pragma unroll
+          for (int c = 0; c <= a; ++c) af[q++] += r[a] * r[c];
+      }
+      double acc[F::NATA];
+#pragma unroll
+      for (int q = 0; q < F::NATA; ++q) acc[q] = (double)af[q];
+      cta_reduce<F::NATA>(acc, slot.red + GCR_WARPS * 64);
+    }
+    if (threadIdx.x == 0) {
+      double F0[9];
+      F::eight_point_from_ata(slot.red + GCR_WARPS * 64, F0);
+      F::FactF ff;
+      F::factf_from(F0, ff);
+      for (int q = 0; q < 9; ++q) { sh.lm_f[q] = ff.U[q]; sh.lm_f[9 + q] = ff.V[q]; }
+      sh.lm_f[18] = ff.sigma;
+    }
+    sync();
+    const float inv_n = 1.f / (float)n;
+    // truncated Sampson cost of the factorisation f19 (thread 0 forms F)
+    auto cost_of = [&](const double* f19) {
+      if (threadIdx.x == 0) {
+        F::FactF ff;
+        for (int q = 0; q < 9; ++q) { ff.U[q] = f19[q]; ff.V[q] = f19[9 + q]; }
+        ff.sigma = f19[18];
+        F::factf_F(ff, sh.lm_G);
+      }
+      sync();
+      float G[9];
+#pragma unroll
+      for (int q = 0; q < 9; ++q) G[q] = (float)sh.lm_G[q];
+      float c = 0.f;
+      for (int k = threadIdx.x; k < n; k += GCR_BLOCK) {
+        float p0, p1, q0, q1;
+        row(k, p0, p1, q0, q1);
+        const float l = lo32::cost_point(G, p0, p1, q0, q1);
+        c += weight_mode == 0 ? l : weight(k) * l;
+      }
+      return block_sum((double)c, sh.red_d);
+    };
+    double lambda = 1e-3;
+    double cost = cost_of(sh.lm_f);
+    bool recompute = true;
+    for (int iter = 0; iter < 25; ++iter) {
+      if (recompute) {
+        if (threadIdx.x == 0) {
+          F::FactF ff;
+          for (int q = 0; q < 9; ++q) { ff.U[q] = sh.lm_f[q]; ff.V[q] = sh.lm_f[9 + q]; }
+          ff.sigma = sh.lm_f[18];
+          F::factf_F(ff, sh.lm_G);
+        }
+        sync();
+        float G[9], ds[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) G[q] = (float)sh.lm_G[q];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) ds[i * 3 + j] = (float)(sh.lm_f[i * 3 + 1] * sh.lm_f[9 + j * 3 + 1]);
+        float af[F::NLM];
+#pragma unroll
+        for (int q = 0; q < F::NLM; ++q) af[q] = 0.f;
+        for (int k = threadIdx.x; k < n; k += GCR_BLOCK) {
+          float p0, p1, q0, q1;
+          row(k, p0, p1, q0, q1);
+          lo32::accumulate_point(G, ds, p0, p1, q0, q1, weight(k) * inv_n, af);
+        }
+        double acc[F::NLM];
+#pragma unroll
+        for (int q = 0; q < F::NLM; ++q) acc[q] = (double)af[q];
+        cta_reduce<F::NLM>(acc, sh.lm_acc);
+        double gn = 0;
+        for (int a = 0; a < 7; ++a) gn += sh.lm_acc[28 + a] * sh.lm_acc[28 + a];
+        if (sqrt(gn) < 1e-8) break;
+      }
+      if (threadIdx.x == 0) {
+        F::FactF ff, fn;
+        for (int q = 0; q < 9; ++q) { ff.U[q] = sh.lm_f[q]; ff.V[q] = sh.lm_f[9 + q]; }
+        ff.sigma = sh.lm_f[18];
+        sh.lm_flag = F::lm_step(sh.lm_acc, lambda, ff, fn) ? 1 : 0;
+        for (int q = 0; q < 9; ++q) { sh.lm_fn[q] = fn.U[q]; sh.lm_fn[9 + q] = fn.V[q]; }
+        sh.lm_fn[18] = fn.sigma;
+      }
+      sync();
+      if (!sh.lm_flag) break;
+      const double cn = cost_of(sh.lm_fn);
+      if (cn < cost) {
+        sync();
+        if (threadIdx.x < 19) sh.lm_f[threadIdx.x] = sh.lm_fn[threadIdx.x];
+        sync();
+        lambda /= 10;
+        cost = cn;
+        recompute = true;
+      } else {
+        lambda *= 10;
+        recompute = false;
+      }
+    }
+    if (threadIdx.x == 0) {
+      F::FactF ff;
+      for (int q = 0; q < 9; ++q) { ff.U[q] = sh.lm_f[q]; ff.V[q] = sh.lm_f[9 + q]; }
+      ff.sigma = sh.lm_f[18];
+      double Fn[9];
+      F::factf_F(ff, Fn);
+      if (normalise) F::denormalise(nm, Fn, sh.fit_model);
+      else
+        for (int q = 0; q < 9; ++q) sh.fit_model[q] = Fn[q];
+    }
+    sync();
+    return true;
+  }
+
   __device__ bool fit_cta_f(const int* list, int n, int weight_mode, bool normalise, bool lm = true) {
     using F = FundamentalModel;
     if (n < 8) return false;  // 7 rows never reach the non-minimal solver in the loop
+    if (prm.lo_fp32 && lm) return fit_cta_f_fast(list, n, weight_mode, normalise);
     slot_list_ = list;
     HomographyModel::Norm nm;
     if (normalise) cta_norm(list, n, nm);

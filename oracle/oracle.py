@@ -16,22 +16,44 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
+# the same sources with multiply-adds contracted into FMAs (the rounding of
+# the reference built by gcc for aarch64); see `contracted`
+LIB_CONTRACT = os.path.join(HERE, "_build", "liboracle_contract.so")
 sys.path.insert(0, os.path.join(os.path.dirname(HERE), "graph-cut-ransac_gb300"))
 from pygcransac import _abi  # noqa: E402  (POD types shared with the engine)
 
-_lib = None
+_libs = {}
+_contract = False
+
+
+class contracted:
+    """Inside the block every oracle call runs the FMA-contracted build. A
+    pair whose result differs between the two builds sits on a rounding-level
+    tie (two scores equal to the last bits, a residual at the threshold): its
+    outcome is not fixed by the algorithm at FP64 precision."""
+
+    def __enter__(self):
+        global _contract
+        self._prev, _contract = _contract, True
+        return self
+
+    def __exit__(self, *exc):
+        global _contract
+        _contract = self._prev
+        return False
 
 
 def build():
     subprocess.check_call(["sh", os.path.join(HERE, "build.sh")])
 
 
-def load():
-    global _lib
-    if _lib is None:
-        if not os.path.exists(LIB):
+def load(contract=None):
+    contract = _contract if contract is None else bool(contract)
+    if contract not in _libs:
+        path = LIB_CONTRACT if contract else LIB
+        if not os.path.exists(path):
             build()
-        lib = ctypes.CDLL(LIB)
+        lib = ctypes.CDLL(path)
         P = ctypes.c_void_p
         lib.oracle_find.restype = ctypes.c_int
         lib.oracle_find.argtypes = [ctypes.c_int, P, ctypes.c_int64, P, P, P, P, ctypes.c_uint64, P, P, P]
@@ -68,8 +90,8 @@ def load():
         lib.oracle_set_sample_tape.argtypes = [P, ctypes.c_int64]
         lib.oracle_draw_u32.restype = ctypes.c_uint32
         lib.oracle_draw_u32.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32]
-        _lib = lib
-    return _lib
+        _libs[contract] = lib
+    return _libs[contract]
 
 
 def _p(a):

@@ -3,9 +3,9 @@ per batch 64 / 128 / 256, one or two CTAs per SM, caller's or largest-first
 pair order) gives bit-identical masks, statistics and models on a ragged
 calibration batch (autotune.tune raises otherwise); the fastest shape,
 recorded in a cache and installed on a context, is the one
-gcr_batch_prepare selects, and the tuned run equals the oracle."""
+gcr_batch_prepare selects, and the tuned run equals the oracle (a pair on a
+rounding-level tie equals the oracle's FMA-contracted build)."""
 import ctypes
-import os
 
 import numpy as np
 import pytest
@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.parametrize("kind,sampler", [(_abi.GCR_FUNDAMENTAL, 1), (_abi.GCR_HOMOGRAPHY, 2),
                                           (_abi.GCR_ESSENTIAL, 0)])
-def test_shapes_agree_and_tuned_run_matches_oracle(oracle, kind, sampler, tmp_path):
+def test_shapes_agree_and_tuned_run_matches_oracle(batch_parity, kind, sampler, tmp_path):
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(5)
     P = 40
@@ -68,8 +68,4 @@ def test_shapes_agree_and_tuned_run_matches_oracle(oracle, kind, sampler, tmp_pa
         lib.gcr_context_destroy(ctx)
     stats = np.frombuffer(ps.cpu().numpy().tobytes(), _abi.STATS_DTYPE)
     masks = pk.cpu().numpy().astype(bool)
-    m_o, k_o, st_o, _ = oracle.find_batch(kind, corr, off, sz, p, seeds=seeds, K=K, threads=os.cpu_count() or 1)
-    assert np.array_equal(stats["status"], st_o["status"])
-    assert np.array_equal(stats["iteration_number"], st_o["iteration_number"])
-    assert np.array_equal(stats["graph_cut_number"], st_o["graph_cut_number"])
-    assert np.array_equal(masks, k_o)
+    batch_parity(kind, corr, off, sz, p, seeds, K, stats, masks)

@@ -194,3 +194,27 @@ def test_oracle_sample_tape_replays_its_own_draws(oracle):
     p.max_iterations = 200
     rc4, _, mask4, st4 = oracle.find(0, pr["corr"], sz, p, seed=11, sample_tape=dead)
     assert rc4 == _abi.GCR_NO_MODEL and not mask4.any() and st4.iteration_number >= 200
+
+
+def test_contracted_build_moves_only_rounding_ties(oracle):
+    """The FMA-contracted oracle build agrees with the plain build on ordinary
+    pairs and differs on a pair whose local optimisation ends on a score tie
+    at the last bits (a ragged 3489-point homography pair under P-NAPSAC):
+    the plain build runs one more graph cut than the contracted one."""
+    p = _abi.Params(threshold=3.0, confidence=0.99, spatial_coherence_weight=0.975, neighborhood_size=8,
+                    max_iterations=2000, min_iterations=50, sampler=2, neighborhood=0, lo_number=20)
+    res = {}
+    for seed, n, s in ((528, 3489, 45), (11, 1200, 4)):
+        pr = S.homography_pair(seed, n=n, inlier_ratio=0.4)
+        for c in (False, True):
+            if c:
+                with oracle.contracted():
+                    res[(seed, c)] = oracle.find(0, pr["corr"], oracle.make_size(*pr["size"]), p, seed=s)
+            else:
+                res[(seed, c)] = oracle.find(0, pr["corr"], oracle.make_size(*pr["size"]), p, seed=s)
+    a, b = res[(11, False)], res[(11, True)]
+    assert a[0] == b[0] == 0 and np.array_equal(a[2], b[2]) and a[3].graph_cut_number == b[3].graph_cut_number
+    a, b = res[(528, False)], res[(528, True)]
+    assert a[0] == b[0] == 0
+    assert (a[3].graph_cut_number, b[3].graph_cut_number) == (5, 4)
+    assert a[3].iteration_number == b[3].iteration_number
