@@ -376,18 +376,20 @@ def vp(t):
     return ctypes.c_void_p(t.data_ptr())
 
 
-def tune_shape(torch, args, kind, d_corr, offsets, sizes, params, seeds, K=None, candidates=None):
+def tune_shape(torch, args, kind, d_corr, offsets, sizes, params, seeds, K=None, candidates=None, lo_precision=None):
     """Autotunes the engine's launch shape on the first pairs of the batch
     (results are identical for every shape) and records it in the tuning
     cache. Returns the gcr_tuning table for the whole batch and a summary."""
     P = len(offsets) - 1
-    n = min(P, args.tune_pairs)
+    # the calibration batch is the step's own batch unless limited: the best
+    # shape depends on how many waves of pairs the CTAs run
+    n = P if args.tune_pairs <= 0 else min(P, args.tune_pairs)
     max_n = int(np.diff(offsets).max())
     if args.no_tune:
         return [], {"shape": "defaults (256 calls per batch, CTAs per SM as the occupancy allows, caller's order)"}
     best, timings = autotune.tune(kind, d_corr, offsets[:n + 1], sizes[:n], params, seeds[:n],
                                   None if K is None else K[:n], candidates=candidates or autotune.CANDIDATES,
-                                  repeats=1)
+                                  repeats=1, lo_precision=lo_precision, staged=candidates is None)
     gpu = autotune.gpu_name()
     try:
         autotune.save_cache(autotune.record(autotune.load_cache(), gpu, kind, max_n, best, timings))
@@ -397,6 +399,8 @@ def tune_shape(torch, args, kind, d_corr, offsets, sizes, params, seeds, K=None,
                       reserved=0)
     summary = {"batch_calls": best[0], "ctas_per_sm": best[1], "order": ["caller", "largest first"][best[2]],
                "calibration_pairs": n, "candidates": len(timings),
+               "search": "staged (CTAs per SM x order at 256 calls, then calls per batch)" if candidates is None
+               else "given candidates",
                "calibration_ms": {f"{c[0]}/{c[1]}/{c[2]}": round(t, 3) for c, t in sorted(timings.items())}}
     return [row], summary
 
@@ -499,14 +503,20 @@ def run_learned(args, P, w, cfg, world, rank, local_rank, dist, torch):
     p_l.min_iterations = min(50, w["learned_iters"])
     p_l.lo_number = args.learned_lo
     cfg["learned_lo_number"] = args.learned_lo
-    b = LearnedBatch(net, kind, d_corr, offsets, sizes, p_l, seeds)
+    lo_prec = _abi.GCR_LO_FP32 if args.learned_lo_precision == "fp32" else _abi.GCR_LO_FP64
+    cfg["learned_lo_precision"] = (
+        "fp32 per-correspondence terms in every fundamental-matrix fit after the minimal solver "
+        "(LO trials, IRLS, final refit, epilogue), fp64 reductions and solves" if lo_prec == _abi.GCR_LO_FP32
+        else "fp64")
+    b = LearnedBatch(net, kind, d_corr, offsets, sizes, p_l, seeds, lo_precision=lo_prec)
     # the learned engine's shape, tuned on the ordered correspondences
     assert lib.gcr_learned_propose(vp(d_corr), vp(b.d_off), vp(b.d_sz), P, b.max_n, total, vp(net.bf16),
                                    vp(b.d_feat), vp(b.d_logits), vp(b.d_sorted), vp(b.d_perm), None) == 0
     torch.cuda.synchronize()
     p_tune = _abi.Params(**{f: getattr(p_l, f) for f, _ in p_l._fields_})
     p_tune.sampler = 1
-    rows, cfg["tuning"] = tune_shape(torch, args, kind, b.d_sorted, offsets, sizes, p_tune, seeds)
+    rows, cfg["tuning"] = tune_shape(torch, args, kind, b.d_sorted, offsets, sizes, p_tune, seeds,
+                                     lo_precision=lo_prec)
     autotune.set_table(b.ctx, rows)
     b.prepare()
     g_prop, g_eng = torch.cuda.CUDAGraph(), torch.cuda.CUDAGraph()
@@ -541,9 +551,42 @@ def run_learned(args, P, w, cfg, world, rank, local_rank, dist, torch):
     plain_value, _ = aggregate_rate(P * args.steps, plain_ms / 1e3, world, dist, "cuda")
 
     models, _, stats = b.results()
+    err_l = model_errors(args.workload, models, gts)
+    lo_compare = None
+    if not args.no_lo_compare:
+        # the same ordered pairs through the engine in the other LO precision:
+        # engine time and median model error of each
+        other = _abi.GCR_LO_FP64 if lo_prec == _abi.GCR_LO_FP32 else _abi.GCR_LO_FP32
+        bo = LearnedBatch(net, kind, d_corr, offsets, sizes, p_l, seeds, lo_precision=other)
+        autotune.set_table(bo.ctx, rows)
+        bo.prepare()
+        assert lib.gcr_learned_propose(vp(d_corr), vp(bo.d_off), vp(bo.d_sz), P, bo.max_n, total, vp(net.bf16),
+                                       vp(bo.d_feat), vp(bo.d_logits), vp(bo.d_sorted), vp(bo.d_perm), None) == 0
+        g_other = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(cap):
+            with torch.cuda.graph(g_other, stream=cap):
+                assert lib.gcr_batch_launch(bo.ctx, sp) == 0, _abi.last_error()
+                assert lib.gcr_learned_unpermute_mask(vp(bo.d_sorted_masks), vp(bo.d_perm), vp(bo.d_off),
+                                                      vp(bo.d_por), total, vp(bo.d_masks), sp) == 0
+        for _ in range(args.warmup):
+            g_other.replay()
+        torch.cuda.synchronize()
+        other_ms = sum(timed_steps(torch, [g_other.replay], args.steps, flush, stream))
+        mo, _, so = bo.results()
+        eo = model_errors(args.workload, mo, gts)
+        bo.close()
+        name = {_abi.GCR_LO_FP32: "fp32", _abi.GCR_LO_FP64: "fp64"}
+        lo_compare = {
+            name[lo_prec]: {"engine_ms_per_step": eng_ms / args.steps, "median_model_error": float(np.median(err_l)),
+                            "status_ok_fraction": float(np.mean(stats["status"] == 0))},
+            name[other]: {"engine_ms_per_step": other_ms / args.steps, "median_model_error": float(np.median(eo)),
+                          "status_ok_fraction": float(np.mean(so["status"] == 0))},
+        }
+        f64, f32 = lo_compare["fp64"], lo_compare["fp32"]
+        lo_compare["fp64_over_fp32_engine_time"] = f64["engine_ms_per_step"] / f32["engine_ms_per_step"]
+        lo_compare["equal_error"] = equal_error(f32["median_model_error"], f64["median_model_error"])
     plain_models = pm.cpu().numpy().reshape(P, 3, 3)
     plain_stats = np.frombuffer(ps.cpu().numpy().tobytes(), _abi.STATS_DTYPE)
-    err_l = model_errors(args.workload, models, gts)
     err_p = model_errors(args.workload, plain_models, gts)
 
     # end to end through the LearnedBatch API: pinned host correspondences in,
@@ -575,7 +618,7 @@ def run_learned(args, P, w, cfg, world, rank, local_rank, dist, torch):
     sweep = None
     if not args.no_sweep:
         def learned_eval(n):
-            bl = LearnedBatch(net, kind, d_corr, offsets[:n + 1], sizes[:n], p_l, seeds[:n])
+            bl = LearnedBatch(net, kind, d_corr, offsets[:n + 1], sizes[:n], p_l, seeds[:n], lo_precision=lo_prec)
             autotune.set_table(bl.ctx, rows)
             bl.prepare()
             bl.launch()
@@ -612,7 +655,9 @@ def run_learned(args, P, w, cfg, world, rank, local_rank, dist, torch):
     line = {
         "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "fp32 scoring / fp64 solvers / bf16 weights, fp32 accumulation (MLP)",
+        "vs_baseline": None, "dtype": ("fp32 scoring / fp32 per-point LO terms, fp64 solves / bf16 weights, fp32 accumulation (MLP)"
+                  if lo_prec == _abi.GCR_LO_FP32 else
+                  "fp32 scoring / fp64 solvers / bf16 weights, fp32 accumulation (MLP)"),
         "data": "synthetic", "config": cfg,
         "median_model_error": float(np.median(err_l)),
         "status_ok_fraction": float(np.mean(stats["status"] == 0)),
@@ -623,6 +668,7 @@ def run_learned(args, P, w, cfg, world, rank, local_rank, dist, torch):
         "equal_error": sweep,
         "error_unit": "px, mean Sampson distance of 100 noise-free ground-truth correspondences per pair",
         "proposal_ms_per_step": prop_ms / args.steps, "engine_ms_per_step": eng_ms / args.steps,
+        "lo_precision": lo_compare,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak if peak else None, "traffic": traffic, "traffic_source": traffic_note,
                      "peak_source": "cuBLAS SGEMM 8192^3, TF32 off, measured in this run",
@@ -1020,13 +1066,18 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--learned-lo", type=int, default=50,
                     help="LO trials of the learned form (the reference's default is 50)")
+    ap.add_argument("--learned-lo-precision", default="fp32", choices=["fp32", "fp64"],
+                    help="arithmetic of the learned form's fundamental-matrix fits after the minimal solver")
+    ap.add_argument("--no-lo-compare", action="store_true",
+                    help="skip the learned engine's run in the other LO precision")
     ap.add_argument("--no-side", action="store_true", help="skip the other workloads")
     ap.add_argument("--side-steps", type=int, default=3, help="timed steps of each other workload")
     ap.add_argument("--no-sweep", action="store_true", help="skip the plain-budget sweep of the learned workload")
     ap.add_argument("--sweep-pairs", type=int, default=304)
     ap.add_argument("--sweep-budgets", default=",".join(str(b) for b in SWEEP_BUDGETS))
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape (no autotuning)")
-    ap.add_argument("--tune-pairs", type=int, default=304, help="calibration pairs of the autotuner")
+    ap.add_argument("--tune-pairs", type=int, default=0,
+                    help="calibration pairs of the autotuner (0: the whole batch of the step)")
     args = ap.parse_args()
     args.sweep_budgets = [int(float(x)) for x in args.sweep_budgets.split(",") if x]
 
@@ -1073,11 +1124,11 @@ def main():
                 continue
             sw = WORKLOADS[name]
             if name == "serving":
-                sub = run_serving(args, sw["pairs"], args.side_steps, 1, world, rank, local_rank, dist, torch,
-                                  clocks_on=False)
+                sub = run_serving(args, sw["pairs"], args.side_steps, max(3, args.warmup), world, rank, local_rank,
+                                  dist, torch, clocks_on=False)
             else:
-                sub = run_kind(args, name, sw["pairs"], args.side_steps, 1, world, rank, local_rank, dist, torch,
-                               clocks_on=False)
+                sub = run_kind(args, name, sw["pairs"], args.side_steps, max(3, args.warmup), world, rank, local_rank,
+                               dist, torch, clocks_on=False)
             if sub is not None:
                 sub["config"] = {**describe(name, sw["pairs"], world), **sub.get("config", {})}
                 side[name] = sub

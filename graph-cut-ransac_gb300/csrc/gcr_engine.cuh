@@ -1572,6 +1572,7 @@ struct Engine {
       if (f) list[total + pos] = i;
       total += tot;
     }
+    sync();  // callers read entries other threads wrote after the last scan
     return total;
   }
 
@@ -1683,17 +1684,19 @@ struct Engine {
 
   const int* slot_list_ = nullptr;
 
-  // fit_cta_f with the per-correspondence terms in FP32 (the fast precision
-  // mode, prm.lo_fp32): each thread forms its rows' 8-point products, weights,
-  // Jacobian terms and costs in FP32 from the FP32 tile, its partial sums go
-  // to FP64 for the CTA reductions, and the normal equations are solved in
-  // FP64 (the 8-point null vector, the damped 7x7 LM steps). The
-  // normalisation is FP64 (cta_norm).
-  __device__ bool fit_cta_f_fast(const int* list, int n, int weight_mode, bool normalise) {
+  // fit_cta_f on normalised coordinates in FP32 (the fast precision mode,
+  // prm.lo_fp32): each thread forms its rows' 8-point products, weights,
+  // Jacobian terms and costs in FP32 from the FP32 tile; the partial sums are
+  // reduced across the CTA in FP64; thread 0 runs the small solves in FP32
+  // like the local-optimisation trials (the 8-point null vector by pivoted QR,
+  // the 3x3 SVD of the factorisation, the damped 7x7 Cholesky steps). The
+  // normalisation and the denormalised model are FP64. Fits on raw pixel
+  // coordinates (the epilogue's bundle adjustment) stay in FP64: products of
+  // pixel coordinates span ten decades, beyond FP32.
+  __device__ bool fit_cta_f_fast(const int* list, int n, int weight_mode) {
     using F = FundamentalModel;
     HomographyModel::Norm nm;
-    if (normalise) cta_norm(list, n, nm);
-    else { nm.ms0 = nm.ms1 = nm.md0 = nm.md1 = 0.0; nm.rs = nm.rd = 1.0; }
+    cta_norm(list, n, nm);
     // the tile is centred: x_n = (x_c - (ms - c)) rs
     const float a0 = (float)(nm.ms0 - pd.centre[0]), a1 = (float)(nm.ms1 - pd.centre[1]);
     const float b0 = (float)(nm.md0 - pd.centre[2]), b1 = (float)(nm.md1 - pd.centre[3]);
@@ -1745,23 +1748,49 @@ struct Engine {
       for (int q = 0; q < F::NATA; ++q) acc[q] = (double)af[q];
       cta_reduce<F::NATA>(acc, slot.red + GCR_WARPS * 64);
     }
+    // the factorisation lives in sh.lm_f / sh.lm_fn as FP32 values
+    auto load_fact = [&](const double* f19, lo32::FactF& f) {
+#pragma unroll
+      for (int q = 0; q < 9; ++q) {
+        f.U[q] = (float)f19[q];
+        f.V[q] = (float)f19[9 + q];
+      }
+      f.sigma = (float)f19[18];
+    };
+    auto store_fact = [&](const lo32::FactF& f, double* f19) {
+#pragma unroll
+      for (int q = 0; q < 9; ++q) {
+        f19[q] = f.U[q];
+        f19[9 + q] = f.V[q];
+      }
+      f19[18] = f.sigma;
+    };
     if (threadIdx.x == 0) {
-      double F0[9];
-      F::eight_point_from_ata(slot.red + GCR_WARPS * 64, F0);
-      F::FactF ff;
-      F::factf_from(F0, ff);
-      for (int q = 0; q < 9; ++q) { sh.lm_f[q] = ff.U[q]; sh.lm_f[9 + q] = ff.V[q]; }
-      sh.lm_f[18] = ff.sigma;
+      const double* ata = slot.red + GCR_WARPS * 64;
+      float M[81], F0[9], sv[3];
+      int k = 0;
+      for (int r = 0; r < 9; ++r)
+        for (int c = 0; c <= r; ++c) {
+          const float v = (float)ata[k++];
+          M[r * 9 + c] = v;
+          M[c * 9 + r] = v;
+        }
+      lo32::qr9_null(M, F0);
+      lo32::FactF ff;
+      lo32::svd3(F0, ff.U, sv, ff.V);
+      ff.sigma = sv[0] > 0.f ? sv[1] / sv[0] : 0.f;
+      store_fact(ff, sh.lm_f);
     }
     sync();
     const float inv_n = 1.f / (float)n;
     // truncated Sampson cost of the factorisation f19 (thread 0 forms F)
     auto cost_of = [&](const double* f19) {
       if (threadIdx.x == 0) {
-        F::FactF ff;
-        for (int q = 0; q < 9; ++q) { ff.U[q] = f19[q]; ff.V[q] = f19[9 + q]; }
-        ff.sigma = f19[18];
-        F::factf_F(ff, sh.lm_G);
+        lo32::FactF ff;
+        float Gf[9];
+        load_fact(f19, ff);
+        lo32::fact_to_F(ff, Gf);
+        for (int q = 0; q < 9; ++q) sh.lm_G[q] = Gf[q];
       }
       sync();
       float G[9];
@@ -1782,10 +1811,11 @@ struct Engine {
     for (int iter = 0; iter < 25; ++iter) {
       if (recompute) {
         if (threadIdx.x == 0) {
-          F::FactF ff;
-          for (int q = 0; q < 9; ++q) { ff.U[q] = sh.lm_f[q]; ff.V[q] = sh.lm_f[9 + q]; }
-          ff.sigma = sh.lm_f[18];
-          F::factf_F(ff, sh.lm_G);
+          lo32::FactF ff;
+          float Gf[9];
+          load_fact(sh.lm_f, ff);
+          lo32::fact_to_F(ff, Gf);
+          for (int q = 0; q < 9; ++q) sh.lm_G[q] = Gf[q];
         }
         sync();
         float G[9], ds[9];
@@ -1807,17 +1837,18 @@ struct Engine {
 #pragma unroll
         for (int q = 0; q < F::NLM; ++q) acc[q] = (double)af[q];
         cta_reduce<F::NLM>(acc, sh.lm_acc);
-        double gn = 0;
-        for (int a = 0; a < 7; ++a) gn += sh.lm_acc[28 + a] * sh.lm_acc[28 + a];
-        if (sqrt(gn) < 1e-8) break;
+        float gn = 0.f;
+        for (int a = 0; a < 7; ++a) gn += (float)sh.lm_acc[28 + a] * (float)sh.lm_acc[28 + a];
+        if (!(sqrtf(gn) >= 1e-7f)) break;  // the FP32 tolerance of the trials' fits
       }
       if (threadIdx.x == 0) {
-        F::FactF ff, fn;
-        for (int q = 0; q < 9; ++q) { ff.U[q] = sh.lm_f[q]; ff.V[q] = sh.lm_f[9 + q]; }
-        ff.sigma = sh.lm_f[18];
-        sh.lm_flag = F::lm_step(sh.lm_acc, lambda, ff, fn) ? 1 : 0;
-        for (int q = 0; q < 9; ++q) { sh.lm_fn[q] = fn.U[q]; sh.lm_fn[9 + q] = fn.V[q]; }
-        sh.lm_fn[18] = fn.sigma;
+        lo32::FactF ff, fn;
+        float a35[F::NLM];
+        for (int q = 0; q < F::NLM; ++q) a35[q] = (float)sh.lm_acc[q];
+        load_fact(sh.lm_f, ff);
+        const bool ok = lo32::step(a35, (float)lambda, ff, fn);
+        sh.lm_flag = ok ? 1 : 0;
+        store_fact(ok ? fn : ff, sh.lm_fn);
       }
       sync();
       if (!sh.lm_flag) break;
@@ -1835,14 +1866,13 @@ struct Engine {
       }
     }
     if (threadIdx.x == 0) {
-      F::FactF ff;
-      for (int q = 0; q < 9; ++q) { ff.U[q] = sh.lm_f[q]; ff.V[q] = sh.lm_f[9 + q]; }
-      ff.sigma = sh.lm_f[18];
+      lo32::FactF ff;
+      float Ff[9];
+      load_fact(sh.lm_f, ff);
+      lo32::fact_to_F(ff, Ff);
       double Fn[9];
-      F::factf_F(ff, Fn);
-      if (normalise) F::denormalise(nm, Fn, sh.fit_model);
-      else
-        for (int q = 0; q < 9; ++q) sh.fit_model[q] = Fn[q];
+      for (int q = 0; q < 9; ++q) Fn[q] = Ff[q];
+      F::denormalise(nm, Fn, sh.fit_model);
     }
     sync();
     return true;
@@ -1851,7 +1881,7 @@ struct Engine {
   __device__ bool fit_cta_f(const int* list, int n, int weight_mode, bool normalise, bool lm = true) {
     using F = FundamentalModel;
     if (n < 8) return false;  // 7 rows never reach the non-minimal solver in the loop
-    if (prm.lo_fp32 && lm) return fit_cta_f_fast(list, n, weight_mode, normalise);
+    if (prm.lo_fp32 && lm && normalise) return fit_cta_f_fast(list, n, weight_mode);
     slot_list_ = list;
     HomographyModel::Norm nm;
     if (normalise) cta_norm(list, n, nm);
@@ -2368,6 +2398,7 @@ struct Engine {
       if (f) slot.list2[total + pos] = list[k];
       total += tot;
     }
+    sync();  // the fit reads entries other threads wrote after the last scan
     if (total < HomographyModel::NONMIN) return false;
     // plane homography from its inliers, then the plane-and-parallax GC-RANSAC
     if (!fit_cta_h(slot.list2, total, 0)) return false;

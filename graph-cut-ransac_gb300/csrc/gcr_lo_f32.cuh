@@ -10,10 +10,12 @@
 // at about 1/64 of its FP32 rate, and the graph-cut local optimisation (50
 // such fits per labelling) is where the learned form spends most of its FP64
 // work. A fit's model is only a candidate: it is scored exactly (FP64 inlier
-// decisions) like every other model, and the run's final iteratively
-// reweighted fits and the drivers' bundle adjustment stay in FP64. Masks can
-// differ from the FP64 fits' in the last bits of a candidate, so parity runs
-// keep the FP64 fits (the engine's default).
+// decisions) like every other model. The same solver pieces (pivoted-QR null
+// vector, 3x3 SVD, damped Cholesky step) serve the CTA-wide iteratively
+// reweighted fits and final refit of the fast mode; the drivers' bundle
+// adjustment on raw pixel coordinates stays in FP64. Masks can differ from
+// the FP64 fits' in the last bits of a candidate, so parity runs keep the FP64
+// fits (the engine's default).
 #pragma once
 
 #include "gcr_fundamental.cuh"

@@ -125,11 +125,30 @@ def gpu_name():
     return torch.cuda.get_device_name()
 
 
-def tune(kind, d_corr, offsets, sizes, params, seeds=None, K=None, candidates=CANDIDATES, repeats=2):
+def stage_one():
+    """First stage of the staged search: every (CTAs per SM, order) at the
+    largest batch."""
+    return tuple((max(BATCH_CALLS), c, o) for c in CTAS_PER_SM for o in ORDERS)
+
+
+def stage_two(timings):
+    """Second stage: the other batch sizes at the fastest (CTAs per SM, order)
+    of the first stage (`timings`: {shape: ms})."""
+    _, c, o = min(timings, key=timings.get)
+    return tuple((b, c, o) for b in BATCH_CALLS if (b, c, o) not in timings)
+
+
+def tune(kind, d_corr, offsets, sizes, params, seeds=None, K=None, candidates=CANDIDATES, repeats=2,
+         lo_precision=None, staged=False):
     """Times each candidate shape on the device-resident calibration batch
     (d_corr a torch CUDA tensor of [total, 4] doubles; offsets, sizes, seeds,
-    K host arrays as for gcr_batch_run_device). Returns (fastest shape,
-    {shape: best milliseconds}). Raises if two shapes disagree on any result."""
+    K host arrays as for gcr_batch_run_device; lo_precision, when given, is
+    set on the calibration context). With `staged` the search times
+    stage_one() and then stage_two() of its timings (6 shapes instead of 12):
+    the order and CTAs per SM set how the pairs spread over the SMs, the batch
+    size mostly how many hypotheses are drawn past termination, so the two
+    are searched one after the other. Returns (fastest shape, {shape: best
+    milliseconds}). Raises if two shapes disagree on any result."""
     import torch
     lib = _abi.load()
     offsets = np.ascontiguousarray(offsets, np.int64)
@@ -149,8 +168,18 @@ def tune(kind, d_corr, offsets, sizes, params, seeds=None, K=None, candidates=CA
     ctx = ctypes.c_void_p()
     assert lib.gcr_context_create(ctypes.byref(ctx)) == _abi.GCR_OK, _abi.last_error()
     timings, ref = {}, None
+
+    def stages():
+        if not staged:
+            yield from candidates
+            return
+        yield from stage_one()
+        yield from stage_two(timings)
+
     try:
-        for shape in candidates:
+        if lo_precision is not None and lib.gcr_context_set_lo_precision(ctx, int(lo_precision)) != _abi.GCR_OK:
+            raise RuntimeError(f"gcr_context_set_lo_precision: {_abi.last_error()}")
+        for shape in stages():
             set_table(ctx, [_abi.Tuning(kind=int(kind), max_n=max_n, batch_calls=shape[0], ctas_per_sm=shape[1],
                                         order=shape[2], reserved=0)])
             best = float("inf")

@@ -60,3 +60,13 @@ def test_library_refuses_bad_tables():
     t = _abi.Tuning()
     assert lib.gcr_context_last_tuning(None, ctypes.byref(t)) == _abi.GCR_INVALID_ARG
     assert ctypes.sizeof(_abi.Tuning) == 24
+
+
+def test_staged_search_plan():
+    s1 = A.stage_one()
+    assert len(s1) == 4 and all(b == max(A.BATCH_CALLS) for b, _, _ in s1)
+    assert {(c, o) for _, c, o in s1} == {(c, o) for c in A.CTAS_PER_SM for o in A.ORDERS}
+    timings = {(256, 1, 0): 9.0, (256, 1, 1): 7.0, (256, 2, 0): 8.0, (256, 2, 1): 7.5}
+    s2 = A.stage_two(timings)
+    assert s2 == ((64, 1, 1), (128, 1, 1))
+    assert set(s1) | set(s2) <= set(A.CANDIDATES)

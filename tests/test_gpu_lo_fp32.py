@@ -1,12 +1,14 @@
-"""The FP32 local optimisation (gcr_context_set_lo_precision(GCR_LO_FP32)):
-the fundamental-matrix fits of the graph-cut local optimisation in FP32.
+"""The FP32 fits (gcr_context_set_lo_precision(GCR_LO_FP32)): the
+fundamental-matrix fits on normalised coordinates after the minimal solver
+(local-optimisation trials, iteratively reweighted fits, final refit) in FP32.
 It is a throughput mode, judged on model error rather than mask parity:
 
 * on hard pairs (4000 correspondences, 5-10 % inliers, the learned proposal's
   workload) the learned form's median model error with FP32 fits is within 5 %
   (or 0.05 px) of the FP64 fits' and every pair still ends with a model;
-* on easier pairs run by the plain form, the models agree with the FP64 run's
-  within the threshold-scale error and the inlier counts within 2 %;
+* on easier pairs run by the plain form, the median model error matches the
+  FP64 run's and no pair loses more than 2 % of the FP64 run's inliers (the
+  FP32 iteratively reweighted fits may converge to a larger consensus);
 * GCR_LO_FP64 stays the default and keeps the oracle's results.
 """
 import ctypes
@@ -92,5 +94,5 @@ def test_fp32_lo_models_agree_on_plain_runs(gcr):
     e64 = np.array([S.fundamental_error(m, q, n=200) for m, q in zip(m64, pairs)])
     e32 = np.array([S.fundamental_error(m, q, n=200) for m, q in zip(m32, pairs)])
     assert np.median(e32) <= np.median(e64) * 1.05 + 0.02, (np.median(e32), np.median(e64))
-    assert np.all(np.abs(s32["inlier_number"] - s64["inlier_number"]) <= np.maximum(2, 0.02 * s64["inlier_number"]))
+    assert np.all(s32["inlier_number"] >= s64["inlier_number"] - np.maximum(2, 0.02 * s64["inlier_number"]))
     assert lib.gcr_context_set_lo_precision(None, 1) == _abi.GCR_INVALID_ARG
