@@ -267,6 +267,7 @@ struct Shared {
   int ar_size;                    // entries in the AR sampler's heap
   int ar_overflow;
   int big_cells;                  // grid cells of the current labelling above kMaxFlowCap points
+  int out_tmax[33];               // source-set size of a cell of n <= 32 points all beyond the threshold
 };
 
 // GCRANSAC::getIterationNumber (GCRANSAC.h:156-172)
@@ -1321,6 +1322,141 @@ struct Engine {
   }
 
   // ------------------------------------------------------------------
+  // Minimum cut of one grid cell of 2..32 points by the closed form of
+  // clique_cut_cta (below, where the energy is derived), one warp and one
+  // point per lane, everything in registers: the inliers' keys sorted by a
+  // warp bitonic network, the prefix sums of d by a warp scan, the energy of
+  // every source-set size t on lane t. The arithmetic follows clique_cut_cta
+  // step for step, so both give the same cut. Writes slot.flag for the
+  // cell's points.
+  // The largest minimising source-set size of a clique of n points that all
+  // lie beyond the threshold (d = 1, a = -(1 - lambda)): the energies of
+  // clique_cut_warp with no inliers, E(t) = t c' + lambda t (n - t) with
+  // c' = lambda (t - 1) / 2 - (1 - lambda). One thread per n.
+  __device__ int outlier_clique_tmax(int n) const {
+    if (n < 2) return 0;
+    const double lam = prm.lambda;
+    const double oml = 1.0 - lam;
+    double e[33];
+    double fmin = 0.0;
+    for (int t = 0; t <= n; ++t) {
+      const double c = 0.5 * lam * (double)(t - 1);
+      const double ko = c - oml;
+      const double S = 0.0 + (double)t * ko;
+      e[t] = t == 0 ? 0.0 : S + lam * (double)t * (double)(n - t);
+      fmin = e[t] < fmin ? e[t] : fmin;
+    }
+    const double tol = 1e-12 * (1.0 + oml * n + 0.5 * lam * (double)(n - 1) * 0.0 + 0.25 * lam * (double)n * n);
+    int tmax = 0;
+    for (int t = 0; t <= n; ++t)
+      if (e[t] <= fmin + tol) tmax = t;
+    return tmax;
+  }
+
+  __device__ void clique_cut_warp(int c0, int n) {
+    constexpr unsigned kAll = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const double lam = prm.lambda;
+    const double oml = 1.0 - lam;
+    const int* gp = slot.cell_pts + c0;
+    const bool live = lane < n;
+    const int p = live ? gp[lane] : 0;
+    const double trv = live ? slot.tr[p] : 1.0;
+    const double dv = live ? slot.dres[p] : 0.0;
+    const bool inl = live && !(trv > 0);
+    const unsigned b_in = __ballot_sync(kAll, inl);
+    const unsigned b_out = __ballot_sync(kAll, live && trv > 0);
+    const int m = __popc(b_in);
+    const int n_out = n - m;
+    if (m == 0) {
+      // every point beyond the threshold: one shared key, the cut depends on n
+      // only (sh.out_tmax, the same energies with no inliers)
+      if (live) slot.flag[p] = lane < sh.out_tmax[n] ? 0 : 1;
+      return;
+    }
+    const int ib = 32 - __clz(n);
+    const unsigned long long low = (1ull << ib) - 1ull;
+    unsigned long long key =
+        inl ? ((((unsigned long long)__double_as_longlong(dv)) << 2) & ~low) | (unsigned long long)lane : ~0ull;
+#pragma unroll
+    for (int k = 2; k <= 32; k <<= 1)
+#pragma unroll
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        const unsigned long long o = __shfl_xor_sync(kAll, key, j);
+        const bool keep_min = ((lane & k) == 0) == ((lane & j) == 0);
+        key = keep_min ? (o < key ? o : key) : (o > key ? o : key);
+      }
+    // lane r: the inlier of rank r (ascending d), its d and the exclusive
+    // prefix sum of d over the ranks
+    const int owner = (int)(key & low) & 31;
+    const double dsh = __shfl_sync(kAll, dv, owner);
+    const double v = lane < m ? dsh : 0.0;
+    double x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double y = __shfl_up_sync(kAll, x, o);
+      if (lane >= o) x += y;
+    }
+    const double Dex = 0.0 + (x - v);
+    const double Dm = __shfl_sync(kAll, x, 31);
+    auto pref = [&](int j) {  // every lane calls it (shuffle)
+      const double s = __shfl_sync(kAll, Dex, j & 31);
+      return j >= m ? Dm : s;
+    };
+    auto inl_sum = [&](int j, double sl) {
+      const double a = pref(j), b = pref(m - j);
+      return sl >= 0 ? oml * j + sl * a : oml * j + sl * (Dm - b);
+    };
+    auto count_le = [&](double sl, double ko) {  // inliers with key <= ko
+      int lo = 0, hi = m;
+#pragma unroll
+      for (int it = 0; it < 6; ++it) {
+        const int mid = (lo + hi) >> 1;
+        const double d = __shfl_sync(kAll, v, (sl >= 0 ? mid : m - 1 - mid) & 31);
+        if (lo < hi) {
+          if (oml + sl * d <= ko) lo = mid + 1;
+          else hi = mid;
+        }
+      }
+      return lo;
+    };
+    auto energy = [&](int t) -> double {  // every lane calls it; t may exceed n (ignored)
+      const double c = 0.5 * lam * (double)(t - 1);
+      const double sl = c - oml, ko = c - oml;
+      const int J = count_le(sl, ko);
+      const double s1 = inl_sum(t, sl);
+      const double s2 = inl_sum(J, sl) + (double)(t - J) * ko;
+      const double s3 = inl_sum(t - n_out, sl) + (double)n_out * ko;
+      const double S = t <= J ? s1 : (t <= J + n_out ? s2 : s3);
+      return t == 0 ? 0.0 : S + lam * (double)t * (double)(n - t);
+    };
+    const double e0 = energy(lane);
+    const double e1 = n == 32 ? energy(32) : 0.0;  // t = 32, a full cell
+    double fmin = 0.0;
+    if (lane <= n) fmin = e0 < fmin ? e0 : fmin;
+    if (n == 32) fmin = e1 < fmin ? e1 : fmin;
+    fmin = warp_min(fmin);
+    const double tol = 1e-12 * (1.0 + oml * n + 0.5 * lam * (double)(n - 1) * Dm + 0.25 * lam * (double)n * n);
+    int tmax = 0;
+    if (lane <= n && e0 <= fmin + tol) tmax = lane;
+    if (n == 32 && e1 <= fmin + tol) tmax = 32;
+    tmax = -warp_min(-tmax);
+    const double c = 0.5 * lam * (double)(tmax - 1);
+    const double sl = c - oml;
+    const int J = count_le(sl, sl);
+    const int in_T = tmax == 0 ? 0 : (tmax <= J ? tmax : (tmax <= J + n_out ? J : tmax - n_out));
+    const int out_T = tmax - in_T;
+    if (lane < m) {
+      const int r = sl >= 0 ? lane : m - 1 - lane;
+      slot.flag[gp[owner]] = r < in_T ? 0 : 1;
+    }
+    if (live && trv > 0) {
+      const int pos = __popc(b_out & ((1u << lane) - 1u));
+      slot.flag[p] = pos < out_T ? 0 : 1;
+    }
+  }
+
+  // ------------------------------------------------------------------
   // Minimum cut of one grid cell of n > kMaxFlowCap points by its closed form
   // (the whole CTA; `scratch` holds n ints and is free during the cut).
   //
@@ -1524,6 +1660,7 @@ struct Engine {
       sync();
     }
     if (threadIdx.x == 0) sh.big_cells = 0;
+    if (pairwise && prm.neighborhood == 0 && threadIdx.x <= 32) sh.out_tmax[threadIdx.x] = outlier_clique_tmax(threadIdx.x);
     sync();
     for (int c = warp; pairwise && prm.neighborhood == 0 && c < ncells; c += GCR_WARPS) {
       const int c0 = slot.cell_start[c], n = slot.cell_start[c + 1] - c0;
@@ -1532,7 +1669,9 @@ struct Engine {
         continue;
       }
       if (n == 1) continue;  // unary label, set above
-      if (n > kMaxFlowCap) {
+      if (n <= 32) {
+        clique_cut_warp(c0, n);
+      } else if (n > kMaxFlowCap) {
         if (lane == 0) atomicAdd(&sh.big_cells, 1);  // cut below by the whole CTA
       } else if (!mincut_cell(c0, n, warp)) {
         if (lane == 0) atomicMax(&sh.flow_status, ST_TIMEOUT);
