@@ -1823,19 +1823,32 @@ struct Engine {
 
   const int* slot_list_ = nullptr;
 
-  // fit_cta_f on normalised coordinates in FP32 (the fast precision mode,
-  // prm.lo_fp32): each thread forms its rows' 8-point products, weights,
-  // Jacobian terms and costs in FP32 from the FP32 tile; the partial sums are
-  // reduced across the CTA in FP64; thread 0 runs the small solves in FP32
-  // like the local-optimisation trials (the 8-point null vector by pivoted QR,
-  // the 3x3 SVD of the factorisation, the damped 7x7 Cholesky steps). The
-  // normalisation and the denormalised model are FP64. Fits on raw pixel
-  // coordinates (the epilogue's bundle adjustment) stay in FP64: products of
-  // pixel coordinates span ten decades, beyond FP32.
-  __device__ bool fit_cta_f_fast(const int* list, int n, int weight_mode) {
+  // fit_cta_f in FP32 (the fast precision mode, prm.lo_fp32): each thread
+  // forms its rows' 8-point products, weights, Jacobian terms and costs in
+  // FP32 from the FP32 tile; the partial sums are reduced across the CTA in
+  // FP64; thread 0 runs the small solves in FP32 like the local-optimisation
+  // trials (the 8-point null vector by pivoted QR, the 3x3 SVD of the
+  // factorisation, the damped 7x7 Cholesky steps). Normalised fits use the
+  // estimator's normalisation (FP64, cta_norm). A fit on raw pixel
+  // coordinates (`raw`, the drivers' bundle adjustment) runs on the pair's
+  // centred coordinates scaled by s = 1 / (largest centred coordinate): the
+  // Sampson distance scales by s under a common similarity of both images,
+  // so the loss truncated at 1 px^2 is truncated at s^2 there and the
+  // minimiser is the same; FP32 products of raw pixel coordinates would span
+  // ten decades. The model is mapped back in FP64.
+  __device__ bool fit_cta_f_fast(const int* list, int n, int weight_mode, bool raw, const double* init) {
     using F = FundamentalModel;
     HomographyModel::Norm nm;
-    cta_norm(list, n, nm);
+    float trunc2 = 1.f;
+    if (raw) {
+      const double s = scale > 0.0 ? 1.0 / scale : 1.0;
+      nm.ms0 = pd.centre[0]; nm.ms1 = pd.centre[1];
+      nm.md0 = pd.centre[2]; nm.md1 = pd.centre[3];
+      nm.rs = nm.rd = s;
+      trunc2 = (float)(s * s);
+    } else {
+      cta_norm(list, n, nm);
+    }
     // the tile is centred: x_n = (x_c - (ms - c)) rs
     const float a0 = (float)(nm.ms0 - pd.centre[0]), a1 = (float)(nm.ms1 - pd.centre[1]);
     const float b0 = (float)(nm.md0 - pd.centre[2]), b1 = (float)(nm.md1 - pd.centre[3]);
@@ -1867,7 +1880,44 @@ struct Engine {
       q0 = (p.z - b0) * rd;
       q1 = (p.w - b1) * rd;
     };
-    {
+    // the factorisation lives in sh.lm_f / sh.lm_fn as FP32 values
+    auto load_fact = [&](const double* f19, lo32::FactF& f) {
+#pragma unroll
+      for (int q = 0; q < 9; ++q) {
+        f.U[q] = (float)f19[q];
+        f.V[q] = (float)f19[9 + q];
+      }
+      f.sigma = (float)f19[18];
+    };
+    auto store_fact = [&](const lo32::FactF& f, double* f19) {
+#pragma unroll
+      for (int q = 0; q < 9; ++q) {
+        f19[q] = f.U[q];
+        f19[9 + q] = f.V[q];
+      }
+      f19[18] = f.sigma;
+    };
+    if (init != nullptr) {
+      // warm start: the given model in this fit's normalised coordinates,
+      // Fn = Td^-T F Ts^-1, unit norm, factorised
+      if (threadIdx.x == 0) {
+        const double A[9] = {1.0 / nm.rd, 0, 0, 0, 1.0 / nm.rd, 0, nm.md0, nm.md1, 1};
+        const double B[9] = {1.0 / nm.rs, 0, nm.ms0, 0, 1.0 / nm.rs, nm.ms1, 0, 0, 1};
+        double t[9], G[9];
+        matmul3(A, init, t);
+        matmul3(t, B, G);
+        double nrm = 0;
+        for (int q = 0; q < 9; ++q) nrm += G[q] * G[q];
+        nrm = sqrt(nrm);
+        float F0[9], sv[3];
+        for (int q = 0; q < 9; ++q) F0[q] = (float)(G[q] / nrm);
+        lo32::FactF ff;
+        lo32::svd3(F0, ff.U, sv, ff.V);
+        ff.sigma = sv[0] > 0.f ? sv[1] / sv[0] : 0.f;
+        store_fact(ff, sh.lm_f);
+      }
+    } else {
+      // the 8-point start: null vector of the CTA-reduced A^T A
       float af[F::NATA];
 #pragma unroll
       for (int q = 0; q < F::NATA; ++q) af[q] = 0.f;
@@ -1886,39 +1936,22 @@ struct Engine {
 #pragma unroll
       for (int q = 0; q < F::NATA; ++q) acc[q] = (double)af[q];
       cta_reduce<F::NATA>(acc, slot.red + GCR_WARPS * 64);
-    }
-    // the factorisation lives in sh.lm_f / sh.lm_fn as FP32 values
-    auto load_fact = [&](const double* f19, lo32::FactF& f) {
-#pragma unroll
-      for (int q = 0; q < 9; ++q) {
-        f.U[q] = (float)f19[q];
-        f.V[q] = (float)f19[9 + q];
+      if (threadIdx.x == 0) {
+        const double* ata = slot.red + GCR_WARPS * 64;
+        float M[81], F0[9], sv[3];
+        int k = 0;
+        for (int r = 0; r < 9; ++r)
+          for (int c = 0; c <= r; ++c) {
+            const float v = (float)ata[k++];
+            M[r * 9 + c] = v;
+            M[c * 9 + r] = v;
+          }
+        lo32::qr9_null(M, F0);
+        lo32::FactF ff;
+        lo32::svd3(F0, ff.U, sv, ff.V);
+        ff.sigma = sv[0] > 0.f ? sv[1] / sv[0] : 0.f;
+        store_fact(ff, sh.lm_f);
       }
-      f.sigma = (float)f19[18];
-    };
-    auto store_fact = [&](const lo32::FactF& f, double* f19) {
-#pragma unroll
-      for (int q = 0; q < 9; ++q) {
-        f19[q] = f.U[q];
-        f19[9 + q] = f.V[q];
-      }
-      f19[18] = f.sigma;
-    };
-    if (threadIdx.x == 0) {
-      const double* ata = slot.red + GCR_WARPS * 64;
-      float M[81], F0[9], sv[3];
-      int k = 0;
-      for (int r = 0; r < 9; ++r)
-        for (int c = 0; c <= r; ++c) {
-          const float v = (float)ata[k++];
-          M[r * 9 + c] = v;
-          M[c * 9 + r] = v;
-        }
-      lo32::qr9_null(M, F0);
-      lo32::FactF ff;
-      lo32::svd3(F0, ff.U, sv, ff.V);
-      ff.sigma = sv[0] > 0.f ? sv[1] / sv[0] : 0.f;
-      store_fact(ff, sh.lm_f);
     }
     sync();
     const float inv_n = 1.f / (float)n;
@@ -1939,7 +1972,7 @@ struct Engine {
       for (int k = threadIdx.x; k < n; k += GCR_BLOCK) {
         float p0, p1, q0, q1;
         row(k, p0, p1, q0, q1);
-        const float l = lo32::cost_point(G, p0, p1, q0, q1);
+        const float l = lo32::cost_point(G, p0, p1, q0, q1, trunc2);
         c += weight_mode == 0 ? l : weight(k) * l;
       }
       return block_sum((double)c, sh.red_d);
@@ -1970,7 +2003,7 @@ struct Engine {
         for (int k = threadIdx.x; k < n; k += GCR_BLOCK) {
           float p0, p1, q0, q1;
           row(k, p0, p1, q0, q1);
-          lo32::accumulate_point(G, ds, p0, p1, q0, q1, weight(k) * inv_n, af);
+          lo32::accumulate_point(G, ds, p0, p1, q0, q1, weight(k) * inv_n, af, trunc2);
         }
         double acc[F::NLM];
 #pragma unroll
@@ -2017,10 +2050,13 @@ struct Engine {
     return true;
   }
 
-  __device__ bool fit_cta_f(const int* list, int n, int weight_mode, bool normalise, bool lm = true) {
+  // `init`: the warm start of the FP32 mode's fits (ignored by the FP64 fits,
+  // which start from the 8-point solution like the reference's solver)
+  __device__ bool fit_cta_f(const int* list, int n, int weight_mode, bool normalise, bool lm = true,
+                            const double* init = nullptr) {
     using F = FundamentalModel;
     if (n < 8) return false;  // 7 rows never reach the non-minimal solver in the loop
-    if (prm.lo_fp32 && lm && normalise) return fit_cta_f_fast(list, n, weight_mode);
+    if (prm.lo_fp32 && lm) return fit_cta_f_fast(list, n, weight_mode, !normalise, init);
     slot_list_ = list;
     HomographyModel::Norm nm;
     if (normalise) cta_norm(list, n, nm);
@@ -2128,9 +2164,9 @@ struct Engine {
     return true;
   }
 
-  __device__ bool fit_cta(const int* list, int n, int weight_mode) {
+  __device__ bool fit_cta(const int* list, int n, int weight_mode, const double* init = nullptr) {
     if constexpr (Est::LO_MAXSOL > 1) return false;  // multi-model estimators use fit_cta_multi
-    if constexpr (Est::KIND == 1) return fit_cta_f(list, n, weight_mode, true);
+    if constexpr (Est::KIND == 1) return fit_cta_f(list, n, weight_mode, true, true, init);
     if constexpr (Est::KIND == 2) return fit_cta_f(list, n, weight_mode, true, false);
     return fit_cta_h(list, n, weight_mode);
   }
@@ -3025,7 +3061,8 @@ struct Engine {
       for (int k = threadIdx.x; k < n; k += GCR_BLOCK)
         if (row_ok(list[k])) slot.flag[list[k]] = 1;
       sync();
-      if (!fit_cta(list, n, 1)) break;
+      // the FP32 mode starts each refit from the current model
+      if (!fit_cta(list, n, 1, prm.lo_fp32 ? sh.work_model : nullptr)) break;
       const Score sc = exact_score(sh.fit_model, spare);
       ++models_scored;
       if (sc.count < m) break;
@@ -3551,7 +3588,7 @@ struct Engine {
       }
     } else if (!irls_applied) {
       // one least-squares fit on the first best.count points of the container
-      if (fit_cta(list, best.count < n ? best.count : n, 0)) {
+      if (fit_cta(list, best.count < n ? best.count : n, 0, prm.lo_fp32 ? sh.best_model : nullptr)) {
         const int idx = off ^ 1;
         const Score sc = exact_score(sh.fit_model, nullptr);
         copy_model(sh.cont_model[idx], sh.fit_model);
@@ -3579,7 +3616,7 @@ struct Engine {
         for (int k = threadIdx.x; k < cnt; k += GCR_BLOCK)
           slot.dres[k] = fmax(0.0, 1.0 - Est::r2_f64(row64(list[k]), Fb) / t2);
         sync();
-        if (fit_cta_f(list, cnt, 2, false)) {
+        if (fit_cta_f(list, cnt, 2, false, true, prm.lo_fp32 ? sh.best_model : nullptr)) {
           const Score sc = exact_score(sh.fit_model, spare, nullptr, true);
           if (final_score < sc.value) {
             final_score = sc.value;

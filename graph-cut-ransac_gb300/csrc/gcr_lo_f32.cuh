@@ -12,10 +12,9 @@
 // work. A fit's model is only a candidate: it is scored exactly (FP64 inlier
 // decisions) like every other model. The same solver pieces (pivoted-QR null
 // vector, 3x3 SVD, damped Cholesky step) serve the CTA-wide iteratively
-// reweighted fits and final refit of the fast mode; the drivers' bundle
-// adjustment on raw pixel coordinates stays in FP64. Masks can differ from
-// the FP64 fits' in the last bits of a candidate, so parity runs keep the FP64
-// fits (the engine's default).
+// reweighted fits, the final refit and the drivers' bundle adjustment of the
+// fast mode. Masks can differ from the FP64 fits' in the last bits of a
+// candidate, so parity runs keep the FP64 fits (the engine's default).
 #pragma once
 
 #include "gcr_fundamental.cuh"
@@ -242,13 +241,16 @@ __device__ __forceinline__ void fact_to_F(const FactF& f, float* F) {
 }
 
 // truncated Sampson cost of one normalised correspondence (loss scale 1)
-__device__ __forceinline__ float cost_point(const float* F, float p0, float p1, float q0, float q1) {
+// (truncated at trunc2: 1 in the solver's coordinates; s^2 for coordinates
+// scaled by s from a loss truncated at 1 in the original ones)
+__device__ __forceinline__ float cost_point(const float* F, float p0, float p1, float q0, float q1,
+                                           float trunc2 = 1.f) {
   const float Fx0 = F[0] * p0 + F[1] * p1 + F[2], Fx1 = F[3] * p0 + F[4] * p1 + F[5],
               Fx2 = F[6] * p0 + F[7] * p1 + F[8];
   const float C = q0 * Fx0 + q1 * Fx1 + Fx2;
   const float a0 = F[0] * q0 + F[3] * q1 + F[6], a1 = F[1] * q0 + F[4] * q1 + F[7];
   const float r2 = C * C / (Fx0 * Fx0 + Fx1 * Fx1 + a0 * a0 + a1 * a1);
-  return r2 < 1.f ? r2 : 1.f;
+  return r2 < trunc2 ? r2 : trunc2;
 }
 
 // J^T J (lower, 28) and J^T r (7) of one correspondence, weight 1/n for the
@@ -257,7 +259,7 @@ __device__ __forceinline__ float cost_point(const float* F, float p0, float p1, 
 // structure of dF/dparams (rotation columns: signed entries of F; sigma column:
 // U[:,1] V[:,1]^T).
 __device__ __forceinline__ void accumulate_point(const float* F, const float* ds, float p0, float p1, float q0,
-                                                 float q1, float inv_n, float* acc) {
+                                                 float q1, float inv_n, float* acc, float trunc2 = 1.f) {
   const float Fx0 = F[0] * p0 + F[1] * p1 + F[2], Fx1 = F[3] * p0 + F[4] * p1 + F[5],
               Fx2 = F[6] * p0 + F[7] * p1 + F[8];
   const float C = q0 * Fx0 + q1 * Fx1 + Fx2;
@@ -265,7 +267,7 @@ __device__ __forceinline__ void accumulate_point(const float* F, const float* ds
   const float J2 = Fx0, J3 = Fx1;
   const float inv = rsqrtf(J0 * J0 + J1 * J1 + J2 * J2 + J3 * J3);
   const float r = C * inv;
-  if (!(r * r < 1.f)) return;
+  if (!(r * r < trunc2)) return;
   float dF[9] = {p0 * q0, p0 * q1, p0, p1 * q0, p1 * q1, p1, q0, q1, 1.f};
   const float s = C * inv * inv;
   dF[0] -= s * (J2 * p0 + J0 * q0);

@@ -261,16 +261,16 @@ gcr_status gcr_context_last_tuning(const gcr_context* ctx, gcr_tuning* out);
  * computes in double throughout):
  *   GCR_LO_FP64  (default) the reference's arithmetic: masks and counts equal
  *                the FP64 oracle's
- *   GCR_LO_FP32  fundamental-matrix fits on normalised coordinates after the
- *                minimal solver (the graph-cut local optimisation's trials,
- *                the iteratively reweighted fits and the final refit) take
- *                their per-correspondence terms in FP32 from the FP32 tile:
- *                the LO trials run 8-point and Levenberg-Marquardt wholly in
- *                FP32, the CTA-wide fits reduce in FP64 and solve their normal
- *                equations in FP64. Every fit is still scored with exact inlier
- *                decisions; the drivers' bundle adjustment on raw pixel
- *                coordinates stays FP64. Models agree with the FP64 fits to
- *                model tolerance, masks can differ in borderline points. For
+ *   GCR_LO_FP32  every fundamental-matrix fit after the minimal solver (the
+ *                graph-cut local optimisation's trials, the iteratively
+ *                reweighted fits, the final refit and the drivers' bundle
+ *                adjustment) runs 8-point and Levenberg-Marquardt in FP32 from
+ *                the FP32 tile, CTA-wide sums reduced in FP64; the bundle
+ *                adjustment on raw pixel coordinates works on the pair's
+ *                centred coordinates scaled into [-1, 1] with its loss
+ *                truncation scaled alike. Every fit is still scored with exact
+ *                inlier decisions. Models agree with the FP64 fits to model
+ *                tolerance, masks can differ in borderline points. For
  *                throughput forms (the learned proposal), not for parity runs. */
 enum { GCR_LO_FP64 = 0, GCR_LO_FP32 = 1 };
 gcr_status gcr_context_set_lo_precision(gcr_context* ctx, int32_t precision);

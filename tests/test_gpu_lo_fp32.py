@@ -1,6 +1,7 @@
-"""The FP32 fits (gcr_context_set_lo_precision(GCR_LO_FP32)): the
-fundamental-matrix fits on normalised coordinates after the minimal solver
-(local-optimisation trials, iteratively reweighted fits, final refit) in FP32.
+"""The FP32 fits (gcr_context_set_lo_precision(GCR_LO_FP32)): every
+fundamental-matrix fit after the minimal solver (local-optimisation trials,
+iteratively reweighted fits, final refit, the drivers' bundle adjustment) in
+FP32.
 It is a throughput mode, judged on model error rather than mask parity:
 
 * on hard pairs (4000 correspondences, 5-10 % inliers, the learned proposal's
