@@ -326,24 +326,43 @@ __device__ __forceinline__ float4 bf4(const __nv_bfloat16* w, int i) {
   return make_float4(a.x, a.y, b.x, b.y);
 }
 
-// ---- Forward pass on the tensor cores: mma.sync m16n8k16, BF16 x BF16 ->
-// FP32. Each warp owns 16 rows; a layer is 16 n-tiles of 8 columns x K/16
-// k-steps. The FP32 accumulator fragment of n-tiles (2j, 2j+1) has exactly
-// the layout of the next layer's A fragment for k-step j (rows g and g + 8,
-// columns 2t, 2t + 1 and 8 + 2t, 9 + 2t of the 16), so activations stay in
-// registers between layers: bias, ReLU, rounding to BF16, next layer. The
-// weights sit in shared memory transposed ([n][k], rows padded by 8 so the
-// warp's B-fragment loads hit 32 distinct banks) and are loaded once per
-// persistent CTA. The output layer (128 -> 1) is an FP32 dot product of the
-// third layer's FP32 activations, reduced over the four lanes of each row.
+// ---- Forward pass on the fifth-generation tensor cores (tcgen05) ----------
+// A persistent CTA of four warps takes tiles of 128 rows (correspondences).
+// Each layer is one chain of K/16 tcgen05.mma instructions (kind::f16: BF16
+// operands read from shared memory through matrix descriptors, M = N = 128,
+// FP32 accumulator in tensor memory), issued by one thread; its completion
+// arrives on an mbarrier through tcgen05.commit. The epilogue reads the
+// accumulator back with tcgen05.ld (thread i of warp w owns TMEM lane
+// 32w + i, which holds row 32w + i of the tile), adds the bias, applies ReLU,
+// rounds to BF16 and writes the next layer's A operand into shared memory.
+// The output layer (128 -> 1) is each thread's FP32 dot product over its row.
 // Activations: layer inputs are rounded to BF16 (the features included); A1
 // and A2 are stored rounded (what the next layer read), A3 in FP32.
-constexpr int kMmaWarps = 4;
-constexpr int kTileRows = 16 * kMmaWarps;
-constexpr int kLd1 = kIn + 8;
-constexpr int kLdH = kH + 8;
-constexpr size_t kForwardSmem =
-    sizeof(__nv_bfloat16) * (size_t)(kH * kLd1 + 2 * kH * kLdH) + sizeof(float) * (size_t)(4 * kH + 4);
+//
+// Operand layout in shared memory: no swizzle, K-major, 8 x 8 BF16 core
+// matrices of 128 contiguous bytes (8 rows x 16 bytes). For an operand of
+// 128 rows (the activations' M or the weights' N), element (row, k) sits at
+// (k / 8) * 2048 + (row / 8) * 128 + (row % 8) * 16 + (k % 8) * 2: the
+// descriptors' leading byte offset (next core matrix along K) is 2048 and the
+// stride byte offset (next group of 8 rows) is 128. Weights are stored as
+// W^T ([n][k]); the features' 32 columns use the first 8 KB of the
+// activation buffer in the same layout.
+constexpr int kUmmaRows = 128;  // rows per tile = MMA M = TMEM lanes
+constexpr int kUmmaThreads = 128;
+constexpr uint32_t kUmmaLbo = 2048, kUmmaSbo = 128;
+constexpr uint32_t kTmemCols = 128;  // one FP32 accumulator of 128 x 128
+constexpr size_t kSmW1 = 0;
+constexpr size_t kSmW2 = kSmW1 + sizeof(__nv_bfloat16) * kH * kIn;
+constexpr size_t kSmW3 = kSmW2 + sizeof(__nv_bfloat16) * kH * kH;
+constexpr size_t kSmAct = kSmW3 + sizeof(__nv_bfloat16) * kH * kH;
+constexpr size_t kSmVec = kSmAct + sizeof(__nv_bfloat16) * kUmmaRows * kH;
+constexpr size_t kSmBar = kSmVec + ((sizeof(float) * (4 * kH + 1) + 15) & ~size_t(15));
+constexpr size_t kForwardSmem = kSmBar + 16;  // mbarrier + TMEM address
+// instruction descriptor of kind::f16: D FP32 (bits 4-5 = 1), A and B BF16
+// (bits 7-9 and 10-12 = 1), both K-major (bits 15, 16 = 0), N / 8 at bit 17,
+// M / 16 at bit 24
+constexpr uint32_t kUmmaIdesc =
+    (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kH >> 3) << 17) | ((uint32_t)(kUmmaRows >> 4) << 24);
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
   const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
@@ -351,130 +370,227 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
 }
 __device__ __forceinline__ float round_bf16(float v) { return __bfloat162float(__float2bfloat16_rn(v)); }
 
-__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+// byte offset of element (row, k) of a 128-row operand (layout above)
+__device__ __forceinline__ uint32_t core_offset(int row, int k) {
+  return (uint32_t)((k >> 3) * kUmmaLbo + (row >> 3) * kUmmaSbo + (row & 7) * 16 + (k & 7) * 2);
+}
+// shared-memory matrix descriptor: start address, leading and stride byte
+// offsets (all >> 4), descriptor version 1 at bit 46, no swizzle (bits 61-63)
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)(kUmmaLbo >> 4) << 16) |
+         ((uint64_t)(kUmmaSbo >> 4) << 32) | (1ull << 46);
+}
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
   asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+      ::"r"(tmem_d), "l"(a), "l"(b), "r"(kUmmaIdesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit(unsigned long long* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// orders this thread's generic-proxy writes of shared memory before the
+// tensor cores' (async-proxy) reads
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_init1(unsigned long long* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// waits for the phase of the given parity with a bounded number of polls
+__device__ __forceinline__ bool mbar_wait_parity(unsigned long long* bar, unsigned parity) {
+  constexpr int kPolls = 1 << 22;
+  for (int it = 0; it < kPolls; ++it) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+// 32 consecutive FP32 accumulator columns of this thread's TMEM lane; the
+// wait for the load is part of the same statement, so no use of the
+// registers can move before it
+__device__ __forceinline__ void tmem_load32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
+      "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// c = bias + A W for one warp's 16 rows; Wt is [kH][ld] (n-major), K the layer width
+// One layer: the A operand (this tile's activations) and B (the layer's W^T)
+// in shared memory, K / 16 MMAs into the TMEM accumulator, then every thread
+// waits for their completion. Returns false when the bounded wait ran out.
 template <int K>
-__device__ __forceinline__ void mma_layer(const uint32_t (&a)[K / 16][4], const __nv_bfloat16* Wt, int ld,
-                                          const float* bias, float (&c)[kH / 8][4], int g, int t) {
+__device__ __forceinline__ bool umma_layer(uint32_t tmem, uint32_t a_base, uint32_t b_base, unsigned long long* bar,
+                                           unsigned& phase) {
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    tc_fence_after();
 #pragma unroll
-  for (int nt = 0; nt < kH / 8; ++nt) {
-    const float b0 = bias[8 * nt + 2 * t], b1 = bias[8 * nt + 2 * t + 1];
-    c[nt][0] = b0;
-    c[nt][1] = b1;
-    c[nt][2] = b0;
-    c[nt][3] = b1;
-    const __nv_bfloat16* w = Wt + (8 * nt + g) * ld + 2 * t;
+    for (int ks = 0; ks < K / 16; ++ks)
+      umma_bf16(tmem, umma_desc(a_base + 2 * ks * kUmmaLbo), umma_desc(b_base + 2 * ks * kUmmaLbo), ks > 0);
+    umma_commit(bar);
+  }
+  const bool done = mbar_wait_parity(bar, phase);
+  phase ^= 1u;
+  tc_fence_after();
+  return done;
+}
+
+// bias + ReLU + BF16 rounding of one hidden layer's accumulator row; the
+// rounded values become the next layer's A operand (row r of the tile) and
+// are stored to out when given
+__device__ __forceinline__ void umma_hidden_epilogue(uint32_t t_row, const float* bias, unsigned char* act, int r,
+                                                     float* out, int64_t row, int64_t n) {
+#pragma unroll 1
+  for (int c0 = 0; c0 < kH; c0 += 32) {
+    float v[32];
+    tmem_load32(t_row + (uint32_t)c0, v);
 #pragma unroll
-    for (int ks = 0; ks < K / 16; ++ks) {
-      const uint32_t w0 = *reinterpret_cast<const uint32_t*>(w + 16 * ks);
-      const uint32_t w1 = *reinterpret_cast<const uint32_t*>(w + 16 * ks + 8);
-      mma_bf16(c[nt], a[ks], w0, w1);
+    for (int j = 0; j < 32; ++j) v[j] = round_bf16(fmaxf(v[j] + bias[c0 + j], 0.f));
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      uint4 u;
+      u.x = pack_bf16(v[8 * q], v[8 * q + 1]);
+      u.y = pack_bf16(v[8 * q + 2], v[8 * q + 3]);
+      u.z = pack_bf16(v[8 * q + 4], v[8 * q + 5]);
+      u.w = pack_bf16(v[8 * q + 6], v[8 * q + 7]);
+      *reinterpret_cast<uint4*>(act + core_offset(r, c0 + 8 * q)) = u;
+    }
+    if (out && row < n) {
+      float4* o = reinterpret_cast<float4*>(out + row * kH + c0);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
     }
   }
 }
 
-// ReLU of the accumulators, packed as the next layer's A fragments; the
-// rounded activations are stored to out (when not NULL) for rows ra, rb
-__device__ __forceinline__ void relu_pack(float (&c)[kH / 8][4], uint32_t (&a)[kH / 16][4], float* out, int64_t ra,
-                                          int64_t rb, int64_t n, int t) {
-#pragma unroll
-  for (int nt = 0; nt < kH / 8; ++nt) {
-#pragma unroll
-    for (int q = 0; q < 4; ++q) c[nt][q] = round_bf16(fmaxf(c[nt][q], 0.f));
-    if (out) {
-      const int col = 8 * nt + 2 * t;
-      if (ra < n) *reinterpret_cast<float2*>(out + ra * kH + col) = make_float2(c[nt][0], c[nt][1]);
-      if (rb < n) *reinterpret_cast<float2*>(out + rb * kH + col) = make_float2(c[nt][2], c[nt][3]);
-    }
+__global__ void __launch_bounds__(kUmmaThreads, 2) forward_kernel(const float* feat, int64_t n,
+                                                                  const __nv_bfloat16* P, float* A1, float* A2,
+                                                                  float* A3, float* logits) {
+  extern __shared__ __align__(1024) unsigned char fsm[];
+  unsigned char* act = fsm + kSmAct;
+  float* vec = reinterpret_cast<float*>(fsm + kSmVec);  // b1, b2, b3, w4, b4
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(fsm + kSmBar);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(fsm + kSmBar + 8);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  // W^T in the core-matrix layout; P holds W as [k][n]
+  for (int i = tid; i < kIn * kH; i += kUmmaThreads)
+    *reinterpret_cast<__nv_bfloat16*>(fsm + kSmW1 + core_offset(i % kH, i / kH)) = P[kOffW1 + i];
+  for (int i = tid; i < kH * kH; i += kUmmaThreads) {
+    *reinterpret_cast<__nv_bfloat16*>(fsm + kSmW2 + core_offset(i % kH, i / kH)) = P[kOffW2 + i];
+    *reinterpret_cast<__nv_bfloat16*>(fsm + kSmW3 + core_offset(i % kH, i / kH)) = P[kOffW3 + i];
   }
-#pragma unroll
-  for (int j = 0; j < kH / 16; ++j) {
-    a[j][0] = pack_bf16(c[2 * j][0], c[2 * j][1]);
-    a[j][1] = pack_bf16(c[2 * j][2], c[2 * j][3]);
-    a[j][2] = pack_bf16(c[2 * j + 1][0], c[2 * j + 1][1]);
-    a[j][3] = pack_bf16(c[2 * j + 1][2], c[2 * j + 1][3]);
-  }
-}
-
-__global__ void __launch_bounds__(32 * kMmaWarps, 2) forward_kernel(const float* feat, int64_t n,
-                                                                    const __nv_bfloat16* P, float* A1, float* A2,
-                                                                    float* A3, float* logits) {
-  extern __shared__ __align__(16) unsigned char fsm[];
-  __nv_bfloat16* W1t = reinterpret_cast<__nv_bfloat16*>(fsm);
-  __nv_bfloat16* W2t = W1t + kH * kLd1;
-  __nv_bfloat16* W3t = W2t + kH * kLdH;
-  float* vec = reinterpret_cast<float*>(W3t + kH * kLdH);  // b1, b2, b3, w4, b4
-  for (int i = threadIdx.x; i < kIn * kH; i += blockDim.x) W1t[(i % kH) * kLd1 + i / kH] = P[kOffW1 + i];
-  for (int i = threadIdx.x; i < kH * kH; i += blockDim.x) {
-    W2t[(i % kH) * kLdH + i / kH] = P[kOffW2 + i];
-    W3t[(i % kH) * kLdH + i / kH] = P[kOffW3 + i];
-  }
-  for (int i = threadIdx.x; i < kH; i += blockDim.x) {
+  for (int i = tid; i < kH; i += kUmmaThreads) {
     vec[i] = __bfloat162float(P[kOffB1 + i]);
     vec[kH + i] = __bfloat162float(P[kOffB2 + i]);
     vec[2 * kH + i] = __bfloat162float(P[kOffB3 + i]);
     vec[3 * kH + i] = __bfloat162float(P[kOffW4 + i]);
   }
-  if (threadIdx.x == 0) vec[4 * kH] = __bfloat162float(P[kOffB4]);
+  if (tid == 0) {
+    vec[4 * kH] = __bfloat162float(P[kOffB4]);
+    mbar_init1(bar);
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
   __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int g = lane >> 2, t = lane & 3;
-  const int64_t tiles = (n + kTileRows - 1) / kTileRows;
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t t_row = tmem + ((uint32_t)(32 * warp) << 16);  // this warp's 32 TMEM lanes
+  const uint32_t s_w1 = smem_u32(fsm + kSmW1), s_w2 = smem_u32(fsm + kSmW2), s_w3 = smem_u32(fsm + kSmW3);
+  const uint32_t s_act = smem_u32(act);
+  unsigned phase = 0;
+  int64_t failed_tile = -1;
+  const int64_t tiles = (n + kUmmaRows - 1) / kUmmaRows;
   for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-    const int64_t ra = tile * kTileRows + 16 * warp + g, rb = ra + 8;
-    uint32_t a1[kIn / 16][4];
+    const int64_t row = tile * kUmmaRows + tid;
+    // layer 1's A operand: this row's 32 features rounded to BF16
+    {
+      float4 x[kIn / 4];
+      if (row < n) {
+        const float4* src = reinterpret_cast<const float4*>(feat + row * kIn);
 #pragma unroll
-    for (int ks = 0; ks < kIn / 16; ++ks) {
-      const int c0 = 16 * ks + 2 * t;
-      float2 x00 = make_float2(0.f, 0.f), x01 = x00, x10 = x00, x11 = x00;
-      if (ra < n) {
-        x00 = *reinterpret_cast<const float2*>(feat + ra * kIn + c0);
-        x01 = *reinterpret_cast<const float2*>(feat + ra * kIn + c0 + 8);
-      }
-      if (rb < n) {
-        x10 = *reinterpret_cast<const float2*>(feat + rb * kIn + c0);
-        x11 = *reinterpret_cast<const float2*>(feat + rb * kIn + c0 + 8);
-      }
-      a1[ks][0] = pack_bf16(x00.x, x00.y);
-      a1[ks][1] = pack_bf16(x10.x, x10.y);
-      a1[ks][2] = pack_bf16(x01.x, x01.y);
-      a1[ks][3] = pack_bf16(x11.x, x11.y);
-    }
-    float c[kH / 8][4];
-    uint32_t a[kH / 16][4];
-    mma_layer<kIn>(a1, W1t, kLd1, vec, c, g, t);
-    relu_pack(c, a, A1, ra, rb, n, t);
-    mma_layer<kH>(a, W2t, kLdH, vec + kH, c, g, t);
-    relu_pack(c, a, A2, ra, rb, n, t);
-    mma_layer<kH>(a, W3t, kLdH, vec + 2 * kH, c, g, t);
-    float sa = 0.f, sb = 0.f;
+        for (int j = 0; j < kIn / 4; ++j) x[j] = src[j];
+      } else {
 #pragma unroll
-    for (int nt = 0; nt < kH / 8; ++nt) {
-      const int col = 8 * nt + 2 * t;
-      const float h0 = fmaxf(c[nt][0], 0.f), h1 = fmaxf(c[nt][1], 0.f);
-      const float h2 = fmaxf(c[nt][2], 0.f), h3 = fmaxf(c[nt][3], 0.f);
-      sa = fmaf(h0, vec[3 * kH + col], fmaf(h1, vec[3 * kH + col + 1], sa));
-      sb = fmaf(h2, vec[3 * kH + col], fmaf(h3, vec[3 * kH + col + 1], sb));
-      if (A3) {
-        if (ra < n) *reinterpret_cast<float2*>(A3 + ra * kH + col) = make_float2(h0, h1);
-        if (rb < n) *reinterpret_cast<float2*>(A3 + rb * kH + col) = make_float2(h2, h3);
+        for (int j = 0; j < kIn / 4; ++j) x[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int kg = 0; kg < kIn / 8; ++kg) {
+        uint4 u;
+        u.x = pack_bf16(x[2 * kg].x, x[2 * kg].y);
+        u.y = pack_bf16(x[2 * kg].z, x[2 * kg].w);
+        u.z = pack_bf16(x[2 * kg + 1].x, x[2 * kg + 1].y);
+        u.w = pack_bf16(x[2 * kg + 1].z, x[2 * kg + 1].w);
+        *reinterpret_cast<uint4*>(act + core_offset(tid, 8 * kg)) = u;
       }
     }
-    sa += __shfl_xor_sync(0xffffffffu, sa, 1);
-    sa += __shfl_xor_sync(0xffffffffu, sa, 2);
-    sb += __shfl_xor_sync(0xffffffffu, sb, 1);
-    sb += __shfl_xor_sync(0xffffffffu, sb, 2);
-    if (t == 0) {
-      if (ra < n) logits[ra] = sa + vec[4 * kH];
-      if (rb < n) logits[rb] = sb + vec[4 * kH];
+    bool ok = umma_layer<kIn>(tmem, s_act, s_w1, bar, phase);
+    if (__syncthreads_or(!ok)) { failed_tile = tile; break; }
+    umma_hidden_epilogue(t_row, vec, act, tid, A1, row, n);
+    ok = umma_layer<kH>(tmem, s_act, s_w2, bar, phase);
+    if (__syncthreads_or(!ok)) { failed_tile = tile; break; }
+    umma_hidden_epilogue(t_row, vec + kH, act, tid, A2, row, n);
+    ok = umma_layer<kH>(tmem, s_act, s_w3, bar, phase);
+    if (__syncthreads_or(!ok)) { failed_tile = tile; break; }
+    float s = 0.f;
+#pragma unroll 1
+    for (int c0 = 0; c0 < kH; c0 += 32) {
+      float v[32];
+      tmem_load32(t_row + (uint32_t)c0, v);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        v[j] = fmaxf(v[j] + vec[2 * kH + c0 + j], 0.f);
+        s = fmaf(v[j], vec[3 * kH + c0 + j], s);
+      }
+      if (A3 && row < n) {
+        float4* o = reinterpret_cast<float4*>(A3 + row * kH + c0);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+      }
     }
+    if (row < n) logits[row] = s + vec[4 * kH];
+  }
+  if (failed_tile >= 0) {
+    // a commit that never arrived: give the MMAs in flight one more bounded
+    // wait and set this CTA's remaining logits to NaN (they sort last)
+    mbar_wait_parity(bar, phase ^ 1u);
+    for (int64_t tile = failed_tile; tile < tiles; tile += gridDim.x) {
+      const int64_t row = tile * kUmmaRows + tid;
+      if (row < n) logits[row] = __int_as_float(0x7fc00000);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
   }
 }
 
@@ -749,14 +865,16 @@ gcr_status gcr_learned_params_to_bf16(const float* d_master, void* d_bf16, void*
 gcr_status gcr_learned_forward(const float* d_feat, int64_t n, const void* d_bf16, float* d_a1, float* d_a2,
                                float* d_a3, float* d_logits, void* stream) {
   if (!d_feat || !d_bf16 || !d_logits) return fail(GCR_INVALID_ARG, "NULL buffer");
+  if (((uintptr_t)d_feat | (uintptr_t)d_a1 | (uintptr_t)d_a2 | (uintptr_t)d_a3) & 15)
+    return fail(GCR_INVALID_ARG, "feature and activation buffers must be 16-byte aligned");
   if (n <= 0) return GCR_OK;
   int dev = 0, sms = 0;
   CUDA_TRY(cudaGetDevice(&dev));
   CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   CUDA_TRY(cudaFuncSetAttribute(forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kForwardSmem));
-  const int64_t tiles = (n + kTileRows - 1) / kTileRows;
+  const int64_t tiles = (n + kUmmaRows - 1) / kUmmaRows;
   const unsigned grid = (unsigned)(tiles < 2 * sms ? tiles : 2 * sms);
-  forward_kernel<<<grid, 32 * kMmaWarps, kForwardSmem, (cudaStream_t)stream>>>(
+  forward_kernel<<<grid, kUmmaThreads, kForwardSmem, (cudaStream_t)stream>>>(
       d_feat, n, (const __nv_bfloat16*)d_bf16, d_a1, d_a2, d_a3, d_logits);
   CUDA_TRY(cudaGetLastError());
   return GCR_OK;

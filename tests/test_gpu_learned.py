@@ -92,6 +92,33 @@ def test_forward_matches_oracle(torch, net):
     np.testing.assert_allclose(a3, A3, rtol=1e-2, atol=1e-2 * np.abs(A3).max())
 
 
+@pytest.mark.parametrize("n", [1, 127, 128, 129, 383, 20000])
+def test_forward_tile_edges(torch, net, n):
+    """The forward kernel works on tiles of 128 rows (one tensor-core MMA of
+    M = 128 per layer); partial tiles, single rows and more tiles than
+    resident CTAs give the oracle's logits, and every row is written."""
+    rng = np.random.Generator(np.random.PCG64(100 + n))
+    X = np.zeros((n, 32), np.float32)
+    X[:, :20] = rng.uniform(-0.5, 2.0, (n, 20)).astype(np.float32)
+    _, (a1, a2, a3), zd = _device_forward(torch, net, X)
+    A1, A2, A3, ref = M.forward(X, net.bf16_parameters())
+    got = zd.cpu().numpy()
+    assert np.isfinite(got).all()
+    scale = max(np.abs(ref).max(), 1e-3)
+    d = np.abs(got - ref)
+    assert np.percentile(d, 99) <= LOGIT_RTOL * scale, (np.percentile(d, 99), scale)
+    assert d.max() <= 1e-2 * scale
+    for dev, orc in ((a1, A1), (a2, A2)):
+        assert np.mean(dev != orc) < 2e-3
+    # logits without the activation outputs equal those with them
+    d_x = torch.from_numpy(X).cuda()
+    z2 = torch.empty(n, dtype=torch.float32, device="cuda")
+    import ctypes
+    assert net.lib.gcr_learned_forward(ctypes.c_void_p(d_x.data_ptr()), n, ctypes.c_void_p(net.bf16.data_ptr()),
+                                       None, None, None, ctypes.c_void_p(z2.data_ptr()), None) == 0
+    assert np.array_equal(z2.cpu().numpy(), got)
+
+
 def test_backward_matches_oracle(torch, net):
     """Gradient of the device backward pass vs the FP64 restatement on the
     device forward's own layer inputs (so only the backward arithmetic is
