@@ -70,9 +70,19 @@ const gcr::KindOps* ops_for(gcr_model_kind kind) {
     case GCR_HOMOGRAPHY: return gcr::homography_ops();
     case GCR_FUNDAMENTAL: return gcr::fundamental_ops();
     case GCR_ESSENTIAL: return gcr::essential_ops();
+    case GCR_HOMOGRAPHY_AFFINE: return gcr::homography_affine_ops();
   }
   return nullptr;
 }
+
+// Doubles per correspondence row of a model kind (gcr_model_kind).
+int kind_columns(gcr_model_kind kind) { return kind == GCR_HOMOGRAPHY_AFFINE ? 8 : 4; }
+
+// The homography drivers construct their SPRT test without the
+// min_inlier_ratio_for_sprt argument (gcransac_python.cpp:4394-4396,
+// 4719-4721), so it starts from the constructor's default inlier ratio 0.01
+// (preemption_sprt.h:141-143); the other drivers pass the argument.
+bool homography_driver(gcr_model_kind kind) { return kind == GCR_HOMOGRAPHY || kind == GCR_HOMOGRAPHY_AFFINE; }
 
 }  // namespace
 
@@ -84,6 +94,7 @@ struct gcr_context {
   int device = 0;
   int num_sms = 0;
   DevBuf pairs, slots_meta, slot_mem, pts32, ticket, norm_pts, kinv, row_pair, phase, aux;
+  DevBuf affine;  // affine correspondences: the point columns, then the affine maps ([total][4] each)
   // staging of the host-buffer entry points
   DevBuf corr, models, masks, stats;
   DevBuf magsac;  // the MAGSAC++ weight table, uploaded on first use
@@ -95,12 +106,14 @@ struct gcr_context {
     gcr::Workspace ws{};
     gcr::EngineParams prm{};
     bool normalise = false;
+    bool split_affine = false;      // affine correspondences: split the rows of 8 before the engine runs
+    int64_t total = 0;
     const double* probs = nullptr;  // importance sampler: probabilities to tabulate
     const double* d_corr = nullptr;
     int num_pairs = 0;
   } pending;
   int slot_kind = -1, slot_max_n = 0, slot_count = 0;
-  bool prepared[3] = {false, false, false};
+  bool prepared[4] = {false, false, false, false};
   unsigned long long* pair_times = nullptr;  // see gcr_context_set_pair_times
   DevBuf rg_int, rg_dbl, rg_px;              // radius-graph scratch (one region per resident CTA)
   DevBuf ar_p, ar_i, ar_ab, ar_cnt;          // AR sampler heaps and per-point state (per resident CTA)
@@ -146,7 +159,13 @@ gcr_status check_params(gcr_model_kind kind, const gcr_params* p) {
     return fail(GCR_UNSUPPORTED, "neighborhood_size must be at most 1024 grid divisions");
   if (p->neighborhood == GCR_NEIGHBORHOOD_FLANN && !(p->neighborhood_size > 0 && std::isfinite(p->neighborhood_size)))
     return fail(GCR_INVALID_ARG, "neighborhood_size (the radius) must be > 0 and finite for the radius graph");
-  (void)kind;
+  if (kind == GCR_HOMOGRAPHY_AFFINE) {
+    // findHomographyAC_ (gcransac_python.cpp:4553-4811): MSAC, and no P-NAPSAC
+    if (p->sampler == GCR_SAMPLER_PNAPSAC)
+      return fail(GCR_UNSUPPORTED, "the affine-correspondence homography provides samplers 0, 1, 3 and 4");
+    if (p->scoring != GCR_SCORING_MSAC)
+      return fail(GCR_UNSUPPORTED, "the affine-correspondence homography scores with MSAC only");
+  }
   return GCR_OK;
 }
 
@@ -209,10 +228,11 @@ void gcr_default_params(gcr_model_kind kind, gcr_params* p) {
   p->sampler_variance = 0.1;
   switch (kind) {
     case GCR_HOMOGRAPHY:  // bindings.cpp:1158-1178
+    case GCR_HOMOGRAPHY_AFFINE:  // the same python entry with solver = 2
       p->spatial_coherence_weight = 0.975;
       p->neighborhood = GCR_NEIGHBORHOOD_GRID;
       p->neighborhood_size = 4.0;
-      p->use_space_partitioning = 1;
+      p->use_space_partitioning = kind == GCR_HOMOGRAPHY ? 1 : 0;
       break;
     case GCR_FUNDAMENTAL:  // bindings.cpp:1003-1022
       p->spatial_coherence_weight = 0.0;
@@ -250,7 +270,7 @@ gcr_status gcr_context_create(gcr_context** ctx) {
 
 gcr_status gcr_context_destroy(gcr_context* c) {
   if (!c) return GCR_OK;
-  for (DevBuf* b : {&c->pairs, &c->slots_meta, &c->slot_mem, &c->pts32, &c->aux, &c->ticket, &c->norm_pts, &c->kinv,
+  for (DevBuf* b : {&c->pairs, &c->slots_meta, &c->slot_mem, &c->pts32, &c->aux, &c->affine, &c->ticket, &c->norm_pts, &c->kinv,
                     &c->row_pair, &c->phase, &c->corr, &c->models, &c->masks, &c->stats, &c->magsac, &c->rg_int,
                     &c->rg_dbl, &c->rg_px, &c->ar_p, &c->ar_i, &c->ar_ab, &c->ar_cnt, &c->cdf, &c->probs_stage, &c->tape_stage, &c->order})
     b->release();
@@ -291,6 +311,8 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
   if (!d_corr || !h_offsets || !h_sizes || !d_models_out || !d_masks_out || !d_stats_out)
     return fail(GCR_INVALID_ARG, "NULL buffer");
   if (kind == GCR_ESSENTIAL && !h_K && !run_only) return fail(GCR_INVALID_ARG, "essential matrices need intrinsics");
+  if (kind == GCR_HOMOGRAPHY_AFFINE && run_only)
+    return fail(GCR_UNSUPPORTED, "gcr_run takes point correspondences; affine ones run through gcr_find_batch");
   const int m = ops->sample_size;
   int max_n = 0;
   for (int64_t i = 0; i < num_pairs; ++i) {
@@ -437,6 +459,14 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
     CUDA_TRY(c->norm_pts.ensure(sizeof(double) * 4 * (size_t)std::max<int64_t>(total, 1)));
     run_pts = (const double*)c->norm_pts.p;
   }
+  const double* affine_maps = nullptr;
+  if (kind == GCR_HOMOGRAPHY_AFFINE) {
+    // rows of 8 are split into the point columns (what every step but the
+    // minimal solver reads) and the affine maps
+    CUDA_TRY(c->affine.ensure(sizeof(double) * 8 * (size_t)std::max<int64_t>(total, 1)));
+    run_pts = (const double*)c->affine.p;
+    affine_maps = run_pts + 4 * (size_t)std::max<int64_t>(total, 1);
+  }
   // the centred FP32 copy of every pair (staging kernel) and its per-pair results
   CUDA_TRY(c->pts32.ensure(sizeof(float4) * (size_t)std::max<int64_t>(total, 1)));
   CUDA_TRY(c->aux.ensure(sizeof(gcr::PairAux) * (size_t)num_pairs));
@@ -457,7 +487,8 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
 
   gcr::Workspace ws;
   ws.pts64 = run_pts;
-  ws.pix64 = run_only ? run_only->d_pixels : d_corr;
+  ws.pix64 = run_only ? run_only->d_pixels : (kind == GCR_HOMOGRAPHY_AFFINE ? run_pts : d_corr);
+  ws.affine64 = affine_maps;
   ws.pts32 = (float4*)c->pts32.p;
   ws.pairs = (const gcr::PairDesc*)c->pairs.p;
   ws.slots = (gcr::Slot*)c->slots_meta.p;
@@ -496,7 +527,7 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
   prm.pp_h = nullptr;
   prm.use_sprt = params->use_sprt ? 1 : 0;
   prm.use_sp = (kind == GCR_HOMOGRAPHY && params->use_space_partitioning) ? 1 : 0;
-  prm.sprt_min_ratio = params->min_inlier_ratio_for_sprt;
+  prm.sprt_min_ratio = homography_driver(kind) && !run_only ? 0.01 : params->min_inlier_ratio_for_sprt;
   prm.epilogue = run_only ? 0 : 1;
   prm.flow_cap = c->flow_cap;
   prm.tape = c->tape;
@@ -579,6 +610,8 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
   L->ws = ws;
   L->prm = prm;
   L->normalise = kind == GCR_ESSENTIAL && !run_only;
+  L->split_affine = kind == GCR_HOMOGRAPHY_AFFINE;
+  L->total = total;
   L->probs = params->sampler == GCR_SAMPLER_IMPORTANCE ? c->probs : nullptr;
   L->d_corr = d_corr;
   L->num_pairs = (int)num_pairs;
@@ -594,6 +627,11 @@ static gcr_status launch_batch(gcr_context* c, const gcr_context::Pending& L, cu
   if (L.normalise) {
     CUDA_TRY(gcr::launch_normalise_essential(L.d_corr, (const double*)c->kinv.p, (const gcr::PairDesc*)c->pairs.p,
                                              L.num_pairs, (double*)c->norm_pts.p, s));
+    ++launches;
+  }
+  if (L.split_affine) {
+    double* pts = (double*)c->affine.p;
+    CUDA_TRY(gcr::launch_split_affine(L.d_corr, L.total, pts, pts + 4 * std::max<int64_t>(L.total, 1), s));
     ++launches;
   }
   if (L.probs) {
@@ -626,6 +664,27 @@ __global__ void importance_cdf_kernel(const double* probs, const PairDesc* pairs
     c[i] = acc;
   }
   if (pd.n > 0) c[pd.n - 1] = 1.0;
+}
+
+// Affine correspondences: rows of 8 (x1, y1, x2, y2, a11, a12, a21, a22) into
+// the point rows [total][4] and the affine maps [total][4] (grid-stride, two
+// 16-byte loads and stores per row when the input is 16-byte aligned).
+__global__ void split_affine_kernel(const double* corr8, int64_t total, double* pts, double* aff) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const double* r = corr8 + 8 * i;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      pts[4 * i + k] = r[k];
+      aff[4 * i + k] = r[4 + k];
+    }
+  }
+}
+
+cudaError_t launch_split_affine(const double* corr8, int64_t total, double* pts, double* aff, cudaStream_t s) {
+  if (total <= 0) return cudaSuccess;
+  const int64_t blocks = std::min<int64_t>((total + 255) / 256, 4096);
+  split_affine_kernel<<<(unsigned)blocks, 256, 0, s>>>(corr8, total, pts, aff);
+  return cudaGetLastError();
 }
 
 // Staging kernel, one CTA per pair (grid-stride over pairs): the centred FP32
@@ -787,12 +846,13 @@ gcr_status gcr_find_batch(gcr_model_kind kind, int64_t num_pairs, const double* 
     if (s != GCR_OK) return s;
   }
   const int64_t total = offsets[num_pairs];
-  CUDA_TRY(ctx->corr.ensure(sizeof(double) * 4 * (size_t)std::max<int64_t>(total, 1)));
+  const int cols = kind_columns(kind);
+  CUDA_TRY(ctx->corr.ensure(sizeof(double) * cols * (size_t)std::max<int64_t>(total, 1)));
   CUDA_TRY(ctx->models.ensure(sizeof(double) * 9 * num_pairs));
   CUDA_TRY(ctx->masks.ensure((size_t)std::max<int64_t>(total, 1)));
   CUDA_TRY(ctx->stats.ensure(sizeof(gcr_stats) * num_pairs));
   cudaStream_t s = 0;
-  CUDA_TRY(cudaMemcpyAsync(ctx->corr.p, corr, sizeof(double) * 4 * total, cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(ctx->corr.p, corr, sizeof(double) * cols * total, cudaMemcpyHostToDevice, s));
   ctx->probs = nullptr;
   if (g_batch_probs) {
     CUDA_TRY(ctx->probs_stage.ensure(sizeof(double) * (size_t)std::max<int64_t>(total, 1)));
@@ -826,7 +886,8 @@ static gcr_status find_one(gcr_model_kind kind, const double* corr, int64_t n, c
                            const gcr_image_size* size, const double* probabilities, const gcr_params* params,
                            double* model_out9, uint8_t* mask_out, gcr_stats* stats_out) {
   if (!corr || !size || !params || !model_out9 || !mask_out) return fail(GCR_INVALID_ARG, "NULL argument");
-  const int m = kind == GCR_HOMOGRAPHY ? 4 : (kind == GCR_FUNDAMENTAL ? 7 : 5);
+  if (!ops_for(kind)) return fail(GCR_UNSUPPORTED, "model kind %d is not provided by this build", (int)kind);
+  const int m = ops_for(kind)->sample_size;
   if (n < m) return fail(GCR_TOO_FEW_POINTS, "%lld correspondences, needs >= %d", (long long)n, m);
   const int64_t offsets[2] = {0, n};
   double K[18];
@@ -873,6 +934,13 @@ gcr_status gcr_find_essential(const double* corr, int64_t n, const double* K1, c
   return find_one(GCR_ESSENTIAL, corr, n, K1, K2, size, probabilities, params, model_out9, mask_out, stats_out);
 }
 
+gcr_status gcr_find_homography_affine(const double* corr, int64_t n, const gcr_image_size* size,
+                                      const double* probabilities, const gcr_params* params, double* model_out9,
+                                      uint8_t* mask_out, gcr_stats* stats_out) {
+  return find_one(GCR_HOMOGRAPHY_AFFINE, corr, n, nullptr, nullptr, size, probabilities, params, model_out9,
+                  mask_out, stats_out);
+}
+
 }  // extern "C"
 
 // GCRANSAC::run on one pair (gcr_run and gcr_run_with_probabilities):
@@ -885,7 +953,8 @@ static gcr_status run_single(gcr_model_kind kind, const double* points, const do
   g_last_launches = 0;
   if (!points || !cell_sizes || !size || !params || !model_out9 || !mask_out)
     return fail(GCR_INVALID_ARG, "NULL argument");
-  const int m = kind == GCR_HOMOGRAPHY ? 4 : (kind == GCR_FUNDAMENTAL ? 7 : 5);
+  if (!ops_for(kind)) return fail(GCR_UNSUPPORTED, "model kind %d is not provided by this build", (int)kind);
+  const int m = ops_for(kind)->sample_size;
   if (n < m) return fail(GCR_TOO_FEW_POINTS, "%lld points, needs >= %d", (long long)n, m);
   if (divisions < 1) return fail(GCR_INVALID_ARG, "the grid needs at least one division per axis");
   for (int q = 0; q < 4; ++q)
@@ -977,4 +1046,5 @@ namespace gcr {
 // Kinds not compiled into this build.
 __attribute__((weak)) const KindOps* fundamental_ops() { return nullptr; }
 __attribute__((weak)) const KindOps* essential_ops() { return nullptr; }
+__attribute__((weak)) const KindOps* homography_affine_ops() { return nullptr; }
 }  // namespace gcr

@@ -203,6 +203,7 @@ struct Workspace {
   unsigned long long* times;  // [P][2] global timer (ns) when a CTA takes the pair and when it is done, or null
   const int* order;     // [P] pair of each work ticket (largest pairs first), or null for ticket order
   const PairAux* aux;   // [P] staging results (centre_kernel)
+  const double* affine64;  // [total][4] local affine maps (a11, a12, a21, a22) of affine correspondences, or null
 };
 
 struct Score {
@@ -294,6 +295,7 @@ struct Engine {
   const Slot& slot;
   int pair;
   const double* pts64;
+  const double* affine64;  // this pair's local affine maps (affine correspondences), or null
   const float4* pts32;   // shared-memory or global FP32 copy of this pair
   double scale = 1.0;    // max |centred coordinate| of this pair
   int N;
@@ -329,6 +331,7 @@ struct Engine {
       : sh(s), ws(w), prm(p), pd(d), slot(sl), pair(pair_) {
     N = pd.n;
     pts64 = ws.pts64 + 4 * pd.offset;
+    affine64 = ws.affine64 ? ws.affine64 + 4 * pd.offset : nullptr;
     const double tt = 1.5 * pd.threshold;
     t2 = tt * tt;
     log_prob = log(1.0 - prm.confidence);
@@ -3310,7 +3313,11 @@ struct Engine {
     }
     double mloc[9 * Est::MAXSOL];
     int nm = 0;
-    if (ok && Est::valid_sample(pts64, s)) nm = Est::minimal(pts64, s, mloc, prm.pp_h);
+    if constexpr (Est::AFFINE) {
+      if (ok && Est::valid_sample_affine(pts64, affine64, s)) nm = Est::minimal_affine(pts64, affine64, s, mloc);
+    } else {
+      if (ok && Est::valid_sample(pts64, s)) nm = Est::minimal(pts64, s, mloc, prm.pp_h);
+    }
 #pragma unroll
     for (int q = 0; q < Est::M; ++q) slot.bsamples[j * Est::M + q] = s[q];
     int total;

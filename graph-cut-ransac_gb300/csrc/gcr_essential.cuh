@@ -1211,6 +1211,7 @@ struct EssentialModel {
   static constexpr int NONMIN = 5;
   static constexpr int INLIER_LIMIT = 7 * M;
   static constexpr int SAMPLE_CAP = INLIER_LIMIT;
+  static constexpr bool AFFINE = false;
   static constexpr bool CTA_VALIDITY = true;
 
   __device__ static bool valid_sample(const double*, const int*) { return true; }

@@ -171,6 +171,7 @@ struct FundamentalModel {
   static constexpr int NONMIN = 7;
   static constexpr int INLIER_LIMIT = 7 * M;
   static constexpr int SAMPLE_CAP = INLIER_LIMIT;
+  static constexpr bool AFFINE = false;
   static constexpr bool CTA_VALIDITY = true;
 
   // oriented epipolar constraint of a sample (getEpipole + isOrientationValid)
@@ -815,6 +816,7 @@ struct PlaneParallaxModel {
   static constexpr int NONMIN = 8;
   static constexpr int INLIER_LIMIT = 7 * M;
   static constexpr int SAMPLE_CAP = INLIER_LIMIT;
+  static constexpr bool AFFINE = false;
   static constexpr bool CTA_VALIDITY = true;
   using Norm = HomographyModel::Norm;
 

@@ -22,6 +22,7 @@ struct HomographyModel {
   static constexpr int INLIER_LIMIT = 7 * M;
   static constexpr bool WEIGHTED = true;
   static constexpr int SAMPLE_CAP = INLIER_LIMIT;
+  static constexpr bool AFFINE = false;  // minimal samples need no local affine maps
 
   // orientation test: the four points keep the same side of the lines through
   // two of them in both images
@@ -251,6 +252,110 @@ struct HomographyModel {
     for (int k = 0; k < NACC; ++k) acc[k] = 0;
     for (int i = 0; i < n; ++i) accumulate(N, pts + 4 * idx[i], 1.0, acc);
     return solve_normal(N, acc, out);
+  }
+};
+
+// Affine-correspondence homography (findHomographyAC_, solver = 2 of the
+// python entry; src/pygcransac/include/estimators/homography_affine_correspondence_estimator.h:58-403
+// with the minimal solver of solver_homography_two_affine.h:88-237). The
+// minimal sample is two correspondences whose local affine maps (a11, a12,
+// a21, a22) sit in the engine's aux array; residuals, the non-minimal fit and
+// the model check are the point estimator's, the inner sample of the local
+// optimisation is 7 x 2 correspondences.
+struct HomographyAffineModel : HomographyModel {
+  static constexpr int M = 2;
+  static constexpr int INLIER_LIMIT = 7 * M;
+  static constexpr int SAMPLE_CAP = INLIER_LIMIT;
+  static constexpr bool AFFINE = true;
+
+  // isValidSample (:346-400): the point estimator's oriented test on the two
+  // points and two points built from the first affine map,
+  // c = (1, 0, A (1, 0)^T), d = (1, 0, A (0, 1)^T).
+  __device__ static bool valid_sample_affine(const double* pts, const double* aff, const int* s) {
+    const double *a = pts + 4 * s[0], *b = pts + 4 * s[1];
+    const double* A = aff + 4 * s[0];
+    const double c[4] = {1.0, 0.0, A[0], A[2]};
+    const double d[4] = {1.0, 0.0, A[1], A[3]};
+    auto cross = [](double r[3], const double* u, const double* v) {
+      r[0] = u[1] - v[1];
+      r[1] = v[0] - u[0];
+      r[2] = u[0] * v[1] - u[1] * v[0];
+    };
+    double p[3], q[3];
+    cross(p, a, b);
+    cross(q, a + 2, b + 2);
+    if ((p[0] * c[0] + p[1] * c[1] + p[2]) * (q[0] * c[2] + q[1] * c[3] + q[2]) < 0) return false;
+    if ((p[0] * d[0] + p[1] * d[1] + p[2]) * (q[0] * d[2] + q[1] * d[3] + q[2]) < 0) return false;
+    cross(p, c, d);
+    cross(q, c + 2, d + 2);
+    if ((p[0] * a[0] + p[1] * a[1] + p[2]) * (q[0] * a[2] + q[1] * a[3] + q[2]) < 0) return false;
+    if ((p[0] * b[0] + p[1] * b[1] + p[2]) * (q[0] * b[2] + q[1] * b[3] + q[2]) < 0) return false;
+    return true;
+  }
+
+  // The minimal case's 8 x 9 system (both correspondences' point rows, the
+  // first one's four affine rows) has a one-dimensional null space; the
+  // reference takes it from an SVD and divides by h33. With h33 = 1 the first
+  // eight columns form a square system, solved here by Gaussian elimination
+  // with partial pivoting. A singular system gives no model.
+  __device__ static int minimal_affine(const double* pts, const double* aff, const int* s, double* out) {
+    double A[8][9];
+    auto point_rows = [](double (*r)[9], const double* p) {
+      const double x1 = p[0], y1 = p[1], x2 = p[2], y2 = p[3];
+      r[0][0] = -x1; r[0][1] = -y1; r[0][2] = -1.0; r[0][3] = 0.0; r[0][4] = 0.0; r[0][5] = 0.0;
+      r[0][6] = x2 * x1; r[0][7] = x2 * y1; r[0][8] = -x2;
+      r[1][0] = 0.0; r[1][1] = 0.0; r[1][2] = 0.0; r[1][3] = -x1; r[1][4] = -y1; r[1][5] = -1.0;
+      r[1][6] = y2 * x1; r[1][7] = y2 * y1; r[1][8] = -y2;
+    };
+    const double* a = pts + 4 * s[0];
+    const double* m = aff + 4 * s[0];
+    point_rows(A, a);
+    {
+      const double x1 = a[0], y1 = a[1], x2 = a[2], y2 = a[3];
+      const double a11 = m[0], a12 = m[1], a21 = m[2], a22 = m[3];
+      double* r = A[2];
+      r[0] = -1.0; r[1] = 0.0; r[2] = 0.0; r[3] = 0.0; r[4] = 0.0; r[5] = 0.0;
+      r[6] = x2 + a11 * x1; r[7] = a11 * y1; r[8] = -a11;
+      r = A[3];
+      r[0] = 0.0; r[1] = -1.0; r[2] = 0.0; r[3] = 0.0; r[4] = 0.0; r[5] = 0.0;
+      r[6] = a12 * x1; r[7] = x2 + a12 * y1; r[8] = -a12;
+      r = A[4];
+      r[0] = 0.0; r[1] = 0.0; r[2] = 0.0; r[3] = -1.0; r[4] = 0.0; r[5] = 0.0;
+      r[6] = y2 + a21 * x1; r[7] = a21 * y1; r[8] = -a21;
+      r = A[5];
+      r[0] = 0.0; r[1] = 0.0; r[2] = 0.0; r[3] = 0.0; r[4] = -1.0; r[5] = 0.0;
+      r[6] = a22 * x1; r[7] = y2 + a22 * y1; r[8] = -a22;
+    }
+    point_rows(A + 6, pts + 4 * s[1]);
+    // column 8 holds the right-hand side -A[:, 8] (negated above)
+    for (int col = 0; col < 8; ++col) {
+      int piv = col;
+      for (int r = col + 1; r < 8; ++r)
+        if (fabs(A[r][col]) > fabs(A[piv][col])) piv = r;
+      if (!(fabs(A[piv][col]) > 0.0)) return 0;
+      if (piv != col)
+        for (int k = 0; k < 9; ++k) {
+          const double t = A[piv][k];
+          A[piv][k] = A[col][k];
+          A[col][k] = t;
+        }
+      for (int r = col + 1; r < 8; ++r) {
+        const double f = A[r][col] / A[col][col];
+        for (int k = col; k < 9; ++k) A[r][k] -= f * A[col][k];
+      }
+    }
+    double h[8];
+    for (int i = 7; i >= 0; --i) {
+      double acc = A[i][8];
+      for (int k = i + 1; k < 8; ++k) acc -= A[i][k] * h[k];
+      h[i] = acc / A[i][i];
+    }
+    for (int i = 0; i < 8; ++i) {
+      if (!isfinite(h[i])) return 0;
+      out[i] = h[i];
+    }
+    out[8] = 1.0;
+    return 1;
   }
 };
 

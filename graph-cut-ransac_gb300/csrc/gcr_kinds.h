@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <cstddef>
+#include <cstdint>
 
 namespace gcr {
 
@@ -28,6 +29,7 @@ struct KindOps {
 const KindOps* homography_ops();
 const KindOps* fundamental_ops();
 const KindOps* essential_ops();
+const KindOps* homography_affine_ops();  // affine correspondences (gcr_kind_ha.cu)
 
 struct PairDesc;
 struct PairAux;
@@ -41,6 +43,10 @@ cudaError_t launch_centre(const Workspace& ws, PairAux* aux, int num_pairs, cuda
 // per pair.
 cudaError_t launch_normalise_essential(const double* corr, const double* kinv, const PairDesc* pairs, int num_pairs,
                                        double* out, cudaStream_t stream);
+
+// Affine correspondences: rows of 8 doubles into the point rows pts [total][4]
+// and the local affine maps aff [total][4].
+cudaError_t launch_split_affine(const double* corr8, int64_t total, double* pts, double* aff, cudaStream_t stream);
 
 // Cumulative normalised probabilities of the importance sampler, one table per
 // pair laid out like the correspondences.

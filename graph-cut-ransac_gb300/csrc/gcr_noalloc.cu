@@ -204,7 +204,9 @@ extern "C" gcr_status gcr_find_homography_device_noalloc(const double* d_corr, i
   prm.epilogue = 1;
   prm.batch_calls = GCR_BLOCK;
   prm.lo_fp32 = 0;
-  prm.sprt_min_ratio = p.min_inlier_ratio_for_sprt;
+  // the homography driver's SPRT starts from the inlier ratio 0.01 whatever
+  // min_inlier_ratio_for_sprt holds (gcransac_python.cpp:4394-4396)
+  prm.sprt_min_ratio = 0.01;
 
   single_pair_kernel<<<1, GCR_BLOCK, gcr::shared_bytes<Est>(), (cudaStream_t)stream>>>(ws, prm, pd, slot);
   e = cudaGetLastError();

@@ -54,9 +54,11 @@ def _params(kind, threshold, conf, spatial_coherence_weight, max_iters, min_iter
     return p
 
 
-def _check_corr(correspondences, m, what):
+def _check_corr(correspondences, m, what, cols=4):
     c = np.ascontiguousarray(correspondences, dtype=np.float64)
-    if c.ndim != 2 or c.shape[1] != 4:
+    if c.ndim != 2 or c.shape[1] != cols:
+        if cols == 8:
+            raise ValueError(f"SIFT or affine correspondences should be an array with dims [n,8], n>={m}")
         raise ValueError(f"correspondences should be an array with dims [n,4], n>={m}")
     if c.shape[0] < m:
         raise ValueError(f"correspondences should be an array with dims [n,d], n>={m}")
@@ -116,7 +118,10 @@ class _SampleTape:
         return False
 
 
-_SAMPLE_SIZE = {_abi.GCR_HOMOGRAPHY: 4, _abi.GCR_FUNDAMENTAL: 7, _abi.GCR_ESSENTIAL: 5}
+_SAMPLE_SIZE = {_abi.GCR_HOMOGRAPHY: 4, _abi.GCR_FUNDAMENTAL: 7, _abi.GCR_ESSENTIAL: 5,
+                _abi.GCR_HOMOGRAPHY_AFFINE: 2}
+_ENTRY_NAME = {_abi.GCR_HOMOGRAPHY: "findHomography", _abi.GCR_FUNDAMENTAL: "findFundamentalMatrix",
+               _abi.GCR_ESSENTIAL: "findEssentialMatrix", _abi.GCR_HOMOGRAPHY_AFFINE: "findHomography"}
 
 
 def _run_one(kind, corr, size, params, K1=None, K2=None, return_stats=False, probabilities=None, sample_tape=None):
@@ -136,6 +141,9 @@ def _run_one_(kind, corr, size, params, K1=None, K2=None, return_stats=False, pr
     if kind == _abi.GCR_HOMOGRAPHY:
         rc = lib.gcr_find_homography(_abi.ptr(corr), n, ctypes.byref(sz), _abi.ptr(prob), ctypes.byref(params),
                                      _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
+    elif kind == _abi.GCR_HOMOGRAPHY_AFFINE:
+        rc = lib.gcr_find_homography_affine(_abi.ptr(corr), n, ctypes.byref(sz), _abi.ptr(prob),
+                                            ctypes.byref(params), _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
     elif kind == _abi.GCR_FUNDAMENTAL:
         rc = lib.gcr_find_fundamental(_abi.ptr(corr), n, ctypes.byref(sz), _abi.ptr(prob), ctypes.byref(params),
                                       _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
@@ -144,7 +152,7 @@ def _run_one_(kind, corr, size, params, K1=None, K2=None, return_stats=False, pr
         K2 = np.ascontiguousarray(K2, np.float64).reshape(9)
         rc = lib.gcr_find_essential(_abi.ptr(corr), n, _abi.ptr(K1), _abi.ptr(K2), ctypes.byref(sz), _abi.ptr(prob),
                                     ctypes.byref(params), _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
-    _raise_for(rc, ["findHomography", "findFundamentalMatrix", "findEssentialMatrix"][kind])
+    _raise_for(rc, _ENTRY_NAME[kind])
     maskb = mask.astype(bool)
     out = (None if rc == _abi.GCR_NO_MODEL or maskb.sum() == 0 else model.reshape(3, 3), maskb)
     return out + (st,) if return_stats else out
@@ -156,10 +164,21 @@ def findHomography(correspondences, h1, w1, h2, w2, probabilities=None, threshol
                    use_space_partitioning=True, lo_number=50, sampler_variance=0.1, solver=0, seed=0,
                    return_stats=False, sample_tape=None):
     """Robust homography by Graph-Cut RANSAC (reference: bindings.cpp:859-983).
-    `sample_tape` [calls, 4] replays recorded minimal samples in place of the
-    main sampler's draws (gcr_set_sample_tape)."""
+    solver 0: point correspondences [n, 4]; solver 2: affine correspondences
+    [n, 8] (x1, y1, x2, y2, a11, a12, a21, a22), two per minimal sample
+    (findHomographyAC_, gcransac_python.cpp:4553-4811; its driver takes
+    samplers 0, 1, 3, 4 and no space partitioning). `sample_tape` [calls, m]
+    replays recorded minimal samples in place of the main sampler's draws
+    (gcr_set_sample_tape)."""
+    if solver == 2:
+        c = _check_corr(correspondences, 4, "homography", cols=8)
+        p = _params(_abi.GCR_HOMOGRAPHY_AFFINE, threshold, conf, spatial_coherence_weight, max_iters, min_iters,
+                    use_sprt, sampler, neighborhood, neighborhood_size, lo_number, False, seed,
+                    min_inlier_ratio_for_sprt=min_inlier_ratio_for_sprt, sampler_variance=sampler_variance)
+        return _run_one(_abi.GCR_HOMOGRAPHY_AFFINE, c, (h1, w1, h2, w2), p, return_stats=return_stats,
+                        probabilities=probabilities, sample_tape=sample_tape)
     if solver != 0:
-        raise NotImplementedError("only point correspondences (solver=0) are provided")
+        raise NotImplementedError("SIFT correspondences (solver=1) are not provided; solver 0 and 2 are")
     c = _check_corr(correspondences, 4, "homography")
     p = _params(_abi.GCR_HOMOGRAPHY, threshold, conf, spatial_coherence_weight, max_iters, min_iters, use_sprt,
                 sampler, neighborhood, neighborhood_size, lo_number, use_space_partitioning, seed,
@@ -205,7 +224,8 @@ def findEssentialMatrix(correspondences, K1, K2, h1, w1, h2, w2, probabilities=N
 def find_batch(kind, correspondences, sizes, params, seeds=None, K=None, sample_tape=None):
     """Many pairs of one model kind in one device launch (host buffers).
 
-    correspondences: list of [n_i, 4] arrays or (concatenated [sum n_i, 4], offsets [P+1]).
+    correspondences: list of [n_i, 4] arrays (rows of 8 for GCR_HOMOGRAPHY_AFFINE) or (concatenated
+    [sum n_i, 4 or 8], offsets [P+1]).
     sizes: [P, 4] (h1, w1, h2, w2); params: an _abi.Params; K: [P, 18] for essential matrices.
     sample_tape: [P, calls, m] recorded minimal samples replacing the main sampler's draws.
     Returns (models [P, 3, 3], masks list of bool arrays, stats structured array).

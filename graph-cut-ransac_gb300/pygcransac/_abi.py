@@ -41,6 +41,7 @@ GCR_LO_FP32 = 1
 GCR_HOMOGRAPHY = 0
 GCR_FUNDAMENTAL = 1
 GCR_ESSENTIAL = 2
+GCR_HOMOGRAPHY_AFFINE = 3  # rows of 8: points, then the local affine map
 
 GCR_FLAG_LO_APPLIED = 1
 GCR_FLAG_IRLS_APPLIED = 2
@@ -107,6 +108,7 @@ _EXPORTS = {
     "gcr_find_homography": (ctypes.c_int, [_P, ctypes.c_int64, _P, _P, _P, _P, _P, _P]),
     "gcr_find_fundamental": (ctypes.c_int, [_P, ctypes.c_int64, _P, _P, _P, _P, _P, _P]),
     "gcr_find_essential": (ctypes.c_int, [_P, ctypes.c_int64, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "gcr_find_homography_affine": (ctypes.c_int, [_P, ctypes.c_int64, _P, _P, _P, _P, _P, _P]),
     "gcr_find_batch": (ctypes.c_int, [ctypes.c_int, ctypes.c_int64, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "gcr_context_create": (ctypes.c_int, [_P]),
     "gcr_context_destroy": (ctypes.c_int, [_P]),

@@ -77,6 +77,39 @@ def homography_pair(seed, n=2000, inlier_ratio=0.4, sigma=1.0, w=W, h=H):
     return dict(corr=corr[perm], H_gt=Hm, inlier_gt=gt[perm], size=(h, w, h, w))
 
 
+def homography_jacobian(Hm, x):
+    """[n, 4] row-major 2x2 Jacobians (a11, a12, a21, a22) of x -> H x at the
+    points x [n, 2]: the local affine map of an affine correspondence."""
+    X = np.c_[x, np.ones(len(x))] @ Hm.T
+    s = X[:, 2]
+    u, v = X[:, 0] / s, X[:, 1] / s
+    a11 = (Hm[0, 0] - u * Hm[2, 0]) / s
+    a12 = (Hm[0, 1] - u * Hm[2, 1]) / s
+    a21 = (Hm[1, 0] - v * Hm[2, 0]) / s
+    a22 = (Hm[1, 1] - v * Hm[2, 1]) / s
+    return np.c_[a11, a12, a21, a22]
+
+
+def homography_affine_pair(seed, n=2000, inlier_ratio=0.4, sigma=1.0, affine_sigma=0.02, w=W, h=H):
+    """Affine correspondences of a homography: the point pairs of
+    homography_pair and, per row, the local affine map (a11, a12, a21, a22) —
+    the Jacobian of the true homography at x1 plus N(0, affine_sigma) noise
+    for inliers, a random map (rotation by U(-pi, pi), scales U(0.5, 2)) for
+    outliers. Returns dict(corr [n, 8], H_gt, inlier_gt, size)."""
+    pr = homography_pair(seed, n=n, inlier_ratio=inlier_ratio, sigma=sigma, w=w, h=h)
+    rng = _rng(seed + 7919)
+    corr = pr["corr"]
+    A = homography_jacobian(pr["H_gt"], corr[:, :2]) + rng.normal(0, affine_sigma, size=(n, 4))
+    out = ~pr["inlier_gt"]
+    k = int(out.sum())
+    ang = rng.uniform(-np.pi, np.pi, k)
+    sc = rng.uniform(0.5, 2.0, (k, 2))
+    c, si = np.cos(ang), np.sin(ang)
+    A[out] = np.c_[c * sc[:, 0], -si * sc[:, 1], si * sc[:, 0], c * sc[:, 1]]
+    return dict(corr=np.ascontiguousarray(np.c_[corr, A]), H_gt=pr["H_gt"], inlier_gt=pr["inlier_gt"],
+                size=pr["size"])
+
+
 def intrinsics(f=800.0, w=W, h=H):
     return np.array([[f, 0, w / 2], [0, f, h / 2], [0, 0, 1.0]])
 

@@ -43,10 +43,16 @@ typedef enum gcr_status {
   GCR_UNSUPPORTED = 7      /* option combination not provided by this build */
 } gcr_status;
 
+/* Correspondence rows hold 4 doubles (x1, y1, x2, y2) for the point kinds and
+ * 8 for GCR_HOMOGRAPHY_AFFINE: the point pair followed by the 2x2 local affine
+ * map (a11, a12, a21, a22) of the affine correspondence, the layout of the
+ * reference's findHomographyAC_ (gcransac_python.cpp:4553, solver = 2 of the
+ * python findHomography). */
 typedef enum gcr_model_kind {
   GCR_HOMOGRAPHY = 0,
   GCR_FUNDAMENTAL = 1,
-  GCR_ESSENTIAL = 2
+  GCR_ESSENTIAL = 2,
+  GCR_HOMOGRAPHY_AFFINE = 3
 } gcr_model_kind;
 
 /* Sampler ids follow examples/gcransac_parameter_types.py:8-12 of the reference. */
@@ -79,7 +85,9 @@ typedef struct gcr_params {
   int32_t use_sprt;                /* SPRT preemptive verification of main-loop models */
   int32_t use_space_partitioning;  /* homographies: space-partitioning pre-selection of models */
   uint64_t seed;                   /* seed of the counter-based sampler streams */
-  double min_inlier_ratio_for_sprt; /* SPRT's initial inlier-ratio guess (epsilon) */
+  double min_inlier_ratio_for_sprt; /* SPRT's initial inlier-ratio guess (epsilon); the homography
+                                      drivers start from 0.01 whatever this holds, as the reference's
+                                      findHomography_ / findHomographyAC_ construct their SPRT test */
   double sampler_variance;         /* AR sampler (4): variance of the inlier-probability estimator */
 } gcr_params;
 
@@ -129,8 +137,23 @@ gcr_status gcr_find_essential(const double* corr, int64_t n, const double* K1, c
                               const gcr_params* params, double* model_out9, uint8_t* mask_out,
                               gcr_stats* stats_out);
 
+/* Affine-correspondence homography on one image pair (findHomographyAC_,
+ * gcransac_python.cpp:4553-4811; python findHomography with solver = 2).
+ *   corr  n x 8 row-major doubles (x1, y1, x2, y2, a11, a12, a21, a22); the
+ *         minimal sample is two correspondences: the point rows of both and
+ *         the affine rows of the first (solver_homography_two_affine.h:88-237)
+ * Samplers 0, 1, 3, 4 (the reference's driver refuses P-NAPSAC), MSAC; the
+ * grid is built on the point columns with cells w / n only when the spatial
+ * weight is above machine epsilon; SPRT starts from the inlier ratio 0.01, as
+ * the reference's driver constructs it; no space partitioning. Other
+ * arguments as for gcr_find_homography. */
+gcr_status gcr_find_homography_affine(const double* corr, int64_t n, const gcr_image_size* size,
+                                      const double* probabilities, const gcr_params* params,
+                                      double* model_out9, uint8_t* mask_out, gcr_stats* stats_out);
+
 /* Many image pairs of one model kind in one device launch, host buffers.
  *   corr        concatenated correspondences, offsets[num_pairs] rows in total
+ *               (rows of 4 doubles, or of 8 for GCR_HOMOGRAPHY_AFFINE)
  *   offsets     num_pairs + 1 row offsets (ragged pairs)
  *   K           num_pairs * 18 doubles (K1 then K2 per pair) for GCR_ESSENTIAL, else NULL
  *   sizes       num_pairs image sizes

@@ -112,9 +112,15 @@ static int run_generic(const Mat& run_pts, const Mat& pixel_pts, const Est& est,
   return GCR_OK;
 }
 
-static int find_homography(const double* corr, int64_t n, const gcr_image_size& sz, const gcr_params& p,
+// findHomography_ (gcransac_python.cpp:4221-4552). Its SPRT is constructed
+// without the driver's min_inlier_ratio_for_sprt (4394-4396), so the test
+// starts from the constructor's default inlier ratio 0.01
+// (preemption_sprt.h:141-143) whatever the argument holds.
+static int find_homography(const double* corr, int64_t n, const gcr_image_size& sz, const gcr_params& p_in,
                            uint64_t seed, double* model_out, uint8_t* mask, gcr_stats* st) {
   if (n < 4) return GCR_TOO_FEW_POINTS;
+  gcr_params p = p_in;
+  p.min_inlier_ratio_for_sprt = 0.01;
   const Mat pts{corr, n, 4};
   // the homography driver keeps the grid under space partitioning
   // (gcransac_python.cpp:4282-4286)
@@ -131,6 +137,43 @@ static int find_homography(const double* corr, int64_t n, const gcr_image_size& 
   else
     rc = run_generic<HomographyEstimator, MSACScoring>(pts, pts, est, p, sz, seed, grid.get(), p.threshold,
                                                        model, inl, st, p.threshold);
+  std::memset(mask, 0, (size_t)n);
+  for (size_t i : inl) mask[i] = 1;
+  if (st) st->inlier_number = (int64_t)inl.size();
+  if (rc == GCR_OK) std::memcpy(model_out, model.data(), 9 * sizeof(double));
+  else std::memset(model_out, 0, 9 * sizeof(double));
+  return rc;
+}
+
+// findHomographyAC_ (gcransac_python.cpp:4553-4811): rows of eight values
+// (points and local affine maps). The neighbourhood is built on the point
+// columns only when the spatial weight is above machine epsilon, with cells
+// w / n (no padding), or as the radius graph; samplers 0, 1, 3 and 4 (the
+// driver refuses P-NAPSAC); MSAC; SPRT from the default inlier ratio 0.01
+// (4719-4721); no space partitioning and no epilogue.
+static int find_homography_affine(const double* corr, int64_t n, const gcr_image_size& sz, const gcr_params& p_in,
+                                  uint64_t seed, double* model_out, uint8_t* mask, gcr_stats* st) {
+  if (n < 2) return GCR_TOO_FEW_POINTS;
+  if (p_in.sampler == GCR_SAMPLER_PNAPSAC || p_in.scoring != GCR_SCORING_MSAC) return GCR_UNSUPPORTED;
+  gcr_params p = p_in;
+  p.min_inlier_ratio_for_sprt = 0.01;
+  p.use_space_partitioning = 0;
+  const Mat pts{corr, n, 8};
+  std::unique_ptr<Grid> grid;
+  if (p.spatial_coherence_weight > std::numeric_limits<double>::epsilon()) {
+    if (p.neighborhood == GCR_NEIGHBORHOOD_FLANN) {
+      grid = std::make_unique<Grid>(Grid::radius_graph(pts, p.neighborhood_size));
+    } else {
+      const size_t nd = (size_t)p.neighborhood_size;
+      const double cs[4] = {sz.w1 / (double)nd, sz.h1 / (double)nd, sz.w2 / (double)nd, sz.h2 / (double)nd};
+      grid = std::make_unique<Grid>(pts, cs, nd);
+    }
+  }
+  HomographyAffineEstimator est;
+  Model model{};
+  std::vector<size_t> inl;
+  const int rc = run_generic<HomographyAffineEstimator, MSACScoring>(pts, pts, est, p, sz, seed, grid.get(),
+                                                                     p.threshold, model, inl, st, p.threshold);
   std::memset(mask, 0, (size_t)n);
   for (size_t i : inl) mask[i] = 1;
   if (st) st->inlier_number = (int64_t)inl.size();
@@ -293,6 +336,18 @@ static int find_essential(const double* corr, int64_t n, const double* K1, const
   return rc;
 }
 
+// Values per correspondence row and minimal sample size of a model kind.
+static int kind_columns(int kind) { return kind == GCR_HOMOGRAPHY_AFFINE ? 8 : 4; }
+static int kind_sample_size(int kind) {
+  switch (kind) {
+    case GCR_HOMOGRAPHY: return 4;
+    case GCR_FUNDAMENTAL: return 7;
+    case GCR_ESSENTIAL: return 5;
+    case GCR_HOMOGRAPHY_AFFINE: return 2;
+    default: return 0;
+  }
+}
+
 // One driver call; `tape` (or NULL) holds this pair's rows of the sample tape.
 static int find_pair(int kind, const double* corr, int64_t n, const double* K1, const double* K2,
                      const gcr_image_size* sz, const gcr_params* p, uint64_t seed, double* model_out,
@@ -306,6 +361,9 @@ static int find_pair(int kind, const double* corr, int64_t n, const double* K1, 
     case GCR_HOMOGRAPHY: rc = find_homography(corr, n, *sz, *p, seed, model_out, mask_out, s); break;
     case GCR_FUNDAMENTAL: rc = find_fundamental(corr, n, *sz, *p, seed, model_out, mask_out, s); break;
     case GCR_ESSENTIAL: rc = find_essential(corr, n, K1, K2, *sz, *p, seed, model_out, mask_out, s); break;
+    case GCR_HOMOGRAPHY_AFFINE:
+      rc = find_homography_affine(corr, n, *sz, *p, seed, model_out, mask_out, s);
+      break;
     default: rc = GCR_INVALID_ARG;
   }
   t_tape = nullptr;
@@ -434,9 +492,9 @@ double oracle_find_batch(int kind, int64_t num_pairs, const double* corr, const 
       if (i >= num_pairs) return;
       const int64_t o = offsets[i], n = offsets[i + 1] - offsets[i];
       const uint64_t seed = seeds ? seeds[i] : p->seed + (uint64_t)i;
-      const int m = kind == GCR_HOMOGRAPHY ? 4 : (kind == GCR_FUNDAMENTAL ? 7 : 5);
+      const int m = kind_sample_size(kind);
       const int32_t* tape = g_tape ? g_tape + (size_t)i * (size_t)g_tape_calls * m : nullptr;
-      find_pair(kind, corr + o * 4, n, K ? K + 18 * i : nullptr, K ? K + 18 * i + 9 : nullptr, &sizes[i], p,
+      find_pair(kind, corr + o * kind_columns(kind), n, K ? K + 18 * i : nullptr, K ? K + 18 * i + 9 : nullptr, &sizes[i], p,
                 seed, models_out + 9 * i, masks_out + o, stats_out ? stats_out + i : nullptr, tape);
     }
   };

@@ -153,3 +153,111 @@ struct HomographyEstimator {
 };
 
 }  // namespace oracle
+
+namespace oracle {
+
+// Affine-correspondence homography estimator (test infrastructure only),
+// restated from src/pygcransac/include/estimators/homography_affine_correspondence_estimator.h:58-403
+// (RobustHomographyAffineCorrespondenceEstimator) with the minimal solver of
+// solver_homography_two_affine.h:88-237. Rows hold eight values: the point
+// pair (x1, y1, x2, y2) and the 2x2 local affine map (a11, a12, a21, a22);
+// residuals, the non-minimal fit (four-point solver on the point columns) and
+// the model check are the point estimator's.
+struct HomographyAffineEstimator : HomographyEstimator {
+  static constexpr size_t sample_size() { return 2; }
+  static constexpr bool space_partitioning = false;
+  size_t sample_size_rt() const { return 2; }
+  size_t inlier_limit() const { return 7 * sample_size(); }
+
+  // The 8 x 9 system of the minimal case: the two point rows of both
+  // correspondences and the four affine rows of the first (the reference
+  // stops after the second one's point rows). Its null vector with h33 = 1 is
+  // the model the reference's SVD returns after dividing by h33; here it is
+  // solved by Gaussian elimination with partial pivoting on the first eight
+  // columns.
+  static bool minimal_affine(const double* a, const double* b, Model& out) {
+    double A[8][9];
+    auto point_rows = [](double (*r)[9], const double* p) {
+      const double x1 = p[0], y1 = p[1], x2 = p[2], y2 = p[3];
+      const double r0[9] = {-x1, -y1, -1.0, 0.0, 0.0, 0.0, x2 * x1, x2 * y1, x2};
+      const double r1[9] = {0.0, 0.0, 0.0, -x1, -y1, -1.0, y2 * x1, y2 * y1, y2};
+      for (int k = 0; k < 9; ++k) {
+        r[0][k] = r0[k];
+        r[1][k] = r1[k];
+      }
+    };
+    point_rows(A, a);
+    {
+      const double x1 = a[0], y1 = a[1], x2 = a[2], y2 = a[3];
+      const double a11 = a[4], a12 = a[5], a21 = a[6], a22 = a[7];
+      const double r2[9] = {-1.0, 0.0, 0.0, 0.0, 0.0, 0.0, x2 + a11 * x1, a11 * y1, a11};
+      const double r3[9] = {0.0, -1.0, 0.0, 0.0, 0.0, 0.0, a12 * x1, x2 + a12 * y1, a12};
+      const double r4[9] = {0.0, 0.0, 0.0, -1.0, 0.0, 0.0, y2 + a21 * x1, a21 * y1, a21};
+      const double r5[9] = {0.0, 0.0, 0.0, 0.0, -1.0, 0.0, a22 * x1, y2 + a22 * y1, a22};
+      for (int k = 0; k < 9; ++k) {
+        A[2][k] = r2[k];
+        A[3][k] = r3[k];
+        A[4][k] = r4[k];
+        A[5][k] = r5[k];
+      }
+    }
+    point_rows(A + 6, b);
+    // A[:, 0:8] h = -A[:, 8]
+    for (int i = 0; i < 8; ++i) A[i][8] = -A[i][8];
+    for (int col = 0; col < 8; ++col) {
+      int piv = col;
+      for (int r = col + 1; r < 8; ++r)
+        if (std::abs(A[r][col]) > std::abs(A[piv][col])) piv = r;
+      if (!(std::abs(A[piv][col]) > 0.0)) return false;
+      if (piv != col)
+        for (int k = 0; k < 9; ++k) std::swap(A[piv][k], A[col][k]);
+      for (int r = col + 1; r < 8; ++r) {
+        const double f = A[r][col] / A[col][col];
+        for (int k = col; k < 9; ++k) A[r][k] -= f * A[col][k];
+      }
+    }
+    double h[8];
+    for (int i = 7; i >= 0; --i) {
+      double s = A[i][8];
+      for (int k = i + 1; k < 8; ++k) s -= A[i][k] * h[k];
+      h[i] = s / A[i][i];
+    }
+    for (int i = 0; i < 8; ++i)
+      if (!std::isfinite(h[i])) return false;
+    out = {h[0], h[1], h[2], h[3], h[4], h[5], h[6], h[7], 1.0};
+    return true;
+  }
+
+  bool estimate_minimal(const Mat& pts, const size_t* s, std::vector<Model>& models) const {
+    Model h;
+    if (!minimal_affine(pts.row(s[0]), pts.row(s[1]), h)) return false;
+    models.push_back(h);
+    return true;
+  }
+
+  // isValidSample (:346-400): the oriented test of the point estimator on the
+  // two points and two points built from the first correspondence's affine
+  // map, c = (1, 0, A (1, 0)^T) and d = (1, 0, A (0, 1)^T).
+  bool is_valid_sample(const Mat& pts, const size_t* s) const {
+    const double *a = pts.row(s[0]), *b = pts.row(s[1]);
+    const double c[4] = {1.0, 0.0, a[4], a[6]};
+    const double d[4] = {1.0, 0.0, a[5], a[7]};
+    auto cross = [](double r[3], const double* u, const double* v) {
+      r[0] = u[1] - v[1];
+      r[1] = v[0] - u[0];
+      r[2] = u[0] * v[1] - u[1] * v[0];
+    };
+    double p[3], q[3];
+    cross(p, a, b);
+    cross(q, a + 2, b + 2);
+    if ((p[0] * c[0] + p[1] * c[1] + p[2]) * (q[0] * c[2] + q[1] * c[3] + q[2]) < 0) return false;
+    if ((p[0] * d[0] + p[1] * d[1] + p[2]) * (q[0] * d[2] + q[1] * d[3] + q[2]) < 0) return false;
+    cross(p, c, d);
+    cross(q, c + 2, d + 2);
+    if ((p[0] * a[0] + p[1] * a[1] + p[2]) * (q[0] * a[2] + q[1] * a[3] + q[2]) < 0) return false;
+    if ((p[0] * b[0] + p[1] * b[1] + p[2]) * (q[0] * b[2] + q[1] * b[3] + q[2]) < 0) return false;
+    return true;
+  }
+};
+
+}  // namespace oracle
