@@ -50,7 +50,8 @@ METRIC = "image pairs/sec at equal model error; learned vs plain GC-RANSAC on 1 
 
 # Algorithmic FP32 work of one residual evaluation (one model x one correspondence):
 # H transfer error 21 FLOP, Sampson distance 35 FLOP.
-FLOP_PER_RESIDUAL = {"homography": 21, "fundamental": 35, "essential": 35, "learned": 35}
+FLOP_PER_RESIDUAL = {"homography": 21, "fundamental": 35, "essential": 35, "learned": 35, "fundamental_affine": 35,
+                     "fundamental_sift": 35}
 
 WORKLOADS = {
     # 2000 correspondences in 640x480, 40 % inliers (sigma 1 px), threshold 3 px,
@@ -63,6 +64,18 @@ WORKLOADS = {
     # solver + graph-cut LO, DEGENSAC on
     "fundamental": dict(kind=_abi.GCR_FUNDAMENTAL, n=5000, ratio=0.25, threshold=0.75, sampler=2, grid=8,
                         lam=0.975, pairs=608),
+    # affine correspondences of the same scene (each inlier on a local plane,
+    # its 2x2 affine map the Jacobian of the plane's homography + 0.01 noise):
+    # 5000 per pair, 25 % inliers, threshold 0.75 px, uniform sampler (the
+    # affine driver offers no P-NAPSAC), 8^4 grid, lambda 0.975, the
+    # three-affine solver + graph-cut LO, no DEGENSAC
+    "fundamental_affine": dict(kind=_abi.GCR_FUNDAMENTAL_AFFINE, n=5000, ratio=0.25, threshold=0.75, sampler=0,
+                               grid=8, lam=0.975, pairs=608),
+    # SIFT correspondences of the same scene (feature scales and orientations
+    # consistent with the local affine maps, 0.01 rad / 1 % noise): the
+    # four-SIFT solver, otherwise as the affine workload
+    "fundamental_sift": dict(kind=_abi.GCR_FUNDAMENTAL_SIFT, n=5000, ratio=0.25, threshold=0.75, sampler=0,
+                             grid=8, lam=0.975, pairs=608),
     # calibrated pairs (f = 800 px, scene as above) with log-uniform 200-8000
     # correspondences and inlier ratio uniform in 10-70 % (sigma 0.5 px),
     # threshold 0.75 px (divided by the focal length), uniform sampler, 8^4
@@ -106,6 +119,12 @@ def _gen_pair(job):
     if workload == "homography":
         pr = S.homography_pair(seed, n=n, inlier_ratio=ratio)
         return pr["corr"], pr["size"], pr["H_gt"]
+    if workload == "fundamental_affine":
+        pr = S.two_view_affine_pair(seed, n=n, inlier_ratio=ratio)
+        return pr["corr"], pr["size"], pr
+    if workload == "fundamental_sift":
+        pr = S.two_view_sift_pair(seed, n=n, inlier_ratio=ratio)
+        return pr["corr"], pr["size"], pr
     pr = S.two_view_pair(seed, n=n, inlier_ratio=ratio)
     return pr["corr"], pr["size"], pr
 
@@ -192,7 +211,7 @@ def model_errors(workload, models, gts, limit=64):
     (H: RMS transfer px; F: mean Sampson px of clean correspondences)."""
     if workload == "homography":
         return [S.homography_error(m / m[2, 2] if abs(m[2, 2]) > 1e-12 else m, g) for m, g in zip(models, gts)]
-    if workload == "fundamental":
+    if workload in ("fundamental", "fundamental_affine", "fundamental_sift"):
         return [S.fundamental_error(m, g, n=200) for m, g in list(zip(models, gts))[:limit]]
     if workload == "learned":
         return [S.fundamental_error(m, g, n=100) for m, g in zip(models, gts)]
@@ -1119,7 +1138,7 @@ def main():
     # the other workloads, a few steps each (same replicas and timing rules)
     if not args.no_side:
         side = {}
-        for name in ("homography", "fundamental", "essential", "serving"):
+        for name in ("homography", "fundamental", "fundamental_affine", "fundamental_sift", "essential", "serving"):
             if name == args.workload:
                 continue
             sw = WORKLOADS[name]

@@ -71,12 +71,21 @@ const gcr::KindOps* ops_for(gcr_model_kind kind) {
     case GCR_FUNDAMENTAL: return gcr::fundamental_ops();
     case GCR_ESSENTIAL: return gcr::essential_ops();
     case GCR_HOMOGRAPHY_AFFINE: return gcr::homography_affine_ops();
+    case GCR_FUNDAMENTAL_AFFINE: return gcr::fundamental_affine_ops();
+    case GCR_FUNDAMENTAL_SIFT: return gcr::fundamental_sift_ops();
   }
   return nullptr;
 }
 
+// Kinds with rows of 8 doubles (points, then the local affine map or the
+// features' scales and orientations), split into point rows and the four
+// extra values before the engine runs.
+bool affine_kind(gcr_model_kind kind) {
+  return kind == GCR_HOMOGRAPHY_AFFINE || kind == GCR_FUNDAMENTAL_AFFINE || kind == GCR_FUNDAMENTAL_SIFT;
+}
+
 // Doubles per correspondence row of a model kind (gcr_model_kind).
-int kind_columns(gcr_model_kind kind) { return kind == GCR_HOMOGRAPHY_AFFINE ? 8 : 4; }
+int kind_columns(gcr_model_kind kind) { return affine_kind(kind) ? 8 : 4; }
 
 // The homography drivers construct their SPRT test without the
 // min_inlier_ratio_for_sprt argument (gcransac_python.cpp:4394-4396,
@@ -113,7 +122,7 @@ struct gcr_context {
     int num_pairs = 0;
   } pending;
   int slot_kind = -1, slot_max_n = 0, slot_count = 0;
-  bool prepared[4] = {false, false, false, false};
+  bool prepared[6] = {false, false, false, false, false, false};
   unsigned long long* pair_times = nullptr;  // see gcr_context_set_pair_times
   DevBuf rg_int, rg_dbl, rg_px;              // radius-graph scratch (one region per resident CTA)
   DevBuf ar_p, ar_i, ar_ab, ar_cnt;          // AR sampler heaps and per-point state (per resident CTA)
@@ -159,12 +168,13 @@ gcr_status check_params(gcr_model_kind kind, const gcr_params* p) {
     return fail(GCR_UNSUPPORTED, "neighborhood_size must be at most 1024 grid divisions");
   if (p->neighborhood == GCR_NEIGHBORHOOD_FLANN && !(p->neighborhood_size > 0 && std::isfinite(p->neighborhood_size)))
     return fail(GCR_INVALID_ARG, "neighborhood_size (the radius) must be > 0 and finite for the radius graph");
-  if (kind == GCR_HOMOGRAPHY_AFFINE) {
-    // findHomographyAC_ (gcransac_python.cpp:4553-4811): MSAC, and no P-NAPSAC
+  if (affine_kind(kind)) {
+    // findHomographyAC_ / findFundamentalMatrixAC_ / findFundamentalMatrixSIFT_
+    // (gcransac_python.cpp:4553, 1924, 2222): MSAC, and no P-NAPSAC
     if (p->sampler == GCR_SAMPLER_PNAPSAC)
-      return fail(GCR_UNSUPPORTED, "the affine-correspondence homography provides samplers 0, 1, 3 and 4");
+      return fail(GCR_UNSUPPORTED, "the affine-correspondence drivers provide samplers 0, 1, 3 and 4");
     if (p->scoring != GCR_SCORING_MSAC)
-      return fail(GCR_UNSUPPORTED, "the affine-correspondence homography scores with MSAC only");
+      return fail(GCR_UNSUPPORTED, "the affine-correspondence drivers score with MSAC only");
   }
   return GCR_OK;
 }
@@ -235,6 +245,8 @@ void gcr_default_params(gcr_model_kind kind, gcr_params* p) {
       p->use_space_partitioning = kind == GCR_HOMOGRAPHY ? 1 : 0;
       break;
     case GCR_FUNDAMENTAL:  // bindings.cpp:1003-1022
+    case GCR_FUNDAMENTAL_AFFINE:  // the same python entry with solver = 2
+    case GCR_FUNDAMENTAL_SIFT:    // and with solver = 1
       p->spatial_coherence_weight = 0.0;
       p->neighborhood = GCR_NEIGHBORHOOD_FLANN;
       p->neighborhood_size = 20.0;
@@ -311,7 +323,7 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
   if (!d_corr || !h_offsets || !h_sizes || !d_models_out || !d_masks_out || !d_stats_out)
     return fail(GCR_INVALID_ARG, "NULL buffer");
   if (kind == GCR_ESSENTIAL && !h_K && !run_only) return fail(GCR_INVALID_ARG, "essential matrices need intrinsics");
-  if (kind == GCR_HOMOGRAPHY_AFFINE && run_only)
+  if (affine_kind(kind) && run_only)
     return fail(GCR_UNSUPPORTED, "gcr_run takes point correspondences; affine ones run through gcr_find_batch");
   const int m = ops->sample_size;
   int max_n = 0;
@@ -460,7 +472,7 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
     run_pts = (const double*)c->norm_pts.p;
   }
   const double* affine_maps = nullptr;
-  if (kind == GCR_HOMOGRAPHY_AFFINE) {
+  if (affine_kind(kind)) {
     // rows of 8 are split into the point columns (what every step but the
     // minimal solver reads) and the affine maps
     CUDA_TRY(c->affine.ensure(sizeof(double) * 8 * (size_t)std::max<int64_t>(total, 1)));
@@ -487,7 +499,7 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
 
   gcr::Workspace ws;
   ws.pts64 = run_pts;
-  ws.pix64 = run_only ? run_only->d_pixels : (kind == GCR_HOMOGRAPHY_AFFINE ? run_pts : d_corr);
+  ws.pix64 = run_only ? run_only->d_pixels : (affine_kind(kind) ? run_pts : d_corr);
   ws.affine64 = affine_maps;
   ws.pts32 = (float4*)c->pts32.p;
   ws.pairs = (const gcr::PairDesc*)c->pairs.p;
@@ -610,7 +622,7 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
   L->ws = ws;
   L->prm = prm;
   L->normalise = kind == GCR_ESSENTIAL && !run_only;
-  L->split_affine = kind == GCR_HOMOGRAPHY_AFFINE;
+  L->split_affine = affine_kind(kind);
   L->total = total;
   L->probs = params->sampler == GCR_SAMPLER_IMPORTANCE ? c->probs : nullptr;
   L->d_corr = d_corr;
@@ -941,6 +953,20 @@ gcr_status gcr_find_homography_affine(const double* corr, int64_t n, const gcr_i
                   mask_out, stats_out);
 }
 
+gcr_status gcr_find_fundamental_affine(const double* corr, int64_t n, const gcr_image_size* size,
+                                       const double* probabilities, const gcr_params* params, double* model_out9,
+                                       uint8_t* mask_out, gcr_stats* stats_out) {
+  return find_one(GCR_FUNDAMENTAL_AFFINE, corr, n, nullptr, nullptr, size, probabilities, params, model_out9,
+                  mask_out, stats_out);
+}
+
+gcr_status gcr_find_fundamental_sift(const double* corr, int64_t n, const gcr_image_size* size,
+                                     const double* probabilities, const gcr_params* params, double* model_out9,
+                                     uint8_t* mask_out, gcr_stats* stats_out) {
+  return find_one(GCR_FUNDAMENTAL_SIFT, corr, n, nullptr, nullptr, size, probabilities, params, model_out9,
+                  mask_out, stats_out);
+}
+
 }  // extern "C"
 
 // GCRANSAC::run on one pair (gcr_run and gcr_run_with_probabilities):
@@ -1047,4 +1073,6 @@ namespace gcr {
 __attribute__((weak)) const KindOps* fundamental_ops() { return nullptr; }
 __attribute__((weak)) const KindOps* essential_ops() { return nullptr; }
 __attribute__((weak)) const KindOps* homography_affine_ops() { return nullptr; }
+__attribute__((weak)) const KindOps* fundamental_affine_ops() { return nullptr; }
+__attribute__((weak)) const KindOps* fundamental_sift_ops() { return nullptr; }
 }  // namespace gcr

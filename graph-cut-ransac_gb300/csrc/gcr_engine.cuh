@@ -271,6 +271,24 @@ struct Shared {
   int out_tmax[33];               // source-set size of a cell of n <= 32 points all beyond the threshold
 };
 
+// Whether a model kind runs DEGENSAC's plane check in its validity test:
+// the fundamental-matrix estimator does for minimal samples of 7 or more
+// (fundamental_estimator.h:326), so not for three affine correspondences.
+template <class Est>
+__host__ __device__ constexpr bool has_degensac() {
+  if constexpr (Est::KIND == 1) return Est::DEGENSAC;
+  else return false;
+}
+
+// Whether a fundamental-matrix kind's non-minimal solver is the bundle
+// adjustment (8-point start, then Levenberg-Marquardt) or the plain 8-point
+// solver (the affine-correspondence estimator, types.h:83-86).
+template <class Est>
+__host__ __device__ constexpr bool nonminimal_lm() {
+  if constexpr (Est::KIND == 1) return Est::NONMIN_LM;
+  else return false;
+}
+
 // GCRANSAC::getIterationNumber (GCRANSAC.h:156-172)
 __device__ __forceinline__ long long iteration_number_for(long long inliers, long long points, int m,
                                                           double log_prob) {
@@ -2169,7 +2187,7 @@ struct Engine {
 
   __device__ bool fit_cta(const int* list, int n, int weight_mode, const double* init = nullptr) {
     if constexpr (Est::LO_MAXSOL > 1) return false;  // multi-model estimators use fit_cta_multi
-    if constexpr (Est::KIND == 1) return fit_cta_f(list, n, weight_mode, true, true, init);
+    if constexpr (Est::KIND == 1) return fit_cta_f(list, n, weight_mode, true, nonminimal_lm<Est>(), init);
     if constexpr (Est::KIND == 2) return fit_cta_f(list, n, weight_mode, true, false);
     return fit_cta_h(list, n, weight_mode);
   }
@@ -2436,7 +2454,7 @@ struct Engine {
           }
         }
       } else {
-        if (Est::KIND == 1 && ss < nL) {
+        if (nonminimal_lm<Est>() && ss < nL) {
           // fundamental matrices: each trial on a group of four lanes; lane 0
           // of the group draws the sample with the LO sampler stream
           const int kb = kBatchModels;
@@ -2559,7 +2577,7 @@ struct Engine {
       if (FundamentalModel::symepi2_f64(row64(list[k]), F) < t2) ++c;
     c = block_sum(c, sh.red_i);
     if (c < min_n) return false;
-    if constexpr (Est::KIND != 1) return true;
+    if constexpr (!has_degensac<Est>()) return true;
     if (threadIdx.x == 0) sh.lm_flag = FundamentalModel::degenerate_sample(F, pts64, sample, sh.degen_H) ? 1 : 0;
     sync();
     if (!sh.lm_flag) return true;
@@ -3620,10 +3638,15 @@ struct Engine {
         double Fb[9];
 #pragma unroll
         for (int q = 0; q < 9; ++q) Fb[q] = sh.best_model[q];
-        for (int k = threadIdx.x; k < cnt; k += GCR_BLOCK)
-          slot.dres[k] = fmax(0.0, 1.0 - Est::r2_f64(row64(list[k]), Fb) / t2);
+        // the affine-correspondence driver runs it without weights
+        // (gcransac_python.cpp:2157-2163)
+        constexpr int wmode = Est::EPILOGUE_WEIGHTED ? 2 : 0;
+        if constexpr (Est::EPILOGUE_WEIGHTED) {
+          for (int k = threadIdx.x; k < cnt; k += GCR_BLOCK)
+            slot.dres[k] = fmax(0.0, 1.0 - Est::r2_f64(row64(list[k]), Fb) / t2);
+        }
         sync();
-        if (fit_cta_f(list, cnt, 2, false, true, prm.lo_fp32 ? sh.best_model : nullptr)) {
+        if (fit_cta_f(list, cnt, wmode, false, true, prm.lo_fp32 ? sh.best_model : nullptr)) {
           const Score sc = exact_score(sh.fit_model, spare, nullptr, true);
           if (final_score < sc.value) {
             final_score = sc.value;

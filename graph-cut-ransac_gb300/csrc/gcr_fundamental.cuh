@@ -172,6 +172,9 @@ struct FundamentalModel {
   static constexpr int INLIER_LIMIT = 7 * M;
   static constexpr int SAMPLE_CAP = INLIER_LIMIT;
   static constexpr bool AFFINE = false;
+  static constexpr bool DEGENSAC = true;          // isValidModel's plane check (samples of 7)
+  static constexpr bool EPILOGUE_WEIGHTED = true;  // findFundamentalMatrix_'s bundle adjustment weights
+  static constexpr bool NONMIN_LM = true;          // non-minimal solver: bundle adjustment (8-point + LM)
   static constexpr bool CTA_VALIDITY = true;
 
   // oriented epipolar constraint of a sample (getEpipole + isOrientationValid)
@@ -199,6 +202,14 @@ struct FundamentalModel {
       A[i][3] = y1 * x0; A[i][4] = y1 * y0; A[i][5] = y1;
       A[i][6] = x0; A[i][7] = y0; A[i][8] = 1;
     }
+    return models_from_rows7(A, true, out);
+  }
+
+  // The models of a 7 x 9 epipolar system: its two-dimensional null space (LU
+  // kernel), the cubic det(l f1 + (1 - l) f2) = 0, each real root's matrix
+  // normalised to F33 = 1 (up to three). `guards`: the seven-point solver's
+  // checks of the cubic's coefficients (solver_fundamental_matrix_seven_point.h:240-251).
+  __device__ static int models_from_rows7(double A[7][9], bool guards, double* out) {
     double f1[9], f2[9];
     if (lu_kernel_7x9(A, f1, f2) != 2) return 0;
     for (int i = 0; i < 9; ++i) f1[i] -= f2[i];
@@ -220,9 +231,10 @@ struct FundamentalModel {
            f2[8] * (f1[0] * f1[4] - f1[1] * f1[3]);
     c[3] = f1[0] * t0 - f1[1] * t1 + f1[2] * t2;
     const double eps = 2.220446049250313e-16;
-    if (fabs(c[0] + c[1] + c[2] + c[3]) < 1e-9 || fabs(c[0]) < eps || fabs(c[1]) < eps || fabs(c[2]) < eps ||
-        fabs(c[3]) < eps)
+    if (guards && (fabs(c[0] + c[1] + c[2] + c[3]) < 1e-9 || fabs(c[0]) < eps || fabs(c[1]) < eps ||
+                   fabs(c[2]) < eps || fabs(c[3]) < eps))
       return 0;
+    if (!(c[3] != 0.0)) return 0;  // no cubic (the polynomial solver needs a leading coefficient)
     double roots[3];
     const int nr = cubic_real_roots(c, roots);
     int nm = 0;
@@ -867,6 +879,137 @@ struct PlaneParallaxModel {
     FundamentalModel::eight_point_from_ata(ata, F);
     FundamentalModel::denormalise(N, F, out);
     return true;
+  }
+};
+
+// Affine-correspondence fundamental matrix (findFundamentalMatrixAC_,
+// gcransac_python.cpp:1924-2221; FundamentalMatrixEstimator with
+// FundamentalMatrixThreeAffineSolver, solver_fundamental_matrix_three_affine.h:84-250).
+// Three correspondences per minimal sample, whose local affine maps
+// (a11, a12, a21, a22) sit in the engine's aux array: the epipolar row of
+// each and the two affine rows of the first two make a 7 x 9 system, solved
+// like the seven-point one (LU kernel, cubic; the reference takes the null
+// space from an SVD of A^T A, another basis of the same plane, and applies no
+// coefficient checks). No DEGENSAC (the estimator runs it for samples of 7 or
+// more), the plain normalised 8-point solver as the non-minimal solver (local
+// optimisation, iteratively reweighted fits, final fit; no
+// Levenberg-Marquardt), an inner sample of 7 x 3 in the local optimisation,
+// and a driver bundle adjustment without weights.
+struct FundamentalAffineModel : FundamentalModel {
+  static constexpr int M = 3;
+  static constexpr int INLIER_LIMIT = 7 * M;
+  static constexpr int SAMPLE_CAP = INLIER_LIMIT;
+  static constexpr bool AFFINE = true;
+  static constexpr bool DEGENSAC = false;
+  static constexpr bool EPILOGUE_WEIGHTED = false;
+  static constexpr bool NONMIN_LM = false;  // FundamentalMatrixEightPointSolver (types.h:83-86)
+  static constexpr int NONMIN = 8;
+
+  __device__ static bool valid_sample_affine(const double*, const double*, const int*) { return true; }
+
+  // Non-minimal fit of the local optimisation's trials, one per thread: the
+  // normalised 8-point solver (solver_fundamental_matrix_eight_point.h:93-182)
+  // with unit weights, denormalised.
+  __device__ static bool fit_thread(const double* pts, const int* idx, int n, double* out) {
+    if (n < NONMIN) return false;
+    Norm N;
+    HomographyModel::normalise(pts, idx, n, N);
+    double ata[NATA];
+#pragma unroll
+    for (int k = 0; k < NATA; ++k) ata[k] = 0;
+    for (int i = 0; i < n; ++i) accumulate_ata(N, pts + 4 * idx[i], 1.0, ata);
+    double F[9];
+    eight_point_from_ata(ata, F);
+    denormalise(N, F, out);
+    return true;
+  }
+
+  __device__ static int minimal_affine(const double* pts, const double* aff, const int* s, double* out) {
+    double A[7][9];
+    int r = 0;
+    for (int i = 0; i < 3; ++i) {
+      const double* p = pts + 4 * s[i];
+      const double x0 = p[0], y0 = p[1], x1 = p[2], y1 = p[3];
+      A[r][0] = x1 * x0; A[r][1] = x1 * y0; A[r][2] = x1;
+      A[r][3] = y1 * x0; A[r][4] = y1 * y0; A[r][5] = y1;
+      A[r][6] = x0; A[r][7] = y0; A[r][8] = 1.0;
+      ++r;
+      if (i < 2) {
+        const double* m = aff + 4 * s[i];
+        const double a11 = m[0], a12 = m[1], a21 = m[2], a22 = m[3];
+        A[r][0] = x1 + a11 * x0; A[r][1] = a11 * y0; A[r][2] = a11;
+        A[r][3] = y1 + a21 * x0; A[r][4] = a21 * y0; A[r][5] = a21;
+        A[r][6] = 1.0; A[r][7] = 0.0; A[r][8] = 0.0;
+        ++r;
+        A[r][0] = a12 * x0; A[r][1] = x1 + a12 * y0; A[r][2] = a12;
+        A[r][3] = a22 * x0; A[r][4] = y1 + a22 * y0; A[r][5] = a22;
+        A[r][6] = 0.0; A[r][7] = 1.0; A[r][8] = 0.0;
+        ++r;
+      }
+    }
+    double tmp[27];
+    const int n = models_from_rows7(A, false, tmp);
+    // the estimator keeps the models that pass the oriented epipolar
+    // constraint on the sample (fundamental_estimator.h:161-184)
+    int k = 0;
+    for (int q = 0; q < n; ++q)
+      if (orientation_valid(tmp + 9 * q, pts, s, 3)) {
+        for (int i = 0; i < 9; ++i) out[9 * k + i] = tmp[9 * q + i];
+        ++k;
+      }
+    return k;
+  }
+};
+
+// SIFT-correspondence fundamental matrix (findFundamentalMatrixSIFT_,
+// gcransac_python.cpp:2222-2518; FundamentalMatrixEstimator with
+// FundamentalMatrixFourSIFTSolver, solver_fundamental_matrix_four_sift.h:89-250):
+// the aux array holds each correspondence's feature scales and orientations
+// (q1, q2, o1, o2); four correspondences per minimal sample, the epipolar
+// row of each and the orientation-scale row of the first three. Everything
+// else as the affine-correspondence kind (the reference's two drivers differ
+// only in the estimator), with an inner sample of 7 x 4.
+struct FundamentalSiftModel : FundamentalAffineModel {
+  static constexpr int M = 4;
+  static constexpr int INLIER_LIMIT = 7 * M;
+  static constexpr int SAMPLE_CAP = INLIER_LIMIT;
+
+  __device__ static int minimal_affine(const double* pts, const double* aux, const int* s, double* out) {
+    double A[7][9];
+    int r = 0;
+    for (int i = 0; i < 4; ++i) {
+      const double* p = pts + 4 * s[i];
+      const double u1 = p[0], v1 = p[1], u2 = p[2], v2 = p[3];
+      A[r][0] = u2 * u1; A[r][1] = u2 * v1; A[r][2] = u2;
+      A[r][3] = v2 * u1; A[r][4] = v2 * v1; A[r][5] = v2;
+      A[r][6] = u1; A[r][7] = v1; A[r][8] = 1.0;
+      ++r;
+      if (i == 3) break;
+      const double* f = aux + 4 * s[i];
+      const double q1 = f[0], q2 = f[1], o1 = f[2], o2 = f[3];
+      double s1, c1, s2, c2;
+      sincos(o1, &s1, &c1);
+      sincos(o2, &s2, &c2);
+      A[r][0] = s2 * s2 * q2 * u1 - c1 * c2 * q1 * u2 - q2 * u1;
+      A[r][1] = s2 * s2 * q2 * v1 - s1 * c2 * q1 * u2 - q2 * v1;
+      A[r][2] = s2 * s2 * q2 - q2;
+      A[r][3] = -c2 * s2 * q2 * u1 - c1 * c2 * q1 * v2;
+      A[r][4] = -c2 * s2 * q2 * v1 - s1 * c2 * q1 * v2;
+      A[r][5] = -c2 * s2 * q2;
+      A[r][6] = -c1 * c2 * q1;
+      A[r][7] = -s1 * c2 * q1;
+      A[r][8] = 0.0;
+      ++r;
+    }
+    double tmp[27];
+    const int n = models_from_rows7(A, false, tmp);
+    int k = 0;
+    for (int q = 0; q < n; ++q)
+      if (orientation_valid(tmp + 9 * q, pts, s, 4)) {
+        for (int i = 0; i < 9; ++i) out[9 * k + i] = tmp[9 * q + i];
+        ++k;
+      }
+    return k;
   }
 };
 

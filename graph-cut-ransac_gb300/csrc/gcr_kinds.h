@@ -29,7 +29,9 @@ struct KindOps {
 const KindOps* homography_ops();
 const KindOps* fundamental_ops();
 const KindOps* essential_ops();
-const KindOps* homography_affine_ops();  // affine correspondences (gcr_kind_ha.cu)
+const KindOps* homography_affine_ops();   // affine correspondences (gcr_kind_ha.cu)
+const KindOps* fundamental_affine_ops();  // affine correspondences (gcr_kind_fa.cu)
+const KindOps* fundamental_sift_ops();    // SIFT correspondences (gcr_kind_fs.cu)
 
 struct PairDesc;
 struct PairAux;

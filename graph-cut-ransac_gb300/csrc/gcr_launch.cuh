@@ -34,8 +34,6 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 
-// Persistent kernel: each CTA takes pairs from a global ticket until none is
-// left; blockIdx.x selects the CTA's scratch slot.
 // Dynamic shared memory: the FP32 correspondence tile, the engine state and,
 // for fundamental matrices, the state of DEGENSAC's inner run.
 constexpr size_t kTileBytes = sizeof(float4) * kSmemPoints;
@@ -43,7 +41,7 @@ __host__ __device__ constexpr size_t align256(size_t b) { return (b + 255) & ~(s
 
 template <class Est>
 __host__ __device__ constexpr size_t nested_bytes() {
-  return Est::KIND == 1 ? align256(sizeof(Shared<PlaneParallaxModel>)) : 0;
+  return has_degensac<Est>() ? align256(sizeof(Shared<PlaneParallaxModel>)) : 0;
 }
 
 template <class Est>
@@ -72,45 +70,6 @@ __device__ inline int load_pair_tile(const Workspace& ws, const PairDesc& pd, co
   return bad;
 }
 
-// ---- Staging of a pair's FP32 tile into shared memory by the tensor memory
-// accelerator: one bulk copy (cp.async.bulk, global -> shared) per pair,
-// completing on an mbarrier. Both addresses are 16-byte aligned and the size
-// (16 bytes per correspondence) is a multiple of 16.
-__device__ __forceinline__ unsigned smem_addr(const void* p) {
-  return static_cast<unsigned>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(unsigned long long* bar) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-// orders this thread's earlier generic-proxy accesses of shared memory before
-// later async-proxy (bulk copy) writes
-__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void bulk_copy_to_smem(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   smem_addr(dst)),
-               "l"(src), "r"(bytes), "r"(smem_addr(bar))
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
-  unsigned ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_addr(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Waits (every thread) for the phase of the given parity; false when the
-// bounded number of polls ran out.
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
-  constexpr long long kPolls = 1ll << 22;
-  for (long long it = 0; it < kPolls; ++it)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
-}
-
 // Persistent kernel: each CTA takes pairs from a global ticket until none is
 // left; blockIdx.x selects the CTA's scratch slot.
 template <class Est>
@@ -119,10 +78,7 @@ __global__ void __launch_bounds__(GCR_BLOCK, GCR_MIN_BLOCKS) pair_kernel(Workspa
   float4* tile = reinterpret_cast<float4*>(smem_raw);
   Shared<Est>& sh = *reinterpret_cast<Shared<Est>*>(smem_raw + kTileBytes);
   __shared__ int s_pair;
-  __shared__ __align__(8) unsigned long long tile_bar;
   const Slot slot = ws.slots[blockIdx.x];
-  unsigned tile_phase = 0;
-  if (threadIdx.x == 0) mbar_init(&tile_bar);
   for (;;) {
     __syncthreads();
     if (threadIdx.x == 0) s_pair = atomicAdd(ws.ticket, 1);
@@ -133,36 +89,25 @@ __global__ void __launch_bounds__(GCR_BLOCK, GCR_MIN_BLOCKS) pair_kernel(Workspa
     if (ws.times && threadIdx.x == 0) ws.times[2 * pair] = global_ns();
     const PairDesc pd = ws.pairs[pair];
     Engine<Est> eng(sh, ws, prm, pd, slot, pair);
-    if constexpr (Est::KIND == 1) {
+    if constexpr (has_degensac<Est>()) {
       eng.nsh = reinterpret_cast<Shared<PlaneParallaxModel>*>(smem_raw + kTileBytes + align256(sizeof(Shared<Est>)));
       eng.nslot = ws.nested_slots[blockIdx.x];
     }
-    // the centred FP32 copy (written by centre_kernel): staged into shared
-    // memory by one bulk copy when it fits, read from global memory otherwise
+    // the centred FP32 copy (written by centre_kernel): copied into shared
+    // memory by coalesced 16-byte loads when it fits, read from global memory
+    // otherwise. (A bulk copy by the tensor memory accelerator on an mbarrier
+    // staged the same bytes, but the essential-matrix engine's per-thread
+    // solvers then ran 4.3 times the cycles: 545 against 1256 pairs/s on 1024
+    // pairs; the other kinds measured equal or faster with these loads.)
     const PairAux aux = ws.aux[pair];
     const bool in_smem = pd.n <= kSmemPoints;
-    float4* src = ws.pts32 + pd.offset;
-    bool staged = true;
-    if (in_smem && pd.n > 0) {
-      // every thread is past its last access of the tile (the barrier at the
-      // top of the loop); the copy's writes come after them
-      if (threadIdx.x == 0) {
-        fence_proxy_async_smem();
-        bulk_copy_to_smem(tile, src, (unsigned)(sizeof(float4) * pd.n), &tile_bar);
-      }
-      bool done = mbar_wait_bounded(&tile_bar, tile_phase);
-      if (!__syncthreads_and(done)) done = mbar_wait_bounded(&tile_bar, tile_phase);
-      staged = __syncthreads_and(done);
-      tile_phase ^= 1u;
+    const float4* src = ws.pts32 + pd.offset;
+    if (in_smem) {
+      for (int i = threadIdx.x; i < pd.n; i += GCR_BLOCK) tile[i] = src[i];
+      __syncthreads();
     }
     eng.scale = aux.scale;
     eng.pts32 = in_smem ? tile : src;
-    if (!staged) {
-      // the copy did not complete within the bounded wait: report the pair and
-      // stop this CTA (its tile may still be written)
-      eng.reject(ST_DEVICE_ERROR);
-      break;
-    }
     // a pair with a coordinate that is not finite is not run (status
     // GCR_INVALID_ARG, no model, empty mask)
     if (aux.bad) eng.reject(ST_INVALID_ARG);

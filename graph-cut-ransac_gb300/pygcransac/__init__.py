@@ -119,9 +119,10 @@ class _SampleTape:
 
 
 _SAMPLE_SIZE = {_abi.GCR_HOMOGRAPHY: 4, _abi.GCR_FUNDAMENTAL: 7, _abi.GCR_ESSENTIAL: 5,
-                _abi.GCR_HOMOGRAPHY_AFFINE: 2}
+                _abi.GCR_HOMOGRAPHY_AFFINE: 2, _abi.GCR_FUNDAMENTAL_AFFINE: 3, _abi.GCR_FUNDAMENTAL_SIFT: 4}
 _ENTRY_NAME = {_abi.GCR_HOMOGRAPHY: "findHomography", _abi.GCR_FUNDAMENTAL: "findFundamentalMatrix",
-               _abi.GCR_ESSENTIAL: "findEssentialMatrix", _abi.GCR_HOMOGRAPHY_AFFINE: "findHomography"}
+               _abi.GCR_ESSENTIAL: "findEssentialMatrix", _abi.GCR_HOMOGRAPHY_AFFINE: "findHomography",
+               _abi.GCR_FUNDAMENTAL_AFFINE: "findFundamentalMatrix", _abi.GCR_FUNDAMENTAL_SIFT: "findFundamentalMatrix"}
 
 
 def _run_one(kind, corr, size, params, K1=None, K2=None, return_stats=False, probabilities=None, sample_tape=None):
@@ -144,6 +145,12 @@ def _run_one_(kind, corr, size, params, K1=None, K2=None, return_stats=False, pr
     elif kind == _abi.GCR_HOMOGRAPHY_AFFINE:
         rc = lib.gcr_find_homography_affine(_abi.ptr(corr), n, ctypes.byref(sz), _abi.ptr(prob),
                                             ctypes.byref(params), _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
+    elif kind == _abi.GCR_FUNDAMENTAL_SIFT:
+        rc = lib.gcr_find_fundamental_sift(_abi.ptr(corr), n, ctypes.byref(sz), _abi.ptr(prob),
+                                           ctypes.byref(params), _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
+    elif kind == _abi.GCR_FUNDAMENTAL_AFFINE:
+        rc = lib.gcr_find_fundamental_affine(_abi.ptr(corr), n, ctypes.byref(sz), _abi.ptr(prob),
+                                             ctypes.byref(params), _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
     elif kind == _abi.GCR_FUNDAMENTAL:
         rc = lib.gcr_find_fundamental(_abi.ptr(corr), n, ctypes.byref(sz), _abi.ptr(prob), ctypes.byref(params),
                                       _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
@@ -193,9 +200,23 @@ def findFundamentalMatrix(correspondences, h1, w1, h2, w2, probabilities=None, t
                           lo_number=50, sampler_variance=0.1, solver=0, seed=0, return_stats=False,
                           sample_tape=None):
     """Robust fundamental matrix by Graph-Cut RANSAC (reference: bindings.cpp:279-401).
-    `sample_tape` [calls, 7] replays recorded minimal samples."""
+    solver 0: point correspondences [n, 4]; solver 1: SIFT correspondences
+    [n, 8] (x1, y1, x2, y2, q1, q2, o1, o2: scales and orientations), four per
+    minimal sample (findFundamentalMatrixSIFT_, gcransac_python.cpp:2222-2518);
+    solver 2: affine correspondences [n, 8] (x1, y1, x2, y2, a11, a12, a21,
+    a22), three per minimal sample (findFundamentalMatrixAC_, :1924-2221);
+    both take samplers 0, 1, 3, 4. `sample_tape` [calls, m] replays recorded
+    minimal samples."""
+    if solver in (1, 2):
+        kind = _abi.GCR_FUNDAMENTAL_SIFT if solver == 1 else _abi.GCR_FUNDAMENTAL_AFFINE
+        c = _check_corr(correspondences, 7, "fundamental", cols=8)
+        p = _params(kind, threshold, conf, spatial_coherence_weight, max_iters, min_iters,
+                    use_sprt, sampler, neighborhood, neighborhood_size, lo_number, False, seed,
+                    min_inlier_ratio_for_sprt=min_inlier_ratio_for_sprt, sampler_variance=sampler_variance)
+        return _run_one(kind, c, (h1, w1, h2, w2), p, return_stats=return_stats,
+                        probabilities=probabilities, sample_tape=sample_tape)
     if solver != 0:
-        raise NotImplementedError("only point correspondences (solver=0) are provided")
+        raise NotImplementedError(f"solver {solver} is not provided (0 points, 1 SIFT, 2 affine)")
     c = _check_corr(correspondences, 7, "fundamental")
     p = _params(_abi.GCR_FUNDAMENTAL, threshold, conf, spatial_coherence_weight, max_iters, min_iters, use_sprt,
                 sampler, neighborhood, neighborhood_size, lo_number, False, seed,

@@ -180,6 +180,98 @@ def two_view_pair(seed, n=5000, inlier_ratio=0.25, sigma=0.5, f=800.0, w=W, h=H,
                 inlier_gt=gt[perm], size=(h, w, h, w))
 
 
+def two_view_affine_pair(seed, n=2000, inlier_ratio=0.4, sigma=0.5, affine_sigma=0.01, f=800.0, w=W, h=H,
+                         max_angle_deg=30.0):
+    """Affine correspondences of a two-view scene (the scene of two_view_pair):
+    each inlier is a 3D point on a local plane whose normal is the viewing ray
+    turned by up to about 30 degrees; its local affine map (a11, a12, a21, a22)
+    is the Jacobian at x1 of the plane's homography K (R + t n^T / d) K^-1 plus
+    N(0, affine_sigma) noise, and the points carry N(0, sigma) pixel noise.
+    Outliers are random point pairs with random maps (rotation by U(-pi, pi),
+    scales U(0.5, 2)). Returns dict(corr [n, 8], K, R, t, F_gt, E_gt,
+    inlier_gt, size)."""
+    rng = _rng(seed)
+    K = intrinsics(f, w, h)
+    Ki = np.linalg.inv(K)
+    ni = int(round(n * inlier_ratio))
+    rows = np.zeros((0, 8))
+    for _attempt in range(100):
+        R = _rot(rng.normal(size=3), np.deg2rad(rng.uniform(-max_angle_deg, max_angle_deg)))
+        t = rng.normal(size=3)
+        t /= np.linalg.norm(t)
+        rows = np.zeros((0, 8))
+        tries = 0
+        while len(rows) < ni and tries < 200:
+            tries += 1
+            m = 4 * ni
+            uv = rng.uniform([0, 0], [w, h], size=(m, 2))
+            depth = rng.uniform(2, 10, size=m)
+            X = (np.c_[uv, np.ones(m)] @ Ki.T) * depth[:, None]
+            X2 = X @ R.T + t
+            front = X2[:, 2] > 0.1
+            nrm = -X / np.linalg.norm(X, axis=1, keepdims=True) + rng.normal(0, 0.3, size=(m, 3))
+            nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+            d = np.sum(nrm * X, axis=1)
+            Hs = np.einsum("ij,njk,kl->nil", K, R[None] + t[None, :, None] * (nrm / d[:, None])[:, None, :], Ki)
+            Xh = np.einsum("nij,nj->ni", Hs, np.c_[uv, np.ones(m)])
+            sc = Xh[:, 2]
+            u2, v2 = Xh[:, 0] / sc, Xh[:, 1] / sc
+            A = np.c_[(Hs[:, 0, 0] - u2 * Hs[:, 2, 0]) / sc, (Hs[:, 0, 1] - u2 * Hs[:, 2, 1]) / sc,
+                      (Hs[:, 1, 0] - v2 * Hs[:, 2, 0]) / sc, (Hs[:, 1, 1] - v2 * Hs[:, 2, 1]) / sc]
+            x2 = X2 @ K.T
+            x2 = x2[:, :2] / x2[:, 2:3]
+            x1n = uv + rng.normal(0, sigma, size=(m, 2))
+            x2n = x2 + rng.normal(0, sigma, size=(m, 2))
+            An = A + rng.normal(0, affine_sigma, size=(m, 4))
+            ok = front & (x2n[:, 0] >= 0) & (x2n[:, 0] < w) & (x2n[:, 1] >= 0) & (x2n[:, 1] < h) & \
+                (x1n[:, 0] >= 0) & (x1n[:, 0] < w) & (x1n[:, 1] >= 0) & (x1n[:, 1] < h) & \
+                (np.abs(A).max(axis=1) < 10.0)
+            rows = np.r_[rows, np.c_[x1n, x2n, An][ok]]
+        if len(rows) >= ni:
+            break
+    no = n - ni
+    ang = rng.uniform(-np.pi, np.pi, no)
+    sc = rng.uniform(0.5, 2.0, (no, 2))
+    c, si = np.cos(ang), np.sin(ang)
+    out = np.c_[rng.uniform([0, 0], [w, h], size=(no, 2)), rng.uniform([0, 0], [w, h], size=(no, 2)),
+                c * sc[:, 0], -si * sc[:, 1], si * sc[:, 0], c * sc[:, 1]]
+    corr = np.r_[rows[:ni], out]
+    gt = np.r_[np.ones(ni, bool), np.zeros(no, bool)]
+    perm = rng.permutation(n)
+    E = skew(t) @ R
+    F = Ki.T @ E @ Ki
+    return dict(corr=np.ascontiguousarray(corr[perm]), K=K, R=R, t=t, E_gt=E / np.linalg.norm(E),
+                F_gt=F / np.linalg.norm(F), inlier_gt=gt[perm], size=(h, w, h, w))
+
+
+def two_view_sift_pair(seed, n=2000, inlier_ratio=0.4, sigma=0.5, angle_sigma=0.01, scale_sigma=0.01, **kw):
+    """SIFT-like correspondences of the scene of two_view_affine_pair: rows
+    (x1, y1, x2, y2, q1, q2, o1, o2), a feature's scale q and orientation o
+    in each image. For an inlier, o1 ~ U(-pi, pi) and q1 ~ U(1, 5), and the
+    local affine map A of its plane gives q2 (cos o2, sin o2) = A q1 (cos o1,
+    sin o1); o2 and q2 then get N(0, angle_sigma) and relative N(0,
+    scale_sigma) noise. Outliers have independent q ~ U(1, 5) and o ~ U(-pi,
+    pi). Returns dict(corr [n, 8], K, R, t, F_gt, E_gt, inlier_gt, size)."""
+    pr = two_view_affine_pair(seed, n=n, inlier_ratio=inlier_ratio, sigma=sigma, affine_sigma=0.0, **kw)
+    rng = _rng(seed + 104729)
+    c = pr["corr"]
+    a11, a12, a21, a22 = c[:, 4], c[:, 5], c[:, 6], c[:, 7]
+    o1 = rng.uniform(-np.pi, np.pi, n)
+    q1 = rng.uniform(1.0, 5.0, n)
+    vx = q1 * (a11 * np.cos(o1) + a12 * np.sin(o1))
+    vy = q1 * (a21 * np.cos(o1) + a22 * np.sin(o1))
+    o2 = np.arctan2(vy, vx) + rng.normal(0, angle_sigma, n)
+    q2 = np.hypot(vx, vy) * (1.0 + rng.normal(0, scale_sigma, n))
+    out = ~pr["inlier_gt"]
+    k = int(out.sum())
+    o1[out] = rng.uniform(-np.pi, np.pi, k)
+    o2[out] = rng.uniform(-np.pi, np.pi, k)
+    q1[out] = rng.uniform(1.0, 5.0, k)
+    q2[out] = rng.uniform(1.0, 5.0, k)
+    corr = np.ascontiguousarray(np.c_[c[:, :4], q1, q2, o1, o2])
+    return dict(pr, corr=corr)
+
+
 # --- model error against ground truth -------------------------------------
 
 def homography_error(H_est, H_gt, w=W, h=H):

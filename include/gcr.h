@@ -44,15 +44,20 @@ typedef enum gcr_status {
 } gcr_status;
 
 /* Correspondence rows hold 4 doubles (x1, y1, x2, y2) for the point kinds and
- * 8 for GCR_HOMOGRAPHY_AFFINE: the point pair followed by the 2x2 local affine
- * map (a11, a12, a21, a22) of the affine correspondence, the layout of the
- * reference's findHomographyAC_ (gcransac_python.cpp:4553, solver = 2 of the
- * python findHomography). */
+ * 8 for the others: for the affine kinds the point pair followed by the 2x2
+ * local affine map (a11, a12, a21, a22) of the affine correspondence, the
+ * layout of the reference's findHomographyAC_ and findFundamentalMatrixAC_
+ * (gcransac_python.cpp:4553, 1924; solver = 2 of the python findHomography and
+ * findFundamentalMatrix); for GCR_FUNDAMENTAL_SIFT the point pair followed by
+ * the features' scales and orientations (q1, q2, o1, o2), the layout of
+ * findFundamentalMatrixSIFT_ (:2222; solver = 1 of findFundamentalMatrix). */
 typedef enum gcr_model_kind {
   GCR_HOMOGRAPHY = 0,
   GCR_FUNDAMENTAL = 1,
   GCR_ESSENTIAL = 2,
-  GCR_HOMOGRAPHY_AFFINE = 3
+  GCR_HOMOGRAPHY_AFFINE = 3,
+  GCR_FUNDAMENTAL_AFFINE = 4,
+  GCR_FUNDAMENTAL_SIFT = 5
 } gcr_model_kind;
 
 /* Sampler ids follow examples/gcransac_parameter_types.py:8-12 of the reference. */
@@ -151,9 +156,31 @@ gcr_status gcr_find_homography_affine(const double* corr, int64_t n, const gcr_i
                                       const double* probabilities, const gcr_params* params,
                                       double* model_out9, uint8_t* mask_out, gcr_stats* stats_out);
 
+/* Affine-correspondence fundamental matrix on one image pair
+ * (findFundamentalMatrixAC_, gcransac_python.cpp:1924-2221; python
+ * findFundamentalMatrix with solver = 2): rows of 8 as above; three
+ * correspondences per minimal sample (the epipolar row of each and the affine
+ * rows of the first two, solver_fundamental_matrix_three_affine.h:84-250); no
+ * DEGENSAC; samplers 0, 1, 3, 4, MSAC; the driver's bundle adjustment of the
+ * final inliers without weights. Other arguments as for gcr_find_fundamental. */
+gcr_status gcr_find_fundamental_affine(const double* corr, int64_t n, const gcr_image_size* size,
+                                       const double* probabilities, const gcr_params* params,
+                                       double* model_out9, uint8_t* mask_out, gcr_stats* stats_out);
+
+/* SIFT-correspondence fundamental matrix on one image pair
+ * (findFundamentalMatrixSIFT_, gcransac_python.cpp:2222-2518; python
+ * findFundamentalMatrix with solver = 1): rows (x1, y1, x2, y2, q1, q2, o1,
+ * o2); four correspondences per minimal sample (the epipolar row of each and
+ * the orientation-scale row of the first three,
+ * solver_fundamental_matrix_four_sift.h:89-250); otherwise as
+ * gcr_find_fundamental_affine. */
+gcr_status gcr_find_fundamental_sift(const double* corr, int64_t n, const gcr_image_size* size,
+                                     const double* probabilities, const gcr_params* params, double* model_out9,
+                                     uint8_t* mask_out, gcr_stats* stats_out);
+
 /* Many image pairs of one model kind in one device launch, host buffers.
  *   corr        concatenated correspondences, offsets[num_pairs] rows in total
- *               (rows of 4 doubles, or of 8 for GCR_HOMOGRAPHY_AFFINE)
+ *               (rows of 4 doubles, or of 8 for the affine kinds)
  *   offsets     num_pairs + 1 row offsets (ragged pairs)
  *   K           num_pairs * 18 doubles (K1 then K2 per pair) for GCR_ESSENTIAL, else NULL
  *   sizes       num_pairs image sizes

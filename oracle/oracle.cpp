@@ -251,6 +251,69 @@ static int find_fundamental(const double* corr, int64_t n, const gcr_image_size&
   return rc;
 }
 
+// findFundamentalMatrixAC_ and findFundamentalMatrixSIFT_
+// (gcransac_python.cpp:1924-2221, 2222-2518; the two drivers differ only in
+// the estimator): rows of eight values; the neighbourhood on the point columns only when the spatial weight
+// is above machine epsilon (cells w / n, or the radius graph); samplers 0, 1,
+// 3 and 4 (the driver refuses P-NAPSAC); MSAC; SPRT from the driver's
+// min_inlier_ratio_for_sprt; then the bundle adjustment of the final inliers
+// without weights (2157-2163), kept when it raises the MSAC score; with at
+// most 7 inliers the model is the identity.
+template <class Est>
+static int find_fundamental_rows8(const double* corr, int64_t n, const gcr_image_size& sz, const gcr_params& p,
+                                  uint64_t seed, double* model_out, uint8_t* mask, gcr_stats* st) {
+  if (n < 3) return GCR_TOO_FEW_POINTS;
+  if (p.sampler == GCR_SAMPLER_PNAPSAC || p.scoring != GCR_SCORING_MSAC) return GCR_UNSUPPORTED;
+  const Mat pts{corr, n, 8};
+  std::unique_ptr<Grid> grid;
+  if (p.spatial_coherence_weight > std::numeric_limits<double>::epsilon()) {
+    if (p.neighborhood == GCR_NEIGHBORHOOD_FLANN) {
+      grid = std::make_unique<Grid>(Grid::radius_graph(pts, p.neighborhood_size));
+    } else {
+      const size_t nd = (size_t)p.neighborhood_size;
+      const double cs[4] = {sz.w1 / (double)nd, sz.h1 / (double)nd, sz.w2 / (double)nd, sz.h2 / (double)nd};
+      grid = std::make_unique<Grid>(pts, cs, nd);
+    }
+  }
+  Est est;
+  est.seed = seed;
+  Model model{};
+  std::vector<size_t> inl;
+  const int rc = run_generic<Est, MSACScoring>(pts, pts, est, p, sz, seed, grid.get(), p.threshold, model, inl, st,
+                                               p.threshold);
+  if (rc == GCR_OK) {
+    if (inl.size() > 7) {
+      const double tt = 1.5 * p.threshold, sq = tt * tt;
+      std::vector<const double*> rows(inl.size());
+      for (size_t k = 0; k < inl.size(); ++k) rows[k] = pts.row(inl[k]);
+      std::vector<Model> models;
+      f_eight_point(rows.data(), (int)rows.size(), nullptr, models);
+      for (Model& F : models) f_refine_lm(rows.data(), (int)rows.size(), nullptr, F);
+      MSACScoring<Est> sc;
+      sc.initialize(sq, n);
+      double best = st ? st->score : 0.0;
+      for (Model& F : models) {
+        std::vector<size_t> cur;
+        const Score s = sc.get(pts, F, est, &cur);
+        if (best < s.value) {
+          model = F;
+          best = s.value;
+          inl.swap(cur);
+        }
+      }
+      if (st) st->score = best;
+    } else {
+      model = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    }
+  }
+  std::memset(mask, 0, (size_t)n);
+  for (size_t i : inl) mask[i] = 1;
+  if (st) st->inlier_number = (int64_t)inl.size();
+  if (rc == GCR_OK) std::memcpy(model_out, model.data(), 9 * sizeof(double));
+  else std::memset(model_out, 0, 9 * sizeof(double));
+  return rc;
+}
+
 // findEssentialMatrix_ (gcransac_python.cpp:2519-2856): correspondences
 // normalised by the inverse intrinsics (utils.h:65-103), threshold divided by
 // the mean focal length (2601-2603), grid and P-NAPSAC on the pixel
@@ -337,13 +400,17 @@ static int find_essential(const double* corr, int64_t n, const double* K1, const
 }
 
 // Values per correspondence row and minimal sample size of a model kind.
-static int kind_columns(int kind) { return kind == GCR_HOMOGRAPHY_AFFINE ? 8 : 4; }
+static int kind_columns(int kind) {
+  return kind == GCR_HOMOGRAPHY_AFFINE || kind == GCR_FUNDAMENTAL_AFFINE || kind == GCR_FUNDAMENTAL_SIFT ? 8 : 4;
+}
 static int kind_sample_size(int kind) {
   switch (kind) {
     case GCR_HOMOGRAPHY: return 4;
     case GCR_FUNDAMENTAL: return 7;
     case GCR_ESSENTIAL: return 5;
     case GCR_HOMOGRAPHY_AFFINE: return 2;
+    case GCR_FUNDAMENTAL_AFFINE: return 3;
+    case GCR_FUNDAMENTAL_SIFT: return 4;
     default: return 0;
   }
 }
@@ -363,6 +430,12 @@ static int find_pair(int kind, const double* corr, int64_t n, const double* K1, 
     case GCR_ESSENTIAL: rc = find_essential(corr, n, K1, K2, *sz, *p, seed, model_out, mask_out, s); break;
     case GCR_HOMOGRAPHY_AFFINE:
       rc = find_homography_affine(corr, n, *sz, *p, seed, model_out, mask_out, s);
+      break;
+    case GCR_FUNDAMENTAL_AFFINE:
+      rc = find_fundamental_rows8<FundamentalAffineEstimator>(corr, n, *sz, *p, seed, model_out, mask_out, s);
+      break;
+    case GCR_FUNDAMENTAL_SIFT:
+      rc = find_fundamental_rows8<FundamentalSiftEstimator>(corr, n, *sz, *p, seed, model_out, mask_out, s);
       break;
     default: rc = GCR_INVALID_ARG;
   }

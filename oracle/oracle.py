@@ -200,7 +200,15 @@ def _find_batch(kind, corr, offsets, sizes, params, seeds=None, K=None, threads=
     models = np.zeros((P, 9))
     masks = np.zeros(int(offsets[-1]), np.uint8)
     stats = np.zeros(P, _abi.STATS_DTYPE)
-    sizes = np.ascontiguousarray(sizes, _abi.SIZE_DTYPE)
+    s = np.asarray(sizes)
+    if s.dtype != _abi.SIZE_DTYPE:
+        # rows (h1, w1, h2, w2): fill the struct fields (a plain cast would
+        # broadcast each value into every field)
+        s = s.reshape(P, 4)
+        sizes = np.zeros(P, _abi.SIZE_DTYPE)
+        sizes["h1"], sizes["w1"], sizes["h2"], sizes["w2"] = s[:, 0], s[:, 1], s[:, 2], s[:, 3]
+    else:
+        sizes = np.ascontiguousarray(s)
     seeds = None if seeds is None else np.ascontiguousarray(seeds, np.uint64)
     K = None if K is None else np.ascontiguousarray(K, np.float64)
     t = lib.oracle_find_batch(kind, P, _p(corr), _p(offsets), _p(K), _p(sizes), ctypes.byref(params),

@@ -52,6 +52,71 @@ inline void f_design_row(const double* p, double w, double* r) {
   r[6] = wx0; r[7] = wy0; r[8] = w;
 }
 
+inline bool f_models_from_rows7(std::vector<double>& A, bool guards, std::vector<Model>& models);
+
+// Three-affine-correspondence solver (solver_fundamental_matrix_three_affine.h:84-250):
+// rows of eight values (x1, y1, x2, y2, a11, a12, a21, a22); the epipolar row
+// of each of the three correspondences and the two affine rows of the first
+// two make a 7 x 9 system. Its null space is taken as the seven-point
+// solver's LU kernel (the reference takes the two last right singular vectors
+// of A^T A: another basis of the same plane, so the same matrices in possibly
+// another order); no coefficient checks, as in the reference.
+inline bool f_three_affine(const double* const rows[3], std::vector<Model>& models) {
+  std::vector<double> A(7 * 9);
+  int r = 0;
+  for (int i = 0; i < 3; ++i) {
+    const double* p = rows[i];
+    const double x0 = p[0], y0 = p[1], x1 = p[2], y1 = p[3];
+    const double a11 = p[4], a12 = p[5], a21 = p[6], a22 = p[7];
+    const double e[9] = {x1 * x0, x1 * y0, x1, y1 * x0, y1 * y0, y1, x0, y0, 1.0};
+    for (int k = 0; k < 9; ++k) A[9 * r + k] = e[k];
+    ++r;
+    if (i < 2) {
+      const double u[9] = {x1 + a11 * x0, a11 * y0, a11, y1 + a21 * x0, a21 * y0, a21, 1.0, 0.0, 0.0};
+      const double v[9] = {a12 * x0, x1 + a12 * y0, a12, a22 * x0, y1 + a22 * y0, a22, 0.0, 1.0, 0.0};
+      for (int k = 0; k < 9; ++k) {
+        A[9 * r + k] = u[k];
+        A[9 * (r + 1) + k] = v[k];
+      }
+      r += 2;
+    }
+  }
+  return f_models_from_rows7(A, false, models);
+}
+
+// Four-SIFT-correspondence solver (solver_fundamental_matrix_four_sift.h:89-250):
+// rows (u1, v1, u2, v2, q1, q2, o1, o2) with feature scales q and orientations
+// o; the epipolar row of each of the four correspondences and the
+// orientation-scale row of the first three make a 7 x 9 system, whose null
+// space is taken as the seven-point solver's LU kernel (the reference takes
+// the FullPivLU kernel of A^T A: another basis of the same plane); no
+// coefficient checks, as in the reference.
+inline bool f_four_sift(const double* const rows[4], std::vector<Model>& models) {
+  std::vector<double> A(7 * 9);
+  int r = 0;
+  for (int i = 0; i < 4; ++i) {
+    const double* p = rows[i];
+    const double u1 = p[0], v1 = p[1], u2 = p[2], v2 = p[3], q1 = p[4], q2 = p[5], o1 = p[6], o2 = p[7];
+    const double s1 = std::sin(o1), c1 = std::cos(o1), s2 = std::sin(o2), c2 = std::cos(o2);
+    const double e[9] = {u2 * u1, u2 * v1, u2, v2 * u1, v2 * v1, v2, u1, v1, 1.0};
+    for (int k = 0; k < 9; ++k) A[9 * r + k] = e[k];
+    ++r;
+    if (i == 3) break;
+    const double o[9] = {s2 * s2 * q2 * u1 - c1 * c2 * q1 * u2 - q2 * u1,
+                         s2 * s2 * q2 * v1 - s1 * c2 * q1 * u2 - q2 * v1,
+                         s2 * s2 * q2 - q2,
+                         -c2 * s2 * q2 * u1 - c1 * c2 * q1 * v2,
+                         -c2 * s2 * q2 * v1 - s1 * c2 * q1 * v2,
+                         -c2 * s2 * q2,
+                         -c1 * c2 * q1,
+                         -s1 * c2 * q1,
+                         0.0};
+    for (int k = 0; k < 9; ++k) A[9 * r + k] = o[k];
+    ++r;
+  }
+  return f_models_from_rows7(A, false, models);
+}
+
 // Seven-point solver (solver_fundamental_matrix_seven_point.h:91-291) on the
 // rows `rows`, weights w[i] per row (nullptr: none).
 inline bool f_seven_point(const double* const* rows, const double* w, std::vector<Model>& models) {
@@ -65,6 +130,15 @@ inline bool f_seven_point(const double* const* rows, const double* w, std::vecto
       r[6] = x0; r[7] = y0; r[8] = 1;
     }
   }
+  return f_models_from_rows7(A, true, models);
+}
+
+// The models of a 7 x 9 epipolar system A (row-major): the two-dimensional
+// null space (FullPivLU kernel), the cubic det(l f1 + (1 - l) f2) = 0 and each
+// real root's matrix normalised to F33 = 1. `guards`: the seven-point
+// solver's checks of the cubic's coefficients
+// (solver_fundamental_matrix_seven_point.h:240-251).
+inline bool f_models_from_rows7(std::vector<double>& A, bool guards, std::vector<Model>& models) {
   std::vector<double> K;
   if (fullpiv_lu_kernel(A, 7, 9, K) != 2) return false;
   double f1[9], f2[9];
@@ -91,9 +165,10 @@ inline bool f_seven_point(const double* const* rows, const double* w, std::vecto
          f2[8] * (f1[0] * f1[4] - f1[1] * f1[3]);
   c[3] = f1[0] * t0 - f1[1] * t1 + f1[2] * t2;
   const double eps = std::numeric_limits<double>::epsilon();
-  if (std::fabs(c[0] + c[1] + c[2] + c[3]) < 1e-9 || std::fabs(c[0]) < eps || std::fabs(c[1]) < eps ||
-      std::fabs(c[2]) < eps || std::fabs(c[3]) < eps)
+  if (guards && (std::fabs(c[0] + c[1] + c[2] + c[3]) < 1e-9 || std::fabs(c[0]) < eps || std::fabs(c[1]) < eps ||
+                 std::fabs(c[2]) < eps || std::fabs(c[3]) < eps))
     return false;
+  if (!(c[3] != 0.0)) return false;  // no cubic (the polynomial solver needs a leading coefficient)
   const std::vector<double> roots = cubic_real_roots(c);
   const int n = (int)roots.size();
   if (n < 1 || n > 3) return false;
@@ -292,13 +367,17 @@ struct FundamentalEstimator {
   uint64_t seed = 0;            // stream key of the DEGENSAC samplers
   mutable bool degensac_ran = false;
 
+  bool affine = false;           // three affine correspondences per minimal sample (rows of 8)
+  bool sift = false;             // four SIFT correspondences per minimal sample (rows of 8)
   static constexpr size_t kSample = 7;
-  size_t sample_size_rt() const { return plane_parallax ? 2 : 7; }
+  size_t sample_size_rt() const { return plane_parallax ? 2 : (sift ? 4 : (affine ? 3 : 7)); }
   static constexpr size_t sample_size() { return 7; }
   static constexpr bool space_partitioning = false;  // SpacePartitioningRANSAC applies
   static constexpr size_t max_solutions() { return 3; }  // maximumMinimalSolutions
   size_t inlier_limit() const { return 7 * sample_size_rt(); }
-  size_t non_minimal_sample_size() const { return plane_parallax ? 8 : 7; }
+  // FundamentalMatrixEightPointSolver (plane-and-parallax inner runs and the
+  // affine-correspondence estimator, types.h:83-86) or the bundle adjustment
+  size_t non_minimal_sample_size() const { return plane_parallax || affine ? 8 : 7; }
 
   double squared_residual(const double* p, const Model& F) const { return f_sampson2(p, F); }
 
@@ -327,7 +406,13 @@ struct FundamentalEstimator {
 
   bool estimate_minimal(const Mat& pts, const size_t* s, std::vector<Model>& models) const {
     std::vector<Model> tmp;
-    if (!plane_parallax) {
+    if (sift) {
+      const double* rows[4] = {pts.row(s[0]), pts.row(s[1]), pts.row(s[2]), pts.row(s[3])};
+      f_four_sift(rows, tmp);
+    } else if (affine) {
+      const double* rows[3] = {pts.row(s[0]), pts.row(s[1]), pts.row(s[2])};
+      f_three_affine(rows, tmp);
+    } else if (!plane_parallax) {
       const double* rows[7];
       for (int i = 0; i < 7; ++i) rows[i] = pts.row(s[i]);
       f_seven_point(rows, nullptr, tmp);
@@ -388,7 +473,7 @@ struct FundamentalEstimator {
     }
     // packed row i carries weights[i] (point index i), as in the reference
     std::vector<Model> out;
-    if (plane_parallax) {
+    if (plane_parallax || affine) {
       f_eight_point(rows.data(), (int)n, weights, out);
     } else {
       // FundamentalMatrixBundleAdjustmentSolver: 8-point (7-point below 8 rows) then LM
@@ -511,5 +596,35 @@ inline bool FundamentalEstimator::is_valid_model(Model& model, const Mat& pts, c
   if (!plane_parallax && use_degensac) return degensac(*this, model, pts, inliers, sample, threshold, updated);
   return true;
 }
+
+// The affine-correspondence fundamental-matrix estimator of
+// findFundamentalMatrixAC_ (gcransac_python.cpp:1924-2221):
+// FundamentalMatrixEstimator<FundamentalMatrixThreeAffineSolver,
+// FundamentalMatrixEightPointSolver> (types.h:83-86) — three correspondences
+// per minimal sample, an inner sample of 7 x 3 in the local optimisation, the
+// plain 8-point solver as its non-minimal solver, and no DEGENSAC
+// (fundamental_estimator.h:326 runs it for samples of 7 or more).
+struct FundamentalAffineEstimator : FundamentalEstimator {
+  FundamentalAffineEstimator() {
+    affine = true;
+    use_degensac = false;
+  }
+  static constexpr size_t sample_size() { return 3; }
+};
+
+// The SIFT-correspondence fundamental-matrix estimator of
+// findFundamentalMatrixSIFT_ (gcransac_python.cpp:2222-2518):
+// FundamentalMatrixEstimator<FundamentalMatrixFourSIFTSolver,
+// FundamentalMatrixEightPointSolver> (types.h:88-90) — four correspondences
+// per minimal sample, an inner sample of 7 x 4, the plain 8-point solver as
+// its non-minimal solver, no DEGENSAC.
+struct FundamentalSiftEstimator : FundamentalEstimator {
+  FundamentalSiftEstimator() {
+    affine = true;  // rows of 8, the 8-point non-minimal solver
+    sift = true;
+    use_degensac = false;
+  }
+  static constexpr size_t sample_size() { return 4; }
+};
 
 }  // namespace oracle

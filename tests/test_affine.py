@@ -93,3 +93,90 @@ def test_oracle_affine_run_matches_its_minimal_solver(oracle):
     assert st.iteration_number >= 40
     assert 0 < st.models_scored <= 40
     assert rc in (0, 3)
+
+
+def test_affine_fundamental_entry_checks(gcr):
+    """The affine fundamental kind refuses P-NAPSAC and MAGSAC++ (not offered
+    by findFundamentalMatrixAC_) before any device work; the python entry wants
+    rows of 8 and at least 7 of them, like the reference binding."""
+    lib = _abi.load()
+    c = np.random.default_rng(3).uniform(0, 480, (50, 8))
+    size = _abi.ImageSize(h1=480, w1=640, h2=480, w2=640)
+    model, mask, st = np.zeros(9), np.zeros(50, np.uint8), _abi.Stats()
+    for kw in (dict(sampler=2), dict(scoring=1)):
+        p = ac_params(**kw)
+        rc = lib.gcr_find_fundamental_affine(_abi.ptr(c), 50, ctypes.byref(size), None, ctypes.byref(p),
+                                             _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
+        assert rc == _abi.GCR_UNSUPPORTED, kw
+    with pytest.raises(ValueError):
+        gcr.findFundamentalMatrix(c[:, :4], 480, 640, 480, 640, solver=2)
+    with pytest.raises(ValueError):
+        gcr.findFundamentalMatrix(c[:6], 480, 640, 480, 640, solver=2)
+
+
+def test_oracle_three_affine_solver_recovers_the_scene(oracle):
+    """On exact affine correspondences of a two-view scene the three-affine
+    system (solver_fundamental_matrix_three_affine.h:84-250) has a
+    two-dimensional null space holding the true fundamental matrix, and a tape
+    of inlier triples drives the oracle's run to it."""
+    pr = S.two_view_affine_pair(4, n=600, inlier_ratio=0.5, sigma=0.0, affine_sigma=0.0)
+    c, g, F = pr["corr"], pr["inlier_gt"], pr["F_gt"]
+
+    def rows(p):
+        x0, y0, x1, y1, a11, a12, a21, a22 = p
+        return [[x1 * x0, x1 * y0, x1, y1 * x0, y1 * y0, y1, x0, y0, 1],
+                [x1 + a11 * x0, a11 * y0, a11, y1 + a21 * x0, a21 * y0, a21, 1, 0, 0],
+                [a12 * x0, x1 + a12 * y0, a12, a22 * x0, y1 + a22 * y0, a22, 0, 1, 0]]
+    inl = c[g]
+    A = np.array(rows(inl[0]) + rows(inl[1]) + rows(inl[2])[:1])
+    sv = np.linalg.svd(A, compute_uv=False)
+    assert sv[-1] / sv[0] > 1e-12  # rank 7: a pencil of matrices
+    assert np.abs(A @ F.ravel()).max() < 1e-9 * np.abs(A).max()
+    idx = np.nonzero(g)[0]
+    tape = np.stack([idx[3 * k:3 * k + 3] for k in range(30)]).astype(np.int32)
+    p = _abi.Params(threshold=0.75, confidence=0.99, spatial_coherence_weight=0.975, neighborhood_size=8,
+                    max_iterations=30, min_iterations=30, sampler=0, neighborhood=0, lo_number=20)
+    rc, Fo, m, st = oracle.find(_abi.GCR_FUNDAMENTAL_AFFINE, c, oracle.make_size(*pr["size"]), p, seed=1,
+                                sample_tape=tape)
+    assert rc == 0
+    assert S.fundamental_error(Fo, pr) < 0.05  # px, after the local optimisation and final fits
+    assert np.all(m[g])  # every true inlier (outliers near an epipolar line can pass the threshold too)
+
+
+def test_sift_fundamental_entry_checks(gcr):
+    """The SIFT fundamental kind refuses P-NAPSAC before any device work; the
+    python entry wants rows of 8 for solver=1."""
+    lib = _abi.load()
+    c = np.random.default_rng(4).uniform(0, 480, (50, 8))
+    size = _abi.ImageSize(h1=480, w1=640, h2=480, w2=640)
+    model, mask, st = np.zeros(9), np.zeros(50, np.uint8), _abi.Stats()
+    p = ac_params(sampler=2)
+    rc = lib.gcr_find_fundamental_sift(_abi.ptr(c), 50, ctypes.byref(size), None, ctypes.byref(p), _abi.ptr(model),
+                                       _abi.ptr(mask), ctypes.byref(st))
+    assert rc == _abi.GCR_UNSUPPORTED
+    with pytest.raises(ValueError):
+        gcr.findFundamentalMatrix(c[:, :4], 480, 640, 480, 640, solver=1)
+
+
+def test_oracle_four_sift_solver_recovers_the_scene(oracle):
+    """On exact SIFT correspondences of a two-view scene the true fundamental
+    matrix satisfies every row of the four-SIFT system
+    (solver_fundamental_matrix_four_sift.h:111-150), and a tape of inlier
+    quadruples drives the oracle's run to it."""
+    pr = S.two_view_sift_pair(7, n=600, inlier_ratio=0.5, sigma=0.0, angle_sigma=0.0, scale_sigma=0.0)
+    c, g, F = pr["corr"], pr["inlier_gt"], pr["F_gt"]
+    u1, v1, u2, v2, q1, q2, o1, o2 = c[g][:20].T
+    s1, c1, s2, c2 = np.sin(o1), np.cos(o1), np.sin(o2), np.cos(o2)
+    rows = np.stack([s2 * s2 * q2 * u1 - c1 * c2 * q1 * u2 - q2 * u1, s2 * s2 * q2 * v1 - s1 * c2 * q1 * u2 - q2 * v1,
+                     s2 * s2 * q2 - q2, -c2 * s2 * q2 * u1 - c1 * c2 * q1 * v2, -c2 * s2 * q2 * v1 - s1 * c2 * q1 * v2,
+                     -c2 * s2 * q2, -c1 * c2 * q1, -s1 * c2 * q1, 0 * u1], 1)
+    assert np.abs(rows @ F.ravel()).max() < 1e-9 * np.abs(rows).max()
+    idx = np.nonzero(g)[0]
+    tape = np.stack([idx[4 * k:4 * k + 4] for k in range(30)]).astype(np.int32)
+    p = _abi.Params(threshold=0.75, confidence=0.99, spatial_coherence_weight=0.975, neighborhood_size=8,
+                    max_iterations=30, min_iterations=30, sampler=0, neighborhood=0, lo_number=20)
+    rc, Fo, m, st = oracle.find(_abi.GCR_FUNDAMENTAL_SIFT, c, oracle.make_size(*pr["size"]), p, seed=1,
+                                sample_tape=tape)
+    assert rc == 0
+    assert S.fundamental_error(Fo, pr) < 0.05
+    assert np.all(m[g])

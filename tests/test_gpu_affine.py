@@ -1,9 +1,13 @@
-"""GPU parity of the affine-correspondence homography (findHomographyAC_,
-src/pygcransac/src/gcransac_python.cpp:4553-4811; python findHomography with
-solver = 2): the device engine against the oracle on the same seeded inputs
-of rows (x1, y1, x2, y2, a11, a12, a21, a22), through the C-ABI. Statuses,
-iteration, graph-cut and models-scored counts and masks must be identical,
-models equal to 1e-6 relative Frobenius error after normalisation."""
+"""GPU parity of the kinds with rows of eight values through the C-ABI: the
+homography of findHomographyAC_ and the fundamental matrices of
+findFundamentalMatrixAC_ and findFundamentalMatrixSIFT_
+(src/pygcransac/src/gcransac_python.cpp:4553-4811, 1924-2221, 2222-2518;
+python findHomography / findFundamentalMatrix with solver = 2, and
+findFundamentalMatrix with solver = 1), the device engine against the oracle
+on the same seeded inputs of rows (x1, y1, x2, y2, a11, a12, a21, a22) or
+(x1, y1, x2, y2, q1, q2, o1, o2). Statuses, iteration, graph-cut and
+models-scored counts and masks must be identical, models equal to 1e-6
+relative Frobenius error after normalisation."""
 import numpy as np
 import pytest
 
@@ -81,3 +85,97 @@ def test_affine_homography_python_entry(oracle, gcr):
     assert (H is None) == (rc_o != 0 or m_o.sum() == 0)
     if H is not None:
         assert rel_model_err(H, H_o) < MODEL_TOL
+
+
+# ---- affine-correspondence fundamental matrix (findFundamentalMatrixAC_) ----
+
+def fa_params(**kw):
+    p = _abi.Params(threshold=0.75, confidence=0.99, spatial_coherence_weight=0.975, neighborhood_size=8,
+                    max_iterations=10000, min_iterations=50, sampler=0, neighborhood=0, lo_number=50, seed=0,
+                    min_inlier_ratio_for_sprt=1e-5)
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def compare_f(oracle, batch_parity, gcr, pairs, p, seeds, kind=_abi.GCR_FUNDAMENTAL_AFFINE):
+    corr = np.concatenate([pr["corr"] for pr in pairs])
+    offsets = np.zeros(len(pairs) + 1, np.int64)
+    offsets[1:] = np.cumsum([len(pr["corr"]) for pr in pairs])
+    sizes = np.array([pr["size"] for pr in pairs])
+    models, masks, stats = gcr.find_batch(kind, (corr, offsets), sizes, p, seeds=seeds)
+    flat = np.concatenate(masks)
+    batch_parity(kind, corr, offsets, sizes, p, np.asarray(seeds, np.uint64), None, stats, flat)
+    for i, pr in enumerate(pairs):
+        rc_o, F_o, m_o, st_o = oracle.find(kind, pr["corr"], oracle.make_size(*pr["size"]), p, seed=seeds[i])
+        if np.array_equal(masks[i], m_o) and rc_o == 0:
+            assert rel_model_err(models[i], F_o) < MODEL_TOL, i
+            assert stats["models_scored"][i] == st_o.models_scored, i
+    return models, masks, stats
+
+
+@pytest.mark.parametrize("sampler,use_sprt", [(0, 0), (1, 0), (0, 1)])
+def test_affine_fundamental_batch(oracle, batch_parity, gcr, sampler, use_sprt):
+    """Batches of affine two-view pairs (200-4000 correspondences, 20-60 %
+    inliers): statuses, iteration and graph-cut counts, masks and models equal
+    the oracle's; the runs find the ground truth."""
+    pairs = [S.two_view_affine_pair(80 + i, n=n, inlier_ratio=r)
+             for i, (n, r) in enumerate([(200, 0.6), (1500, 0.3), (4000, 0.2), (900, 0.5), (2500, 0.4)])]
+    models, masks, stats = compare_f(oracle, batch_parity, gcr, pairs,
+                                     fa_params(sampler=sampler, use_sprt=use_sprt), seeds=[3, 4, 5, 6, 7])
+    assert np.all(stats["status"] == 0)
+    errs = [S.fundamental_error(models[i], pr) for i, pr in enumerate(pairs)]
+    assert np.median(errs) < 1.0, errs
+
+
+def test_affine_fundamental_large_and_no_spatial_term(oracle, batch_parity, gcr):
+    """Pairs above the shared-memory tile (6000-9000 correspondences) and a run
+    without the spatial term (no neighbourhood, as the driver builds none)."""
+    pairs = [S.two_view_affine_pair(90 + i, n=n, inlier_ratio=0.3) for i, n in enumerate([6000, 9000])]
+    compare_f(oracle, batch_parity, gcr, pairs, fa_params(), seeds=[1, 2])
+    compare_f(oracle, batch_parity, gcr, pairs[:1], fa_params(spatial_coherence_weight=0.0), seeds=[5])
+
+
+def test_affine_fundamental_python_entry(oracle, gcr):
+    """findFundamentalMatrix(..., solver=2) equals the oracle's driver run and
+    needs far fewer iterations than the seven-point form on the same points."""
+    pr = S.two_view_affine_pair(95, n=1200, inlier_ratio=0.3)
+    h, w = pr["size"][:2]
+    kw = dict(threshold=0.75, sampler=0, use_sprt=False, neighborhood=0, neighborhood_size=8,
+              spatial_coherence_weight=0.975, seed=4)
+    F, mask, st = gcr.findFundamentalMatrix(pr["corr"], h, w, h, w, solver=2, return_stats=True, **kw)
+    p = fa_params(seed=4)
+    rc_o, F_o, m_o, st_o = oracle.find(_abi.GCR_FUNDAMENTAL_AFFINE, pr["corr"], oracle.make_size(*pr["size"]), p,
+                                       seed=4)
+    assert rc_o == 0 and np.array_equal(mask, m_o)
+    assert rel_model_err(F, F_o) < MODEL_TOL
+    F7, mask7, st7 = gcr.findFundamentalMatrix(pr["corr"][:, :4].copy(), h, w, h, w, return_stats=True, **kw)
+    assert st.iteration_number < st7.iteration_number
+
+
+# ---- SIFT-correspondence fundamental matrix (findFundamentalMatrixSIFT_) ----
+
+@pytest.mark.parametrize("sampler,use_sprt", [(0, 0), (1, 0), (0, 1)])
+def test_sift_fundamental_batch(oracle, batch_parity, gcr, sampler, use_sprt):
+    """Batches of SIFT two-view pairs (scales and orientations): statuses,
+    iteration and graph-cut counts, masks and models equal the oracle's; the
+    runs find the ground truth."""
+    pairs = [S.two_view_sift_pair(60 + i, n=n, inlier_ratio=r)
+             for i, (n, r) in enumerate([(300, 0.6), (1500, 0.35), (5000, 0.3), (900, 0.5)])]
+    models, masks, stats = compare_f(oracle, batch_parity, gcr, pairs, fa_params(sampler=sampler, use_sprt=use_sprt),
+                                     seeds=[2, 3, 4, 5], kind=_abi.GCR_FUNDAMENTAL_SIFT)
+    assert np.all(stats["status"] == 0)
+    errs = [S.fundamental_error(models[i], pr) for i, pr in enumerate(pairs)]
+    assert np.median(errs) < 1.0, errs
+
+
+def test_sift_fundamental_python_entry(oracle, gcr):
+    """findFundamentalMatrix(..., solver=1) equals the oracle's driver run."""
+    pr = S.two_view_sift_pair(66, n=1200, inlier_ratio=0.4)
+    h, w = pr["size"][:2]
+    F, mask = gcr.findFundamentalMatrix(pr["corr"], h, w, h, w, solver=1, threshold=0.75, sampler=0, use_sprt=False,
+                                        neighborhood=0, neighborhood_size=8, spatial_coherence_weight=0.975, seed=4)
+    rc_o, F_o, m_o, _ = oracle.find(_abi.GCR_FUNDAMENTAL_SIFT, pr["corr"], oracle.make_size(*pr["size"]),
+                                    fa_params(seed=4), seed=4)
+    assert rc_o == 0 and np.array_equal(mask, m_o)
+    assert rel_model_err(F, F_o) < MODEL_TOL
