@@ -51,7 +51,7 @@ METRIC = "image pairs/sec at equal model error; learned vs plain GC-RANSAC on 1 
 # Algorithmic FP32 work of one residual evaluation (one model x one correspondence):
 # H transfer error 21 FLOP, Sampson distance 35 FLOP.
 FLOP_PER_RESIDUAL = {"homography": 21, "fundamental": 35, "essential": 35, "learned": 35, "fundamental_affine": 35,
-                     "fundamental_sift": 35}
+                     "fundamental_sift": 35, "homography_sift": 21, "essential_planar": 35}
 
 WORKLOADS = {
     # 2000 correspondences in 640x480, 40 % inliers (sigma 1 px), threshold 3 px,
@@ -64,6 +64,12 @@ WORKLOADS = {
     # solver + graph-cut LO, DEGENSAC on
     "fundamental": dict(kind=_abi.GCR_FUNDAMENTAL, n=5000, ratio=0.25, threshold=0.75, sampler=2, grid=8,
                         lam=0.975, pairs=608),
+    # SIFT correspondences of the same homography scenes (feature scales and
+    # orientations consistent with the homography's Jacobian, 0.01 rad / 1 %
+    # noise): the two-SIFT solver, otherwise as the homography workload
+    # without space partitioning
+    "homography_sift": dict(kind=_abi.GCR_HOMOGRAPHY_SIFT, n=2000, ratio=0.4, threshold=3.0, sampler=0, grid=4,
+                            lam=0.975, pairs=1216),
     # affine correspondences of the same scene (each inlier on a local plane,
     # its 2x2 affine map the Jacobian of the plane's homography + 0.01 noise):
     # 5000 per pair, 25 % inliers, threshold 0.75 px, uniform sampler (the
@@ -82,6 +88,13 @@ WORKLOADS = {
     # grid, lambda 0.1, 5-point solver + graph-cut LO, MAGSAC++ scoring
     "essential": dict(kind=_abi.GCR_ESSENTIAL, n=(200, 8000), ratio=(0.1, 0.7), threshold=0.75, sampler=0, grid=8,
                       lam=0.1, pairs=1024, scoring=_abi.GCR_SCORING_MAGSAC),
+    # planar camera motion (rotation about the camera's y axis up to 30 deg,
+    # unit translation in its x-z plane; scene, f and noise as above): 1024
+    # pairs x 2000 correspondences, 30 % inliers, threshold 0.75 px, uniform
+    # sampler, 8^4 grid, lambda 0.975, the two-point planar solver with the
+    # bundle-adjustment non-minimal fits, MSAC, SPRT off
+    "essential_planar": dict(kind=_abi.GCR_ESSENTIAL_PLANAR, n=2000, ratio=0.3, threshold=0.75, sampler=0, grid=8,
+                             lam=0.975, pairs=1024),
     # hard fundamental-matrix pairs: 4000 correspondences of the two-view scene
     # above at 5-10 % inliers. Plain form: uniform sampler with the reference's
     # 10000-iteration budget; learned form: the network's order drives PROSAC
@@ -125,6 +138,12 @@ def _gen_pair(job):
     if workload == "fundamental_sift":
         pr = S.two_view_sift_pair(seed, n=n, inlier_ratio=ratio)
         return pr["corr"], pr["size"], pr
+    if workload == "homography_sift":
+        pr = S.homography_sift_pair(seed, n=n, inlier_ratio=ratio)
+        return pr["corr"], pr["size"], pr["H_gt"]
+    if workload == "essential_planar":
+        pr = S.two_view_pair(seed, n=n, inlier_ratio=ratio, planar_motion=True)
+        return pr["corr"], pr["size"], pr
     pr = S.two_view_pair(seed, n=n, inlier_ratio=ratio)
     return pr["corr"], pr["size"], pr
 
@@ -157,7 +176,8 @@ def build_pairs(workload, pairs, seed0):
     corr = [c for c, _, _ in out]
     sizes = [z for _, z, _ in out]
     gts = [g for _, _, g in out]
-    Ks = [np.concatenate([g["K"].ravel(), g["K"].ravel()]) for g in gts] if workload == "essential" else []
+    Ks = ([np.concatenate([g["K"].ravel(), g["K"].ravel()]) for g in gts]
+          if workload in ("essential", "essential_planar") else [])
     offsets = np.zeros(pairs + 1, np.int64)
     offsets[1:] = np.cumsum([len(c) for c in corr])
     K = np.ascontiguousarray(np.array(Ks), np.float64) if Ks else None
@@ -209,13 +229,13 @@ def size_array(sizes):
 def model_errors(workload, models, gts, limit=64):
     """Median-ready model errors against ground truth on the first `limit` pairs
     (H: RMS transfer px; F: mean Sampson px of clean correspondences)."""
-    if workload == "homography":
+    if workload in ("homography", "homography_sift"):
         return [S.homography_error(m / m[2, 2] if abs(m[2, 2]) > 1e-12 else m, g) for m, g in zip(models, gts)]
     if workload in ("fundamental", "fundamental_affine", "fundamental_sift"):
         return [S.fundamental_error(m, g, n=200) for m, g in list(zip(models, gts))[:limit]]
     if workload == "learned":
         return [S.fundamental_error(m, g, n=100) for m, g in zip(models, gts)]
-    if workload == "essential":
+    if workload in ("essential", "essential_planar"):
         return [S.essential_error(m, g) for m, g in zip(models, gts)]
     return []
 
@@ -1138,7 +1158,8 @@ def main():
     # the other workloads, a few steps each (same replicas and timing rules)
     if not args.no_side:
         side = {}
-        for name in ("homography", "fundamental", "fundamental_affine", "fundamental_sift", "essential", "serving"):
+        for name in ("homography", "homography_sift", "fundamental", "fundamental_affine", "fundamental_sift",
+                     "essential", "essential_planar", "serving"):
             if name == args.workload:
                 continue
             sw = WORKLOADS[name]

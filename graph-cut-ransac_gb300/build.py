@@ -14,8 +14,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
-SOURCES = ["gcr_kind_f.cu", "gcr_kind_fa.cu", "gcr_kind_fs.cu", "gcr_kind_e.cu", "gcr_api.cu", "gcr_kind_h.cu", "gcr_kind_ha.cu", "gcr_noalloc.cu",
-           "gcr_learned.cu"]
+SOURCES = ["gcr_kind_f.cu", "gcr_kind_fa.cu", "gcr_kind_fs.cu", "gcr_kind_e.cu", "gcr_api.cu", "gcr_kind_h.cu", "gcr_kind_ha.cu",
+           "gcr_kind_hs.cu", "gcr_kind_ep.cu", "gcr_noalloc.cu", "gcr_learned.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
          "--expt-relaxed-constexpr",

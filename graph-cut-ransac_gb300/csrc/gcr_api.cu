@@ -73,6 +73,8 @@ const gcr::KindOps* ops_for(gcr_model_kind kind) {
     case GCR_HOMOGRAPHY_AFFINE: return gcr::homography_affine_ops();
     case GCR_FUNDAMENTAL_AFFINE: return gcr::fundamental_affine_ops();
     case GCR_FUNDAMENTAL_SIFT: return gcr::fundamental_sift_ops();
+    case GCR_HOMOGRAPHY_SIFT: return gcr::homography_sift_ops();
+    case GCR_ESSENTIAL_PLANAR: return gcr::essential_planar_ops();
   }
   return nullptr;
 }
@@ -81,17 +83,24 @@ const gcr::KindOps* ops_for(gcr_model_kind kind) {
 // features' scales and orientations), split into point rows and the four
 // extra values before the engine runs.
 bool affine_kind(gcr_model_kind kind) {
-  return kind == GCR_HOMOGRAPHY_AFFINE || kind == GCR_FUNDAMENTAL_AFFINE || kind == GCR_FUNDAMENTAL_SIFT;
+  return kind == GCR_HOMOGRAPHY_AFFINE || kind == GCR_FUNDAMENTAL_AFFINE || kind == GCR_FUNDAMENTAL_SIFT ||
+         kind == GCR_HOMOGRAPHY_SIFT;
 }
+
+// Essential-matrix kinds: K^-1 normalisation of the rows, thresholds divided
+// by the mean focal length, the pose epilogue.
+bool essential_kind(gcr_model_kind kind) { return kind == GCR_ESSENTIAL || kind == GCR_ESSENTIAL_PLANAR; }
 
 // Doubles per correspondence row of a model kind (gcr_model_kind).
 int kind_columns(gcr_model_kind kind) { return affine_kind(kind) ? 8 : 4; }
 
 // The homography drivers construct their SPRT test without the
 // min_inlier_ratio_for_sprt argument (gcransac_python.cpp:4394-4396,
-// 4719-4721), so it starts from the constructor's default inlier ratio 0.01
+// 4719-4721, 4979-4981), so it starts from the constructor's default inlier ratio 0.01
 // (preemption_sprt.h:141-143); the other drivers pass the argument.
-bool homography_driver(gcr_model_kind kind) { return kind == GCR_HOMOGRAPHY || kind == GCR_HOMOGRAPHY_AFFINE; }
+bool homography_driver(gcr_model_kind kind) {
+  return kind == GCR_HOMOGRAPHY || kind == GCR_HOMOGRAPHY_AFFINE || kind == GCR_HOMOGRAPHY_SIFT;
+}
 
 }  // namespace
 
@@ -122,7 +131,7 @@ struct gcr_context {
     int num_pairs = 0;
   } pending;
   int slot_kind = -1, slot_max_n = 0, slot_count = 0;
-  bool prepared[6] = {false, false, false, false, false, false};
+  bool prepared[8] = {false, false, false, false, false, false, false, false};
   unsigned long long* pair_times = nullptr;  // see gcr_context_set_pair_times
   DevBuf rg_int, rg_dbl, rg_px;              // radius-graph scratch (one region per resident CTA)
   DevBuf ar_p, ar_i, ar_ab, ar_cnt;          // AR sampler heaps and per-point state (per resident CTA)
@@ -168,9 +177,12 @@ gcr_status check_params(gcr_model_kind kind, const gcr_params* p) {
     return fail(GCR_UNSUPPORTED, "neighborhood_size must be at most 1024 grid divisions");
   if (p->neighborhood == GCR_NEIGHBORHOOD_FLANN && !(p->neighborhood_size > 0 && std::isfinite(p->neighborhood_size)))
     return fail(GCR_INVALID_ARG, "neighborhood_size (the radius) must be > 0 and finite for the radius graph");
+  if (kind == GCR_ESSENTIAL_PLANAR && p->scoring != GCR_SCORING_MSAC)
+    return fail(GCR_UNSUPPORTED, "the planar essential-matrix driver scores with MSAC only");
   if (affine_kind(kind)) {
-    // findHomographyAC_ / findFundamentalMatrixAC_ / findFundamentalMatrixSIFT_
-    // (gcransac_python.cpp:4553, 1924, 2222): MSAC, and no P-NAPSAC
+    // findHomographyAC_ / findFundamentalMatrixAC_ / findFundamentalMatrixSIFT_ /
+    // findHomographySIFT_ (gcransac_python.cpp:4553, 1924, 2222, 4813): MSAC,
+    // and no P-NAPSAC
     if (p->sampler == GCR_SAMPLER_PNAPSAC)
       return fail(GCR_UNSUPPORTED, "the affine-correspondence drivers provide samplers 0, 1, 3 and 4");
     if (p->scoring != GCR_SCORING_MSAC)
@@ -239,6 +251,7 @@ void gcr_default_params(gcr_model_kind kind, gcr_params* p) {
   switch (kind) {
     case GCR_HOMOGRAPHY:  // bindings.cpp:1158-1178
     case GCR_HOMOGRAPHY_AFFINE:  // the same python entry with solver = 2
+    case GCR_HOMOGRAPHY_SIFT:    // and with solver = 1
       p->spatial_coherence_weight = 0.975;
       p->neighborhood = GCR_NEIGHBORHOOD_GRID;
       p->neighborhood_size = 4.0;
@@ -253,6 +266,11 @@ void gcr_default_params(gcr_model_kind kind, gcr_params* p) {
       break;
     case GCR_ESSENTIAL:  // bindings.cpp:1091-1112
       p->spatial_coherence_weight = 0.1;
+      p->neighborhood = GCR_NEIGHBORHOOD_FLANN;
+      p->neighborhood_size = 20.0;
+      break;
+    case GCR_ESSENTIAL_PLANAR:  // bindings.cpp:1114-1133
+      p->spatial_coherence_weight = 0.975;
       p->neighborhood = GCR_NEIGHBORHOOD_FLANN;
       p->neighborhood_size = 20.0;
       break;
@@ -322,7 +340,9 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
   if (num_pairs > (1 << 30)) return fail(GCR_CAPACITY, "too many pairs");
   if (!d_corr || !h_offsets || !h_sizes || !d_models_out || !d_masks_out || !d_stats_out)
     return fail(GCR_INVALID_ARG, "NULL buffer");
-  if (kind == GCR_ESSENTIAL && !h_K && !run_only) return fail(GCR_INVALID_ARG, "essential matrices need intrinsics");
+  if (essential_kind(kind) && !h_K && !run_only) return fail(GCR_INVALID_ARG, "essential matrices need intrinsics");
+  if (kind == GCR_ESSENTIAL_PLANAR && run_only)
+    return fail(GCR_UNSUPPORTED, "gcr_run provides the homography, fundamental and essential estimators");
   if (affine_kind(kind) && run_only)
     return fail(GCR_UNSUPPORTED, "gcr_run takes point correspondences; affine ones run through gcr_find_batch");
   const int m = ops->sample_size;
@@ -422,7 +442,7 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
     // (gcransac_python.cpp:4290-4297), the fundamental/essential ones do not
     // (1670-1677)
     const double pad = kind == GCR_HOMOGRAPHY ? eps : 0.0;
-    const bool essential = kind == GCR_ESSENTIAL;
+    const bool essential = essential_kind(kind);
     d.cell[0] = (z.w1 + pad) / nd;
     d.cell[1] = (z.h1 + pad) / nd;
     d.cell[2] = (z.w2 + pad) / nd;
@@ -458,7 +478,7 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
   CUDA_TRY(c->pairs.ensure(sizeof(gcr::PairDesc) * num_pairs));
   CUDA_TRY(cudaMemcpyAsync(c->pairs.p, pd.data(), sizeof(gcr::PairDesc) * num_pairs, cudaMemcpyHostToDevice, s));
   const double* run_pts = d_corr;
-  if (kind == GCR_ESSENTIAL && !run_only) {
+  if (essential_kind(kind) && !run_only) {
     // K^-1 of both cameras per pair (a singular K is rejected)
     std::vector<double> kinv(18 * (size_t)num_pairs);
     for (int64_t i = 0; i < num_pairs; ++i)
@@ -539,6 +559,12 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
   prm.pp_h = nullptr;
   prm.use_sprt = params->use_sprt ? 1 : 0;
   prm.use_sp = (kind == GCR_HOMOGRAPHY && params->use_space_partitioning) ? 1 : 0;
+  // the planar driver's SPRT branch sets max_graph_cut_number = 100 and
+  // do_final_iterated_least_squares = false (gcransac_python.cpp:3741-3742);
+  // its other branch and the other drivers keep the defaults (10, true)
+  const bool planar_sprt = kind == GCR_ESSENTIAL_PLANAR && params->use_sprt && !run_only;
+  prm.gc_max = planar_sprt ? 100 : 10;
+  prm.final_irls = planar_sprt ? 0 : 1;
   prm.sprt_min_ratio = homography_driver(kind) && !run_only ? 0.01 : params->min_inlier_ratio_for_sprt;
   prm.epilogue = run_only ? 0 : 1;
   prm.flow_cap = c->flow_cap;
@@ -573,7 +599,9 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
     prm.rg_px = (float4*)c->rg_px.p;
   }
   prm.probs = nullptr;
-  prm.sampler_variance = params->sampler_variance;
+  // the planar driver's AR sampler takes the variance 0.1 whatever the
+  // argument holds (gcransac_python.cpp:3675)
+  prm.sampler_variance = kind == GCR_ESSENTIAL_PLANAR && !run_only ? 0.1 : params->sampler_variance;
   prm.ar_p = nullptr;
   prm.ar_i = nullptr;
   prm.ar_ab = nullptr;
@@ -621,7 +649,7 @@ static gcr_status prepare_batch(gcr_context* c, gcr_model_kind kind, int64_t num
   L->grid = grid;
   L->ws = ws;
   L->prm = prm;
-  L->normalise = kind == GCR_ESSENTIAL && !run_only;
+  L->normalise = essential_kind(kind) && !run_only;
   L->split_affine = affine_kind(kind);
   L->total = total;
   L->probs = params->sampler == GCR_SAMPLER_IMPORTANCE ? c->probs : nullptr;
@@ -903,7 +931,7 @@ static gcr_status find_one(gcr_model_kind kind, const double* corr, int64_t n, c
   if (n < m) return fail(GCR_TOO_FEW_POINTS, "%lld correspondences, needs >= %d", (long long)n, m);
   const int64_t offsets[2] = {0, n};
   double K[18];
-  if (kind == GCR_ESSENTIAL) {
+  if (essential_kind(kind)) {
     if (!K1 || !K2) return fail(GCR_INVALID_ARG, "essential matrices need K1 and K2");
     std::memcpy(K, K1, 9 * sizeof(double));
     std::memcpy(K + 9, K2, 9 * sizeof(double));
@@ -914,7 +942,7 @@ static gcr_status find_one(gcr_model_kind kind, const double* corr, int64_t n, c
   if (weighted && !probabilities)
     return fail(GCR_INVALID_ARG, "samplers 3 and 4 need per-correspondence probabilities");
   g_batch_probs = weighted ? probabilities : nullptr;
-  gcr_status rc = gcr_find_batch(kind, 1, corr, offsets, kind == GCR_ESSENTIAL ? K : nullptr, size, params, &seed,
+  gcr_status rc = gcr_find_batch(kind, 1, corr, offsets, essential_kind(kind) ? K : nullptr, size, params, &seed,
                                  model_out9, mask_out, &st);
   g_batch_probs = nullptr;
   if (rc != GCR_OK) return rc;
@@ -964,6 +992,20 @@ gcr_status gcr_find_fundamental_sift(const double* corr, int64_t n, const gcr_im
                                      const double* probabilities, const gcr_params* params, double* model_out9,
                                      uint8_t* mask_out, gcr_stats* stats_out) {
   return find_one(GCR_FUNDAMENTAL_SIFT, corr, n, nullptr, nullptr, size, probabilities, params, model_out9,
+                  mask_out, stats_out);
+}
+
+gcr_status gcr_find_essential_planar(const double* corr, int64_t n, const double* K1, const double* K2,
+                                     const gcr_image_size* size, const double* probabilities, const gcr_params* params,
+                                     double* model_out9, uint8_t* mask_out, gcr_stats* stats_out) {
+  return find_one(GCR_ESSENTIAL_PLANAR, corr, n, K1, K2, size, probabilities, params, model_out9, mask_out,
+                  stats_out);
+}
+
+gcr_status gcr_find_homography_sift(const double* corr, int64_t n, const gcr_image_size* size,
+                                    const double* probabilities, const gcr_params* params, double* model_out9,
+                                    uint8_t* mask_out, gcr_stats* stats_out) {
+  return find_one(GCR_HOMOGRAPHY_SIFT, corr, n, nullptr, nullptr, size, probabilities, params, model_out9,
                   mask_out, stats_out);
 }
 
@@ -1075,4 +1117,6 @@ __attribute__((weak)) const KindOps* essential_ops() { return nullptr; }
 __attribute__((weak)) const KindOps* homography_affine_ops() { return nullptr; }
 __attribute__((weak)) const KindOps* fundamental_affine_ops() { return nullptr; }
 __attribute__((weak)) const KindOps* fundamental_sift_ops() { return nullptr; }
+__attribute__((weak)) const KindOps* homography_sift_ops() { return nullptr; }
+__attribute__((weak)) const KindOps* essential_planar_ops() { return nullptr; }
 }  // namespace gcr

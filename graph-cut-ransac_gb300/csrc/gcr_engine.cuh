@@ -107,6 +107,10 @@ struct EngineParams {
   double sprt_min_ratio;
   // space-partitioning pre-selection of homography models
   int32_t use_sp;
+  // graph cuts per run (GCRANSAC::settings.max_graph_cut_number) and the
+  // final iteratively reweighted fit (do_final_iterated_least_squares)
+  int32_t gc_max;
+  int32_t final_irls;
   // 1: the Python drivers' epilogue after the run (bundle adjustment of the
   // final inliers for F and E); 0: GCRANSAC::run alone
   int32_t epilogue;
@@ -286,6 +290,25 @@ __host__ __device__ constexpr bool has_degensac() {
 template <class Est>
 __host__ __device__ constexpr bool nonminimal_lm() {
   if constexpr (Est::KIND == 1) return Est::NONMIN_LM;
+  else return false;
+}
+
+// Models per minimal sample in SPRT's cost model: the minimal solver's
+// declared maximumSolutions (preemption_sprt.h:134). Every homography solver
+// declares one, the two-SIFT solver although its two conics meet in up to
+// four points (solver_homography_two_sift.h:83-86).
+template <class Est>
+__host__ __device__ constexpr int sprt_solutions() {
+  if constexpr (Est::KIND == 0) return 1;
+  else if constexpr (Est::KIND == 3) return Est::DECLARED_SOLUTIONS;
+  else return Est::MAXSOL;
+}
+
+// Whether an essential-matrix kind's non-minimal solver is the bundle
+// adjustment solver (the planar-motion estimator, types.h:121-126).
+template <class Est>
+__host__ __device__ constexpr bool nonmin_ba() {
+  if constexpr (Est::KIND == 3) return Est::NONMIN_BA;
   else return false;
 }
 
@@ -2248,12 +2271,88 @@ struct Engine {
           sh.multi_count = ess::stewenius_from_ata(full, sh.multi_models);
         }
       }
+      if constexpr (nonmin_ba<Est>()) {
+        sync();
+        bundle_adjust_models(list, n, weight_mode);
+      }
       if (threadIdx.x == 0 && normalise)
         for (int q = 0; q < sh.multi_count; ++q) ess::normalise_sign(sh.multi_models + 9 * q);
       sync();
       return sh.multi_count;
     } else {
       return 0;
+    }
+  }
+
+  // EssentialMatrixBundleAdjustmentSolver::estimateModel after its Stewenius
+  // start (solver_essential_matrix_bundle_adjustment.h:141-183): the models
+  // in sh.multi_models are replaced by every cheirality-consistent pose of
+  // each (checked on the first row of the list) refined over the rows, at
+  // most kMulti of them. The refinement reads its weights by row position
+  // (jacobian_impl.h:327-342) from the array the Stewenius start reads by
+  // point: unit weights for weight_mode 0, slot.dres for 2, and for 3 the
+  // weight array of the iteratively reweighted fit, which holds the squared
+  // Tukey weight of each listed point and 0 elsewhere, read at index k for
+  // row k (slot.sp_flag marks the listed points; space partitioning, its
+  // other user, runs for homographies only).
+  __device__ void bundle_adjust_models(const int* list, int n, int weight_mode) {
+    if constexpr (nonmin_ba<Est>()) {
+      if (weight_mode == 0) {
+        for (int k = threadIdx.x; k < n; k += GCR_BLOCK) slot.dres[k] = 1.0;
+      } else if (weight_mode == 3) {
+        for (int p = threadIdx.x; p < N; p += GCR_BLOCK) slot.sp_flag[p] = 0;
+        sync();
+        for (int k = threadIdx.x; k < n; k += GCR_BLOCK) slot.sp_flag[list[k]] = 1;
+        sync();
+        double wm[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) wm[q] = sh.work_model[q];
+        for (int k = threadIdx.x; k < n; k += GCR_BLOCK) {
+          double w = 0.0;
+          if (slot.sp_flag[k]) {
+            const double r2 = Est::r2_f64(row64(k), wm);
+            const double t = fmax(0.0, 1.0 - r2 / t2);
+            w = t * t;
+          }
+          slot.dres[k] = w;
+        }
+      }
+      sync();
+      double x1[3], x2[3];
+      {
+        const double* p0 = row64(list[0]);
+        x1[0] = p0[0]; x1[1] = p0[1]; x1[2] = 1.0;
+        x2[0] = p0[2]; x2[1] = p0[3]; x2[2] = 1.0;
+        const double n1 = sqrt(x1[0] * x1[0] + x1[1] * x1[1] + 1.0);
+        const double n2 = sqrt(x2[0] * x2[0] + x2[1] * x2[1] + 1.0);
+        for (int i = 0; i < 3; ++i) {
+          x1[i] /= n1;
+          x2[i] /= n2;
+        }
+      }
+      const int nin = sh.multi_count;
+      double Em[9 * Shared<Est>::kMulti];
+      for (int q = 0; q < 9 * nin; ++q) Em[q] = sh.multi_models[q];
+      sync();
+      int nout = 0;
+      for (int q = 0; q < nin; ++q) {
+        double Eq[9];
+#pragma unroll
+        for (int e = 0; e < 9; ++e) Eq[e] = Em[9 * q + e];
+        ess::Pose poses[4];
+        const int np = ess::poses_from_essential(Eq, x1, x2, poses);
+        for (int v = 0; v < np && nout < Shared<Est>::kMulti; ++v) {
+          ess::Pose P = poses[v];
+          refine_relpose_cta(list, n, P);
+          double Eo[9];
+          ess::essential_from_pose(P, Eo);
+          if (threadIdx.x == 0)
+            for (int e = 0; e < 9; ++e) sh.multi_models[9 * nout + e] = Eo[e];
+          ++nout;
+        }
+      }
+      if (threadIdx.x == 0) sh.multi_count = nout;
+      sync();
     }
   }
 
@@ -2426,7 +2525,7 @@ struct Engine {
     int* L = slot.list0;
     const int trials = prm.lo_number;
     ++lo_number;
-    while (++gc_number < 10) {
+    while (++gc_number < prm.gc_max) {
       bool updated = false;
       long long t0 = tick();
       const int nL = labeling(sh.lo_best_model, ncells, L);
@@ -2677,7 +2776,7 @@ struct Engine {
     sprt = true;
     sprt_cursor = 0;
     sprt_tM = 1.0 / (double)m;
-    sprt_mS = (double)Est::MAXSOL;
+    sprt_mS = (double)sprt_solutions<Est>();
     sprt_delta = prm.sprt_min_ratio / 10.0;
     sprt_eps = prm.sprt_min_ratio;
     sprt_A = sprt_threshold_A(sprt_eps, sprt_delta);
@@ -3580,9 +3679,11 @@ struct Engine {
     int n = materialise(cont[off], list);
     copy_model(sh.work_model, sh.best_model);
     bool irls_applied = false;
-    bool ok;
-    if constexpr (Est::LO_MAXSOL > 1) ok = irls_multi(list, n, spare);
-    else ok = irls(list, n, spare);
+    bool ok = false;
+    if (prm.final_irls) {
+      if constexpr (Est::LO_MAXSOL > 1) ok = irls_multi(list, n, spare);
+      else ok = irls(list, n, spare);
+    }
     if (ok) {
       // the container now holds the inliers of the IRLS model
       copy_model(sh.cont_model[off], sh.work_model);
@@ -3697,26 +3798,35 @@ struct Engine {
         int* tmp = spare;
         double Em[9 * Shared<Est>::kMulti];
         for (int q = 0; q < 9 * nm; ++q) Em[q] = sh.multi_models[q];
+        auto consider = [&](const double* Eq) {
+          sync();
+          if (threadIdx.x < 9) sh.fit_model[threadIdx.x] = Eq[threadIdx.x];
+          sync();
+          const Score sc = exact_score(sh.fit_model, tmp, nullptr, true);
+          if (final_score < sc.value) {
+            final_score = sc.value;
+            copy_model(sh.best_model, sh.fit_model);
+            cur = tmp;
+            tmp = (tmp == spare) ? slot.list0 : spare;
+            cnt = sc.count;
+          }
+        };
         for (int q = 0; q < nm; ++q) {
           double Eq[9];
 #pragma unroll
           for (int e = 0; e < 9; ++e) Eq[e] = Em[9 * q + e];
-          ess::Pose poses[4];
-          const int np = ess::poses_from_essential(Eq, x1, x2, poses);
-          for (int v = 0; v < np; ++v) {
-            ess::Pose P = poses[v];
-            refine_relpose_cta(ba, ba_n, P);
-            ess::essential_from_pose(P, Eq);
-            sync();
-            if (threadIdx.x < 9) sh.fit_model[threadIdx.x] = Eq[threadIdx.x];
-            sync();
-            const Score sc = exact_score(sh.fit_model, tmp, nullptr, true);
-            if (final_score < sc.value) {
-              final_score = sc.value;
-              copy_model(sh.best_model, sh.fit_model);
-              cur = tmp;
-              tmp = (tmp == spare) ? slot.list0 : spare;
-              cnt = sc.count;
+          if constexpr (nonmin_ba<Est>()) {
+            // the non-minimal solver is the bundle adjustment itself: its
+            // models are already the refined poses
+            consider(Eq);
+          } else {
+            ess::Pose poses[4];
+            const int np = ess::poses_from_essential(Eq, x1, x2, poses);
+            for (int v = 0; v < np; ++v) {
+              ess::Pose P = poses[v];
+              refine_relpose_cta(ba, ba_n, P);
+              ess::essential_from_pose(P, Eq);
+              consider(Eq);
             }
           }
         }

@@ -1213,6 +1213,11 @@ struct EssentialModel {
   static constexpr int SAMPLE_CAP = INLIER_LIMIT;
   static constexpr bool AFFINE = false;
   static constexpr bool CTA_VALIDITY = true;
+  // maximumSolutions of the minimal solver (the count SPRT uses)
+  static constexpr int DECLARED_SOLUTIONS = 10;
+  // the non-minimal solver is EssentialMatrixBundleAdjustmentSolver
+  // (Stewenius, then every cheirality-consistent pose refined)
+  static constexpr bool NONMIN_BA = false;
 
   __device__ static bool valid_sample(const double*, const int*) { return true; }
 
@@ -1247,6 +1252,14 @@ struct EssentialModel {
   // Stewenius on the rows, each model normalised. Returns the model count.
   __device__ static int fit_thread_multi(const double* pts, const int* idx, int n, double* out) {
     if (n < NONMIN) return 0;
+    const int nm = stewenius_thread(pts, idx, n, out);
+    for (int q = 0; q < nm; ++q) ess::normalise_sign(out + 9 * q);
+    return nm;
+  }
+
+  // Stewenius on the rows idx[0..n) (n >= 5) with unit weights, by one
+  // thread; the models as the solver returns them.
+  __device__ static int stewenius_thread(const double* pts, const int* idx, int n, double* out) {
     int nm;
     if (n == 5) {
       double rows[5][9];
@@ -1275,8 +1288,164 @@ struct EssentialModel {
         }
       nm = ess::stewenius_from_ata(full, out);
     }
-    for (int q = 0; q < nm; ++q) ess::normalise_sign(out + 9 * q);
     return nm;
+  }
+};
+
+// Planar-motion essential matrix (findPlanarEssentialMatrix_,
+// gcransac_python.cpp:3531-3870): EssentialMatrixEstimator<
+// EssentialMatrixTwoPointsPlanar, EssentialMatrixBundleAdjustmentSolver>
+// (types.h:121-126) on K^-1-normalised coordinates.
+struct EssentialPlanarModel : EssentialModel {
+  static constexpr int M = 2;
+  static constexpr int MAXSOL = 4;
+  static constexpr int NONMIN = 6;  // EssentialMatrixBundleAdjustmentSolver::sampleSize
+  static constexpr int INLIER_LIMIT = 7 * M;
+  static constexpr int SAMPLE_CAP = INLIER_LIMIT;
+  static constexpr int DECLARED_SOLUTIONS = 1;  // the solver declares none (SolverEngine's 1)
+  static constexpr bool NONMIN_BA = true;
+
+  // EssentialMatrixTwoPointsPlanar::estimateModel
+  // (solver_essential_matrix_two_points_planar.h:92-175): rotation about the
+  // camera's y axis and translation in its x-z plane. With rows
+  // A1 = (y1, -y1 x2) and A2 = (-y2, x1 y2) of the two points, C = -A2^+ A1
+  // maps the rotation direction v1 = (cos a, sin a) onto the direction of
+  // (a - b); |C v1| = 1 gives a quadratic in cos 2a (coefficients from
+  // C^T C), and each root gives the angles +-acos / 2. Models whose entries
+  // are not finite (no real root, or |cos 2a| > 1) are dropped here (the
+  // reference keeps and scores them; they cannot win); the rest pass the
+  // estimator's orientation test on the two points (essential_estimator.h:
+  // 166-172).
+  __device__ static int minimal(const double* pts, const int* s, double* out, const double* = nullptr) {
+    double A1[2][2], A2[2][2];
+    for (int i = 0; i < 2; ++i) {
+      const double* p = pts + 4 * s[i];
+      const double x1 = p[0], y1 = p[1], x2 = p[2], y2 = p[3];
+      A1[i][0] = y1;
+      A1[i][1] = -y1 * x2;
+      A2[i][0] = -y2;
+      A2[i][1] = x1 * y2;
+    }
+    // (A2^T A2)^-1 A2^T
+    const double g00 = A2[0][0] * A2[0][0] + A2[1][0] * A2[1][0];
+    const double g01 = A2[0][0] * A2[0][1] + A2[1][0] * A2[1][1];
+    const double g11 = A2[0][1] * A2[0][1] + A2[1][1] * A2[1][1];
+    const double det = g00 * g11 - g01 * g01;
+    const double i00 = g11 / det, i01 = -g01 / det, i11 = g00 / det;
+    double P[2][2];
+    for (int j = 0; j < 2; ++j) {
+      P[0][j] = i00 * A2[j][0] + i01 * A2[j][1];
+      P[1][j] = i01 * A2[j][0] + i11 * A2[j][1];
+    }
+    double C[2][2];
+    for (int r = 0; r < 2; ++r)
+      for (int c = 0; c < 2; ++c) C[r][c] = -(P[r][0] * A1[0][c] + P[r][1] * A1[1][c]);
+    const double a = C[0][0] * C[0][0] + C[1][0] * C[1][0];
+    const double b = C[0][1] * C[0][0] + C[1][1] * C[1][0];
+    const double c = C[0][1] * C[0][1] + C[1][1] * C[1][1];
+    const double cf1 = 4 * b * b + (a - c) * (a - c);
+    const double cf2 = -2 * (a - c) * (2 - a - c);
+    const double cf3 = (2 - a - c) * (2 - a - c) - 4 * b * b;
+    const double disc = sqrt(cf2 * cf2 - 4 * cf1 * cf3);
+    const double c2a1 = (-cf2 + disc) / (2 * cf1), c2a2 = (-cf2 - disc) / (2 * cf1);
+    const double alphas[4] = {acos(c2a1) / 2, acos(c2a2) / 2, -acos(c2a1) / 2, -acos(c2a2) / 2};
+    int k = 0;
+    for (int q = 0; q < 4; ++q) {
+      double sa, ca;
+      sincos(alphas[q], &sa, &ca);
+      double w0 = C[0][0] * ca + C[0][1] * sa, w1 = C[1][0] * ca + C[1][1] * sa;
+      const double nw = sqrt(w0 * w0 + w1 * w1);
+      w0 /= nw;
+      w1 /= nw;
+      const double al = atan2(sa, ca), amb = atan2(w1, w0);
+      double* E = out + 9 * k;
+      E[0] = 0.0; E[1] = -sin(al); E[2] = 0.0;
+      E[3] = sin(amb); E[4] = 0.0; E[5] = -cos(amb);
+      E[6] = 0.0; E[7] = cos(al); E[8] = 0.0;
+      bool fin = true;
+      for (int e = 0; e < 9; ++e) fin = fin && isfinite(E[e]);
+      if (fin && FundamentalModel::orientation_valid(E, pts, s, 2)) ++k;
+    }
+    return k;
+  }
+
+  // refine_relpose (bundle.cpp:412-452; lm_5dof_impl 176-250) of P over the
+  // rows idx[0..n) with unit weights, by one thread: the same LM as the
+  // CTA-wide refinement, with sequential sums.
+  __device__ static void refine_relpose_thread(const double* pts, const int* idx, int n, ess::Pose& P) {
+    auto residual = [&](const ess::Pose& Q) {
+      double E[9];
+      ess::essential_from_pose(Q, E);
+      double c = 0;
+      for (int k = 0; k < n; ++k) c += ess::relpose_loss(E, pts + 4 * idx[k]);
+      return c;
+    };
+    double lambda = 1e-3;
+    double cost = residual(P);
+    bool recompute = true;
+    double tot[20];
+    ess::PoseJac J;
+    for (int iter = 0; iter < 25; ++iter) {
+      if (recompute) {
+        ess::pose_jacobians(P, J);
+        for (int q = 0; q < 20; ++q) tot[q] = 0;
+        for (int k = 0; k < n; ++k) ess::relpose_accumulate(J, pts + 4 * idx[k], 1.0, n, tot);
+        double gn = 0;
+        for (int a = 0; a < 5; ++a) gn += tot[15 + a] * tot[15 + a];
+        if (sqrt(gn) < 1e-8) break;
+      }
+      constexpr int diag[5] = {0, 2, 5, 9, 14};
+      for (int a = 0; a < 5; ++a) tot[diag[a]] += lambda;
+      ess::Pose Pn;
+      if (!ess::relpose_step(tot, tot + 15, J, P, Pn)) break;
+      const double cn = residual(Pn);
+      if (cn < cost) {
+        P = Pn;
+        lambda /= 10;
+        cost = cn;
+        recompute = true;
+      } else {
+        for (int a = 0; a < 5; ++a) tot[diag[a]] -= lambda;
+        lambda *= 10;
+        recompute = false;
+      }
+    }
+  }
+
+  // Per-thread non-minimal fit of the local-optimisation trials (unit
+  // weights): EssentialMatrixBundleAdjustmentSolver::estimateModel
+  // (solver_essential_matrix_bundle_adjustment.h:114-188), Stewenius, then
+  // every cheirality-consistent pose (checked on the first row) refined, at
+  // most LO_MAXSOL models, each normalised with E33 >= 0.
+  __device__ static int fit_thread_multi(const double* pts, const int* idx, int n, double* out) {
+    if (n < NONMIN) return 0;
+    double init[9 * LO_MAXSOL];
+    const int ni = stewenius_thread(pts, idx, n, init);
+    double x1[3], x2[3];
+    {
+      const double* p0 = pts + 4 * idx[0];
+      x1[0] = p0[0]; x1[1] = p0[1]; x1[2] = 1.0;
+      x2[0] = p0[2]; x2[1] = p0[3]; x2[2] = 1.0;
+      const double n1 = sqrt(x1[0] * x1[0] + x1[1] * x1[1] + 1.0);
+      const double n2 = sqrt(x2[0] * x2[0] + x2[1] * x2[1] + 1.0);
+      for (int i = 0; i < 3; ++i) {
+        x1[i] /= n1;
+        x2[i] /= n2;
+      }
+    }
+    int nout = 0;
+    for (int q = 0; q < ni; ++q) {
+      ess::Pose poses[4];
+      const int np = ess::poses_from_essential(init + 9 * q, x1, x2, poses);
+      for (int v = 0; v < np && nout < LO_MAXSOL; ++v) {
+        ess::Pose P = poses[v];
+        refine_relpose_thread(pts, idx, n, P);
+        ess::essential_from_pose(P, out + 9 * nout);
+        ess::normalise_sign(out + 9 * nout);
+        ++nout;
+      }
+    }
+    return nout;
   }
 };
 

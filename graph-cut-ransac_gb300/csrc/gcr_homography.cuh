@@ -359,4 +359,233 @@ struct HomographyAffineModel : HomographyModel {
   }
 };
 
+// Real roots, in ascending order, of c[0] + c[1] x + ... + c[deg] x^deg
+// (deg <= 4). The roots of the quadratic derivative come in closed form; the
+// roots of each higher derivative, and of the polynomial itself, are then
+// isolated between consecutive roots of the next derivative and the Cauchy
+// bound and bisected to the last representable midpoint. Leading
+// coefficients that are exactly zero lower the degree. Returns the count.
+__device__ inline int poly_quadratic_roots(const double* c, double* roots) {
+  const double disc = c[1] * c[1] - 4.0 * c[2] * c[0];
+  if (disc < 0.0) return 0;
+  const double q = -0.5 * (c[1] + copysign(sqrt(disc), c[1]));
+  double r0 = q / c[2], r1 = q != 0.0 ? c[0] / q : r0;
+  if (r1 < r0) {
+    const double t = r0;
+    r0 = r1;
+    r1 = t;
+  }
+  roots[0] = r0;
+  roots[1] = r1;
+  return 2;
+}
+
+// roots of c (degree deg, c[deg] != 0) given the ascending real roots cp of
+// its derivative
+__device__ inline int poly_bracketed_roots(const double* c, int deg, const double* cp, int ncp, double* roots) {
+  double bound = 0.0;
+  for (int i = 0; i < deg; ++i) bound = fmax(bound, fabs(c[i] / c[deg]));
+  bound += 1.0;
+  auto f = [&](double x) {
+    double v = c[deg];
+    for (int i = deg - 1; i >= 0; --i) v = v * x + c[i];
+    return v;
+  };
+  double edges[6];
+  int ne = 0;
+  edges[ne++] = -bound;
+  for (int i = 0; i < ncp; ++i)
+    if (cp[i] > -bound && cp[i] < bound) edges[ne++] = cp[i];
+  edges[ne++] = bound;
+  int nr = 0;
+  for (int k = 0; k + 1 < ne; ++k) {
+    double lo = edges[k], hi = edges[k + 1];
+    double flo = f(lo);
+    const double fhi = f(hi);
+    if (flo == 0.0) {
+      if (nr == 0 || roots[nr - 1] != lo) roots[nr++] = lo;
+      continue;
+    }
+    if ((flo < 0.0) == (fhi < 0.0)) continue;
+    for (int it = 0; it < 200; ++it) {
+      const double mid = 0.5 * (lo + hi);
+      if (mid <= lo || mid >= hi) break;
+      const double fm = f(mid);
+      if (fm == 0.0) {
+        lo = hi = mid;
+        break;
+      }
+      if ((fm < 0.0) == (flo < 0.0)) {
+        lo = mid;
+        flo = fm;
+      } else {
+        hi = mid;
+      }
+    }
+    roots[nr++] = 0.5 * (lo + hi);
+  }
+  return nr;
+}
+
+__device__ inline int poly_real_roots(const double* c_in, int deg, double* roots) {
+  while (deg > 0 && c_in[deg] == 0.0) --deg;
+  if (deg <= 0) return 0;
+  if (deg == 1) {
+    roots[0] = -c_in[0] / c_in[1];
+    return isfinite(roots[0]) ? 1 : 0;
+  }
+  // lv[j]: the (deg - j)-th derivative, of degree j
+  double lv[5][5];
+  for (int i = 0; i <= deg; ++i) lv[deg][i] = c_in[i];
+  for (int j = deg - 1; j >= 2; --j)
+    for (int i = 0; i <= j; ++i) lv[j][i] = (i + 1) * lv[j + 1][i + 1];
+  double cur[4], nxt[4];
+  int n = poly_quadratic_roots(lv[2], cur);
+  for (int j = 3; j <= deg; ++j) {
+    n = poly_bracketed_roots(lv[j], j, cur, n, nxt);
+    for (int i = 0; i < n; ++i) cur[i] = nxt[i];
+  }
+  for (int i = 0; i < n; ++i) roots[i] = cur[i];
+  return n;
+}
+
+// SIFT-correspondence homography (findHomographySIFT_,
+// gcransac_python.cpp:4813-5069): rows (x1, y1, x2, y2, q1, q2, o1, o2) with
+// the features' scales q and orientations o; the point estimator
+// (RobustHomographyEstimator: residual, validity, the 4-point non-minimal
+// fit) with the two-correspondence minimal solver HomographyTwoSIFTSolver
+// (solver_homography_two_sift.h:113-480).
+struct HomographySiftModel : HomographyModel {
+  static constexpr int M = 2;
+  static constexpr int MAXSOL = 4;  // conic intersections
+  static constexpr int INLIER_LIMIT = 7 * M;
+  static constexpr int SAMPLE_CAP = INLIER_LIMIT;
+  static constexpr bool AFFINE = true;
+
+  // isValidSample (homography_estimator.h:350-351): samples of fewer than
+  // four correspondences are not tested
+  __device__ static bool valid_sample_affine(const double*, const double*, const int*) { return true; }
+
+  // Each correspondence gives its two point rows and one orientation row
+  // (J o1 parallel to o2 for the homography's Jacobian J at x1): a 6 x 9
+  // system with a three-dimensional null space. Each correspondence's scale
+  // ratio then gives a quadratic form in the null-space coordinates,
+  // q2 w(h)^2 - q1 D(h) = 0 with w = h7 x1 + h8 y1 + h9 and
+  // D = (h1 h5 - h2 h4) + x2 (h4 h8 - h5 h7) + y2 (h2 h7 - h1 h8)
+  // (w^2 det J); the two conics meet in up to four points. The reference
+  // takes the null space from an SVD and intersects the conics by an
+  // elimination template and a 4 x 4 eigenproblem; here the null space comes
+  // from Gaussian elimination with full pivoting over h1..h8 (h9 stays free,
+  // so its basis vector carries h9 = 1 and the others h9 = 0), and the
+  // intersections from the resultant quartic in the second coordinate, whose
+  // real roots are isolated by bisection; the first coordinate follows
+  // linearly. Models come in ascending order of that root, each with h9 = 1.
+  __device__ static int minimal_affine(const double* pts, const double* aux, const int* s, double* out) {
+    double A[6][9];
+    double u1[2], v1[2], u2[2], v2[2], q1[2], q2[2];
+    for (int c = 0; c < 2; ++c) {
+      const double* p = pts + 4 * s[c];
+      const double* f = aux + 4 * s[c];
+      u1[c] = p[0]; v1[c] = p[1]; u2[c] = p[2]; v2[c] = p[3];
+      q1[c] = f[0]; q2[c] = f[1];
+      double s1, c1, s2, c2;
+      sincos(f[2], &s1, &c1);
+      sincos(f[3], &s2, &c2);
+      double* r = A[3 * c];
+      r[0] = 0.0; r[1] = 0.0; r[2] = 0.0; r[3] = u1[c]; r[4] = v1[c]; r[5] = 1.0;
+      r[6] = -u1[c] * v2[c]; r[7] = -v1[c] * v2[c]; r[8] = -v2[c];
+      r = A[3 * c + 1];
+      r[0] = u1[c]; r[1] = v1[c]; r[2] = 1.0; r[3] = 0.0; r[4] = 0.0; r[5] = 0.0;
+      r[6] = -u1[c] * u2[c]; r[7] = -v1[c] * u2[c]; r[8] = -u2[c];
+      r = A[3 * c + 2];
+      r[0] = -c1 * s2; r[1] = -s1 * s2; r[2] = 0.0; r[3] = c1 * c2; r[4] = s1 * c2; r[5] = 0.0;
+      r[6] = u2[c] * c1 * s2 - v2[c] * c1 * c2; r[7] = u2[c] * s1 * s2 - v2[c] * s1 * c2; r[8] = 0.0;
+    }
+    // elimination with full pivoting over columns 0..7
+    int col_of[6];
+    bool used[8] = {false, false, false, false, false, false, false, false};
+    for (int k = 0; k < 6; ++k) {
+      int pr = -1, pc = -1;
+      double best = 0.0;
+      for (int r = k; r < 6; ++r)
+        for (int c = 0; c < 8; ++c)
+          if (!used[c] && fabs(A[r][c]) > best) { best = fabs(A[r][c]); pr = r; pc = c; }
+      if (!(best > 0.0)) return 0;
+      if (pr != k)
+        for (int j = 0; j < 9; ++j) { const double t = A[pr][j]; A[pr][j] = A[k][j]; A[k][j] = t; }
+      used[pc] = true;
+      col_of[k] = pc;
+      const double inv = 1.0 / A[k][pc];
+      for (int j = 0; j < 9; ++j) A[k][j] *= inv;
+      for (int r = 0; r < 6; ++r) {
+        if (r == k) continue;
+        const double fct = A[r][pc];
+        if (fct != 0.0)
+          for (int j = 0; j < 9; ++j) A[r][j] -= fct * A[k][j];
+      }
+    }
+    int fr[3];
+    int nf = 0;
+    for (int c = 0; c < 8; ++c)
+      if (!used[c]) fr[nf++] = c;
+    fr[2] = 8;
+    // basis vectors: N[b] has 1 at free column fr[b], 0 at the other free
+    // columns, and -A[k][fr[b]] at pivot column col_of[k]
+    double N[3][9];
+    for (int b = 0; b < 3; ++b) {
+      for (int j = 0; j < 9; ++j) N[b][j] = 0.0;
+      N[b][fr[b]] = 1.0;
+      for (int k = 0; k < 6; ++k) N[b][col_of[k]] = -A[k][fr[b]];
+    }
+    // conic of each correspondence in (a, b) for h = a N0 + b N1 + N2:
+    // k[0] a^2 + k[1] a b + k[2] b^2 + k[3] a + k[4] b + k[5]
+    double K[2][6];
+    for (int c = 0; c < 2; ++c) {
+      auto form = [&](const double* x, const double* y) {
+        const double wx = x[6] * u1[c] + x[7] * v1[c] + x[8];
+        const double wy = y[6] * u1[c] + y[7] * v1[c] + y[8];
+        const double dxy = 0.5 * ((x[0] * y[4] + y[0] * x[4] - x[1] * y[3] - y[1] * x[3]) +
+                                  u2[c] * (x[3] * y[7] + y[3] * x[7] - x[4] * y[6] - y[4] * x[6]) +
+                                  v2[c] * (x[1] * y[6] + y[1] * x[6] - x[0] * y[7] - y[0] * x[7]));
+        return q2[c] * wx * wy - q1[c] * dxy;
+      };
+      K[c][0] = form(N[0], N[0]);
+      K[c][1] = 2.0 * form(N[0], N[1]);
+      K[c][2] = form(N[1], N[1]);
+      K[c][3] = 2.0 * form(N[0], N[2]);
+      K[c][4] = 2.0 * form(N[1], N[2]);
+      K[c][5] = form(N[2], N[2]);
+    }
+    // as quadratics in a: A_c a^2 + (K1 b + K3) a + (K2 b^2 + K4 b + K5);
+    // resultant (A1 C2 - A2 C1)^2 - (A1 B2 - A2 B1)(B1 C2 - B2 C1)
+    const double a1 = K[0][0], a2 = K[1][0];
+    const double p2 = a1 * K[1][2] - a2 * K[0][2], p1 = a1 * K[1][4] - a2 * K[0][4], p0 = a1 * K[1][5] - a2 * K[0][5];
+    const double l1 = a1 * K[1][1] - a2 * K[0][1], l0 = a1 * K[1][3] - a2 * K[0][3];
+    const double k3 = K[0][1] * K[1][2] - K[1][1] * K[0][2];
+    const double k2 = K[0][1] * K[1][4] + K[0][3] * K[1][2] - K[1][1] * K[0][4] - K[1][3] * K[0][2];
+    const double k1 = K[0][1] * K[1][5] + K[0][3] * K[1][4] - K[1][1] * K[0][5] - K[1][3] * K[0][4];
+    const double k0 = K[0][3] * K[1][5] - K[1][3] * K[0][5];
+    const double r[5] = {p0 * p0 - l0 * k0, 2.0 * p1 * p0 - (l1 * k0 + l0 * k1),
+                         p1 * p1 + 2.0 * p2 * p0 - (l1 * k1 + l0 * k2), 2.0 * p2 * p1 - (l1 * k2 + l0 * k3),
+                         p2 * p2 - l1 * k3};
+    double roots[4];
+    const int nr = poly_real_roots(r, 4, roots);
+    int nm = 0;
+    for (int i = 0; i < nr; ++i) {
+      const double b = roots[i];
+      // A2 Q1 - A1 Q2 = -(L(b) a + P(b)) = 0
+      const double L = l1 * b + l0, P = (p2 * b + p1) * b + p0;
+      const double a = -P / L;
+      double* h = out + 9 * nm;
+      bool fin = true;
+      for (int j = 0; j < 9; ++j) {
+        h[j] = a * N[0][j] + b * N[1][j] + N[2][j];
+        fin = fin && isfinite(h[j]);
+      }
+      if (fin) ++nm;
+    }
+    return nm;
+  }
+};
+
 }  // namespace gcr

@@ -32,6 +32,8 @@ const KindOps* essential_ops();
 const KindOps* homography_affine_ops();   // affine correspondences (gcr_kind_ha.cu)
 const KindOps* fundamental_affine_ops();  // affine correspondences (gcr_kind_fa.cu)
 const KindOps* fundamental_sift_ops();    // SIFT correspondences (gcr_kind_fs.cu)
+const KindOps* homography_sift_ops();     // SIFT correspondences (gcr_kind_hs.cu)
+const KindOps* essential_planar_ops();    // planar motion (gcr_kind_ep.cu)
 
 struct PairDesc;
 struct PairAux;

@@ -201,6 +201,8 @@ extern "C" gcr_status gcr_find_homography_device_noalloc(const double* d_corr, i
   prm.pp_h = nullptr;
   prm.use_sprt = p.use_sprt ? 1 : 0;
   prm.use_sp = p.use_space_partitioning ? 1 : 0;
+  prm.gc_max = 10;      // GCRANSAC's default max_graph_cut_number
+  prm.final_irls = 1;   // and do_final_iterated_least_squares
   prm.epilogue = 1;
   prm.batch_calls = GCR_BLOCK;
   prm.lo_fp32 = 0;

@@ -14,7 +14,8 @@ import numpy as np
 
 from . import _abi
 
-__all__ = ["findHomography", "findFundamentalMatrix", "findEssentialMatrix", "find_batch", "default_params",
+__all__ = ["findHomography", "findFundamentalMatrix", "findEssentialMatrix", "findPlanarEssentialMatrix", "find_batch",
+           "default_params",
            "GCRError"]
 
 
@@ -119,10 +120,17 @@ class _SampleTape:
 
 
 _SAMPLE_SIZE = {_abi.GCR_HOMOGRAPHY: 4, _abi.GCR_FUNDAMENTAL: 7, _abi.GCR_ESSENTIAL: 5,
-                _abi.GCR_HOMOGRAPHY_AFFINE: 2, _abi.GCR_FUNDAMENTAL_AFFINE: 3, _abi.GCR_FUNDAMENTAL_SIFT: 4}
+                _abi.GCR_HOMOGRAPHY_AFFINE: 2, _abi.GCR_FUNDAMENTAL_AFFINE: 3, _abi.GCR_FUNDAMENTAL_SIFT: 4,
+                _abi.GCR_HOMOGRAPHY_SIFT: 2, _abi.GCR_ESSENTIAL_PLANAR: 2}
 _ENTRY_NAME = {_abi.GCR_HOMOGRAPHY: "findHomography", _abi.GCR_FUNDAMENTAL: "findFundamentalMatrix",
                _abi.GCR_ESSENTIAL: "findEssentialMatrix", _abi.GCR_HOMOGRAPHY_AFFINE: "findHomography",
-               _abi.GCR_FUNDAMENTAL_AFFINE: "findFundamentalMatrix", _abi.GCR_FUNDAMENTAL_SIFT: "findFundamentalMatrix"}
+               _abi.GCR_FUNDAMENTAL_AFFINE: "findFundamentalMatrix", _abi.GCR_FUNDAMENTAL_SIFT: "findFundamentalMatrix",
+               _abi.GCR_HOMOGRAPHY_SIFT: "findHomography", _abi.GCR_ESSENTIAL_PLANAR: "findPlanarEssentialMatrix"}
+# entry points of the kinds with rows of 8 (same signature as gcr_find_homography)
+_ROWS8_ENTRY = {_abi.GCR_HOMOGRAPHY_AFFINE: "gcr_find_homography_affine",
+                _abi.GCR_HOMOGRAPHY_SIFT: "gcr_find_homography_sift",
+                _abi.GCR_FUNDAMENTAL_AFFINE: "gcr_find_fundamental_affine",
+                _abi.GCR_FUNDAMENTAL_SIFT: "gcr_find_fundamental_sift"}
 
 
 def _run_one(kind, corr, size, params, K1=None, K2=None, return_stats=False, probabilities=None, sample_tape=None):
@@ -142,23 +150,18 @@ def _run_one_(kind, corr, size, params, K1=None, K2=None, return_stats=False, pr
     if kind == _abi.GCR_HOMOGRAPHY:
         rc = lib.gcr_find_homography(_abi.ptr(corr), n, ctypes.byref(sz), _abi.ptr(prob), ctypes.byref(params),
                                      _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
-    elif kind == _abi.GCR_HOMOGRAPHY_AFFINE:
-        rc = lib.gcr_find_homography_affine(_abi.ptr(corr), n, ctypes.byref(sz), _abi.ptr(prob),
-                                            ctypes.byref(params), _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
-    elif kind == _abi.GCR_FUNDAMENTAL_SIFT:
-        rc = lib.gcr_find_fundamental_sift(_abi.ptr(corr), n, ctypes.byref(sz), _abi.ptr(prob),
-                                           ctypes.byref(params), _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
-    elif kind == _abi.GCR_FUNDAMENTAL_AFFINE:
-        rc = lib.gcr_find_fundamental_affine(_abi.ptr(corr), n, ctypes.byref(sz), _abi.ptr(prob),
-                                             ctypes.byref(params), _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
+    elif kind in _ROWS8_ENTRY:
+        rc = getattr(lib, _ROWS8_ENTRY[kind])(_abi.ptr(corr), n, ctypes.byref(sz), _abi.ptr(prob),
+                                              ctypes.byref(params), _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
     elif kind == _abi.GCR_FUNDAMENTAL:
         rc = lib.gcr_find_fundamental(_abi.ptr(corr), n, ctypes.byref(sz), _abi.ptr(prob), ctypes.byref(params),
                                       _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
     else:
         K1 = np.ascontiguousarray(K1, np.float64).reshape(9)
         K2 = np.ascontiguousarray(K2, np.float64).reshape(9)
-        rc = lib.gcr_find_essential(_abi.ptr(corr), n, _abi.ptr(K1), _abi.ptr(K2), ctypes.byref(sz), _abi.ptr(prob),
-                                    ctypes.byref(params), _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
+        entry = lib.gcr_find_essential_planar if kind == _abi.GCR_ESSENTIAL_PLANAR else lib.gcr_find_essential
+        rc = entry(_abi.ptr(corr), n, _abi.ptr(K1), _abi.ptr(K2), ctypes.byref(sz), _abi.ptr(prob),
+                   ctypes.byref(params), _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
     _raise_for(rc, _ENTRY_NAME[kind])
     maskb = mask.astype(bool)
     out = (None if rc == _abi.GCR_NO_MODEL or maskb.sum() == 0 else model.reshape(3, 3), maskb)
@@ -171,21 +174,24 @@ def findHomography(correspondences, h1, w1, h2, w2, probabilities=None, threshol
                    use_space_partitioning=True, lo_number=50, sampler_variance=0.1, solver=0, seed=0,
                    return_stats=False, sample_tape=None):
     """Robust homography by Graph-Cut RANSAC (reference: bindings.cpp:859-983).
-    solver 0: point correspondences [n, 4]; solver 2: affine correspondences
-    [n, 8] (x1, y1, x2, y2, a11, a12, a21, a22), two per minimal sample
-    (findHomographyAC_, gcransac_python.cpp:4553-4811; its driver takes
-    samplers 0, 1, 3, 4 and no space partitioning). `sample_tape` [calls, m]
-    replays recorded minimal samples in place of the main sampler's draws
-    (gcr_set_sample_tape)."""
-    if solver == 2:
+    solver 0: point correspondences [n, 4]; solver 1: SIFT correspondences
+    [n, 8] (x1, y1, x2, y2, q1, q2, o1, o2: scales and orientations), two per
+    minimal sample (findHomographySIFT_, gcransac_python.cpp:4813-5069);
+    solver 2: affine correspondences [n, 8] (x1, y1, x2, y2, a11, a12, a21,
+    a22), two per minimal sample (findHomographyAC_, :4553-4811); both
+    drivers take samplers 0, 1, 3, 4 and no space partitioning.
+    `sample_tape` [calls, m] replays recorded minimal samples in place of the
+    main sampler's draws (gcr_set_sample_tape)."""
+    if solver in (1, 2):
+        kind = _abi.GCR_HOMOGRAPHY_SIFT if solver == 1 else _abi.GCR_HOMOGRAPHY_AFFINE
         c = _check_corr(correspondences, 4, "homography", cols=8)
-        p = _params(_abi.GCR_HOMOGRAPHY_AFFINE, threshold, conf, spatial_coherence_weight, max_iters, min_iters,
+        p = _params(kind, threshold, conf, spatial_coherence_weight, max_iters, min_iters,
                     use_sprt, sampler, neighborhood, neighborhood_size, lo_number, False, seed,
                     min_inlier_ratio_for_sprt=min_inlier_ratio_for_sprt, sampler_variance=sampler_variance)
-        return _run_one(_abi.GCR_HOMOGRAPHY_AFFINE, c, (h1, w1, h2, w2), p, return_stats=return_stats,
+        return _run_one(kind, c, (h1, w1, h2, w2), p, return_stats=return_stats,
                         probabilities=probabilities, sample_tape=sample_tape)
     if solver != 0:
-        raise NotImplementedError("SIFT correspondences (solver=1) are not provided; solver 0 and 2 are")
+        raise NotImplementedError(f"solver {solver} is not provided (0 points, 1 SIFT, 2 affine)")
     c = _check_corr(correspondences, 4, "homography")
     p = _params(_abi.GCR_HOMOGRAPHY, threshold, conf, spatial_coherence_weight, max_iters, min_iters, use_sprt,
                 sampler, neighborhood, neighborhood_size, lo_number, use_space_partitioning, seed,
@@ -239,6 +245,24 @@ def findEssentialMatrix(correspondences, K1, K2, h1, w1, h2, w2, probabilities=N
                 sampler, neighborhood, neighborhood_size, lo_number, False, seed,
                 min_inlier_ratio_for_sprt=min_inlier_ratio_for_sprt, sampler_variance=sampler_variance)
     return _run_one(_abi.GCR_ESSENTIAL, c, (h1, w1, h2, w2), p, K1=K1, K2=K2, return_stats=return_stats,
+                    probabilities=probabilities, sample_tape=sample_tape)
+
+
+def findPlanarEssentialMatrix(correspondences, K1, K2, h1, w1, h2, w2, probabilities=None, threshold=1.0, conf=0.99,
+                              spatial_coherence_weight=0.975, max_iters=10000, min_iters=50, use_sprt=True,
+                              min_inlier_ratio_for_sprt=0.00001, sampler=1, neighborhood=1, lo_number=50,
+                              neighborhood_size=20.0, seed=0, return_stats=False, sample_tape=None):
+    """Essential matrix of a planar camera motion (rotation about the
+    camera's y axis, translation in its x-z plane) by Graph-Cut RANSAC
+    (reference: bindings.cpp:610-707, 1114-1133; findPlanarEssentialMatrix_,
+    gcransac_python.cpp:3531-3870): rows [n, 4] of pixels, n >= 3, two per
+    minimal sample; MSAC; the AR sampler's variance is 0.1. `sample_tape`
+    [calls, 2] replays recorded minimal samples."""
+    c = _check_corr(correspondences, 3, "planar essential")
+    p = _params(_abi.GCR_ESSENTIAL_PLANAR, threshold, conf, spatial_coherence_weight, max_iters, min_iters, use_sprt,
+                sampler, neighborhood, neighborhood_size, lo_number, False, seed,
+                min_inlier_ratio_for_sprt=min_inlier_ratio_for_sprt, sampler_variance=0.1)
+    return _run_one(_abi.GCR_ESSENTIAL_PLANAR, c, (h1, w1, h2, w2), p, K1=K1, K2=K2, return_stats=return_stats,
                     probabilities=probabilities, sample_tape=sample_tape)
 
 

@@ -44,6 +44,8 @@ GCR_ESSENTIAL = 2
 GCR_HOMOGRAPHY_AFFINE = 3  # rows of 8: points, then the local affine map
 GCR_FUNDAMENTAL_AFFINE = 4  # rows of 8
 GCR_FUNDAMENTAL_SIFT = 5  # rows of 8: points, then scales and orientations (q1, q2, o1, o2)
+GCR_HOMOGRAPHY_SIFT = 6  # rows of 8: points, then scales and orientations (q1, q2, o1, o2)
+GCR_ESSENTIAL_PLANAR = 7  # rows of 4; planar camera motion
 
 GCR_FLAG_LO_APPLIED = 1
 GCR_FLAG_IRLS_APPLIED = 2
@@ -113,6 +115,8 @@ _EXPORTS = {
     "gcr_find_homography_affine": (ctypes.c_int, [_P, ctypes.c_int64, _P, _P, _P, _P, _P, _P]),
     "gcr_find_fundamental_affine": (ctypes.c_int, [_P, ctypes.c_int64, _P, _P, _P, _P, _P, _P]),
     "gcr_find_fundamental_sift": (ctypes.c_int, [_P, ctypes.c_int64, _P, _P, _P, _P, _P, _P]),
+    "gcr_find_homography_sift": (ctypes.c_int, [_P, ctypes.c_int64, _P, _P, _P, _P, _P, _P]),
+    "gcr_find_essential_planar": (ctypes.c_int, [_P, ctypes.c_int64, _P, _P, _P, _P, _P, _P, _P, _P]),
     "gcr_find_batch": (ctypes.c_int, [ctypes.c_int, ctypes.c_int64, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "gcr_context_create": (ctypes.c_int, [_P]),
     "gcr_context_destroy": (ctypes.c_int, [_P]),

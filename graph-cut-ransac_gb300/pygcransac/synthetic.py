@@ -110,6 +110,34 @@ def homography_affine_pair(seed, n=2000, inlier_ratio=0.4, sigma=1.0, affine_sig
                 size=pr["size"])
 
 
+def homography_sift_pair(seed, n=2000, inlier_ratio=0.4, sigma=1.0, angle_sigma=0.01, scale_sigma=0.01, w=W, h=H):
+    """SIFT-like correspondences of a homography: the point pairs of
+    homography_pair and, per row, the features' scales and orientations
+    (q1, q2, o1, o2). For an inlier, o1 ~ U(-pi, pi) and q1 ~ U(1, 5); the
+    Jacobian J of the true homography at x1 gives o2 = the direction of
+    J (cos o1, sin o1) and q2 = q1 det J (the scale equation of the
+    two-SIFT homography solver); o2 and q2 then get N(0, angle_sigma) and
+    relative N(0, scale_sigma) noise. Outliers have independent q ~ U(1, 5)
+    and o ~ U(-pi, pi). Returns dict(corr [n, 8], H_gt, inlier_gt, size)."""
+    pr = homography_pair(seed, n=n, inlier_ratio=inlier_ratio, sigma=sigma, w=w, h=h)
+    rng = _rng(seed + 15485863)
+    corr = pr["corr"]
+    J = homography_jacobian(pr["H_gt"], corr[:, :2])
+    o1 = rng.uniform(-np.pi, np.pi, n)
+    q1 = rng.uniform(1.0, 5.0, n)
+    vx = J[:, 0] * np.cos(o1) + J[:, 1] * np.sin(o1)
+    vy = J[:, 2] * np.cos(o1) + J[:, 3] * np.sin(o1)
+    o2 = np.arctan2(vy, vx) + rng.normal(0, angle_sigma, n)
+    q2 = q1 * (J[:, 0] * J[:, 3] - J[:, 1] * J[:, 2]) * (1.0 + rng.normal(0, scale_sigma, n))
+    out = ~pr["inlier_gt"]
+    k = int(out.sum())
+    o1[out] = rng.uniform(-np.pi, np.pi, k)
+    o2[out] = rng.uniform(-np.pi, np.pi, k)
+    q1[out] = rng.uniform(1.0, 5.0, k)
+    q2[out] = rng.uniform(1.0, 5.0, k)
+    return dict(pr, corr=np.ascontiguousarray(np.c_[corr, q1, q2, o1, o2]))
+
+
 def intrinsics(f=800.0, w=W, h=H):
     return np.array([[f, 0, w / 2], [0, f, h / 2], [0, 0, 1.0]])
 
@@ -136,17 +164,25 @@ def depth_field(rng, w=W, h=H):
 
 
 def two_view_pair(seed, n=5000, inlier_ratio=0.25, sigma=0.5, f=800.0, w=W, h=H, max_angle_deg=30.0,
-                  smooth_depth=False):
-    """Returns dict(corr [n,4] pixels, K, R, t, F_gt, E_gt, inlier_gt, size)."""
+                  smooth_depth=False, planar_motion=False):
+    """Returns dict(corr [n,4] pixels, K, R, t, F_gt, E_gt, inlier_gt, size).
+    planar_motion: rotation about the camera's y axis by up to max_angle_deg
+    and a unit translation in its x-z plane (the motion model of the planar
+    essential-matrix solver)."""
     rng = _rng(seed)
     Zf = depth_field(rng, w, h) if smooth_depth else None
     K = intrinsics(f, w, h)
     Ki = np.linalg.inv(K)
     ni = int(round(n * inlier_ratio))
     for _attempt in range(100):
-        R = _rot(rng.normal(size=3), np.deg2rad(rng.uniform(-max_angle_deg, max_angle_deg)))
-        t = rng.normal(size=3)
-        t /= np.linalg.norm(t)
+        if planar_motion:
+            R = _rot(np.array([0.0, 1.0, 0.0]), np.deg2rad(rng.uniform(-max_angle_deg, max_angle_deg)))
+            phi = rng.uniform(-np.pi, np.pi)
+            t = np.array([np.sin(phi), 0.0, np.cos(phi)])
+        else:
+            R = _rot(rng.normal(size=3), np.deg2rad(rng.uniform(-max_angle_deg, max_angle_deg)))
+            t = rng.normal(size=3)
+            t /= np.linalg.norm(t)
         pts1 = np.zeros((0, 2))
         pts2 = np.zeros((0, 2))
         tries = 0

@@ -48,16 +48,19 @@ typedef enum gcr_status {
  * local affine map (a11, a12, a21, a22) of the affine correspondence, the
  * layout of the reference's findHomographyAC_ and findFundamentalMatrixAC_
  * (gcransac_python.cpp:4553, 1924; solver = 2 of the python findHomography and
- * findFundamentalMatrix); for GCR_FUNDAMENTAL_SIFT the point pair followed by
- * the features' scales and orientations (q1, q2, o1, o2), the layout of
- * findFundamentalMatrixSIFT_ (:2222; solver = 1 of findFundamentalMatrix). */
+ * findFundamentalMatrix); for the SIFT kinds the point pair followed by the
+ * features' scales and orientations (q1, q2, o1, o2), the layout of
+ * findFundamentalMatrixSIFT_ and findHomographySIFT_ (:2222, 4813; solver = 1
+ * of findFundamentalMatrix and findHomography). */
 typedef enum gcr_model_kind {
   GCR_HOMOGRAPHY = 0,
   GCR_FUNDAMENTAL = 1,
   GCR_ESSENTIAL = 2,
   GCR_HOMOGRAPHY_AFFINE = 3,
   GCR_FUNDAMENTAL_AFFINE = 4,
-  GCR_FUNDAMENTAL_SIFT = 5
+  GCR_FUNDAMENTAL_SIFT = 5,
+  GCR_HOMOGRAPHY_SIFT = 6,
+  GCR_ESSENTIAL_PLANAR = 7  /* rows of 4; planar camera motion */
 } gcr_model_kind;
 
 /* Sampler ids follow examples/gcransac_parameter_types.py:8-12 of the reference. */
@@ -177,6 +180,32 @@ gcr_status gcr_find_fundamental_affine(const double* corr, int64_t n, const gcr_
 gcr_status gcr_find_fundamental_sift(const double* corr, int64_t n, const gcr_image_size* size,
                                      const double* probabilities, const gcr_params* params, double* model_out9,
                                      uint8_t* mask_out, gcr_stats* stats_out);
+
+/* Essential matrix of a planar camera motion (rotation about the camera's y
+ * axis, translation in its x-z plane) on one image pair
+ * (findPlanarEssentialMatrix_, gcransac_python.cpp:3531-3870; python
+ * findPlanarEssentialMatrix): rows of 4 pixels, K1 and K2 as for
+ * gcr_find_essential. Two correspondences per minimal sample
+ * (solver_essential_matrix_two_points_planar.h:92-175, up to four models);
+ * the non-minimal solver is the essential-matrix bundle adjustment (Stewenius
+ * start, every cheirality-consistent pose refined, at least 6 rows); MSAC
+ * only; with use_sprt the run makes up to 100 graph cuts and skips the final
+ * iteratively reweighted fit (3741-3742); the AR sampler's variance is 0.1;
+ * the driver's epilogue as for gcr_find_essential. */
+gcr_status gcr_find_essential_planar(const double* corr, int64_t n, const double* K1, const double* K2,
+                                     const gcr_image_size* size, const double* probabilities, const gcr_params* params,
+                                     double* model_out9, uint8_t* mask_out, gcr_stats* stats_out);
+
+/* SIFT-correspondence homography on one image pair (findHomographySIFT_,
+ * gcransac_python.cpp:4813-5069; python findHomography with solver = 1): rows
+ * (x1, y1, x2, y2, q1, q2, o1, o2); two correspondences per minimal sample
+ * (two point rows and one orientation row each, then the two scale-ratio
+ * conics on the null space, solver_homography_two_sift.h:113-480, up to four
+ * models); samplers 0, 1, 3, 4, MSAC, no space partitioning, SPRT from the
+ * inlier ratio 0.01. Other arguments as for gcr_find_homography. */
+gcr_status gcr_find_homography_sift(const double* corr, int64_t n, const gcr_image_size* size,
+                                    const double* probabilities, const gcr_params* params, double* model_out9,
+                                    uint8_t* mask_out, gcr_stats* stats_out);
 
 /* Many image pairs of one model kind in one device launch, host buffers.
  *   corr        concatenated correspondences, offsets[num_pairs] rows in total

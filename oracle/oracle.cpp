@@ -88,7 +88,8 @@ static std::unique_ptr<Grid> make_grid(const Mat& pixel_pts, const gcr_image_siz
 template <class Est, template <class> class Scoring>
 static int run_generic(const Mat& run_pts, const Mat& pixel_pts, const Est& est, const gcr_params& p,
                        const gcr_image_size& sz, uint64_t seed, const Grid* grid, double threshold,
-                       Model& model, std::vector<size_t>& inliers, gcr_stats* st, double mag_threshold) {
+                       Model& model, std::vector<size_t>& inliers, gcr_stats* st, double mag_threshold,
+                       size_t max_graph_cuts = 10, bool final_irls = true) {
   auto main_s = make_main_sampler(p, pixel_pts, Est::sample_size(), sz, seed);
   if (!main_s) return GCR_UNSUPPORTED;
   UniformSampler lo_s(seed, STREAM_LO);
@@ -96,6 +97,8 @@ static int run_generic(const Mat& run_pts, const Mat& pixel_pts, const Est& est,
   fill_settings(g.settings, p);
   g.sprt_seed = seed;
   g.settings.threshold = threshold;
+  g.settings.max_graph_cut_number = max_graph_cuts;
+  g.settings.do_final_iterated_least_squares = final_irls;
   if constexpr (std::is_same<Scoring<Est>, MAGSACScoring<Est>>::value) g.scoring.threshold = mag_threshold;
   const bool ok = g.run(run_pts, est, main_s.get(), &lo_s, grid, model);
   if (st) {
@@ -145,14 +148,16 @@ static int find_homography(const double* corr, int64_t n, const gcr_image_size& 
   return rc;
 }
 
-// findHomographyAC_ (gcransac_python.cpp:4553-4811): rows of eight values
-// (points and local affine maps). The neighbourhood is built on the point
+// findHomographyAC_ and findHomographySIFT_ (gcransac_python.cpp:4553-4811,
+// 4813-5069): rows of eight values (points, then the local affine maps or the
+// features' scales and orientations). The neighbourhood is built on the point
 // columns only when the spatial weight is above machine epsilon, with cells
 // w / n (no padding), or as the radius graph; samplers 0, 1, 3 and 4 (the
-// driver refuses P-NAPSAC); MSAC; SPRT from the default inlier ratio 0.01
-// (4719-4721); no space partitioning and no epilogue.
-static int find_homography_affine(const double* corr, int64_t n, const gcr_image_size& sz, const gcr_params& p_in,
-                                  uint64_t seed, double* model_out, uint8_t* mask, gcr_stats* st) {
+// drivers refuse P-NAPSAC); MSAC; SPRT from the default inlier ratio 0.01
+// (4719-4721, 4979-4981); no space partitioning and no epilogue.
+template <class Est>
+static int find_homography_rows8(const double* corr, int64_t n, const gcr_image_size& sz, const gcr_params& p_in,
+                                 uint64_t seed, double* model_out, uint8_t* mask, gcr_stats* st) {
   if (n < 2) return GCR_TOO_FEW_POINTS;
   if (p_in.sampler == GCR_SAMPLER_PNAPSAC || p_in.scoring != GCR_SCORING_MSAC) return GCR_UNSUPPORTED;
   gcr_params p = p_in;
@@ -169,11 +174,11 @@ static int find_homography_affine(const double* corr, int64_t n, const gcr_image
       grid = std::make_unique<Grid>(pts, cs, nd);
     }
   }
-  HomographyAffineEstimator est;
+  Est est;
   Model model{};
   std::vector<size_t> inl;
-  const int rc = run_generic<HomographyAffineEstimator, MSACScoring>(pts, pts, est, p, sz, seed, grid.get(),
-                                                                     p.threshold, model, inl, st, p.threshold);
+  const int rc = run_generic<Est, MSACScoring>(pts, pts, est, p, sz, seed, grid.get(), p.threshold, model, inl, st,
+                                               p.threshold);
   std::memset(mask, 0, (size_t)n);
   for (size_t i : inl) mask[i] = 1;
   if (st) st->inlier_number = (int64_t)inl.size();
@@ -324,11 +329,25 @@ static int find_fundamental_rows8(const double* corr, int64_t n, const gcr_image
 // weights by point index (the reference indexes an inlier-sized array by
 // point index there); the weights are placed at the inliers' point indices,
 // so both steps see the weight of each inlier.
-static int find_essential(const double* corr, int64_t n, const double* K1, const double* K2,
-                          const gcr_image_size& sz, const gcr_params& p, uint64_t seed, double* model_out,
-                          uint8_t* mask, gcr_stats* st) {
-  if (n < 5) return GCR_TOO_FEW_POINTS;
+//
+// findPlanarEssentialMatrix_ (gcransac_python.cpp:3531-3870) is the same
+// driver with the planar estimator: MSAC only, the AR sampler's variance
+// fixed at 0.1 (3675), and with SPRT up to 100 graph cuts and no final
+// iteratively reweighted fit (3741-3742).
+template <class Est>
+static int find_essential_kind(const double* corr, int64_t n, const double* K1, const double* K2,
+                               const gcr_image_size& sz, const gcr_params& p_in, uint64_t seed, double* model_out,
+                               uint8_t* mask, gcr_stats* st) {
+  constexpr bool planar = std::is_same<Est, EssentialPlanarEstimator>::value;
+  if (n < (int64_t)Est::sample_size()) return GCR_TOO_FEW_POINTS;
   if (!K1 || !K2) return GCR_INVALID_ARG;
+  gcr_params p = p_in;
+  if (planar) {
+    if (p.scoring != GCR_SCORING_MSAC) return GCR_UNSUPPORTED;
+    p.sampler_variance = 0.1;
+  }
+  const size_t gc_max = planar && p.use_sprt ? 100 : 10;
+  const bool final_irls = !(planar && p.use_sprt);
   const Mat pix{corr, n, 4};
   double Ki1[9], Ki2[9];
   inverse3(K1, Ki1);
@@ -354,16 +373,16 @@ static int find_essential(const double* corr, int64_t n, const double* K1, const
       grid = std::make_unique<Grid>(pix, cs, nd);
     }
   }
-  EssentialEstimator est;
+  Est est;
   Model model{};
   std::vector<size_t> inl;
   int rc;
   if (p.scoring == GCR_SCORING_MAGSAC)
-    rc = run_generic<EssentialEstimator, MAGSACScoring>(pts, pix, est, p, sz, seed, grid.get(), thr, model, inl,
-                                                        st, thr);
+    rc = run_generic<Est, MAGSACScoring>(pts, pix, est, p, sz, seed, grid.get(), thr, model, inl, st, thr, gc_max,
+                                         final_irls);
   else
-    rc = run_generic<EssentialEstimator, MSACScoring>(pts, pix, est, p, sz, seed, grid.get(), thr, model, inl, st,
-                                                      thr);
+    rc = run_generic<Est, MSACScoring>(pts, pix, est, p, sz, seed, grid.get(), thr, model, inl, st, thr, gc_max,
+                                       final_irls);
   if (rc == GCR_OK) {
     if (inl.size() > 5) {
       const double tt = 1.5 * thr, sq = tt * tt;
@@ -374,7 +393,7 @@ static int find_essential(const double* corr, int64_t n, const double* K1, const
       }
       std::vector<Model> models;
       e_bundle_adjust(pts, inl.data(), inl.size(), w_pt.data(), w_pos.data(), models);
-      MSACScoring<EssentialEstimator> sc;
+      MSACScoring<Est> sc;
       sc.initialize(sq, n);
       double best = st ? st->score : 0.0;
       for (Model& E : models) {
@@ -401,7 +420,10 @@ static int find_essential(const double* corr, int64_t n, const double* K1, const
 
 // Values per correspondence row and minimal sample size of a model kind.
 static int kind_columns(int kind) {
-  return kind == GCR_HOMOGRAPHY_AFFINE || kind == GCR_FUNDAMENTAL_AFFINE || kind == GCR_FUNDAMENTAL_SIFT ? 8 : 4;
+  return kind == GCR_HOMOGRAPHY_AFFINE || kind == GCR_FUNDAMENTAL_AFFINE || kind == GCR_FUNDAMENTAL_SIFT ||
+                 kind == GCR_HOMOGRAPHY_SIFT
+             ? 8
+             : 4;
 }
 static int kind_sample_size(int kind) {
   switch (kind) {
@@ -411,6 +433,8 @@ static int kind_sample_size(int kind) {
     case GCR_HOMOGRAPHY_AFFINE: return 2;
     case GCR_FUNDAMENTAL_AFFINE: return 3;
     case GCR_FUNDAMENTAL_SIFT: return 4;
+    case GCR_HOMOGRAPHY_SIFT: return 2;
+    case GCR_ESSENTIAL_PLANAR: return 2;
     default: return 0;
   }
 }
@@ -427,9 +451,17 @@ static int find_pair(int kind, const double* corr, int64_t n, const double* K1, 
   switch (kind) {
     case GCR_HOMOGRAPHY: rc = find_homography(corr, n, *sz, *p, seed, model_out, mask_out, s); break;
     case GCR_FUNDAMENTAL: rc = find_fundamental(corr, n, *sz, *p, seed, model_out, mask_out, s); break;
-    case GCR_ESSENTIAL: rc = find_essential(corr, n, K1, K2, *sz, *p, seed, model_out, mask_out, s); break;
+    case GCR_ESSENTIAL:
+      rc = find_essential_kind<EssentialEstimator>(corr, n, K1, K2, *sz, *p, seed, model_out, mask_out, s);
+      break;
+    case GCR_ESSENTIAL_PLANAR:
+      rc = find_essential_kind<EssentialPlanarEstimator>(corr, n, K1, K2, *sz, *p, seed, model_out, mask_out, s);
+      break;
     case GCR_HOMOGRAPHY_AFFINE:
-      rc = find_homography_affine(corr, n, *sz, *p, seed, model_out, mask_out, s);
+      rc = find_homography_rows8<HomographyAffineEstimator>(corr, n, *sz, *p, seed, model_out, mask_out, s);
+      break;
+    case GCR_HOMOGRAPHY_SIFT:
+      rc = find_homography_rows8<HomographySiftEstimator>(corr, n, *sz, *p, seed, model_out, mask_out, s);
       break;
     case GCR_FUNDAMENTAL_AFFINE:
       rc = find_fundamental_rows8<FundamentalAffineEstimator>(corr, n, *sz, *p, seed, model_out, mask_out, s);
@@ -632,12 +664,22 @@ double oracle_msac_score(int kind, const double* corr, int64_t n, const double* 
   return s.value;
 }
 
-// Minimal-sample solve for tests: writes up to 10 models, returns their count (-1 invalid sample).
+// Minimal-sample solve for tests: writes up to 10 models, returns their count (-1 invalid sample);
+// rows of 8 for GCR_HOMOGRAPHY_SIFT, of 4 otherwise.
 int oracle_minimal(int kind, const double* corr, int64_t n, const int64_t* sample, double* models_out) {
   const Mat pts{corr, n, 4};
   std::vector<size_t> s;
   std::vector<Model> models;
-  if (kind == GCR_HOMOGRAPHY) {
+  if (kind == GCR_HOMOGRAPHY_SIFT) {
+    const Mat rows8{corr, n, 8};
+    HomographySiftEstimator e;
+    s.assign(sample, sample + 2);
+    e.estimate_minimal(rows8, s.data(), models);
+  } else if (kind == GCR_ESSENTIAL_PLANAR) {
+    EssentialPlanarEstimator e;
+    s.assign(sample, sample + 2);
+    e.estimate_minimal(pts, s.data(), models);
+  } else if (kind == GCR_HOMOGRAPHY) {
     HomographyEstimator e;
     s.assign(sample, sample + 4);
     if (!e.is_valid_sample(pts, s.data())) return -1;

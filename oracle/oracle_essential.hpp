@@ -1222,4 +1222,96 @@ struct EssentialEstimator {
   }
 };
 
+// EssentialMatrixEstimator<EssentialMatrixTwoPointsPlanar,
+// EssentialMatrixBundleAdjustmentSolver> (types.h:121-126): planar camera
+// motion, rotation about the camera's y axis and translation in its x-z
+// plane.
+struct EssentialPlanarEstimator : EssentialEstimator {
+  static constexpr size_t sample_size() { return 2; }
+  static constexpr size_t max_solutions() { return 1; }  // SolverEngine::maximumSolutions (solver_engine.h:73-76)
+  size_t sample_size_rt() const { return 2; }
+  static constexpr size_t non_minimal_sample_size() { return 6; }
+  size_t inlier_limit() const { return 7 * sample_size(); }
+
+  // EssentialMatrixTwoPointsPlanar::estimateModel
+  // (solver_essential_matrix_two_points_planar.h:92-175): C = -A2^+ A1 from
+  // the rows A1 = (y1, -y1 x2), A2 = (-y2, x1 y2); the quadratic in cos 2a
+  // from C^T C; angles +-acos(root) / 2; the direction of C (cos a, sin a)
+  // gives a - b. Models with non-finite entries are dropped (the reference
+  // keeps them; they score nothing); the rest pass the orientation test on
+  // the two points (essential_estimator.h:166-172).
+  bool estimate_minimal(const Mat& pts, const size_t* s, std::vector<Model>& models) const {
+    models.clear();
+    double A1[2][2], A2[2][2];
+    for (int i = 0; i < 2; ++i) {
+      const double* p = pts.row(s[i]);
+      const double x1 = p[0], y1 = p[1], x2 = p[2], y2 = p[3];
+      A1[i][0] = y1;
+      A1[i][1] = -y1 * x2;
+      A2[i][0] = -y2;
+      A2[i][1] = x1 * y2;
+    }
+    const double g00 = A2[0][0] * A2[0][0] + A2[1][0] * A2[1][0];
+    const double g01 = A2[0][0] * A2[0][1] + A2[1][0] * A2[1][1];
+    const double g11 = A2[0][1] * A2[0][1] + A2[1][1] * A2[1][1];
+    const double det = g00 * g11 - g01 * g01;
+    const double i00 = g11 / det, i01 = -g01 / det, i11 = g00 / det;
+    double P[2][2];
+    for (int j = 0; j < 2; ++j) {
+      P[0][j] = i00 * A2[j][0] + i01 * A2[j][1];
+      P[1][j] = i01 * A2[j][0] + i11 * A2[j][1];
+    }
+    double C[2][2];
+    for (int r = 0; r < 2; ++r)
+      for (int c = 0; c < 2; ++c) C[r][c] = -(P[r][0] * A1[0][c] + P[r][1] * A1[1][c]);
+    const double a = C[0][0] * C[0][0] + C[1][0] * C[1][0];
+    const double b = C[0][1] * C[0][0] + C[1][1] * C[1][0];
+    const double c = C[0][1] * C[0][1] + C[1][1] * C[1][1];
+    const double cf1 = 4 * b * b + (a - c) * (a - c);
+    const double cf2 = -2 * (a - c) * (2 - a - c);
+    const double cf3 = (2 - a - c) * (2 - a - c) - 4 * b * b;
+    const double disc = std::sqrt(cf2 * cf2 - 4 * cf1 * cf3);
+    const double c2a1 = (-cf2 + disc) / (2 * cf1), c2a2 = (-cf2 - disc) / (2 * cf1);
+    const double alphas[4] = {std::acos(c2a1) / 2, std::acos(c2a2) / 2, -std::acos(c2a1) / 2, -std::acos(c2a2) / 2};
+    for (int q = 0; q < 4; ++q) {
+      const double sa = std::sin(alphas[q]), ca = std::cos(alphas[q]);
+      double w0 = C[0][0] * ca + C[0][1] * sa, w1 = C[1][0] * ca + C[1][1] * sa;
+      const double nw = std::sqrt(w0 * w0 + w1 * w1);
+      w0 /= nw;
+      w1 /= nw;
+      const double al = std::atan2(sa, ca), amb = std::atan2(w1, w0);
+      const Model E = {0.0, -std::sin(al), 0.0, std::sin(amb), 0.0, -std::cos(amb), 0.0, std::cos(al), 0.0};
+      bool fin = true;
+      for (double v : E) fin = fin && std::isfinite(v);
+      if (fin && e_orientation_valid(E, pts, s, 2)) models.push_back(E);
+    }
+    return !models.empty();
+  }
+
+  // EssentialMatrixBundleAdjustmentSolver::estimateModel with no initial
+  // model (solver_essential_matrix_bundle_adjustment.h:114-188) through
+  // estimateModelNonminimal (essential_estimator.h:307-333): the weight
+  // pointer goes to both the Stewenius start (read by point) and the pose
+  // refinement (read by sample position, jacobian_impl.h:327-342); at most
+  // ten models are kept; each is normalised with E33 >= 0.
+  bool estimate_nonminimal(const Mat& pts, const size_t* s, size_t n, std::vector<Model>& models,
+                           const double* weights) const {
+    if (n < non_minimal_sample_size()) return false;
+    std::vector<Model> out;
+    e_bundle_adjust(pts, s, n, weights, weights, out);
+    if (out.size() > 10) out.resize(10);
+    if (out.empty()) return false;
+    for (Model& E : out) {
+      double nr = 0;
+      for (double v : E) nr += v * v;
+      nr = std::sqrt(nr);
+      for (double& v : E) v /= nr;
+      if (E[8] < 0)
+        for (double& v : E) v = -v;
+      models.push_back(E);
+    }
+    return true;
+  }
+};
+
 }  // namespace oracle

@@ -260,4 +260,222 @@ struct HomographyAffineEstimator : HomographyEstimator {
   }
 };
 
+// Real roots, ascending, of c[0] + c[1] x + ... + c[deg] x^deg (deg <= 4):
+// the quadratic derivative's roots in closed form, then each higher
+// derivative's roots and the polynomial's own isolated between the next
+// derivative's roots and the Cauchy bound and bisected to the last
+// representable midpoint; exactly-zero leading coefficients lower the degree.
+inline int poly_quadratic_roots(const double* c, double* roots) {
+  const double disc = c[1] * c[1] - 4.0 * c[2] * c[0];
+  if (disc < 0.0) return 0;
+  const double q = -0.5 * (c[1] + std::copysign(std::sqrt(disc), c[1]));
+  double r0 = q / c[2], r1 = q != 0.0 ? c[0] / q : r0;
+  if (r1 < r0) std::swap(r0, r1);
+  roots[0] = r0;
+  roots[1] = r1;
+  return 2;
+}
+
+inline int poly_bracketed_roots(const double* c, int deg, const double* cp, int ncp, double* roots) {
+  double bound = 0.0;
+  for (int i = 0; i < deg; ++i) bound = std::max(bound, std::abs(c[i] / c[deg]));
+  bound += 1.0;
+  auto f = [&](double x) {
+    double v = c[deg];
+    for (int i = deg - 1; i >= 0; --i) v = v * x + c[i];
+    return v;
+  };
+  std::vector<double> edges{-bound};
+  for (int i = 0; i < ncp; ++i)
+    if (cp[i] > -bound && cp[i] < bound) edges.push_back(cp[i]);
+  edges.push_back(bound);
+  int nr = 0;
+  for (size_t k = 0; k + 1 < edges.size(); ++k) {
+    double lo = edges[k], hi = edges[k + 1];
+    double flo = f(lo);
+    const double fhi = f(hi);
+    if (flo == 0.0) {
+      if (nr == 0 || roots[nr - 1] != lo) roots[nr++] = lo;
+      continue;
+    }
+    if ((flo < 0.0) == (fhi < 0.0)) continue;
+    for (int it = 0; it < 200; ++it) {
+      const double mid = 0.5 * (lo + hi);
+      if (mid <= lo || mid >= hi) break;
+      const double fm = f(mid);
+      if (fm == 0.0) {
+        lo = hi = mid;
+        break;
+      }
+      if ((fm < 0.0) == (flo < 0.0)) {
+        lo = mid;
+        flo = fm;
+      } else {
+        hi = mid;
+      }
+    }
+    roots[nr++] = 0.5 * (lo + hi);
+  }
+  return nr;
+}
+
+inline int poly_real_roots(const double* c_in, int deg, double* roots) {
+  while (deg > 0 && c_in[deg] == 0.0) --deg;
+  if (deg <= 0) return 0;
+  if (deg == 1) {
+    roots[0] = -c_in[0] / c_in[1];
+    return std::isfinite(roots[0]) ? 1 : 0;
+  }
+  double lv[5][5];
+  for (int i = 0; i <= deg; ++i) lv[deg][i] = c_in[i];
+  for (int j = deg - 1; j >= 2; --j)
+    for (int i = 0; i <= j; ++i) lv[j][i] = (i + 1) * lv[j + 1][i + 1];
+  double cur[4], nxt[4];
+  int n = poly_quadratic_roots(lv[2], cur);
+  for (int j = 3; j <= deg; ++j) {
+    n = poly_bracketed_roots(lv[j], j, cur, n, nxt);
+    for (int i = 0; i < n; ++i) cur[i] = nxt[i];
+  }
+  for (int i = 0; i < n; ++i) roots[i] = cur[i];
+  return n;
+}
+
+// findHomographySIFT_ (gcransac_python.cpp:4813-5069): the point estimator
+// (RobustHomographyEstimator) on rows (x1, y1, x2, y2, q1, q2, o1, o2) with
+// the minimal solver HomographyTwoSIFTSolver (solver_homography_two_sift.h:
+// 113-480), which declares one solution (maximumSolutions, :83-86, the
+// count SPRT uses) and returns every conic intersection.
+struct HomographySiftEstimator : HomographyEstimator {
+  static constexpr size_t sample_size() { return 2; }
+  static constexpr bool space_partitioning = false;
+  size_t sample_size_rt() const { return 2; }
+  size_t inlier_limit() const { return 7 * sample_size(); }
+
+  // Two point rows and one orientation row per correspondence (the
+  // homography's Jacobian J at x1 maps the direction o1 onto a multiple of
+  // o2): a 6 x 9 system, null space of dimension three. The scale ratio of
+  // each correspondence is the quadratic q2 w(h)^2 - q1 D(h) = 0, with
+  // w = h7 x1 + h8 y1 + h9 and D = (h1 h5 - h2 h4) + x2 (h4 h8 - h5 h7) +
+  // y2 (h2 h7 - h1 h8) (the reference's coefficient expressions, :226-355).
+  // The reference takes the null space from an SVD and intersects the two
+  // conics with an elimination template and an eigenproblem (:356-478),
+  // building a model from the real part of every eigenvalue. Here: the null
+  // space by Gaussian elimination with full pivoting over h1..h8 (h9 free:
+  // its basis vector has h9 = 1, the others h9 = 0), the intersections from
+  // the resultant quartic in the second null-space coordinate (real roots by
+  // bisection), the first coordinate from the conics' linear combination;
+  // real intersections only, ascending in that root, each with h9 = 1.
+  static int minimal_sift(const double* const rows[2], Model* out) {
+    double A[6][9];
+    double u1[2], v1[2], u2[2], v2[2], q1[2], q2[2];
+    for (int c = 0; c < 2; ++c) {
+      const double* p = rows[c];
+      u1[c] = p[0]; v1[c] = p[1]; u2[c] = p[2]; v2[c] = p[3];
+      q1[c] = p[4]; q2[c] = p[5];
+      const double s1 = std::sin(p[6]), c1 = std::cos(p[6]);
+      const double s2 = std::sin(p[7]), c2 = std::cos(p[7]);
+      const double r0[9] = {0.0, 0.0, 0.0, u1[c], v1[c], 1.0, -u1[c] * v2[c], -v1[c] * v2[c], -v2[c]};
+      const double r1[9] = {u1[c], v1[c], 1.0, 0.0, 0.0, 0.0, -u1[c] * u2[c], -v1[c] * u2[c], -u2[c]};
+      const double r2[9] = {-c1 * s2, -s1 * s2, 0.0, c1 * c2, s1 * c2, 0.0,
+                            u2[c] * c1 * s2 - v2[c] * c1 * c2, u2[c] * s1 * s2 - v2[c] * s1 * c2, 0.0};
+      for (int k = 0; k < 9; ++k) {
+        A[3 * c][k] = r0[k];
+        A[3 * c + 1][k] = r1[k];
+        A[3 * c + 2][k] = r2[k];
+      }
+    }
+    int col_of[6];
+    bool used[8] = {false, false, false, false, false, false, false, false};
+    for (int k = 0; k < 6; ++k) {
+      int pr = -1, pc = -1;
+      double best = 0.0;
+      for (int r = k; r < 6; ++r)
+        for (int c = 0; c < 8; ++c)
+          if (!used[c] && std::abs(A[r][c]) > best) {
+            best = std::abs(A[r][c]);
+            pr = r;
+            pc = c;
+          }
+      if (!(best > 0.0)) return 0;
+      if (pr != k)
+        for (int j = 0; j < 9; ++j) std::swap(A[pr][j], A[k][j]);
+      used[pc] = true;
+      col_of[k] = pc;
+      const double inv = 1.0 / A[k][pc];
+      for (int j = 0; j < 9; ++j) A[k][j] *= inv;
+      for (int r = 0; r < 6; ++r) {
+        if (r == k) continue;
+        const double fct = A[r][pc];
+        if (fct != 0.0)
+          for (int j = 0; j < 9; ++j) A[r][j] -= fct * A[k][j];
+      }
+    }
+    int fr[3];
+    int nf = 0;
+    for (int c = 0; c < 8; ++c)
+      if (!used[c]) fr[nf++] = c;
+    fr[2] = 8;
+    double N[3][9];
+    for (int b = 0; b < 3; ++b) {
+      for (int j = 0; j < 9; ++j) N[b][j] = 0.0;
+      N[b][fr[b]] = 1.0;
+      for (int k = 0; k < 6; ++k) N[b][col_of[k]] = -A[k][fr[b]];
+    }
+    double K[2][6];
+    for (int c = 0; c < 2; ++c) {
+      auto form = [&](const double* x, const double* y) {
+        const double wx = x[6] * u1[c] + x[7] * v1[c] + x[8];
+        const double wy = y[6] * u1[c] + y[7] * v1[c] + y[8];
+        const double dxy = 0.5 * ((x[0] * y[4] + y[0] * x[4] - x[1] * y[3] - y[1] * x[3]) +
+                                  u2[c] * (x[3] * y[7] + y[3] * x[7] - x[4] * y[6] - y[4] * x[6]) +
+                                  v2[c] * (x[1] * y[6] + y[1] * x[6] - x[0] * y[7] - y[0] * x[7]));
+        return q2[c] * wx * wy - q1[c] * dxy;
+      };
+      K[c][0] = form(N[0], N[0]);
+      K[c][1] = 2.0 * form(N[0], N[1]);
+      K[c][2] = form(N[1], N[1]);
+      K[c][3] = 2.0 * form(N[0], N[2]);
+      K[c][4] = 2.0 * form(N[1], N[2]);
+      K[c][5] = form(N[2], N[2]);
+    }
+    const double a1 = K[0][0], a2 = K[1][0];
+    const double p2 = a1 * K[1][2] - a2 * K[0][2], p1 = a1 * K[1][4] - a2 * K[0][4], p0 = a1 * K[1][5] - a2 * K[0][5];
+    const double l1 = a1 * K[1][1] - a2 * K[0][1], l0 = a1 * K[1][3] - a2 * K[0][3];
+    const double k3 = K[0][1] * K[1][2] - K[1][1] * K[0][2];
+    const double k2 = K[0][1] * K[1][4] + K[0][3] * K[1][2] - K[1][1] * K[0][4] - K[1][3] * K[0][2];
+    const double k1 = K[0][1] * K[1][5] + K[0][3] * K[1][4] - K[1][1] * K[0][5] - K[1][3] * K[0][4];
+    const double k0 = K[0][3] * K[1][5] - K[1][3] * K[0][5];
+    const double r[5] = {p0 * p0 - l0 * k0, 2.0 * p1 * p0 - (l1 * k0 + l0 * k1),
+                         p1 * p1 + 2.0 * p2 * p0 - (l1 * k1 + l0 * k2), 2.0 * p2 * p1 - (l1 * k2 + l0 * k3),
+                         p2 * p2 - l1 * k3};
+    double roots[4];
+    const int nr = poly_real_roots(r, 4, roots);
+    int nm = 0;
+    for (int i = 0; i < nr; ++i) {
+      const double b = roots[i];
+      const double L = l1 * b + l0, P = (p2 * b + p1) * b + p0;
+      const double a = -P / L;
+      Model h;
+      bool fin = true;
+      for (int j = 0; j < 9; ++j) {
+        h[j] = a * N[0][j] + b * N[1][j] + N[2][j];
+        fin = fin && std::isfinite(h[j]);
+      }
+      if (fin) out[nm++] = h;
+    }
+    return nm;
+  }
+
+  bool estimate_minimal(const Mat& pts, const size_t* s, std::vector<Model>& models) const {
+    const double* rows[2] = {pts.row(s[0]), pts.row(s[1])};
+    Model m[4];
+    const int nm = minimal_sift(rows, m);
+    for (int i = 0; i < nm; ++i) models.push_back(m[i]);
+    return nm > 0;
+  }
+
+  // isValidSample (homography_estimator.h:350-351): not tested below four
+  bool is_valid_sample(const Mat&, const size_t*) const { return true; }
+};
+
 }  // namespace oracle

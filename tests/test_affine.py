@@ -180,3 +180,80 @@ def test_oracle_four_sift_solver_recovers_the_scene(oracle):
     assert rc == 0
     assert S.fundamental_error(Fo, pr) < 0.05
     assert np.all(m[g])
+
+
+def test_sift_homography_entry_checks(gcr):
+    """The SIFT homography kind (findHomographySIFT_,
+    gcransac_python.cpp:4813-5069) refuses P-NAPSAC and MAGSAC++ before any
+    device work; the python entry wants rows of 8 for solver=1; its defaults
+    are the homography entry's without space partitioning."""
+    lib = _abi.load()
+    c = np.random.default_rng(5).uniform(0, 480, (50, 8))
+    size = _abi.ImageSize(h1=480, w1=640, h2=480, w2=640)
+    model, mask, st = np.zeros(9), np.zeros(50, np.uint8), _abi.Stats()
+    for kw in (dict(sampler=2), dict(scoring=1)):
+        p = ac_params(**kw)
+        rc = lib.gcr_find_homography_sift(_abi.ptr(c), 50, ctypes.byref(size), None, ctypes.byref(p),
+                                          _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
+        assert rc == _abi.GCR_UNSUPPORTED, kw
+    with pytest.raises(ValueError):
+        gcr.findHomography(c[:, :4], 480, 640, 480, 640, solver=1)
+    with pytest.raises(NotImplementedError):
+        gcr.findHomography(c, 480, 640, 480, 640, solver=3)
+    p = gcr.default_params(_abi.GCR_HOMOGRAPHY_SIFT)
+    assert (p.spatial_coherence_weight, p.neighborhood, p.neighborhood_size, p.use_space_partitioning) == \
+        (0.975, 0, 4.0, 0)
+
+
+def _sift_h_rows(p):
+    """The reference's three rows of one SIFT correspondence
+    (solver_homography_two_sift.h:150-185)."""
+    u1, v1, u2, v2, q1, q2, a1, a2 = p
+    s1, c1, s2, c2 = np.sin(a1), np.cos(a1), np.sin(a2), np.cos(a2)
+    return [[0, 0, 0, u1, v1, 1, -u1 * v2, -v1 * v2, -v2], [u1, v1, 1, 0, 0, 0, -u1 * u2, -v1 * u2, -u2],
+            [-c1 * s2, -s1 * s2, 0, c1 * c2, s1 * c2, 0, u2 * c1 * s2 - v2 * c1 * c2, u2 * s1 * s2 - v2 * s1 * c2, 0]]
+
+
+def test_oracle_two_sift_homography_solver(oracle):
+    """On exact SIFT correspondences of a homography the true homography
+    satisfies the reference's six linear rows and both scale equations
+    (q2 w^2 = q1 (w^2 det J), the coefficient expressions of
+    solver_homography_two_sift.h:226-355), and the restated solver (null space
+    by elimination, resultant quartic, bisection) returns it among its models
+    for every sample of 200 scenes."""
+    lib = oracle.load()
+    for seed in range(200):
+        pr = S.homography_sift_pair(seed, n=50, inlier_ratio=1.0, sigma=0.0, angle_sigma=0.0, scale_sigma=0.0)
+        c = np.ascontiguousarray(pr["corr"])
+        H = pr["H_gt"] / pr["H_gt"][2, 2]
+        s = np.random.default_rng(seed).choice(50, 2, replace=False).astype(np.int64)
+        if seed < 20:
+            A = np.array(_sift_h_rows(c[s[0]]) + _sift_h_rows(c[s[1]]))
+            assert np.abs(A @ H.ravel()).max() < 1e-9 * np.abs(A).max()
+            for r in c[s]:
+                u1, v1, u2, v2, q1, q2 = r[:6]
+                h = H.ravel()
+                w = h[6] * u1 + h[7] * v1 + h[8]
+                D = (h[0] * h[4] - h[1] * h[3]) + u2 * (h[3] * h[7] - h[4] * h[6]) + v2 * (h[1] * h[6] - h[0] * h[7])
+                assert abs(q2 * w * w - q1 * D) < 1e-9 * q2 * w * w
+        out = np.zeros(90)
+        k = lib.oracle_minimal(_abi.GCR_HOMOGRAPHY_SIFT, oracle._p(c), 50, oracle._p(s), oracle._p(out))
+        assert 1 <= k <= 4
+        err = min(np.abs(out[9 * i:9 * i + 9].reshape(3, 3) - H).max() / np.abs(H).max() for i in range(k))
+        assert err < 1e-6, (seed, err)
+
+
+def test_oracle_sift_homography_run_recovers_the_scene(oracle):
+    """A tape of inlier pairs drives the oracle's SIFT-homography run to the
+    true homography on a noisy scene (the local optimisation's 4-point fits
+    average the noise), with every true inlier in the mask."""
+    pr = S.homography_sift_pair(13, n=600, inlier_ratio=0.5, sigma=0.5)
+    g = pr["inlier_gt"]
+    idx = np.nonzero(g)[0]
+    tape = np.stack([idx[2 * k:2 * k + 2] for k in range(30)]).astype(np.int32)
+    p = ac_params(max_iterations=30, min_iterations=30, lo_number=20)
+    rc, H, m, st = oracle.find(_abi.GCR_HOMOGRAPHY_SIFT, pr["corr"], oracle.make_size(*pr["size"]), p, seed=1,
+                               sample_tape=tape)
+    assert rc == 0
+    assert S.homography_error(H, pr["H_gt"]) < 1.0  # px RMS over the image
+    assert m[g].mean() > 0.97

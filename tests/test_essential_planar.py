@@ -1,0 +1,90 @@
+"""CPU checks of the planar-motion essential matrix
+(findPlanarEssentialMatrix_, src/pygcransac/src/gcransac_python.cpp:
+3531-3870): the entry points' argument checks before any device work, and
+the oracle's restatement of the two-point planar solver
+(solver_essential_matrix_two_points_planar.h:92-175) and of the run with the
+bundle-adjustment non-minimal solver."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from pygcransac import _abi, synthetic as S
+
+
+def planar_params(**kw):
+    base = dict(threshold=0.75, confidence=0.99, spatial_coherence_weight=0.975, neighborhood_size=8,
+                max_iterations=200, min_iterations=50, sampler=0, neighborhood=0, lo_number=20)
+    base.update(kw)
+    return _abi.Params(**base)
+
+
+def normalised(pr):
+    Ki = np.linalg.inv(pr["K"])
+    c = pr["corr"]
+    x1 = np.c_[c[:, :2], np.ones(len(c))] @ Ki.T
+    x2 = np.c_[c[:, 2:], np.ones(len(c))] @ Ki.T
+    return np.ascontiguousarray(np.c_[x1[:, :2], x2[:, :2]])
+
+
+def test_planar_entry_checks(gcr):
+    """MAGSAC++ (which the planar driver does not offer) is refused, and so
+    are missing intrinsics, before any device work; the python entry wants
+    rows of 4 and at least 3 of them, like the reference binding; its
+    defaults are the binding's."""
+    lib = _abi.load()
+    pr = S.two_view_pair(1, n=50, inlier_ratio=0.5, planar_motion=True)
+    c = np.ascontiguousarray(pr["corr"])
+    K = np.ascontiguousarray(pr["K"]).ravel()
+    size = _abi.ImageSize(h1=480, w1=640, h2=480, w2=640)
+    model, mask, st = np.zeros(9), np.zeros(50, np.uint8), _abi.Stats()
+    p = planar_params(scoring=1)
+    rc = lib.gcr_find_essential_planar(_abi.ptr(c), 50, _abi.ptr(K), _abi.ptr(K), ctypes.byref(size), None,
+                                       ctypes.byref(p), _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
+    assert rc == _abi.GCR_UNSUPPORTED
+    p = planar_params()
+    rc = lib.gcr_find_essential_planar(_abi.ptr(c), 50, None, _abi.ptr(K), ctypes.byref(size), None,
+                                       ctypes.byref(p), _abi.ptr(model), _abi.ptr(mask), ctypes.byref(st))
+    assert rc == _abi.GCR_INVALID_ARG
+    with pytest.raises(ValueError):
+        gcr.findPlanarEssentialMatrix(c[:2], pr["K"], pr["K"], 480, 640, 480, 640)
+    with pytest.raises(ValueError):
+        gcr.findPlanarEssentialMatrix(np.c_[c, c], pr["K"], pr["K"], 480, 640, 480, 640)
+    d = gcr.default_params(_abi.GCR_ESSENTIAL_PLANAR)
+    assert (d.spatial_coherence_weight, d.neighborhood, d.neighborhood_size, d.sampler, d.use_sprt) == \
+        (0.975, 1, 20.0, 1, 1)
+
+
+def test_oracle_planar_solver_recovers_the_motion(oracle):
+    """On exact correspondences of a planar motion the restated two-point
+    solver returns the true essential matrix (up to sign and scale) among its
+    models for every sample of 100 scenes, and every model has the planar
+    structure (zeros at E11, E13, E22, E31, E33)."""
+    lib = oracle.load()
+    for seed in range(100):
+        pr = S.two_view_pair(seed, n=60, inlier_ratio=1.0, sigma=0.0, planar_motion=True)
+        nrm = normalised(pr)
+        E = pr["E_gt"] / np.linalg.norm(pr["E_gt"])
+        s = np.random.default_rng(seed).choice(60, 2, replace=False).astype(np.int64)
+        out = np.zeros(90)
+        k = lib.oracle_minimal(_abi.GCR_ESSENTIAL_PLANAR, oracle._p(nrm), 60, oracle._p(s), oracle._p(out))
+        assert 1 <= k <= 4
+        Ms = [out[9 * i:9 * i + 9].reshape(3, 3) for i in range(k)]
+        for M in Ms:
+            assert np.abs(M.ravel()[[0, 2, 4, 6, 8]]).max() == 0.0
+        err = min(np.abs(M / np.linalg.norm(M) - sg * E).max() for M in Ms for sg in (1, -1))
+        assert err < 1e-6, (seed, err)
+
+
+@pytest.mark.parametrize("use_sprt", [0, 1])
+def test_oracle_planar_run_recovers_the_scene(oracle, use_sprt):
+    """The oracle's planar driver (bundle-adjustment non-minimal fits; with
+    SPRT up to 100 graph cuts and no final reweighted fit) recovers a noisy
+    planar-motion scene."""
+    pr = S.two_view_pair(21, n=800, inlier_ratio=0.5, planar_motion=True)
+    K = pr["K"]
+    rc, E, m, st = oracle.find(_abi.GCR_ESSENTIAL_PLANAR, pr["corr"], oracle.make_size(*pr["size"]),
+                               planar_params(use_sprt=use_sprt), seed=3, K1=K, K2=K)
+    assert rc == 0
+    assert S.essential_error(E, pr) < 1.0  # degrees
+    assert m[pr["inlier_gt"]].mean() > 0.95
