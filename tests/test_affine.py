@@ -257,3 +257,19 @@ def test_oracle_sift_homography_run_recovers_the_scene(oracle):
     assert rc == 0
     assert S.homography_error(H, pr["H_gt"]) < 1.0  # px RMS over the image
     assert m[g].mean() > 0.97
+
+
+def test_oracle_two_sift_homography_degenerate_samples(oracle):
+    """A repeated SIFT correspondence (rank-deficient 6 x 9 system) and a
+    pair with zero scales give no model or only finite ones."""
+    lib = oracle.load()
+    c = np.array([[100.0, 120.0, 110.0, 130.0, 2.0, 2.2, 0.3, 0.35],
+                  [100.0, 120.0, 110.0, 130.0, 2.0, 2.2, 0.3, 0.35],
+                  [300.0, 220.0, 310.0, 240.0, 0.0, 0.0, 1.0, 1.1],
+                  [200.0, 320.0, 205.0, 335.0, 0.0, 0.0, -1.0, -0.9]], np.float64)
+    for s in ([0, 1], [2, 3]):
+        out = np.full(90, np.nan)
+        k = lib.oracle_minimal(_abi.GCR_HOMOGRAPHY_SIFT, oracle._p(c), 4, oracle._p(np.array(s, np.int64)),
+                               oracle._p(out))
+        assert 0 <= k <= 4
+        assert np.all(np.isfinite(out[:9 * k]))

@@ -88,3 +88,18 @@ def test_oracle_planar_run_recovers_the_scene(oracle, use_sprt):
     assert rc == 0
     assert S.essential_error(E, pr) < 1.0  # degrees
     assert m[pr["inlier_gt"]].mean() > 0.95
+
+
+def test_oracle_planar_solver_degenerate_samples(oracle):
+    """Degenerate two-point samples (a repeated point, points on the image
+    row through the principal point, which zero the A2 rows) give no model
+    or only finite ones: models with non-finite entries are dropped."""
+    lib = oracle.load()
+    pts = np.array([[0.1, 0.2, 0.15, 0.25], [0.1, 0.2, 0.15, 0.25],
+                    [0.1, 0.0, 0.15, 0.0], [-0.2, 0.0, -0.1, 0.0]], np.float64)
+    for s in ([0, 1], [2, 3]):
+        out = np.full(90, np.nan)
+        k = lib.oracle_minimal(_abi.GCR_ESSENTIAL_PLANAR, oracle._p(pts), 4, oracle._p(np.array(s, np.int64)),
+                               oracle._p(out))
+        assert 0 <= k <= 4
+        assert np.all(np.isfinite(out[:9 * k]))
