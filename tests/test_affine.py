@@ -273,3 +273,73 @@ def test_oracle_two_sift_homography_degenerate_samples(oracle):
                                oracle._p(out))
         assert 0 <= k <= 4
         assert np.all(np.isfinite(out[:9 * k]))
+
+
+def test_oracle_two_sift_homography_matches_an_svd_restatement(oracle):
+    """On noisy SIFT correspondences (where the minimal models are not the
+    true homography) the oracle's models equal those of an independent
+    restatement of the reference's steps: the null space of the six rows by
+    SVD (solver_homography_two_sift.h:187-190), h = a n1 + b n2 + n3, the two
+    scale equations as conics in (a, b), their real intersections from
+    NumPy's polynomial roots, each model divided by h33 (:469). Samples whose
+    resultant has nearly double roots are skipped (their real-root count is
+    decided by rounding); the models agree to 1e-3 relative, most to 1e-5
+    (ill-conditioned samples lose digits on either route)."""
+    lib = oracle.load()
+    checked = 0
+    rel = []
+    for seed in range(60):
+        pr = S.homography_sift_pair(300 + seed, n=40, inlier_ratio=1.0, sigma=1.0, angle_sigma=0.05,
+                                    scale_sigma=0.05)
+        c = np.ascontiguousarray(pr["corr"])
+        s = np.random.default_rng(seed).choice(40, 2, replace=False)
+        A = np.array(_sift_h_rows(c[s[0]]) + _sift_h_rows(c[s[1]]))
+        N = np.linalg.svd(A)[2][-3:]
+
+        def conic(r):
+            u1, v1, u2, v2, q1, q2 = r[:6]
+
+            def g(h):
+                w = h[6] * u1 + h[7] * v1 + h[8]
+                D = (h[0] * h[4] - h[1] * h[3]) + u2 * (h[3] * h[7] - h[4] * h[6]) + v2 * (h[1] * h[6] - h[0] * h[7])
+                return q2 * w * w - q1 * D
+            # quadratic form coefficients by polarisation
+            f = lambda a, b: g(a * N[0] + b * N[1] + N[2])  # noqa: E731
+            c5 = f(0, 0)
+            c0 = (f(1, 0) + f(-1, 0)) / 2 - c5
+            c3 = (f(1, 0) - f(-1, 0)) / 2
+            c2 = (f(0, 1) + f(0, -1)) / 2 - c5
+            c4 = (f(0, 1) - f(0, -1)) / 2
+            c1 = f(1, 1) - c0 - c2 - c3 - c4 - c5
+            return c0, c1, c2, c3, c4, c5
+        K1, K2 = conic(c[s[0]]), conic(c[s[1]])
+        # resultant in b of the two quadratics in a
+        A1, A2 = float(K1[0]), float(K2[0])
+        B1, B2 = np.poly1d([K1[1], K1[3]]), np.poly1d([K2[1], K2[3]])
+        C1, C2 = np.poly1d([K1[2], K1[4], K1[5]]), np.poly1d([K2[2], K2[4], K2[5]])
+        P = A1 * C2 - A2 * C1
+        L = A1 * B2 - A2 * B1
+        R = P * P - L * (B1 * C2 - B2 * C1)
+        roots = np.roots(R.coeffs)
+        if np.any(np.abs(roots.imag) < 1e-3 * (1 + np.abs(roots.real))) and \
+                np.any((np.abs(roots.imag) > 0) & (np.abs(roots.imag) < 1e-3 * (1 + np.abs(roots.real)))):
+            continue
+        ref = []
+        for b in roots[np.abs(roots.imag) == 0].real:
+            a = -P(b) / L(b)
+            h = a * N[0] + b * N[1] + N[2]
+            ref.append(h / h[8])
+        out = np.zeros(90)
+        k = lib.oracle_minimal(_abi.GCR_HOMOGRAPHY_SIFT, oracle._p(c), 40, oracle._p(s.astype(np.int64)),
+                               oracle._p(out))
+        assert k == len(ref), (seed, k, len(ref))
+        for i in range(k):
+            h = out[9 * i:9 * i + 9]
+            # two independent numerical routes on raw pixel coordinates (rows
+            # with entries up to 1e5): every model within 1e-3 relative of one
+            # of the other route's, most within 1e-5
+            rel.append(min(np.abs(h - r).max() / np.abs(r).max() for r in ref))
+            assert rel[-1] < 1e-3, (seed, i, rel[-1])
+        checked += 1
+    assert checked >= 40
+    assert np.mean(np.array(rel) < 1e-5) > 0.9, np.sort(rel)[-5:]

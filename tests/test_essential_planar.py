@@ -103,3 +103,51 @@ def test_oracle_planar_solver_degenerate_samples(oracle):
                                oracle._p(out))
         assert 0 <= k <= 4
         assert np.all(np.isfinite(out[:9 * k]))
+
+
+def _orientation_ok(E, pts):
+    """isOrientationValid (essential_estimator.h:336-401) on the rows pts."""
+    e = np.cross(E[0], E[2])
+    if np.all(np.abs(e) <= 1.9984e-15):
+        e = np.cross(E[1], E[2])
+    sg = [(E[0, 0] * p[2] + E[1, 0] * p[3] + E[2, 0]) * (e[1] - e[2] * p[1]) for p in pts]
+    return all(not (sg[0] * v < 0) for v in sg[1:])
+
+
+def test_oracle_planar_solver_matches_a_numpy_restatement(oracle):
+    """On noisy planar-motion samples the oracle's models equal a NumPy
+    transliteration of the reference's steps (pseudo-inverse of A2, the
+    quadratic in cos 2a, the four angles, atan2 of the mapped direction,
+    solver_essential_matrix_two_points_planar.h:115-173) after the
+    orientation test, in the same order."""
+    lib = oracle.load()
+    for seed in range(60):
+        pr = S.two_view_pair(400 + seed, n=30, inlier_ratio=1.0, sigma=1.0, planar_motion=True)
+        nrm = normalised(pr)
+        s = np.random.default_rng(seed).choice(30, 2, replace=False)
+        p = nrm[s]
+        A1 = np.array([[q[1], -q[1] * q[2]] for q in p])
+        A2 = np.array([[-q[3], q[0] * q[3]] for q in p])
+        C = -np.linalg.inv(A2.T @ A2) @ A2.T @ A1
+        C2 = C.T @ C
+        a, b, c = C2[0, 0], C2[1, 0], C2[1, 1]
+        cf1, cf2, cf3 = 4 * b * b + (a - c) ** 2, -2 * (a - c) * (2 - a - c), (2 - a - c) ** 2 - 4 * b * b
+        with np.errstate(invalid="ignore"):
+            d = np.sqrt(cf2 * cf2 - 4 * cf1 * cf3)
+            r1, r2 = (-cf2 + d) / (2 * cf1), (-cf2 - d) / (2 * cf1)
+            alphas = [np.arccos(r1) / 2, np.arccos(r2) / 2, -np.arccos(r1) / 2, -np.arccos(r2) / 2]
+        ref = []
+        for al in alphas:
+            v1 = np.array([np.cos(al), np.sin(al)])
+            v2 = C @ v1
+            v2 = v2 / np.linalg.norm(v2)
+            a1, amb = np.arctan2(v1[1], v1[0]), np.arctan2(v2[1], v2[0])
+            E = np.array([[0, -np.sin(a1), 0], [np.sin(amb), 0, -np.cos(amb)], [0, np.cos(a1), 0]])
+            if np.all(np.isfinite(E)) and _orientation_ok(E, p):
+                ref.append(E.ravel())
+        out = np.zeros(90)
+        k = lib.oracle_minimal(_abi.GCR_ESSENTIAL_PLANAR, oracle._p(nrm), 30, oracle._p(s.astype(np.int64)),
+                               oracle._p(out))
+        assert k == len(ref), (seed, k, len(ref))
+        for i in range(k):
+            assert np.abs(out[9 * i:9 * i + 9] - ref[i]).max() < 1e-9, (seed, i)
