@@ -665,7 +665,7 @@ double oracle_msac_score(int kind, const double* corr, int64_t n, const double* 
 }
 
 // Minimal-sample solve for tests: writes up to 10 models, returns their count (-1 invalid sample);
-// rows of 8 for GCR_HOMOGRAPHY_SIFT, of 4 otherwise.
+// rows of 8 for the SIFT and affine kinds, of 4 otherwise.
 int oracle_minimal(int kind, const double* corr, int64_t n, const int64_t* sample, double* models_out) {
   const Mat pts{corr, n, 4};
   std::vector<size_t> s;
@@ -675,6 +675,17 @@ int oracle_minimal(int kind, const double* corr, int64_t n, const int64_t* sampl
     HomographySiftEstimator e;
     s.assign(sample, sample + 2);
     e.estimate_minimal(rows8, s.data(), models);
+  } else if (kind == GCR_FUNDAMENTAL_AFFINE || kind == GCR_FUNDAMENTAL_SIFT) {
+    const Mat rows8{corr, n, 8};
+    if (kind == GCR_FUNDAMENTAL_AFFINE) {
+      FundamentalAffineEstimator e;
+      s.assign(sample, sample + 3);
+      e.estimate_minimal(rows8, s.data(), models);
+    } else {
+      FundamentalSiftEstimator e;
+      s.assign(sample, sample + 4);
+      e.estimate_minimal(rows8, s.data(), models);
+    }
   } else if (kind == GCR_ESSENTIAL_PLANAR) {
     EssentialPlanarEstimator e;
     s.assign(sample, sample + 2);

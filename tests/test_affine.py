@@ -343,3 +343,81 @@ def test_oracle_two_sift_homography_matches_an_svd_restatement(oracle):
         checked += 1
     assert checked >= 40
     assert np.mean(np.array(rel) < 1e-5) > 0.9, np.sort(rel)[-5:]
+
+
+def _orientation_ok(F, pts):
+    """isOrientationValid (fundamental_estimator.h) on the rows pts."""
+    e = np.cross(F[0], F[2])
+    if np.all(np.abs(e) <= 1.9984e-15):
+        e = np.cross(F[1], F[2])
+    sg = [(F[0, 0] * p[2] + F[1, 0] * p[3] + F[2, 0]) * (e[1] - e[2] * p[1]) for p in pts]
+    return all(not (sg[0] * v < 0) for v in sg[1:])
+
+
+def _epipolar_row(p):
+    x0, y0, x1, y1 = p[:4]
+    return [x1 * x0, x1 * y0, x1, y1 * x0, y1 * y0, y1, x0, y0, 1.0]
+
+
+def _affine_rows(p):
+    x0, y0, x1, y1, a11, a12, a21, a22 = p
+    return [[x1 + a11 * x0, a11 * y0, a11, y1 + a21 * x0, a21 * y0, a21, 1, 0, 0],
+            [a12 * x0, x1 + a12 * y0, a12, a22 * x0, y1 + a22 * y0, a22, 0, 1, 0]]
+
+
+def _sift_row(p):
+    u1, v1, u2, v2, q1, q2, o1, o2 = p
+    s1, c1, s2, c2 = np.sin(o1), np.cos(o1), np.sin(o2), np.cos(o2)
+    return [s2 * s2 * q2 * u1 - c1 * c2 * q1 * u2 - q2 * u1, s2 * s2 * q2 * v1 - s1 * c2 * q1 * u2 - q2 * v1,
+            s2 * s2 * q2 - q2, -c2 * s2 * q2 * u1 - c1 * c2 * q1 * v2, -c2 * s2 * q2 * v1 - s1 * c2 * q1 * v2,
+            -c2 * s2 * q2, -c1 * c2 * q1, -s1 * c2 * q1, 0.0]
+
+
+@pytest.mark.parametrize("kind", ["affine", "sift"])
+def test_oracle_fundamental_rows8_solvers_match_an_svd_restatement(oracle, kind):
+    """On noisy affine / SIFT correspondences the oracle's minimal models equal
+    an independent restatement: the reference's seven rows (three-affine:
+    epipolar rows of all three and affine rows of the first two,
+    solver_fundamental_matrix_three_affine.h:118-170; four-SIFT: epipolar
+    rows of all four and the orientation-scale rows of the first three,
+    solver_fundamental_matrix_four_sift.h:111-150), their two-dimensional
+    null space by SVD, det(x F1 + (1 - x) F2) = 0 by NumPy's roots, the
+    oriented constraint on the sample. Compared as sets of unit-norm models
+    up to sign; samples with nearly double roots are skipped."""
+    lib = oracle.load()
+    gen = S.two_view_affine_pair if kind == "affine" else S.two_view_sift_pair
+    code = _abi.GCR_FUNDAMENTAL_AFFINE if kind == "affine" else _abi.GCR_FUNDAMENTAL_SIFT
+    m = 3 if kind == "affine" else 4
+    checked = 0
+    for seed in range(40):
+        pr = gen(500 + seed, n=40, inlier_ratio=1.0)
+        c = np.ascontiguousarray(pr["corr"])
+        s = np.random.default_rng(seed).choice(40, m, replace=False)
+        p = c[s]
+        if kind == "affine":
+            A = np.array([_epipolar_row(q) for q in p] + _affine_rows(p[0]) + _affine_rows(p[1]))
+        else:
+            A = np.array([_epipolar_row(q) for q in p] + [_sift_row(q) for q in p[:3]])
+        V = np.linalg.svd(A)[2]
+        F1, F2 = V[-2].reshape(3, 3), V[-1].reshape(3, 3)
+        xs = np.linspace(-2, 2, 4)
+        dets = [np.linalg.det(x * F1 + (1 - x) * F2) for x in xs]
+        cub = np.polyfit(xs, dets, 3)
+        roots = np.roots(cub)
+        near = (np.abs(roots.imag) > 0) & (np.abs(roots.imag) < 1e-4 * (1 + np.abs(roots.real)))
+        if np.any(near):
+            continue
+        ref = []
+        for x in roots[roots.imag == 0].real:
+            F = x * F1 + (1 - x) * F2
+            if _orientation_ok(F, p):
+                ref.append(F.ravel() / np.linalg.norm(F))
+        out = np.zeros(90)
+        k = lib.oracle_minimal(code, oracle._p(c), 40, oracle._p(s.astype(np.int64)), oracle._p(out))
+        assert k == len(ref), (seed, k, len(ref))
+        for i in range(k):
+            f = out[9 * i:9 * i + 9] / np.linalg.norm(out[9 * i:9 * i + 9])
+            err = min(min(np.abs(f - r).max(), np.abs(f + r).max()) for r in ref)
+            assert err < 1e-6, (seed, i, err)
+        checked += 1
+    assert checked >= 30
